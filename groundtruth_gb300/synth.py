@@ -1,0 +1,349 @@
+"""Seeded synthetic boards for the solver's workloads.
+
+A board here is what GroundTruth hands its PEEC solver after rasterising copper (peec.build_grid with
+sub=1, src/groundtruth/solver/peec.py:329-449): per plane layer a node mask and x/y strip masks on one
+shared grid, the layers' heights and copper thickness, plane-pair capacitances, lumped branches, and per
+net the known signal path as straight filaments with its driver / receiver return nodes.
+
+Rasterisation follows the sub=1 rules of peec.py:385-393 and 432-435: a node is copper when its point lies
+strictly inside the copper (shapely.contains_xy: a point on an edge is outside), an x strip exists when
+both end nodes and the midpoint half a pitch to the right are copper of the net, a y strip likewise with the
+midpoint half a pitch up.  Copper is a board outline minus cut-outs, both polygons.
+
+Workloads (metres unless named otherwise):
+
+* ``plain_plane``   one solid plane 96 x 96 at 0.5 mm, a 0.2 mm trace 0.2 mm above it from cell (10, 48)
+                    to (86, 48), 100 MHz (the reference's CPU-runnable case).
+* ``slotted_pair``  Sig/GND/PWR/Sig, gaps 0.2/1.0/0.2 mm, 256 x 256 at 0.25 mm, a seeded 1 mm slot across
+                    60 % of the GND plane, 8 Manhattan random-walk nets crossing it, 32 log-spaced
+                    frequencies 1 MHz - 1 GHz (8 x 32 = 256 solves).
+* ``small_*``       reduced boards of the same kinds for golden fixtures and fast tests.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+
+EPS0 = 8.8541878128e-12
+SIGMA_CU = 5.8e7
+MU0 = 4e-7 * math.pi
+
+
+# ------------------------------------------------------------------------------------------ geometry
+def polygon_contains(px: np.ndarray, py: np.ndarray, poly: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """(strictly inside, on the boundary) for points against a simple polygon (k, 2), crossing-number rule
+    with an exact on-edge test, FP64, vectorised over the points."""
+    px = np.asarray(px, float)
+    py = np.asarray(py, float)
+    inside = np.zeros(px.shape, bool)
+    on_edge = np.zeros(px.shape, bool)
+    n = len(poly)
+    for e in range(n):
+        x1, y1 = poly[e]
+        x2, y2 = poly[(e + 1) % n]
+        cross = (x2 - x1) * (py - y1) - (y2 - y1) * (px - x1)
+        within = ((np.minimum(x1, x2) <= px) & (px <= np.maximum(x1, x2))
+                  & (np.minimum(y1, y2) <= py) & (py <= np.maximum(y1, y2)))
+        on_edge |= (cross == 0.0) & within
+        straddle = (y1 > py) != (y2 > py)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            xint = x1 + (py - y1) * (x2 - x1) / (y2 - y1)
+        inside ^= straddle & (px < xint)
+    return inside & ~on_edge, on_edge
+
+
+def copper_at(px, py, outline: np.ndarray, cutouts: list) -> np.ndarray:
+    """Points strictly inside the copper = outline minus the closed cut-outs (contains_xy semantics)."""
+    inside, _ = polygon_contains(px, py, outline)
+    for c in cutouts:
+        cin, con = polygon_contains(px, py, c)
+        inside &= ~(cin | con)
+    return inside
+
+
+def raster_layer(nx: int, ny: int, d: float, outline: np.ndarray, cutouts: list):
+    """(node, xb, yb) masks for one layer's copper by the sub=1 rules (node at (i d, j d), coordinates in
+    the same unit as d)."""
+    xs = np.arange(nx) * d
+    ys = np.arange(ny) * d
+    X, Y = np.meshgrid(xs, ys, indexing="ij")
+    node = copper_at(X, Y, outline, cutouts)
+    mx = copper_at(X[:-1, :] + d / 2, Y[:-1, :], outline, cutouts)
+    my = copper_at(X[:, :-1], Y[:, :-1] + d / 2, outline, cutouts)
+    xb = node[:-1, :] & node[1:, :] & mx
+    yb = node[:, :-1] & node[:, 1:] & my
+    return node, xb, yb
+
+
+def rect_polygon(cx: float, cy: float, length: float, width: float, angle: float) -> np.ndarray:
+    """A rectangle centred at (cx, cy), `length` along direction `angle` (rad), `width` across."""
+    u = np.array([math.cos(angle), math.sin(angle)])
+    v = np.array([-u[1], u[0]])
+    c = np.array([cx, cy])
+    a, b = 0.5 * length, 0.5 * width
+    return np.array([c - a * u - b * v, c + a * u - b * v, c + a * u + b * v, c - a * u + b * v])
+
+
+# ------------------------------------------------------------------------------------------ board
+@dataclass
+class Layer:
+    name: str
+    z: float
+    thickness: float
+    node: np.ndarray
+    xb: np.ndarray
+    yb: np.ndarray
+
+
+@dataclass
+class Pair:
+    upper: int
+    lower: int
+    c_per_area: float
+    tan_delta: float = 0.02
+
+
+@dataclass
+class BranchSpec:
+    """Lumped branch a -> b, impedance R + jwL (+ 1/(jwC) when C > 0)."""
+    a: tuple
+    b: tuple
+    R: float
+    L: float
+    C: float = 0.0
+    kind: str = "part"
+    radius: float = 1.5e-4
+
+    def z(self, f: float) -> complex:
+        w = 2 * math.pi * f
+        z = complex(self.R, w * self.L)
+        if self.C > 0:
+            z += 1.0 / (1j * w * self.C)
+        return z
+
+
+@dataclass
+class Net:
+    """Known signal path: rows (ax, ay, az, bx, by, bz, width, i), metres relative to node (0, 0)."""
+    segments: np.ndarray
+    driver: tuple
+    receiver: tuple
+    trace_t: float = 35e-6
+
+
+@dataclass
+class Board:
+    name: str
+    d: float                      # pitch, metres
+    nx: int
+    ny: int
+    layers: list
+    pairs: list = field(default_factory=list)
+    branches: list = field(default_factory=list)
+    nets: list = field(default_factory=list)
+    freqs: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    precond: str = "diag"
+    tol: float = 1e-10
+    restart: int = 50
+    sigma: float = SIGMA_CU
+
+    # -- flat arrays (fixtures, the C-ABI) -----------------------------------------------------------
+    def to_arrays(self) -> dict:
+        out = {"name": np.array(self.name), "d": np.float64(self.d), "nx": np.int64(self.nx),
+               "ny": np.int64(self.ny), "precond": np.array(self.precond), "tol": np.float64(self.tol),
+               "restart": np.int64(self.restart), "sigma": np.float64(self.sigma),
+               "freqs": np.asarray(self.freqs, float),
+               "layer_z": np.array([l.z for l in self.layers]), "layer_t": np.array([l.thickness for l in self.layers]),
+               "layer_node": np.stack([l.node for l in self.layers]), "layer_xb": np.stack([l.xb for l in self.layers]),
+               "layer_yb": np.stack([l.yb for l in self.layers]),
+               "pairs": np.array([[p.upper, p.lower, p.c_per_area, p.tan_delta] for p in self.pairs], float).reshape(-1, 4),
+               "branch_ab": np.array([[*b.a, *b.b] for b in self.branches], np.int64).reshape(-1, 6),
+               "branch_rlc": np.array([[b.R, b.L, b.C, b.radius] for b in self.branches], float).reshape(-1, 4),
+               "branch_via": np.array([b.kind == "via" for b in self.branches], bool),
+               "net_count": np.int64(len(self.nets))}
+        for n, net in enumerate(self.nets):
+            out[f"net{n}_seg"] = net.segments
+            out[f"net{n}_ends"] = np.array([*net.driver, *net.receiver], np.int64)
+            out[f"net{n}_trace_t"] = np.float64(net.trace_t)
+        return out
+
+    @staticmethod
+    def from_arrays(a) -> "Board":
+        layers = [Layer(f"L{k}", float(a["layer_z"][k]), float(a["layer_t"][k]), a["layer_node"][k].astype(bool),
+                        a["layer_xb"][k].astype(bool), a["layer_yb"][k].astype(bool)) for k in range(len(a["layer_z"]))]
+        pairs = [Pair(int(p[0]), int(p[1]), float(p[2]), float(p[3])) for p in a["pairs"]]
+        branches = [BranchSpec(tuple(int(v) for v in ab[:3]), tuple(int(v) for v in ab[3:]), float(r[0]), float(r[1]),
+                               float(r[2]), "via" if via else "part", float(r[3]))
+                    for ab, r, via in zip(a["branch_ab"], a["branch_rlc"], a["branch_via"])]
+        nets = []
+        for n in range(int(a["net_count"])):
+            e = a[f"net{n}_ends"]
+            nets.append(Net(np.asarray(a[f"net{n}_seg"], float), tuple(int(v) for v in e[:3]),
+                            tuple(int(v) for v in e[3:]), float(a[f"net{n}_trace_t"])))
+        return Board(str(a["name"]), float(a["d"]), int(a["nx"]), int(a["ny"]), layers, pairs, branches, nets,
+                     np.asarray(a["freqs"], float), str(a["precond"]), float(a["tol"]), int(a["restart"]),
+                     float(a["sigma"]))
+
+
+def _full_layer(name, z, t, nx, ny, d, cutouts=()):
+    """A plane whose outline reaches half a pitch beyond the grid (every grid node inside), minus cut-outs."""
+    h = 0.5 * d
+    outline = np.array([[-h, -h], [(nx - 1) * d + h, -h], [(nx - 1) * d + h, (ny - 1) * d + h], [-h, (ny - 1) * d + h]])
+    node, xb, yb = raster_layer(nx, ny, d, outline, list(cutouts))
+    return Layer(name, z, t, node, xb, yb)
+
+
+def _segments(points: list, z_sig: float, z_face: float, width: float) -> np.ndarray:
+    """Filaments: up from the plane's face at the first point, along the walk at z_sig, down at the last."""
+    rows = []
+    p0, p1 = points[0], points[-1]
+    rows.append([p0[0], p0[1], z_face, p0[0], p0[1], z_sig, width, 1.0])
+    for a, b in zip(points[:-1], points[1:]):
+        rows.append([a[0], a[1], z_sig, b[0], b[1], z_sig, width, 1.0])
+    rows.append([p1[0], p1[1], z_sig, p1[0], p1[1], z_face, width, 1.0])
+    return np.array(rows, float)
+
+
+def plain_plane(n: int = 96, d_mm: float = 0.5, f: float = 1e8) -> Board:
+    """One solid plane, a straight trace 0.2 mm above its top face from (10, 48) to (86, 48)."""
+    d = d_mm * 1e-3
+    t = 35e-6
+    layer = _full_layer("GND", 0.0, t, n, n, d)
+    i0, i1, j = round(10 * n / 96), round(86 * n / 96), n // 2
+    z_face, z_sig = 0.5 * t, 0.5 * t + 0.2e-3
+    pts = [(i0 * d, j * d), (i1 * d, j * d)]
+    net = Net(_segments(pts, z_sig, z_face, 0.2e-3), (0, i0, j), (0, i1, j))
+    return Board("plain_plane", d, n, n, [layer], nets=[net], freqs=np.array([f]), precond="diag",
+                 tol=1e-10, restart=50)
+
+
+def _manhattan_walk(rng, start, mid, end, nseg: int, lo: int, hi_x: int, hi_y: int) -> list:
+    """Cell coordinates of an axis-aligned walk start -> mid -> end with about `nseg` segments; each leg
+    wanders with random steps biased toward its goal and closes with one x and one y move."""
+    pts = [tuple(start)]
+    legs = [(mid, nseg // 2), (end, nseg - nseg // 2)]
+    axis = 0
+    for goal, n in legs:
+        cur = list(pts[-1])
+        for _ in range(max(n - 2, 0)):
+            gap = goal[axis] - cur[axis]
+            step = int(rng.integers(1, 9)) * (1 if rng.random() < 0.5 + 0.35 * np.sign(gap) else -1)
+            nxt = cur.copy()
+            nxt[axis] = int(np.clip(cur[axis] + step, lo, (hi_x if axis == 0 else hi_y)))
+            if nxt[axis] != cur[axis]:
+                cur = nxt
+                pts.append(tuple(cur))
+            axis ^= 1
+        for ax in (axis, axis ^ 1):
+            if cur[ax] != goal[ax]:
+                cur = cur.copy()
+                cur[ax] = goal[ax]
+                pts.append(tuple(cur))
+        axis = 0
+    return pts
+
+
+def slotted_pair(n: int = 256, d_mm: float = 0.25, n_nets: int = 8, n_freq: int = 32, seed: int = 2,
+                 f_lo: float = 1e6, f_hi: float = 1e9, seg_range=(20, 60)) -> Board:
+    """Sig/GND/PWR/Sig with a seeded 1 mm slot across 60 % of the GND plane and random-walk nets on the top
+    signal layer, each crossing the slot, returning in GND (driver/receiver vias at the walk's ends)."""
+    rng = np.random.default_rng(seed)
+    d = d_mm * 1e-3
+    t = 35e-6
+    side = (n - 1) * d
+    length = 0.6 * n * d
+    cx, cy = side * rng.uniform(0.4, 0.6), side * rng.uniform(0.4, 0.6)
+    ang = rng.uniform(0, math.pi)
+    slot = rect_polygon(cx, cy, length, 1e-3, ang)
+    gnd = _full_layer("GND", 0.0, t, n, n, d, [slot])
+    pwr = _full_layer("PWR", -(1.0e-3 + t), t, n, n, d)
+    pair = Pair(0, 1, EPS0 * 4.3 / 1.0e-3, 0.02)
+    z_face, z_sig = 0.5 * t, 0.2e-3 + t
+    u = np.array([math.cos(ang), math.sin(ang)])
+    v = np.array([-u[1], u[0]])
+    margin = max(4, n // 32)
+    nets = []
+    for k in range(n_nets):
+        for _ in range(1000):
+            along = rng.uniform(-0.35, 0.35) * length
+            off = rng.uniform(0.15, 0.4) * side
+            s = np.array([cx, cy]) + along * u - off * v
+            e = np.array([cx, cy]) + rng.uniform(-0.35, 0.35) * length * u + rng.uniform(0.15, 0.4) * side * v
+            m = np.array([cx, cy]) + rng.uniform(-0.3, 0.3) * length * u
+            cs, ce, cm = (np.round(p / d).astype(int) for p in (s, e, m))
+            ok = all(margin <= c[0] < n - margin and margin <= c[1] < n - margin for c in (cs, ce, cm))
+            if ok and gnd.node[cs[0], cs[1]] and gnd.node[ce[0], ce[1]]:
+                break
+        nseg = int(rng.integers(seg_range[0], seg_range[1] + 1))
+        cells = _manhattan_walk(rng, cs, cm, ce, nseg, margin, n - 1 - margin, n - 1 - margin)
+        pts = [(c[0] * d, c[1] * d) for c in cells]
+        nets.append(Net(_segments(pts, z_sig, z_face, 0.15e-3), (0, int(cs[0]), int(cs[1])),
+                        (0, int(ce[0]), int(ce[1]))))
+    freqs = np.logspace(math.log10(f_lo), math.log10(f_hi), n_freq)
+    return Board("slotted_pair", d, n, n, [gnd, pwr], [pair], [], nets, freqs, precond="sheet", tol=1e-10,
+                 restart=50)
+
+
+def small_pair(seed: int = 5) -> Board:
+    """A reduced slotted plane pair (40 x 36 at 0.5 mm) with a decoupling part and a stitching via."""
+    rng = np.random.default_rng(seed)
+    nx, ny, d = 40, 36, 0.5e-3
+    t = 35e-6
+    slot = rect_polygon(20 * d, 17 * d, 0.6 * 36 * d, 1.0e-3, rng.uniform(0.2, 1.2))
+    gnd = _full_layer("GND", 0.0, t, nx, ny, d, [slot])
+    pwr = _full_layer("PWR", -(0.5e-3 + t), 18e-6, nx, ny, d)
+    pair = Pair(0, 1, EPS0 * 4.3 / 0.5e-3, 0.02)
+    # a decap (ESR 20 mohm, ESL 0.5 nH, 100 nF) between GND and PWR, and one via joining them elsewhere
+    decap = BranchSpec((0, 6, 30), (1, 6, 30), 0.02, 0.5e-9, 100e-9, "part")
+    via_len = 0.5e-3 + t
+    via = BranchSpec((0, 33, 4), (1, 33, 4), via_len / (SIGMA_CU * math.pi * 2 * 1.5e-4 * 25e-6), 2.0e-10, 0.0, "via",
+                     1.5e-4)
+    z_face, z_sig = 0.5 * t, 0.2e-3 + t
+    nets = []
+    for (s, m, e) in (((6, 6), (20, 17), (33, 29)), ((34, 8), (18, 18), (8, 26))):
+        cells = _manhattan_walk(rng, s, m, e, 12, 2, nx - 3, ny - 3)
+        pts = [(c[0] * d, c[1] * d) for c in cells]
+        nets.append(Net(_segments(pts, z_sig, z_face, 0.15e-3), (0, *s), (0, *e)))
+    return Board("small_pair", d, nx, ny, [gnd, pwr], [pair], [decap, via], nets, np.array([1e6, 1e8, 1e9]),
+                 precond="sheet", tol=1e-10, restart=50)
+
+
+def small_stack3(seed: int = 9) -> Board:
+    """Three planes (non-square 30 x 44 at 0.4 mm) with polygon cut-outs, stitching vias, diag precond."""
+    rng = np.random.default_rng(seed)
+    nx, ny, d = 30, 44, 0.4e-3
+    t = 35e-6
+    layers = []
+    zs = [0.0, -(0.3e-3 + t), -(1.5e-3 + 2 * t)]
+    for k, z in enumerate(zs):
+        cuts = []
+        for _ in range(int(rng.integers(0, 3))):
+            c = np.array([rng.uniform(0.2, 0.8) * (nx - 1) * d, rng.uniform(0.2, 0.8) * (ny - 1) * d])
+            nv = int(rng.integers(3, 7))
+            ang = np.sort(rng.uniform(0, 2 * math.pi, nv))
+            rad = rng.uniform(0.6e-3, 1.6e-3, nv)
+            cuts.append(c + np.stack([rad * np.cos(ang), rad * np.sin(ang)], 1))
+        layers.append(_full_layer(f"L{k}", z, t, nx, ny, d, cuts))
+    branches = []
+    for _ in range(6):
+        i, j = int(rng.integers(2, nx - 2)), int(rng.integers(2, ny - 2))
+        k0, k1 = 0, int(rng.integers(1, 3))
+        if layers[k0].node[i, j] and layers[k1].node[i, j]:
+            length = abs(zs[k0] - zs[k1])
+            branches.append(BranchSpec((k0, i, j), (k1, i, j), length / (SIGMA_CU * math.pi * 2 * 1.5e-4 * 25e-6),
+                                       2e-10 * length / 1e-3, 0.0, "via", 1.5e-4))
+    z_face, z_sig = 0.5 * t, 0.15e-3 + t
+    ends = [c for c in ((3, 5), (26, 38), (4, 40), (25, 4), (15, 2), (15, 41)) if layers[0].node[c]]
+    s, e = ends[0], ends[1]
+    cells = _manhattan_walk(rng, s, (15, 22), e, 10, 2, nx - 3, ny - 3)
+    pts = [(c[0] * d, c[1] * d) for c in cells]
+    nets = [Net(_segments(pts, z_sig, z_face, 0.2e-3), (0, *s), (0, *e))]
+    return Board("small_stack3", d, nx, ny, layers, [], branches, nets, np.array([3e6, 3e8]), precond="diag",
+                 tol=1e-10, restart=50)
+
+
+WORKLOADS = {"plain_plane": plain_plane, "slotted_pair": slotted_pair, "small_pair": small_pair,
+             "small_stack3": small_stack3}

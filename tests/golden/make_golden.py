@@ -1,0 +1,159 @@
+"""Generate the golden fixtures in this folder by running GroundTruth's own FP64 solver.
+
+Run in a container that has the reference checked out (it is read-only and never travels with the tests):
+
+    python tests/golden/make_golden.py --reference /path/to/GroundTruth [--full]
+
+The reference's solver module imports shapely at module level but uses it only to rasterise copper
+(peec.build_grid), so a stub module is installed before the import and the rasterised grids come from
+``groundtruth_gb300.synth`` (the same masks the GPU build solves).  For each board the script records:
+
+* the board itself (masks, heights, pairs, branches, nets, frequencies)
+* the reference's topology (strip lists, node ids, reference nodes, incidence ends)
+* kernel quadrants, L_self, centre / sum values, sheet blocks
+* the operator at the first frequency (R_strip, z_tail, D^-1, S as COO) and the products
+  matvec(x), precond(x), Lp_matvec(I) on seeded vectors
+* per net and frequency the solve at rtol = board.tol with GMRES(board.restart): unknown vector, its,
+  Z_loop, magnetic moment, psi
+
+``--full`` additionally runs the 256 x 256 slotted plane pair (a few nets x frequencies, minutes per solve)
+and stores only its scalar outputs (Z_loop, its, current norms).
+"""
+from __future__ import annotations
+
+import argparse
+import math
+import sys
+import time
+import types
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parent.parent))
+
+from groundtruth_gb300 import synth  # noqa: E402
+
+
+def import_reference(root: str):
+    sys.modules.setdefault("shapely", types.ModuleType("shapely"))
+    sys.path.insert(0, str(Path(root) / "src"))
+    from groundtruth.solver import kernel, peec  # noqa: E402
+    return peec, kernel
+
+
+def build_reference(peec, board: synth.Board):
+    grids = [peec.Grid(0.0, 0.0, board.d * 1e3, board.nx, board.ny, l.node.copy(), l.xb.copy(), l.yb.copy())
+             for l in board.layers]
+    layers = [peec.PlaneLayer(l.name, l.z, g, l.thickness) for l, g in zip(board.layers, grids)]
+    branches = [peec.Branch(b.a, b.b, (lambda f, b=b: b.z(f)), f"br{n}", b.kind, b.radius)
+                for n, b in enumerate(board.branches)]
+    pairs = [peec.PlanePair(p.upper, p.lower, p.c_per_area, p.tan_delta) for p in board.pairs]
+    st = peec.PlaneStack(layers, branches, pairs, board.sigma, precond=board.precond, screen=False)
+    routes = []
+    for net in board.nets:
+        trace = [peec.TraceSegment(s[0:3].copy(), s[3:6].copy(), float(s[6]), float(s[7])) for s in net.segments]
+        routes.append(peec.RouteExcitation(st, trace, net.driver, net.receiver, net.trace_t))
+    return st, routes
+
+
+def coo(M):
+    M = M.tocoo()
+    return np.stack([M.row, M.col]).astype(np.int64), M.data
+
+
+def record(peec, board: synth.Board, solve: bool = True) -> dict:
+    peec.gmres_restart = lambda n, r=board.restart: r
+    peec.PlaneStack.solve.__defaults__ = (board.tol, 8, None)
+    st, routes = build_reference(peec, board)
+    out = {f"board_{k}": v for k, v in board.to_arrays().items()}
+    out.update(xa=st.xa, ya=st.ya, nid=st.nid, keep=st.keep, a_nodes=st.a_nodes, b_nodes=st.b_nodes,
+               full_label=st.full_label, cond_label=st.cond_label, Px=np.array(st.Px), Py=np.array(st.Py),
+               Kq_x=st._kq["x"], Kq_y=st._kq["y"], L_self=np.float64(st.L_self), nb=np.int64(st.nb),
+               ns=np.int64(st.ns), ncap=np.int64(st.ncap), nbr=np.int64(st.nbr), cap=st.cap)
+    if getattr(st, "B_x", None) is not None:
+        out.update(B_x=st.B_x, B_y=st.B_y)
+    f0 = float(board.freqs[0])
+    op = st.operator(f0)
+    out.update(op_f=np.float64(f0), op_R=op.R_strip, op_z=op.z_tail)
+    out["op_Dinv_ij"], out["op_Dinv"] = coo(op.Dinv)
+    S = (st.ArT @ op.Dinv @ st.Ar)
+    out["op_S_ij"], out["op_S"] = coo(S)
+    rng = np.random.default_rng(123)
+    n = st.nb + st.Ar.shape[1]
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    I = rng.standard_normal(st.ns) + 1j * rng.standard_normal(st.ns)
+    host = peec._HostMath(st)
+    out.update(prod_x=x, prod_matvec=host.matvec(op, x), prod_precond=host.precond(op, x), prod_I=I,
+               prod_Lp=st.Lp_matvec(I))
+    for k, r in enumerate(routes):
+        out[f"psi{k}"] = r.psi
+        out[f"Ltrace{k}"] = np.float64(r.L_trace)
+        if not solve:
+            continue
+        for q, f in enumerate(board.freqs):
+            t0 = time.perf_counter()
+            sol = r.solve(float(f))
+            out[f"Z{k}_{q}"] = np.complex128(sol.Z_loop)
+            out[f"m{k}_{q}"] = sol.m
+            out[f"its{k}_{q}"] = np.int64(sol.iterations)
+            out[f"x{k}_{q}"] = sol.state_for(st)
+            print(f"  {board.name} net {k} f {f:.4g}: its {sol.iterations} Z {sol.Z_loop:.6g} "
+                  f"({time.perf_counter() - t0:.1f} s)", flush=True)
+    return out
+
+
+def kernel_functions(kernel) -> dict:
+    """Point values of the reference's Green's-function helpers."""
+    rng = np.random.default_rng(7)
+    L, ax, rho = 1e-3 * rng.uniform(0.1, 2, 40), 1e-3 * rng.uniform(-5, 5, 40), 1e-3 * rng.uniform(1e-3, 5, 40)
+    tape_args = np.array([[1e-3, 1e-3, 1e-3, 0.0, 0.0, 0.0], [0.5e-3, 0.5e-3, 0.5e-3, 0.5e-3, 0.5e-3, 0.2e-3],
+                          [0.25e-3, 0.25e-3, 0.25e-3, 0.0, 0.75e-3, 1.0e-3], [1e-3, 0.3e-3, 0.7e-3, 2e-3, -0.4e-3, 0.0],
+                          [0.4e-3, 0.4e-3, 0.4e-3, 1.2e-3, 1.6e-3, 1.07e-3]])
+    f = np.logspace(3, 10, 30)
+    return {"fm_args": np.stack([L, ax, rho]), "fm": kernel.filament_mutual(L, ax, rho),
+            "tape_args": tape_args, "tape": np.array([kernel.tape_mutual(*a) for a in tape_args]),
+            "ssn_w": np.array([0.1e-3, 0.25e-3, 1e-3]), "ssn": kernel.strip_self_numeric(1e-3, np.array([0.1e-3, 0.25e-3, 1e-3])),
+            "sk_f": f, "skin35": kernel.skin_thickness(35e-6, f, 5.8e7), "slab18": kernel.slab_impedance(18e-6, f, 5.8e7),
+            "slab35": kernel.slab_impedance(35e-6, f, 5.8e7),
+            "strip_kernel_6x5": kernel.strip_kernel(6, 5, 0.5e-3, 0.3e-3)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", required=True)
+    ap.add_argument("--full", action="store_true")
+    args = ap.parse_args()
+    peec, kernel = import_reference(args.reference)
+    np.savez_compressed(HERE / "kernel_functions.npz", **kernel_functions(kernel))
+    for name in ("small_pair", "small_stack3", "plain_plane"):
+        board = synth.WORKLOADS[name]()
+        print(name, flush=True)
+        np.savez_compressed(HERE / f"{name}.npz", **record(peec, board))
+    if args.full:
+        board = synth.slotted_pair()
+        sub = synth.slotted_pair()
+        sub.nets = sub.nets[:2]
+        sub.freqs = board.freqs[[0, 15, 31]]
+        st, routes = build_reference(peec, sub)
+        peec.gmres_restart = lambda n, r=sub.restart: r
+        peec.PlaneStack.solve.__defaults__ = (sub.tol, 8, None)
+        out = {"freqs": sub.freqs, "Px": np.array(st.Px), "Kq_x_sum": st._kq["x"].sum(axis=(0, 1)),
+               "nb": np.int64(st.nb), "keep_count": np.int64(st.keep.sum())}
+        for k, r in enumerate(routes):
+            out[f"psi{k}_norm"] = np.float64(np.linalg.norm(r.psi))
+            for q, f in enumerate(sub.freqs):
+                t0 = time.perf_counter()
+                sol = r.solve(float(f))
+                out[f"Z{k}_{q}"] = np.complex128(sol.Z_loop)
+                out[f"its{k}_{q}"] = np.int64(sol.iterations)
+                out[f"Ixnorm{k}_{q}"] = np.linalg.norm(sol.I_x.reshape(2, -1), axis=1)
+                out[f"Iynorm{k}_{q}"] = np.linalg.norm(sol.I_y.reshape(2, -1), axis=1)
+                print(f"  slotted_pair net {k} f {f:.4g}: its {sol.iterations} Z {sol.Z_loop:.8g} "
+                      f"({time.perf_counter() - t0:.1f} s)", flush=True)
+        np.savez_compressed(HERE / "slotted_pair_scalars.npz", **out)
+
+
+if __name__ == "__main__":
+    main()

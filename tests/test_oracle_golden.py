@@ -1,0 +1,112 @@
+"""The CPU oracle against the reference's own outputs (tests/golden/*.npz, made by make_golden.py).
+
+These pins are what makes the oracle trustworthy as the GPU build's checker: the restated topology and
+index work must be bit-exact, the kernels, operators and products equal to FP64 rounding, and the solves
+equal to the GMRES tolerance."""
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from groundtruth_gb300 import synth
+from oracle import peec_oracle as po
+
+GOLD = Path(__file__).resolve().parent / "golden"
+CASES = ["small_pair", "small_stack3", "plain_plane"]
+
+
+def load(name):
+    z = np.load(GOLD / f"{name}.npz", allow_pickle=False)
+    board = synth.Board.from_arrays({k[len("board_"):]: z[k] for k in z.files if k.startswith("board_")})
+    return z, board
+
+
+def oracle_stack(board):
+    layers = [po.OLayer(l.z, l.thickness, l.node, l.xb, l.yb) for l in board.layers]
+    pairs = [po.OPair(p.upper, p.lower, p.c_per_area, p.tan_delta) for p in board.pairs]
+    branches = [po.OBranch(b.a, b.b, b.R, b.L, b.C, b.kind, b.radius) for b in board.branches]
+    return po.OracleStack(layers, board.d, branches, pairs, board.sigma, board.precond)
+
+
+def oracle_routes(st, board):
+    out = []
+    for net in board.nets:
+        trace = [po.OSegment(s[0:3].copy(), s[3:6].copy(), float(s[6]), float(s[7])) for s in net.segments]
+        out.append(po.OracleRoute(st, trace, net.driver, net.receiver, net.trace_t))
+    return out
+
+
+@pytest.fixture(scope="module", params=CASES)
+def case(request):
+    z, board = load(request.param)
+    st = oracle_stack(board)
+    return request.param, z, board, st
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(np.asarray(b)), 1e-300)
+
+
+def test_kernel_functions_match_reference():
+    z = np.load(GOLD / "kernel_functions.npz")
+    L, ax, rho = z["fm_args"]
+    assert rel(po.filament_mutual(L, ax, rho), z["fm"]) < 1e-14
+    got = np.array([po.tape_mutual(*a) for a in z["tape_args"]])
+    assert rel(got, z["tape"]) < 1e-13
+    assert rel(po.strip_self_numeric(1e-3, z["ssn_w"]), z["ssn"]) < 1e-14
+    assert rel(po.skin_thickness(35e-6, z["sk_f"], 5.8e7), z["skin35"]) < 1e-14
+    assert rel(po.slab_impedance(18e-6, z["sk_f"], 5.8e7), z["slab18"]) < 1e-14
+    assert rel(po.slab_impedance(35e-6, z["sk_f"], 5.8e7), z["slab35"]) < 1e-14
+    assert rel(po.strip_kernel(6, 5, 0.5e-3, 0.3e-3), z["strip_kernel_6x5"]) < 1e-14
+
+
+def test_topology_is_bit_exact(case):
+    name, z, board, st = case
+    for k in ("xa", "ya", "nid", "keep", "a_nodes", "b_nodes", "full_label", "cond_label"):
+        assert np.array_equal(getattr(st, k), z[k]), k
+    assert (st.nb, st.ns, st.ncap, st.nbr) == (int(z["nb"]), int(z["ns"]), int(z["ncap"]), int(z["nbr"]))
+    assert np.array_equal(st.cap, z["cap"])
+    assert tuple(st.Px) == tuple(z["Px"]) and tuple(st.Py) == tuple(z["Py"])
+
+
+def test_kernels_match_reference(case):
+    name, z, board, st = case
+    assert rel(st.Kq["x"], z["Kq_x"]) < 1e-13
+    assert rel(st.Kq["y"], z["Kq_y"]) < 1e-13
+    assert st.L_self == pytest.approx(float(z["L_self"]), rel=1e-14)
+    if "B_x" in z.files:
+        assert rel(st.B_x, z["B_x"]) < 1e-13 and rel(st.B_y, z["B_y"]) < 1e-13
+
+
+def test_operator_and_products_match_reference(case):
+    name, z, board, st = case
+    op = st.operator(float(z["op_f"]))
+    assert rel(op["R_strip"], z["op_R"]) < 1e-14
+    assert rel(op["z_tail"], z["op_z"]) < 1e-14
+    D = op["Dinv"].tocoo()
+    import scipy.sparse as sp
+    ref = sp.coo_matrix((z["op_Dinv"], tuple(z["op_Dinv_ij"])), shape=D.shape).tocsr()
+    assert abs(op["Dinv"] - ref).max() <= 1e-13 * abs(ref).max()
+    Sref = sp.coo_matrix((z["op_S"], tuple(z["op_S_ij"])), shape=op["S"].shape).tocsr()
+    assert abs(op["S"] - Sref).max() <= 1e-13 * abs(Sref).max()
+    x, I = z["prod_x"], z["prod_I"]
+    assert rel(st.Lp_matvec(I), z["prod_Lp"]) < 1e-12
+    assert rel(st.matvec(op, x), z["prod_matvec"]) < 1e-12
+    assert rel(st.precond(op, x), z["prod_precond"]) < 1e-9
+
+
+def test_coupling_and_solves_match_reference(case):
+    name, z, board, st = case
+    routes = oracle_routes(st, board)
+    for k, r in enumerate(routes):
+        assert rel(r.psi, z[f"psi{k}"]) < 1e-13
+        assert r.L_trace == pytest.approx(float(z[f"Ltrace{k}"]), rel=1e-13)
+        for q, f in enumerate(board.freqs):
+            op = st.operator(float(f))
+            sol = r.solve(float(f), tol=board.tol, restart=board.restart, op=op)
+            # both sides stop at a backward error of tol: the forward difference is within a few cond x tol
+            assert rel(sol["x"], z[f"x{k}_{q}"]) < 1e-7, (k, f)
+            assert abs(sol["Z_loop"] - z[f"Z{k}_{q}"]) <= 1e-8 * abs(z[f"Z{k}_{q}"]), (k, f)
+            assert rel(sol["m"], z[f"m{k}_{q}"]) < 1e-7
+            assert abs(sol["its"] - int(z[f"its{k}_{q}"])) <= 2
