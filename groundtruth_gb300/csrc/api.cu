@@ -1,0 +1,896 @@
+// Host driver and C ABI of the solver (include/gt_gb300.h).
+//
+// A solve (GroundTruth: PlaneStack._solve + _gmres, peec.py:2560-2607, 3093-3224) runs as FP64 iterative
+// refinement around FP32 restarted GMRES: per column
+//     r = b - K x                     FP64 system product (FP64 FFTs), the true residual
+//     stop when ||r|| <= tol ||b||    the reference's stopping rule (peec.py:3119, 3132)
+//     GMRES on K M^-1 u = r / ||r||   FP32 products and preconditioner, FP64 Hessenberg / Givens, up to
+//                                     `restart` iterations or the cycle's target
+//     x += ||r|| M^-1 (V y)           accumulated in FP64
+// precision = 1 runs the same loop with an FP64 inner GMRES (the plain all-FP64 comparator).  Columns are
+// batched: every kernel launch covers all columns still iterating, the factor of a frequency is read once
+// per group of columns that share it.
+#include "../../include/gt_gb300.h"
+#include "solver.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace gt {
+
+static thread_local std::string t_last_error;
+void set_error(const std::string& s) { t_last_error = s; }
+
+struct Invalid : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+// Device allocations owned by an object, freed together.
+struct Pool {
+    std::vector<void*> ptrs;
+    template <typename T> T* alloc(size_t n) {
+        void* p = nullptr;
+        if (n == 0) n = 1;
+        cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+        if (e != cudaSuccess) throw CudaError{e, "cudaMalloc of " + std::to_string(n * sizeof(T)) + " bytes"};
+        ptrs.push_back(p);
+        return static_cast<T*>(p);
+    }
+    template <typename T> T* upload(const T* h, size_t n) {
+        T* d = alloc<T>(n);
+        if (n && h) GT_CUDA(cudaMemcpy(d, h, n * sizeof(T), cudaMemcpyHostToDevice));
+        return d;
+    }
+    void release() {
+        for (void* p : ptrs) cudaFree(p);
+        ptrs.clear();
+    }
+    ~Pool() { release(); }
+};
+
+// Per-kernel-family timing with CUDA events on the launch stream (gt_profile).
+struct Profiler {
+    bool on = false;
+    struct Rec {
+        int fam;
+        cudaEvent_t a, b;
+    };
+    std::vector<Rec> pending;
+    std::vector<cudaEvent_t> free_events;
+    std::vector<std::string> names;
+    std::map<int, std::pair<double, int>> acc;
+    int family(const char* n) {
+        for (size_t i = 0; i < names.size(); ++i)
+            if (names[i] == n) return (int)i;
+        names.push_back(n);
+        return (int)names.size() - 1;
+    }
+    cudaEvent_t ev() {
+        if (!free_events.empty()) {
+            cudaEvent_t e = free_events.back();
+            free_events.pop_back();
+            return e;
+        }
+        cudaEvent_t e;
+        GT_CUDA(cudaEventCreate(&e));
+        return e;
+    }
+    void flush() {
+        for (auto& r : pending) {
+            float ms = 0;
+            GT_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+            auto& a = acc[r.fam];
+            a.first += ms;
+            a.second += 1;
+            free_events.push_back(r.a);
+            free_events.push_back(r.b);
+        }
+        pending.clear();
+    }
+    ~Profiler() {
+        for (auto& r : pending) {
+            cudaEventDestroy(r.a);
+            cudaEventDestroy(r.b);
+        }
+        for (auto e : free_events) cudaEventDestroy(e);
+    }
+};
+
+struct Scope {
+    Profiler* p;
+    int fam;
+    cudaEvent_t a{};
+    cudaStream_t st;
+    Scope(Profiler* prof, const char* name, cudaStream_t s) : p(prof && prof->on ? prof : nullptr), fam(0), st(s) {
+        if (!p) return;
+        fam = p->family(name);
+        a = p->ev();
+        GT_CUDA(cudaEventRecord(a, st));
+    }
+    ~Scope() {
+        if (!p) return;
+        try {
+            cudaEvent_t b = p->ev();
+            if (cudaEventRecord(b, st) == cudaSuccess) p->pending.push_back({fam, a, b});
+        } catch (...) {
+        }
+    }
+};
+
+struct Orient {
+    int n0, n1, P0, P1, di, dj;
+    int64_t off;
+    float* spec32;
+    double* spec64;
+    c32 *tw0_32, *tw1_32;
+    c64 *tw0_64, *tw1_64;
+};
+
+struct Workspace {
+    Pool pool;
+    int ncol = 0, m = 0, prec = -1;
+    // FP64 per column
+    c64 *x64 = nullptr, *r64 = nullptr, *b64 = nullptr, *T64 = nullptr;
+    double *rho = nullptr, *bnorm = nullptr;
+    c64* npart = nullptr;
+    c64* nred = nullptr;
+    // inner (precision R) per slot
+    void *V = nullptr, *w = nullptr, *z = nullptr, *T = nullptr, *zfac = nullptr, *uvec = nullptr;
+    c64* partial = nullptr;
+    GmresState st{};
+    int *slot_col = nullptr, *slot_op = nullptr, *g_col0 = nullptr, *g_ncol = nullptr, *g_op = nullptr, *col_op = nullptr;
+    int* flag_dev = nullptr;
+    int* flag_host = nullptr;
+    int* its_col = nullptr;
+    ~Workspace() {
+        if (flag_host) cudaFreeHost(flag_host);
+    }
+};
+
+}  // namespace gt
+
+using namespace gt;
+
+struct gt_geometry {
+    Geo geo{};
+    Orient o[2]{};
+    Fronts F{};
+    Pool pool;
+    std::vector<int64_t> level_ptr;
+    std::vector<int> level_maxnf;
+    int max_nf = 0;
+    int64_t* d_order = nullptr;
+    int64_t n_compact = 0;
+    int64_t* d_c2d = nullptr;
+    int64_t* d_sterm_ptr = nullptr;
+    int* d_sterm_tab = nullptr;
+    double* d_sterm_coef = nullptr;
+    int64_t maxT = 0;  // largest S * P1 * n0 of the two orientations
+    std::unique_ptr<Workspace> ws;
+    Profiler prof;
+    std::mutex lock;
+};
+
+struct gt_operators {
+    gt_geometry* g = nullptr;
+    int nops = 0;
+    Pool pool;
+    double* omega = nullptr;
+    c64 *zs = nullptr, *zcap = nullptr, *zbr = nullptr, *tab = nullptr;
+    c64* panel64 = nullptr;
+    c32* panel32 = nullptr;
+};
+
+namespace gt {
+
+static int status_of(const CudaError& e) {
+    set_error(std::string(cudaGetErrorString(e.code)) + " (" + e.where + ")");
+    return e.code == cudaErrorMemoryAllocation ? GT_OUT_OF_MEMORY : GT_DEVICE_ERROR;
+}
+
+template <typename R> static const R* spec_of(const Orient& o);
+template <> const float* spec_of<float>(const Orient& o) { return o.spec32; }
+template <> const double* spec_of<double>(const Orient& o) { return o.spec64; }
+template <typename R> static const cx<R>* tw0_of(const Orient& o);
+template <> const c32* tw0_of<float>(const Orient& o) { return o.tw0_32; }
+template <> const c64* tw0_of<double>(const Orient& o) { return o.tw0_64; }
+template <typename R> static const cx<R>* tw1_of(const Orient& o);
+template <> const c32* tw1_of<float>(const Orient& o) { return o.tw1_32; }
+template <> const c64* tw1_of<double>(const Orient& o) { return o.tw1_64; }
+template <typename R> static const cx<R>* panel_of(const gt_operators* ops);
+template <> const c32* panel_of<float>(const gt_operators* ops) { return ops->panel32; }
+template <> const c64* panel_of<double>(const gt_operators* ops) { return ops->panel64; }
+
+static bool good_fft_size(int P) {
+    if (P < 8) return false;
+    if (P % 3 == 0) P /= 3;
+    return P >= 8 && (P & (P - 1)) == 0;
+}
+
+// System product out = K x (mode 0), rhs - K x (1), or the L_p product of the strips (2).
+template <typename R>
+static void matvec(gt_geometry* G, gt_operators* ops, const cx<R>* x, const cx<R>* rhs, cx<R>* out, int64_t ld, int ncol,
+                   const int* col_op, int mode, cx<R>* T, cudaStream_t st) {
+    Profiler* P = &G->prof;
+    for (int k = 0; k < 2; ++k) {
+        const Orient& o = G->o[k];
+        if ((int64_t)o.n0 * o.n1 == 0) continue;
+        LpArgs<R> a{};
+        a.x = x;
+        a.rhs = rhs;
+        a.out = out;
+        a.ld = ld;
+        a.off = o.off;
+        a.off_v = G->geo.off_v;
+        a.S = G->geo.S;
+        a.n0 = o.n0;
+        a.n1 = o.n1;
+        a.nx = G->geo.nx;
+        a.ny = G->geo.ny;
+        a.di = o.di;
+        a.dj = o.dj;
+        a.P0 = o.P0;
+        a.P1 = o.P1;
+        a.ncol = ncol;
+        a.tw0 = tw0_of<R>(o);
+        a.tw1 = tw1_of<R>(o);
+        a.spec = spec_of<R>(o);
+        a.T = T;
+        a.mask = G->geo.mask;
+        a.col_op = col_op;
+        a.omega = ops->omega;
+        a.zs = ops->zs;
+        a.mode = mode;
+        a.col_list = nullptr;
+        Scope s(P, sizeof(R) == 4 ? "lp_fft_f32" : "lp_fft_f64", st);
+        launch_lp<R>(a, st);
+    }
+    if (mode != 2) {
+        Scope s(P, sizeof(R) == 4 ? "tail_f32" : "tail_f64", st);
+        launch_tail<R>(G->geo, x, rhs, out, ld, ncol, col_op, ops->zcap, ops->zbr, mode, st);
+    }
+}
+
+// out = M^-1 r for nslot slots whose vectors are ldr apart (inputs) and ldo apart (outputs)
+template <typename R>
+static void precond(gt_geometry* G, gt_operators* ops, const cx<R>* r, int64_t ldr, cx<R>* out, int64_t ldo, int nslot,
+                    const int* slot_op, const Groups& grp, int gmax, cx<R>* zfac, cx<R>* uvec, cudaStream_t st) {
+    Profiler* P = &G->prof;
+    {
+        Scope s(P, "pc_node", st);
+        launch_pc_node<R>(G->geo, r, ldr, zfac, nslot, slot_op, ops->tab, st);
+    }
+    const cx<R>* panel = panel_of<R>(ops);
+    const int nlev = (int)G->level_ptr.size() - 1;
+    {
+        Scope s(P, sizeof(R) == 4 ? "fwd_f32" : "fwd_f64", st);
+        for (int h = 0; h < nlev; ++h) {
+            int nf = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);
+            launch_fwd_level<R>(G->F, G->d_order + G->level_ptr[h], nf, G->level_maxnf[h], panel, zfac, uvec, grp, gmax, st);
+        }
+    }
+    {
+        Scope s(P, sizeof(R) == 4 ? "bwd_f32" : "bwd_f64", st);
+        for (int h = nlev - 1; h >= 0; --h) {
+            int nf = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);
+            launch_bwd_level<R>(G->F, G->d_order + G->level_ptr[h], nf, G->level_maxnf[h], panel, zfac, grp, gmax, st);
+        }
+    }
+    {
+        Scope s(P, "pc_strip", st);
+        launch_pc_strip<R>(G->geo, r, ldr, zfac, out, ldo, nslot, slot_op, ops->tab, st);
+    }
+}
+
+static int group_max(const gt_geometry* G, size_t elem) {
+    int g = 8;
+    while (g > 1 && (size_t)G->max_nf * g * elem > 200 * 1024) g /= 2;
+    return g;
+}
+
+// slots sorted by operator -> groups of <= gmax consecutive slots sharing one
+static void make_groups(const std::vector<int>& slot_op, int gmax, std::vector<int>& c0, std::vector<int>& nc,
+                        std::vector<int>& op) {
+    c0.clear();
+    nc.clear();
+    op.clear();
+    int n = (int)slot_op.size();
+    for (int s = 0; s < n;) {
+        int e = s;
+        while (e < n && slot_op[e] == slot_op[s] && e - s < gmax) ++e;
+        c0.push_back(s);
+        nc.push_back(e - s);
+        op.push_back(slot_op[s]);
+        s = e;
+    }
+}
+
+static int nchunks(int64_t n) { return (int)((n + 2047) / 2048); }  // DOT_CHUNK in gmres.cu
+
+static void ensure_ws(gt_geometry* G, int ncol, int m, int prec) {
+    auto& w = G->ws;
+    if (w && w->ncol >= ncol && w->m >= m && w->prec == prec) return;
+    w.reset();
+    cudaDeviceSynchronize();
+    w.reset(new Workspace());
+    Workspace& W = *w;
+    W.ncol = ncol;
+    W.m = m;
+    W.prec = prec;
+    const int64_t n = G->geo.n;
+    const size_t es = prec == 1 ? sizeof(c64) : sizeof(c32);
+    Pool& p = W.pool;
+    W.x64 = p.alloc<c64>((size_t)ncol * n);
+    W.r64 = p.alloc<c64>((size_t)ncol * n);
+    W.b64 = p.alloc<c64>((size_t)ncol * n);
+    W.T64 = p.alloc<c64>((size_t)ncol * G->maxT);
+    W.rho = p.alloc<double>(ncol);
+    W.bnorm = p.alloc<double>(ncol);
+    const int nch = nchunks(n);
+    W.npart = p.alloc<c64>((size_t)ncol * nch);
+    W.nred = p.alloc<c64>(ncol);
+    W.V = p.alloc<unsigned char>((size_t)ncol * (m + 1) * n * es);
+    W.w = p.alloc<unsigned char>((size_t)ncol * n * es);
+    W.z = p.alloc<unsigned char>((size_t)ncol * n * es);
+    W.T = p.alloc<unsigned char>((size_t)ncol * G->maxT * es);
+    W.zfac = p.alloc<unsigned char>((size_t)ncol * G->F.nfac * es);
+    W.uvec = p.alloc<unsigned char>((size_t)ncol * std::max<int64_t>(G->F.vec_total, 1) * es);
+    W.partial = p.alloc<c64>((size_t)ncol * nch * (m + 2));
+    GmresState& s = W.st;
+    s.nslot = ncol;
+    s.m = m;
+    s.ldh = m + 2;
+    s.H = p.alloc<c64>((size_t)ncol * (m + 1) * m);
+    s.cs = p.alloc<double>((size_t)ncol * m);
+    s.sn = p.alloc<c64>((size_t)ncol * m);
+    s.g = p.alloc<c64>((size_t)ncol * (m + 1));
+    s.hvec = p.alloc<c64>((size_t)ncol * s.ldh);
+    s.h2vec = p.alloc<c64>((size_t)ncol * s.ldh);
+    s.y = p.alloc<c64>((size_t)ncol * s.ldh);
+    s.hn2 = p.alloc<c64>(ncol);
+    s.hn2b = p.alloc<c64>(ncol);
+    s.it = p.alloc<int>(ncol);
+    s.its_total = p.alloc<int>(ncol);
+    s.active = p.alloc<int>(ncol);
+    s.reorth = p.alloc<int>(ncol);
+    s.eta = p.alloc<double>(ncol);
+    s.inv_hn = p.alloc<double>(ncol);
+    s.resid_est = p.alloc<double>(ncol);
+    W.slot_col = p.alloc<int>(ncol);
+    W.slot_op = p.alloc<int>(ncol);
+    W.g_col0 = p.alloc<int>(ncol);
+    W.g_ncol = p.alloc<int>(ncol);
+    W.g_op = p.alloc<int>(ncol);
+    W.col_op = p.alloc<int>(ncol);
+    W.flag_dev = p.alloc<int>(1);
+    W.its_col = p.alloc<int>(ncol);
+    GT_CUDA(cudaMallocHost(&W.flag_host, sizeof(int)));
+    GT_CUDA(cudaMemset(W.V, 0, (size_t)ncol * (m + 1) * n * es));
+}
+
+// ||v_c|| for ncol FP64 dense vectors -> out (device)
+static void norms64(gt_geometry* G, const c64* v, int64_t ld, int ncol, double* out, cudaStream_t st) {
+    Workspace& W = *G->ws;
+    const int nch = nchunks(G->geo.n);
+    launch_dots<double>(v, 0, ld, 0, v, ld, G->geo.n, ncol, nullptr, W.npart, nch, st);
+    launch_reduce(W.npart, nch, 0, ncol, nullptr, W.nred, 1, 0, st);
+    launch_sqrt_norms(W.nred, 1, ncol, out, st);
+}
+
+template <typename R>
+static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_col_op, const gt_solve_opts& o,
+                      int* its_out, double* resid_out, cudaStream_t st) {
+    Workspace& W = *G->ws;
+    const int64_t n = G->geo.n;
+    const int m = o.restart;
+    const int nch = nchunks(n);
+    Profiler* P = &G->prof;
+    GT_CUDA(cudaMemcpyAsync(W.col_op, h_col_op, ncol * sizeof(int), cudaMemcpyHostToDevice, st));
+    GT_CUDA(cudaMemsetAsync(W.x64, 0, (size_t)ncol * n * sizeof(c64), st));
+    GT_CUDA(cudaMemsetAsync(W.its_col, 0, ncol * sizeof(int), st));
+    GT_CUDA(cudaMemcpyAsync(W.r64, W.b64, (size_t)ncol * n * sizeof(c64), cudaMemcpyDeviceToDevice, st));
+    norms64(G, W.b64, n, ncol, W.bnorm, st);
+    GT_CUDA(cudaMemcpyAsync(W.rho, W.bnorm, ncol * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    std::vector<double> h_bnorm(ncol), h_rho(ncol);
+    std::vector<int> h_its(ncol, 0);
+    GT_CUDA(cudaMemcpyAsync(h_bnorm.data(), W.bnorm, ncol * sizeof(double), cudaMemcpyDeviceToHost, st));
+    GT_CUDA(cudaStreamSynchronize(st));
+    h_rho = h_bnorm;
+    const int gmax = group_max(G, sizeof(cx<R>));
+    cx<R>* V = static_cast<cx<R>*>(W.V);
+    cx<R>* w = static_cast<cx<R>*>(W.w);
+    cx<R>* z = static_cast<cx<R>*>(W.z);
+    cx<R>* T = static_cast<cx<R>*>(W.T);
+    cx<R>* zfac = static_cast<cx<R>*>(W.zfac);
+    cx<R>* uvec = static_cast<cx<R>*>(W.uvec);
+    const int64_t lds = (int64_t)(m + 1) * n;
+    std::vector<int> slot_col, slot_op, c0, nc, gop;
+    for (int outer = 0; outer < o.max_outer; ++outer) {
+        slot_col.clear();
+        for (int c = 0; c < ncol; ++c)
+            if (h_bnorm[c] > 0 && h_rho[c] > o.tol * h_bnorm[c] && h_its[c] < o.max_its) slot_col.push_back(c);
+        if (slot_col.empty()) break;
+        std::stable_sort(slot_col.begin(), slot_col.end(), [&](int a, int b) { return h_col_op[a] < h_col_op[b]; });
+        const int ns = (int)slot_col.size();
+        slot_op.resize(ns);
+        for (int s = 0; s < ns; ++s) slot_op[s] = h_col_op[slot_col[s]];
+        make_groups(slot_op, gmax, c0, nc, gop);
+        GT_CUDA(cudaMemcpyAsync(W.slot_col, slot_col.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
+        GT_CUDA(cudaMemcpyAsync(W.slot_op, slot_op.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
+        GT_CUDA(cudaMemcpyAsync(W.g_col0, c0.data(), c0.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        GT_CUDA(cudaMemcpyAsync(W.g_ncol, nc.data(), nc.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        GT_CUDA(cudaMemcpyAsync(W.g_op, gop.data(), gop.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        std::vector<int> its_slot(ns);
+        for (int s = 0; s < ns; ++s) its_slot[s] = h_its[slot_col[s]];
+        GmresState S = W.st;
+        S.nslot = ns;
+        S.m = m;
+        S.max_its = o.max_its;
+        GT_CUDA(cudaMemcpyAsync(S.its_total, its_slot.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
+        Groups grp{(int)c0.size(), W.g_col0, W.g_ncol, W.g_op};
+        GmresStateT<R> ST{ns, S.active, S.inv_hn, V, w, n, lds};
+        {
+            Scope sc(P, "gmres_small", st);
+            launch_init_state(S, W.slot_col, W.rho, W.bnorm, o.tol, o.inner_tol, st);
+            launch_init_cycle<R>(ST, W.r64, n, W.slot_col, W.rho, n, st);
+        }
+        int jdone = 0;
+        for (int j = 0; j < m; ++j) {
+            precond<R>(G, ops, V + (int64_t)j * n, lds, z, n, ns, W.slot_op, grp, gmax, zfac, uvec, st);
+            matvec<R>(G, ops, z, nullptr, w, n, ns, W.slot_op, 0, T, st);
+            {
+                Scope sc(P, sizeof(R) == 4 ? "gs_f32" : "gs_f64", st);
+                launch_dots<R>(V, n, lds, j + 1, w, n, n, ns, S.active, W.partial, nch, st);
+                launch_reduce(W.partial, nch, j + 1, ns, S.active, S.hvec, S.ldh, 0, st);
+                launch_update<R>(V, n, lds, j + 1, S.hvec, S.ldh, w, n, n, ns, S.active, W.partial, nch, -1, st);
+                launch_reduce(W.partial, nch, 0, ns, S.active, S.hn2, 1, 0, st);
+                launch_dgks(S, j, st);
+                launch_dots<R>(V, n, lds, j + 1, w, n, n, ns, S.reorth, W.partial, nch, st);
+                launch_reduce(W.partial, nch, j + 1, ns, S.reorth, S.h2vec, S.ldh, 0, st);
+                launch_update<R>(V, n, lds, j + 1, S.h2vec, S.ldh, w, n, n, ns, S.reorth, W.partial, nch, -1, st);
+                launch_reduce(W.partial, nch, 0, ns, S.reorth, S.hn2b, 1, 0, st);
+            }
+            {
+                Scope sc(P, "gmres_small", st);
+                launch_givens(S, j, st);
+                if (j + 1 < m) launch_scale<R>(ST, j, n, st);
+                launch_any_active(S.active, ns, W.flag_dev, st);
+            }
+            GT_CUDA(cudaMemcpyAsync(W.flag_host, W.flag_dev, sizeof(int), cudaMemcpyDeviceToHost, st));
+            GT_CUDA(cudaStreamSynchronize(st));
+            jdone = j + 1;
+            if (!*W.flag_host) break;
+        }
+        // the cycle's correction: x += rho * M^-1 (V y)
+        {
+            Scope sc(P, "gmres_small", st);
+            launch_hsolve(S, st);
+        }
+        GT_CUDA(cudaMemsetAsync(w, 0, (size_t)ns * n * sizeof(cx<R>), st));
+        {
+            Scope sc(P, sizeof(R) == 4 ? "gs_f32" : "gs_f64", st);
+            launch_update<R>(V, n, lds, jdone, S.y, S.ldh, w, n, n, ns, nullptr, nullptr, nch, 1, st);
+        }
+        precond<R>(G, ops, w, n, z, n, ns, W.slot_op, grp, gmax, zfac, uvec, st);
+        {
+            Scope sc(P, "refine", st);
+            launch_refine<R>(W.x64, n, z, n, W.slot_col, W.rho, n, ns, st);
+        }
+        // the true residual in FP64
+        matvec<double>(G, ops, W.x64, W.b64, W.r64, n, ncol, W.col_op, 1, W.T64, st);
+        {
+            Scope sc(P, "norms", st);
+            norms64(G, W.r64, n, ncol, W.rho, st);
+        }
+        GT_CUDA(cudaMemcpyAsync(h_rho.data(), W.rho, ncol * sizeof(double), cudaMemcpyDeviceToHost, st));
+        GT_CUDA(cudaMemcpyAsync(its_slot.data(), S.its_total, ns * sizeof(int), cudaMemcpyDeviceToHost, st));
+        GT_CUDA(cudaStreamSynchronize(st));
+        for (int s = 0; s < ns; ++s) h_its[slot_col[s]] = its_slot[s];
+        P->flush();
+    }
+    bool all = true;
+    for (int c = 0; c < ncol; ++c) {
+        double rr = h_bnorm[c] > 0 ? h_rho[c] / h_bnorm[c] : 0.0;
+        if (its_out) its_out[c] = h_its[c];
+        if (resid_out) resid_out[c] = rr;
+        if (!(rr <= o.tol)) all = false;
+    }
+    return all ? GT_OK : GT_NOT_CONVERGED;
+}
+
+static int run_solve(gt_geometry* G, gt_operators* ops, int ncol, const int* col_op, const gt_solve_opts* opts,
+                     int* its, double* res, cudaStream_t st) {
+    gt_solve_opts o = *opts;
+    if (o.restart < 1 || o.restart > 250) throw Invalid("restart must be in 1..250");
+    if (o.max_outer < 1) o.max_outer = 1;
+    for (int c = 0; c < ncol; ++c)
+        if (col_op[c] < 0 || col_op[c] >= ops->nops) throw Invalid("column operator index out of range");
+    if (o.precision == 1) return solve_impl<double>(G, ops, ncol, col_op, o, its, res, st);
+    return solve_impl<float>(G, ops, ncol, col_op, o, its, res, st);
+}
+
+}  // namespace gt
+
+// ------------------------------------------------------------------------------------------ C ABI
+#define GT_GUARD_BEGIN try {
+#define GT_GUARD_END                                                 \
+    }                                                                \
+    catch (const gt::CudaError& e) {                                 \
+        return gt::status_of(e);                                     \
+    }                                                                \
+    catch (const gt::Invalid& e) {                                   \
+        gt::set_error(e.what());                                     \
+        return GT_INVALID_ARGUMENT;                                  \
+    }                                                                \
+    catch (const std::bad_alloc&) {                                  \
+        gt::set_error("host allocation failed");                     \
+        return GT_OUT_OF_MEMORY;                                     \
+    }                                                                \
+    catch (const std::exception& e) {                                \
+        gt::set_error(e.what());                                     \
+        return GT_DEVICE_ERROR;                                      \
+    }
+
+extern "C" {
+
+int gt_version(void) { return 100; }
+
+const char* gt_last_error(void) { return gt::t_last_error.c_str(); }
+
+int gt_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+    return n;
+}
+
+int gt_geometry_create(const gt_geometry_desc* d, gt_geometry** out) {
+    GT_GUARD_BEGIN
+    if (!d || !out) throw Invalid("null argument");
+    if (d->n_sheets < 1 || d->n_sheets > 6) throw Invalid("1 to 6 sheets are supported");
+    if (d->nx < 3 || d->ny < 3) throw Invalid("grid must be at least 3 x 3");
+    for (int k = 0; k < 4; ++k)
+        if (!good_fft_size(d->fft_p[k])) throw Invalid("FFT sizes must be 2^a or 3*2^a with a >= 3");
+    std::unique_ptr<gt_geometry> G(new gt_geometry());
+    Pool& p = G->pool;
+    Geo& g = G->geo;
+    const int S = d->n_sheets, nx = d->nx, ny = d->ny;
+    const int64_t nn = (int64_t)S * nx * ny;
+    g.S = S;
+    g.nx = nx;
+    g.ny = ny;
+    g.np = d->n_pairs;
+    g.nbr = d->n_branches;
+    g.sheet = d->precond_sheet;
+    g.n = d->n_dense;
+    g.off_x = d->off_x;
+    g.off_y = d->off_y;
+    g.off_c = d->off_c;
+    g.off_b = d->off_b;
+    g.off_v = d->off_v;
+    g.mask = p.upload(d->mask, d->n_dense);
+    g.code_x = p.upload(d->code_x, (size_t)(nx - 1) * ny);
+    g.code_y = p.upload(d->code_y, (size_t)nx * (ny - 1));
+    g.pair_layers = p.upload(d->pair_layers, (size_t)2 * d->n_pairs);
+    g.branch_nodes = p.upload(d->branch_nodes, (size_t)2 * d->n_branches);
+    // branch ends per node (CSR over dense nodes)
+    std::vector<int> cnt(nn + 1, 0);
+    for (int b = 0; b < d->n_branches; ++b)
+        for (int e = 0; e < 2; ++e) {
+            int node = d->branch_nodes[2 * b + e];
+            if (node < 0 || node >= nn) throw Invalid("branch node out of range");
+            cnt[node + 1]++;
+        }
+    for (int64_t i = 0; i < nn; ++i) cnt[i + 1] += cnt[i];
+    std::vector<int> idx(std::max(cnt[nn], 1)), fill(cnt.begin(), cnt.end() - 1);
+    for (int b = 0; b < d->n_branches; ++b) {
+        idx[fill[d->branch_nodes[2 * b]]++] = b + 1;
+        idx[fill[d->branch_nodes[2 * b + 1]]++] = -(b + 1);
+    }
+    g.node_br_ptr = p.upload(cnt.data(), cnt.size());
+    g.node_br_idx = p.upload(idx.data(), idx.size());
+    g.perm = p.upload(d->perm, nn);
+    g.nfac = d->n_factor;
+    g.ntab = d->n_table;
+    g.tab_cap0 = 2 * (1 << S) * S * S;
+    g.tab_br0 = g.tab_cap0 + d->n_pairs;
+    if (g.tab_br0 + d->n_branches != d->n_table) throw Invalid("admittance table length mismatch");
+    G->n_compact = d->n_compact;
+    G->d_c2d = p.upload(d->compact_to_dense, d->n_compact);
+    // FFT orientations
+    const double* specs[2] = {d->spectrum_x, d->spectrum_y};
+    for (int k = 0; k < 2; ++k) {
+        Orient& o = G->o[k];
+        o.n0 = k == 0 ? nx - 1 : nx;
+        o.n1 = k == 0 ? ny : ny - 1;
+        o.P0 = d->fft_p[2 * k];
+        o.P1 = d->fft_p[2 * k + 1];
+        if (o.P0 < 2 * o.n0 - 1 || o.P1 < 2 * o.n1 - 1) throw Invalid("FFT size below 2n - 1");
+        if (o.P1 / 8 > 1024 || o.P0 / 8 > 1024) throw Invalid("FFT size too large");
+        o.di = k == 0;
+        o.dj = k == 1;
+        o.off = k == 0 ? d->off_x : d->off_y;
+        size_t q = (size_t)(o.P1 / 2 + 1) * (o.P0 / 2 + 1) * S * S;
+        o.spec64 = p.upload(specs[k], q);
+        std::vector<float> s32(q);
+        for (size_t i = 0; i < q; ++i) s32[i] = (float)specs[k][i];
+        o.spec32 = p.upload(s32.data(), q);
+        for (int ax = 0; ax < 2; ++ax) {
+            int P = ax == 0 ? o.P0 : o.P1;
+            std::vector<c64> t64(P);
+            std::vector<c32> t32(P);
+            for (int m = 0; m < P; ++m) {
+                double a = -2.0 * M_PI * (double)m / (double)P;
+                t64[m] = mk<double>(std::cos(a), std::sin(a));
+                t32[m] = mk<float>((float)t64[m].re, (float)t64[m].im);
+            }
+            (ax == 0 ? o.tw0_64 : o.tw1_64) = p.upload(t64.data(), P);
+            (ax == 0 ? o.tw0_32 : o.tw1_32) = p.upload(t32.data(), P);
+        }
+        G->maxT = std::max<int64_t>(G->maxT, (int64_t)S * o.P1 * o.n0);
+    }
+    // fronts
+    const int nf = d->n_fronts;
+    Fronts& F = G->F;
+    F.nfront = nf;
+    F.own_start = p.upload(d->own_start, nf);
+    F.nown = p.upload(d->nown, nf);
+    F.nbnd = p.upload(d->nbnd, nf);
+    F.bnd_ptr = p.upload(d->bnd_ptr, nf + 1);
+    F.bnd_idx = p.upload(d->bnd_idx, d->bnd_ptr[nf]);
+    F.child_ptr = p.upload(d->child_ptr, nf + 1);
+    F.child_idx = p.upload(d->child_idx, d->child_ptr[nf]);
+    const int64_t nch = d->child_ptr[nf];
+    F.cmap_ptr = p.upload(d->cmap_ptr, nch + 1);
+    F.cmap_idx = p.upload(d->cmap_idx, d->cmap_ptr[nch]);
+    F.panel_off = p.upload(d->panel_off, nf);
+    F.upd_off = p.upload(d->upd_off, nf);
+    F.vec_off = p.upload(d->vec_off, nf);
+    F.ent_ptr = p.upload(d->ent_ptr, nf + 1);
+    F.ent_row = p.upload(d->ent_row, d->ent_ptr[nf]);
+    F.ent_col = p.upload(d->ent_col, d->ent_ptr[nf]);
+    F.ent_s = p.upload(d->ent_s, d->ent_ptr[nf]);
+    F.panel_total = d->panel_total;
+    F.upd_total = d->upd_total;
+    F.vec_total = d->vec_total;
+    F.nsv = d->n_svalues;
+    F.nfac = d->n_factor;
+    G->level_ptr.assign(d->level_ptr, d->level_ptr + d->n_levels + 1);
+    G->d_order = p.upload(d->front_order, nf);
+    for (int h = 0; h < d->n_levels; ++h) {
+        int mx = 1;
+        for (int64_t q = d->level_ptr[h]; q < d->level_ptr[h + 1]; ++q) {
+            int64_t f = d->front_order[q];
+            mx = std::max<int>(mx, (int)(d->nown[f] + d->nbnd[f]));
+        }
+        G->level_maxnf.push_back(mx);
+        G->max_nf = std::max(G->max_nf, mx);
+    }
+    G->d_sterm_ptr = p.upload(d->sterm_ptr, d->n_svalues + 1);
+    G->d_sterm_tab = p.upload(d->sterm_tab, d->sterm_ptr[d->n_svalues]);
+    G->d_sterm_coef = p.upload(d->sterm_coef, d->sterm_ptr[d->n_svalues]);
+    GT_CUDA(cudaDeviceSynchronize());
+    *out = G.release();
+    return GT_OK;
+    GT_GUARD_END
+}
+
+void gt_geometry_free(gt_geometry* g) {
+    if (!g) return;
+    cudaDeviceSynchronize();
+    delete g;
+}
+
+int gt_operators_create(gt_geometry* G, int32_t n_ops, const double* omega, const double* zs, const double* zcap,
+                        const double* zbr, const double* table, gt_operators** out) {
+    GT_GUARD_BEGIN
+    if (!G || !out || n_ops < 1) throw Invalid("bad arguments");
+    std::lock_guard<std::mutex> lk(G->lock);
+    std::unique_ptr<gt_operators> O(new gt_operators());
+    O->g = G;
+    O->nops = n_ops;
+    Pool& p = O->pool;
+    const Geo& g = G->geo;
+    O->omega = p.upload(omega, n_ops);
+    O->zs = p.upload(reinterpret_cast<const c64*>(zs), (size_t)n_ops * g.S);
+    O->zcap = p.upload(reinterpret_cast<const c64*>(zcap), (size_t)n_ops * g.np);
+    O->zbr = p.upload(reinterpret_cast<const c64*>(zbr), (size_t)n_ops * g.nbr);
+    O->tab = p.upload(reinterpret_cast<const c64*>(table), (size_t)n_ops * g.ntab);
+    cudaStream_t st = 0;
+    const Fronts& F = G->F;
+    Pool tmp;
+    c64* svals = tmp.alloc<c64>((size_t)n_ops * F.nsv);
+    c64* upd = tmp.alloc<c64>((size_t)n_ops * std::max<int64_t>(F.upd_total, 1));
+    int* status = tmp.alloc<int>(1);
+    GT_CUDA(cudaMemsetAsync(status, 0, sizeof(int), st));
+    O->panel64 = p.alloc<c64>((size_t)n_ops * F.panel_total);
+    O->panel32 = p.alloc<c32>((size_t)n_ops * F.panel_total);
+    launch_assemble_s(G->d_sterm_ptr, G->d_sterm_tab, G->d_sterm_coef, F.nsv, O->tab, g.ntab, svals, n_ops, st);
+    const int nlev = (int)G->level_ptr.size() - 1;
+    for (int h = 0; h < nlev; ++h) {
+        int nfl = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);
+        launch_factor_level(F, G->d_order + G->level_ptr[h], nfl, G->level_maxnf[h], svals, O->panel64, upd, n_ops, status, st);
+    }
+    launch_panel_to32(O->panel64, O->panel32, (int64_t)n_ops * F.panel_total, st);
+    int h_status = 0;
+    GT_CUDA(cudaMemcpy(&h_status, status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h_status) throw Invalid("the Schur complement has a zero or non-finite pivot (a piece of copper with no "
+                                "path to its reference node?)");
+    *out = O.release();
+    return GT_OK;
+    GT_GUARD_END
+}
+
+void gt_operators_free(gt_operators* ops) {
+    if (!ops) return;
+    cudaDeviceSynchronize();
+    delete ops;
+}
+
+int gt_to_dense(gt_geometry* G, int32_t n_cols, const double* compact, void* dense, void* stream) {
+    GT_GUARD_BEGIN
+    cudaStream_t st = (cudaStream_t)stream;
+    Pool tmp;
+    c64* d_in = tmp.upload(reinterpret_cast<const c64*>(compact), (size_t)n_cols * G->n_compact);
+    GT_CUDA(cudaMemsetAsync(dense, 0, (size_t)n_cols * G->geo.n * sizeof(c64), st));
+    launch_scatter(G->d_c2d, G->n_compact, d_in, G->n_compact, static_cast<c64*>(dense), G->geo.n, n_cols, st);
+    GT_CUDA(cudaStreamSynchronize(st));
+    return GT_OK;
+    GT_GUARD_END
+}
+
+int gt_to_compact(gt_geometry* G, int32_t n_cols, const void* dense, double* compact, void* stream) {
+    GT_GUARD_BEGIN
+    cudaStream_t st = (cudaStream_t)stream;
+    Pool tmp;
+    c64* d_out = tmp.alloc<c64>((size_t)n_cols * G->n_compact);
+    launch_gather(G->d_c2d, G->n_compact, static_cast<const c64*>(dense), G->geo.n, d_out, G->n_compact, n_cols, st);
+    GT_CUDA(cudaMemcpyAsync(compact, d_out, (size_t)n_cols * G->n_compact * sizeof(c64), cudaMemcpyDeviceToHost, st));
+    GT_CUDA(cudaStreamSynchronize(st));
+    return GT_OK;
+    GT_GUARD_END
+}
+
+int gt_solve_device(gt_geometry* G, gt_operators* ops, int32_t n_cols, const int32_t* col_op, const void* rhs_device,
+                    const gt_solve_opts* opts, void* x_device, int32_t* its_out, double* resid_out, void* stream) {
+    GT_GUARD_BEGIN
+    if (!G || !ops || !opts || n_cols < 1) throw Invalid("bad arguments");
+    std::lock_guard<std::mutex> lk(G->lock);
+    cudaStream_t st = (cudaStream_t)stream;
+    ensure_ws(G, n_cols, opts->restart, opts->precision == 1 ? 1 : 0);
+    Workspace& W = *G->ws;
+    GT_CUDA(cudaMemcpyAsync(W.b64, rhs_device, (size_t)n_cols * G->geo.n * sizeof(c64), cudaMemcpyDeviceToDevice, st));
+    int rc = run_solve(G, ops, n_cols, col_op, opts, its_out, resid_out, st);
+    GT_CUDA(cudaMemcpyAsync(x_device, W.x64, (size_t)n_cols * G->geo.n * sizeof(c64), cudaMemcpyDeviceToDevice, st));
+    GT_CUDA(cudaStreamSynchronize(st));
+    if (rc != GT_OK) gt::set_error("GMRES did not converge for at least one column");
+    return rc;
+    GT_GUARD_END
+}
+
+int gt_solve(gt_geometry* G, gt_operators* ops, int32_t n_cols, const int32_t* col_op, const double* rhs,
+             const gt_solve_opts* opts, double* x_out, int32_t* its_out, double* resid_out, void* stream) {
+    GT_GUARD_BEGIN
+    if (!G || !ops || !opts || n_cols < 1 || !rhs || !x_out) throw Invalid("bad arguments");
+    std::lock_guard<std::mutex> lk(G->lock);
+    cudaStream_t st = (cudaStream_t)stream;
+    ensure_ws(G, n_cols, opts->restart, opts->precision == 1 ? 1 : 0);
+    Workspace& W = *G->ws;
+    const int64_t nc = G->n_compact;
+    Pool tmp;
+    c64* d_c = tmp.alloc<c64>((size_t)n_cols * nc);
+    GT_CUDA(cudaMemcpyAsync(d_c, rhs, (size_t)n_cols * nc * sizeof(c64), cudaMemcpyHostToDevice, st));
+    GT_CUDA(cudaMemsetAsync(W.b64, 0, (size_t)n_cols * G->geo.n * sizeof(c64), st));
+    launch_scatter(G->d_c2d, nc, d_c, nc, W.b64, G->geo.n, n_cols, st);
+    int rc = run_solve(G, ops, n_cols, col_op, opts, its_out, resid_out, st);
+    launch_gather(G->d_c2d, nc, W.x64, G->geo.n, d_c, nc, n_cols, st);
+    GT_CUDA(cudaMemcpyAsync(x_out, d_c, (size_t)n_cols * nc * sizeof(c64), cudaMemcpyDeviceToHost, st));
+    GT_CUDA(cudaStreamSynchronize(st));
+    if (rc != GT_OK) gt::set_error("GMRES did not converge for at least one column");
+    return rc;
+    GT_GUARD_END
+}
+
+int gt_apply(gt_geometry* G, gt_operators* ops, int32_t kind, int32_t precision, int32_t n_cols, const int32_t* col_op,
+             const double* x, double* y, void* stream) {
+    GT_GUARD_BEGIN
+    if (!G || !ops || n_cols < 1 || kind < 0 || kind > 2) throw Invalid("bad arguments");
+    std::lock_guard<std::mutex> lk(G->lock);
+    for (int c = 0; c < n_cols; ++c)
+        if (col_op[c] < 0 || col_op[c] >= ops->nops) throw Invalid("column operator index out of range");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t n = G->geo.n, nc = G->n_compact;
+    Pool tmp;
+    c64* d_c = tmp.upload(reinterpret_cast<const c64*>(x), (size_t)n_cols * nc);
+    c64* xin = tmp.alloc<c64>((size_t)n_cols * n);
+    c64* yout = tmp.alloc<c64>((size_t)n_cols * n);
+    int* d_op = tmp.upload(col_op, n_cols);
+    GT_CUDA(cudaMemsetAsync(xin, 0, (size_t)n_cols * n * sizeof(c64), st));
+    GT_CUDA(cudaMemsetAsync(yout, 0, (size_t)n_cols * n * sizeof(c64), st));
+    launch_scatter(G->d_c2d, nc, d_c, nc, xin, n, n_cols, st);
+    std::vector<int> h_op(col_op, col_op + n_cols);
+    // kind 1 groups columns by operator: require them sorted
+    for (int c = 1; c < n_cols; ++c)
+        if (kind == 1 && h_op[c] < h_op[c - 1]) throw Invalid("preconditioner columns must be sorted by operator");
+    auto run = [&](auto tag) {
+        using R = decltype(tag);
+        cx<R>* xi;
+        cx<R>* yo;
+        if constexpr (sizeof(R) == 8) {
+            xi = xin;
+            yo = yout;
+        } else {
+            xi = tmp.alloc<c32>((size_t)n_cols * n);
+            yo = tmp.alloc<c32>((size_t)n_cols * n);
+            // round the input to FP32 through a refine-style copy: y = 1.0 * x
+            std::vector<c64> hx((size_t)n_cols * n);
+            GT_CUDA(cudaMemcpy(hx.data(), xin, hx.size() * sizeof(c64), cudaMemcpyDeviceToHost));
+            std::vector<c32> h32(hx.size());
+            for (size_t i = 0; i < hx.size(); ++i) h32[i] = cvt<float>(hx[i]);
+            GT_CUDA(cudaMemcpy(xi, h32.data(), h32.size() * sizeof(c32), cudaMemcpyHostToDevice));
+        }
+        if (kind == 0 || kind == 2) {
+            cx<R>* T = tmp.alloc<cx<R>>((size_t)n_cols * G->maxT);
+            matvec<R>(G, ops, xi, nullptr, yo, n, n_cols, d_op, kind == 0 ? 0 : 2, T, st);
+        } else {
+            std::vector<int> c0, ncv, gop;
+            const int gmax = group_max(G, sizeof(cx<R>));
+            make_groups(h_op, gmax, c0, ncv, gop);
+            int* g0 = tmp.upload(c0.data(), c0.size());
+            int* g1 = tmp.upload(ncv.data(), ncv.size());
+            int* g2 = tmp.upload(gop.data(), gop.size());
+            Groups grp{(int)c0.size(), g0, g1, g2};
+            cx<R>* zf = tmp.alloc<cx<R>>((size_t)n_cols * G->F.nfac);
+            cx<R>* uv = tmp.alloc<cx<R>>((size_t)n_cols * std::max<int64_t>(G->F.vec_total, 1));
+            precond<R>(G, ops, xi, n, yo, n, n_cols, d_op, grp, gmax, zf, uv, st);
+        }
+        if constexpr (sizeof(R) == 4) {
+            std::vector<c32> h32((size_t)n_cols * n);
+            GT_CUDA(cudaStreamSynchronize(st));
+            GT_CUDA(cudaMemcpy(h32.data(), yo, h32.size() * sizeof(c32), cudaMemcpyDeviceToHost));
+            std::vector<c64> h64(h32.size());
+            for (size_t i = 0; i < h32.size(); ++i) h64[i] = cvt<double>(h32[i]);
+            GT_CUDA(cudaMemcpy(yout, h64.data(), h64.size() * sizeof(c64), cudaMemcpyHostToDevice));
+        }
+    };
+    if (precision == 1) run(double{});
+    else run(float{});
+    launch_gather(G->d_c2d, nc, yout, n, d_c, nc, n_cols, st);
+    GT_CUDA(cudaMemcpyAsync(y, d_c, (size_t)n_cols * nc * sizeof(c64), cudaMemcpyDeviceToHost, st));
+    GT_CUDA(cudaStreamSynchronize(st));
+    return GT_OK;
+    GT_GUARD_END
+}
+
+int gt_profile(gt_geometry* G, char* names, int32_t names_cap, double* ms, int32_t* launches, int32_t cap) {
+    if (!G) return 0;
+    if (names == nullptr && cap < 0) {  // toggle: cap = -1 off, -2 on (and reset)
+        G->prof.on = cap == -2;
+        G->prof.acc.clear();
+        return 0;
+    }
+    std::string s;
+    int k = 0;
+    for (auto& kv : G->prof.acc) {
+        if (k >= cap) break;
+        if (!s.empty()) s += ",";
+        s += G->prof.names[kv.first];
+        ms[k] = kv.second.first;
+        launches[k] = kv.second.second;
+        ++k;
+    }
+    if (names && names_cap > 0) {
+        std::strncpy(names, s.c_str(), names_cap - 1);
+        names[names_cap - 1] = 0;
+    }
+    return k;
+}
+
+}  // extern "C"

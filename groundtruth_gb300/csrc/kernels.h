@@ -1,0 +1,116 @@
+// Launch interfaces between the kernel files and the host driver (api.cu).
+#pragma once
+#include "common.cuh"
+
+namespace gt {
+
+// The geometry as the kernels see it (device pointers, sizes).
+struct Geo {
+    int S, nx, ny, np, nbr, sheet;
+    int64_t n, off_x, off_y, off_c, off_b, off_v;
+    const uint8_t* mask;
+    const uint8_t* code_x;
+    const uint8_t* code_y;
+    const int* pair_layers;      // [np*2]
+    const int* branch_nodes;     // [nbr*2] dense node index
+    const int* node_br_ptr;      // [S*nx*ny + 1] CSR of branch ends per dense node
+    const int* node_br_idx;      // branch index + 1, negated for the b end
+    const int64_t* perm;         // dense node -> factor index or -1
+    int64_t nfac;
+    int ntab, tab_cap0, tab_br0;
+};
+
+template <typename R> struct LpArgs {
+    const cx<R>* x;
+    const cx<R>* rhs;
+    cx<R>* out;
+    int64_t ld, off, off_v;
+    int S, n0, n1, nx, ny, di, dj, P0, P1, ncol;
+    const cx<R>* tw0;      // twiddles of the column length P0
+    const cx<R>* tw1;      // of the row length P1
+    const R* spec;         // (Q1, Q0, S, S)
+    cx<R>* T;              // [ncol][S][P1][n0]
+    const uint8_t* mask;
+    const int* col_op;
+    const double* omega;
+    const c64* zs;
+    int mode;
+    const int* col_list;
+};
+
+template <typename R> void launch_lp(const LpArgs<R>& a, cudaStream_t st);
+
+// capacitance / branch / node rows of the system product (mode 0: K x, 1: rhs - K x); also zeroes the
+// padding between segments
+template <typename R>
+void launch_tail(const Geo& g, const cx<R>* x, const cx<R>* rhs, cx<R>* out, int64_t ld, int ncol, const int* col_op,
+                 const c64* zcap, const c64* zbr, int mode, cudaStream_t st);
+
+// preconditioner: s = r_V - Ar^T D^-1 r_1 into factor order; then out = [D^-1 (r_1 + Ar y); y]
+template <typename R>
+void launch_pc_node(const Geo& g, const cx<R>* r, int64_t ld, cx<R>* s_fac, int ncol, const int* col_op,
+                    const c64* tab, cudaStream_t st);
+template <typename R>
+void launch_pc_strip(const Geo& g, const cx<R>* r, int64_t ldr, const cx<R>* y_fac, cx<R>* out, int64_t ldo, int ncol,
+                     const int* col_op, const c64* tab, cudaStream_t st);
+
+// compact <-> dense
+void launch_scatter(const int64_t* c2d, int64_t ncomp, const c64* in, int64_t ldin, c64* out, int64_t ldout, int ncol,
+                    cudaStream_t st);
+void launch_gather(const int64_t* c2d, int64_t ncomp, const c64* in, int64_t ldin, c64* out, int64_t ldout, int ncol,
+                   cudaStream_t st);
+
+// --- multifrontal factorisation and solves
+struct Fronts {
+    int nfront;
+    const int64_t* own_start;
+    const int64_t* nown;
+    const int64_t* nbnd;
+    const int64_t* bnd_ptr;
+    const int64_t* bnd_idx;
+    const int64_t* child_ptr;
+    const int64_t* child_idx;
+    const int64_t* cmap_ptr;
+    const int64_t* cmap_idx;
+    const int64_t* panel_off;
+    const int64_t* upd_off;
+    const int64_t* vec_off;
+    const int64_t* ent_ptr;
+    const int* ent_row;
+    const int* ent_col;
+    const int64_t* ent_s;
+    int64_t panel_total, upd_total, vec_total, nsv, nfac;
+};
+
+void launch_assemble_s(const int64_t* ptr, const int* tab_idx, const double* coef, int64_t nsv, const c64* table,
+                       int ntab, c64* svals, int nops, cudaStream_t st);
+// one elimination level: fronts front_list[0..nf) for each operator
+void launch_factor_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, const c64* svals,
+                         c64* panel, c64* upd, int nops, int* status, cudaStream_t st);
+void launch_panel_to32(const c64* p64, c32* p32, int64_t n, cudaStream_t st);
+
+// triangular solves, per level; groups of columns sharing an operator
+struct Groups {
+    int ngroup;
+    const int* col0;
+    const int* ncol;
+    const int* op;
+};
+template <typename R>
+void launch_fwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, const cx<R>* panel,
+                      cx<R>* z, cx<R>* uvec, const Groups& G, int gmax, cudaStream_t st);
+template <typename R>
+void launch_bwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, const cx<R>* panel,
+                      cx<R>* z, const Groups& G, int gmax, cudaStream_t st);
+
+// --- Krylov vector work (batched, one basis per slot)
+template <typename R>
+void launch_dots(const cx<R>* V, int64_t ldv, int64_t lds, int nv, const cx<R>* w, int64_t ldw, int64_t n, int nslot,
+                 const int* active, c64* partial, int nchunk, cudaStream_t st);
+void launch_reduce(const c64* partial, int nchunk, int nv, int nslot, const int* active, c64* out, int ldo, int mode,
+                   cudaStream_t st);
+template <typename R>
+void launch_update(const cx<R>* V, int64_t ldv, int64_t lds, int nv, const c64* h, int ldh, cx<R>* w, int64_t ldw,
+                   int64_t n, int nslot, const int* active, c64* partial, int nchunk, int sign, cudaStream_t st);
+
+}  // namespace gt

@@ -1,0 +1,191 @@
+// The partial-inductance product and the strip rows of the system product, as three FFT passes per strip
+// orientation over a batch of columns (GroundTruth: PlaneStack.Lp_matvec / _conv, peec.py:2054-2135, and
+// the strip rows of _HostMath.matvec, peec.py:3043-3062).
+//
+// An orientation's currents are a grid (S, n0, n1) of the dense vector; the FFT grid is (P0, P1) with
+// P >= 2n - 1 per axis, so the circular convolution equals the linear one on the grid.
+//   pass A  row FFTs (length P1) of the n0 rows, zero padded; written transposed T[col][s][c][i]
+//   pass B  per pixel column c: column FFTs (length P0) of all sheets, the per-pixel S x S real spectrum
+//           multiply-add (the quadrant mirrored: K(p0, p1) = Kq(min(p0, P0-p0), min(p1, P1-p1))), inverse
+//           column FFTs; rows i < n0 written back in place
+//   pass C  inverse row FFTs, then the fused epilogue on the strips:
+//           out = R_t x + j w L_p x - (V[a] - V[b])     (or rhs - that, for residuals; or L_p x alone)
+// The spectrum is stored (Q1, Q0, S, S) and pre-scaled by 1/(P0 P1).
+#include "common.cuh"
+#include "fft.cuh"
+#include "kernels.h"
+
+namespace gt {
+
+constexpr int MAXS = 8;
+
+template <typename R>
+__global__ void __launch_bounds__(1024) lp_pass_a(const cx<R>* __restrict__ x, int64_t ldx, int64_t off, int S, int n0, int n1, int P1,
+                          int rows, const cx<R>* __restrict__ tw, cx<R>* __restrict__ T, const int* __restrict__ col_list) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw);
+    const int stride = P1 + 1;
+    const int i0 = blockIdx.x * rows;
+    const int s = blockIdx.y;
+    const int col = col_list ? col_list[blockIdx.z] : blockIdx.z;
+    const cx<R>* xs = x + (int64_t)col * ldx + off + (int64_t)s * n0 * n1;
+    for (int idx = threadIdx.x; idx < rows * P1; idx += blockDim.x) {
+        int r = idx / P1, j = idx - r * P1;
+        int i = i0 + r;
+        buf[r * stride + j] = (i < n0 && j < n1) ? xs[(int64_t)i * n1 + j] : zero<R>();
+    }
+    __syncthreads();
+    const int team = P1 / 8;
+    const int r = threadIdx.x / team, t = threadIdx.x - r * team;
+    fft_row<R, false>(buf + r * stride, r < rows, P1, tw, team, t);
+    cx<R>* Ts = T + ((int64_t)blockIdx.z * S + s) * (int64_t)P1 * n0;
+    for (int idx = threadIdx.x; idx < rows * P1; idx += blockDim.x) {
+        int c = idx / rows, rr = idx - c * rows;
+        int i = i0 + rr;
+        if (i < n0) Ts[(int64_t)c * n0 + i] = buf[rr * stride + c];
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(1024) lp_pass_b(int S, int n0, int P0, int P1, int ncol, int bt, const R* __restrict__ spec,
+                          const cx<R>* __restrict__ tw, cx<R>* __restrict__ T) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw);
+    const int stride = P0 + 1;
+    const int c = blockIdx.x;
+    const int b0 = blockIdx.y * bt;
+    const int nb = min(bt, ncol - b0);
+    const int nrows = nb * S;
+    for (int idx = threadIdx.x; idx < nrows * P0; idx += blockDim.x) {
+        int row = idx / P0, p = idx - row * P0;
+        int b = row / S, s = row - b * S;
+        buf[row * stride + p] = p < n0 ? T[(((int64_t)(b0 + b) * S + s) * P1 + c) * n0 + p] : zero<R>();
+    }
+    __syncthreads();
+    const int team = P0 / 8;
+    const int row = threadIdx.x / team, t = threadIdx.x - row * team;
+    fft_row<R, false>(buf + row * stride, row < nrows, P0, tw, team, t);
+    // spectrum multiply-add over sheets, one (column, pixel) per thread iteration
+    const int Q0 = P0 / 2 + 1;
+    const int q1 = min(c, P1 - c);
+    const R* Kc = spec + (int64_t)q1 * Q0 * S * S;
+    for (int idx = threadIdx.x; idx < nb * P0; idx += blockDim.x) {
+        int b = idx / P0, p = idx - b * P0;
+        int q0 = min(p, P0 - p);
+        const R* K = Kc + (int64_t)q0 * S * S;
+        cx<R> u[MAXS];
+#pragma unroll
+        for (int s = 0; s < MAXS; ++s)
+            if (s < S) u[s] = buf[(b * S + s) * stride + p];
+#pragma unroll
+        for (int tt = 0; tt < MAXS; ++tt) {
+            if (tt < S) {
+                cx<R> acc = zero<R>();
+#pragma unroll
+                for (int s = 0; s < MAXS; ++s)
+                    if (s < S) {
+                        R k = __ldg(K + tt * S + s);
+                        acc.re += k * u[s].re;
+                        acc.im += k * u[s].im;
+                    }
+                buf[(b * S + tt) * stride + p] = acc;
+            }
+        }
+    }
+    __syncthreads();
+    fft_row<R, true>(buf + row * stride, row < nrows, P0, tw, team, t);
+    for (int idx = threadIdx.x; idx < nrows * n0; idx += blockDim.x) {
+        int rr = idx / n0, p = idx - rr * n0;
+        int b = rr / S, s = rr - b * S;
+        T[(((int64_t)(b0 + b) * S + s) * P1 + c) * n0 + p] = buf[rr * stride + p];
+    }
+}
+
+// mode 0: out = R_t x + j w L - (V[a] - V[b]); 1: out = rhs - (that); 2: out = L
+template <typename R>
+__global__ void __launch_bounds__(1024) lp_pass_c(const cx<R>* __restrict__ T, const cx<R>* __restrict__ x, const cx<R>* __restrict__ rhs,
+                          cx<R>* __restrict__ out, int64_t ld, int64_t off, int64_t off_v, int S, int n0, int n1,
+                          int nx, int ny, int di, int dj, int P1, int rows, const cx<R>* __restrict__ tw,
+                          const uint8_t* __restrict__ mask, const int* __restrict__ col_op,
+                          const double* __restrict__ omega, const c64* __restrict__ zs, int mode,
+                          const int* __restrict__ col_list) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw);
+    const int stride = P1 + 1;
+    const int i0 = blockIdx.x * rows;
+    const int s = blockIdx.y;
+    const int col = col_list ? col_list[blockIdx.z] : blockIdx.z;
+    const cx<R>* Ts = T + ((int64_t)blockIdx.z * S + s) * (int64_t)P1 * n0;
+    for (int idx = threadIdx.x; idx < rows * P1; idx += blockDim.x) {
+        int c = idx / rows, rr = idx - c * rows;
+        int i = i0 + rr;
+        buf[rr * stride + c] = i < n0 ? Ts[(int64_t)c * n0 + i] : zero<R>();
+    }
+    __syncthreads();
+    const int team = P1 / 8;
+    const int r = threadIdx.x / team, t = threadIdx.x - r * team;
+    fft_row<R, true>(buf + r * stride, r < rows, P1, tw, team, t);
+    const int op = col_op ? col_op[col] : 0;
+    const R w = omega ? R(omega[op]) : R(0);
+    const cx<R> z = zs ? cvt<R>(zs[(int64_t)op * S + s]) : zero<R>();
+    const int64_t base = (int64_t)col * ld;
+    for (int idx = threadIdx.x; idx < rows * n1; idx += blockDim.x) {
+        int rr = idx / n1, j = idx - rr * n1;
+        int i = i0 + rr;
+        if (i >= n0) continue;
+        int64_t pos = off + ((int64_t)s * n0 + i) * n1 + j;
+        cx<R> L = buf[rr * stride + j];
+        cx<R> y;
+        if (mode == 2) {
+            y = mask[pos] ? L : zero<R>();
+        } else if (!mask[pos]) {
+            y = zero<R>();
+        } else {
+            cx<R> xv = x[base + pos];
+            int64_t va = off_v + ((int64_t)s * nx + i) * ny + j;
+            int64_t vb = va + (int64_t)di * ny + dj;
+            cx<R> dv = x[base + va] - x[base + vb];
+            y = z * xv + w * jmul(L) - dv;
+            if (mode == 1) y = rhs[base + pos] - y;
+        }
+        out[base + pos] = y;
+    }
+}
+
+// ------------------------------------------------------------------------------------------ launchers
+template <typename R>
+static void set_smem(const void* fn, size_t bytes) {
+    if (bytes > 48 * 1024) GT_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+}
+
+template <typename R>
+void launch_lp(const LpArgs<R>& a, cudaStream_t st) {
+    // pass A / C: rows per block so that the transposed stores are >= 128 B per row segment when possible
+    const int teamA = a.P1 / 8;
+    int rows = (sizeof(R) == 4 ? 16 : 8);
+    while (rows > 1 && (rows * teamA > 1024 || (size_t)rows * (a.P1 + 1) * sizeof(cx<R>) > 160 * 1024)) rows /= 2;
+    size_t smA = (size_t)rows * (a.P1 + 1) * sizeof(cx<R>);
+    dim3 gA(ceil_div(a.n0, rows), a.S, a.ncol);
+    set_smem<R>((const void*)lp_pass_a<R>, smA);
+    lp_pass_a<R><<<gA, rows * teamA, smA, st>>>(a.x, a.ld, a.off, a.S, a.n0, a.n1, a.P1, rows, a.tw1, a.T, a.col_list);
+    GT_LAUNCH_CHECK();
+    const int teamB = a.P0 / 8;
+    int bt = 1;
+    while (bt < 8 && (bt * 2) * a.S * teamB <= 1024 && (size_t)(bt * 2) * a.S * (a.P0 + 1) * sizeof(cx<R>) <= 100 * 1024)
+        bt *= 2;
+    size_t smB = (size_t)bt * a.S * (a.P0 + 1) * sizeof(cx<R>);
+    dim3 gB(a.P1, ceil_div(a.ncol, bt));
+    set_smem<R>((const void*)lp_pass_b<R>, smB);
+    lp_pass_b<R><<<gB, bt * a.S * teamB, smB, st>>>(a.S, a.n0, a.P0, a.P1, a.ncol, bt, a.spec, a.tw0, a.T);
+    GT_LAUNCH_CHECK();
+    set_smem<R>((const void*)lp_pass_c<R>, smA);
+    lp_pass_c<R><<<gA, rows * teamA, smA, st>>>(a.T, a.x, a.rhs, a.out, a.ld, a.off, a.off_v, a.S, a.n0, a.n1, a.nx, a.ny,
+                                                a.di, a.dj, a.P1, rows, a.tw1, a.mask, a.col_op, a.omega, a.zs, a.mode,
+                                                a.col_list);
+    GT_LAUNCH_CHECK();
+}
+
+template void launch_lp<float>(const LpArgs<float>&, cudaStream_t);
+template void launch_lp<double>(const LpArgs<double>&, cudaStream_t);
+
+}  // namespace gt

@@ -1,0 +1,51 @@
+// Per-slot GMRES state shared by gmres.cu and the driver.
+#pragma once
+#include "kernels.h"
+
+namespace gt {
+
+struct GmresState {
+    int nslot, m, ldh, max_its;
+    c64* H;            // [slot][m][m+1] rotated Hessenberg columns
+    double* cs;        // [slot][m]
+    c64* sn;           // [slot][m]
+    c64* g;            // [slot][m+1]
+    c64* hvec;         // [slot][ldh] first-pass projections, |w|^2 at index j+1
+    c64* h2vec;        // [slot][ldh] second-pass projections
+    c64* y;            // [slot][ldh] least-squares solution
+    c64* hn2;          // [slot] |w|^2 after the first pass
+    c64* hn2b;         // [slot] after the second
+    int* it;           // [slot] iterations of the current cycle
+    int* its_total;    // [slot] iterations of the column so far (copied in and out per cycle)
+    int* active;       // [slot]
+    int* reorth;       // [slot]
+    double* eta;       // [slot] the cycle's relative target
+    double* inv_hn;    // [slot]
+    double* resid_est; // [slot]
+};
+
+template <typename R> struct GmresStateT {
+    int nslot;
+    int* active;
+    double* inv_hn;
+    cx<R>* V;          // [slot][m+1][ldv]
+    cx<R>* w;          // [slot][ldv]
+    int64_t ldv, lds;
+};
+
+void launch_dgks(const GmresState& s, int j, cudaStream_t st);
+void launch_givens(const GmresState& s, int j, cudaStream_t st);
+template <typename R> void launch_scale(const GmresStateT<R>& s, int j, int64_t n, cudaStream_t st);
+void launch_hsolve(const GmresState& s, cudaStream_t st);
+template <typename R>
+void launch_init_cycle(const GmresStateT<R>& s, const c64* r, int64_t ldr, const int* slot_col, const double* rho,
+                       int64_t n, cudaStream_t st);
+void launch_init_state(const GmresState& s, const int* slot_col, const double* rho, const double* bnorm, double tol,
+                       double inner_tol, cudaStream_t st);
+template <typename R>
+void launch_refine(c64* x, int64_t ldx, const cx<R>* e, int64_t lde, const int* slot_col, const double* rho, int64_t n,
+                   int nslot, cudaStream_t st);
+void launch_any_active(const int* active, int n, int* flag, cudaStream_t st);
+void launch_sqrt_norms(const c64* nrm2, int ld, int n, double* out, cudaStream_t st);
+
+}  // namespace gt

@@ -1,0 +1,250 @@
+"""Host-side FP64 setup physics of the plane solve: partial inductances, strip kernels and their spectra,
+sheet impedances, the signal path's coupling into the strips, its own inductance and resistance.
+
+These run once per geometry (kernels, coupling) or once per frequency (impedances) on the host; the
+per-iteration work is in the CUDA library.  The formulas are GroundTruth's:
+
+* filament mutual inductance (Neumann, closed form)      src/groundtruth/solver/kernel.py:165-176
+* flat-tape mutual by the width-difference integral       src/groundtruth/solver/kernel.py:219-265
+* strip self inductance (numeric) / GMD formula           src/groundtruth/solver/kernel.py:179-206
+* strip kernel: filaments far, tapes for |offset| <= 4    src/groundtruth/solver/kernel.py:268-294
+* one-face slab impedance, Dowell skin thickness          src/groundtruth/solver/kernel.py:23-75
+* vector potential of a filament, segment mutual          src/groundtruth/solver/kernel.py:297-337
+* strip coupling psi (3 x 3 Gauss points near the trace)  src/groundtruth/solver/peec.py:2615-2656
+* trace self inductance and resistance                    src/groundtruth/solver/peec.py:3227-3250
+
+The spectra are computed at this build's own padded FFT sizes (any size >= 2n - 1 gives the same linear
+convolution; the reference uses scipy's next_fast_len, peec.py:1952-1953).
+"""
+from __future__ import annotations
+
+import math
+from functools import lru_cache
+
+import numpy as np
+from numpy.polynomial import legendre
+
+MU0 = 4e-7 * np.pi
+GMD_FLAT = 0.2235
+NEAR = 4                 # kernel.py:287: offsets integrated as tapes
+PANELS, ORDER = 30, 8    # kernel.py:215-216
+
+
+def round12(v: float) -> float:
+    """A pitch or gap as the kernels are computed for it: 12 significant digits (peec.py:3264-3273)."""
+    return float(f"{float(v):.12g}")
+
+
+@lru_cache(maxsize=None)
+def gauss(n: int):
+    x, w = legendre.leggauss(n)
+    return x, w
+
+
+def filament_mutual(length, axial, rho):
+    rho = np.maximum(rho, 1e-12 * length)
+
+    def G(u):
+        return u * np.arcsinh(u / rho) - np.sqrt(u * u + rho * rho)
+    return MU0 / (4 * np.pi) * (G(axial + length) - 2 * G(axial) + G(axial - length))
+
+
+def _graded(p: float, q: float, toward, panels: int, order: int):
+    x, w = gauss(order)
+    if toward is None:
+        e = np.linspace(0.0, 1.0, panels + 1)
+    else:
+        e = np.concatenate([[0.0], 0.5 ** np.arange(panels - 1, -1, -1)])
+        if toward == q:
+            e = 1.0 - e[::-1]
+    a, b = e[:-1, None], e[1:, None]
+    return (p + (q - p) * (a + (b - a) * (x[None] + 1.0) / 2.0)).ravel(), ((q - p) * (b - a) * w[None] / 2.0).ravel()
+
+
+def tape_mutual(length, wa, wb, axial, lateral, dz) -> float:
+    h, k, s = 0.5 * (wa + wb), 0.5 * abs(wa - wb), -lateral
+    cuts = {-h, -k, k, h}
+    if -h < s < h:
+        cuts.add(s)
+    pts = sorted(cuts)
+    tot = 0.0
+    for p, q in zip(pts[:-1], pts[1:]):
+        if q - p <= 0.0:
+            continue
+        toward = p if p == s else q if q == s else None
+        v, wt = _graded(p, q, toward, PANELS if toward is not None else 4, ORDER)
+        W = np.clip(np.minimum(0.5 * wa, v + 0.5 * wb) - np.maximum(-0.5 * wa, v - 0.5 * wb), 0.0, None)
+        tot += float(np.sum(wt * W * filament_mutual(length, np.full(len(v), axial), np.sqrt((lateral + v) ** 2 + dz * dz))))
+    return tot / (wa * wb)
+
+
+def strip_self(length: float, width: float, thickness: float = 0.0) -> float:
+    return float(filament_mutual(length, np.array(0.0), np.array(GMD_FLAT * (width + thickness))))
+
+
+def strip_kernel(n_axial: int, n_lateral: int, d: float, dz: float) -> np.ndarray:
+    """(2 n_axial - 1, 2 n_lateral - 1) mutual inductances of square strips at every grid offset."""
+    ia = np.arange(-(n_axial - 1), n_axial) * d
+    il = np.arange(-(n_lateral - 1), n_lateral) * d
+    K = filament_mutual(d, ia[:, None], np.sqrt(il[None, :] ** 2 + dz * dz))
+    ca, cl = n_axial - 1, n_lateral - 1
+    for oa in range(min(NEAR, n_axial - 1) + 1):
+        for ol in range(min(NEAR, n_lateral - 1) + 1):
+            m = tape_mutual(d, d, d, oa * d, ol * d, dz)
+            for pa in {ca + oa, ca - oa}:
+                for pl in {cl + ol, cl - ol}:
+                    K[pa, pl] = m
+    return K
+
+
+def spectrum_quadrant(K: np.ndarray, P0: int, P1: int) -> np.ndarray:
+    """Real (P0//2+1, P1//2+1) quadrant of the DFT of the centred even kernel wrapped onto a P0 x P1 torus."""
+    Z = np.zeros((P0, P1))
+    c0, c1 = K.shape[0] // 2, K.shape[1] // 2
+    Z[: K.shape[0], : K.shape[1]] = K
+    Z = np.roll(Z, (-c0, -c1), axis=(0, 1))
+    return np.ascontiguousarray(np.fft.fft2(Z).real[: P0 // 2 + 1, : P1 // 2 + 1])
+
+
+def slab_impedance(t, f, sigma):
+    """Internal impedance per square of a one-face slab (kernel.py:47-75)."""
+    t = np.asarray(t, float)
+    f = np.asarray(f, float)
+    with np.errstate(divide="ignore", over="ignore", invalid="ignore"):
+        delta = 1.0 / np.sqrt(np.pi * np.maximum(f, 1e-300) * MU0 * sigma)
+        x = np.where(f > 0, t / delta, 0.0)
+        u = (1 + 1j) * np.minimum(x, 30.0)
+        exact = (1 + 1j) * x / np.tanh(np.where(x > 0, u, 1.0))
+        series = 1.0 + 4.0 * x ** 4 / 45.0 + 1j * (2.0 * x ** 2 / 3.0)
+        out = np.where(x < 0.1, series, exact) / (sigma * t)
+    return complex(out) if out.ndim == 0 else out
+
+
+def skin_thickness(t, f, sigma):
+    t = np.asarray(t, float)
+    f = np.asarray(f, float)
+    with np.errstate(divide="ignore", over="ignore", invalid="ignore"):
+        delta = 1.0 / np.sqrt(np.pi * np.maximum(f, 1e-300) * MU0 * sigma)
+        x = np.where(f > 0, t / delta, 0.0)
+        y = np.minimum(2 * x, 60.0)
+        exact = x * (np.sinh(y) + np.sin(y)) / (np.cosh(y) - np.cos(y))
+        out = t / np.where(x < 0.1, 1.0 + 4.0 * x ** 4 / 45.0, exact)
+    return float(out) if out.ndim == 0 else out
+
+
+def vector_potential(a, b, pts, rho_min: float) -> np.ndarray:
+    ab = b - a
+    L = float(np.linalg.norm(ab))
+    if L == 0:
+        return np.zeros(len(pts))
+    u = ab / L
+    p = pts - a
+    pu = p @ u
+    rho = np.sqrt(np.maximum(np.einsum("ij,ij->i", p, p) - pu * pu, rho_min * rho_min))
+    return MU0 / (4 * np.pi) * (np.arcsinh((L - pu) / rho) + np.arcsinh(pu / rho))
+
+
+def segment_mutual(a1, b1, a2, b2, rho_min: float, n: int = 16) -> float:
+    d2 = b2 - a2
+    L2 = float(np.linalg.norm(d2))
+    L1 = float(np.linalg.norm(b1 - a1))
+    if L2 == 0 or L1 == 0:
+        return 0.0
+    x, w = gauss(n)
+    pts = a2 + (0.5 * (x + 1))[:, None] * d2
+    return float(np.dot((b1 - a1) / L1, d2 / L2) * 0.5 * L2 * np.sum(w * vector_potential(a1, b1, pts, rho_min)))
+
+
+def _dist_to_segment(P, a, b):
+    ab = b - a
+    L2 = float(ab @ ab)
+    if L2 == 0:
+        return np.linalg.norm(P - a, axis=1)
+    t = np.clip((P - a) @ ab / L2, 0, 1)
+    return np.linalg.norm(P - (a + t[:, None] * ab), axis=1)
+
+
+def strip_coupling(segments: np.ndarray, strips: list, d: float, zs: np.ndarray, ts: np.ndarray) -> list:
+    """psi (flux per ampere of signal) along each strip of each orientation.
+
+    segments: rows (ax, ay, az, bx, by, bz, width, i); strips: [(k, i, j) arrays of the x strips,
+    of the y strips].  Returns [psi_x, psi_y]."""
+    x, w = gauss(3)
+    q = 0.5 * x
+    W = np.outer(w, w).ravel() / 4.0
+    qa, ql = (g.ravel() for g in np.meshgrid(q, q, indexing="ij"))
+    horiz = [s for s in segments if np.linalg.norm(s[3:5] - s[0:2]) > 0]
+    out = []
+    for axis, idx in enumerate(strips):
+        if len(idx) == 0:
+            out.append(np.zeros(0))
+            continue
+        k, i, j = idx[:, 0], idx[:, 1], idx[:, 2]
+        cen = np.stack([i * d + (d / 2 if axis == 0 else 0.0), j * d + (d / 2 if axis == 1 else 0.0), zs[k]], 1)
+        acc = np.zeros(len(idx))
+        half = 0.5 * ts[k]
+        for s in horiz:
+            a, b, width, cur = s[0:3], s[3:6], float(s[6]), float(s[7])
+            ab = b - a
+            L = float(np.linalg.norm(ab))
+            if abs(ab[axis]) < 1e-15 * L:
+                continue
+            cen[:, 2] = zs[k] + np.where(0.5 * (a[2] + b[2]) > zs[k], half, -half)
+            rmin = max(0.5 * width, 1e-7)
+            ac = vector_potential(a, b, cen, rmin)
+            near = _dist_to_segment(cen, a, b) < 3 * d + 2 * width
+            if near.any():
+                c = cen[near]
+                da, dl = (qa, ql) if axis == 0 else (ql, qa)
+                pts = np.stack([c[:, 0, None] + da * d, c[:, 1, None] + dl * d,
+                                np.broadcast_to(c[:, 2, None], (len(c), len(W)))], 2)
+                ac[near] = (vector_potential(a, b, pts.reshape(-1, 3), rmin).reshape(len(c), len(W)) * W).sum(1)
+            acc += (cur * ab[axis] / L) * ac
+        out.append(d * acc)
+    return out
+
+
+def trace_self(segments: np.ndarray, trace_t: float) -> float:
+    segs = [s for s in segments if np.linalg.norm(s[3:6] - s[0:3]) > 0]
+    L = 0.0
+    for n, si in enumerate(segs):
+        L += si[7] ** 2 * strip_self(float(np.linalg.norm(si[3:6] - si[0:3])), float(si[6]), trace_t)
+        for sj in segs[n + 1:]:
+            L += 2 * si[7] * sj[7] * segment_mutual(si[0:3], si[3:6], sj[0:3], sj[3:6], GMD_FLAT * (si[6] + trace_t))
+    return float(L)
+
+
+def trace_resistance(segments: np.ndarray, f: float, sigma: float, trace_t: float) -> float:
+    R = 0.0
+    for s in segments:
+        L = float(np.linalg.norm(s[3:6] - s[0:3]))
+        if L == 0 or abs(s[5] - s[2]) > 0:
+            continue
+        R += s[7] ** 2 * L / (sigma * s[6] * skin_thickness(trace_t, f, sigma))
+    return R
+
+
+def sheet_blocks(L_self: float, centre: np.ndarray, sums: np.ndarray) -> np.ndarray:
+    """Per-position layer block with each pair's cavity inductance (peec.py:3344-3359)."""
+    N = len(sums)
+    D = np.maximum(2.0 * (sums[0, 0] - sums), 0.0)
+    np.fill_diagonal(D, 0.0)
+    beta = max((L_self + centre[k, l]) / 2 + D[k, l] / 4 for k in range(N) for l in range(N) if k != l)
+    B = beta - D / 2
+    for _ in range(60):
+        if np.linalg.eigvalsh(B).min() > 0.05 * L_self:
+            break
+        B += 0.25 * L_self
+    return B
+
+
+def fft_size(m: int) -> int:
+    """The padded FFT length this build uses for a linear convolution needing >= m points: the smallest
+    2^a or 3 * 2^a (a >= 3) at least m (radix-2/4/8 stages plus at most one radix-3 stage)."""
+    best = None
+    for base in (1, 3):
+        p = 8 * base
+        while p < m:
+            p *= 2
+        best = p if best is None else min(best, p)
+    return best

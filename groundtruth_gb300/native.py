@@ -1,0 +1,233 @@
+"""ctypes binding of the CUDA library's C ABI (include/gt_gb300.h).
+
+``load()`` opens groundtruth_gb300/libgtgb300.so (built in-tree by groundtruth_gb300.build) and fails loudly
+when it is missing or no CUDA device is visible: the solver has no CPU path.  ``Geometry`` uploads a
+PlaneStack, ``Operators`` factorises frequencies, ``solve`` / ``apply`` run batches."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "libgtgb300.so"
+GT_OK, GT_NOT_CONVERGED, GT_OUT_OF_MEMORY, GT_TIMEOUT, GT_INVALID_ARGUMENT, GT_DEVICE_ERROR = range(6)
+
+_LIB = None
+
+P = C.c_void_p
+I64P = C.POINTER(C.c_int64)
+I32P = C.POINTER(C.c_int32)
+U8P = C.POINTER(C.c_uint8)
+DP = C.POINTER(C.c_double)
+
+
+class GeometryDesc(C.Structure):
+    _fields_ = [("n_sheets", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32), ("n_pairs", C.c_int32),
+                ("n_branches", C.c_int32), ("precond_sheet", C.c_int32),
+                ("n_dense", C.c_int64), ("off_x", C.c_int64), ("off_y", C.c_int64), ("off_c", C.c_int64),
+                ("off_b", C.c_int64), ("off_v", C.c_int64),
+                ("mask", U8P), ("code_x", U8P), ("code_y", U8P), ("pair_layers", I32P), ("branch_nodes", I32P),
+                ("n_compact", C.c_int64), ("compact_to_dense", I64P),
+                ("fft_p", C.c_int32 * 4), ("spectrum_x", DP), ("spectrum_y", DP),
+                ("n_factor", C.c_int64), ("perm", I64P), ("n_fronts", C.c_int32), ("n_levels", C.c_int32),
+                ("level_ptr", I64P), ("front_order", I64P), ("own_start", I64P), ("nown", I64P), ("nbnd", I64P),
+                ("bnd_ptr", I64P), ("bnd_idx", I64P), ("child_ptr", I64P), ("child_idx", I64P),
+                ("cmap_ptr", I64P), ("cmap_idx", I64P), ("panel_off", I64P), ("upd_off", I64P), ("vec_off", I64P),
+                ("panel_total", C.c_int64), ("upd_total", C.c_int64), ("vec_total", C.c_int64),
+                ("ent_ptr", I64P), ("ent_row", I32P), ("ent_col", I32P), ("ent_s", I64P),
+                ("n_svalues", C.c_int64), ("n_table", C.c_int32), ("sterm_ptr", I64P), ("sterm_tab", I32P),
+                ("sterm_coef", DP)]
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("tol", C.c_double), ("restart", C.c_int32), ("max_its", C.c_int32), ("inner_tol", C.c_double),
+                ("precision", C.c_int32), ("max_outer", C.c_int32)]
+
+
+def load():
+    """The library, opened once.  Raises ImportError when it is not built, RuntimeError without a GPU."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = Path(os.environ.get("GT_GB300_LIB", LIB_PATH))
+    if not path.exists():
+        raise ImportError(f"the groundtruth_gb300 CUDA library is not built ({path}); run "
+                          "python -m groundtruth_gb300.build")
+    lib = C.CDLL(str(path))
+    lib.gt_version.restype = C.c_int
+    lib.gt_last_error.restype = C.c_char_p
+    lib.gt_device_count.restype = C.c_int
+    lib.gt_geometry_create.argtypes = [C.POINTER(GeometryDesc), C.POINTER(P)]
+    lib.gt_geometry_free.argtypes = [P]
+    lib.gt_geometry_free.restype = None
+    lib.gt_operators_create.argtypes = [P, C.c_int32, DP, DP, DP, DP, DP, C.POINTER(P)]
+    lib.gt_operators_free.argtypes = [P]
+    lib.gt_operators_free.restype = None
+    lib.gt_solve.argtypes = [P, P, C.c_int32, I32P, DP, C.POINTER(SolveOpts), DP, I32P, DP, P]
+    lib.gt_solve_device.argtypes = [P, P, C.c_int32, I32P, P, C.POINTER(SolveOpts), P, I32P, DP, P]
+    lib.gt_to_dense.argtypes = [P, C.c_int32, DP, P, P]
+    lib.gt_to_compact.argtypes = [P, C.c_int32, P, DP, P]
+    lib.gt_apply.argtypes = [P, P, C.c_int32, C.c_int32, C.c_int32, I32P, DP, DP, P]
+    lib.gt_profile.argtypes = [P, C.c_char_p, C.c_int32, DP, I32P, C.c_int32]
+    if lib.gt_device_count() < 1:
+        raise RuntimeError("no CUDA device is visible: the groundtruth_gb300 solver runs on the GPU only")
+    _LIB = lib
+    return lib
+
+
+def _ptr(a: np.ndarray, ctype):
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def check(lib, rc: int, what: str):
+    if rc == GT_OK:
+        return
+    msg = lib.gt_last_error().decode(errors="replace")
+    if rc == GT_OUT_OF_MEMORY:
+        raise MemoryError(f"{what}: device out of memory ({msg})")
+    if rc == GT_INVALID_ARGUMENT:
+        raise ValueError(f"{what}: {msg}")
+    raise RuntimeError(f"{what} failed (status {rc}): {msg}")
+
+
+class Geometry:
+    """A PlaneStack on the device (gt_geometry_create)."""
+
+    def __init__(self, st):
+        lib = load()
+        self.lib = lib
+        t, D, sym = st.top, st.dense, st.sym
+        S, nx, ny = t.S, t.nx, t.ny
+        keep_arrays = []
+
+        def arr(x, dtype):
+            a = np.ascontiguousarray(x, dtype=dtype)
+            keep_arrays.append(a)
+            return a
+
+        d = GeometryDesc()
+        d.n_sheets, d.nx, d.ny = S, nx, ny
+        d.n_pairs, d.n_branches = len(t.pair_layers), t.nbr
+        d.precond_sheet = int(st.sheet)
+        d.n_dense = D.n
+        d.off_x, d.off_y, d.off_c, d.off_b, d.off_v = D.off_x, D.off_y, D.off_c, D.off_b, D.off_v
+        d.mask = _ptr(arr(D.mask, np.uint8), C.c_uint8)
+        d.code_x = _ptr(arr(st.code["x"], np.uint8), C.c_uint8)
+        d.code_y = _ptr(arr(st.code["y"], np.uint8), C.c_uint8)
+        d.pair_layers = _ptr(arr(t.pair_layers.reshape(-1), np.int32), C.c_int32)
+        node_dense = np.flatnonzero(t.node.ravel())
+        d.branch_nodes = _ptr(arr(node_dense[t.branch_ab].reshape(-1) if t.nbr else np.zeros(2), np.int32), C.c_int32)
+        d.n_compact = len(D.compact_to_dense)
+        d.compact_to_dense = _ptr(arr(D.compact_to_dense, np.int64), C.c_int64)
+        for k, v in enumerate((*st.P["x"], *st.P["y"])):
+            d.fft_p[k] = v
+        d.spectrum_x = _ptr(arr(st.spectrum["x"], np.float64), C.c_double)
+        d.spectrum_y = _ptr(arr(st.spectrum["y"], np.float64), C.c_double)
+        d.n_factor = sym.n
+        d.perm = _ptr(arr(sym.perm, np.int64), C.c_int64)
+        d.n_fronts = len(sym.nown)
+        d.n_levels = len(sym.level_ptr) - 1
+        for name in ("level_ptr", "own_start", "nown", "nbnd", "bnd_ptr", "bnd_idx", "child_ptr", "child_idx",
+                     "cmap_ptr", "cmap_idx", "panel_off", "upd_off", "vec_off", "ent_ptr", "ent_s"):
+            setattr(d, name, _ptr(arr(getattr(sym, name), np.int64), C.c_int64))
+        d.front_order = _ptr(arr(sym.order, np.int64), C.c_int64)
+        d.ent_row = _ptr(arr(sym.ent_row, np.int32), C.c_int32)
+        d.ent_col = _ptr(arr(sym.ent_col, np.int32), C.c_int32)
+        d.panel_total, d.upd_total, d.vec_total = sym.panel_total, sym.upd_total, sym.vec_total
+        M = st.sterm
+        d.n_svalues = M.shape[0]
+        d.n_table = st.n_table
+        d.sterm_ptr = _ptr(arr(M.indptr, np.int64), C.c_int64)
+        d.sterm_tab = _ptr(arr(M.indices, np.int32), C.c_int32)
+        d.sterm_coef = _ptr(arr(M.data, np.float64), C.c_double)
+        h = P()
+        check(lib, lib.gt_geometry_create(C.byref(d), C.byref(h)), "gt_geometry_create")
+        self.h = h
+        self.n_dense = D.n
+        self.n_compact = len(D.compact_to_dense)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _LIB is not None:
+            _LIB.gt_geometry_free(self.h)
+            self.h = None
+
+    def profile(self, on: bool | None = None) -> dict:
+        """Toggle (on=True/False: reset) or read {kernel family: (ms, launches)} of the last solves."""
+        if on is not None:
+            self.lib.gt_profile(self.h, None, 0, None, None, -2 if on else -1)
+            return {}
+        cap = 64
+        names = C.create_string_buffer(4096)
+        ms = np.zeros(cap)
+        launches = np.zeros(cap, np.int32)
+        k = self.lib.gt_profile(self.h, names, 4096, _ptr(ms, C.c_double), _ptr(launches, C.c_int32), cap)
+        keys = names.value.decode().split(",") if k else []
+        return {n: (float(ms[i]), int(launches[i])) for i, n in enumerate(keys)}
+
+
+class Operators:
+    """Factorised Schur complements at several frequencies (gt_operators_create)."""
+
+    def __init__(self, geom: Geometry, keys: list, data: list):
+        lib = geom.lib
+        self.geom = geom
+        w = np.array([x[0] for x in data], np.float64)
+        zs = np.ascontiguousarray(np.stack([x[1] for x in data]).astype(np.complex128))
+        zc = np.ascontiguousarray(np.stack([x[2] for x in data]).astype(np.complex128)).reshape(len(data), -1)
+        zb = np.ascontiguousarray(np.stack([x[3] for x in data]).astype(np.complex128)).reshape(len(data), -1)
+        tab = np.ascontiguousarray(np.stack([x[4] for x in data]).astype(np.complex128))
+        self._keep = (zs, zc, zb, tab)
+        h = P()
+        check(lib, lib.gt_operators_create(geom.h, len(data), _ptr(w, C.c_double), _ptr(zs.view(np.float64), C.c_double),
+                                           _ptr(zc.view(np.float64), C.c_double), _ptr(zb.view(np.float64), C.c_double),
+                                           _ptr(tab.view(np.float64), C.c_double), C.byref(h)), "gt_operators_create")
+        self.h = h
+        self.keys = list(keys)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _LIB is not None:
+            _LIB.gt_operators_free(self.h)
+            self.h = None
+
+
+def _ops_and_index(ops: list):
+    """[(Operators, index)] of the columns -> one Operators object and the per-column index into it."""
+    objs = {id(o): o for o, _ in ops}
+    if len(objs) != 1:
+        raise ValueError("all columns of one batch must use operators made together (PlaneStack.factorise)")
+    obj = next(iter(objs.values()))
+    return obj, np.array([k for _, k in ops], np.int32)
+
+
+def solve(geom: Geometry, ops: list, rhs: np.ndarray, tol: float, restart: int = 50, max_its: int = 2000,
+          inner_tol: float = 1e-5, precision: str = "mixed", max_outer: int = 40):
+    """rhs: (ncol, n_compact) complex in the reference's order.  Returns (x, its, resid, converged)."""
+    lib = geom.lib
+    obj, idx = _ops_and_index(ops)
+    rhs = np.ascontiguousarray(rhs, np.complex128)
+    ncol = rhs.shape[0]
+    x = np.zeros_like(rhs)
+    its = np.zeros(ncol, np.int32)
+    res = np.zeros(ncol)
+    o = SolveOpts(tol, restart, max_its, inner_tol, 1 if precision == "fp64" else 0, max_outer)
+    rc = lib.gt_solve(geom.h, obj.h, ncol, _ptr(idx, C.c_int32), _ptr(rhs.view(np.float64), C.c_double), C.byref(o),
+                      _ptr(x.view(np.float64), C.c_double), _ptr(its, C.c_int32), _ptr(res, C.c_double), None)
+    if rc not in (GT_OK, GT_NOT_CONVERGED):
+        check(lib, rc, "gt_solve")
+    return x, its, res, res <= tol
+
+
+def apply(geom: Geometry, obj: Operators, kind: str, x: np.ndarray, op_index, precision: str = "fp64") -> np.ndarray:
+    """One operator application on compact vectors: kind "matvec", "precond" or "lp"."""
+    lib = geom.lib
+    x = np.ascontiguousarray(np.atleast_2d(x), np.complex128)
+    ncol = x.shape[0]
+    idx = np.ascontiguousarray(np.broadcast_to(np.asarray(op_index, np.int32), (ncol,)))
+    y = np.zeros_like(x)
+    k = {"matvec": 0, "precond": 1, "lp": 2}[kind]
+    rc = lib.gt_apply(geom.h, obj.h, k, 1 if precision == "fp64" else 0, ncol, _ptr(idx, C.c_int32),
+                      _ptr(x.view(np.float64), C.c_double), _ptr(y.view(np.float64), C.c_double), None)
+    check(lib, rc, "gt_apply")
+    return y

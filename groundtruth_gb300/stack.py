@@ -1,0 +1,515 @@
+"""The solver's Python interface, mirroring GroundTruth's (src/groundtruth/solver/peec.py):
+
+    PlaneStack(layers, branches, capacitance, sigma, precond, screen)        peec.py:1555-1593
+    PlaneStack.solve(f, rhs_top, J, tol, max_cycles, guess) -> (Ib, V, its, x)  peec.py:2513-2607
+    RouteExcitation(stack, trace, inject_driver, inject_receiver, ...)       peec.py:2703-2769
+    RouteExcitation.solve(f, guess) -> Solution                              peec.py:2787-2817
+
+with the same argument meanings, unknown numbering and error behaviour (SolverError for unsolvable models
+and non-convergence, MemoryError when the device cannot hold a model).  A batched entry point,
+``PlaneStack.solve_batch``, solves many (excitation, frequency) columns in one device run.
+
+Everything per iteration runs in the CUDA library (``groundtruth_gb300/csrc``) through its C ABI
+(``include/gt_gb300.h``); there is no CPU fallback: without the library the constructor raises.  The host
+does the once-per-geometry index work (``layout``) and FP64 kernels (``greens``), and the cheap
+per-frequency impedance tables.
+
+Scope: one current sheet per layer (``screen`` face sheets are not modelled: a stack that would split a
+layer raises NotImplementedError) and full-width strips (grids without wx/wy widths).
+"""
+from __future__ import annotations
+
+import math
+import threading
+from collections import OrderedDict
+from dataclasses import dataclass, field
+from typing import Callable, Optional
+
+import numpy as np
+import scipy.sparse as sp
+
+from . import greens, layout
+
+SIGMA_CU = 5.8e7
+SCREEN_MIN_NODES = 16
+OPERATOR_CACHE = 64           # factorised frequencies kept on the device per stack
+
+
+class SolverError(RuntimeError):
+    """A model that cannot be solved (peec.py:124-127)."""
+
+
+@dataclass
+class Grid:
+    """One layer's copper on the shared grid (peec.py:197-223; the fields this solver reads)."""
+    x0: float
+    y0: float
+    d: float                 # mm
+    nx: int
+    ny: int
+    node: np.ndarray
+    xb: np.ndarray
+    yb: np.ndarray
+    wx: Optional[np.ndarray] = None
+    wy: Optional[np.ndarray] = None
+
+
+@dataclass
+class PlaneLayer:
+    name: str
+    z: float
+    grid: Grid
+    thickness: float = 35e-6
+
+
+@dataclass
+class Branch:
+    a: tuple
+    b: tuple
+    z: Callable[[float], complex]
+    name: str = ""
+    kind: str = "part"
+    radius: float = 1.5e-4
+
+
+@dataclass
+class PlanePair:
+    upper: int
+    lower: int
+    c_per_area: float
+    tan_delta: float = 0.02
+
+
+@dataclass
+class TraceSegment:
+    a: np.ndarray
+    b: np.ndarray
+    width: float
+    i: float = 1.0
+
+
+@dataclass
+class Solution:
+    """One solve at one frequency per A of loop current (peec.py:1092-1115)."""
+    f: float
+    I_x: np.ndarray
+    I_y: np.ndarray
+    V: np.ndarray
+    I_branch: np.ndarray
+    Z_loop: complex
+    m: np.ndarray
+    iterations: int
+    I_cap: np.ndarray = field(default_factory=lambda: np.zeros(0, complex))
+    residual: float = 0.0          # final relative FP64 residual ||b - K x|| / ||b||
+
+    @property
+    def L_loop(self) -> float:
+        return self.Z_loop.imag / (2 * math.pi * self.f)
+
+
+def freq_key(f: float) -> float:
+    """f to 12 significant digits (peec.py:2292-2296, 3264-3267)."""
+    return float(f"{float(f):.12g}")
+
+
+class PlaneStack:
+    """Plane layers with their branches and plane-pair capacitance on one GPU."""
+
+    def __init__(self, layers: list, branches: Optional[list] = None, capacitance: Optional[list] = None,
+                 sigma: float = SIGMA_CU, precond: str = "diag", screen: bool = True, *, leaf: int = 48,
+                 _device: bool = True):
+        from . import native
+        if not layers:
+            raise SolverError("no plane layers")
+        if precond not in ("diag", "sheet"):
+            raise ValueError("precond must be 'diag' or 'sheet'")
+        g0 = layers[0].grid
+        for l in layers:
+            if (l.grid.nx, l.grid.ny, l.grid.d) != (g0.nx, g0.ny, g0.d):
+                raise SolverError("all layers must share one grid")
+            if l.grid.wx is not None or l.grid.wy is not None:
+                raise NotImplementedError("strips narrower than the pitch (Grid.wx/wy) are not modelled")
+        self.lib = native.load() if _device else None
+        self.layers = list(layers)
+        self.N = self.n_sheets = len(layers)
+        self.nx, self.ny = g0.nx, g0.ny
+        self.d = g0.d * 1e-3
+        self.zs = np.array([l.z for l in layers], float)
+        self.ts = np.array([l.thickness for l in layers], float)
+        self.sigma = sigma
+        self.precond_mode = precond
+        self.pairs = list(capacitance or [])
+        self._check_screen(screen)
+        self.branches_all = list(branches or [])
+        t, kept = layout.topology([l.grid.node for l in layers], [l.grid.xb for l in layers],
+                                  [l.grid.yb for l in layers], self.d,
+                                  [(p.upper, p.lower, p.c_per_area, p.tan_delta) for p in self.pairs],
+                                  [(b.a, b.b) for b in self.branches_all])
+        self.top = t
+        self.branches = [self.branches_all[k] for k in kept]
+        self.node, self.nid, self.xa, self.ya, self.keep = t.node, t.nid, t.xa, t.ya, t.keep
+        self.nxb, self.nyb, self.ns, self.ncap, self.nbr, self.nb = t.nxb, len(t.ya), t.ns, t.ncap, t.nbr, t.nb
+        self.n_nodes = self.n_grid = t.n_nodes
+        self.full_label, self.cond_label = t.full_label, t.cond_label
+        self.dense = layout.dense_layout(t)
+        self._kernels()
+        self._schur_structure(leaf)
+        self._lock = threading.Lock()
+        self._ops: OrderedDict = OrderedDict()
+        self.handle = native.Geometry(self) if _device else None
+
+    # ------------------------------------------------------------------ construction
+    def _check_screen(self, screen: bool):
+        if not screen or self.N < 3:
+            return
+        node = np.stack([l.grid.node for l in self.layers])
+        for k in range(self.N):
+            above = np.zeros(node.shape[1:], bool)
+            below = np.zeros(node.shape[1:], bool)
+            for m in range(self.N):
+                if self.zs[m] > self.zs[k]:
+                    above |= node[m]
+                elif self.zs[m] < self.zs[k]:
+                    below |= node[m]
+            if int(np.count_nonzero(node[k] & above & below)) >= SCREEN_MIN_NODES:
+                raise NotImplementedError("a layer with copper above and below (screen=True) needs face sheets, "
+                                          "which this build does not model; pass screen=False")
+
+    def face_gap(self, s: int, t: int) -> float:
+        if s == t:
+            return 0.0
+        return max(abs(self.zs[s] - self.zs[t]) - 0.5 * (self.ts[s] + self.ts[t]), 1e-6)
+
+    def _kernels(self):
+        """Strip kernels per sheet pair and their spectra at this build's FFT sizes (peec.py:1941-1988)."""
+        nx, ny, S = self.nx, self.ny, self.N
+        d = greens.round12(self.d)
+        self.P = {"x": (greens.fft_size(2 * (nx - 1) - 1), greens.fft_size(2 * ny - 1)),
+                  "y": (greens.fft_size(2 * nx - 1), greens.fft_size(2 * (ny - 1) - 1))}
+        spec = {o: np.zeros((self.P[o][1] // 2 + 1, self.P[o][0] // 2 + 1, S, S)) for o in "xy"}
+        centre, sx, sy = np.zeros((S, S)), np.zeros((S, S)), np.zeros((S, S))
+        cache: dict = {}
+        for s in range(S):
+            for t in range(s, S):
+                dz = greens.round12(self.face_gap(s, t))
+                if dz not in cache:
+                    kx = greens.strip_kernel(nx - 1, ny, d, dz)
+                    ky = greens.strip_kernel(ny - 1, nx, d, dz).T
+                    cache[dz] = (greens.spectrum_quadrant(kx, *self.P["x"]).T, greens.spectrum_quadrant(ky, *self.P["y"]).T,
+                                 float(kx[nx - 2, ny - 1]), float(kx.sum()), float(ky.sum()))
+                qx, qy, c, a, b = cache[dz]
+                spec["x"][:, :, s, t] = spec["x"][:, :, t, s] = qx
+                spec["y"][:, :, s, t] = spec["y"][:, :, t, s] = qy
+                centre[s, t] = centre[t, s] = c
+                sx[s, t] = sx[t, s] = a
+                sy[s, t] = sy[t, s] = b
+        dz0 = greens.round12(0.0)
+        self.L_self = cache[dz0][2] if dz0 in cache else float(greens.strip_kernel(nx - 1, ny, d, 0.0)[nx - 2, ny - 1])
+        # layout (Q1, Q0, S, S): the column pass reads one pixel column's quadrant rows contiguously; scaled by
+        # the inverse transform's 1 / (P0 P1)
+        self.spectrum = {o: np.ascontiguousarray(spec[o] / (self.P[o][0] * self.P[o][1])) for o in "xy"}
+        self.centre, self.sum_x, self.sum_y = centre, sx, sy
+        self.B = None
+        if self.precond_mode == "sheet" and S > 1:
+            self.B = {"x": greens.sheet_blocks(self.L_self, centre, sx), "y": greens.sheet_blocks(self.L_self, centre, sy)}
+
+    def _schur_structure(self, leaf: int):
+        """S = Ar^T D^-1 Ar as a linear map of the per-frequency admittance table, and its symbolic analysis."""
+        t, S, nx, ny = self.top, self.N, self.nx, self.ny
+        nxy = nx * ny
+        self.sheet = self.B is not None
+        ncode = 1 << S
+        self.code = {"x": np.zeros((nx - 1, ny), np.uint8), "y": np.zeros((nx, ny - 1), np.uint8)}
+        for k in range(S):
+            self.code["x"] |= (t.xb[k].astype(np.uint8) << k)
+            self.code["y"] |= (t.yb[k].astype(np.uint8) << k)
+        self.tab_cap0 = 2 * ncode * S * S
+        self.tab_br0 = self.tab_cap0 + len(t.pair_layers)
+        self.n_table = self.tab_br0 + self.nbr
+        kept_of_nid = -np.ones(t.n_nodes, np.int64)
+        kept_of_nid[t.keep] = np.arange(t.n_keep)
+        U, Vv, T, C = [], [], [], []
+
+        def add(s1_nodes, s2_nodes, tab):
+            """D^-1 entry tab between strips with ends s1 (a, b) and s2 (a, b): all (u, v) terms."""
+            for (u, su) in ((s1_nodes[0], 1.0), (s1_nodes[1], -1.0)):
+                for (v, sv) in ((s2_nodes[0], 1.0), (s2_nodes[1], -1.0)):
+                    ku, kv = kept_of_nid[u], kept_of_nid[v]
+                    ok = (ku >= 0) & (kv >= 0)
+                    U.append(ku[ok]); Vv.append(kv[ok]); T.append(tab[ok]); C.append(np.full(int(ok.sum()), su * sv))
+
+        for o, idx, di, dj in ((0, t.xa, 1, 0), (1, t.ya, 0, 1)):
+            if len(idx) == 0:
+                continue
+            k, i, j = idx[:, 0], idx[:, 1], idx[:, 2]
+            code = self.code["x" if o == 0 else "y"][i, j].astype(np.int64)
+            ends1 = (t.nid[k, i, j], t.nid[k, i + di, j + dj])
+            partners = range(S) if self.sheet else [None]
+            for l in partners:
+                if l is None:                      # diagonal D: each strip with itself
+                    ll = k
+                    sel = np.ones(len(k), bool)
+                else:                              # blocks: every strip present at the same position
+                    ll = np.full(len(k), l)
+                    sel = (code >> l) & 1 == 1
+                tab = ((o * ncode + code) * S + k) * S + ll
+                e1 = (ends1[0][sel], ends1[1][sel])
+                e2 = (t.nid[ll[sel], i[sel], j[sel]], t.nid[ll[sel], i[sel] + di, j[sel] + dj])
+                add(e1, e2, tab[sel])
+        cu = t.cap[:, :4].astype(np.int64)
+        if len(cu):
+            pidx = np.concatenate([np.full(int(t.cap_mask[p].sum()), p) for p in range(len(t.pair_layers))])
+            e = (t.nid[cu[:, 0], cu[:, 2], cu[:, 3]], t.nid[cu[:, 1], cu[:, 2], cu[:, 3]])
+            add(e, e, self.tab_cap0 + pidx)
+        if self.nbr:
+            e = (t.branch_ab[:, 0], t.branch_ab[:, 1])
+            add(e, e, self.tab_br0 + np.arange(self.nbr))
+        U, Vv, T, C = (np.concatenate(a) for a in (U, Vv, T, C))
+        n = t.n_keep
+        pattern = sp.coo_matrix((np.ones(len(U)), (U, Vv)), shape=(n, n)).tocsr()
+        pattern = ((pattern + pattern.T) != 0).astype(np.float64)
+        self.sym = layout.symbolic(t, pattern, leaf)
+        sym = self.sym
+        # kept index -> factor index
+        node_dense = np.flatnonzero(t.node.ravel())
+        fac = sym.perm[node_dense[t.keep]]
+        fu, fv = fac[U], fac[Vv]
+        low = fu >= fv
+        fu, fv, T, C = fu[low], fv[low], T[low], C[low]
+        # S entry index of (row, col) in the symbolic's column-major lower list
+        key_s = sym.s_col * n + sym.s_row
+        e = np.searchsorted(key_s, fv * n + fu)
+        assert np.all(key_s[e] == fv * n + fu)
+        M = sp.coo_matrix((C, (e, T)), shape=(len(key_s), self.n_table)).tocsr()
+        M.sum_duplicates()
+        M.eliminate_zeros()
+        self.sterm = M
+
+    # ------------------------------------------------------------------ per-frequency data
+    def _freq_tables(self, f: float):
+        """(omega, sheet impedances (S,), cap impedances (npairs,), branch impedances (nbr,), admittance
+        table (n_table,)) at f: peec.py:2150-2178 and 2465-2511 restated over the table."""
+        w = 2 * math.pi * f
+        S = self.N
+        zs = np.array([complex(greens.slab_impedance(l.thickness, f, self.sigma)) for l in self.layers])
+        pl = self.top.pair_layers
+        C = np.array([p.c_per_area for p in self.pairs]) * self.d ** 2
+        tand = np.array([p.tan_delta for p in self.pairs])
+        zcap = 1.0 / (w * C * tand + 1j * w * C) if w > 0 else np.full(len(pl), 1e18 + 0j)
+        zbr = np.array([complex(b.z(f)) for b in self.branches], complex)
+        ncode = 1 << S
+        tab = np.zeros(self.n_table, complex)
+        dself = 1.0 / (zs + 1j * w * self.L_self)
+        for o, name in enumerate("xy"):
+            for code in range(1, ncode):
+                lay = [k for k in range(S) if code >> k & 1]
+                blk = np.zeros((S, S), complex)
+                if self.sheet and len(lay) >= 2:
+                    Bo = self.B[name][np.ix_(lay, lay)]
+                    Zi = np.linalg.inv(np.diag(zs[lay]) + 1j * w * Bo)
+                    blk[np.ix_(lay, lay)] = Zi
+                else:
+                    for k in lay:
+                        blk[k, k] = dself[k]
+                tab[(o * ncode + code) * S * S: (o * ncode + code + 1) * S * S] = blk.ravel()
+        tab[self.tab_cap0: self.tab_br0] = 1.0 / zcap if len(pl) else []
+        tab[self.tab_br0:] = 1.0 / zbr if self.nbr else []
+        return w, zs, zcap, zbr, tab
+
+    def operator(self, f: float):
+        """The device operator (factorised Schur complement) at f's key, made once and cached."""
+        key = freq_key(f)
+        with self._lock:
+            op = self._ops.get(key)
+            if op is not None:
+                self._ops.move_to_end(key)
+                return op
+        op = self.factorise([key])[0]
+        return op
+
+    def factorise(self, freqs, together: bool = False) -> list:
+        """Factorise the Schur complement at each frequency key on the device (one batched launch per
+        elimination level); returns the cached operators [(Operators, index)].  together: all of them in one
+        Operators object (what a batched solve needs), refactorising cached ones that live elsewhere."""
+        from . import native
+        keys = [freq_key(f) for f in freqs]
+        todo = [k for k in dict.fromkeys(keys) if k not in self._ops]
+        if together and not todo and len({id(self._ops[k][0]) for k in keys}) > 1:
+            todo = list(dict.fromkeys(keys))
+        elif together and todo and len(todo) < len(set(keys)):
+            todo = list(dict.fromkeys(keys))
+        if todo:
+            data = [self._freq_tables(k) for k in todo]
+            ops = native.Operators(self.handle, todo, data)
+            with self._lock:
+                for n, k in enumerate(todo):
+                    self._ops[k] = (ops, n)
+                while len(self._ops) > max(OPERATOR_CACHE, len(keys)):
+                    self._ops.popitem(last=False)
+        return [self._ops[k] for k in keys]
+
+    # ------------------------------------------------------------------ solves
+    def solve(self, f: float, rhs_top: np.ndarray, J: np.ndarray, tol: float = 1e-5, max_cycles: int = 8,
+              guess: Optional[list] = None):
+        """Solve K [I; V] = [rhs_top; J] (peec.py:2513-2607).  Returns (Ib (nb), V (n_nodes), its, x)."""
+        out = self.solve_batch([f], [np.asarray(rhs_top, complex)], [np.asarray(J, float)], tol=tol,
+                               max_cycles=max_cycles, guesses=[guess])
+        return out[0]
+
+    def rhs_vector(self, rhs_top: np.ndarray, J: np.ndarray) -> np.ndarray:
+        return np.concatenate([np.asarray(rhs_top, complex), np.asarray(J, float)[self.keep].astype(complex)])
+
+    def solve_batch(self, freqs, rhs_tops, Js, tol: float = 1e-5, max_cycles: int = 8, guesses=None,
+                    restart: int = 50, max_its: int = 2000, inner_tol: float = 1e-5, precision: str = "mixed"):
+        """Many columns (frequency, right-hand side) in one device run: returns [(Ib, V, its, x)]."""
+        from . import native
+        ncol = len(freqs)
+        ops = self.factorise(freqs, together=True)
+        rhs = np.stack([self.rhs_vector(r, j) for r, j in zip(rhs_tops, Js)])
+        x0 = None
+        if guesses is not None and any(g for g in guesses if g):
+            raise NotImplementedError("warm-start guesses are not supported yet")
+        x, its, res, ok = native.solve(self.handle, ops, rhs, tol=tol, restart=restart, max_its=max_its,
+                                       inner_tol=inner_tol, precision=precision)
+        out = []
+        for c in range(ncol):
+            if not ok[c]:
+                raise SolverError(f"GMRES did not converge at {freqs[c]:.4g} Hz ({its[c]} iterations, "
+                                  f"residual {res[c]:.3g})")
+            V = np.zeros(self.n_nodes, complex)
+            V[self.keep] = x[c, self.nb:]
+            out.append((x[c, : self.nb], V, int(its[c]), x[c], float(res[c])))
+        return out
+
+    # ------------------------------------------------------------------ coupling to a signal path
+    def strip_coupling(self, segments: np.ndarray) -> np.ndarray:
+        px, py = greens.strip_coupling(segments, [self.xa, self.ya], self.d, self.zs, self.ts)
+        return np.concatenate([px, py])
+
+    def branch_coupling(self, segments: np.ndarray) -> np.ndarray:
+        vert = [s for s in segments if abs(s[5] - s[2]) > 0 and np.linalg.norm(s[3:5] - s[0:2]) < 1e-12]
+        out = np.zeros(self.nbr)
+        for n, b in enumerate(self.branches):
+            if b.kind == "via" and vert:
+                pa, pb = self.pos(b.a), self.pos(b.b)
+                out[n] = sum(s[7] * greens.segment_mutual(s[0:3], s[3:6], pa, pb, b.radius) for s in vert)
+        return out
+
+    def pos(self, node) -> np.ndarray:
+        k, i, j = node
+        return np.array([i * self.d, j * self.d, self.zs[k]])
+
+    def moment(self, segments: np.ndarray, Ib: np.ndarray) -> np.ndarray:
+        """m = 1/2 sum r x I dl over the closed loop (peec.py:2668-2700)."""
+        m = np.zeros(3, complex)
+        for s in segments:
+            m += 0.5 * s[7] * np.cross(s[0:3], s[3:6])
+        d = self.d
+        Ix, Iy = Ib[: self.nxb], Ib[self.nxb: self.ns]
+        k, _, j = self.xa.T
+        m[1] += 0.5 * np.sum(self.zs[k] * d * Ix)
+        m[2] += 0.5 * np.sum(-(j * d) * d * Ix)
+        k, i, _ = self.ya.T
+        m[0] += 0.5 * np.sum(-self.zs[k] * d * Iy)
+        m[2] += 0.5 * np.sum((i * d) * d * Iy)
+        I_cap = Ib[self.ns: self.ns + self.ncap]
+        if len(I_cap):
+            cu = self.top.cap[:, :4].astype(int)
+            x, y = cu[:, 2] * d, cu[:, 3] * d
+            dz = self.zs[cu[:, 1]] - self.zs[cu[:, 0]]
+            m[0] += 0.5 * np.sum(y * dz * I_cap)
+            m[1] += 0.5 * np.sum(-x * dz * I_cap)
+        for b, cur in zip(self.branches, Ib[self.ns + self.ncap:]):
+            m += 0.5 * np.cross(self.pos(b.a), self.pos(b.b)) * cur
+        return m
+
+
+class RouteExcitation:
+    """A current loop on a PlaneStack: the known trace current plus the driver/receiver injections
+    (peec.py:2703-2817)."""
+
+    def __init__(self, stack: PlaneStack, trace: list, inject_driver=None, inject_receiver=None,
+                 trace_thickness: float = 35e-6, injections: Optional[list] = None):
+        self.stack = stack
+        self.trace = trace
+        self.trace_t = trace_thickness
+        self.segments = np.array([[*s.a, *s.b, s.width, s.i] for s in trace], float).reshape(-1, 8)
+        terms = []
+        if inject_driver is not None:
+            terms.append((inject_driver, -1.0, "driver return node"))
+        if inject_receiver is not None:
+            terms.append((inject_receiver, 1.0, "receiver return node"))
+        terms += [(node, float(a), f"current injection at {node}") for node, a in (injections or [])]
+        if not terms:
+            raise SolverError("no current is injected")
+        ids = []
+        for node, amps, what in terms:
+            n = int(stack.nid[tuple(node)])
+            if n < 0:
+                raise SolverError(f"{what} is not on plane copper")
+            ids.append((n, amps))
+        bal: dict = {}
+        for n, amps in ids:
+            c = int(stack.full_label[n])
+            bal[c] = bal.get(c, 0.0) + amps
+        if any(abs(v) > 1e-9 for v in bal.values()):
+            if inject_driver is not None and inject_receiver is not None and not injections:
+                raise SolverError("receiver return node is not connected to the driver's return node")
+            raise SolverError("the injected currents do not balance on every connected piece of copper")
+        self.injections = ids
+        self.strip_psi = stack.strip_coupling(self.segments)
+        self.branch_psi = stack.branch_coupling(self.segments)
+        self.psi = np.concatenate([self.strip_psi, np.zeros(stack.ncap), self.branch_psi])
+        self.L_trace = greens.trace_self(self.segments, trace_thickness) if len(trace) else 0.0
+
+    def J(self) -> np.ndarray:
+        J = np.zeros(self.stack.n_nodes)
+        for n, amps in self.injections:
+            J[n] += amps
+        return J
+
+    def rhs_top(self, f: float) -> np.ndarray:
+        return -1j * 2 * math.pi * f * self.psi
+
+    def solution(self, f: float, Ib: np.ndarray, V: np.ndarray, its: int, res: float = 0.0) -> Solution:
+        st = self.stack
+        w = 2 * math.pi * f
+        I_x = np.zeros((st.N, st.nx - 1, st.ny), complex)
+        I_y = np.zeros((st.N, st.nx, st.ny - 1), complex)
+        I_x[tuple(st.xa.T)] = Ib[: st.nxb]
+        I_y[tuple(st.ya.T)] = Ib[st.nxb: st.ns]
+        Vg = np.zeros((st.N, st.nx, st.ny), complex)
+        Vg[np.nonzero(st.node)] = V[: st.n_grid]
+        v_inj = sum(a * V[n] for n, a in self.injections)
+        Z = complex(greens.trace_resistance(self.segments, f, st.sigma, self.trace_t) + v_inj
+                    + 1j * w * (self.L_trace + np.dot(self.psi, Ib)))
+        return Solution(f, I_x, I_y, Vg, Ib[st.ns + st.ncap:].copy(), Z, st.moment(self.segments, Ib), its,
+                        Ib[st.ns: st.ns + st.ncap].copy(), res)
+
+    def solve(self, f: float, guess=None, tol: float = 1e-5) -> Solution:
+        Ib, V, its, x = self.stack.solve(f, self.rhs_top(f), self.J(), tol=tol, guess=guess)[:4]
+        return self.solution(f, Ib, V, its)
+
+
+def solve_many(excitations: list, freqs, tol: float = 1e-5, **kw) -> list:
+    """Every (excitation, frequency) pair on one stack in one device batch: [[Solution per f] per excitation]."""
+    st = excitations[0].stack
+    cols = [(e, f) for e in excitations for f in freqs]
+    out = st.solve_batch([f for _, f in cols], [e.rhs_top(f) for e, f in cols], [e.J() for e, _ in cols], tol=tol, **kw)
+    sols = [e.solution(f, Ib, V, its, res) for (e, f), (Ib, V, its, x, res) in zip(cols, out)]
+    n = len(freqs)
+    return [sols[k * n:(k + 1) * n] for k in range(len(excitations))]
+
+
+def from_board(board, _device: bool = True):
+    """A PlaneStack and its RouteExcitations for a ``synth.Board`` (the workloads' boards)."""
+    grids = [Grid(0.0, 0.0, board.d * 1e3, board.nx, board.ny, l.node, l.xb, l.yb) for l in board.layers]
+    layers = [PlaneLayer(l.name, l.z, g, l.thickness) for l, g in zip(board.layers, grids)]
+    branches = [Branch(b.a, b.b, b.z, f"br{n}", b.kind, b.radius) for n, b in enumerate(board.branches)]
+    pairs = [PlanePair(p.upper, p.lower, p.c_per_area, p.tan_delta) for p in board.pairs]
+    st = PlaneStack(layers, branches, pairs, board.sigma, precond=board.precond, screen=False, _device=_device)
+    routes = []
+    for net in board.nets:
+        trace = [TraceSegment(s[0:3].copy(), s[3:6].copy(), float(s[6]), float(s[7])) for s in net.segments]
+        routes.append(RouteExcitation(st, trace, net.driver, net.receiver, net.trace_t))
+    return st, routes

@@ -1,0 +1,136 @@
+/*
+ * gt_gb300.h - C ABI of the GB300 (sm_103a) PEEC plane-current solver.
+ *
+ * The library replaces the per-net, per-frequency solve of GroundTruth's quasi-static PEEC solver:
+ *   PlaneStack.__init__ / _topology / _kernels   src/groundtruth/solver/peec.py:1559-1593, 1596-1656, 1941-1988
+ *   PlaneStack.operator / _factorise             src/groundtruth/solver/peec.py:2227-2290, 2345-2445
+ *   PlaneStack.solve / _solve / _gmres           src/groundtruth/solver/peec.py:2513-2607, 3093-3224
+ *   _HostMath.matvec / precond                   src/groundtruth/solver/peec.py:3043-3083
+ *   gpu.TorchMath (the reference's device seam)  src/groundtruth/solver/gpu.py:471-573
+ *
+ * The reference is pure Python and has no FFI of its own; these entry points are what its backend seam
+ * (_solve_here choosing a math object, peec.py:2544-2558) would bind through ctypes: geometry handles built
+ * once per PlaneStack, operator handles once per factorised frequency, and batched solves.  All arguments
+ * are plain pointers and sizes.  Complex arrays are interleaved (re, im) doubles.  Host pointers unless a
+ * name says _device.  Every entry returns a gt_status; gt_last_error() describes the last failure of the
+ * calling thread.  No entry point falls back to the CPU.
+ */
+#ifndef GT_GB300_H
+#define GT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gt_status {
+    GT_OK = 0,
+    GT_NOT_CONVERGED = 1,     /* peec.SolverError "GMRES did not converge" (peec.py:2599-2600) */
+    GT_OUT_OF_MEMORY = 2,     /* MemoryError: the relief ladder's signal (peec.py:2425-2430) */
+    GT_TIMEOUT = 3,           /* a bounded device wait ran out */
+    GT_INVALID_ARGUMENT = 4,  /* malformed sizes or indices (ValueError / SolverError at the caller) */
+    GT_DEVICE_ERROR = 5       /* any other CUDA failure */
+} gt_status;
+
+typedef struct gt_geometry gt_geometry;
+typedef struct gt_operators gt_operators;
+
+/* Everything of a PlaneStack that does not depend on the frequency, in the device's dense on-grid layout:
+ * an unknown vector is [X (S,nx-1,ny) | Y (S,nx,ny-1) | C (n_pairs,nx,ny) | B (n_branches) | V (S,nx,ny)],
+ * each segment at its offset, masked entries zero.  Replaces PlaneStack.__init__ (peec.py:1559-1593). */
+typedef struct gt_geometry_desc {
+    int32_t n_sheets, nx, ny, n_pairs, n_branches;
+    int32_t precond_sheet;              /* 0: diagonal D (precond "diag"), 1: per-position blocks ("sheet") */
+    int64_t n_dense;                    /* dense vector length */
+    int64_t off_x, off_y, off_c, off_b, off_v;
+    const uint8_t* mask;                /* [n_dense] 1 where an unknown lives (strips, caps, branches, kept nodes) */
+    const uint8_t* code_x;              /* [(nx-1)*ny] bit k: sheet k has an x strip at the position */
+    const uint8_t* code_y;              /* [nx*(ny-1)] */
+    const int32_t* pair_layers;         /* [n_pairs*2] upper, lower sheet */
+    const int32_t* branch_nodes;        /* [n_branches*2] dense node index (k*nx*ny + i*ny + j) of ends a, b */
+    int64_t n_compact;                  /* nb + n_keep: the reference's unknown count (peec.py:2565) */
+    const int64_t* compact_to_dense;    /* [n_compact] */
+    int32_t fft_p[4];                   /* x: P0, P1; y: P0, P1 (each 2^a or 3*2^a, a >= 3) */
+    const double* spectrum_x;           /* [(P1/2+1)*(P0/2+1)*S*S] real kernel quadrant, scaled 1/(P0*P1) */
+    const double* spectrum_y;
+    /* Schur complement S = Ar^T D^-1 Ar: nested-dissection multifrontal structure (host analysis) */
+    int64_t n_factor;                   /* kept nodes */
+    const int64_t* perm;                /* [S*nx*ny] dense node -> factor index, -1 when not kept */
+    int32_t n_fronts, n_levels;
+    const int64_t* level_ptr;           /* [n_levels+1] into front_order */
+    const int64_t* front_order;         /* [n_fronts] fronts sorted by height */
+    const int64_t* own_start, *nown, *nbnd;      /* [n_fronts] */
+    const int64_t* bnd_ptr, *bnd_idx;            /* CSR: boundary factor indices per front */
+    const int64_t* child_ptr, *child_idx;        /* CSR: children per front */
+    const int64_t* cmap_ptr, *cmap_idx;          /* per child entry: its boundary's rows in the parent front */
+    const int64_t* panel_off, *upd_off, *vec_off;/* [n_fronts] element offsets */
+    int64_t panel_total, upd_total, vec_total;
+    const int64_t* ent_ptr;             /* [n_fronts+1] assembly entries per front */
+    const int32_t* ent_row, *ent_col;   /* front row / own column */
+    const int64_t* ent_s;               /* index of the S value */
+    int64_t n_svalues;                  /* lower-triangle entries of S */
+    int32_t n_table;                    /* per-frequency admittance table length */
+    const int64_t* sterm_ptr;           /* [n_svalues+1] CSR: S value = sum coef * table[tab] */
+    const int32_t* sterm_tab;
+    const double* sterm_coef;
+} gt_geometry_desc;
+
+typedef struct gt_solve_opts {
+    double tol;             /* stop when ||b - K x|| <= tol * ||b|| in FP64 (peec.py:3098-3099) */
+    int32_t restart;        /* inner GMRES cycle length */
+    int32_t max_its;        /* total inner iterations allowed per column */
+    double inner_tol;       /* relative residual reduction each inner FP32 cycle aims at */
+    int32_t precision;      /* 0: FP32 inner GMRES + FP64 refinement, 1: all FP64 (plain drop-in) */
+    int32_t max_outer;      /* refinement steps */
+} gt_solve_opts;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int gt_version(void);
+/* Text of the calling thread's last failure ("" when none). */
+const char* gt_last_error(void);
+/* Number of CUDA devices visible (0 when none); the library needs one. */
+int gt_device_count(void);
+
+/* Build a geometry on the current CUDA device (peec.py:1559-1593, gpu.py:617-666). */
+int gt_geometry_create(const gt_geometry_desc* desc, gt_geometry** out);
+void gt_geometry_free(gt_geometry* g);
+
+/* Factorise the Schur complement at n_ops frequencies (peec.py:2345-2445, 2465-2511):
+ * omega[n_ops]; zs[n_ops*S] sheet impedances per square; zcap[n_ops*n_pairs] and zbr[n_ops*n_branches]
+ * the capacitance / branch impedances; table[n_ops*n_table] the admittance table D^-1 draws from. */
+int gt_operators_create(gt_geometry* g, int32_t n_ops, const double* omega, const double* zs,
+                        const double* zcap, const double* zbr, const double* table, gt_operators** out);
+void gt_operators_free(gt_operators* ops);
+
+/* Solve n_cols columns K x = rhs (peec.py:2560-2607): col_op[n_cols] the operator of each column,
+ * rhs[n_cols*n_compact] complex in the reference's unknown order, x_out the same shape; its_out the inner
+ * iterations, resid_out the final relative FP64 residual per column.  stream: a cudaStream_t or NULL.
+ * Returns GT_NOT_CONVERGED when any column missed tol (its x is still the best found). */
+int gt_solve(gt_geometry* g, gt_operators* ops, int32_t n_cols, const int32_t* col_op, const double* rhs,
+             const gt_solve_opts* opts, double* x_out, int32_t* its_out, double* resid_out, void* stream);
+
+/* The same with device-resident dense vectors: rhs_device / x_device are [n_cols*n_dense] complex128 in the
+ * dense layout; nothing crosses to the host but the per-column scalars. */
+int gt_solve_device(gt_geometry* g, gt_operators* ops, int32_t n_cols, const int32_t* col_op,
+                    const void* rhs_device, const gt_solve_opts* opts, void* x_device, int32_t* its_out,
+                    double* resid_out, void* stream);
+
+/* Scatter compact (reference-order) complex vectors to the dense layout on the device and back. */
+int gt_to_dense(gt_geometry* g, int32_t n_cols, const double* compact, void* dense_device, void* stream);
+int gt_to_compact(gt_geometry* g, int32_t n_cols, const void* dense_device, double* compact, void* stream);
+
+/* Single operator applications for parity tests, compact vectors in and out:
+ * kind 0: system product K x (peec.py:3043-3062), 1: preconditioner M^-1 x (3064-3083),
+ * 2: L_p product of the strip part (2115-2135); precision 0: FP32, 1: FP64. */
+int gt_apply(gt_geometry* g, gt_operators* ops, int32_t kind, int32_t precision, int32_t n_cols,
+             const int32_t* col_op, const double* x, double* y, void* stream);
+
+/* Per-kernel timing of the last gt_solve / gt_solve_device on this geometry: count names, fills
+ * names (comma separated) and ms (milliseconds per kernel family) up to cap entries. */
+int gt_profile(gt_geometry* g, char* names, int32_t names_cap, double* ms, int32_t* launches, int32_t cap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GT_GB300_H */

@@ -1,0 +1,215 @@
+"""A numpy model of the device algorithm on the dense on-grid layout (test infrastructure).
+
+It executes, with numpy, the same arithmetic the CUDA kernels do on the same uploaded arrays: the 3-pass
+FFT L_p product on this build's padded sizes, the stencil tail of the system product, the per-position
+admittance blocks, and the multifrontal LDL^T factorisation / triangular solves driven by the symbolic
+analysis.  Tests compare it with the oracle (so the arrays are right) and the GPU with it (so the kernels
+are)."""
+import numpy as np
+
+
+class DenseModel:
+    def __init__(self, st):
+        self.st = st
+        t, D = st.top, st.dense
+        self.S, self.nx, self.ny = t.S, t.nx, t.ny
+        self.D = D
+        self.np_ = len(t.pair_layers)
+
+    # ---------------------------------------------------------------- views
+    def seg(self, v, name):
+        S, nx, ny, D = self.S, self.nx, self.ny, self.D
+        if name == "X":
+            return v[..., D.off_x: D.off_x + S * (nx - 1) * ny].reshape(v.shape[:-1] + (S, nx - 1, ny))
+        if name == "Y":
+            return v[..., D.off_y: D.off_y + S * nx * (ny - 1)].reshape(v.shape[:-1] + (S, nx, ny - 1))
+        if name == "C":
+            return v[..., D.off_c: D.off_c + self.np_ * nx * ny].reshape(v.shape[:-1] + (self.np_, nx, ny))
+        if name == "B":
+            return v[..., D.off_b: D.off_b + self.st.nbr]
+        if name == "V":
+            return v[..., D.off_v: D.off_v + S * nx * ny].reshape(v.shape[:-1] + (S, nx, ny))
+
+    def to_dense(self, x_compact):
+        v = np.zeros(self.D.n, complex)
+        v[self.D.compact_to_dense] = x_compact
+        return v
+
+    def to_compact(self, v):
+        return v[self.D.compact_to_dense]
+
+    # ---------------------------------------------------------------- L_p (3-pass FFT)
+    def lp(self, Xg, orient):
+        """(S, n0, n1) currents -> (S, n0, n1) L_p product, through the quadrant spectrum."""
+        P0, P1 = self.st.P[orient]
+        Kq = self.st.spectrum[orient]            # (Q1, Q0, S, S), scaled by 1/(P0 P1)
+        S, n0, n1 = Xg.shape
+        T = np.fft.fft(Xg, n=P1, axis=2)          # pass A: row FFTs
+        F = np.fft.fft(T, n=P0, axis=1)           # pass B: column FFTs ...
+        q0 = np.minimum(np.arange(P0), P0 - np.arange(P0))
+        q1 = np.minimum(np.arange(P1), P1 - np.arange(P1))
+        K = Kq[q1][:, q0]                         # (P1, P0, S, S)
+        G = np.einsum("cpts,spc->tpc", K, F)      # ... spectrum multiply-add ...
+        T2 = np.fft.ifft(G, axis=1)[:, :n0, :] * P0   # ... inverse column FFT (unscaled)
+        Y = np.fft.ifft(T2, axis=2)[:, :, :n1] * P1    # pass C: inverse row FFTs (unscaled)
+        return Y
+
+    # ---------------------------------------------------------------- system product
+    def matvec(self, v, w, zs, zcap, zbr):
+        st = self.st
+        t = st.top
+        out = np.zeros_like(v)
+        X, Y, C, B, Vn = (self.seg(v, n) for n in "XYCBV")
+        oX, oY, oC, oB, oV = (self.seg(out, n) for n in "XYCBV")
+        oX[:] = (zs[:, None, None] * X + 1j * w * self.lp(X, "x") - (Vn[:, :-1, :] - Vn[:, 1:, :])) * t.xb
+        oY[:] = (zs[:, None, None] * Y + 1j * w * self.lp(Y, "y") - (Vn[:, :, :-1] - Vn[:, :, 1:])) * t.yb
+        for p, (u, l) in enumerate(t.pair_layers):
+            oC[p] = (zcap[p] * C[p] - (Vn[u] - Vn[l])) * t.cap_mask[p]
+        Vf = Vn.reshape(-1)
+        for n, (a, b) in enumerate(self.branch_dense()):
+            oB[n] = zbr[n] * B[n] - (Vf[a] - Vf[b])
+        kcl = np.zeros_like(Vn)
+        kcl[:, :-1, :] += X
+        kcl[:, 1:, :] -= X
+        kcl[:, :, :-1] += Y
+        kcl[:, :, 1:] -= Y
+        for p, (u, l) in enumerate(t.pair_layers):
+            kcl[u] += C[p]
+            kcl[l] -= C[p]
+        kf = kcl.reshape(-1)
+        for n, (a, b) in enumerate(self.branch_dense()):
+            kf[a] += B[n]
+            kf[b] -= B[n]
+        oV[:] = kcl * self.vmask()
+        return out
+
+    def vmask(self):
+        m = np.zeros(self.S * self.nx * self.ny, bool)
+        node_dense = np.flatnonzero(self.st.top.node.ravel())
+        m[node_dense[self.st.top.keep]] = True
+        return m.reshape(self.S, self.nx, self.ny)
+
+    def branch_dense(self):
+        node_dense = np.flatnonzero(self.st.top.node.ravel())
+        return node_dense[self.st.top.branch_ab]
+
+    # ---------------------------------------------------------------- preconditioner
+    def dinv(self, v, tab):
+        """Apply D^-1 to the branch segments of v (per-position code tables, caps, branches)."""
+        st = self.st
+        S, ncode = self.S, 1 << self.S
+        out = np.zeros_like(v)
+        for o, name in ((0, "X"), (1, "Y")):
+            A = self.seg(v, name)
+            O = self.seg(out, name)
+            code = st.code["x" if o == 0 else "y"].astype(np.int64)
+            T = tab[: 2 * ncode * S * S].reshape(2, ncode, S, S)[o][code]      # (n0, n1, S, S)
+            O[:] = np.einsum("ijkl,lij->kij", T, A)
+        C, oC = self.seg(v, "C"), self.seg(out, "C")
+        for p in range(self.np_):
+            oC[p] = tab[st.tab_cap0 + p] * C[p] * st.top.cap_mask[p]
+        self.seg(out, "B")[:] = tab[st.tab_br0: st.tab_br0 + st.nbr] * self.seg(v, "B")
+        return out
+
+    def kcl(self, v):
+        """Ar^T applied to the branch segments: the node rows (masked by the kept nodes)."""
+        t = self.st.top
+        X, Y, C, B = (self.seg(v, n) for n in "XYCB")
+        k = np.zeros((self.S, self.nx, self.ny), complex)
+        k[:, :-1, :] += X
+        k[:, 1:, :] -= X
+        k[:, :, :-1] += Y
+        k[:, :, 1:] -= Y
+        for p, (u, l) in enumerate(t.pair_layers):
+            k[u] += C[p]
+            k[l] -= C[p]
+        kf = k.reshape(-1)
+        for n, (a, b) in enumerate(self.branch_dense()):
+            kf[a] += B[n]
+            kf[b] -= B[n]
+        return k * self.vmask()
+
+    def grad(self, Vn):
+        """Ar applied to node potentials: per-branch-segment differences V[a] - V[b] (dense, unmasked)."""
+        out = np.zeros(self.D.n, complex)
+        self.seg(out, "X")[:] = Vn[:, :-1, :] - Vn[:, 1:, :]
+        self.seg(out, "Y")[:] = Vn[:, :, :-1] - Vn[:, :, 1:]
+        C = self.seg(out, "C")
+        for p, (u, l) in enumerate(self.st.top.pair_layers):
+            C[p] = Vn[u] - Vn[l]
+        Vf = Vn.reshape(-1)
+        B = self.seg(out, "B")
+        for n, (a, b) in enumerate(self.branch_dense()):
+            B[n] = Vf[a] - Vf[b]
+        return out
+
+    def precond(self, v, tab, fac):
+        sym = self.st.sym
+        t1 = self.dinv(v, tab)
+        s = self.seg(v, "V") - self.kcl(t1)
+        s_fac = s.reshape(-1)[sym.iperm]
+        y_fac = fac.solve(s_fac)
+        yv = np.zeros(self.S * self.nx * self.ny, complex)
+        yv[sym.iperm] = y_fac
+        yv = yv.reshape(self.S, self.nx, self.ny)
+        u = v + self.grad(yv)
+        out = self.dinv(u, tab)
+        out *= self.D.mask
+        self.seg(out, "V")[:] = yv
+        return out
+
+
+class Multifrontal:
+    """LDL^T of S by the symbolic analysis's fronts (what the device factorisation kernels do)."""
+
+    def __init__(self, st, s_values):
+        sym = st.sym
+        self.sym = sym
+        nfront = len(sym.nown)
+        self.panels = [None] * nfront
+        upd = [None] * nfront
+        for h in range(len(sym.level_ptr) - 1):
+            for f in sym.order[sym.level_ptr[h]: sym.level_ptr[h + 1]]:
+                no, nbd = sym.nown[f], sym.nbnd[f]
+                nf = no + nbd
+                F = np.zeros((nf, nf), complex)
+                e = slice(sym.ent_ptr[f], sym.ent_ptr[f + 1])
+                np.add.at(F, (sym.ent_row[e], sym.ent_col[e]), s_values[sym.ent_s[e]])
+                for ci in range(sym.child_ptr[f], sym.child_ptr[f + 1]):
+                    c = sym.child_idx[ci]
+                    m = sym.cmap_idx[sym.cmap_ptr[ci]: sym.cmap_ptr[ci + 1]]
+                    F[np.ix_(m, m)] += upd[c]
+                    upd[c] = None
+                # F holds the lower triangle (assembly) plus update blocks (full): symmetrise from the lower
+                F = np.tril(F) + np.tril(F, -1).T
+                for k in range(no):
+                    dk = F[k, k]
+                    l = F[k + 1:, k] / dk
+                    F[k + 1:, k + 1:] -= np.outer(l, l) * dk
+                    F[k + 1:, k] = l
+                self.panels[f] = F[:, :no].copy()
+                upd[f] = F[no:, no:].copy()
+
+    def solve(self, b):
+        sym = self.sym
+        z = b.astype(complex).copy()
+        nlev = len(sym.level_ptr) - 1
+        for h in range(nlev):
+            for f in sym.order[sym.level_ptr[h]: sym.level_ptr[h + 1]]:
+                o0, no = sym.own_start[f], sym.nown[f]
+                Lp = self.panels[f]
+                bnd = sym.bnd_idx[sym.bnd_ptr[f]: sym.bnd_ptr[f + 1]]
+                for k in range(no):
+                    z[o0 + k + 1: o0 + no] -= Lp[k + 1: no, k] * z[o0 + k]
+                    z[bnd] -= Lp[no:, k] * z[o0 + k]
+        for f in range(len(sym.nown)):
+            o0, no = sym.own_start[f], sym.nown[f]
+            z[o0: o0 + no] /= np.diag(self.panels[f][:no, :no])
+        for h in range(nlev - 1, -1, -1):
+            for f in sym.order[sym.level_ptr[h]: sym.level_ptr[h + 1]]:
+                o0, no = sym.own_start[f], sym.nown[f]
+                Lp = self.panels[f]
+                bnd = sym.bnd_idx[sym.bnd_ptr[f]: sym.bnd_ptr[f + 1]]
+                for k in range(no - 1, -1, -1):
+                    z[o0 + k] -= Lp[no:, k] @ z[bnd] + Lp[k + 1: no, k] @ z[o0 + k + 1: o0 + no]
+        return z

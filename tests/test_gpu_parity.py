@@ -1,0 +1,82 @@
+"""Parity of the CUDA path with the reference: device products against the reference's own products and
+solves (golden fixtures), through the C ABI.  Needs a GPU."""
+import numpy as np
+import pytest
+
+from groundtruth_gb300 import native, stack as gs
+from test_oracle_golden import load
+
+pytestmark = pytest.mark.gpu
+CASES = ["small_pair", "small_stack3", "plain_plane"]
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.fixture(scope="module", params=CASES)
+def case(request):
+    z, board = load(request.param)
+    st, routes = gs.from_board(board)
+    return request.param, z, board, st, routes
+
+
+def _op(st, f):
+    obj, k = st.factorise([f])[0]
+    return obj, k
+
+
+# FP64 products: rounding-level agreement with the reference (its FFT sizes differ from ours)
+def test_fp64_system_product(case):
+    name, z, board, st, routes = case
+    obj, k = _op(st, float(z["op_f"]))
+    y = native.apply(st.handle, obj, "matvec", z["prod_x"], k, "fp64")[0]
+    assert rel(y, z["prod_matvec"]) < 1e-12
+
+
+def test_fp64_lp_product(case):
+    name, z, board, st, routes = case
+    obj, k = _op(st, float(z["op_f"]))
+    x = np.zeros(st.nb + int(st.keep.sum()), complex)
+    x[: st.ns] = z["prod_I"]
+    y = native.apply(st.handle, obj, "lp", x, k, "fp64")[0][: st.ns]
+    assert rel(y, z["prod_Lp"]) < 1e-12
+
+
+def test_fp64_preconditioner(case):
+    name, z, board, st, routes = case
+    obj, k = _op(st, float(z["op_f"]))
+    y = native.apply(st.handle, obj, "precond", z["prod_x"], k, "fp64")[0]
+    assert rel(y, z["prod_precond"]) < 1e-9
+
+
+# FP32 products: within single-precision rounding of the FP64 reference
+def test_fp32_system_product(case):
+    name, z, board, st, routes = case
+    obj, k = _op(st, float(z["op_f"]))
+    y = native.apply(st.handle, obj, "matvec", z["prod_x"], k, "fp32")[0]
+    assert rel(y, z["prod_matvec"]) < 2e-6
+
+
+def test_fp32_preconditioner(case):
+    name, z, board, st, routes = case
+    obj, k = _op(st, float(z["op_f"]))
+    y = native.apply(st.handle, obj, "precond", z["prod_x"], k, "fp32")[0]
+    assert rel(y, z["prod_precond"]) < 1e-3
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_solves_match_reference(case, precision):
+    """Every (net, frequency) of the fixture in one batch; rtol 1e-10 like the reference run.  Both stop at a
+    backward error of 1e-10, so the solutions agree to within the conditioning times that."""
+    name, z, board, st, routes = case
+    sols = gs.solve_many(routes, list(board.freqs), tol=board.tol, precision=precision)
+    for k, per in enumerate(sols):
+        for q, sol in enumerate(per):
+            x_ref = z[f"x{k}_{q}"]
+            Ib = x_ref[: st.nb]
+            assert rel(np.concatenate([sol.I_x[tuple(st.xa.T)], sol.I_y[tuple(st.ya.T)]]), Ib[: st.ns]) < 1e-7, (k, q)
+            Zr = complex(z[f"Z{k}_{q}"])
+            assert abs(sol.Z_loop - Zr) <= 1e-8 * abs(Zr), (k, q, sol.Z_loop, Zr)
+            assert rel(sol.m, z[f"m{k}_{q}"]) < 1e-7
+            assert sol.residual <= board.tol

@@ -1,0 +1,88 @@
+"""The host-side setup (topology, dense layout, spectra, Schur structure) against the oracle, through the
+numpy model of the device algorithm (tests/host_model.py).  CPU only."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from groundtruth_gb300 import stack as gs, synth
+from oracle import peec_oracle as po
+from test_oracle_golden import load, oracle_stack
+from host_model import DenseModel, Multifrontal
+
+CASES = ["small_pair", "small_stack3", "plain_plane"]
+
+
+@pytest.fixture(scope="module", params=CASES)
+def case(request):
+    z, board = load(request.param)
+    st, routes = gs.from_board(board, _device=False)
+    ost = oracle_stack(board)
+    return request.param, z, board, st, routes, ost
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def test_topology_matches_reference(case):
+    name, z, board, st, routes, ost = case
+    for k in ("xa", "ya", "nid", "keep", "a_nodes", "b_nodes", "full_label", "cond_label"):
+        assert np.array_equal(getattr(st.top, k), z[k]), k
+    assert np.array_equal(st.top.cap, z["cap"])
+    assert st.nb == int(z["nb"])
+
+
+def test_dense_matvec_matches_oracle(case):
+    name, z, board, st, routes, ost = case
+    m = DenseModel(st)
+    f = float(z["op_f"])
+    op = ost.operator(f)
+    w, zs, zcap, zbr, tab = st._freq_tables(f)
+    x = z["prod_x"]
+    got = m.to_compact(m.matvec(m.to_dense(x), w, zs, zcap, zbr))
+    assert rel(got, z["prod_matvec"]) < 1e-12
+    I = z["prod_I"]
+    v = np.zeros(m.D.n, complex)
+    v[m.D.compact_to_dense[: st.ns]] = I
+    lp = np.concatenate([m.lp(m.seg(v, "X"), "x")[tuple(st.xa.T)], m.lp(m.seg(v, "Y"), "y")[tuple(st.ya.T)]])
+    assert rel(lp, z["prod_Lp"]) < 1e-12
+
+
+def test_schur_assembly_and_factor_match_oracle(case):
+    name, z, board, st, routes, ost = case
+    f = float(z["op_f"])
+    op = ost.operator(f)
+    w, zs, zcap, zbr, tab = st._freq_tables(f)
+    svals = st.sterm @ tab
+    sym = st.sym
+    n = sym.n
+    Sl = sp.coo_matrix((svals, (sym.s_row, sym.s_col)), shape=(n, n)).toarray()
+    Sfull = np.tril(Sl) + np.tril(Sl, -1).T
+    # oracle S in reference kept order -> factor order
+    node_dense = np.flatnonzero(st.top.node.ravel())
+    fac = sym.perm[node_dense[st.top.keep]]
+    So = np.zeros((n, n), complex)
+    Sd = op["S"].toarray()
+    So[np.ix_(fac, fac)] = Sd
+    assert np.abs(Sfull - So).max() <= 1e-12 * np.abs(So).max()
+    mf = Multifrontal(st, svals)
+    b = np.random.default_rng(0).standard_normal(n) + 1j * np.random.default_rng(1).standard_normal(n)
+    y = mf.solve(b)
+    assert rel(Sfull @ y, b) < 1e-10
+
+
+def test_dense_precond_matches_oracle(case):
+    name, z, board, st, routes, ost = case
+    m = DenseModel(st)
+    f = float(z["op_f"])
+    w, zs, zcap, zbr, tab = st._freq_tables(f)
+    mf = Multifrontal(st, st.sterm @ tab)
+    got = m.to_compact(m.precond(m.to_dense(z["prod_x"]), tab, mf))
+    assert rel(got, z["prod_precond"]) < 1e-9
+
+
+def test_excitation_matches_reference(case):
+    name, z, board, st, routes, ost = case
+    for k, r in enumerate(routes):
+        assert rel(r.psi, z[f"psi{k}"]) < 1e-13
+        assert r.L_trace == pytest.approx(float(z[f"Ltrace{k}"]), rel=1e-13)
