@@ -27,6 +27,7 @@
 namespace gt {
 
 static thread_local std::string t_last_error;
+std::atomic<long long> g_launches{0};
 void set_error(const std::string& s) { t_last_error = s; }
 
 struct Invalid : std::runtime_error {
@@ -62,11 +63,16 @@ struct Profiler {
     struct Rec {
         int fam;
         cudaEvent_t a, b;
+        double bytes;
     };
     std::vector<Rec> pending;
     std::vector<cudaEvent_t> free_events;
     std::vector<std::string> names;
-    std::map<int, std::pair<double, int>> acc;
+    struct Acc {
+        double ms = 0, bytes = 0;
+        int launches = 0;
+    };
+    std::map<int, Acc> acc;
     int family(const char* n) {
         for (size_t i = 0; i < names.size(); ++i)
             if (names[i] == n) return (int)i;
@@ -88,8 +94,9 @@ struct Profiler {
             float ms = 0;
             GT_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
             auto& a = acc[r.fam];
-            a.first += ms;
-            a.second += 1;
+            a.ms += ms;
+            a.launches += 1;
+            a.bytes += r.bytes;
             free_events.push_back(r.a);
             free_events.push_back(r.b);
         }
@@ -109,7 +116,9 @@ struct Scope {
     int fam;
     cudaEvent_t a{};
     cudaStream_t st;
-    Scope(Profiler* prof, const char* name, cudaStream_t s) : p(prof && prof->on ? prof : nullptr), fam(0), st(s) {
+    double bytes;
+    Scope(Profiler* prof, const char* name, cudaStream_t s, double algo_bytes = 0)
+        : p(prof && prof->on ? prof : nullptr), fam(0), st(s), bytes(algo_bytes) {
         if (!p) return;
         fam = p->family(name);
         a = p->ev();
@@ -119,7 +128,7 @@ struct Scope {
         if (!p) return;
         try {
             cudaEvent_t b = p->ev();
-            if (cudaEventRecord(b, st) == cudaSuccess) p->pending.push_back({fam, a, b});
+            if (cudaEventRecord(b, st) == cudaSuccess) p->pending.push_back({fam, a, b, bytes});
         } catch (...) {
         }
     }
@@ -250,11 +259,18 @@ static void matvec(gt_geometry* G, gt_operators* ops, const cx<R>* x, const cx<R
         a.zs = ops->zs;
         a.mode = mode;
         a.col_list = nullptr;
-        Scope s(P, sizeof(R) == 4 ? "lp_fft_f32" : "lp_fft_f64", st);
+        // algorithmic bytes: x, V and out over the strips, the intermediate grid written by pass A, read and
+        // written by pass B, read by pass C, the spectrum once per column group of pass B
+        const double es = sizeof(cx<R>), plane = (double)a.S * o.n0 * o.n1;
+        const double bytes = ncol * es * (3 * plane + 4.0 * a.S * o.n0 * o.P1) +
+                             std::ceil(ncol / 8.0) * sizeof(R) * a.S * a.S * (o.P0 / 2 + 1) * (o.P1 / 2 + 1);
+        Scope s(P, sizeof(R) == 4 ? "lp_fft_f32" : "lp_fft_f64", st, bytes);
         launch_lp<R>(a, st);
     }
     if (mode != 2) {
-        Scope s(P, sizeof(R) == 4 ? "tail_f32" : "tail_f64", st);
+        const double nXY = (double)(G->geo.off_c - G->geo.off_x);
+        Scope s(P, sizeof(R) == 4 ? "tail_f32" : "tail_f64", st,
+                ncol * (double)sizeof(cx<R>) * (2.0 * (G->geo.n - nXY) + nXY));
         launch_tail<R>(G->geo, x, rhs, out, ld, ncol, col_op, ops->zcap, ops->zbr, mode, st);
     }
 }
@@ -264,28 +280,32 @@ template <typename R>
 static void precond(gt_geometry* G, gt_operators* ops, const cx<R>* r, int64_t ldr, cx<R>* out, int64_t ldo, int nslot,
                     const int* slot_op, const Groups& grp, int gmax, cx<R>* zfac, cx<R>* uvec, cudaStream_t st) {
     Profiler* P = &G->prof;
+    const double es = sizeof(cx<R>), n = (double)G->geo.n, nfac = (double)G->F.nfac;
+    const double nodes = (double)G->geo.S * G->geo.nx * G->geo.ny, nXYC = (double)(G->geo.off_b - G->geo.off_x);
+    // the factor's panels are read once per column group in each direction
+    const double panel = (double)grp.ngroup * es * G->F.panel_total;
     {
-        Scope s(P, "pc_node", st);
+        Scope s(P, "pc_node", st, nslot * es * (nXYC + nodes + nfac));
         launch_pc_node<R>(G->geo, r, ldr, zfac, nslot, slot_op, ops->tab, st);
     }
-    const cx<R>* panel = panel_of<R>(ops);
+    const cx<R>* pan = panel_of<R>(ops);
     const int nlev = (int)G->level_ptr.size() - 1;
     {
-        Scope s(P, sizeof(R) == 4 ? "fwd_f32" : "fwd_f64", st);
+        Scope s(P, sizeof(R) == 4 ? "fwd_f32" : "fwd_f64", st, panel + nslot * es * (2 * nfac + 2.0 * G->F.vec_total));
         for (int h = 0; h < nlev; ++h) {
             int nf = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);
-            launch_fwd_level<R>(G->F, G->d_order + G->level_ptr[h], nf, G->level_maxnf[h], panel, zfac, uvec, grp, gmax, st);
+            launch_fwd_level<R>(G->F, G->d_order + G->level_ptr[h], nf, G->level_maxnf[h], pan, zfac, uvec, grp, gmax, st);
         }
     }
     {
-        Scope s(P, sizeof(R) == 4 ? "bwd_f32" : "bwd_f64", st);
+        Scope s(P, sizeof(R) == 4 ? "bwd_f32" : "bwd_f64", st, panel + nslot * es * 2 * nfac);
         for (int h = nlev - 1; h >= 0; --h) {
             int nf = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);
-            launch_bwd_level<R>(G->F, G->d_order + G->level_ptr[h], nf, G->level_maxnf[h], panel, zfac, grp, gmax, st);
+            launch_bwd_level<R>(G->F, G->d_order + G->level_ptr[h], nf, G->level_maxnf[h], pan, zfac, grp, gmax, st);
         }
     }
     {
-        Scope s(P, "pc_strip", st);
+        Scope s(P, "pc_strip", st, nslot * es * (2 * n + nfac));
         launch_pc_strip<R>(G->geo, r, ldr, zfac, out, ldo, nslot, slot_op, ops->tab, st);
     }
 }
@@ -447,12 +467,16 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
             precond<R>(G, ops, V + (int64_t)j * n, lds, z, n, ns, W.slot_op, grp, gmax, zfac, uvec, st);
             matvec<R>(G, ops, z, nullptr, w, n, ns, W.slot_op, 0, T, st);
             {
-                Scope sc(P, sizeof(R) == 4 ? "gs_f32" : "gs_f64", st);
+                // classical Gram-Schmidt: the j+1 basis vectors read twice, w read twice and written once
+                Scope sc(P, sizeof(R) == 4 ? "gs_f32" : "gs_f64", st, (double)ns * sizeof(cx<R>) * n * (2.0 * (j + 1) + 3));
                 launch_dots<R>(V, n, lds, j + 1, w, n, n, ns, S.active, W.partial, nch, st);
                 launch_reduce(W.partial, nch, j + 1, ns, S.active, S.hvec, S.ldh, 0, st);
                 launch_update<R>(V, n, lds, j + 1, S.hvec, S.ldh, w, n, n, ns, S.active, W.partial, nch, -1, st);
                 launch_reduce(W.partial, nch, 0, ns, S.active, S.hn2, 1, 0, st);
                 launch_dgks(S, j, st);
+            }
+            {
+                Scope sc(P, "gs_reorth", st);
                 launch_dots<R>(V, n, lds, j + 1, w, n, n, ns, S.reorth, W.partial, nch, st);
                 launch_reduce(W.partial, nch, j + 1, ns, S.reorth, S.h2vec, S.ldh, 0, st);
                 launch_update<R>(V, n, lds, j + 1, S.h2vec, S.ldh, w, n, n, ns, S.reorth, W.partial, nch, -1, st);
@@ -476,18 +500,18 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
         }
         GT_CUDA(cudaMemsetAsync(w, 0, (size_t)ns * n * sizeof(cx<R>), st));
         {
-            Scope sc(P, sizeof(R) == 4 ? "gs_f32" : "gs_f64", st);
+            Scope sc(P, "combine", st, (double)ns * sizeof(cx<R>) * n * (jdone + 2.0));
             launch_update<R>(V, n, lds, jdone, S.y, S.ldh, w, n, n, ns, nullptr, nullptr, nch, 1, st);
         }
         precond<R>(G, ops, w, n, z, n, ns, W.slot_op, grp, gmax, zfac, uvec, st);
         {
-            Scope sc(P, "refine", st);
+            Scope sc(P, "refine", st, (double)ns * n * (32.0 + sizeof(cx<R>)));
             launch_refine<R>(W.x64, n, z, n, W.slot_col, W.rho, n, ns, st);
         }
         // the true residual in FP64
         matvec<double>(G, ops, W.x64, W.b64, W.r64, n, ncol, W.col_op, 1, W.T64, st);
         {
-            Scope sc(P, "norms", st);
+            Scope sc(P, "norms", st, 16.0 * ncol * n);
             norms64(G, W.r64, n, ncol, W.rho, st);
         }
         GT_CUDA(cudaMemcpyAsync(h_rho.data(), W.rho, ncol * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -542,6 +566,8 @@ static int run_solve(gt_geometry* G, gt_operators* ops, int ncol, const int* col
 extern "C" {
 
 int gt_version(void) { return 100; }
+
+int64_t gt_launch_count(void) { return gt::g_launches.load(); }
 
 const char* gt_last_error(void) { return gt::t_last_error.c_str(); }
 
@@ -869,7 +895,8 @@ int gt_apply(gt_geometry* G, gt_operators* ops, int32_t kind, int32_t precision,
     GT_GUARD_END
 }
 
-int gt_profile(gt_geometry* G, char* names, int32_t names_cap, double* ms, int32_t* launches, int32_t cap) {
+int gt_profile(gt_geometry* G, char* names, int32_t names_cap, double* ms, double* bytes, int32_t* launches,
+               int32_t cap) {
     if (!G) return 0;
     if (names == nullptr && cap < 0) {  // toggle: cap = -1 off, -2 on (and reset)
         G->prof.on = cap == -2;
@@ -882,8 +909,9 @@ int gt_profile(gt_geometry* G, char* names, int32_t names_cap, double* ms, int32
         if (k >= cap) break;
         if (!s.empty()) s += ",";
         s += G->prof.names[kv.first];
-        ms[k] = kv.second.first;
-        launches[k] = kv.second.second;
+        ms[k] = kv.second.ms;
+        bytes[k] = kv.second.bytes;
+        launches[k] = kv.second.launches;
         ++k;
     }
     if (names && names_cap > 0) {

@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <atomic>
 #include <string>
 
 namespace gt {
@@ -52,6 +53,13 @@ struct CudaError {
                                                     __FILE__ + ":" + std::to_string(__LINE__)}; \
     } while (0)
 
-#define GT_LAUNCH_CHECK() GT_CUDA(cudaGetLastError())
+// kernels launched by the library (gt_launch_count)
+extern std::atomic<long long> g_launches;
+
+#define GT_LAUNCH_CHECK()               \
+    do {                                \
+        ::gt::g_launches.fetch_add(1);  \
+        GT_CUDA(cudaGetLastError());    \
+    } while (0)
 
 }  // namespace gt

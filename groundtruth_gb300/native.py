@@ -59,6 +59,7 @@ def load():
     lib.gt_version.restype = C.c_int
     lib.gt_last_error.restype = C.c_char_p
     lib.gt_device_count.restype = C.c_int
+    lib.gt_launch_count.restype = C.c_int64
     lib.gt_geometry_create.argtypes = [C.POINTER(GeometryDesc), C.POINTER(P)]
     lib.gt_geometry_free.argtypes = [P]
     lib.gt_geometry_free.restype = None
@@ -70,7 +71,7 @@ def load():
     lib.gt_to_dense.argtypes = [P, C.c_int32, DP, P, P]
     lib.gt_to_compact.argtypes = [P, C.c_int32, P, DP, P]
     lib.gt_apply.argtypes = [P, P, C.c_int32, C.c_int32, C.c_int32, I32P, DP, DP, P]
-    lib.gt_profile.argtypes = [P, C.c_char_p, C.c_int32, DP, I32P, C.c_int32]
+    lib.gt_profile.argtypes = [P, C.c_char_p, C.c_int32, DP, DP, I32P, C.c_int32]
     if lib.gt_device_count() < 1:
         raise RuntimeError("no CUDA device is visible: the groundtruth_gb300 solver runs on the GPU only")
     _LIB = lib
@@ -153,18 +154,45 @@ class Geometry:
             _LIB.gt_geometry_free(self.h)
             self.h = None
 
+    def solve_device(self, obj, col_op: np.ndarray, rhs_ptr: int, x_ptr: int, tol: float, restart: int = 50,
+                     max_its: int = 2000, inner_tol: float = 1e-5, precision: str = "mixed", max_outer: int = 40,
+                     stream: int = 0):
+        """gt_solve_device on dense complex128 device buffers (pointers); returns (its, resid)."""
+        idx = np.ascontiguousarray(col_op, np.int32)
+        ncol = len(idx)
+        its = np.zeros(ncol, np.int32)
+        res = np.zeros(ncol)
+        o = SolveOpts(tol, restart, max_its, inner_tol, 1 if precision == "fp64" else 0, max_outer)
+        rc = self.lib.gt_solve_device(self.h, obj.h, ncol, _ptr(idx, C.c_int32), P(rhs_ptr), C.byref(o), P(x_ptr),
+                                      _ptr(its, C.c_int32), _ptr(res, C.c_double), P(stream))
+        if rc not in (GT_OK, GT_NOT_CONVERGED):
+            check(self.lib, rc, "gt_solve_device")
+        return its, res
+
+    def to_dense(self, compact: np.ndarray, dense_ptr: int, stream: int = 0):
+        c = np.ascontiguousarray(np.atleast_2d(compact), np.complex128)
+        check(self.lib, self.lib.gt_to_dense(self.h, c.shape[0], _ptr(c.view(np.float64), C.c_double), P(dense_ptr),
+                                             P(stream)), "gt_to_dense")
+
+    def to_compact(self, dense_ptr: int, ncol: int, stream: int = 0) -> np.ndarray:
+        out = np.zeros((ncol, self.n_compact), np.complex128)
+        check(self.lib, self.lib.gt_to_compact(self.h, ncol, P(dense_ptr), _ptr(out.view(np.float64), C.c_double),
+                                               P(stream)), "gt_to_compact")
+        return out
+
     def profile(self, on: bool | None = None) -> dict:
-        """Toggle (on=True/False: reset) or read {kernel family: (ms, launches)} of the last solves."""
+        """Toggle (on=True/False: reset) or read {kernel family: (ms, algorithmic bytes, timed regions)}."""
         if on is not None:
-            self.lib.gt_profile(self.h, None, 0, None, None, -2 if on else -1)
+            self.lib.gt_profile(self.h, None, 0, None, None, None, -2 if on else -1)
             return {}
         cap = 64
         names = C.create_string_buffer(4096)
-        ms = np.zeros(cap)
+        ms, by = np.zeros(cap), np.zeros(cap)
         launches = np.zeros(cap, np.int32)
-        k = self.lib.gt_profile(self.h, names, 4096, _ptr(ms, C.c_double), _ptr(launches, C.c_int32), cap)
+        k = self.lib.gt_profile(self.h, names, 4096, _ptr(ms, C.c_double), _ptr(by, C.c_double),
+                                _ptr(launches, C.c_int32), cap)
         keys = names.value.decode().split(",") if k else []
-        return {n: (float(ms[i]), int(launches[i])) for i, n in enumerate(keys)}
+        return {n: (float(ms[i]), float(by[i]), int(launches[i])) for i, n in enumerate(keys)}
 
 
 class Operators:

@@ -91,6 +91,8 @@ int gt_version(void);
 const char* gt_last_error(void);
 /* Number of CUDA devices visible (0 when none); the library needs one. */
 int gt_device_count(void);
+/* Kernels this library has launched since it was loaded (all threads). */
+int64_t gt_launch_count(void);
 
 /* Build a geometry on the current CUDA device (peec.py:1559-1593, gpu.py:617-666). */
 int gt_geometry_create(const gt_geometry_desc* desc, gt_geometry** out);
@@ -126,9 +128,12 @@ int gt_to_compact(gt_geometry* g, int32_t n_cols, const void* dense_device, doub
 int gt_apply(gt_geometry* g, gt_operators* ops, int32_t kind, int32_t precision, int32_t n_cols,
              const int32_t* col_op, const double* x, double* y, void* stream);
 
-/* Per-kernel timing of the last gt_solve / gt_solve_device on this geometry: count names, fills
- * names (comma separated) and ms (milliseconds per kernel family) up to cap entries. */
-int gt_profile(gt_geometry* g, char* names, int32_t names_cap, double* ms, int32_t* launches, int32_t cap);
+/* Per-kernel-family timing of the solves on this geometry, by CUDA events on the launch stream.
+ * names == NULL and cap == -2: reset and switch timing on; cap == -1: switch it off.  Otherwise fills
+ * names (comma separated), ms (milliseconds), bytes (algorithmic bytes moved) and launches (timed
+ * regions) per family, up to cap families, and returns their count. */
+int gt_profile(gt_geometry* g, char* names, int32_t names_cap, double* ms, double* bytes, int32_t* launches,
+               int32_t cap);
 
 #ifdef __cplusplus
 }

@@ -523,7 +523,14 @@ class OracleStack:
         i, j = np.arange(P[0]), np.arange(P[1])
         return Kq[np.minimum(i, P[0] - i)[:, None], np.minimum(j, P[1] - j)[None, :], t, s]
 
-    # -- L_p product (peec.py:2054-2135)
+    def _full(self, orient: str, t: int, s: int) -> np.ndarray:
+        cache = self.__dict__.setdefault("_full_cache", {})
+        key = (orient, t, s)
+        if key not in cache:
+            cache[key] = self.full_kernel(orient, t, s)
+        return cache[key]
+
+    # -- L_p product (peec.py:2054-2135; FFTs on all host cores as fft_workers() = -1, peec.py:136-138)
     def Lp_matvec(self, I_s: np.ndarray) -> np.ndarray:
         out = np.empty(self.ns, complex)
         S = self.N
@@ -533,12 +540,12 @@ class OracleStack:
                 continue
             X = np.zeros(shape, complex)
             X[tuple(idx.T)] = I_s[lo:hi]
-            F = fft2(X, s=P, axes=(1, 2))
+            F = fft2(X, s=P, axes=(1, 2), workers=-1)
             G = np.zeros_like(F)
             for t in range(S):
                 for s in range(S):
-                    G[t] += self.full_kernel(orient, t, s) * F[s]
-            Y = ifft2(G, axes=(1, 2))
+                    G[t] += self._full(orient, t, s) * F[s]
+            Y = ifft2(G, axes=(1, 2), workers=-1, overwrite_x=True)
             out[lo:hi] = Y[tuple(idx.T)]
         return out
 

@@ -10,7 +10,7 @@ ROOT = Path(__file__).resolve().parent.parent
 
 def declared():
     text = (ROOT / "include" / "gt_gb300.h").read_text()
-    return sorted(set(re.findall(r"^\s*(?:int|void|const char\*)\s+(gt_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t|void|const char\*)\s+(gt_\w+)\s*\(", text, re.M)))
 
 
 @pytest.fixture(scope="module")
