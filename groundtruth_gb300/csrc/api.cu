@@ -541,6 +541,41 @@ static int run_solve(gt_geometry* G, gt_operators* ops, int ncol, const int* col
     return solve_impl<float>(G, ops, ncol, col_op, o, its, res, st);
 }
 
+// The L_p product of n_cols dense FP64 vectors into the strip segments of y, with the FFT passes'
+// intermediate grid in caller-provided scratch (used by gt_lp_product_noalloc, noalloc.cu).  Launches
+// kernels only: no allocation, no synchronisation.
+size_t lp_scratch_bytes(const gt_geometry* G, int ncol) { return (size_t)ncol * (size_t)G->maxT * sizeof(c64); }
+
+void lp_with_scratch(gt_geometry* G, int ncol, const c64* x, c64* y, void* scratch, cudaStream_t st) {
+    for (int k = 0; k < 2; ++k) {
+        const Orient& o = G->o[k];
+        if ((int64_t)o.n0 * o.n1 == 0) continue;
+        LpArgs<double> a{};
+        a.x = x;
+        a.out = y;
+        a.ld = G->geo.n;
+        a.off = o.off;
+        a.off_v = G->geo.off_v;
+        a.S = G->geo.S;
+        a.n0 = o.n0;
+        a.n1 = o.n1;
+        a.nx = G->geo.nx;
+        a.ny = G->geo.ny;
+        a.di = o.di;
+        a.dj = o.dj;
+        a.P0 = o.P0;
+        a.P1 = o.P1;
+        a.ncol = ncol;
+        a.tw0 = o.tw0_64;
+        a.tw1 = o.tw1_64;
+        a.spec = o.spec64;
+        a.T = static_cast<c64*>(scratch);
+        a.mask = G->geo.mask;
+        a.mode = 2;
+        launch_lp<double>(a, st);
+    }
+}
+
 }  // namespace gt
 
 // ------------------------------------------------------------------------------------------ C ABI

@@ -72,6 +72,7 @@ def load():
     lib.gt_to_compact.argtypes = [P, C.c_int32, P, DP, P]
     lib.gt_apply.argtypes = [P, P, C.c_int32, C.c_int32, C.c_int32, I32P, DP, DP, P]
     lib.gt_profile.argtypes = [P, C.c_char_p, C.c_int32, DP, DP, I32P, C.c_int32]
+    lib.gt_lp_product_noalloc.argtypes = [P, C.c_int32, P, P, P]
     if lib.gt_device_count() < 1:
         raise RuntimeError("no CUDA device is visible: the groundtruth_gb300 solver runs on the GPU only")
     _LIB = lib

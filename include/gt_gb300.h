@@ -128,6 +128,20 @@ int gt_to_compact(gt_geometry* g, int32_t n_cols, const void* dense_device, doub
 int gt_apply(gt_geometry* g, gt_operators* ops, int32_t kind, int32_t precision, int32_t n_cols,
              const int32_t* col_op, const double* x, double* y, void* stream);
 
+/* Size of the fixed device scratch array gt_lp_product_noalloc uses (bytes). */
+#define GT_LP_NOALLOC_SCRATCH_BYTES (32u << 20)
+
+/* The L_p (partial-inductance) product of the strip currents of n_cols dense complex128 vectors
+ * (x_device, n_cols * n_dense, the dense layout), written into the strip segments of y_device (its other
+ * segments are left as they are), without allocating any device memory: for callers that may not allocate
+ * while they compute (a process under a fixed device-memory budget, a latency-critical caller that cannot
+ * afford cudaMalloc's device-wide synchronisation).  The FFT scratch comes from a fixed array of
+ * GT_LP_NOALLOC_SCRATCH_BYTES held by every GPU that loads this library; n_cols beyond what it holds is
+ * rejected with GT_INVALID_ARGUMENT.  The first call on a device looks the array's address up (make it before
+ * any stream capture); calls whose kernels overlap on the GPU race on the shared array.  No counterpart in
+ * the reference: it is an addition of this library. */
+int gt_lp_product_noalloc(gt_geometry* g, int32_t n_cols, const void* x_device, void* y_device, void* stream);
+
 /* Per-kernel-family timing of the solves on this geometry, by CUDA events on the launch stream.
  * names == NULL and cap == -2: reset and switch timing on; cap == -1: switch it off.  Otherwise fills
  * names (comma separated), ms (milliseconds), bytes (algorithmic bytes moved) and launches (timed
