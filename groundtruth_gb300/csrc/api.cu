@@ -137,6 +137,7 @@ struct Scope {
 struct Orient {
     int n0, n1, P0, P1, di, dj;
     int64_t off;
+    int rows[2] = {0, 0}, bt[2] = {0, 0};   // tuned launch shapes per precision (0: not tuned)
     float* spec32;
     double* spec64;
     c32 *tw0_32, *tw1_32;
@@ -155,12 +156,15 @@ struct Workspace {
     void *V = nullptr, *w = nullptr, *z = nullptr, *T = nullptr, *zfac = nullptr, *uvec = nullptr;
     c64* partial = nullptr;
     GmresState st{};
-    int *slot_col = nullptr, *slot_op = nullptr, *g_col0 = nullptr, *g_ncol = nullptr, *g_op = nullptr, *col_op = nullptr;
+    int *slot_col = nullptr, *slot_op = nullptr, *g_ptr = nullptr, *g_slot = nullptr, *g_op = nullptr, *col_op = nullptr;
+    int* act = nullptr;
+    int* act_host = nullptr;
     int* flag_dev = nullptr;
     int* flag_host = nullptr;
     int* its_col = nullptr;
     ~Workspace() {
         if (flag_host) cudaFreeHost(flag_host);
+        if (act_host) cudaFreeHost(act_host);
     }
 };
 
@@ -224,13 +228,50 @@ static bool good_fft_size(int P) {
     return P >= 8 && (P & (P - 1)) == 0;
 }
 
+// The FFT passes' launch shapes (rows per row-pass block, columns per column-pass block), chosen once per
+// orientation and precision by timing each candidate on the call's own data (two runs each, CUDA events).
+template <typename R>
+static void tune_lp(Orient& o, LpArgs<R> a, int pr, cudaStream_t st) {
+    static const int cand_rows[] = {1, 2, 4, 8, 16};
+    static const int cand_bt[] = {1, 2, 4, 8};
+    cudaEvent_t e0, e1;
+    GT_CUDA(cudaEventCreate(&e0));
+    GT_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int br = 4, bb = 2;
+    for (int r : cand_rows)
+        for (int b : cand_bt) {
+            a.rows = r;
+            a.bt = b;
+            int rr, bb2;
+            lp_shapes<R>(a, &rr, &bb2);
+            if (rr != r || bb2 != b) continue;   // not a legal shape here
+            launch_lp<R>(a, st);
+            GT_CUDA(cudaEventRecord(e0, st));
+            launch_lp<R>(a, st);
+            GT_CUDA(cudaEventRecord(e1, st));
+            GT_CUDA(cudaEventSynchronize(e1));
+            float ms = 0;
+            GT_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) {
+                best = ms;
+                br = r;
+                bb = b;
+            }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    o.rows[pr] = br;
+    o.bt[pr] = bb;
+}
+
 // System product out = K x (mode 0), rhs - K x (1), or the L_p product of the strips (2).
 template <typename R>
 static void matvec(gt_geometry* G, gt_operators* ops, const cx<R>* x, const cx<R>* rhs, cx<R>* out, int64_t ld, int ncol,
-                   const int* col_op, int mode, cx<R>* T, cudaStream_t st) {
+                   const int* col_op, int mode, cx<R>* T, cudaStream_t st, const int* col_list = nullptr) {
     Profiler* P = &G->prof;
     for (int k = 0; k < 2; ++k) {
-        const Orient& o = G->o[k];
+        Orient& o = G->o[k];
         if ((int64_t)o.n0 * o.n1 == 0) continue;
         LpArgs<R> a{};
         a.x = x;
@@ -258,7 +299,11 @@ static void matvec(gt_geometry* G, gt_operators* ops, const cx<R>* x, const cx<R
         a.omega = ops->omega;
         a.zs = ops->zs;
         a.mode = mode;
-        a.col_list = nullptr;
+        a.col_list = col_list;
+        const int pr = sizeof(R) == 8;
+        if (G->o[k].rows[pr] == 0 && ncol >= 8 && mode != 2) tune_lp<R>(G->o[k], a, pr, st);
+        a.rows = o.rows[pr];
+        a.bt = o.bt[pr];
         // algorithmic bytes: x, V and out over the strips, the intermediate grid written by pass A, read and
         // written by pass B, read by pass C, the spectrum once per column group of pass B
         const double es = sizeof(cx<R>), plane = (double)a.S * o.n0 * o.n1;
@@ -271,14 +316,15 @@ static void matvec(gt_geometry* G, gt_operators* ops, const cx<R>* x, const cx<R
         const double nXY = (double)(G->geo.off_c - G->geo.off_x);
         Scope s(P, sizeof(R) == 4 ? "tail_f32" : "tail_f64", st,
                 ncol * (double)sizeof(cx<R>) * (2.0 * (G->geo.n - nXY) + nXY));
-        launch_tail<R>(G->geo, x, rhs, out, ld, ncol, col_op, ops->zcap, ops->zbr, mode, st);
+        launch_tail<R>(G->geo, x, rhs, out, ld, ncol, col_op, ops->zcap, ops->zbr, mode, col_list, st);
     }
 }
 
 // out = M^-1 r for nslot slots whose vectors are ldr apart (inputs) and ldo apart (outputs)
 template <typename R>
 static void precond(gt_geometry* G, gt_operators* ops, const cx<R>* r, int64_t ldr, cx<R>* out, int64_t ldo, int nslot,
-                    const int* slot_op, const Groups& grp, int gmax, cx<R>* zfac, cx<R>* uvec, cudaStream_t st) {
+                    const int* slot_op, const Groups& grp, int gmax, cx<R>* zfac, cx<R>* uvec, cudaStream_t st,
+                    const int* col_list = nullptr) {
     Profiler* P = &G->prof;
     const double es = sizeof(cx<R>), n = (double)G->geo.n, nfac = (double)G->F.nfac;
     const double nodes = (double)G->geo.S * G->geo.nx * G->geo.ny, nXYC = (double)(G->geo.off_b - G->geo.off_x);
@@ -286,7 +332,7 @@ static void precond(gt_geometry* G, gt_operators* ops, const cx<R>* r, int64_t l
     const double panel = (double)grp.ngroup * es * G->F.panel_total;
     {
         Scope s(P, "pc_node", st, nslot * es * (nXYC + nodes + nfac));
-        launch_pc_node<R>(G->geo, r, ldr, zfac, nslot, slot_op, ops->tab, st);
+        launch_pc_node<R>(G->geo, r, ldr, zfac, nslot, slot_op, ops->tab, col_list, st);
     }
     const cx<R>* pan = panel_of<R>(ops);
     const int nlev = (int)G->level_ptr.size() - 1;
@@ -306,29 +352,31 @@ static void precond(gt_geometry* G, gt_operators* ops, const cx<R>* r, int64_t l
     }
     {
         Scope s(P, "pc_strip", st, nslot * es * (2 * n + nfac));
-        launch_pc_strip<R>(G->geo, r, ldr, zfac, out, ldo, nslot, slot_op, ops->tab, st);
+        launch_pc_strip<R>(G->geo, r, ldr, zfac, out, ldo, nslot, slot_op, ops->tab, col_list, st);
     }
 }
 
 static int group_max(const gt_geometry* G, size_t elem) {
-    int g = 8;
-    while (g > 1 && (size_t)G->max_nf * g * elem > 200 * 1024) g /= 2;
-    return g;
+    // the triangular-solve kernels hold a front's rows for 8 columns plus a 32 x 32 block in shared memory
+    if ((size_t)(32 * 32 + (size_t)G->max_nf * 8) * elem > 220 * 1024)
+        throw Invalid("a front is too large for the triangular-solve kernels' shared memory");
+    return 8;
 }
 
-// slots sorted by operator -> groups of <= gmax consecutive slots sharing one
-static void make_groups(const std::vector<int>& slot_op, int gmax, std::vector<int>& c0, std::vector<int>& nc,
-                        std::vector<int>& op) {
-    c0.clear();
-    nc.clear();
+// the listed slots (sorted by operator) -> groups of <= gmax slots sharing one operator:
+// group g holds gslot[gptr[g] .. gptr[g+1])
+static void make_groups(const std::vector<int>& slots, const std::vector<int>& slot_op, int gmax, std::vector<int>& gptr,
+                        std::vector<int>& gslot, std::vector<int>& op) {
+    gptr.assign(1, 0);
+    gslot.clear();
     op.clear();
-    int n = (int)slot_op.size();
+    int n = (int)slots.size();
     for (int s = 0; s < n;) {
         int e = s;
-        while (e < n && slot_op[e] == slot_op[s] && e - s < gmax) ++e;
-        c0.push_back(s);
-        nc.push_back(e - s);
-        op.push_back(slot_op[s]);
+        while (e < n && slot_op[slots[e]] == slot_op[slots[s]] && e - s < gmax) ++e;
+        for (int q = s; q < e; ++q) gslot.push_back(slots[q]);
+        gptr.push_back((int)gslot.size());
+        op.push_back(slot_op[slots[s]]);
         s = e;
     }
 }
@@ -386,9 +434,11 @@ static void ensure_ws(gt_geometry* G, int ncol, int m, int prec) {
     s.resid_est = p.alloc<double>(ncol);
     W.slot_col = p.alloc<int>(ncol);
     W.slot_op = p.alloc<int>(ncol);
-    W.g_col0 = p.alloc<int>(ncol);
-    W.g_ncol = p.alloc<int>(ncol);
+    W.g_ptr = p.alloc<int>(ncol + 1);
+    W.g_slot = p.alloc<int>(ncol);
     W.g_op = p.alloc<int>(ncol);
+    W.act = p.alloc<int>(ncol);
+    GT_CUDA(cudaMallocHost(&W.act_host, ncol * sizeof(int)));
     W.col_op = p.alloc<int>(ncol);
     W.flag_dev = p.alloc<int>(1);
     W.its_col = p.alloc<int>(ncol);
@@ -432,7 +482,15 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
     cx<R>* zfac = static_cast<cx<R>*>(W.zfac);
     cx<R>* uvec = static_cast<cx<R>*>(W.uvec);
     const int64_t lds = (int64_t)(m + 1) * n;
-    std::vector<int> slot_col, slot_op, c0, nc, gop;
+    std::vector<int> slot_col, slot_op, gptr, gslot, gop, act;
+    auto upload_groups = [&](const std::vector<int>& slots) {
+        make_groups(slots, slot_op, gmax, gptr, gslot, gop);
+        GT_CUDA(cudaMemcpyAsync(W.act, slots.data(), slots.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        GT_CUDA(cudaMemcpyAsync(W.g_ptr, gptr.data(), gptr.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        GT_CUDA(cudaMemcpyAsync(W.g_slot, gslot.data(), gslot.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        GT_CUDA(cudaMemcpyAsync(W.g_op, gop.data(), gop.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        return Groups{(int)gop.size(), W.g_ptr, W.g_slot, W.g_op};
+    };
     for (int outer = 0; outer < o.max_outer; ++outer) {
         slot_col.clear();
         for (int c = 0; c < ncol; ++c)
@@ -442,20 +500,19 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
         const int ns = (int)slot_col.size();
         slot_op.resize(ns);
         for (int s = 0; s < ns; ++s) slot_op[s] = h_col_op[slot_col[s]];
-        make_groups(slot_op, gmax, c0, nc, gop);
         GT_CUDA(cudaMemcpyAsync(W.slot_col, slot_col.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
         GT_CUDA(cudaMemcpyAsync(W.slot_op, slot_op.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
-        GT_CUDA(cudaMemcpyAsync(W.g_col0, c0.data(), c0.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-        GT_CUDA(cudaMemcpyAsync(W.g_ncol, nc.data(), nc.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-        GT_CUDA(cudaMemcpyAsync(W.g_op, gop.data(), gop.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        act.resize(ns);
+        for (int q = 0; q < ns; ++q) act[q] = q;
         std::vector<int> its_slot(ns);
         for (int s = 0; s < ns; ++s) its_slot[s] = h_its[slot_col[s]];
         GmresState S = W.st;
         S.nslot = ns;
         S.m = m;
         S.max_its = o.max_its;
+        S.reorth_ratio = o.reorth;
         GT_CUDA(cudaMemcpyAsync(S.its_total, its_slot.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
-        Groups grp{(int)c0.size(), W.g_col0, W.g_ncol, W.g_op};
+        Groups grp = upload_groups(act);
         GmresStateT<R> ST{ns, S.active, S.inv_hn, V, w, n, lds};
         {
             Scope sc(P, "gmres_small", st);
@@ -464,8 +521,10 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
         }
         int jdone = 0;
         for (int j = 0; j < m; ++j) {
-            precond<R>(G, ops, V + (int64_t)j * n, lds, z, n, ns, W.slot_op, grp, gmax, zfac, uvec, st);
-            matvec<R>(G, ops, z, nullptr, w, n, ns, W.slot_op, 0, T, st);
+            // the products run on the slots still iterating in this cycle (W.act, grp)
+            const int na = (int)act.size();
+            precond<R>(G, ops, V + (int64_t)j * n, lds, z, n, na, W.slot_op, grp, gmax, zfac, uvec, st, W.act);
+            matvec<R>(G, ops, z, nullptr, w, n, na, W.slot_op, 0, T, st, W.act);
             {
                 // classical Gram-Schmidt: the j+1 basis vectors read twice, w read twice and written once
                 Scope sc(P, sizeof(R) == 4 ? "gs_f32" : "gs_f64", st, (double)ns * sizeof(cx<R>) * n * (2.0 * (j + 1) + 3));
@@ -486,12 +545,18 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
                 Scope sc(P, "gmres_small", st);
                 launch_givens(S, j, st);
                 if (j + 1 < m) launch_scale<R>(ST, j, n, st);
-                launch_any_active(S.active, ns, W.flag_dev, st);
             }
-            GT_CUDA(cudaMemcpyAsync(W.flag_host, W.flag_dev, sizeof(int), cudaMemcpyDeviceToHost, st));
+            GT_CUDA(cudaMemcpyAsync(W.act_host, S.active, ns * sizeof(int), cudaMemcpyDeviceToHost, st));
             GT_CUDA(cudaStreamSynchronize(st));
             jdone = j + 1;
-            if (!*W.flag_host) break;
+            std::vector<int> still;
+            for (int q : act)
+                if (W.act_host[q]) still.push_back(q);
+            if (still.empty()) break;
+            if (still.size() < act.size()) {
+                act.swap(still);
+                grp = upload_groups(act);
+            }
         }
         // the cycle's correction: x += rho * M^-1 (V y)
         {
@@ -503,7 +568,10 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
             Scope sc(P, "combine", st, (double)ns * sizeof(cx<R>) * n * (jdone + 2.0));
             launch_update<R>(V, n, lds, jdone, S.y, S.ldh, w, n, n, ns, nullptr, nullptr, nch, 1, st);
         }
-        precond<R>(G, ops, w, n, z, n, ns, W.slot_op, grp, gmax, zfac, uvec, st);
+        act.resize(ns);
+        for (int q = 0; q < ns; ++q) act[q] = q;
+        grp = upload_groups(act);
+        precond<R>(G, ops, w, n, z, n, ns, W.slot_op, grp, gmax, zfac, uvec, st, W.act);
         {
             Scope sc(P, "refine", st, (double)ns * n * (32.0 + sizeof(cx<R>)));
             launch_refine<R>(W.x64, n, z, n, W.slot_col, W.rho, n, ns, st);
@@ -901,13 +969,14 @@ int gt_apply(gt_geometry* G, gt_operators* ops, int32_t kind, int32_t precision,
             cx<R>* T = tmp.alloc<cx<R>>((size_t)n_cols * G->maxT);
             matvec<R>(G, ops, xi, nullptr, yo, n, n_cols, d_op, kind == 0 ? 0 : 2, T, st);
         } else {
-            std::vector<int> c0, ncv, gop;
+            std::vector<int> gptr, gslot, gop, all(n_cols);
+            for (int c = 0; c < n_cols; ++c) all[c] = c;
             const int gmax = group_max(G, sizeof(cx<R>));
-            make_groups(h_op, gmax, c0, ncv, gop);
-            int* g0 = tmp.upload(c0.data(), c0.size());
-            int* g1 = tmp.upload(ncv.data(), ncv.size());
+            make_groups(all, h_op, gmax, gptr, gslot, gop);
+            int* g0 = tmp.upload(gptr.data(), gptr.size());
+            int* g1 = tmp.upload(gslot.data(), gslot.size());
             int* g2 = tmp.upload(gop.data(), gop.size());
-            Groups grp{(int)c0.size(), g0, g1, g2};
+            Groups grp{(int)gop.size(), g0, g1, g2};
             cx<R>* zf = tmp.alloc<cx<R>>((size_t)n_cols * G->F.nfac);
             cx<R>* uv = tmp.alloc<cx<R>>((size_t)n_cols * std::max<int64_t>(G->F.vec_total, 1));
             precond<R>(G, ops, xi, n, yo, n, n_cols, d_op, grp, gmax, zf, uv, st);

@@ -115,22 +115,41 @@ void launch_panel_to32(const c64* p64, c32* p32, int64_t n, cudaStream_t st) {
 }
 
 // ------------------------------------------------------------------------------------------ solves
-// z: [col][nfac] in factor order; uvec: [col][vec_total] update vectors; w in shared memory [nf][gc]
+// z: [col][nfac] in factor order; uvec: [col][vec_total] update vectors.  Shared memory: w [GMAXC][ldw] (the
+// front's rows for each of the group's columns, column-major so that consecutive threads touch consecutive
+// rows) and the current 32 x 32 diagonal block of the panel.  The own block is processed in blocks of 32
+// columns: the diagonal block by one warp per column, warp-synchronously (the lanes hold the block's 32
+// rows); the rest of the front by sweeps in which every panel element is read once, coalesced, with the
+// 32 loads of a block row issued back to back.
+constexpr int GMAXC = 8;
+constexpr int TB = 32;
+
 template <typename R>
-__global__ void fwd_level_kernel(Fronts F, const int64_t* __restrict__ front_list, const cx<R>* __restrict__ panel,
-                                 cx<R>* __restrict__ z, cx<R>* __restrict__ uvec, Groups G) {
+__device__ __forceinline__ void load_diag(cx<R>* Dsm, const cx<R>* __restrict__ L, int nf, int k0, int kb) {
+    for (int q = threadIdx.x; q < TB * TB; q += blockDim.x) {
+        int c = q / TB, r = q - c * TB;                 // column c, row r of the block
+        Dsm[q] = (c < kb && r < kb) ? L[(int64_t)(k0 + c) * nf + k0 + r] : zero<R>();
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(1024) fwd_level_kernel(Fronts F, const int64_t* __restrict__ front_list,
+                                                         const cx<R>* __restrict__ panel, cx<R>* __restrict__ z,
+                                                         cx<R>* __restrict__ uvec, Groups G, int ldw) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    cx<R>* w = reinterpret_cast<cx<R>*>(smem_raw);
+    cx<R>* Dsm = reinterpret_cast<cx<R>*>(smem_raw);
+    cx<R>* w = Dsm + TB * TB;
     const int f = (int)front_list[blockIdx.x];
     const int g = blockIdx.y;
-    const int col0 = G.col0[g], gc = G.ncol[g], op = G.op[g];
+    const int* gs = G.gslot + G.gptr[g];
+    const int gc = G.gptr[g + 1] - G.gptr[g], op = G.op[g];
     const int nown = (int)F.nown[f], nbnd = (int)F.nbnd[f], nf = nown + nbnd;
     const int64_t own0 = F.own_start[f];
-    const cx<R>* L = panel + (int64_t)op * F.panel_total + F.panel_off[f];
-    const int tid = threadIdx.x, nth = blockDim.x;
-    for (int q = tid; q < nf * gc; q += nth) {
-        int r = q / gc, c = q - r * gc;
-        w[q] = r < nown ? z[(int64_t)(col0 + c) * F.nfac + own0 + r] : zero<R>();
+    const cx<R>* __restrict__ L = panel + (int64_t)op * F.panel_total + F.panel_off[f];
+    const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, warp = tid >> 5;
+    for (int q = tid; q < gc * nf; q += nth) {
+        int c = q / nf, r = q - c * nf;
+        w[c * ldw + r] = r < nown ? z[(int64_t)gs[c] * F.nfac + own0 + r] : zero<R>();
     }
     __syncthreads();
     for (int64_t ci = F.child_ptr[f]; ci < F.child_ptr[f + 1]; ++ci) {
@@ -138,71 +157,128 @@ __global__ void fwd_level_kernel(Fronts F, const int64_t* __restrict__ front_lis
         const int nb = (int)F.nbnd[ch];
         const int64_t* map = F.cmap_idx + F.cmap_ptr[ci];
         for (int q = tid; q < nb * gc; q += nth) {
-            int i = q / gc, c = q - i * gc;
-            w[map[i] * gc + c] += uvec[(int64_t)(col0 + c) * F.vec_total + F.vec_off[ch] + i];
+            int c = q / nb, i = q - c * nb;
+            w[c * ldw + map[i]] += uvec[(int64_t)gs[c] * F.vec_total + F.vec_off[ch] + i];
         }
         __syncthreads();
     }
-    for (int k = 0; k < nown; ++k) {
-        const cx<R>* Lk = L + (int64_t)k * nf;
-        const int rows = nf - k - 1;
-        for (int q = tid; q < rows * gc; q += nth) {
-            int i = k + 1 + q / gc, c = q % gc;
-            w[i * gc + c] -= Lk[i] * w[k * gc + c];
+    for (int k0 = 0; k0 < nown; k0 += TB) {
+        const int kb = min(TB, nown - k0);
+        load_diag<R>(Dsm, L, nf, k0, kb);
+        __syncthreads();
+        if (warp < gc) {                                 // unit lower triangular solve of the block
+            cx<R>* wc = w + warp * ldw + k0;
+            cx<R> v = lane < kb ? wc[lane] : zero<R>();
+            for (int kk = 0; kk < kb - 1; ++kk) {
+                cx<R> zk = mk<R>(__shfl_sync(0xffffffffu, v.re, kk), __shfl_sync(0xffffffffu, v.im, kk));
+                if (lane > kk && lane < kb) v -= Dsm[kk * TB + lane] * zk;
+            }
+            if (lane < kb) wc[lane] = v;
+        }
+        __syncthreads();
+        // rows below the block: w[c][i] -= sum_kk L[i, k0+kk] z[c][k0+kk], one thread per row
+        for (int i = k0 + kb + tid; i < nf; i += nth) {
+            cx<R> acc[GMAXC];
+#pragma unroll
+            for (int c = 0; c < GMAXC; ++c) acc[c] = zero<R>();
+            const cx<R>* Li = L + (int64_t)k0 * nf + i;
+            if (kb == TB) {
+#pragma unroll
+                for (int k8 = 0; k8 < TB; k8 += 8) {
+                    cx<R> l[8];
+#pragma unroll
+                    for (int kk = 0; kk < 8; ++kk) l[kk] = Li[(int64_t)(k8 + kk) * nf];
+#pragma unroll
+                    for (int kk = 0; kk < 8; ++kk)
+#pragma unroll
+                        for (int c = 0; c < GMAXC; ++c)
+                            if (c < gc) acc[c] += l[kk] * w[c * ldw + k0 + k8 + kk];
+                }
+            } else {
+                for (int kk = 0; kk < kb; ++kk) {
+                    const cx<R> lv = Li[(int64_t)kk * nf];
+#pragma unroll
+                    for (int c = 0; c < GMAXC; ++c)
+                        if (c < gc) acc[c] += lv * w[c * ldw + k0 + kk];
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < GMAXC; ++c)
+                if (c < gc) w[c * ldw + i] -= acc[c];
         }
         __syncthreads();
     }
-    for (int q = tid; q < nf * gc; q += nth) {
-        int r = q / gc, c = q - r * gc;
-        if (r < nown) z[(int64_t)(col0 + c) * F.nfac + own0 + r] = cdiv(w[q], L[(int64_t)r * nf + r]);
-        else uvec[(int64_t)(col0 + c) * F.vec_total + F.vec_off[f] + (r - nown)] = w[q];
+    for (int q = tid; q < gc * nf; q += nth) {
+        int c = q / nf, r = q - c * nf;
+        if (r < nown) z[(int64_t)gs[c] * F.nfac + own0 + r] = cdiv(w[c * ldw + r], L[(int64_t)r * nf + r]);
+        else uvec[(int64_t)gs[c] * F.vec_total + F.vec_off[f] + (r - nown)] = w[c * ldw + r];
     }
 }
 
 template <typename R>
-__global__ void bwd_level_kernel(Fronts F, const int64_t* __restrict__ front_list, const cx<R>* __restrict__ panel,
-                                 cx<R>* __restrict__ z, Groups G) {
+__global__ void __launch_bounds__(1024) bwd_level_kernel(Fronts F, const int64_t* __restrict__ front_list,
+                                                         const cx<R>* __restrict__ panel, cx<R>* __restrict__ z, Groups G,
+                                                         int ldw) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    cx<R>* w = reinterpret_cast<cx<R>*>(smem_raw);
+    cx<R>* Dsm = reinterpret_cast<cx<R>*>(smem_raw);
+    cx<R>* w = Dsm + TB * TB;
     const int f = (int)front_list[blockIdx.x];
     const int g = blockIdx.y;
-    const int col0 = G.col0[g], gc = G.ncol[g], op = G.op[g];
+    const int* gs = G.gslot + G.gptr[g];
+    const int gc = G.gptr[g + 1] - G.gptr[g], op = G.op[g];
     const int nown = (int)F.nown[f], nbnd = (int)F.nbnd[f], nf = nown + nbnd;
     const int64_t own0 = F.own_start[f];
     const int64_t* bnd = F.bnd_idx + F.bnd_ptr[f];
-    const cx<R>* L = panel + (int64_t)op * F.panel_total + F.panel_off[f];
-    const int tid = threadIdx.x, nth = blockDim.x;
-    for (int q = tid; q < nf * gc; q += nth) {
-        int r = q / gc, c = q - r * gc;
-        int64_t idx = r < nown ? own0 + r : bnd[r - nown];
-        w[q] = z[(int64_t)(col0 + c) * F.nfac + idx];
+    const cx<R>* __restrict__ L = panel + (int64_t)op * F.panel_total + F.panel_off[f];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
+    for (int q = tid; q < gc * nf; q += blockDim.x) {
+        int c = q / nf, r = q - c * nf;
+        w[c * ldw + r] = z[(int64_t)gs[c] * F.nfac + (r < nown ? own0 + r : bnd[r - nown])];
     }
     __syncthreads();
-    // boundary part: w_k -= sum_i L[nown+i, k] y_bnd[i], one warp per (k, column)
-    const int warp = tid >> 5, lane = tid & 31, nwarp = nth >> 5;
-    for (int q = warp; q < nown * gc; q += nwarp) {
-        int k = q / gc, c = q - k * gc;
-        const cx<R>* Lk = L + (int64_t)k * nf + nown;
-        cx<R> acc = zero<R>();
-        for (int i = lane; i < nbnd; i += 32) acc += Lk[i] * w[(nown + i) * gc + c];
-        for (int o = 16; o > 0; o >>= 1) {
-            acc.re += __shfl_xor_sync(0xffffffffu, acc.re, o);
-            acc.im += __shfl_xor_sync(0xffffffffu, acc.im, o);
+    const int nblk = (nown + TB - 1) / TB;
+    for (int b = nblk - 1; b >= 0; --b) {
+        const int k0 = b * TB, kb = min(TB, nown - k0), k1 = k0 + kb;
+        // w[c][k] -= sum_{i >= k1} L[i, k] y[c][i] for the block's columns: one warp per column k
+        for (int kk = warp; kk < kb; kk += nwarp) {
+            const cx<R>* Lk = L + (int64_t)(k0 + kk) * nf;
+            cx<R> acc[GMAXC];
+#pragma unroll
+            for (int c = 0; c < GMAXC; ++c) acc[c] = zero<R>();
+#pragma unroll 4
+            for (int i = k1 + lane; i < nf; i += 32) {
+                const cx<R> l = Lk[i];
+#pragma unroll
+                for (int c = 0; c < GMAXC; ++c)
+                    if (c < gc) acc[c] += l * w[c * ldw + i];
+            }
+#pragma unroll
+            for (int c = 0; c < GMAXC; ++c) {
+                if (c >= gc) break;
+                R re = acc[c].re, im = acc[c].im;
+                for (int o = 16; o > 0; o >>= 1) {
+                    re += __shfl_xor_sync(0xffffffffu, re, o);
+                    im += __shfl_xor_sync(0xffffffffu, im, o);
+                }
+                if (lane == 0) w[c * ldw + k0 + kk] -= mk<R>(re, im);
+            }
         }
-        if (lane == 0) w[k * gc + c] -= acc;
-    }
-    __syncthreads();
-    // own block, k descending: y_k final, then w_k' -= L[k, k'] y_k for k' < k
-    for (int k = nown - 1; k > 0; --k) {
-        for (int q = tid; q < k * gc; q += nth) {
-            int kk = q / gc, c = q - kk * gc;
-            w[kk * gc + c] -= L[(int64_t)kk * nf + k] * w[k * gc + c];
+        load_diag<R>(Dsm, L, nf, k0, kb);
+        __syncthreads();
+        if (warp < gc) {                                 // unit upper (L^T) solve of the block from the bottom
+            cx<R>* wc = w + warp * ldw + k0;
+            cx<R> v = lane < kb ? wc[lane] : zero<R>();
+            for (int kk = kb - 1; kk > 0; --kk) {
+                cx<R> yk = mk<R>(__shfl_sync(0xffffffffu, v.re, kk), __shfl_sync(0xffffffffu, v.im, kk));
+                if (lane < kk) v -= Dsm[lane * TB + kk] * yk;    // L[k0+kk, k0+lane]
+            }
+            if (lane < kb) wc[lane] = v;
         }
         __syncthreads();
     }
-    for (int q = tid; q < nown * gc; q += nth) {
-        int r = q / gc, c = q - r * gc;
-        z[(int64_t)(col0 + c) * F.nfac + own0 + r] = w[q];
+    for (int q = tid; q < gc * nown; q += blockDim.x) {
+        int c = q / nown, r = q - c * nown;
+        z[(int64_t)gs[c] * F.nfac + own0 + r] = w[c * ldw + r];
     }
 }
 
@@ -211,23 +287,27 @@ static void smem_attr(const void* fn, size_t bytes) {
     if (bytes > 48 * 1024) GT_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
 }
 
+static int solve_threads(int max_nf) { return max_nf > 512 ? 1024 : max_nf > 192 ? 512 : 256; }
+
 template <typename R>
 void launch_fwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, const cx<R>* panel,
                       cx<R>* z, cx<R>* uvec, const Groups& G, int gmax, cudaStream_t st) {
-    size_t sm = (size_t)max_nf * gmax * sizeof(cx<R>);
+    if (gmax > GMAXC) throw CudaError{cudaErrorInvalidValue, "column group larger than the solve kernels take"};
+    const int ldw = max_nf | 1;
+    size_t sm = (size_t)(TB * TB + (size_t)ldw * GMAXC) * sizeof(cx<R>);
     smem_attr<R>((const void*)fwd_level_kernel<R>, sm);
-    int threads = max_nf * gmax >= 512 ? 512 : 256;
-    fwd_level_kernel<R><<<dim3(nf_level, G.ngroup), threads, sm, st>>>(F, front_list, panel, z, uvec, G);
+    fwd_level_kernel<R><<<dim3(nf_level, G.ngroup), solve_threads(max_nf), sm, st>>>(F, front_list, panel, z, uvec, G, ldw);
     GT_LAUNCH_CHECK();
 }
 
 template <typename R>
 void launch_bwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, const cx<R>* panel,
                       cx<R>* z, const Groups& G, int gmax, cudaStream_t st) {
-    size_t sm = (size_t)max_nf * gmax * sizeof(cx<R>);
+    if (gmax > GMAXC) throw CudaError{cudaErrorInvalidValue, "column group larger than the solve kernels take"};
+    const int ldw = max_nf | 1;
+    size_t sm = (size_t)(TB * TB + (size_t)ldw * GMAXC) * sizeof(cx<R>);
     smem_attr<R>((const void*)bwd_level_kernel<R>, sm);
-    int threads = max_nf * gmax >= 512 ? 512 : 256;
-    bwd_level_kernel<R><<<dim3(nf_level, G.ngroup), threads, sm, st>>>(F, front_list, panel, z, G);
+    bwd_level_kernel<R><<<dim3(nf_level, G.ngroup), solve_threads(max_nf), sm, st>>>(F, front_list, panel, z, G, ldw);
     GT_LAUNCH_CHECK();
 }
 

@@ -169,7 +169,7 @@ __global__ void dgks_kernel(GmresState s, int j) {
     if (s.active[slot]) {
         double before = sqrt(s.hvec[(int64_t)slot * s.ldh + j + 1].re);
         double after = sqrt(s.hn2[slot].re);
-        re = after < 0.7 * before;
+        re = after < s.reorth_ratio * before;
     }
     s.reorth[slot] = re;
 }

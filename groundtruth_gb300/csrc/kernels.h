@@ -36,23 +36,27 @@ template <typename R> struct LpArgs {
     const c64* zs;
     int mode;
     const int* col_list;
+    int rows;              // rows per block of the row passes (0: default)
+    int bt;                // columns per block of the column pass (0: default)
 };
 
 template <typename R> void launch_lp(const LpArgs<R>& a, cudaStream_t st);
+// the launch shapes launch_lp would use for these arguments
+template <typename R> void lp_shapes(const LpArgs<R>& a, int* rows, int* bt);
 
 // capacitance / branch / node rows of the system product (mode 0: K x, 1: rhs - K x); also zeroes the
 // padding between segments
 template <typename R>
 void launch_tail(const Geo& g, const cx<R>* x, const cx<R>* rhs, cx<R>* out, int64_t ld, int ncol, const int* col_op,
-                 const c64* zcap, const c64* zbr, int mode, cudaStream_t st);
+                 const c64* zcap, const c64* zbr, int mode, const int* col_list, cudaStream_t st);
 
 // preconditioner: s = r_V - Ar^T D^-1 r_1 into factor order; then out = [D^-1 (r_1 + Ar y); y]
 template <typename R>
 void launch_pc_node(const Geo& g, const cx<R>* r, int64_t ld, cx<R>* s_fac, int ncol, const int* col_op,
-                    const c64* tab, cudaStream_t st);
+                    const c64* tab, const int* col_list, cudaStream_t st);
 template <typename R>
 void launch_pc_strip(const Geo& g, const cx<R>* r, int64_t ldr, const cx<R>* y_fac, cx<R>* out, int64_t ldo, int ncol,
-                     const int* col_op, const c64* tab, cudaStream_t st);
+                     const int* col_op, const c64* tab, const int* col_list, cudaStream_t st);
 
 // compact <-> dense
 void launch_scatter(const int64_t* c2d, int64_t ncomp, const c64* in, int64_t ldin, c64* out, int64_t ldout, int ncol,
@@ -92,8 +96,8 @@ void launch_panel_to32(const c64* p64, c32* p32, int64_t n, cudaStream_t st);
 // triangular solves, per level; groups of columns sharing an operator
 struct Groups {
     int ngroup;
-    const int* col0;
-    const int* ncol;
+    const int* gptr;       // group g: columns gslot[gptr[g] .. gptr[g+1])
+    const int* gslot;
     const int* op;
 };
 template <typename R>

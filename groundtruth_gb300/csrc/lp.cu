@@ -159,20 +159,26 @@ static void set_smem(const void* fn, size_t bytes) {
 }
 
 template <typename R>
-void launch_lp(const LpArgs<R>& a, cudaStream_t st) {
-    // pass A / C: rows per block so that the transposed stores are >= 128 B per row segment when possible
-    const int teamA = a.P1 / 8;
-    int rows = (sizeof(R) == 4 ? 16 : 8);
+void lp_shapes(const LpArgs<R>& a, int* rows_out, int* bt_out) {
+    const int teamA = a.P1 / 8, teamB = a.P0 / 8;
+    int rows = a.rows > 0 ? a.rows : 4;
     while (rows > 1 && (rows * teamA > 1024 || (size_t)rows * (a.P1 + 1) * sizeof(cx<R>) > 160 * 1024)) rows /= 2;
+    int bt = a.bt > 0 ? a.bt : 2;
+    while (bt > 1 && (bt * a.S * teamB > 1024 || (size_t)bt * a.S * (a.P0 + 1) * sizeof(cx<R>) > 160 * 1024)) bt /= 2;
+    *rows_out = rows;
+    *bt_out = bt;
+}
+
+template <typename R>
+void launch_lp(const LpArgs<R>& a, cudaStream_t st) {
+    int rows, bt;
+    lp_shapes<R>(a, &rows, &bt);
+    const int teamA = a.P1 / 8, teamB = a.P0 / 8;
     size_t smA = (size_t)rows * (a.P1 + 1) * sizeof(cx<R>);
     dim3 gA(ceil_div(a.n0, rows), a.S, a.ncol);
     set_smem<R>((const void*)lp_pass_a<R>, smA);
     lp_pass_a<R><<<gA, rows * teamA, smA, st>>>(a.x, a.ld, a.off, a.S, a.n0, a.n1, a.P1, rows, a.tw1, a.T, a.col_list);
     GT_LAUNCH_CHECK();
-    const int teamB = a.P0 / 8;
-    int bt = 1;
-    while (bt < 8 && (bt * 2) * a.S * teamB <= 1024 && (size_t)(bt * 2) * a.S * (a.P0 + 1) * sizeof(cx<R>) <= 100 * 1024)
-        bt *= 2;
     size_t smB = (size_t)bt * a.S * (a.P0 + 1) * sizeof(cx<R>);
     dim3 gB(a.P1, ceil_div(a.ncol, bt));
     set_smem<R>((const void*)lp_pass_b<R>, smB);
@@ -187,5 +193,7 @@ void launch_lp(const LpArgs<R>& a, cudaStream_t st) {
 
 template void launch_lp<float>(const LpArgs<float>&, cudaStream_t);
 template void launch_lp<double>(const LpArgs<double>&, cudaStream_t);
+template void lp_shapes<float>(const LpArgs<float>&, int*, int*);
+template void lp_shapes<double>(const LpArgs<double>&, int*, int*);
 
 }  // namespace gt

@@ -6,6 +6,7 @@ namespace gt {
 
 struct GmresState {
     int nslot, m, ldh, max_its;
+    double reorth_ratio;
     c64* H;            // [slot][m][m+1] rotated Hessenberg columns
     double* cs;        // [slot][m]
     c64* sn;           // [slot][m]

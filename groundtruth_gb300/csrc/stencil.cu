@@ -46,8 +46,8 @@ __device__ __forceinline__ cx<R> load_or0(const cx<R>* p, bool ok) { return ok ?
 template <typename R>
 __global__ void tail_kernel(Geo g, const cx<R>* __restrict__ x, const cx<R>* __restrict__ rhs, cx<R>* __restrict__ out,
                             int64_t ld, const int* __restrict__ col_op, const c64* __restrict__ zcap,
-                            const c64* __restrict__ zbr, int mode) {
-    const int col = blockIdx.y;
+                            const c64* __restrict__ zbr, int mode, const int* __restrict__ col_list) {
+    const int col = col_list ? col_list[blockIdx.y] : blockIdx.y;
     const int op = col_op ? col_op[col] : 0;
     const int64_t nX = (int64_t)g.S * (g.nx - 1) * g.ny, nY = (int64_t)g.S * g.nx * (g.ny - 1);
     const cx<R>* xc = x + (int64_t)col * ld;
@@ -98,18 +98,18 @@ __global__ void tail_kernel(Geo g, const cx<R>* __restrict__ x, const cx<R>* __r
 
 template <typename R>
 void launch_tail(const Geo& g, const cx<R>* x, const cx<R>* rhs, cx<R>* out, int64_t ld, int ncol, const int* col_op,
-                 const c64* zcap, const c64* zbr, int mode, cudaStream_t st) {
+                 const c64* zcap, const c64* zbr, int mode, const int* col_list, cudaStream_t st) {
     int64_t items = g.n;
     int blocks = (int)std::min<int64_t>((items + 255) / 256, 4096);
-    tail_kernel<R><<<dim3(blocks, ncol), 256, 0, st>>>(g, x, rhs, out, ld, col_op, zcap, zbr, mode);
+    tail_kernel<R><<<dim3(blocks, ncol), 256, 0, st>>>(g, x, rhs, out, ld, col_op, zcap, zbr, mode, col_list);
     GT_LAUNCH_CHECK();
 }
 
 // s[perm[node]] = r_V[node] - (Ar^T D^-1 r_1)[node] for every kept node
 template <typename R>
 __global__ void pc_node_kernel(Geo g, const cx<R>* __restrict__ r, int64_t ld, cx<R>* __restrict__ s_fac,
-                               const int* __restrict__ col_op, const c64* __restrict__ tab) {
-    const int col = blockIdx.y;
+                               const int* __restrict__ col_op, const c64* __restrict__ tab, const int* __restrict__ col_list) {
+    const int col = col_list ? col_list[blockIdx.y] : blockIdx.y;
     const int op = col_op ? col_op[col] : 0;
     const c64* T = tab + (int64_t)op * g.ntab;
     const cx<R>* rc = r + (int64_t)col * ld;
@@ -164,10 +164,10 @@ __global__ void pc_node_kernel(Geo g, const cx<R>* __restrict__ r, int64_t ld, c
 
 template <typename R>
 void launch_pc_node(const Geo& g, const cx<R>* r, int64_t ld, cx<R>* s_fac, int ncol, const int* col_op, const c64* tab,
-                    cudaStream_t st) {
+                    const int* col_list, cudaStream_t st) {
     int64_t items = (int64_t)g.S * g.nx * g.ny;
     int blocks = (int)std::min<int64_t>((items + 255) / 256, 4096);
-    pc_node_kernel<R><<<dim3(blocks, ncol), 256, 0, st>>>(g, r, ld, s_fac, col_op, tab);
+    pc_node_kernel<R><<<dim3(blocks, ncol), 256, 0, st>>>(g, r, ld, s_fac, col_op, tab, col_list);
     GT_LAUNCH_CHECK();
 }
 
@@ -175,8 +175,8 @@ void launch_pc_node(const Geo& g, const cx<R>* r, int64_t ld, cx<R>* s_fac, int 
 template <typename R>
 __global__ void pc_strip_kernel(Geo g, const cx<R>* __restrict__ r, int64_t ldr, const cx<R>* __restrict__ y_fac,
                                 cx<R>* __restrict__ out, int64_t ldo, const int* __restrict__ col_op,
-                                const c64* __restrict__ tab) {
-    const int col = blockIdx.y;
+                                const c64* __restrict__ tab, const int* __restrict__ col_list) {
+    const int col = col_list ? col_list[blockIdx.y] : blockIdx.y;
     const int op = col_op ? col_op[col] : 0;
     const c64* T = tab + (int64_t)op * g.ntab;
     const cx<R>* rc = r + (int64_t)col * ldr;
@@ -231,9 +231,9 @@ __global__ void pc_strip_kernel(Geo g, const cx<R>* __restrict__ r, int64_t ldr,
 
 template <typename R>
 void launch_pc_strip(const Geo& g, const cx<R>* r, int64_t ldr, const cx<R>* y_fac, cx<R>* out, int64_t ldo, int ncol,
-                     const int* col_op, const c64* tab, cudaStream_t st) {
+                     const int* col_op, const c64* tab, const int* col_list, cudaStream_t st) {
     int blocks = (int)std::min<int64_t>((g.n + 255) / 256, 4096);
-    pc_strip_kernel<R><<<dim3(blocks, ncol), 256, 0, st>>>(g, r, ldr, y_fac, out, ldo, col_op, tab);
+    pc_strip_kernel<R><<<dim3(blocks, ncol), 256, 0, st>>>(g, r, ldr, y_fac, out, ldo, col_op, tab, col_list);
     GT_LAUNCH_CHECK();
 }
 
@@ -265,11 +265,11 @@ void launch_gather(const int64_t* c2d, int64_t ncomp, const c64* in, int64_t ldi
     GT_LAUNCH_CHECK();
 }
 
-template void launch_tail<float>(const Geo&, const c32*, const c32*, c32*, int64_t, int, const int*, const c64*, const c64*, int, cudaStream_t);
-template void launch_tail<double>(const Geo&, const c64*, const c64*, c64*, int64_t, int, const int*, const c64*, const c64*, int, cudaStream_t);
-template void launch_pc_node<float>(const Geo&, const c32*, int64_t, c32*, int, const int*, const c64*, cudaStream_t);
-template void launch_pc_node<double>(const Geo&, const c64*, int64_t, c64*, int, const int*, const c64*, cudaStream_t);
-template void launch_pc_strip<float>(const Geo&, const c32*, int64_t, const c32*, c32*, int64_t, int, const int*, const c64*, cudaStream_t);
-template void launch_pc_strip<double>(const Geo&, const c64*, int64_t, const c64*, c64*, int64_t, int, const int*, const c64*, cudaStream_t);
+template void launch_tail<float>(const Geo&, const c32*, const c32*, c32*, int64_t, int, const int*, const c64*, const c64*, int, const int*, cudaStream_t);
+template void launch_tail<double>(const Geo&, const c64*, const c64*, c64*, int64_t, int, const int*, const c64*, const c64*, int, const int*, cudaStream_t);
+template void launch_pc_node<float>(const Geo&, const c32*, int64_t, c32*, int, const int*, const c64*, const int*, cudaStream_t);
+template void launch_pc_node<double>(const Geo&, const c64*, int64_t, c64*, int, const int*, const c64*, const int*, cudaStream_t);
+template void launch_pc_strip<float>(const Geo&, const c32*, int64_t, const c32*, c32*, int64_t, int, const int*, const c64*, const int*, cudaStream_t);
+template void launch_pc_strip<double>(const Geo&, const c64*, int64_t, const c64*, c64*, int64_t, int, const int*, const c64*, const int*, cudaStream_t);
 
 }  // namespace gt

@@ -360,7 +360,8 @@ class PlaneStack:
         return np.concatenate([np.asarray(rhs_top, complex), np.asarray(J, float)[self.keep].astype(complex)])
 
     def solve_batch(self, freqs, rhs_tops, Js, tol: float = 1e-5, max_cycles: int = 8, guesses=None,
-                    restart: int = 50, max_its: int = 2000, inner_tol: float = 1e-5, precision: str = "mixed"):
+                    restart: int = 50, max_its: int = 2000, inner_tol: float = 1e-5, precision: str = "mixed",
+                    reorth: float = 0.7):
         """Many columns (frequency, right-hand side) in one device run: returns [(Ib, V, its, x)]."""
         from . import native
         ncol = len(freqs)
@@ -370,7 +371,7 @@ class PlaneStack:
         if guesses is not None and any(g for g in guesses if g):
             raise NotImplementedError("warm-start guesses are not supported yet")
         x, its, res, ok = native.solve(self.handle, ops, rhs, tol=tol, restart=restart, max_its=max_its,
-                                       inner_tol=inner_tol, precision=precision)
+                                       inner_tol=inner_tol, precision=precision, reorth=reorth)
         out = []
         for c in range(ncol):
             if not ok[c]:

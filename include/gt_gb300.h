@@ -83,6 +83,8 @@ typedef struct gt_solve_opts {
     double inner_tol;       /* relative residual reduction each inner FP32 cycle aims at */
     int32_t precision;      /* 0: FP32 inner GMRES + FP64 refinement, 1: all FP64 (plain drop-in) */
     int32_t max_outer;      /* refinement steps */
+    double reorth;          /* DGKS: re-orthogonalise when ||w|| fell below reorth x its norm before the first
+                               Gram-Schmidt pass (0.7: the reference's rule, peec.py:3156; 0: never) */
 } gt_solve_opts;
 
 /* Library version (major*10000 + minor*100 + patch). */
