@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--reorth", type=float, default=0.0,
                     help="DGKS re-orthogonalisation ratio (0.7: the reference rule; 0: none, the FP64 refinement guards the answer)")
     ap.add_argument("--max-its", type=int, default=4000)
+    ap.add_argument("--outer-k", type=int, default=8, help="FP64 outer GCR directions kept (1: plain refinement)")
     ap.add_argument("--nets", type=int, default=0, help="use only the first N nets (0: all)")
     ap.add_argument("--freqs", type=int, default=0, help="use only every k-th frequency (0: all)")
     return ap.parse_args()
@@ -202,7 +203,7 @@ def run_gpu(args):
     X = torch.zeros_like(B)
     st.handle.to_dense(rhs_c, B.data_ptr(), sptr)
     kw = dict(tol=args.tol, restart=args.restart, inner_tol=args.inner_tol, max_its=args.max_its, stream=sptr,
-              reorth=args.reorth)
+              reorth=args.reorth, outer_k=args.outer_k)
 
     def step():
         return st.handle.solve_device(obj, col_op, B.data_ptr(), X.data_ptr(), **kw)
@@ -274,7 +275,8 @@ def run_gpu(args):
         data = [st._freq_tables(f) for f in freqs]
         ops2 = native.Operators(st.handle, freqs, data)
         xh, its2, res2, ok2 = native.solve(st.handle, [(ops2, q) for (_, q) in cols], rhs_c, args.tol, restart=args.restart,
-                                           inner_tol=args.inner_tol, max_its=4000)
+                                           inner_tol=args.inner_tol, max_its=args.max_its, reorth=args.reorth,
+                                           outer_k=args.outer_k)
         e2e_t.append(time.perf_counter() - t0)
         del ops2
     e2e = None
@@ -290,7 +292,7 @@ def run_gpu(args):
         t0 = time.perf_counter()
         for c in sample:
             native.solve(st.handle, [ops[cols[c][1]]], rhs_c[c: c + 1], args.tol, restart=args.restart,
-                         precision="fp64", max_its=4000)
+                         precision="fp64", max_its=args.max_its, inner_tol=args.tol, outer_k=1, reorth=0.7)
         plain = {"value": len(sample) / (time.perf_counter() - t0), "unit": "solves/s",
                  "sample": "4 columns solved one at a time, FP64 GMRES(50) + FP64 products, operators resident"}
 
@@ -304,7 +306,7 @@ def run_gpu(args):
                 "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "c64 inner / c128 refinement", "data": "synthetic (seeded)",
                 "config": {"workload": WORKLOAD, "solves_per_step": ncol, "tol": args.tol, "restart": args.restart,
-                           "reorth": args.reorth,
+                           "reorth": args.reorth, "outer_gcr_k": args.outer_k,
                            "parallelism": f"replicas x{world}", "l2": "working set >> L2 (Krylov basis ~48 GB)",
                            "operators": "resident (factorised once, timed separately)"},
                 "factorise_s_all_freqs": round(factor_s, 3),

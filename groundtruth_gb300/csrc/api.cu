@@ -151,6 +151,7 @@ struct Workspace {
     c64 *x64 = nullptr, *r64 = nullptr, *b64 = nullptr, *T64 = nullptr;
     double *rho = nullptr, *bnorm = nullptr;
     c64* npart = nullptr;
+    c64* npart_k = nullptr;
     c64* nred = nullptr;
     // inner (precision R) per slot
     void *V = nullptr, *w = nullptr, *z = nullptr, *T = nullptr, *zfac = nullptr, *uvec = nullptr;
@@ -159,6 +160,10 @@ struct Workspace {
     int *slot_col = nullptr, *slot_op = nullptr, *g_ptr = nullptr, *g_slot = nullptr, *g_op = nullptr, *col_op = nullptr;
     int* act = nullptr;
     int* act_host = nullptr;
+    // outer GCR: directions P (corrections) and Q = K P, per column, k-major; step sizes; active columns
+    int kmax = 0;
+    c64 *gP = nullptr, *gQ = nullptr, *gbeta = nullptr, *galpha = nullptr, *gnu2 = nullptr;
+    int* colact = nullptr;
     int* flag_dev = nullptr;
     int* flag_host = nullptr;
     int* its_col = nullptr;
@@ -383,9 +388,9 @@ static void make_groups(const std::vector<int>& slots, const std::vector<int>& s
 
 static int nchunks(int64_t n) { return (int)((n + 2047) / 2048); }  // DOT_CHUNK in gmres.cu
 
-static void ensure_ws(gt_geometry* G, int ncol, int m, int prec) {
+static void ensure_ws(gt_geometry* G, int ncol, int m, int prec, int kmax) {
     auto& w = G->ws;
-    if (w && w->ncol >= ncol && w->m >= m && w->prec == prec) return;
+    if (w && w->ncol >= ncol && w->m >= m && w->prec == prec && w->kmax >= kmax) return;
     w.reset();
     cudaDeviceSynchronize();
     w.reset(new Workspace());
@@ -393,6 +398,7 @@ static void ensure_ws(gt_geometry* G, int ncol, int m, int prec) {
     W.ncol = ncol;
     W.m = m;
     W.prec = prec;
+    W.kmax = kmax;
     const int64_t n = G->geo.n;
     const size_t es = prec == 1 ? sizeof(c64) : sizeof(c32);
     Pool& p = W.pool;
@@ -404,6 +410,7 @@ static void ensure_ws(gt_geometry* G, int ncol, int m, int prec) {
     W.bnorm = p.alloc<double>(ncol);
     const int nch = nchunks(n);
     W.npart = p.alloc<c64>((size_t)ncol * nch);
+    W.npart_k = p.alloc<c64>((size_t)ncol * nch * (kmax + 2));
     W.nred = p.alloc<c64>(ncol);
     W.V = p.alloc<unsigned char>((size_t)ncol * (m + 1) * n * es);
     W.w = p.alloc<unsigned char>((size_t)ncol * n * es);
@@ -439,6 +446,12 @@ static void ensure_ws(gt_geometry* G, int ncol, int m, int prec) {
     W.g_op = p.alloc<int>(ncol);
     W.act = p.alloc<int>(ncol);
     GT_CUDA(cudaMallocHost(&W.act_host, ncol * sizeof(int)));
+    W.gP = p.alloc<c64>((size_t)kmax * ncol * n);
+    W.gQ = p.alloc<c64>((size_t)kmax * ncol * n);
+    W.gbeta = p.alloc<c64>((size_t)ncol * (kmax + 1));
+    W.galpha = p.alloc<c64>((size_t)ncol * 2);
+    W.gnu2 = p.alloc<c64>(ncol);
+    W.colact = p.alloc<int>(ncol);
     W.col_op = p.alloc<int>(ncol);
     W.flag_dev = p.alloc<int>(1);
     W.its_col = p.alloc<int>(ncol);
@@ -491,10 +504,34 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
         GT_CUDA(cudaMemcpyAsync(W.g_op, gop.data(), gop.size() * sizeof(int), cudaMemcpyHostToDevice, st));
         return Groups{(int)gop.size(), W.g_ptr, W.g_slot, W.g_op};
     };
+    const int K = std::max(1, o.outer_k);
+    const int64_t ldk = (int64_t)ncol * n;          // between GCR directions
+    int k = 0;                                      // directions held
+    bool verified = true;                           // rho is the true residual's norm
+    std::vector<int> colact(ncol);
+    // the true residual r = b - K x in FP64 (and its norms), which also restarts the GCR directions
+    auto true_residual = [&]() {
+        matvec<double>(G, ops, W.x64, W.b64, W.r64, n, ncol, W.col_op, 1, W.T64, st);
+        {
+            Scope sc(P, "norms", st, 16.0 * ncol * n);
+            norms64(G, W.r64, n, ncol, W.rho, st);
+        }
+        GT_CUDA(cudaMemcpyAsync(h_rho.data(), W.rho, ncol * sizeof(double), cudaMemcpyDeviceToHost, st));
+        GT_CUDA(cudaStreamSynchronize(st));
+        verified = true;
+        k = 0;
+    };
     for (int outer = 0; outer < o.max_outer; ++outer) {
-        slot_col.clear();
-        for (int c = 0; c < ncol; ++c)
-            if (h_bnorm[c] > 0 && h_rho[c] > o.tol * h_bnorm[c] && h_its[c] < o.max_its) slot_col.push_back(c);
+        auto pick = [&]() {
+            slot_col.clear();
+            for (int c = 0; c < ncol; ++c)
+                if (h_bnorm[c] > 0 && h_rho[c] > o.tol * h_bnorm[c] && h_its[c] < o.max_its) slot_col.push_back(c);
+        };
+        pick();
+        if (slot_col.empty() && !verified) {        // the recurrence says done: confirm on the true residual
+            true_residual();
+            pick();
+        }
         if (slot_col.empty()) break;
         std::stable_sort(slot_col.begin(), slot_col.end(), [&](int a, int b) { return h_col_op[a] < h_col_op[b]; });
         const int ns = (int)slot_col.size();
@@ -572,22 +609,49 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
         for (int q = 0; q < ns; ++q) act[q] = q;
         grp = upload_groups(act);
         precond<R>(G, ops, w, n, z, n, ns, W.slot_op, grp, gmax, zfac, uvec, st, W.act);
+        // GCR step in FP64: p = the cycle's correction, q = K p, both orthogonalised against the directions
+        // held (q orthonormal); then x += alpha p, r -= alpha q with alpha = q^H r
+        if (k == K) k = 0;
+        c64* Pk = W.gP + (int64_t)k * ldk;
+        c64* Qk = W.gQ + (int64_t)k * ldk;
+        std::fill(colact.begin(), colact.end(), 0);
+        for (int c : slot_col) colact[c] = 1;
+        GT_CUDA(cudaMemcpyAsync(W.colact, colact.data(), ncol * sizeof(int), cudaMemcpyHostToDevice, st));
         {
-            Scope sc(P, "refine", st, (double)ns * n * (32.0 + sizeof(cx<R>)));
-            launch_refine<R>(W.x64, n, z, n, W.slot_col, W.rho, n, ns, st);
+            Scope sc(P, "gcr", st, (double)ns * n * (16.0 * (4 * k + 12) + sizeof(cx<R>)));
+            GT_CUDA(cudaMemsetAsync(Pk, 0, (size_t)ldk * sizeof(c64), st));
+            launch_to64<R>(Pk, n, z, n, W.slot_col, n, ns, st);
         }
-        // the true residual in FP64
-        matvec<double>(G, ops, W.x64, W.b64, W.r64, n, ncol, W.col_op, 1, W.T64, st);
+        matvec<double>(G, ops, Pk, nullptr, Qk, n, ns, W.col_op, 0, W.T64, st, W.slot_col);
         {
-            Scope sc(P, "norms", st, 16.0 * ncol * n);
-            norms64(G, W.r64, n, ncol, W.rho, st);
+            Scope sc(P, "gcr", st, 0.0);
+            if (k > 0) {
+                launch_dots<double>(W.gQ, ldk, n, k, Qk, n, n, ncol, W.colact, W.npart_k, nch, st);
+                launch_reduce(W.npart_k, nch, k, ncol, W.colact, W.gbeta, K + 1, 0, st);
+                launch_update<double>(W.gQ, ldk, n, k, W.gbeta, K + 1, Qk, n, n, ncol, W.colact, W.npart, nch, -1, st);
+                launch_update<double>(W.gP, ldk, n, k, W.gbeta, K + 1, Pk, n, n, ncol, W.colact, nullptr, nch, -1, st);
+            } else {
+                launch_dots<double>(Qk, 0, n, 0, Qk, n, n, ncol, W.colact, W.npart, nch, st);
+            }
+            launch_reduce(W.npart, nch, 0, ncol, W.colact, W.gnu2, 1, 0, st);
+            launch_gcr_scale(Pk, Qk, n, W.gnu2, W.colact, n, ncol, st);
+            launch_dots<double>(Qk, 0, n, 1, W.r64, n, n, ncol, W.colact, W.npart_k, nch, st);
+            launch_reduce(W.npart_k, nch, 1, ncol, W.colact, W.galpha, 2, 0, st);
+            launch_update<double>(Pk, 0, n, 1, W.galpha, 2, W.x64, n, n, ncol, W.colact, nullptr, nch, 1, st);
+            launch_update<double>(Qk, 0, n, 1, W.galpha, 2, W.r64, n, n, ncol, W.colact, W.npart, nch, -1, st);
+            launch_reduce(W.npart, nch, 0, ncol, W.colact, W.nred, 1, 0, st);
+            launch_sqrt_norms_active(W.nred, 1, ncol, W.colact, W.rho, st);
         }
+        ++k;
+        verified = false;
         GT_CUDA(cudaMemcpyAsync(h_rho.data(), W.rho, ncol * sizeof(double), cudaMemcpyDeviceToHost, st));
         GT_CUDA(cudaMemcpyAsync(its_slot.data(), S.its_total, ns * sizeof(int), cudaMemcpyDeviceToHost, st));
         GT_CUDA(cudaStreamSynchronize(st));
         for (int s = 0; s < ns; ++s) h_its[slot_col[s]] = its_slot[s];
         P->flush();
     }
+    if (!verified) true_residual();
+    P->flush();
     bool all = true;
     for (int c = 0; c < ncol; ++c) {
         double rr = h_bnorm[c] > 0 ? h_rho[c] / h_bnorm[c] : 0.0;
@@ -893,7 +957,7 @@ int gt_solve_device(gt_geometry* G, gt_operators* ops, int32_t n_cols, const int
     if (!G || !ops || !opts || n_cols < 1) throw Invalid("bad arguments");
     std::lock_guard<std::mutex> lk(G->lock);
     cudaStream_t st = (cudaStream_t)stream;
-    ensure_ws(G, n_cols, opts->restart, opts->precision == 1 ? 1 : 0);
+    ensure_ws(G, n_cols, opts->restart, opts->precision == 1 ? 1 : 0, std::max(1, opts->outer_k));
     Workspace& W = *G->ws;
     GT_CUDA(cudaMemcpyAsync(W.b64, rhs_device, (size_t)n_cols * G->geo.n * sizeof(c64), cudaMemcpyDeviceToDevice, st));
     int rc = run_solve(G, ops, n_cols, col_op, opts, its_out, resid_out, st);
@@ -910,7 +974,7 @@ int gt_solve(gt_geometry* G, gt_operators* ops, int32_t n_cols, const int32_t* c
     if (!G || !ops || !opts || n_cols < 1 || !rhs || !x_out) throw Invalid("bad arguments");
     std::lock_guard<std::mutex> lk(G->lock);
     cudaStream_t st = (cudaStream_t)stream;
-    ensure_ws(G, n_cols, opts->restart, opts->precision == 1 ? 1 : 0);
+    ensure_ws(G, n_cols, opts->restart, opts->precision == 1 ? 1 : 0, std::max(1, opts->outer_k));
     Workspace& W = *G->ws;
     const int64_t nc = G->n_compact;
     Pool tmp;

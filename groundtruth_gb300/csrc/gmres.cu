@@ -313,7 +313,48 @@ __global__ void sqrt_norms_kernel(const c64* __restrict__ nrm2, int ld, int n, d
     if (i < n) out[i] = sqrt(nrm2[(int64_t)i * ld].re);
 }
 
+template <typename R>
+__global__ void to64_kernel(c64* __restrict__ dst, int64_t ldd, const cx<R>* __restrict__ src, int64_t lds,
+                            const int* __restrict__ slot_col, int64_t n) {
+    const int s = blockIdx.y;
+    c64* d = dst + (int64_t)slot_col[s] * ldd;
+    const cx<R>* x = src + (int64_t)s * lds;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+        d[q] = cvt<double>(x[q]);
+}
+
+__global__ void gcr_scale_kernel(c64* __restrict__ p, c64* __restrict__ q, int64_t ld, const c64* __restrict__ nu2,
+                                 const int* __restrict__ active, int64_t n) {
+    const int c = blockIdx.y;
+    if (active && !active[c]) return;
+    const double nu = sqrt(nu2[c].re);
+    const double f = nu > 0 ? 1.0 / nu : 0.0;
+    c64* pc = p + (int64_t)c * ld;
+    c64* qc = q + (int64_t)c * ld;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        pc[i] = f * pc[i];
+        qc[i] = f * qc[i];
+    }
+}
+
 // ------------------------------------------------------------------------------------------ launchers
+template <typename R>
+void launch_to64(c64* dst, int64_t ldd, const cx<R>* src, int64_t lds, const int* slot_col, int64_t n, int nslot,
+                 cudaStream_t st) {
+    int blocks = (int)std::min<int64_t>((n + 255) / 256, 1024);
+    to64_kernel<R><<<dim3(blocks, nslot), 256, 0, st>>>(dst, ldd, src, lds, slot_col, n);
+    GT_LAUNCH_CHECK();
+}
+template void launch_to64<float>(c64*, int64_t, const c32*, int64_t, const int*, int64_t, int, cudaStream_t);
+template void launch_to64<double>(c64*, int64_t, const c64*, int64_t, const int*, int64_t, int, cudaStream_t);
+
+void launch_gcr_scale(c64* p, c64* q, int64_t ld, const c64* nu2, const int* active, int64_t n, int ncol,
+                      cudaStream_t st) {
+    int blocks = (int)std::min<int64_t>((n + 255) / 256, 1024);
+    gcr_scale_kernel<<<dim3(blocks, ncol), 256, 0, st>>>(p, q, ld, nu2, active, n);
+    GT_LAUNCH_CHECK();
+}
+
 void launch_dgks(const GmresState& s, int j, cudaStream_t st) {
     dgks_kernel<<<ceil_div(s.nslot, 128), 128, 0, st>>>(s, j);
     GT_LAUNCH_CHECK();
@@ -355,6 +396,17 @@ void launch_any_active(const int* active, int n, int* flag, cudaStream_t st) {
     any_active_kernel<<<1, 256, 0, st>>>(active, n, flag);
     GT_LAUNCH_CHECK();
 }
+__global__ void sqrt_norms_active_kernel(const c64* __restrict__ nrm2, int ld, int n, const int* __restrict__ active,
+                                         double* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && active[i]) out[i] = sqrt(nrm2[(int64_t)i * ld].re);
+}
+
+void launch_sqrt_norms_active(const c64* nrm2, int ld, int n, const int* active, double* out, cudaStream_t st) {
+    sqrt_norms_active_kernel<<<ceil_div(n, 128), 128, 0, st>>>(nrm2, ld, n, active, out);
+    GT_LAUNCH_CHECK();
+}
+
 void launch_sqrt_norms(const c64* nrm2, int ld, int n, double* out, cudaStream_t st) {
     sqrt_norms_kernel<<<ceil_div(n, 128), 128, 0, st>>>(nrm2, ld, n, out);
     GT_LAUNCH_CHECK();

@@ -47,6 +47,15 @@ template <typename R>
 void launch_refine(c64* x, int64_t ldx, const cx<R>* e, int64_t lde, const int* slot_col, const double* rho, int64_t n,
                    int nslot, cudaStream_t st);
 void launch_any_active(const int* active, int n, int* flag, cudaStream_t st);
+// dst[slot_col[s]] = src[s] (precision R -> FP64), s < nslot
+template <typename R>
+void launch_to64(c64* dst, int64_t ldd, const cx<R>* src, int64_t lds, const int* slot_col, int64_t n, int nslot,
+                 cudaStream_t st);
+// the GCR direction of each active column scaled to a unit product: p /= |q|, q /= |q| (|q|^2 in nu2)
+void launch_gcr_scale(c64* p, c64* q, int64_t ld, const c64* nu2, const int* active, int64_t n, int ncol,
+                      cudaStream_t st);
 void launch_sqrt_norms(const c64* nrm2, int ld, int n, double* out, cudaStream_t st);
+// out[i] = sqrt(nrm2[i * ld].re) for active i only
+void launch_sqrt_norms_active(const c64* nrm2, int ld, int n, const int* active, double* out, cudaStream_t st);
 
 }  // namespace gt

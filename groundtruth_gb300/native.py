@@ -43,7 +43,7 @@ class GeometryDesc(C.Structure):
 
 class SolveOpts(C.Structure):
     _fields_ = [("tol", C.c_double), ("restart", C.c_int32), ("max_its", C.c_int32), ("inner_tol", C.c_double),
-                ("precision", C.c_int32), ("max_outer", C.c_int32), ("reorth", C.c_double)]
+                ("precision", C.c_int32), ("max_outer", C.c_int32), ("reorth", C.c_double), ("outer_k", C.c_int32)]
 
 
 def load():
@@ -157,13 +157,13 @@ class Geometry:
 
     def solve_device(self, obj, col_op: np.ndarray, rhs_ptr: int, x_ptr: int, tol: float, restart: int = 50,
                      max_its: int = 2000, inner_tol: float = 1e-5, precision: str = "mixed", max_outer: int = 40,
-                     stream: int = 0, reorth: float = 0.7):
+                     stream: int = 0, reorth: float = 0.7, outer_k: int = 8):
         """gt_solve_device on dense complex128 device buffers (pointers); returns (its, resid)."""
         idx = np.ascontiguousarray(col_op, np.int32)
         ncol = len(idx)
         its = np.zeros(ncol, np.int32)
         res = np.zeros(ncol)
-        o = SolveOpts(tol, restart, max_its, inner_tol, 1 if precision == "fp64" else 0, max_outer, reorth)
+        o = SolveOpts(tol, restart, max_its, inner_tol, 1 if precision == "fp64" else 0, max_outer, reorth, outer_k)
         rc = self.lib.gt_solve_device(self.h, obj.h, ncol, _ptr(idx, C.c_int32), P(rhs_ptr), C.byref(o), P(x_ptr),
                                       _ptr(its, C.c_int32), _ptr(res, C.c_double), P(stream))
         if rc not in (GT_OK, GT_NOT_CONVERGED):
@@ -231,7 +231,8 @@ def _ops_and_index(ops: list):
 
 
 def solve(geom: Geometry, ops: list, rhs: np.ndarray, tol: float, restart: int = 50, max_its: int = 2000,
-          inner_tol: float = 1e-5, precision: str = "mixed", max_outer: int = 40, reorth: float = 0.7):
+          inner_tol: float = 1e-5, precision: str = "mixed", max_outer: int = 40, reorth: float = 0.7,
+          outer_k: int = 8):
     """rhs: (ncol, n_compact) complex in the reference's order.  Returns (x, its, resid, converged)."""
     lib = geom.lib
     obj, idx = _ops_and_index(ops)
@@ -240,7 +241,7 @@ def solve(geom: Geometry, ops: list, rhs: np.ndarray, tol: float, restart: int =
     x = np.zeros_like(rhs)
     its = np.zeros(ncol, np.int32)
     res = np.zeros(ncol)
-    o = SolveOpts(tol, restart, max_its, inner_tol, 1 if precision == "fp64" else 0, max_outer, reorth)
+    o = SolveOpts(tol, restart, max_its, inner_tol, 1 if precision == "fp64" else 0, max_outer, reorth, outer_k)
     rc = lib.gt_solve(geom.h, obj.h, ncol, _ptr(idx, C.c_int32), _ptr(rhs.view(np.float64), C.c_double), C.byref(o),
                       _ptr(x.view(np.float64), C.c_double), _ptr(its, C.c_int32), _ptr(res, C.c_double), None)
     if rc not in (GT_OK, GT_NOT_CONVERGED):

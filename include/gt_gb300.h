@@ -85,6 +85,8 @@ typedef struct gt_solve_opts {
     int32_t max_outer;      /* refinement steps */
     double reorth;          /* DGKS: re-orthogonalise when ||w|| fell below reorth x its norm before the first
                                Gram-Schmidt pass (0.7: the reference's rule, peec.py:3156; 0: never) */
+    int32_t outer_k;        /* FP64 outer GCR directions kept (each cycle's correction orthogonalised against
+                               the previous ones; 1: a plain refinement step with the optimal step length) */
 } gt_solve_opts;
 
 /* Library version (major*10000 + minor*100 + patch). */
