@@ -183,7 +183,7 @@ struct gt_geometry {
     Fronts F{};
     Pool pool;
     std::vector<int64_t> level_ptr;
-    std::vector<int> level_maxnf;
+    std::vector<int> level_maxnf, level_maxnown;
     int max_nf = 0;
     int64_t* d_order = nullptr;
     int64_t n_compact = 0;
@@ -203,8 +203,10 @@ struct gt_operators {
     Pool pool;
     double* omega = nullptr;
     c64 *zs = nullptr, *zcap = nullptr, *zbr = nullptr, *tab = nullptr;
-    c64* panel64 = nullptr;
+    c64* panel64 = nullptr;      // column-major per front (forward solves)
     c32* panel32 = nullptr;
+    c64* panel64_rm = nullptr;   // row-major copies (backward solves)
+    c32* panel32_rm = nullptr;
 };
 
 namespace gt {
@@ -226,6 +228,9 @@ template <> const c64* tw1_of<double>(const Orient& o) { return o.tw1_64; }
 template <typename R> static const cx<R>* panel_of(const gt_operators* ops);
 template <> const c32* panel_of<float>(const gt_operators* ops) { return ops->panel32; }
 template <> const c64* panel_of<double>(const gt_operators* ops) { return ops->panel64; }
+template <typename R> static const cx<R>* panel_rm_of(const gt_operators* ops);
+template <> const c32* panel_rm_of<float>(const gt_operators* ops) { return ops->panel32_rm; }
+template <> const c64* panel_rm_of<double>(const gt_operators* ops) { return ops->panel64_rm; }
 
 static bool good_fft_size(int P) {
     if (P < 8) return false;
@@ -345,14 +350,16 @@ static void precond(gt_geometry* G, gt_operators* ops, const cx<R>* r, int64_t l
         Scope s(P, sizeof(R) == 4 ? "fwd_f32" : "fwd_f64", st, panel + nslot * es * (2 * nfac + 2.0 * G->F.vec_total));
         for (int h = 0; h < nlev; ++h) {
             int nf = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);
-            launch_fwd_level<R>(G->F, G->d_order + G->level_ptr[h], nf, G->level_maxnf[h], pan, zfac, uvec, grp, gmax, st);
+            launch_fwd_level<R>(G->F, G->d_order + G->level_ptr[h], nf, G->level_maxnf[h], G->level_maxnown[h], pan, zfac,
+                                uvec, grp, gmax, st);
         }
     }
     {
         Scope s(P, sizeof(R) == 4 ? "bwd_f32" : "bwd_f64", st, panel + nslot * es * 2 * nfac);
         for (int h = nlev - 1; h >= 0; --h) {
             int nf = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);
-            launch_bwd_level<R>(G->F, G->d_order + G->level_ptr[h], nf, G->level_maxnf[h], pan, zfac, grp, gmax, st);
+            launch_bwd_level<R>(G->F, G->d_order + G->level_ptr[h], nf, G->level_maxnf[h], G->level_maxnown[h],
+                                pan, panel_rm_of<R>(ops), zfac, grp, gmax, st);
         }
     }
     {
@@ -858,12 +865,14 @@ int gt_geometry_create(const gt_geometry_desc* d, gt_geometry** out) {
     G->level_ptr.assign(d->level_ptr, d->level_ptr + d->n_levels + 1);
     G->d_order = p.upload(d->front_order, nf);
     for (int h = 0; h < d->n_levels; ++h) {
-        int mx = 1;
+        int mx = 1, mo = 1;
         for (int64_t q = d->level_ptr[h]; q < d->level_ptr[h + 1]; ++q) {
             int64_t f = d->front_order[q];
             mx = std::max<int>(mx, (int)(d->nown[f] + d->nbnd[f]));
+            mo = std::max<int>(mo, (int)d->nown[f]);
         }
         G->level_maxnf.push_back(mx);
+        G->level_maxnown.push_back(mo);
         G->max_nf = std::max(G->max_nf, mx);
     }
     G->d_sterm_ptr = p.upload(d->sterm_ptr, d->n_svalues + 1);
@@ -905,13 +914,15 @@ int gt_operators_create(gt_geometry* G, int32_t n_ops, const double* omega, cons
     GT_CUDA(cudaMemsetAsync(status, 0, sizeof(int), st));
     O->panel64 = p.alloc<c64>((size_t)n_ops * F.panel_total);
     O->panel32 = p.alloc<c32>((size_t)n_ops * F.panel_total);
+    O->panel32_rm = p.alloc<c32>((size_t)n_ops * F.panel_total);
+    O->panel64_rm = p.alloc<c64>((size_t)n_ops * F.panel_total);
     launch_assemble_s(G->d_sterm_ptr, G->d_sterm_tab, G->d_sterm_coef, F.nsv, O->tab, g.ntab, svals, n_ops, st);
     const int nlev = (int)G->level_ptr.size() - 1;
     for (int h = 0; h < nlev; ++h) {
         int nfl = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);
         launch_factor_level(F, G->d_order + G->level_ptr[h], nfl, G->level_maxnf[h], svals, O->panel64, upd, n_ops, status, st);
     }
-    launch_panel_to32(O->panel64, O->panel32, (int64_t)n_ops * F.panel_total, st);
+    launch_panel_convert(F, O->panel64, O->panel32, O->panel32_rm, O->panel64_rm, n_ops, st);
     int h_status = 0;
     GT_CUDA(cudaMemcpy(&h_status, status, sizeof(int), cudaMemcpyDeviceToHost));
     if (h_status) throw Invalid("the Schur complement has a zero or non-finite pivot (a piece of copper with no "

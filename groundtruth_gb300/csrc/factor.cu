@@ -103,44 +103,267 @@ void launch_factor_level(const Fronts& F, const int64_t* front_list, int nf_leve
     GT_LAUNCH_CHECK();
 }
 
-__global__ void panel_to32_kernel(const c64* __restrict__ p64, c32* __restrict__ p32, int64_t n) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        p32[i] = cvt<float>(p64[i]);
+// The factor's panels for the solves: FP32 column-major (forward), FP32 and FP64 row-major (backward).
+__global__ void panel_convert_kernel(Fronts F, const c64* __restrict__ p64, c32* __restrict__ p32, c32* __restrict__ r32,
+                                     c64* __restrict__ r64) {
+    const int f = blockIdx.x;
+    const int op = blockIdx.y;
+    const int nown = (int)F.nown[f], nf = nown + (int)F.nbnd[f];
+    const int64_t base = (int64_t)op * F.panel_total + F.panel_off[f];
+    for (int64_t q = threadIdx.x; q < (int64_t)nf * nown; q += blockDim.x) {
+        int k = int(q / nf), i = int(q - (int64_t)k * nf);      // column-major element (i, k)
+        c64 v = p64[base + q];
+        p32[base + q] = cvt<float>(v);
+        r32[base + (int64_t)i * nown + k] = cvt<float>(v);
+        r64[base + (int64_t)i * nown + k] = v;
+    }
 }
 
-void launch_panel_to32(const c64* p64, c32* p32, int64_t n, cudaStream_t st) {
-    int blocks = (int)std::min<int64_t>((n + 255) / 256, 8192);
-    panel_to32_kernel<<<std::max(blocks, 1), 256, 0, st>>>(p64, p32, n);
+void launch_panel_convert(const Fronts& F, const c64* p64, c32* p32, c32* r32, c64* r64, int nops, cudaStream_t st) {
+    panel_convert_kernel<<<dim3(F.nfront, nops), 256, 0, st>>>(F, p64, p32, r32, r64);
     GT_LAUNCH_CHECK();
 }
 
 // ------------------------------------------------------------------------------------------ solves
-// z: [col][nfac] in factor order; uvec: [col][vec_total] update vectors.  Shared memory: w [GMAXC][ldw] (the
-// front's rows for each of the group's columns, column-major so that consecutive threads touch consecutive
-// rows) and the current 32 x 32 diagonal block of the panel.  The own block is processed in blocks of 32
-// columns: the diagonal block by one warp per column, warp-synchronously (the lanes hold the block's 32
-// rows); the rest of the front by sweeps in which every panel element is read once, coalesced, with the
-// 32 loads of a block row issued back to back.
+// z: [col][nfac] in factor order; uvec: [col][vec_total] update vectors.  Two forms, chosen per level:
+//
+// small fronts (nf <= 128, nown <= 64): one warp per task (a front and a group of <= 8 columns sharing its
+//   operator), the front's rows in registers (row r on lane r mod 32), no block barrier.  Forward: a column
+//   sweep of the column-major panel with the next column's loads issued before the current one is used.
+//   Backward: a row sweep of the row-major copy: every boundary row (y known) updates the own rows, then the
+//   own rows from the last.
+// larger fronts: one block per task, w in shared memory [GMAXC][ldw]; the own block in blocks of 32 columns:
+//   the 32 x 32 diagonal block by one warp per column, warp-synchronously, the rest by sweeps in which each
+//   thread owns a row (forward, column-major panel) or a column (backward, row-major panel), every panel
+//   element read once, coalesced, 8 loads in flight per thread.
 constexpr int GMAXC = 8;
 constexpr int TB = 32;
+constexpr int RPL = 4;           // rows per lane of the small-front kernels (nf <= 128)
+constexpr int SMALL_NF = 32 * RPL;
+constexpr int SMALL_NOWN = 64;
 
 template <typename R>
-__device__ __forceinline__ void load_diag(cx<R>* Dsm, const cx<R>* __restrict__ L, int nf, int k0, int kb) {
-    for (int q = threadIdx.x; q < TB * TB; q += blockDim.x) {
-        int c = q / TB, r = q - c * TB;                 // column c, row r of the block
-        Dsm[q] = (c < kb && r < kb) ? L[(int64_t)(k0 + c) * nf + k0 + r] : zero<R>();
+static void smem_attr(const void* fn, size_t bytes) {
+    if (bytes > 48 * 1024) GT_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+}
+
+template <typename R>
+__device__ __forceinline__ cx<R> shfl_cx(cx<R> v, int src) {
+    return mk<R>(__shfl_sync(0xffffffffu, v.re, src), __shfl_sync(0xffffffffu, v.im, src));
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) fwd_small_kernel(Fronts F, const int64_t* __restrict__ front_list, int ntask,
+                                                        const cx<R>* __restrict__ panel, cx<R>* __restrict__ z,
+                                                        cx<R>* __restrict__ uvec, Groups G) {
+    const int lane = threadIdx.x & 31;
+    const int task = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (task >= ntask) return;
+    const int g = task % G.ngroup;
+    const int f = (int)front_list[task / G.ngroup];
+    const int* gs = G.gslot + G.gptr[g];
+    const int gc = G.gptr[g + 1] - G.gptr[g], op = G.op[g];
+    const int nown = (int)F.nown[f], nbnd = (int)F.nbnd[f], nf = nown + nbnd;
+    const int64_t own0 = F.own_start[f];
+    const cx<R>* __restrict__ L = panel + (int64_t)op * F.panel_total + F.panel_off[f];
+    // stage the rows in the warp's shared-memory region: own entries of s, children's update vectors added
+    // one child at a time (their boundaries can share rows), then into registers
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<R>* ws = reinterpret_cast<cx<R>*>(smem_raw) + (int64_t)(threadIdx.x >> 5) * GMAXC * SMALL_NF;
+    for (int c = 0; c < gc; ++c)
+        for (int r = lane; r < nf; r += 32)
+            ws[c * SMALL_NF + r] = r < nown ? z[(int64_t)gs[c] * F.nfac + own0 + r] : zero<R>();
+    __syncwarp();
+    for (int64_t ci = F.child_ptr[f]; ci < F.child_ptr[f + 1]; ++ci) {
+        const int ch = (int)F.child_idx[ci];
+        const int nb = (int)F.nbnd[ch];
+        const int64_t* map = F.cmap_idx + F.cmap_ptr[ci];
+        for (int c = 0; c < gc; ++c) {
+            const cx<R>* u = uvec + (int64_t)gs[c] * F.vec_total + F.vec_off[ch];
+            for (int i = lane; i < nb; i += 32) ws[c * SMALL_NF + map[i]] += u[i];
+        }
+        __syncwarp();
+    }
+    cx<R> w[RPL][GMAXC];
+#pragma unroll
+    for (int q = 0; q < RPL; ++q) {
+        const int r = lane + 32 * q;
+#pragma unroll
+        for (int c = 0; c < GMAXC; ++c) w[q][c] = (c < gc && r < nf) ? ws[c * SMALL_NF + r] : zero<R>();
+    }
+    cx<R> lc[RPL], ln[RPL];
+#pragma unroll
+    for (int q = 0; q < RPL; ++q) {
+        const int r = lane + 32 * q;
+        lc[q] = (nown > 0 && r < nf) ? L[r] : zero<R>();
+    }
+    for (int k = 0; k < nown; ++k) {
+        const int q_k = k >> 5, src = k & 31;
+#pragma unroll
+        for (int q = 0; q < RPL; ++q) {
+            const int r = lane + 32 * q;
+            ln[q] = (k + 1 < nown && r < nf) ? L[(int64_t)(k + 1) * nf + r] : zero<R>();
+        }
+        cx<R> zk[GMAXC];
+#pragma unroll
+        for (int c = 0; c < GMAXC; ++c) {
+            cx<R> mine = zero<R>();
+#pragma unroll
+            for (int q = 0; q < RPL; ++q)
+                if (q == q_k) mine = w[q][c];
+            zk[c] = shfl_cx(mine, src);
+        }
+#pragma unroll
+        for (int q = 0; q < RPL; ++q) {
+            const int r = lane + 32 * q;
+            if (r > k && r < nf) {
+#pragma unroll
+                for (int c = 0; c < GMAXC; ++c)
+                    if (c < gc) w[q][c] -= lc[q] * zk[c];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < RPL; ++q) lc[q] = ln[q];
+    }
+#pragma unroll
+    for (int q = 0; q < RPL; ++q) {
+        const int r = lane + 32 * q;
+        if (r < nown) {
+            const cx<R> d = L[(int64_t)r * nf + r];
+#pragma unroll
+            for (int c = 0; c < GMAXC; ++c)
+                if (c < gc) z[(int64_t)gs[c] * F.nfac + own0 + r] = cdiv(w[q][c], d);
+        } else if (r < nf) {
+#pragma unroll
+            for (int c = 0; c < GMAXC; ++c)
+                if (c < gc) uvec[(int64_t)gs[c] * F.vec_total + F.vec_off[f] + (r - nown)] = w[q][c];
+        }
     }
 }
 
 template <typename R>
-__global__ void __launch_bounds__(1024) fwd_level_kernel(Fronts F, const int64_t* __restrict__ front_list,
+__global__ void __launch_bounds__(256) bwd_small_kernel(Fronts F, const int64_t* __restrict__ front_list, int ntask,
+                                                        const cx<R>* __restrict__ panel_rm, cx<R>* __restrict__ z,
+                                                        Groups G) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31;
+    const int task = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (task >= ntask) return;
+    cx<R>* ws = reinterpret_cast<cx<R>*>(smem_raw) + (int64_t)(threadIdx.x >> 5) * GMAXC * SMALL_NF;
+    const int g = task % G.ngroup;
+    const int f = (int)front_list[task / G.ngroup];
+    const int* gs = G.gslot + G.gptr[g];
+    const int gc = G.gptr[g + 1] - G.gptr[g], op = G.op[g];
+    const int nown = (int)F.nown[f], nbnd = (int)F.nbnd[f], nf = nown + nbnd;
+    const int64_t own0 = F.own_start[f];
+    const int64_t* bnd = F.bnd_idx + F.bnd_ptr[f];
+    const cx<R>* __restrict__ L = panel_rm + (int64_t)op * F.panel_total + F.panel_off[f];   // (nf x nown) row-major
+    for (int c = 0; c < gc; ++c) {
+        const cx<R>* zc = z + (int64_t)gs[c] * F.nfac;
+        for (int r = lane; r < nf; r += 32) ws[c * SMALL_NF + r] = zc[r < nown ? own0 + r : bnd[r - nown]];
+    }
+    __syncwarp();
+    constexpr int OQ = SMALL_NOWN / 32;
+    // boundary rows (y final): acc_k = sum_i L[i, k] y_i, independent over i (4 rows of loads in flight)
+    cx<R> w[OQ][GMAXC];
+#pragma unroll
+    for (int q = 0; q < OQ; ++q)
+#pragma unroll
+        for (int c = 0; c < GMAXC; ++c) w[q][c] = zero<R>();
+    for (int i0 = nown; i0 < nf; i0 += 4) {
+        cx<R> l[4][OQ];
+#pragma unroll
+        for (int ii = 0; ii < 4; ++ii)
+#pragma unroll
+            for (int q = 0; q < OQ; ++q) {
+                const int k = lane + 32 * q, i = i0 + ii;
+                l[ii][q] = (i < nf && k < nown) ? L[(int64_t)i * nown + k] : zero<R>();
+            }
+#pragma unroll
+        for (int ii = 0; ii < 4; ++ii) {
+            const int i = min(i0 + ii, nf - 1);
+#pragma unroll
+            for (int c = 0; c < GMAXC; ++c) {
+                if (c >= gc) break;
+                const cx<R> y = ws[c * SMALL_NF + i];
+#pragma unroll
+                for (int q = 0; q < OQ; ++q) w[q][c] += l[ii][q] * y;
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < OQ; ++q) {
+        const int k = lane + 32 * q;
+#pragma unroll
+        for (int c = 0; c < GMAXC; ++c) w[q][c] = (c < gc && k < nown) ? ws[c * SMALL_NF + k] - w[q][c] : zero<R>();
+    }
+    // own rows from the last: y_j final, own rows k < j updated
+    cx<R> lc[OQ], ln[OQ];
+#pragma unroll
+    for (int q = 0; q < OQ; ++q) {
+        const int k = lane + 32 * q;
+        lc[q] = (nown >= 2 && k < nown - 1) ? L[(int64_t)(nown - 1) * nown + k] : zero<R>();
+    }
+    for (int j = nown - 1; j >= 1; --j) {
+#pragma unroll
+        for (int q = 0; q < OQ; ++q) {
+            const int k = lane + 32 * q;
+            ln[q] = (j - 1 >= 1 && k < j - 1) ? L[(int64_t)(j - 1) * nown + k] : zero<R>();
+        }
+        const int q_j = j >> 5, src = j & 31;
+        cx<R> yj[GMAXC];
+#pragma unroll
+        for (int c = 0; c < GMAXC; ++c) {
+            cx<R> mine = zero<R>();
+#pragma unroll
+            for (int q = 0; q < OQ; ++q)
+                if (q == q_j) mine = w[q][c];
+            yj[c] = shfl_cx(mine, src);
+        }
+#pragma unroll
+        for (int q = 0; q < OQ; ++q) {
+            const int k = lane + 32 * q;
+            if (k < j) {
+#pragma unroll
+                for (int c = 0; c < GMAXC; ++c)
+                    if (c < gc) w[q][c] -= lc[q] * yj[c];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < OQ; ++q) lc[q] = ln[q];
+    }
+#pragma unroll
+    for (int q = 0; q < OQ; ++q) {
+        const int r = lane + 32 * q;
+        if (r < nown) {
+#pragma unroll
+            for (int c = 0; c < GMAXC; ++c)
+                if (c < gc) z[(int64_t)gs[c] * F.nfac + own0 + r] = w[q][c];
+        }
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ void load_diag(cx<R>* Dsm, const cx<R>* __restrict__ L, int ld, int k0, int kb, bool rowmajor) {
+    // Dsm[c * TB + r] = L[k0 + r, k0 + c] (column c, row r of the diagonal block)
+    for (int q = threadIdx.x; q < TB * TB; q += blockDim.x) {
+        int c = q / TB, r = q - c * TB;
+        cx<R> v = zero<R>();
+        if (c < kb && r < kb) v = rowmajor ? L[(int64_t)(k0 + r) * ld + k0 + c] : L[(int64_t)(k0 + c) * ld + k0 + r];
+        Dsm[q] = v;
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(1024) fwd_block_kernel(Fronts F, const int64_t* __restrict__ front_list, int ntask,
                                                          const cx<R>* __restrict__ panel, cx<R>* __restrict__ z,
                                                          cx<R>* __restrict__ uvec, Groups G, int ldw) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<R>* Dsm = reinterpret_cast<cx<R>*>(smem_raw);
     cx<R>* w = Dsm + TB * TB;
-    const int f = (int)front_list[blockIdx.x];
-    const int g = blockIdx.y;
+    const int task = blockIdx.x;
+    const int g = task % G.ngroup;
+    const int f = (int)front_list[task / G.ngroup];
     const int* gs = G.gslot + G.gptr[g];
     const int gc = G.gptr[g + 1] - G.gptr[g], op = G.op[g];
     const int nown = (int)F.nown[f], nbnd = (int)F.nbnd[f], nf = nown + nbnd;
@@ -164,13 +387,13 @@ __global__ void __launch_bounds__(1024) fwd_level_kernel(Fronts F, const int64_t
     }
     for (int k0 = 0; k0 < nown; k0 += TB) {
         const int kb = min(TB, nown - k0);
-        load_diag<R>(Dsm, L, nf, k0, kb);
+        load_diag<R>(Dsm, L, nf, k0, kb, false);
         __syncthreads();
         if (warp < gc) {                                 // unit lower triangular solve of the block
             cx<R>* wc = w + warp * ldw + k0;
             cx<R> v = lane < kb ? wc[lane] : zero<R>();
             for (int kk = 0; kk < kb - 1; ++kk) {
-                cx<R> zk = mk<R>(__shfl_sync(0xffffffffu, v.re, kk), __shfl_sync(0xffffffffu, v.im, kk));
+                cx<R> zk = shfl_cx(v, kk);
                 if (lane > kk && lane < kb) v -= Dsm[kk * TB + lane] * zk;
             }
             if (lane < kb) wc[lane] = v;
@@ -182,25 +405,15 @@ __global__ void __launch_bounds__(1024) fwd_level_kernel(Fronts F, const int64_t
 #pragma unroll
             for (int c = 0; c < GMAXC; ++c) acc[c] = zero<R>();
             const cx<R>* Li = L + (int64_t)k0 * nf + i;
-            if (kb == TB) {
+            for (int k8 = 0; k8 < kb; k8 += 8) {
+                cx<R> l[8];
 #pragma unroll
-                for (int k8 = 0; k8 < TB; k8 += 8) {
-                    cx<R> l[8];
+                for (int kk = 0; kk < 8; ++kk) l[kk] = k8 + kk < kb ? Li[(int64_t)(k8 + kk) * nf] : zero<R>();
 #pragma unroll
-                    for (int kk = 0; kk < 8; ++kk) l[kk] = Li[(int64_t)(k8 + kk) * nf];
-#pragma unroll
-                    for (int kk = 0; kk < 8; ++kk)
-#pragma unroll
-                        for (int c = 0; c < GMAXC; ++c)
-                            if (c < gc) acc[c] += l[kk] * w[c * ldw + k0 + k8 + kk];
-                }
-            } else {
-                for (int kk = 0; kk < kb; ++kk) {
-                    const cx<R> lv = Li[(int64_t)kk * nf];
+                for (int kk = 0; kk < 8; ++kk)
 #pragma unroll
                     for (int c = 0; c < GMAXC; ++c)
-                        if (c < gc) acc[c] += lv * w[c * ldw + k0 + kk];
-                }
+                        if (c < gc) acc[c] += l[kk] * w[c * ldw + k0 + min(k8 + kk, kb - 1)];
             }
 #pragma unroll
             for (int c = 0; c < GMAXC; ++c)
@@ -216,37 +429,60 @@ __global__ void __launch_bounds__(1024) fwd_level_kernel(Fronts F, const int64_t
 }
 
 template <typename R>
-__global__ void __launch_bounds__(1024) bwd_level_kernel(Fronts F, const int64_t* __restrict__ front_list,
-                                                         const cx<R>* __restrict__ panel, cx<R>* __restrict__ z, Groups G,
-                                                         int ldw) {
+__global__ void __launch_bounds__(1024) bwd_block_kernel(Fronts F, const int64_t* __restrict__ front_list, int ntask,
+                                                         const cx<R>* __restrict__ panel, const cx<R>* __restrict__ panel_rm,
+                                                         cx<R>* __restrict__ z, Groups G, int ldw) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<R>* Dsm = reinterpret_cast<cx<R>*>(smem_raw);
     cx<R>* w = Dsm + TB * TB;
-    const int f = (int)front_list[blockIdx.x];
-    const int g = blockIdx.y;
+    const int task = blockIdx.x;
+    const int g = task % G.ngroup;
+    const int f = (int)front_list[task / G.ngroup];
     const int* gs = G.gslot + G.gptr[g];
     const int gc = G.gptr[g + 1] - G.gptr[g], op = G.op[g];
     const int nown = (int)F.nown[f], nbnd = (int)F.nbnd[f], nf = nown + nbnd;
     const int64_t own0 = F.own_start[f];
     const int64_t* bnd = F.bnd_idx + F.bnd_ptr[f];
-    const cx<R>* __restrict__ L = panel + (int64_t)op * F.panel_total + F.panel_off[f];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
-    for (int q = tid; q < gc * nf; q += blockDim.x) {
+    const cx<R>* __restrict__ L = panel_rm + (int64_t)op * F.panel_total + F.panel_off[f];   // (nf x nown) row-major
+    const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, warp = tid >> 5;
+    for (int q = tid; q < gc * nf; q += nth) {
         int c = q / nf, r = q - c * nf;
         w[c * ldw + r] = z[(int64_t)gs[c] * F.nfac + (r < nown ? own0 + r : bnd[r - nown])];
     }
     __syncthreads();
-    const int nblk = (nown + TB - 1) / TB;
-    for (int b = nblk - 1; b >= 0; --b) {
-        const int k0 = b * TB, kb = min(TB, nown - k0), k1 = k0 + kb;
-        // w[c][k] -= sum_{i >= k1} L[i, k] y[c][i] for the block's columns: one warp per column k
-        for (int kk = warp; kk < kb; kk += nwarp) {
-            const cx<R>* Lk = L + (int64_t)(k0 + kk) * nf;
+    // w[c][k] -= sum_{rows j in [j0, j1)} L[j, k] y[c][j], one thread per own column k < kmax
+    auto sweep = [&](int j0, int j1, int kmax) {
+        for (int k = tid; k < kmax; k += nth) {
+            cx<R> acc[GMAXC];
+#pragma unroll
+            for (int c = 0; c < GMAXC; ++c) acc[c] = zero<R>();
+            for (int j8 = j0; j8 < j1; j8 += 8) {
+                cx<R> l[8];
+#pragma unroll
+                for (int jj = 0; jj < 8; ++jj) l[jj] = j8 + jj < j1 ? L[(int64_t)(j8 + jj) * nown + k] : zero<R>();
+#pragma unroll
+                for (int jj = 0; jj < 8; ++jj)
+#pragma unroll
+                    for (int c = 0; c < GMAXC; ++c)
+                        if (c < gc) acc[c] += l[jj] * w[c * ldw + min(j8 + jj, j1 - 1)];
+            }
+#pragma unroll
+            for (int c = 0; c < GMAXC; ++c)
+                if (c < gc) w[c * ldw + k] -= acc[c];
+        }
+    };
+    // the boundary rows (final from the ancestors): w[c][k] -= sum_{i >= nown} L[i, k] y[c][i] as column dot
+    // products of the column-major panel, one warp per own column k, lanes down the rows
+    {
+        const cx<R>* __restrict__ Lc = panel + (int64_t)op * F.panel_total + F.panel_off[f];
+        const int nwarp = nth >> 5;
+        for (int k = warp; k < nown; k += nwarp) {
+            const cx<R>* Lk = Lc + (int64_t)k * nf;
             cx<R> acc[GMAXC];
 #pragma unroll
             for (int c = 0; c < GMAXC; ++c) acc[c] = zero<R>();
 #pragma unroll 4
-            for (int i = k1 + lane; i < nf; i += 32) {
+            for (int i = nown + lane; i < nf; i += 32) {
                 const cx<R> l = Lk[i];
 #pragma unroll
                 for (int c = 0; c < GMAXC; ++c)
@@ -260,60 +496,79 @@ __global__ void __launch_bounds__(1024) bwd_level_kernel(Fronts F, const int64_t
                     re += __shfl_xor_sync(0xffffffffu, re, o);
                     im += __shfl_xor_sync(0xffffffffu, im, o);
                 }
-                if (lane == 0) w[c * ldw + k0 + kk] -= mk<R>(re, im);
+                if (lane == 0) w[c * ldw + k] -= mk<R>(re, im);
             }
         }
-        load_diag<R>(Dsm, L, nf, k0, kb);
+    }
+    __syncthreads();
+    const int nblk = (nown + TB - 1) / TB;
+    for (int b = nblk - 1; b >= 0; --b) {
+        const int k0 = b * TB, kb = min(TB, nown - k0);
+        load_diag<R>(Dsm, L, nown, k0, kb, true);
         __syncthreads();
         if (warp < gc) {                                 // unit upper (L^T) solve of the block from the bottom
             cx<R>* wc = w + warp * ldw + k0;
             cx<R> v = lane < kb ? wc[lane] : zero<R>();
             for (int kk = kb - 1; kk > 0; --kk) {
-                cx<R> yk = mk<R>(__shfl_sync(0xffffffffu, v.re, kk), __shfl_sync(0xffffffffu, v.im, kk));
+                cx<R> yk = shfl_cx(v, kk);
                 if (lane < kk) v -= Dsm[lane * TB + kk] * yk;    // L[k0+kk, k0+lane]
             }
             if (lane < kb) wc[lane] = v;
         }
         __syncthreads();
+        if (k0 > 0) {
+            sweep(k0, k0 + kb, k0);                      // this block's rows update the own columns above it
+            __syncthreads();
+        }
     }
-    for (int q = tid; q < gc * nown; q += blockDim.x) {
+    for (int q = tid; q < gc * nown; q += nth) {
         int c = q / nown, r = q - c * nown;
         z[(int64_t)gs[c] * F.nfac + own0 + r] = w[c * ldw + r];
     }
 }
 
-template <typename R>
-static void smem_attr(const void* fn, size_t bytes) {
-    if (bytes > 48 * 1024) GT_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-}
 
-static int solve_threads(int max_nf) { return max_nf > 512 ? 1024 : max_nf > 192 ? 512 : 256; }
+static int block_threads(int max_nf) { return max_nf > 512 ? 1024 : max_nf > 192 ? 512 : 256; }
 
 template <typename R>
-void launch_fwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, const cx<R>* panel,
-                      cx<R>* z, cx<R>* uvec, const Groups& G, int gmax, cudaStream_t st) {
+void launch_fwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, int max_nown,
+                      const cx<R>* panel, cx<R>* z, cx<R>* uvec, const Groups& G, int gmax, cudaStream_t st) {
     if (gmax > GMAXC) throw CudaError{cudaErrorInvalidValue, "column group larger than the solve kernels take"};
-    const int ldw = max_nf | 1;
-    size_t sm = (size_t)(TB * TB + (size_t)ldw * GMAXC) * sizeof(cx<R>);
-    smem_attr<R>((const void*)fwd_level_kernel<R>, sm);
-    fwd_level_kernel<R><<<dim3(nf_level, G.ngroup), solve_threads(max_nf), sm, st>>>(F, front_list, panel, z, uvec, G, ldw);
+    const int ntask = nf_level * G.ngroup;
+    if (max_nf <= SMALL_NF && max_nown <= SMALL_NOWN) {
+        const size_t sm = (size_t)8 * GMAXC * SMALL_NF * sizeof(cx<R>);
+        smem_attr<R>((const void*)fwd_small_kernel<R>, sm);
+        fwd_small_kernel<R><<<ceil_div(ntask, 8), 256, sm, st>>>(F, front_list, ntask, panel, z, uvec, G);
+    } else {
+        const int ldw = max_nf | 1;
+        size_t sm = (size_t)(TB * TB + (size_t)GMAXC * ldw) * sizeof(cx<R>);
+        smem_attr<R>((const void*)fwd_block_kernel<R>, sm);
+        fwd_block_kernel<R><<<ntask, block_threads(max_nf), sm, st>>>(F, front_list, ntask, panel, z, uvec, G, ldw);
+    }
     GT_LAUNCH_CHECK();
 }
 
 template <typename R>
-void launch_bwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, const cx<R>* panel,
-                      cx<R>* z, const Groups& G, int gmax, cudaStream_t st) {
+void launch_bwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, int max_nown,
+                      const cx<R>* panel, const cx<R>* panel_rm, cx<R>* z, const Groups& G, int gmax, cudaStream_t st) {
     if (gmax > GMAXC) throw CudaError{cudaErrorInvalidValue, "column group larger than the solve kernels take"};
-    const int ldw = max_nf | 1;
-    size_t sm = (size_t)(TB * TB + (size_t)ldw * GMAXC) * sizeof(cx<R>);
-    smem_attr<R>((const void*)bwd_level_kernel<R>, sm);
-    bwd_level_kernel<R><<<dim3(nf_level, G.ngroup), solve_threads(max_nf), sm, st>>>(F, front_list, panel, z, G, ldw);
+    const int ntask = nf_level * G.ngroup;
+    if (max_nf <= SMALL_NF && max_nown <= SMALL_NOWN) {
+        const size_t sm = (size_t)8 * GMAXC * SMALL_NF * sizeof(cx<R>);
+        smem_attr<R>((const void*)bwd_small_kernel<R>, sm);
+        bwd_small_kernel<R><<<ceil_div(ntask, 8), 256, sm, st>>>(F, front_list, ntask, panel_rm, z, G);
+    } else {
+        const int ldw = max_nf | 1;
+        size_t sm = (size_t)(TB * TB + (size_t)GMAXC * ldw) * sizeof(cx<R>);
+        smem_attr<R>((const void*)bwd_block_kernel<R>, sm);
+        bwd_block_kernel<R><<<ntask, block_threads(max_nf), sm, st>>>(F, front_list, ntask, panel, panel_rm, z, G, ldw);
+    }
     GT_LAUNCH_CHECK();
 }
 
-template void launch_fwd_level<float>(const Fronts&, const int64_t*, int, int, const c32*, c32*, c32*, const Groups&, int, cudaStream_t);
-template void launch_fwd_level<double>(const Fronts&, const int64_t*, int, int, const c64*, c64*, c64*, const Groups&, int, cudaStream_t);
-template void launch_bwd_level<float>(const Fronts&, const int64_t*, int, int, const c32*, c32*, const Groups&, int, cudaStream_t);
-template void launch_bwd_level<double>(const Fronts&, const int64_t*, int, int, const c64*, c64*, const Groups&, int, cudaStream_t);
+template void launch_fwd_level<float>(const Fronts&, const int64_t*, int, int, int, const c32*, c32*, c32*, const Groups&, int, cudaStream_t);
+template void launch_fwd_level<double>(const Fronts&, const int64_t*, int, int, int, const c64*, c64*, c64*, const Groups&, int, cudaStream_t);
+template void launch_bwd_level<float>(const Fronts&, const int64_t*, int, int, int, const c32*, const c32*, c32*, const Groups&, int, cudaStream_t);
+template void launch_bwd_level<double>(const Fronts&, const int64_t*, int, int, int, const c64*, const c64*, c64*, const Groups&, int, cudaStream_t);
 
 }  // namespace gt

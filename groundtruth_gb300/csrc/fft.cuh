@@ -13,6 +13,12 @@
 
 namespace gt {
 
+// Shared-memory index of row element i: one padding slot per 32 elements, so that the power-of-two
+// strides of the Stockham stages fall on different banks.
+__device__ __forceinline__ int spad(int i) { return i + (i >> 5); }
+// row stride (elements) for rows of length P
+__host__ __device__ __forceinline__ int srow(int P) { return P + (P >> 5) + 1; }
+
 template <typename R> struct FftConst;
 template <> struct FftConst<float> { static constexpr float h = 0.70710678118654752440f, s3 = 0.86602540378443864676f; };
 template <> struct FftConst<double> { static constexpr double h = 0.70710678118654752440, s3 = 0.86602540378443864676; };
@@ -91,7 +97,7 @@ __device__ __forceinline__ void fft_stage(cx<R>* row, bool active, int P, int Ns
         int j = t + q * team;
         if (active && j < nbf) {
 #pragma unroll
-            for (int r = 0; r < RAD; ++r) v[q][r] = row[j + r * nbf];
+            for (int r = 0; r < RAD; ++r) v[q][r] = row[spad(j + r * nbf)];
         }
     }
     __syncthreads();
@@ -111,7 +117,7 @@ __device__ __forceinline__ void fft_stage(cx<R>* row, bool active, int P, int Ns
             dftr<R, INV, RAD>(v[q]);
             int base = (j / Ns) * Ns * RAD + k;
 #pragma unroll
-            for (int r = 0; r < RAD; ++r) row[base + r * Ns] = v[q][r];
+            for (int r = 0; r < RAD; ++r) row[spad(base + r * Ns)] = v[q][r];
         }
     }
     __syncthreads();

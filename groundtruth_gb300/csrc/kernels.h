@@ -91,7 +91,7 @@ void launch_assemble_s(const int64_t* ptr, const int* tab_idx, const double* coe
 // one elimination level: fronts front_list[0..nf) for each operator
 void launch_factor_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, const c64* svals,
                          c64* panel, c64* upd, int nops, int* status, cudaStream_t st);
-void launch_panel_to32(const c64* p64, c32* p32, int64_t n, cudaStream_t st);
+void launch_panel_convert(const Fronts& F, const c64* p64, c32* p32, c32* r32, c64* r64, int nops, cudaStream_t st);
 
 // triangular solves, per level; groups of columns sharing an operator
 struct Groups {
@@ -101,11 +101,11 @@ struct Groups {
     const int* op;
 };
 template <typename R>
-void launch_fwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, const cx<R>* panel,
-                      cx<R>* z, cx<R>* uvec, const Groups& G, int gmax, cudaStream_t st);
+void launch_fwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, int max_nown,
+                      const cx<R>* panel, cx<R>* z, cx<R>* uvec, const Groups& G, int gmax, cudaStream_t st);
 template <typename R>
-void launch_bwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, const cx<R>* panel,
-                      cx<R>* z, const Groups& G, int gmax, cudaStream_t st);
+void launch_bwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, int max_nown,
+                      const cx<R>* panel, const cx<R>* panel_rm, cx<R>* z, const Groups& G, int gmax, cudaStream_t st);
 
 // --- Krylov vector work (batched, one basis per slot)
 template <typename R>

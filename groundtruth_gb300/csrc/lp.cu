@@ -24,7 +24,7 @@ __global__ void __launch_bounds__(1024) lp_pass_a(const cx<R>* __restrict__ x, i
                           int rows, const cx<R>* __restrict__ tw, cx<R>* __restrict__ T, const int* __restrict__ col_list) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw);
-    const int stride = P1 + 1;
+    const int stride = srow(P1);
     const int i0 = blockIdx.x * rows;
     const int s = blockIdx.y;
     const int col = col_list ? col_list[blockIdx.z] : blockIdx.z;
@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(1024) lp_pass_a(const cx<R>* __restrict__ x, i
     for (int idx = threadIdx.x; idx < rows * P1; idx += blockDim.x) {
         int r = idx / P1, j = idx - r * P1;
         int i = i0 + r;
-        buf[r * stride + j] = (i < n0 && j < n1) ? xs[(int64_t)i * n1 + j] : zero<R>();
+        buf[r * stride + spad(j)] = (i < n0 && j < n1) ? xs[(int64_t)i * n1 + j] : zero<R>();
     }
     __syncthreads();
     const int team = P1 / 8;
@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(1024) lp_pass_a(const cx<R>* __restrict__ x, i
     for (int idx = threadIdx.x; idx < rows * P1; idx += blockDim.x) {
         int c = idx / rows, rr = idx - c * rows;
         int i = i0 + rr;
-        if (i < n0) Ts[(int64_t)c * n0 + i] = buf[rr * stride + c];
+        if (i < n0) Ts[(int64_t)c * n0 + i] = buf[rr * stride + spad(c)];
     }
 }
 
@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(1024) lp_pass_b(int S, int n0, int P0, int P1,
                           const cx<R>* __restrict__ tw, cx<R>* __restrict__ T) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw);
-    const int stride = P0 + 1;
+    const int stride = srow(P0);
     const int c = blockIdx.x;
     const int b0 = blockIdx.y * bt;
     const int nb = min(bt, ncol - b0);
@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(1024) lp_pass_b(int S, int n0, int P0, int P1,
     for (int idx = threadIdx.x; idx < nrows * P0; idx += blockDim.x) {
         int row = idx / P0, p = idx - row * P0;
         int b = row / S, s = row - b * S;
-        buf[row * stride + p] = p < n0 ? T[(((int64_t)(b0 + b) * S + s) * P1 + c) * n0 + p] : zero<R>();
+        buf[row * stride + spad(p)] = p < n0 ? T[(((int64_t)(b0 + b) * S + s) * P1 + c) * n0 + p] : zero<R>();
     }
     __syncthreads();
     const int team = P0 / 8;
@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(1024) lp_pass_b(int S, int n0, int P0, int P1,
         cx<R> u[MAXS];
 #pragma unroll
         for (int s = 0; s < MAXS; ++s)
-            if (s < S) u[s] = buf[(b * S + s) * stride + p];
+            if (s < S) u[s] = buf[(b * S + s) * stride + spad(p)];
 #pragma unroll
         for (int tt = 0; tt < MAXS; ++tt) {
             if (tt < S) {
@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(1024) lp_pass_b(int S, int n0, int P0, int P1,
                         acc.re += k * u[s].re;
                         acc.im += k * u[s].im;
                     }
-                buf[(b * S + tt) * stride + p] = acc;
+                buf[(b * S + tt) * stride + spad(p)] = acc;
             }
         }
     }
@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(1024) lp_pass_b(int S, int n0, int P0, int P1,
     for (int idx = threadIdx.x; idx < nrows * n0; idx += blockDim.x) {
         int rr = idx / n0, p = idx - rr * n0;
         int b = rr / S, s = rr - b * S;
-        T[(((int64_t)(b0 + b) * S + s) * P1 + c) * n0 + p] = buf[rr * stride + p];
+        T[(((int64_t)(b0 + b) * S + s) * P1 + c) * n0 + p] = buf[rr * stride + spad(p)];
     }
 }
 
@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(1024) lp_pass_c(const cx<R>* __restrict__ T, c
                           const int* __restrict__ col_list) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw);
-    const int stride = P1 + 1;
+    const int stride = srow(P1);
     const int i0 = blockIdx.x * rows;
     const int s = blockIdx.y;
     const int col = col_list ? col_list[blockIdx.z] : blockIdx.z;
@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(1024) lp_pass_c(const cx<R>* __restrict__ T, c
     for (int idx = threadIdx.x; idx < rows * P1; idx += blockDim.x) {
         int c = idx / rows, rr = idx - c * rows;
         int i = i0 + rr;
-        buf[rr * stride + c] = i < n0 ? Ts[(int64_t)c * n0 + i] : zero<R>();
+        buf[rr * stride + spad(c)] = i < n0 ? Ts[(int64_t)c * n0 + i] : zero<R>();
     }
     __syncthreads();
     const int team = P1 / 8;
@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(1024) lp_pass_c(const cx<R>* __restrict__ T, c
         int i = i0 + rr;
         if (i >= n0) continue;
         int64_t pos = off + ((int64_t)s * n0 + i) * n1 + j;
-        cx<R> L = buf[rr * stride + j];
+        cx<R> L = buf[rr * stride + spad(j)];
         cx<R> y;
         if (mode == 2) {
             y = mask[pos] ? L : zero<R>();
@@ -162,9 +162,9 @@ template <typename R>
 void lp_shapes(const LpArgs<R>& a, int* rows_out, int* bt_out) {
     const int teamA = a.P1 / 8, teamB = a.P0 / 8;
     int rows = a.rows > 0 ? a.rows : 4;
-    while (rows > 1 && (rows * teamA > 1024 || (size_t)rows * (a.P1 + 1) * sizeof(cx<R>) > 160 * 1024)) rows /= 2;
+    while (rows > 1 && (rows * teamA > 1024 || (size_t)rows * srow(a.P1) * sizeof(cx<R>) > 160 * 1024)) rows /= 2;
     int bt = a.bt > 0 ? a.bt : 2;
-    while (bt > 1 && (bt * a.S * teamB > 1024 || (size_t)bt * a.S * (a.P0 + 1) * sizeof(cx<R>) > 160 * 1024)) bt /= 2;
+    while (bt > 1 && (bt * a.S * teamB > 1024 || (size_t)bt * a.S * srow(a.P0) * sizeof(cx<R>) > 160 * 1024)) bt /= 2;
     *rows_out = rows;
     *bt_out = bt;
 }
@@ -174,12 +174,12 @@ void launch_lp(const LpArgs<R>& a, cudaStream_t st) {
     int rows, bt;
     lp_shapes<R>(a, &rows, &bt);
     const int teamA = a.P1 / 8, teamB = a.P0 / 8;
-    size_t smA = (size_t)rows * (a.P1 + 1) * sizeof(cx<R>);
+    size_t smA = (size_t)rows * srow(a.P1) * sizeof(cx<R>);
     dim3 gA(ceil_div(a.n0, rows), a.S, a.ncol);
     set_smem<R>((const void*)lp_pass_a<R>, smA);
     lp_pass_a<R><<<gA, rows * teamA, smA, st>>>(a.x, a.ld, a.off, a.S, a.n0, a.n1, a.P1, rows, a.tw1, a.T, a.col_list);
     GT_LAUNCH_CHECK();
-    size_t smB = (size_t)bt * a.S * (a.P0 + 1) * sizeof(cx<R>);
+    size_t smB = (size_t)bt * a.S * srow(a.P0) * sizeof(cx<R>);
     dim3 gB(a.P1, ceil_div(a.ncol, bt));
     set_smem<R>((const void*)lp_pass_b<R>, smB);
     lp_pass_b<R><<<gB, bt * a.S * teamB, smB, st>>>(a.S, a.n0, a.P0, a.P1, a.ncol, bt, a.spec, a.tw0, a.T);
