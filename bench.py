@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--outer-k", type=int, default=8, help="FP64 outer GCR directions kept (1: plain refinement)")
     ap.add_argument("--nets", type=int, default=0, help="use only the first N nets (0: all)")
     ap.add_argument("--freqs", type=int, default=0, help="use only every k-th frequency (0: all)")
+    ap.add_argument("--levels", action="store_true",
+                    help="also time each elimination level of the triangular solves (key 'solve_levels')")
     return ap.parse_args()
 
 
@@ -253,11 +255,14 @@ def run_gpu(args):
             zerr.append(abs(sol.Z_loop - Zr) / abs(Zr))
 
     # per-kernel-family timing (CUDA events on the launch stream) of one more step
-    st.handle.profile(True)
+    st.handle.profile(True, levels=args.levels)
     step()
     torch.cuda.synchronize()
     prof = st.handle.profile()
     st.handle.profile(False)
+    levels = {k: {"ms": round(v[0], 3), "GBps": round(v[1] / (v[0] * 1e-3) / 1e9, 1)}
+              for k, v in prof.items() if ".L" in k}
+    prof = {k: v for k, v in prof.items() if ".L" not in k}
     peak, peak_kind = peaks()
     fam = {k: v for k, v in prof.items() if v[1] > 0}
     top = max(fam, key=lambda k: fam[k][0])
@@ -317,6 +322,7 @@ def run_gpu(args):
                 "roofline": {"bound": "hbm", "kernel": top, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                              "frac": round(ach / peak, 4), "peak_kind": peak_kind, "traffic": None},
                 "kernel_families": per_family,
+                **({"solve_levels": levels} if levels else {}),
                 "e2e": e2e, "gpu_launches": launches // max(args.steps, 1) * args.steps,
                 "clocks": clk, "plain_fp64_gpu": plain, "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)

@@ -60,6 +60,7 @@ struct Pool {
 // Per-kernel-family timing with CUDA events on the launch stream (gt_profile).
 struct Profiler {
     bool on = false;
+    bool levels = false;   // also time each elimination level of the triangular solves
     struct Rec {
         int fam;
         cudaEvent_t a, b;
@@ -154,7 +155,8 @@ struct Workspace {
     c64* npart_k = nullptr;
     c64* nred = nullptr;
     // inner (precision R) per slot
-    void *V = nullptr, *w = nullptr, *z = nullptr, *T = nullptr, *zfac = nullptr, *uvec = nullptr;
+    void *V = nullptr, *w = nullptr, *z = nullptr, *T = nullptr, *zfac = nullptr, *yfac = nullptr, *uvec = nullptr,
+         *sd = nullptr;
     c64* partial = nullptr;
     GmresState st{};
     int *slot_col = nullptr, *slot_op = nullptr, *g_ptr = nullptr, *g_slot = nullptr, *g_op = nullptr, *col_op = nullptr;
@@ -184,6 +186,7 @@ struct gt_geometry {
     Pool pool;
     std::vector<int64_t> level_ptr;
     std::vector<int> level_maxnf, level_maxnown;
+    std::vector<double> level_panel;   // panel entries (sum of nf x nown) of each level
     int max_nf = 0;
     int64_t* d_order = nullptr;
     int64_t n_compact = 0;
@@ -203,10 +206,13 @@ struct gt_operators {
     Pool pool;
     double* omega = nullptr;
     c64 *zs = nullptr, *zcap = nullptr, *zbr = nullptr, *tab = nullptr;
+    // per front P = [Linv_own; -L_bnd Linv_own] (nf x nown) and the pivot reciprocals dinv ([op][nfac])
     c64* panel64 = nullptr;      // column-major per front (forward solves)
     c32* panel32 = nullptr;
     c64* panel64_rm = nullptr;   // row-major copies (backward solves)
     c32* panel32_rm = nullptr;
+    c64* dinv64 = nullptr;
+    c32* dinv32 = nullptr;
 };
 
 namespace gt {
@@ -231,6 +237,9 @@ template <> const c64* panel_of<double>(const gt_operators* ops) { return ops->p
 template <typename R> static const cx<R>* panel_rm_of(const gt_operators* ops);
 template <> const c32* panel_rm_of<float>(const gt_operators* ops) { return ops->panel32_rm; }
 template <> const c64* panel_rm_of<double>(const gt_operators* ops) { return ops->panel64_rm; }
+template <typename R> static const cx<R>* dinv_of(const gt_operators* ops);
+template <> const c32* dinv_of<float>(const gt_operators* ops) { return ops->dinv32; }
+template <> const c64* dinv_of<double>(const gt_operators* ops) { return ops->dinv64; }
 
 static bool good_fft_size(int P) {
     if (P < 8) return false;
@@ -333,7 +342,8 @@ static void matvec(gt_geometry* G, gt_operators* ops, const cx<R>* x, const cx<R
 // out = M^-1 r for nslot slots whose vectors are ldr apart (inputs) and ldo apart (outputs)
 template <typename R>
 static void precond(gt_geometry* G, gt_operators* ops, const cx<R>* r, int64_t ldr, cx<R>* out, int64_t ldo, int nslot,
-                    const int* slot_op, const Groups& grp, int gmax, cx<R>* zfac, cx<R>* uvec, cudaStream_t st,
+                    const int* slot_op, const Groups& grp, int gmax, cx<R>* zfac, cx<R>* yfac, cx<R>* uvec, cx<R>* sd,
+                    cudaStream_t st,
                     const int* col_list = nullptr) {
     Profiler* P = &G->prof;
     const double es = sizeof(cx<R>), n = (double)G->geo.n, nfac = (double)G->F.nfac;
@@ -342,7 +352,7 @@ static void precond(gt_geometry* G, gt_operators* ops, const cx<R>* r, int64_t l
     const double panel = (double)grp.ngroup * es * G->F.panel_total;
     {
         Scope s(P, "pc_node", st, nslot * es * (nXYC + nodes + nfac));
-        launch_pc_node<R>(G->geo, r, ldr, zfac, nslot, slot_op, ops->tab, col_list, st);
+        launch_pc_node<R>(G->geo, r, ldr, sd, nslot, slot_op, ops->tab, col_list, st);
     }
     const cx<R>* pan = panel_of<R>(ops);
     const int nlev = (int)G->level_ptr.size() - 1;
@@ -350,27 +360,31 @@ static void precond(gt_geometry* G, gt_operators* ops, const cx<R>* r, int64_t l
         Scope s(P, sizeof(R) == 4 ? "fwd_f32" : "fwd_f64", st, panel + nslot * es * (2 * nfac + 2.0 * G->F.vec_total));
         for (int h = 0; h < nlev; ++h) {
             int nf = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);
-            launch_fwd_level<R>(G->F, G->d_order + G->level_ptr[h], nf, G->level_maxnf[h], G->level_maxnown[h], pan, zfac,
-                                uvec, grp, gmax, st);
+            Scope sl(P->levels ? P : nullptr, (std::string(sizeof(R) == 4 ? "fwd_f32.L" : "fwd_f64.L") +
+                                               std::to_string(h)).c_str(), st, grp.ngroup * es * G->level_panel[h]);
+            launch_fwd_level<R>(G->F, G->d_order + G->level_ptr[h], nf, G->level_maxnf[h], G->level_maxnown[h], pan,
+                                dinv_of<R>(ops), sd, zfac, uvec, yfac, grp, gmax, st);
         }
     }
     {
         Scope s(P, sizeof(R) == 4 ? "bwd_f32" : "bwd_f64", st, panel + nslot * es * 2 * nfac);
         for (int h = nlev - 1; h >= 0; --h) {
             int nf = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);
+            Scope sl(P->levels ? P : nullptr, (std::string(sizeof(R) == 4 ? "bwd_f32.L" : "bwd_f64.L") +
+                                               std::to_string(h)).c_str(), st, grp.ngroup * es * G->level_panel[h]);
             launch_bwd_level<R>(G->F, G->d_order + G->level_ptr[h], nf, G->level_maxnf[h], G->level_maxnown[h],
-                                pan, panel_rm_of<R>(ops), zfac, grp, gmax, st);
+                                panel_rm_of<R>(ops), zfac, yfac, sd, grp, gmax, st);
         }
     }
     {
         Scope s(P, "pc_strip", st, nslot * es * (2 * n + nfac));
-        launch_pc_strip<R>(G->geo, r, ldr, zfac, out, ldo, nslot, slot_op, ops->tab, col_list, st);
+        launch_pc_strip<R>(G->geo, r, ldr, sd, out, ldo, nslot, slot_op, ops->tab, col_list, st);
     }
 }
 
 static int group_max(const gt_geometry* G, size_t elem) {
-    // the triangular-solve kernels hold a front's rows for 8 columns plus a 32 x 32 block in shared memory
-    if ((size_t)(32 * 32 + (size_t)G->max_nf * 8) * elem > 220 * 1024)
+    // the solve kernels hold a front's rows for 8 columns plus up to 16 warps' partial sums in shared memory
+    if ((size_t)(G->max_nf + 16 * 32) * 8 * elem > 220 * 1024)
         throw Invalid("a front is too large for the triangular-solve kernels' shared memory");
     return 8;
 }
@@ -424,7 +438,11 @@ static void ensure_ws(gt_geometry* G, int ncol, int m, int prec, int kmax) {
     W.z = p.alloc<unsigned char>((size_t)ncol * n * es);
     W.T = p.alloc<unsigned char>((size_t)ncol * G->maxT * es);
     W.zfac = p.alloc<unsigned char>((size_t)ncol * G->F.nfac * es);
+    W.yfac = p.alloc<unsigned char>((size_t)ncol * G->F.nfac * es);
     W.uvec = p.alloc<unsigned char>((size_t)ncol * std::max<int64_t>(G->F.vec_total, 1) * es);
+    // node-ordered s / y of the preconditioner: entries of nodes that are not kept stay zero
+    W.sd = p.alloc<unsigned char>((size_t)ncol * G->F.nnode * es);
+    GT_CUDA(cudaMemset(W.sd, 0, (size_t)ncol * G->F.nnode * es));
     W.partial = p.alloc<c64>((size_t)ncol * nch * (m + 2));
     GmresState& s = W.st;
     s.nslot = ncol;
@@ -500,7 +518,9 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
     cx<R>* z = static_cast<cx<R>*>(W.z);
     cx<R>* T = static_cast<cx<R>*>(W.T);
     cx<R>* zfac = static_cast<cx<R>*>(W.zfac);
+    cx<R>* yfac = static_cast<cx<R>*>(W.yfac);
     cx<R>* uvec = static_cast<cx<R>*>(W.uvec);
+    cx<R>* sd = static_cast<cx<R>*>(W.sd);
     const int64_t lds = (int64_t)(m + 1) * n;
     std::vector<int> slot_col, slot_op, gptr, gslot, gop, act;
     auto upload_groups = [&](const std::vector<int>& slots) {
@@ -567,7 +587,7 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
         for (int j = 0; j < m; ++j) {
             // the products run on the slots still iterating in this cycle (W.act, grp)
             const int na = (int)act.size();
-            precond<R>(G, ops, V + (int64_t)j * n, lds, z, n, na, W.slot_op, grp, gmax, zfac, uvec, st, W.act);
+            precond<R>(G, ops, V + (int64_t)j * n, lds, z, n, na, W.slot_op, grp, gmax, zfac, yfac, uvec, sd, st, W.act);
             matvec<R>(G, ops, z, nullptr, w, n, na, W.slot_op, 0, T, st, W.act);
             {
                 // classical Gram-Schmidt: the j+1 basis vectors read twice, w read twice and written once
@@ -615,7 +635,7 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
         act.resize(ns);
         for (int q = 0; q < ns; ++q) act[q] = q;
         grp = upload_groups(act);
-        precond<R>(G, ops, w, n, z, n, ns, W.slot_op, grp, gmax, zfac, uvec, st, W.act);
+        precond<R>(G, ops, w, n, z, n, ns, W.slot_op, grp, gmax, zfac, yfac, uvec, sd, st, W.act);
         // GCR step in FP64: p = the cycle's correction, q = K p, both orthogonalised against the directions
         // held (q orthonormal); then x += alpha p, r -= alpha q with alpha = q^H r
         if (k == K) k = 0;
@@ -862,15 +882,28 @@ int gt_geometry_create(const gt_geometry_desc* d, gt_geometry** out) {
     F.vec_total = d->vec_total;
     F.nsv = d->n_svalues;
     F.nfac = d->n_factor;
+    F.nnode = nn;
+    {
+        std::vector<int64_t> ip(std::max<int64_t>(d->n_factor, 1), 0);
+        for (int64_t node = 0; node < nn; ++node) {
+            int64_t fi = d->perm[node];
+            if (fi >= d->n_factor) throw Invalid("factor index out of range");
+            if (fi >= 0) ip[fi] = node;
+        }
+        F.iperm = p.upload(ip.data(), ip.size());
+    }
     G->level_ptr.assign(d->level_ptr, d->level_ptr + d->n_levels + 1);
     G->d_order = p.upload(d->front_order, nf);
     for (int h = 0; h < d->n_levels; ++h) {
         int mx = 1, mo = 1;
+        double ent = 0;
         for (int64_t q = d->level_ptr[h]; q < d->level_ptr[h + 1]; ++q) {
             int64_t f = d->front_order[q];
             mx = std::max<int>(mx, (int)(d->nown[f] + d->nbnd[f]));
             mo = std::max<int>(mo, (int)d->nown[f]);
+            ent += (double)(d->nown[f] + d->nbnd[f]) * d->nown[f];
         }
+        G->level_panel.push_back(ent);
         G->level_maxnf.push_back(mx);
         G->level_maxnown.push_back(mo);
         G->max_nf = std::max(G->max_nf, mx);
@@ -916,13 +949,19 @@ int gt_operators_create(gt_geometry* G, int32_t n_ops, const double* omega, cons
     O->panel32 = p.alloc<c32>((size_t)n_ops * F.panel_total);
     O->panel32_rm = p.alloc<c32>((size_t)n_ops * F.panel_total);
     O->panel64_rm = p.alloc<c64>((size_t)n_ops * F.panel_total);
+    O->dinv64 = p.alloc<c64>((size_t)n_ops * F.nfac);
+    O->dinv32 = p.alloc<c32>((size_t)n_ops * F.nfac);
     launch_assemble_s(G->d_sterm_ptr, G->d_sterm_tab, G->d_sterm_coef, F.nsv, O->tab, g.ntab, svals, n_ops, st);
     const int nlev = (int)G->level_ptr.size() - 1;
     for (int h = 0; h < nlev; ++h) {
         int nfl = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);
         launch_factor_level(F, G->d_order + G->level_ptr[h], nfl, G->level_maxnf[h], svals, O->panel64, upd, n_ops, status, st);
     }
-    launch_panel_convert(F, O->panel64, O->panel32, O->panel32_rm, O->panel64_rm, n_ops, st);
+    int max_nown = 1;
+    for (int h = 0; h < nlev; ++h) max_nown = std::max(max_nown, G->level_maxnown[h]);
+    launch_invert_own(F, O->panel64, max_nown, n_ops, st);
+    launch_bnd_inv(F, O->panel64, max_nown, n_ops, st);
+    launch_panel_convert(F, O->panel64, O->panel32, O->panel32_rm, O->panel64_rm, O->dinv64, O->dinv32, n_ops, st);
     int h_status = 0;
     GT_CUDA(cudaMemcpy(&h_status, status, sizeof(int), cudaMemcpyDeviceToHost));
     if (h_status) throw Invalid("the Schur complement has a zero or non-finite pivot (a piece of copper with no "
@@ -1053,8 +1092,11 @@ int gt_apply(gt_geometry* G, gt_operators* ops, int32_t kind, int32_t precision,
             int* g2 = tmp.upload(gop.data(), gop.size());
             Groups grp{(int)gop.size(), g0, g1, g2};
             cx<R>* zf = tmp.alloc<cx<R>>((size_t)n_cols * G->F.nfac);
+            cx<R>* yf = tmp.alloc<cx<R>>((size_t)n_cols * G->F.nfac);
             cx<R>* uv = tmp.alloc<cx<R>>((size_t)n_cols * std::max<int64_t>(G->F.vec_total, 1));
-            precond<R>(G, ops, xi, n, yo, n, n_cols, d_op, grp, gmax, zf, uv, st);
+            cx<R>* sdv = tmp.alloc<cx<R>>((size_t)n_cols * G->F.nnode);
+            GT_CUDA(cudaMemsetAsync(sdv, 0, (size_t)n_cols * G->F.nnode * sizeof(cx<R>), st));
+            precond<R>(G, ops, xi, n, yo, n, n_cols, d_op, grp, gmax, zf, yf, uv, sdv, st);
         }
         if constexpr (sizeof(R) == 4) {
             std::vector<c32> h32((size_t)n_cols * n);
@@ -1077,8 +1119,9 @@ int gt_apply(gt_geometry* G, gt_operators* ops, int32_t kind, int32_t precision,
 int gt_profile(gt_geometry* G, char* names, int32_t names_cap, double* ms, double* bytes, int32_t* launches,
                int32_t cap) {
     if (!G) return 0;
-    if (names == nullptr && cap < 0) {  // toggle: cap = -1 off, -2 on (and reset)
-        G->prof.on = cap == -2;
+    if (names == nullptr && cap < 0) {  // toggle: cap = -1 off, -2 on (and reset), -3 on with levels
+        G->prof.on = cap <= -2;
+        G->prof.levels = cap == -3;
         G->prof.acc.clear();
         return 0;
     }

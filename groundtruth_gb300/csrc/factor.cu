@@ -103,472 +103,471 @@ void launch_factor_level(const Fronts& F, const int64_t* front_list, int nf_leve
     GT_LAUNCH_CHECK();
 }
 
-// The factor's panels for the solves: FP32 column-major (forward), FP32 and FP64 row-major (backward).
-__global__ void panel_convert_kernel(Fronts F, const c64* __restrict__ p64, c32* __restrict__ p32, c32* __restrict__ r32,
-                                     c64* __restrict__ r64) {
+// Selective inversion: each front's own block (unit lower triangular, D on the diagonal kept as is) replaced
+// in place by its inverse, so that the solves need no sequential sweep through it.  Column k of the inverse,
+// from the last: X[i, k] = -L[i, k] - sum_{k < m < i} X[i, m] L[m, k] (i > k); the columns m > k are already
+// inverted and column k of L is saved in shared memory before it is overwritten.  FP64.
+__global__ void invert_own_kernel(Fronts F, c64* __restrict__ panel) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    c64* lk = reinterpret_cast<c64*>(smem_raw);
+    const int f = blockIdx.x;
+    const int op = blockIdx.y;
+    const int nown = (int)F.nown[f], nf = nown + (int)F.nbnd[f];
+    c64* L = panel + (int64_t)op * F.panel_total + F.panel_off[f];
+    for (int k = nown - 2; k >= 0; --k) {
+        for (int m = k + 1 + threadIdx.x; m < nown; m += blockDim.x) lk[m] = L[(int64_t)k * nf + m];
+        __syncthreads();
+        for (int i = k + 1 + threadIdx.x; i < nown; i += blockDim.x) {
+            c64 acc = mk<double>(-lk[i].re, -lk[i].im);
+            for (int m = k + 1; m < i; ++m) acc -= L[(int64_t)m * nf + i] * lk[m];
+            L[(int64_t)k * nf + i] = acc;
+        }
+        __syncthreads();
+    }
+}
+
+void launch_invert_own(const Fronts& F, c64* panel, int max_nown, int nops, cudaStream_t st) {
+    const size_t sm = (size_t)std::max(max_nown, 1) * sizeof(c64);
+    if (sm > 48 * 1024) GT_CUDA(cudaFuncSetAttribute((const void*)invert_own_kernel,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    invert_own_kernel<<<dim3(F.nfront, nops), 256, sm, st>>>(F, panel);
+    GT_LAUNCH_CHECK();
+}
+
+// Boundary rows of each front replaced by M = -L_bnd Linv_own (in place, FP64), column by column with k
+// ascending: column k of M needs the factor's boundary columns >= k, which are still unchanged.
+__global__ void bnd_inv_kernel(Fronts F, c64* __restrict__ panel) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    c64* lk = reinterpret_cast<c64*>(smem_raw);
+    const int f = blockIdx.x, op = blockIdx.y;
+    const int nown = (int)F.nown[f], nbnd = (int)F.nbnd[f], nf = nown + nbnd;
+    if (nbnd == 0) return;
+    c64* L = panel + (int64_t)op * F.panel_total + F.panel_off[f];
+    for (int k = 0; k < nown; ++k) {
+        for (int m = k + 1 + threadIdx.x; m < nown; m += blockDim.x) lk[m] = L[(int64_t)k * nf + m];
+        __syncthreads();
+        for (int j = nown + threadIdx.x; j < nf; j += blockDim.x) {
+            c64 acc = L[(int64_t)k * nf + j];
+            for (int m = k + 1; m < nown; ++m) acc += L[(int64_t)m * nf + j] * lk[m];
+            L[(int64_t)k * nf + j] = mk<double>(-acc.re, -acc.im);
+        }
+        __syncthreads();
+    }
+}
+
+void launch_bnd_inv(const Fronts& F, c64* panel, int max_nown, int nops, cudaStream_t st) {
+    const size_t sm = (size_t)std::max(max_nown, 1) * sizeof(c64);
+    if (sm > 48 * 1024) GT_CUDA(cudaFuncSetAttribute((const void*)bnd_inv_kernel,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    bnd_inv_kernel<<<dim3(F.nfront, nops), 256, sm, st>>>(F, panel);
+    GT_LAUNCH_CHECK();
+}
+
+// Finish the solve panels: the own block gets an explicit unit diagonal and zeros above it (the pivots go
+// to dinv as 1/D), and the FP32 column-major, FP32 / FP64 row-major copies are written.
+__global__ void panel_convert_kernel(Fronts F, c64* __restrict__ p64, c32* __restrict__ p32, c32* __restrict__ r32,
+                                     c64* __restrict__ r64, c64* __restrict__ d64, c32* __restrict__ d32) {
     const int f = blockIdx.x;
     const int op = blockIdx.y;
     const int nown = (int)F.nown[f], nf = nown + (int)F.nbnd[f];
     const int64_t base = (int64_t)op * F.panel_total + F.panel_off[f];
+    const int64_t dbase = (int64_t)op * F.nfac + F.own_start[f];
     for (int64_t q = threadIdx.x; q < (int64_t)nf * nown; q += blockDim.x) {
         int k = int(q / nf), i = int(q - (int64_t)k * nf);      // column-major element (i, k)
         c64 v = p64[base + q];
+        if (i < nown && i <= k) {
+            if (i == k) {
+                const c64 dv = cdiv(mk<double>(1.0, 0.0), v);
+                d64[dbase + i] = dv;
+                d32[dbase + i] = cvt<float>(dv);
+                v = mk<double>(1.0, 0.0);
+            } else {
+                v = zero<double>();
+            }
+            p64[base + q] = v;
+        }
         p32[base + q] = cvt<float>(v);
         r32[base + (int64_t)i * nown + k] = cvt<float>(v);
         r64[base + (int64_t)i * nown + k] = v;
     }
 }
 
-void launch_panel_convert(const Fronts& F, const c64* p64, c32* p32, c32* r32, c64* r64, int nops, cudaStream_t st) {
-    panel_convert_kernel<<<dim3(F.nfront, nops), 256, 0, st>>>(F, p64, p32, r32, r64);
+void launch_panel_convert(const Fronts& F, c64* p64, c32* p32, c32* r32, c64* r64, c64* d64, c32* d32, int nops,
+                          cudaStream_t st) {
+    panel_convert_kernel<<<dim3(F.nfront, nops), 256, 0, st>>>(F, p64, p32, r32, r64, d64, d32);
     GT_LAUNCH_CHECK();
 }
 
 // ------------------------------------------------------------------------------------------ solves
-// z: [col][nfac] in factor order; uvec: [col][vec_total] update vectors.  Two forms, chosen per level:
-//
-// small fronts (nf <= 128, nown <= 64): one warp per task (a front and a group of <= 8 columns sharing its
-//   operator), the front's rows in registers (row r on lane r mod 32), no block barrier.  Forward: a column
-//   sweep of the column-major panel with the next column's loads issued before the current one is used.
-//   Backward: a row sweep of the row-major copy: every boundary row (y known) updates the own rows, then the
-//   own rows from the last.
-// larger fronts: one block per task, w in shared memory [GMAXC][ldw]; the own block in blocks of 32 columns:
-//   the 32 x 32 diagonal block by one warp per column, warp-synchronously, the rest by sweeps in which each
-//   thread owns a row (forward, column-major panel) or a column (backward, row-major panel), every panel
-//   element read once, coalesced, 8 loads in flight per thread.
+// z, y: [col][nfac] in factor order; uvec: [col][vec_total] update vectors; sd: [col][S*nx*ny] in node order.
+// After the factorisation each front's panel holds P = [Linv_own; -L_bnd Linv_own] (nf x nown, unit
+// diagonal, zeros above it) and dinv = 1/D of its pivots (selective inversion), so that a front's solves are
+// two dense matrix-vector products without a sequential chain:
+//   forward   out = P w_own: own rows z_own = dinv * out, boundary rows w_bnd + out go up as the update
+//   backward  y_own = P^T [z_own; y_bnd]   (y_bnd: the ancestors' results, final)
+// A task is (front, group of <= 8 columns sharing its operator, block of rows / columns); its warps split
+// the block into 32-row (32-column) tiles and the product's inner dimension into segments whose partial sums
+// meet in shared memory.  The launch shape is chosen per level so that the top of the tree, with few fronts,
+// still spreads over every SM.  Panel elements are read once per task by consecutive lanes, LB loads in flight.
 constexpr int GMAXC = 8;
-constexpr int TB = 32;
-constexpr int RPL = 4;           // rows per lane of the small-front kernels (nf <= 128)
-constexpr int SMALL_NF = 32 * RPL;
-constexpr int SMALL_NOWN = 64;
+constexpr int LB = 8;
+constexpr int SOLVE_THREADS = 512;
 
 template <typename R>
 static void smem_attr(const void* fn, size_t bytes) {
     if (bytes > 48 * 1024) GT_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
 }
 
-template <typename R>
-__device__ __forceinline__ cx<R> shfl_cx(cx<R> v, int src) {
-    return mk<R>(__shfl_sync(0xffffffffu, v.re, src), __shfl_sync(0xffffffffu, v.im, src));
+// two consecutive columns' entries of a k-major shared vector (one 16-byte load in FP32)
+__device__ __forceinline__ void lds2(const c32* p, c32& a, c32& b) {
+    const float4 t = *reinterpret_cast<const float4*>(p);
+    a = mk<float>(t.x, t.y);
+    b = mk<float>(t.z, t.w);
+}
+__device__ __forceinline__ void lds2(const c64* p, c64& a, c64& b) {
+    a = p[0];
+    b = p[1];
 }
 
+// acc[c] += l[kk] * x[k_kk][c] for LB terms, x k-major ([k][GMAXC]); kidx[kk]: the terms' rows of x
 template <typename R>
-__global__ void __launch_bounds__(256) fwd_small_kernel(Fronts F, const int64_t* __restrict__ front_list, int ntask,
-                                                        const cx<R>* __restrict__ panel, cx<R>* __restrict__ z,
-                                                        cx<R>* __restrict__ uvec, Groups G) {
-    const int lane = threadIdx.x & 31;
-    const int task = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (task >= ntask) return;
-    const int g = task % G.ngroup;
-    const int f = (int)front_list[task / G.ngroup];
-    const int* gs = G.gslot + G.gptr[g];
-    const int gc = G.gptr[g + 1] - G.gptr[g], op = G.op[g];
-    const int nown = (int)F.nown[f], nbnd = (int)F.nbnd[f], nf = nown + nbnd;
+__device__ __forceinline__ void mac_batch(cx<R>* acc, const cx<R>* l, const cx<R>* x, const int* kidx, int gc) {
+#pragma unroll
+    for (int kk = 0; kk < LB; ++kk) {
+        const cx<R>* xk = x + kidx[kk] * GMAXC;
+#pragma unroll
+        for (int c2 = 0; c2 < GMAXC / 2; ++c2) {
+            if (2 * c2 >= gc) break;
+            cx<R> a, b;
+            lds2(xk + 2 * c2, a, b);
+            acc[2 * c2] += l[kk] * a;
+            acc[2 * c2 + 1] += l[kk] * b;
+        }
+    }
+}
+
+// The forward rows of front f for a group: own rows of w (node-ordered s plus the children's updates)
+// into ws (k-major, ldw = GMAXC) and boundary rows r0 <= p < r1 into wt ([c][TR]).  Loads are issued four
+// at a time per thread ahead of their stores.
+template <typename R>
+__device__ __forceinline__ void fwd_gather(const Fronts& F, int f, const int* gs, int gc, const cx<R>* __restrict__ sd,
+                                           const cx<R>* __restrict__ uvec, cx<R>* ws, cx<R>* wt, int TR, int r0, int r1) {
+    const int nown = (int)F.nown[f];
     const int64_t own0 = F.own_start[f];
-    const cx<R>* __restrict__ L = panel + (int64_t)op * F.panel_total + F.panel_off[f];
-    // stage the rows in the warp's shared-memory region: own entries of s, children's update vectors added
-    // one child at a time (their boundaries can share rows), then into registers
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    cx<R>* ws = reinterpret_cast<cx<R>*>(smem_raw) + (int64_t)(threadIdx.x >> 5) * GMAXC * SMALL_NF;
-    for (int c = 0; c < gc; ++c)
-        for (int r = lane; r < nf; r += 32)
-            ws[c * SMALL_NF + r] = r < nown ? z[(int64_t)gs[c] * F.nfac + own0 + r] : zero<R>();
-    __syncwarp();
-    for (int64_t ci = F.child_ptr[f]; ci < F.child_ptr[f + 1]; ++ci) {
-        const int ch = (int)F.child_idx[ci];
-        const int nb = (int)F.nbnd[ch];
-        const int64_t* map = F.cmap_idx + F.cmap_ptr[ci];
-        for (int c = 0; c < gc; ++c) {
-            const cx<R>* u = uvec + (int64_t)gs[c] * F.vec_total + F.vec_off[ch];
-            for (int i = lane; i < nb; i += 32) ws[c * SMALL_NF + map[i]] += u[i];
+    const int tid = threadIdx.x, nth = blockDim.x;
+    const int tot = gc * nown;
+    for (int q0 = tid; q0 < tot; q0 += 4 * nth) {
+        int64_t node[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int q = min(q0 + u * nth, tot - 1), r = q % nown;
+            node[u] = F.iperm[own0 + r];
         }
-        __syncwarp();
-    }
-    cx<R> w[RPL][GMAXC];
+        cx<R> v[4];
 #pragma unroll
-    for (int q = 0; q < RPL; ++q) {
-        const int r = lane + 32 * q;
-#pragma unroll
-        for (int c = 0; c < GMAXC; ++c) w[q][c] = (c < gc && r < nf) ? ws[c * SMALL_NF + r] : zero<R>();
-    }
-    cx<R> lc[RPL], ln[RPL];
-#pragma unroll
-    for (int q = 0; q < RPL; ++q) {
-        const int r = lane + 32 * q;
-        lc[q] = (nown > 0 && r < nf) ? L[r] : zero<R>();
-    }
-    for (int k = 0; k < nown; ++k) {
-        const int q_k = k >> 5, src = k & 31;
-#pragma unroll
-        for (int q = 0; q < RPL; ++q) {
-            const int r = lane + 32 * q;
-            ln[q] = (k + 1 < nown && r < nf) ? L[(int64_t)(k + 1) * nf + r] : zero<R>();
-        }
-        cx<R> zk[GMAXC];
-#pragma unroll
-        for (int c = 0; c < GMAXC; ++c) {
-            cx<R> mine = zero<R>();
-#pragma unroll
-            for (int q = 0; q < RPL; ++q)
-                if (q == q_k) mine = w[q][c];
-            zk[c] = shfl_cx(mine, src);
+        for (int u = 0; u < 4; ++u) {
+            const int q = min(q0 + u * nth, tot - 1), c = q / nown;
+            v[u] = sd[(int64_t)gs[c] * F.nnode + node[u]];
         }
 #pragma unroll
-        for (int q = 0; q < RPL; ++q) {
-            const int r = lane + 32 * q;
-            if (r > k && r < nf) {
-#pragma unroll
-                for (int c = 0; c < GMAXC; ++c)
-                    if (c < gc) w[q][c] -= lc[q] * zk[c];
-            }
+        for (int u = 0; u < 4; ++u) {
+            const int q = q0 + u * nth;
+            if (q < tot) ws[(q % nown) * GMAXC + q / nown] = v[u];
         }
-#pragma unroll
-        for (int q = 0; q < RPL; ++q) lc[q] = ln[q];
-    }
-#pragma unroll
-    for (int q = 0; q < RPL; ++q) {
-        const int r = lane + 32 * q;
-        if (r < nown) {
-            const cx<R> d = L[(int64_t)r * nf + r];
-#pragma unroll
-            for (int c = 0; c < GMAXC; ++c)
-                if (c < gc) z[(int64_t)gs[c] * F.nfac + own0 + r] = cdiv(w[q][c], d);
-        } else if (r < nf) {
-#pragma unroll
-            for (int c = 0; c < GMAXC; ++c)
-                if (c < gc) uvec[(int64_t)gs[c] * F.vec_total + F.vec_off[f] + (r - nown)] = w[q][c];
-        }
-    }
-}
-
-template <typename R>
-__global__ void __launch_bounds__(256) bwd_small_kernel(Fronts F, const int64_t* __restrict__ front_list, int ntask,
-                                                        const cx<R>* __restrict__ panel_rm, cx<R>* __restrict__ z,
-                                                        Groups G) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int lane = threadIdx.x & 31;
-    const int task = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (task >= ntask) return;
-    cx<R>* ws = reinterpret_cast<cx<R>*>(smem_raw) + (int64_t)(threadIdx.x >> 5) * GMAXC * SMALL_NF;
-    const int g = task % G.ngroup;
-    const int f = (int)front_list[task / G.ngroup];
-    const int* gs = G.gslot + G.gptr[g];
-    const int gc = G.gptr[g + 1] - G.gptr[g], op = G.op[g];
-    const int nown = (int)F.nown[f], nbnd = (int)F.nbnd[f], nf = nown + nbnd;
-    const int64_t own0 = F.own_start[f];
-    const int64_t* bnd = F.bnd_idx + F.bnd_ptr[f];
-    const cx<R>* __restrict__ L = panel_rm + (int64_t)op * F.panel_total + F.panel_off[f];   // (nf x nown) row-major
-    for (int c = 0; c < gc; ++c) {
-        const cx<R>* zc = z + (int64_t)gs[c] * F.nfac;
-        for (int r = lane; r < nf; r += 32) ws[c * SMALL_NF + r] = zc[r < nown ? own0 + r : bnd[r - nown]];
-    }
-    __syncwarp();
-    constexpr int OQ = SMALL_NOWN / 32;
-    // boundary rows (y final): acc_k = sum_i L[i, k] y_i, independent over i (4 rows of loads in flight)
-    cx<R> w[OQ][GMAXC];
-#pragma unroll
-    for (int q = 0; q < OQ; ++q)
-#pragma unroll
-        for (int c = 0; c < GMAXC; ++c) w[q][c] = zero<R>();
-    for (int i0 = nown; i0 < nf; i0 += 4) {
-        cx<R> l[4][OQ];
-#pragma unroll
-        for (int ii = 0; ii < 4; ++ii)
-#pragma unroll
-            for (int q = 0; q < OQ; ++q) {
-                const int k = lane + 32 * q, i = i0 + ii;
-                l[ii][q] = (i < nf && k < nown) ? L[(int64_t)i * nown + k] : zero<R>();
-            }
-#pragma unroll
-        for (int ii = 0; ii < 4; ++ii) {
-            const int i = min(i0 + ii, nf - 1);
-#pragma unroll
-            for (int c = 0; c < GMAXC; ++c) {
-                if (c >= gc) break;
-                const cx<R> y = ws[c * SMALL_NF + i];
-#pragma unroll
-                for (int q = 0; q < OQ; ++q) w[q][c] += l[ii][q] * y;
-            }
-        }
-    }
-#pragma unroll
-    for (int q = 0; q < OQ; ++q) {
-        const int k = lane + 32 * q;
-#pragma unroll
-        for (int c = 0; c < GMAXC; ++c) w[q][c] = (c < gc && k < nown) ? ws[c * SMALL_NF + k] - w[q][c] : zero<R>();
-    }
-    // own rows from the last: y_j final, own rows k < j updated
-    cx<R> lc[OQ], ln[OQ];
-#pragma unroll
-    for (int q = 0; q < OQ; ++q) {
-        const int k = lane + 32 * q;
-        lc[q] = (nown >= 2 && k < nown - 1) ? L[(int64_t)(nown - 1) * nown + k] : zero<R>();
-    }
-    for (int j = nown - 1; j >= 1; --j) {
-#pragma unroll
-        for (int q = 0; q < OQ; ++q) {
-            const int k = lane + 32 * q;
-            ln[q] = (j - 1 >= 1 && k < j - 1) ? L[(int64_t)(j - 1) * nown + k] : zero<R>();
-        }
-        const int q_j = j >> 5, src = j & 31;
-        cx<R> yj[GMAXC];
-#pragma unroll
-        for (int c = 0; c < GMAXC; ++c) {
-            cx<R> mine = zero<R>();
-#pragma unroll
-            for (int q = 0; q < OQ; ++q)
-                if (q == q_j) mine = w[q][c];
-            yj[c] = shfl_cx(mine, src);
-        }
-#pragma unroll
-        for (int q = 0; q < OQ; ++q) {
-            const int k = lane + 32 * q;
-            if (k < j) {
-#pragma unroll
-                for (int c = 0; c < GMAXC; ++c)
-                    if (c < gc) w[q][c] -= lc[q] * yj[c];
-            }
-        }
-#pragma unroll
-        for (int q = 0; q < OQ; ++q) lc[q] = ln[q];
-    }
-#pragma unroll
-    for (int q = 0; q < OQ; ++q) {
-        const int r = lane + 32 * q;
-        if (r < nown) {
-#pragma unroll
-            for (int c = 0; c < GMAXC; ++c)
-                if (c < gc) z[(int64_t)gs[c] * F.nfac + own0 + r] = w[q][c];
-        }
-    }
-}
-
-template <typename R>
-__device__ __forceinline__ void load_diag(cx<R>* Dsm, const cx<R>* __restrict__ L, int ld, int k0, int kb, bool rowmajor) {
-    // Dsm[c * TB + r] = L[k0 + r, k0 + c] (column c, row r of the diagonal block)
-    for (int q = threadIdx.x; q < TB * TB; q += blockDim.x) {
-        int c = q / TB, r = q - c * TB;
-        cx<R> v = zero<R>();
-        if (c < kb && r < kb) v = rowmajor ? L[(int64_t)(k0 + r) * ld + k0 + c] : L[(int64_t)(k0 + c) * ld + k0 + r];
-        Dsm[q] = v;
-    }
-}
-
-template <typename R>
-__global__ void __launch_bounds__(1024) fwd_block_kernel(Fronts F, const int64_t* __restrict__ front_list, int ntask,
-                                                         const cx<R>* __restrict__ panel, cx<R>* __restrict__ z,
-                                                         cx<R>* __restrict__ uvec, Groups G, int ldw) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    cx<R>* Dsm = reinterpret_cast<cx<R>*>(smem_raw);
-    cx<R>* w = Dsm + TB * TB;
-    const int task = blockIdx.x;
-    const int g = task % G.ngroup;
-    const int f = (int)front_list[task / G.ngroup];
-    const int* gs = G.gslot + G.gptr[g];
-    const int gc = G.gptr[g + 1] - G.gptr[g], op = G.op[g];
-    const int nown = (int)F.nown[f], nbnd = (int)F.nbnd[f], nf = nown + nbnd;
-    const int64_t own0 = F.own_start[f];
-    const cx<R>* __restrict__ L = panel + (int64_t)op * F.panel_total + F.panel_off[f];
-    const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, warp = tid >> 5;
-    for (int q = tid; q < gc * nf; q += nth) {
-        int c = q / nf, r = q - c * nf;
-        w[c * ldw + r] = r < nown ? z[(int64_t)gs[c] * F.nfac + own0 + r] : zero<R>();
     }
     __syncthreads();
     for (int64_t ci = F.child_ptr[f]; ci < F.child_ptr[f + 1]; ++ci) {
         const int ch = (int)F.child_idx[ci];
-        const int nb = (int)F.nbnd[ch];
+        const int nb = (int)F.nbnd[ch], tc = gc * nb;
         const int64_t* map = F.cmap_idx + F.cmap_ptr[ci];
-        for (int q = tid; q < nb * gc; q += nth) {
-            int c = q / nb, i = q - c * nb;
-            w[c * ldw + map[i]] += uvec[(int64_t)gs[c] * F.vec_total + F.vec_off[ch] + i];
+        const int64_t voff = F.vec_off[ch];
+        for (int q0 = tid; q0 < tc; q0 += 4 * nth) {
+            int p[4];
+            cx<R> v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int q = min(q0 + u * nth, tc - 1), c = q / nb, i = q - c * nb;
+                p[u] = (int)map[i];
+                v[u] = uvec[(int64_t)gs[c] * F.vec_total + voff + i];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int q = q0 + u * nth;
+                if (q >= tc) break;
+                const int c = q / nb;
+                if (p[u] < nown) ws[p[u] * GMAXC + c] += v[u];
+                else if (p[u] >= r0 && p[u] < r1) wt[c * TR + p[u] - r0] += v[u];
+            }
         }
         __syncthreads();
     }
-    for (int k0 = 0; k0 < nown; k0 += TB) {
-        const int kb = min(TB, nown - k0);
-        load_diag<R>(Dsm, L, nf, k0, kb, false);
-        __syncthreads();
-        if (warp < gc) {                                 // unit lower triangular solve of the block
-            cx<R>* wc = w + warp * ldw + k0;
-            cx<R> v = lane < kb ? wc[lane] : zero<R>();
-            for (int kk = 0; kk < kb - 1; ++kk) {
-                cx<R> zk = shfl_cx(v, kk);
-                if (lane > kk && lane < kb) v -= Dsm[kk * TB + lane] * zk;
-            }
-            if (lane < kb) wc[lane] = v;
+}
+
+// Forward assembly of a front split over several blocks, once per (front, group): w_own to wasm (factor
+// order), the children's updates of the boundary rows to the front's own update-vector slots.
+template <typename R>
+__global__ void __launch_bounds__(256) fwd_assemble_kernel(Fronts F, const int64_t* __restrict__ front_list,
+                                                           const cx<R>* __restrict__ sd, cx<R>* __restrict__ uvec,
+                                                           cx<R>* __restrict__ wasm, Groups G, int ldw, int TR) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<R>* ws = reinterpret_cast<cx<R>*>(smem_raw);   // [k][GMAXC]
+    cx<R>* wt = ws + GMAXC * ldw;                      // [c][TR] boundary rows
+    const int g = blockIdx.x % G.ngroup;
+    const int f = (int)front_list[blockIdx.x / G.ngroup];
+    const int* gs = G.gslot + G.gptr[g];
+    const int gc = G.gptr[g + 1] - G.gptr[g];
+    const int nown = (int)F.nown[f], nbnd = (int)F.nbnd[f], nf = nown + nbnd;
+    const int64_t own0 = F.own_start[f];
+    for (int q = threadIdx.x; q < GMAXC * TR; q += blockDim.x) wt[q] = zero<R>();
+    __syncthreads();
+    fwd_gather<R>(F, f, gs, gc, sd, uvec, ws, wt, TR, nown, nf);
+    for (int q = threadIdx.x; q < gc * nown; q += blockDim.x) {
+        const int c = q / nown, r = q - c * nown;
+        wasm[(int64_t)gs[c] * F.nfac + own0 + r] = ws[r * GMAXC + c];
+    }
+    for (int q = threadIdx.x; q < gc * nbnd; q += blockDim.x) {
+        const int c = q / nbnd, j = q - c * nbnd;
+        uvec[(int64_t)gs[c] * F.vec_total + F.vec_off[f] + j] = wt[c * TR + j];
+    }
+}
+
+// pre: the front was assembled by fwd_assemble_kernel (own rows in wasm, boundary rows in uvec)
+template <typename R>
+__global__ void __launch_bounds__(SOLVE_THREADS) fwd_gemv_kernel(Fronts F, const int64_t* __restrict__ front_list, int nblk,
+                                                                 int rt, int kseg, const cx<R>* __restrict__ panel,
+                                                                 const cx<R>* __restrict__ dinv, const cx<R>* __restrict__ sd,
+                                                                 cx<R>* __restrict__ z, cx<R>* __restrict__ uvec,
+                                                                 const cx<R>* __restrict__ wasm, Groups G, int ldw, int pre) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int TR = 32 * rt;
+    cx<R>* ws = reinterpret_cast<cx<R>*>(smem_raw);   // [k][GMAXC] own rows of w
+    cx<R>* wt = ws + GMAXC * ldw;                      // [c][TR] the block's boundary rows of w
+    cx<R>* red = wt + GMAXC * TR;                      // [seg][c][TR] partial sums
+    const int b = blockIdx.x % nblk, rest = blockIdx.x / nblk;
+    const int g = rest % G.ngroup;
+    const int f = (int)front_list[rest / G.ngroup];
+    const int nown = (int)F.nown[f], nf = nown + (int)F.nbnd[f];
+    const int r0 = b * TR;
+    if (r0 >= nf) return;
+    const int r1 = min(nf, r0 + TR);
+    const int* gs = G.gslot + G.gptr[g];
+    const int gc = G.gptr[g + 1] - G.gptr[g], op = G.op[g];
+    const int64_t own0 = F.own_start[f];
+    const int tid = threadIdx.x, nth = blockDim.x;
+    if (pre) {
+        for (int q = tid; q < gc * nown; q += nth) {
+            const int c = q / nown, r = q - c * nown;
+            ws[r * GMAXC + c] = wasm[(int64_t)gs[c] * F.nfac + own0 + r];
+        }
+        for (int q = tid; q < GMAXC * TR; q += nth) {
+            const int c = q / TR, rr = q - c * TR, row = r0 + rr;
+            wt[q] = (c < gc && row >= nown && row < r1)
+                        ? uvec[(int64_t)gs[c] * F.vec_total + F.vec_off[f] + (row - nown)] : zero<R>();
         }
         __syncthreads();
-        // rows below the block: w[c][i] -= sum_kk L[i, k0+kk] z[c][k0+kk], one thread per row
-        for (int i = k0 + kb + tid; i < nf; i += nth) {
-            cx<R> acc[GMAXC];
+    } else {
+        for (int q = tid; q < GMAXC * TR; q += nth) wt[q] = zero<R>();
+        __syncthreads();
+        fwd_gather<R>(F, f, gs, gc, sd, uvec, ws, wt, TR, r0, r1);
+    }
+    const cx<R>* __restrict__ P = panel + (int64_t)op * F.panel_total + F.panel_off[f];
+    const int lane = tid & 31, warp = tid >> 5;
+    const int tile = warp % rt, seg = warp / rt;
+    const int rl = tile * 32 + lane, r = r0 + rl;
+    // the tile's rows need columns k < min(nown, last row + 1) (P is zero above its diagonal)
+    const int kmax = min(nown, r0 + tile * 32 + 32);
+    const int ks = (kmax + kseg - 1) / kseg;
+    const int k0 = min(kmax, seg * ks), k1 = min(kmax, k0 + ks);
+    const bool valid = r < r1;
+    cx<R> acc[GMAXC];
 #pragma unroll
-            for (int c = 0; c < GMAXC; ++c) acc[c] = zero<R>();
-            const cx<R>* Li = L + (int64_t)k0 * nf + i;
-            for (int k8 = 0; k8 < kb; k8 += 8) {
-                cx<R> l[8];
+    for (int c = 0; c < GMAXC; ++c) acc[c] = zero<R>();
+    for (int k8 = k0; k8 < k1; k8 += LB) {
+        cx<R> l[LB];
+        int kidx[LB];
 #pragma unroll
-                for (int kk = 0; kk < 8; ++kk) l[kk] = k8 + kk < kb ? Li[(int64_t)(k8 + kk) * nf] : zero<R>();
+        for (int kk = 0; kk < LB; ++kk) {
+            const int k = k8 + kk;
+            l[kk] = (valid && k < k1) ? P[(int64_t)k * nf + r] : zero<R>();
+            kidx[kk] = min(k, k1 - 1);
+        }
+        mac_batch<R>(acc, l, ws, kidx, gc);
+    }
+    if (kseg > 1) {
 #pragma unroll
-                for (int kk = 0; kk < 8; ++kk)
-#pragma unroll
-                    for (int c = 0; c < GMAXC; ++c)
-                        if (c < gc) acc[c] += l[kk] * w[c * ldw + k0 + min(k8 + kk, kb - 1)];
-            }
+        for (int c = 0; c < GMAXC; ++c)
+            if (c < gc) red[(seg * GMAXC + c) * TR + rl] = acc[c];
+        __syncthreads();
+        for (int q = tid; q < gc * TR; q += nth) {
+            const int c = q / TR, rr = q - c * TR;
+            if (r0 + rr >= r1) continue;
+            cx<R> v = red[c * TR + rr];
+            for (int sg = 1; sg < kseg; ++sg) v += red[(sg * GMAXC + c) * TR + rr];
+            const int row = r0 + rr;
+            if (row < nown) z[(int64_t)gs[c] * F.nfac + own0 + row] = dinv[(int64_t)op * F.nfac + own0 + row] * v;
+            else uvec[(int64_t)gs[c] * F.vec_total + F.vec_off[f] + (row - nown)] = wt[c * TR + rr] + v;
+        }
+    } else if (valid) {
+        if (r < nown) {
+            const cx<R> dv = dinv[(int64_t)op * F.nfac + own0 + r];
 #pragma unroll
             for (int c = 0; c < GMAXC; ++c)
-                if (c < gc) w[c * ldw + i] -= acc[c];
+                if (c < gc) z[(int64_t)gs[c] * F.nfac + own0 + r] = dv * acc[c];
+        } else {
+#pragma unroll
+            for (int c = 0; c < GMAXC; ++c)
+                if (c < gc) uvec[(int64_t)gs[c] * F.vec_total + F.vec_off[f] + (r - nown)] = wt[c * TR + rl] + acc[c];
         }
-        __syncthreads();
-    }
-    for (int q = tid; q < gc * nf; q += nth) {
-        int c = q / nf, r = q - c * nf;
-        if (r < nown) z[(int64_t)gs[c] * F.nfac + own0 + r] = cdiv(w[c * ldw + r], L[(int64_t)r * nf + r]);
-        else uvec[(int64_t)gs[c] * F.vec_total + F.vec_off[f] + (r - nown)] = w[c * ldw + r];
     }
 }
 
 template <typename R>
-__global__ void __launch_bounds__(1024) bwd_block_kernel(Fronts F, const int64_t* __restrict__ front_list, int ntask,
-                                                         const cx<R>* __restrict__ panel, const cx<R>* __restrict__ panel_rm,
-                                                         cx<R>* __restrict__ z, Groups G, int ldw) {
+__global__ void __launch_bounds__(SOLVE_THREADS) bwd_gemv_kernel(Fronts F, const int64_t* __restrict__ front_list, int nblk,
+                                                                 int ct, int iseg, const cx<R>* __restrict__ panel_rm,
+                                                                 const cx<R>* __restrict__ z, cx<R>* __restrict__ y,
+                                                                 cx<R>* __restrict__ sd, Groups G, int ldv) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    cx<R>* Dsm = reinterpret_cast<cx<R>*>(smem_raw);
-    cx<R>* w = Dsm + TB * TB;
-    const int task = blockIdx.x;
-    const int g = task % G.ngroup;
-    const int f = (int)front_list[task / G.ngroup];
+    const int TC = 32 * ct;
+    cx<R>* v = reinterpret_cast<cx<R>*>(smem_raw);    // [i - kb0][GMAXC]: rows kb0 .. nf of [z_own; y_bnd]
+    cx<R>* red = v + GMAXC * ldv;                      // [seg][c][TC]
+    const int b = blockIdx.x % nblk, rest = blockIdx.x / nblk;
+    const int g = rest % G.ngroup;
+    const int f = (int)front_list[rest / G.ngroup];
+    const int nown = (int)F.nown[f], nf = nown + (int)F.nbnd[f];
+    const int kb0 = b * TC;
+    if (kb0 >= nown) return;
+    const int kb1 = min(nown, kb0 + TC);
     const int* gs = G.gslot + G.gptr[g];
     const int gc = G.gptr[g + 1] - G.gptr[g], op = G.op[g];
-    const int nown = (int)F.nown[f], nbnd = (int)F.nbnd[f], nf = nown + nbnd;
     const int64_t own0 = F.own_start[f];
     const int64_t* bnd = F.bnd_idx + F.bnd_ptr[f];
-    const cx<R>* __restrict__ L = panel_rm + (int64_t)op * F.panel_total + F.panel_off[f];   // (nf x nown) row-major
-    const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, warp = tid >> 5;
-    for (int q = tid; q < gc * nf; q += nth) {
-        int c = q / nf, r = q - c * nf;
-        w[c * ldw + r] = z[(int64_t)gs[c] * F.nfac + (r < nown ? own0 + r : bnd[r - nown])];
-    }
-    __syncthreads();
-    // w[c][k] -= sum_{rows j in [j0, j1)} L[j, k] y[c][j], one thread per own column k < kmax
-    auto sweep = [&](int j0, int j1, int kmax) {
-        for (int k = tid; k < kmax; k += nth) {
-            cx<R> acc[GMAXC];
+    const int tid = threadIdx.x, nth = blockDim.x;
+    const int nv = nf - kb0, tot = gc * nv;
+    for (int q0 = tid; q0 < tot; q0 += 4 * nth) {
+        int64_t src[4];
 #pragma unroll
-            for (int c = 0; c < GMAXC; ++c) acc[c] = zero<R>();
-            for (int j8 = j0; j8 < j1; j8 += 8) {
-                cx<R> l[8];
-#pragma unroll
-                for (int jj = 0; jj < 8; ++jj) l[jj] = j8 + jj < j1 ? L[(int64_t)(j8 + jj) * nown + k] : zero<R>();
-#pragma unroll
-                for (int jj = 0; jj < 8; ++jj)
-#pragma unroll
-                    for (int c = 0; c < GMAXC; ++c)
-                        if (c < gc) acc[c] += l[jj] * w[c * ldw + min(j8 + jj, j1 - 1)];
-            }
-#pragma unroll
-            for (int c = 0; c < GMAXC; ++c)
-                if (c < gc) w[c * ldw + k] -= acc[c];
+        for (int u = 0; u < 4; ++u) {
+            const int q = min(q0 + u * nth, tot - 1), c = q / nv, i = kb0 + (q - c * nv);
+            src[u] = (int64_t)gs[c] * F.nfac + (i < nown ? own0 + i : bnd[i - nown]);
         }
-    };
-    // the boundary rows (final from the ancestors): w[c][k] -= sum_{i >= nown} L[i, k] y[c][i] as column dot
-    // products of the column-major panel, one warp per own column k, lanes down the rows
-    {
-        const cx<R>* __restrict__ Lc = panel + (int64_t)op * F.panel_total + F.panel_off[f];
-        const int nwarp = nth >> 5;
-        for (int k = warp; k < nown; k += nwarp) {
-            const cx<R>* Lk = Lc + (int64_t)k * nf;
-            cx<R> acc[GMAXC];
+        cx<R> x[4];
 #pragma unroll
-            for (int c = 0; c < GMAXC; ++c) acc[c] = zero<R>();
-#pragma unroll 4
-            for (int i = nown + lane; i < nf; i += 32) {
-                const cx<R> l = Lk[i];
+        for (int u = 0; u < 4; ++u) {
+            const int q = min(q0 + u * nth, tot - 1), c = q / nv, i = kb0 + (q - c * nv);
+            x[u] = i < nown ? z[src[u]] : y[src[u]];
+        }
 #pragma unroll
-                for (int c = 0; c < GMAXC; ++c)
-                    if (c < gc) acc[c] += l * w[c * ldw + i];
-            }
-#pragma unroll
-            for (int c = 0; c < GMAXC; ++c) {
-                if (c >= gc) break;
-                R re = acc[c].re, im = acc[c].im;
-                for (int o = 16; o > 0; o >>= 1) {
-                    re += __shfl_xor_sync(0xffffffffu, re, o);
-                    im += __shfl_xor_sync(0xffffffffu, im, o);
-                }
-                if (lane == 0) w[c * ldw + k] -= mk<R>(re, im);
-            }
+        for (int u = 0; u < 4; ++u) {
+            const int q = q0 + u * nth;
+            if (q < tot) v[(q % nv) * GMAXC + q / nv] = x[u];
         }
     }
     __syncthreads();
-    const int nblk = (nown + TB - 1) / TB;
-    for (int b = nblk - 1; b >= 0; --b) {
-        const int k0 = b * TB, kb = min(TB, nown - k0);
-        load_diag<R>(Dsm, L, nown, k0, kb, true);
-        __syncthreads();
-        if (warp < gc) {                                 // unit upper (L^T) solve of the block from the bottom
-            cx<R>* wc = w + warp * ldw + k0;
-            cx<R> v = lane < kb ? wc[lane] : zero<R>();
-            for (int kk = kb - 1; kk > 0; --kk) {
-                cx<R> yk = shfl_cx(v, kk);
-                if (lane < kk) v -= Dsm[lane * TB + kk] * yk;    // L[k0+kk, k0+lane]
-            }
-            if (lane < kb) wc[lane] = v;
+    const cx<R>* __restrict__ P = panel_rm + (int64_t)op * F.panel_total + F.panel_off[f];   // (nf x nown) row-major
+    const int lane = tid & 31, warp = tid >> 5;
+    const int tile = warp % ct, seg = warp / ct;
+    const int kl = tile * 32 + lane, k = kb0 + kl;
+    // the tile's columns need rows i >= its first column (P is zero above its diagonal)
+    const int it0 = min(nf, kb0 + tile * 32);
+    const int is = (nf - it0 + iseg - 1) / iseg;
+    const int i0 = min(nf, it0 + seg * is), i1 = min(nf, i0 + is);
+    const bool valid = k < kb1;
+    cx<R> acc[GMAXC];
+#pragma unroll
+    for (int c = 0; c < GMAXC; ++c) acc[c] = zero<R>();
+    for (int i8 = i0; i8 < i1; i8 += LB) {
+        cx<R> l[LB];
+        int kidx[LB];
+#pragma unroll
+        for (int ii = 0; ii < LB; ++ii) {
+            const int i = i8 + ii;
+            l[ii] = (valid && i < i1) ? P[(int64_t)i * nown + k] : zero<R>();
+            kidx[ii] = min(i, i1 - 1) - kb0;
         }
-        __syncthreads();
-        if (k0 > 0) {
-            sweep(k0, k0 + kb, k0);                      // this block's rows update the own columns above it
-            __syncthreads();
-        }
+        mac_batch<R>(acc, l, v, kidx, gc);
     }
-    for (int q = tid; q < gc * nown; q += nth) {
-        int c = q / nown, r = q - c * nown;
-        z[(int64_t)gs[c] * F.nfac + own0 + r] = w[c * ldw + r];
+    if (iseg > 1) {
+#pragma unroll
+        for (int c = 0; c < GMAXC; ++c)
+            if (c < gc) red[(seg * GMAXC + c) * TC + kl] = acc[c];
+        __syncthreads();
+        for (int q = tid; q < gc * TC; q += nth) {
+            const int c = q / TC, kk = q - c * TC;
+            if (kb0 + kk >= kb1) continue;
+            cx<R> s = red[c * TC + kk];
+            for (int sg = 1; sg < iseg; ++sg) s += red[(sg * GMAXC + c) * TC + kk];
+            y[(int64_t)gs[c] * F.nfac + own0 + kb0 + kk] = s;
+            sd[(int64_t)gs[c] * F.nnode + F.iperm[own0 + kb0 + kk]] = s;
+        }
+    } else if (valid) {
+        const int64_t node = F.iperm[own0 + k];
+#pragma unroll
+        for (int c = 0; c < GMAXC; ++c)
+            if (c < gc) {
+                y[(int64_t)gs[c] * F.nfac + own0 + k] = acc[c];
+                sd[(int64_t)gs[c] * F.nnode + node] = acc[c];
+            }
     }
 }
 
-
-static int block_threads(int max_nf) { return max_nf > 512 ? 1024 : max_nf > 192 ? 512 : 256; }
+// Launch shape of a level: with enough (front, group) tasks to fill the GPU a block takes a whole small
+// front; otherwise a block takes one 32-row (32-column) tile and splits the inner dimension over warps.
+static void solve_shape(int ntask, int ntile, int inner, int& per_blk, int& nseg) {
+    const int fill = 8 * 152;
+    if ((int64_t)ntask * ntile >= fill && ntile <= 4 && (int64_t)ntask >= fill / 2) {
+        per_blk = ntile;
+        nseg = 1;
+    } else {
+        per_blk = 1;
+        nseg = std::max(1, std::min(SOLVE_THREADS / 32, (inner + 63) / 64));
+    }
+}
 
 template <typename R>
 void launch_fwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, int max_nown,
-                      const cx<R>* panel, cx<R>* z, cx<R>* uvec, const Groups& G, int gmax, cudaStream_t st) {
+                      const cx<R>* panel, const cx<R>* dinv, const cx<R>* sd, cx<R>* z, cx<R>* uvec, cx<R>* wasm,
+                      const Groups& G, int gmax, cudaStream_t st) {
     if (gmax > GMAXC) throw CudaError{cudaErrorInvalidValue, "column group larger than the solve kernels take"};
     const int ntask = nf_level * G.ngroup;
-    if (max_nf <= SMALL_NF && max_nown <= SMALL_NOWN) {
-        const size_t sm = (size_t)8 * GMAXC * SMALL_NF * sizeof(cx<R>);
-        smem_attr<R>((const void*)fwd_small_kernel<R>, sm);
-        fwd_small_kernel<R><<<ceil_div(ntask, 8), 256, sm, st>>>(F, front_list, ntask, panel, z, uvec, G);
-    } else {
-        const int ldw = max_nf | 1;
-        size_t sm = (size_t)(TB * TB + (size_t)GMAXC * ldw) * sizeof(cx<R>);
-        smem_attr<R>((const void*)fwd_block_kernel<R>, sm);
-        fwd_block_kernel<R><<<ntask, block_threads(max_nf), sm, st>>>(F, front_list, ntask, panel, z, uvec, G, ldw);
+    const int ntile = ceil_div(max_nf, 32);
+    int rt, kseg;
+    solve_shape(ntask, ntile, max_nown, rt, kseg);
+    const int nblk = ceil_div(ntile, rt), ldw = std::max(max_nown, 1);
+    const int pre = nblk > 1;
+    if (pre) {
+        const int TRa = std::max(max_nf - 1, 1);
+        const size_t sa = (size_t)GMAXC * (ldw + TRa) * sizeof(cx<R>);
+        smem_attr<R>((const void*)fwd_assemble_kernel<R>, sa);
+        fwd_assemble_kernel<R><<<ntask, 256, sa, st>>>(F, front_list, sd, uvec, wasm, G, ldw, TRa);
+        GT_LAUNCH_CHECK();
     }
+    const size_t sm = (size_t)GMAXC * (ldw + 32 * rt + (kseg > 1 ? kseg * 32 * rt : 0)) * sizeof(cx<R>);
+    smem_attr<R>((const void*)fwd_gemv_kernel<R>, sm);
+    fwd_gemv_kernel<R><<<ntask * nblk, 32 * rt * kseg, sm, st>>>(F, front_list, nblk, rt, kseg, panel, dinv, sd, z, uvec,
+                                                                wasm, G, ldw, pre);
     GT_LAUNCH_CHECK();
 }
 
 template <typename R>
 void launch_bwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, int max_nown,
-                      const cx<R>* panel, const cx<R>* panel_rm, cx<R>* z, const Groups& G, int gmax, cudaStream_t st) {
+                      const cx<R>* panel_rm, const cx<R>* z, cx<R>* y, cx<R>* sd, const Groups& G, int gmax,
+                      cudaStream_t st) {
     if (gmax > GMAXC) throw CudaError{cudaErrorInvalidValue, "column group larger than the solve kernels take"};
     const int ntask = nf_level * G.ngroup;
-    if (max_nf <= SMALL_NF && max_nown <= SMALL_NOWN) {
-        const size_t sm = (size_t)8 * GMAXC * SMALL_NF * sizeof(cx<R>);
-        smem_attr<R>((const void*)bwd_small_kernel<R>, sm);
-        bwd_small_kernel<R><<<ceil_div(ntask, 8), 256, sm, st>>>(F, front_list, ntask, panel_rm, z, G);
-    } else {
-        const int ldw = max_nf | 1;
-        size_t sm = (size_t)(TB * TB + (size_t)GMAXC * ldw) * sizeof(cx<R>);
-        smem_attr<R>((const void*)bwd_block_kernel<R>, sm);
-        bwd_block_kernel<R><<<ntask, block_threads(max_nf), sm, st>>>(F, front_list, ntask, panel, panel_rm, z, G, ldw);
-    }
+    const int ntile = ceil_div(max_nown, 32);
+    int ct, iseg;
+    solve_shape(ntask, ntile, max_nf, ct, iseg);
+    const int nblk = ceil_div(ntile, ct), ldv = std::max(max_nf, 1);
+    const size_t sm = (size_t)GMAXC * (ldv + (iseg > 1 ? iseg * 32 * ct : 0)) * sizeof(cx<R>);
+    smem_attr<R>((const void*)bwd_gemv_kernel<R>, sm);
+    bwd_gemv_kernel<R><<<ntask * nblk, 32 * ct * iseg, sm, st>>>(F, front_list, nblk, ct, iseg, panel_rm, z, y, sd, G,
+                                                                 ldv);
     GT_LAUNCH_CHECK();
 }
 
-template void launch_fwd_level<float>(const Fronts&, const int64_t*, int, int, int, const c32*, c32*, c32*, const Groups&, int, cudaStream_t);
-template void launch_fwd_level<double>(const Fronts&, const int64_t*, int, int, int, const c64*, c64*, c64*, const Groups&, int, cudaStream_t);
-template void launch_bwd_level<float>(const Fronts&, const int64_t*, int, int, int, const c32*, const c32*, c32*, const Groups&, int, cudaStream_t);
-template void launch_bwd_level<double>(const Fronts&, const int64_t*, int, int, int, const c64*, const c64*, c64*, const Groups&, int, cudaStream_t);
+template void launch_fwd_level<float>(const Fronts&, const int64_t*, int, int, int, const c32*, const c32*, const c32*, c32*, c32*, c32*, const Groups&, int, cudaStream_t);
+template void launch_fwd_level<double>(const Fronts&, const int64_t*, int, int, int, const c64*, const c64*, const c64*, c64*, c64*, c64*, const Groups&, int, cudaStream_t);
+template void launch_bwd_level<float>(const Fronts&, const int64_t*, int, int, int, const c32*, const c32*, c32*, c32*, const Groups&, int, cudaStream_t);
+template void launch_bwd_level<double>(const Fronts&, const int64_t*, int, int, int, const c64*, const c64*, c64*, c64*, const Groups&, int, cudaStream_t);
 
 }  // namespace gt

@@ -142,4 +142,62 @@ __device__ void fft_row(cx<R>* row, bool active, int P, const cx<R>* __restrict_
     else if (rest == 2) fft_stage<R, INV, 2>(row, active, P, Ns, tw, team, t);
 }
 
+
+// --- the same transform with the length known at compile time: every stride, plan step and index
+// division constant-folds (the runtime form above serves the lengths without a specialisation)
+template <typename R, bool INV, int RAD, int P, int NS>
+__device__ __forceinline__ void fft_stage_c(cx<R>* row, bool active, const cx<R>* __restrict__ tw, int t) {
+    constexpr int TEAM = P / 8;
+    constexpr int NB = (8 + RAD - 1) / RAD;
+    constexpr int NBF = P / RAD;
+    constexpr int STRIDE = P / (NS * RAD);
+    cx<R> v[NB][RAD];
+#pragma unroll
+    for (int q = 0; q < NB; ++q) {
+        const int j = t + q * TEAM;
+        if (active && j < NBF) {
+#pragma unroll
+            for (int r = 0; r < RAD; ++r) v[q][r] = row[spad(j + r * NBF)];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NB; ++q) {
+        const int j = t + q * TEAM;
+        if (active && j < NBF) {
+            const int k = j % NS;
+            if (NS > 1 && k) {
+#pragma unroll
+                for (int r = 1; r < RAD; ++r) {
+                    cx<R> w = tw[k * r * STRIDE];
+                    if (INV) w.im = -w.im;
+                    v[q][r] = v[q][r] * w;
+                }
+            }
+            dftr<R, INV, RAD>(v[q]);
+            const int base = (j / NS) * NS * RAD + k;
+#pragma unroll
+            for (int r = 0; r < RAD; ++r) row[spad(base + r * NS)] = v[q][r];
+        }
+    }
+    __syncthreads();
+}
+
+template <typename R, bool INV, int P, int NS>
+__device__ __forceinline__ void fft_stages_c(cx<R>* row, bool active, const cx<R>* __restrict__ tw, int t) {
+    constexpr int REST = P / NS;
+    if constexpr (REST > 1) {
+        constexpr int RAD = (NS == 1 && P % 3 == 0) ? 3 : (REST % 8 == 0 ? 8 : REST);
+        fft_stage_c<R, INV, RAD, P, NS>(row, active, tw, t);
+        fft_stages_c<R, INV, P, NS * RAD>(row, active, tw, t);
+    }
+}
+
+// P = 0: the runtime form with length p
+template <typename R, bool INV, int P>
+__device__ __forceinline__ void fft_row_t(cx<R>* row, bool active, int p, const cx<R>* __restrict__ tw, int team, int t) {
+    if constexpr (P == 0) fft_row<R, INV>(row, active, p, tw, team, t);
+    else fft_stages_c<R, INV, P, 1>(row, active, tw, t);
+}
+
 }  // namespace gt

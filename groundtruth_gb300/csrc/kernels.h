@@ -50,12 +50,13 @@ template <typename R>
 void launch_tail(const Geo& g, const cx<R>* x, const cx<R>* rhs, cx<R>* out, int64_t ld, int ncol, const int* col_op,
                  const c64* zcap, const c64* zbr, int mode, const int* col_list, cudaStream_t st);
 
-// preconditioner: s = r_V - Ar^T D^-1 r_1 into factor order; then out = [D^-1 (r_1 + Ar y); y]
+// preconditioner: s = r_V - Ar^T D^-1 r_1 into node order (sd [col][S*nx*ny]); then, with y in node order in
+// sd (zero at nodes that are not kept), out = [D^-1 (r_1 + Ar y); y]
 template <typename R>
-void launch_pc_node(const Geo& g, const cx<R>* r, int64_t ld, cx<R>* s_fac, int ncol, const int* col_op,
+void launch_pc_node(const Geo& g, const cx<R>* r, int64_t ld, cx<R>* sd, int ncol, const int* col_op,
                     const c64* tab, const int* col_list, cudaStream_t st);
 template <typename R>
-void launch_pc_strip(const Geo& g, const cx<R>* r, int64_t ldr, const cx<R>* y_fac, cx<R>* out, int64_t ldo, int ncol,
+void launch_pc_strip(const Geo& g, const cx<R>* r, int64_t ldr, const cx<R>* sd, cx<R>* out, int64_t ldo, int ncol,
                      const int* col_op, const c64* tab, const int* col_list, cudaStream_t st);
 
 // compact <-> dense
@@ -84,6 +85,8 @@ struct Fronts {
     const int* ent_col;
     const int64_t* ent_s;
     int64_t panel_total, upd_total, vec_total, nsv, nfac;
+    const int64_t* iperm;        // factor index -> dense node index
+    int64_t nnode;               // dense nodes S * nx * ny (the node-ordered vectors' length)
 };
 
 void launch_assemble_s(const int64_t* ptr, const int* tab_idx, const double* coef, int64_t nsv, const c64* table,
@@ -91,7 +94,14 @@ void launch_assemble_s(const int64_t* ptr, const int* tab_idx, const double* coe
 // one elimination level: fronts front_list[0..nf) for each operator
 void launch_factor_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, const c64* svals,
                          c64* panel, c64* upd, int nops, int* status, cudaStream_t st);
-void launch_panel_convert(const Fronts& F, const c64* p64, c32* p32, c32* r32, c64* r64, int nops, cudaStream_t st);
+// each front's own block replaced by its inverse (in place, FP64; the unit diagonal and the pivots untouched)
+void launch_invert_own(const Fronts& F, c64* panel, int max_nown, int nops, cudaStream_t st);
+// each front's boundary rows replaced by -L_bnd Linv_own (in place, FP64; after launch_invert_own)
+void launch_bnd_inv(const Fronts& F, c64* panel, int max_nown, int nops, cudaStream_t st);
+// the solve panels: own blocks get a unit diagonal and zeros above it (pivot reciprocals to d64 / d32,
+// [op][nfac]); FP32 column-major, FP32 and FP64 row-major copies
+void launch_panel_convert(const Fronts& F, c64* p64, c32* p32, c32* r32, c64* r64, c64* d64, c32* d32, int nops,
+                          cudaStream_t st);
 
 // triangular solves, per level; groups of columns sharing an operator
 struct Groups {
@@ -100,12 +110,17 @@ struct Groups {
     const int* gslot;
     const int* op;
 };
+// forward: own rows from s in node order (sd), results to z (factor order) and the update vectors (wasm:
+// factor-ordered scratch for fronts assembled ahead of a split product);
+// backward: reads z and the ancestors' y, writes y (factor order) and sd (node order)
 template <typename R>
 void launch_fwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, int max_nown,
-                      const cx<R>* panel, cx<R>* z, cx<R>* uvec, const Groups& G, int gmax, cudaStream_t st);
+                      const cx<R>* panel, const cx<R>* dinv, const cx<R>* sd, cx<R>* z, cx<R>* uvec, cx<R>* wasm,
+                      const Groups& G, int gmax, cudaStream_t st);
 template <typename R>
 void launch_bwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, int max_nown,
-                      const cx<R>* panel, const cx<R>* panel_rm, cx<R>* z, const Groups& G, int gmax, cudaStream_t st);
+                      const cx<R>* panel_rm, const cx<R>* z, cx<R>* y, cx<R>* sd, const Groups& G, int gmax,
+                      cudaStream_t st);
 
 // --- Krylov vector work (batched, one basis per slot)
 template <typename R>

@@ -19,7 +19,7 @@ namespace gt {
 
 constexpr int MAXS = 8;
 
-template <typename R>
+template <typename R, int PL>
 __global__ void __launch_bounds__(1024) lp_pass_a(const cx<R>* __restrict__ x, int64_t ldx, int64_t off, int S, int n0, int n1, int P1,
                           int rows, const cx<R>* __restrict__ tw, cx<R>* __restrict__ T, const int* __restrict__ col_list) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -37,7 +37,7 @@ __global__ void __launch_bounds__(1024) lp_pass_a(const cx<R>* __restrict__ x, i
     __syncthreads();
     const int team = P1 / 8;
     const int r = threadIdx.x / team, t = threadIdx.x - r * team;
-    fft_row<R, false>(buf + r * stride, r < rows, P1, tw, team, t);
+    fft_row_t<R, false, PL>(buf + r * stride, r < rows, P1, tw, team, t);
     cx<R>* Ts = T + ((int64_t)blockIdx.z * S + s) * (int64_t)P1 * n0;
     for (int idx = threadIdx.x; idx < rows * P1; idx += blockDim.x) {
         int c = idx / rows, rr = idx - c * rows;
@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(1024) lp_pass_a(const cx<R>* __restrict__ x, i
     }
 }
 
-template <typename R>
+template <typename R, int PL>
 __global__ void __launch_bounds__(1024) lp_pass_b(int S, int n0, int P0, int P1, int ncol, int bt, const R* __restrict__ spec,
                           const cx<R>* __restrict__ tw, cx<R>* __restrict__ T) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(1024) lp_pass_b(int S, int n0, int P0, int P1,
     __syncthreads();
     const int team = P0 / 8;
     const int row = threadIdx.x / team, t = threadIdx.x - row * team;
-    fft_row<R, false>(buf + row * stride, row < nrows, P0, tw, team, t);
+    fft_row_t<R, false, PL>(buf + row * stride, row < nrows, P0, tw, team, t);
     // spectrum multiply-add over sheets, one (column, pixel) per thread iteration
     const int Q0 = P0 / 2 + 1;
     const int q1 = min(c, P1 - c);
@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(1024) lp_pass_b(int S, int n0, int P0, int P1,
         }
     }
     __syncthreads();
-    fft_row<R, true>(buf + row * stride, row < nrows, P0, tw, team, t);
+    fft_row_t<R, true, PL>(buf + row * stride, row < nrows, P0, tw, team, t);
     for (int idx = threadIdx.x; idx < nrows * n0; idx += blockDim.x) {
         int rr = idx / n0, p = idx - rr * n0;
         int b = rr / S, s = rr - b * S;
@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(1024) lp_pass_b(int S, int n0, int P0, int P1,
 }
 
 // mode 0: out = R_t x + j w L - (V[a] - V[b]); 1: out = rhs - (that); 2: out = L
-template <typename R>
+template <typename R, int PL>
 __global__ void __launch_bounds__(1024) lp_pass_c(const cx<R>* __restrict__ T, const cx<R>* __restrict__ x, const cx<R>* __restrict__ rhs,
                           cx<R>* __restrict__ out, int64_t ld, int64_t off, int64_t off_v, int S, int n0, int n1,
                           int nx, int ny, int di, int dj, int P1, int rows, const cx<R>* __restrict__ tw,
@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(1024) lp_pass_c(const cx<R>* __restrict__ T, c
     __syncthreads();
     const int team = P1 / 8;
     const int r = threadIdx.x / team, t = threadIdx.x - r * team;
-    fft_row<R, true>(buf + r * stride, r < rows, P1, tw, team, t);
+    fft_row_t<R, true, PL>(buf + r * stride, r < rows, P1, tw, team, t);
     const int op = col_op ? col_op[col] : 0;
     const R w = omega ? R(omega[op]) : R(0);
     const cx<R> z = zs ? cvt<R>(zs[(int64_t)op * S + s]) : zero<R>();
@@ -169,26 +169,64 @@ void lp_shapes(const LpArgs<R>& a, int* rows_out, int* bt_out) {
     *bt_out = bt;
 }
 
+// the specialised lengths; others run the runtime-length kernels
+#define GT_LP_LENGTHS(X) X(64) X(96) X(128) X(192) X(256) X(384) X(512) X(768) X(1024) X(1536) X(2048)
+
+template <typename R, int PA>
+static void launch_a(const LpArgs<R>& a, int rows, cudaStream_t st) {
+    size_t smA = (size_t)rows * srow(a.P1) * sizeof(cx<R>);
+    dim3 gA(ceil_div(a.n0, rows), a.S, a.ncol);
+    set_smem<R>((const void*)lp_pass_a<R, PA>, smA);
+    lp_pass_a<R, PA><<<gA, rows * (a.P1 / 8), smA, st>>>(a.x, a.ld, a.off, a.S, a.n0, a.n1, a.P1, rows, a.tw1, a.T,
+                                                          a.col_list);
+    GT_LAUNCH_CHECK();
+}
+
+template <typename R, int PB>
+static void launch_b(const LpArgs<R>& a, int bt, cudaStream_t st) {
+    size_t smB = (size_t)bt * a.S * srow(a.P0) * sizeof(cx<R>);
+    dim3 gB(a.P1, ceil_div(a.ncol, bt));
+    set_smem<R>((const void*)lp_pass_b<R, PB>, smB);
+    lp_pass_b<R, PB><<<gB, bt * a.S * (a.P0 / 8), smB, st>>>(a.S, a.n0, a.P0, a.P1, a.ncol, bt, a.spec, a.tw0, a.T);
+    GT_LAUNCH_CHECK();
+}
+
+template <typename R, int PA>
+static void launch_c(const LpArgs<R>& a, int rows, cudaStream_t st) {
+    size_t smA = (size_t)rows * srow(a.P1) * sizeof(cx<R>);
+    dim3 gA(ceil_div(a.n0, rows), a.S, a.ncol);
+    set_smem<R>((const void*)lp_pass_c<R, PA>, smA);
+    lp_pass_c<R, PA><<<gA, rows * (a.P1 / 8), smA, st>>>(a.T, a.x, a.rhs, a.out, a.ld, a.off, a.off_v, a.S, a.n0, a.n1,
+                                                          a.nx, a.ny, a.di, a.dj, a.P1, rows, a.tw1, a.mask, a.col_op,
+                                                          a.omega, a.zs, a.mode, a.col_list);
+    GT_LAUNCH_CHECK();
+}
+
 template <typename R>
 void launch_lp(const LpArgs<R>& a, cudaStream_t st) {
     int rows, bt;
     lp_shapes<R>(a, &rows, &bt);
-    const int teamA = a.P1 / 8, teamB = a.P0 / 8;
-    size_t smA = (size_t)rows * srow(a.P1) * sizeof(cx<R>);
-    dim3 gA(ceil_div(a.n0, rows), a.S, a.ncol);
-    set_smem<R>((const void*)lp_pass_a<R>, smA);
-    lp_pass_a<R><<<gA, rows * teamA, smA, st>>>(a.x, a.ld, a.off, a.S, a.n0, a.n1, a.P1, rows, a.tw1, a.T, a.col_list);
-    GT_LAUNCH_CHECK();
-    size_t smB = (size_t)bt * a.S * srow(a.P0) * sizeof(cx<R>);
-    dim3 gB(a.P1, ceil_div(a.ncol, bt));
-    set_smem<R>((const void*)lp_pass_b<R>, smB);
-    lp_pass_b<R><<<gB, bt * a.S * teamB, smB, st>>>(a.S, a.n0, a.P0, a.P1, a.ncol, bt, a.spec, a.tw0, a.T);
-    GT_LAUNCH_CHECK();
-    set_smem<R>((const void*)lp_pass_c<R>, smA);
-    lp_pass_c<R><<<gA, rows * teamA, smA, st>>>(a.T, a.x, a.rhs, a.out, a.ld, a.off, a.off_v, a.S, a.n0, a.n1, a.nx, a.ny,
-                                                a.di, a.dj, a.P1, rows, a.tw1, a.mask, a.col_op, a.omega, a.zs, a.mode,
-                                                a.col_list);
-    GT_LAUNCH_CHECK();
+    switch (a.P1) {
+#define GT_CASE(L) \
+    case L: launch_a<R, L>(a, rows, st); break;
+        GT_LP_LENGTHS(GT_CASE)
+#undef GT_CASE
+        default: launch_a<R, 0>(a, rows, st);
+    }
+    switch (a.P0) {
+#define GT_CASE(L) \
+    case L: launch_b<R, L>(a, bt, st); break;
+        GT_LP_LENGTHS(GT_CASE)
+#undef GT_CASE
+        default: launch_b<R, 0>(a, bt, st);
+    }
+    switch (a.P1) {
+#define GT_CASE(L) \
+    case L: launch_c<R, L>(a, rows, st); break;
+        GT_LP_LENGTHS(GT_CASE)
+#undef GT_CASE
+        default: launch_c<R, 0>(a, rows, st);
+    }
 }
 
 template void launch_lp<float>(const LpArgs<float>&, cudaStream_t);

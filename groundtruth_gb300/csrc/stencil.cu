@@ -107,7 +107,7 @@ void launch_tail(const Geo& g, const cx<R>* x, const cx<R>* rhs, cx<R>* out, int
 
 // s[perm[node]] = r_V[node] - (Ar^T D^-1 r_1)[node] for every kept node
 template <typename R>
-__global__ void pc_node_kernel(Geo g, const cx<R>* __restrict__ r, int64_t ld, cx<R>* __restrict__ s_fac,
+__global__ void pc_node_kernel(Geo g, const cx<R>* __restrict__ r, int64_t ld, cx<R>* __restrict__ sd,
                                const int* __restrict__ col_op, const c64* __restrict__ tab, const int* __restrict__ col_list) {
     const int col = col_list ? col_list[blockIdx.y] : blockIdx.y;
     const int op = col_op ? col_op[col] : 0;
@@ -116,8 +116,7 @@ __global__ void pc_node_kernel(Geo g, const cx<R>* __restrict__ r, int64_t ld, c
     const int S = g.S, nx = g.nx, ny = g.ny;
     const int64_t nxy = (int64_t)nx * ny;
     for (int64_t node = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; node < S * nxy; node += (int64_t)gridDim.x * blockDim.x) {
-        int64_t f = g.perm[node];
-        if (f < 0) continue;
+        if (!g.mask[g.off_v + node]) continue;
         int k = int(node / nxy);
         int64_t ij = node - k * nxy;
         int i = int(ij / ny), j = int(ij - (int64_t)i * ny);
@@ -158,36 +157,33 @@ __global__ void pc_node_kernel(Geo g, const cx<R>* __restrict__ r, int64_t ld, c
             cx<R> t = cvt<R>(T[g.tab_br0 + bb]) * rc[g.off_b + bb];
             if (b > 0) kcl += t; else kcl -= t;
         }
-        s_fac[(int64_t)col * g.nfac + f] = rc[g.off_v + node] - kcl;
+        sd[(int64_t)col * S * nxy + node] = rc[g.off_v + node] - kcl;
     }
 }
 
 template <typename R>
-void launch_pc_node(const Geo& g, const cx<R>* r, int64_t ld, cx<R>* s_fac, int ncol, const int* col_op, const c64* tab,
+void launch_pc_node(const Geo& g, const cx<R>* r, int64_t ld, cx<R>* sd, int ncol, const int* col_op, const c64* tab,
                     const int* col_list, cudaStream_t st) {
     int64_t items = (int64_t)g.S * g.nx * g.ny;
     int blocks = (int)std::min<int64_t>((items + 255) / 256, 4096);
-    pc_node_kernel<R><<<dim3(blocks, ncol), 256, 0, st>>>(g, r, ld, s_fac, col_op, tab, col_list);
+    pc_node_kernel<R><<<dim3(blocks, ncol), 256, 0, st>>>(g, r, ld, sd, col_op, tab, col_list);
     GT_LAUNCH_CHECK();
 }
 
 // out = [D^-1 (r_1 + Ar y); y] over the whole dense vector (padding written zero)
 template <typename R>
-__global__ void pc_strip_kernel(Geo g, const cx<R>* __restrict__ r, int64_t ldr, const cx<R>* __restrict__ y_fac,
+__global__ void pc_strip_kernel(Geo g, const cx<R>* __restrict__ r, int64_t ldr, const cx<R>* __restrict__ sd,
                                 cx<R>* __restrict__ out, int64_t ldo, const int* __restrict__ col_op,
                                 const c64* __restrict__ tab, const int* __restrict__ col_list) {
     const int col = col_list ? col_list[blockIdx.y] : blockIdx.y;
     const int op = col_op ? col_op[col] : 0;
     const c64* T = tab + (int64_t)op * g.ntab;
     const cx<R>* rc = r + (int64_t)col * ldr;
-    const cx<R>* yc = y_fac + (int64_t)col * g.nfac;
+    const cx<R>* yc = sd + (int64_t)col * g.S * g.nx * g.ny;
     const int S = g.S, nx = g.nx, ny = g.ny;
     const int64_t nxy = (int64_t)nx * ny;
     const int64_t nX = (int64_t)S * (nx - 1) * ny, nY = (int64_t)S * nx * (ny - 1);
-    auto yv = [&](int64_t node) -> cx<R> {
-        int64_t f = g.perm[node];
-        return f >= 0 ? yc[f] : zero<R>();
-    };
+    auto yv = [&](int64_t node) -> cx<R> { return yc[node]; };     // zero at nodes that are not kept
     for (int64_t pos = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; pos < g.n; pos += (int64_t)gridDim.x * blockDim.x) {
         int seg = seg_of(g, pos, nX, nY);
         cx<R> o = zero<R>();
@@ -230,10 +226,10 @@ __global__ void pc_strip_kernel(Geo g, const cx<R>* __restrict__ r, int64_t ldr,
 }
 
 template <typename R>
-void launch_pc_strip(const Geo& g, const cx<R>* r, int64_t ldr, const cx<R>* y_fac, cx<R>* out, int64_t ldo, int ncol,
+void launch_pc_strip(const Geo& g, const cx<R>* r, int64_t ldr, const cx<R>* sd, cx<R>* out, int64_t ldo, int ncol,
                      const int* col_op, const c64* tab, const int* col_list, cudaStream_t st) {
     int blocks = (int)std::min<int64_t>((g.n + 255) / 256, 4096);
-    pc_strip_kernel<R><<<dim3(blocks, ncol), 256, 0, st>>>(g, r, ldr, y_fac, out, ldo, col_op, tab, col_list);
+    pc_strip_kernel<R><<<dim3(blocks, ncol), 256, 0, st>>>(g, r, ldr, sd, out, ldo, col_op, tab, col_list);
     GT_LAUNCH_CHECK();
 }
 

@@ -181,16 +181,17 @@ class Geometry:
                                                P(stream)), "gt_to_compact")
         return out
 
-    def profile(self, on: bool | None = None) -> dict:
-        """Toggle (on=True/False: reset) or read {kernel family: (ms, algorithmic bytes, timed regions)}."""
+    def profile(self, on: bool | None = None, levels: bool = False) -> dict:
+        """Toggle (on=True/False: reset; levels: time each elimination level too) or read
+        {kernel family: (ms, algorithmic bytes, timed regions)}."""
         if on is not None:
-            self.lib.gt_profile(self.h, None, 0, None, None, None, -2 if on else -1)
+            self.lib.gt_profile(self.h, None, 0, None, None, None, (-3 if levels else -2) if on else -1)
             return {}
-        cap = 64
-        names = C.create_string_buffer(4096)
+        cap = 128
+        names = C.create_string_buffer(16384)
         ms, by = np.zeros(cap), np.zeros(cap)
         launches = np.zeros(cap, np.int32)
-        k = self.lib.gt_profile(self.h, names, 4096, _ptr(ms, C.c_double), _ptr(by, C.c_double),
+        k = self.lib.gt_profile(self.h, names, 16384, _ptr(ms, C.c_double), _ptr(by, C.c_double),
                                 _ptr(launches, C.c_int32), cap)
         keys = names.value.decode().split(",") if k else []
         return {n: (float(ms[i]), float(by[i]), int(launches[i])) for i, n in enumerate(keys)}

@@ -147,7 +147,9 @@ int gt_apply(gt_geometry* g, gt_operators* ops, int32_t kind, int32_t precision,
 int gt_lp_product_noalloc(gt_geometry* g, int32_t n_cols, const void* x_device, void* y_device, void* stream);
 
 /* Per-kernel-family timing of the solves on this geometry, by CUDA events on the launch stream.
- * names == NULL and cap == -2: reset and switch timing on; cap == -1: switch it off.  Otherwise fills
+ * names == NULL and cap == -2: reset and switch timing on; cap == -3: the same, with each elimination level
+ * of the triangular solves also timed as a family of its own ("fwd_f32.L<h>"); cap == -1: switch it off.
+ * Otherwise fills
  * names (comma separated), ms (milliseconds), bytes (algorithmic bytes moved) and launches (timed
  * regions) per family, up to cap families, and returns their count. */
 int gt_profile(gt_geometry* g, char* names, int32_t names_cap, double* ms, double* bytes, int32_t* launches,
