@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--outer-k", type=int, default=8, help="FP64 outer GCR directions kept (1: plain refinement)")
     ap.add_argument("--nets", type=int, default=0, help="use only the first N nets (0: all)")
     ap.add_argument("--freqs", type=int, default=0, help="use only every k-th frequency (0: all)")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "mixed16"],
+                    help="inner GMRES: FP32 with an FP32 (mixed) or FP16 (mixed16) Krylov basis")
     ap.add_argument("--levels", action="store_true",
                     help="also time each elimination level of the triangular solves (key 'solve_levels')")
     return ap.parse_args()
@@ -205,7 +207,7 @@ def run_gpu(args):
     X = torch.zeros_like(B)
     st.handle.to_dense(rhs_c, B.data_ptr(), sptr)
     kw = dict(tol=args.tol, restart=args.restart, inner_tol=args.inner_tol, max_its=args.max_its, stream=sptr,
-              reorth=args.reorth, outer_k=args.outer_k)
+              reorth=args.reorth, outer_k=args.outer_k, precision=args.precision)
 
     def step():
         return st.handle.solve_device(obj, col_op, B.data_ptr(), X.data_ptr(), **kw)
@@ -281,7 +283,7 @@ def run_gpu(args):
         ops2 = native.Operators(st.handle, freqs, data)
         xh, its2, res2, ok2 = native.solve(st.handle, [(ops2, q) for (_, q) in cols], rhs_c, args.tol, restart=args.restart,
                                            inner_tol=args.inner_tol, max_its=args.max_its, reorth=args.reorth,
-                                           outer_k=args.outer_k)
+                                           outer_k=args.outer_k, precision=args.precision)
         e2e_t.append(time.perf_counter() - t0)
         del ops2
     e2e = None

@@ -22,6 +22,7 @@
 #include <mutex>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 namespace gt {
@@ -156,7 +157,7 @@ struct Workspace {
     c64* nred = nullptr;
     // inner (precision R) per slot
     void *V = nullptr, *w = nullptr, *z = nullptr, *T = nullptr, *zfac = nullptr, *yfac = nullptr, *uvec = nullptr,
-         *sd = nullptr;
+         *sd = nullptr, *vcur = nullptr;
     c64* partial = nullptr;
     GmresState st{};
     int *slot_col = nullptr, *slot_op = nullptr, *g_ptr = nullptr, *g_slot = nullptr, *g_op = nullptr, *col_op = nullptr;
@@ -206,6 +207,7 @@ struct gt_operators {
     Pool pool;
     double* omega = nullptr;
     c64 *zs = nullptr, *zcap = nullptr, *zbr = nullptr, *tab = nullptr;
+    c32* tab32 = nullptr;        // the admittance table rounded to FP32 (the FP32 preconditioner's stencils)
     // per front P = [Linv_own; -L_bnd Linv_own] (nf x nown) and the pivot reciprocals dinv ([op][nfac])
     c64* panel64 = nullptr;      // column-major per front (forward solves)
     c32* panel32 = nullptr;
@@ -237,6 +239,9 @@ template <> const c64* panel_of<double>(const gt_operators* ops) { return ops->p
 template <typename R> static const cx<R>* panel_rm_of(const gt_operators* ops);
 template <> const c32* panel_rm_of<float>(const gt_operators* ops) { return ops->panel32_rm; }
 template <> const c64* panel_rm_of<double>(const gt_operators* ops) { return ops->panel64_rm; }
+template <typename R> static const cx<R>* tab_of(const gt_operators* ops);
+template <> const c32* tab_of<float>(const gt_operators* ops) { return ops->tab32; }
+template <> const c64* tab_of<double>(const gt_operators* ops) { return ops->tab; }
 template <typename R> static const cx<R>* dinv_of(const gt_operators* ops);
 template <> const c32* dinv_of<float>(const gt_operators* ops) { return ops->dinv32; }
 template <> const c64* dinv_of<double>(const gt_operators* ops) { return ops->dinv64; }
@@ -352,7 +357,7 @@ static void precond(gt_geometry* G, gt_operators* ops, const cx<R>* r, int64_t l
     const double panel = (double)grp.ngroup * es * G->F.panel_total;
     {
         Scope s(P, "pc_node", st, nslot * es * (nXYC + nodes + nfac));
-        launch_pc_node<R>(G->geo, r, ldr, sd, nslot, slot_op, ops->tab, col_list, st);
+        launch_pc_node<R>(G->geo, r, ldr, sd, nslot, slot_op, tab_of<R>(ops), col_list, st);
     }
     const cx<R>* pan = panel_of<R>(ops);
     const int nlev = (int)G->level_ptr.size() - 1;
@@ -378,7 +383,7 @@ static void precond(gt_geometry* G, gt_operators* ops, const cx<R>* r, int64_t l
     }
     {
         Scope s(P, "pc_strip", st, nslot * es * (2 * n + nfac));
-        launch_pc_strip<R>(G->geo, r, ldr, sd, out, ldo, nslot, slot_op, ops->tab, col_list, st);
+        launch_pc_strip<R>(G->geo, r, ldr, sd, out, ldo, nslot, slot_op, tab_of<R>(ops), col_list, st);
     }
 }
 
@@ -422,6 +427,7 @@ static void ensure_ws(gt_geometry* G, int ncol, int m, int prec, int kmax) {
     W.kmax = kmax;
     const int64_t n = G->geo.n;
     const size_t es = prec == 1 ? sizeof(c64) : sizeof(c32);
+    const size_t eb = prec == 2 ? sizeof(h16c) : es;     // basis entries
     Pool& p = W.pool;
     W.x64 = p.alloc<c64>((size_t)ncol * n);
     W.r64 = p.alloc<c64>((size_t)ncol * n);
@@ -433,7 +439,8 @@ static void ensure_ws(gt_geometry* G, int ncol, int m, int prec, int kmax) {
     W.npart = p.alloc<c64>((size_t)ncol * nch);
     W.npart_k = p.alloc<c64>((size_t)ncol * nch * (kmax + 2));
     W.nred = p.alloc<c64>(ncol);
-    W.V = p.alloc<unsigned char>((size_t)ncol * (m + 1) * n * es);
+    W.V = p.alloc<unsigned char>((size_t)ncol * (m + 1) * n * eb);
+    if (prec == 2) W.vcur = p.alloc<unsigned char>((size_t)ncol * n * es);
     W.w = p.alloc<unsigned char>((size_t)ncol * n * es);
     W.z = p.alloc<unsigned char>((size_t)ncol * n * es);
     W.T = p.alloc<unsigned char>((size_t)ncol * G->maxT * es);
@@ -481,7 +488,7 @@ static void ensure_ws(gt_geometry* G, int ncol, int m, int prec, int kmax) {
     W.flag_dev = p.alloc<int>(1);
     W.its_col = p.alloc<int>(ncol);
     GT_CUDA(cudaMallocHost(&W.flag_host, sizeof(int)));
-    GT_CUDA(cudaMemset(W.V, 0, (size_t)ncol * (m + 1) * n * es));
+    GT_CUDA(cudaMemset(W.V, 0, (size_t)ncol * (m + 1) * n * eb));
 }
 
 // ||v_c|| for ncol FP64 dense vectors -> out (device)
@@ -493,9 +500,12 @@ static void norms64(gt_geometry* G, const c64* v, int64_t ld, int ncol, double* 
     launch_sqrt_norms(W.nred, 1, ncol, out, st);
 }
 
-template <typename R>
+// R: the inner GMRES arithmetic; B: its basis storage (cx<R>, or FP16 pairs scaled by a power of two near
+// sqrt(n) so that a unit vector's entries sit near 1)
+template <typename R, typename B = cx<R>>
 static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_col_op, const gt_solve_opts& o,
                       int* its_out, double* resid_out, cudaStream_t st) {
+    constexpr bool narrow = !std::is_same<B, cx<R>>::value;
     Workspace& W = *G->ws;
     const int64_t n = G->geo.n;
     const int m = o.restart;
@@ -513,7 +523,10 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
     GT_CUDA(cudaStreamSynchronize(st));
     h_rho = h_bnorm;
     const int gmax = group_max(G, sizeof(cx<R>));
-    cx<R>* V = static_cast<cx<R>*>(W.V);
+    B* V = static_cast<B*>(W.V);
+    cx<R>* vcur = narrow ? static_cast<cx<R>*>(W.vcur) : nullptr;
+    const R bscale = narrow ? R(std::ldexp(1.0, (int)std::lround(0.5 * std::log2((double)n)))) : R(1);
+    const R vs = R(1) / bscale;
     cx<R>* w = static_cast<cx<R>*>(W.w);
     cx<R>* z = static_cast<cx<R>*>(W.z);
     cx<R>* T = static_cast<cx<R>*>(W.T);
@@ -577,38 +590,49 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
         S.reorth_ratio = o.reorth;
         GT_CUDA(cudaMemcpyAsync(S.its_total, its_slot.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
         Groups grp = upload_groups(act);
-        GmresStateT<R> ST{ns, S.active, S.inv_hn, V, w, n, lds};
+        GmresStateT<R, B> ST{ns, S.active, S.inv_hn, V, w, n, lds, bscale, vcur};
         {
             Scope sc(P, "gmres_small", st);
             launch_init_state(S, W.slot_col, W.rho, W.bnorm, o.tol, o.inner_tol, st);
-            launch_init_cycle<R>(ST, W.r64, n, W.slot_col, W.rho, n, st);
+            launch_init_cycle<R, B>(ST, W.r64, n, W.slot_col, W.rho, n, st);
         }
         int jdone = 0;
         for (int j = 0; j < m; ++j) {
             // the products run on the slots still iterating in this cycle (W.act, grp)
             const int na = (int)act.size();
-            precond<R>(G, ops, V + (int64_t)j * n, lds, z, n, na, W.slot_op, grp, gmax, zfac, yfac, uvec, sd, st, W.act);
+            // the product is applied to the basis vector as stored
+            const cx<R>* vin;
+            int64_t ldin;
+            if constexpr (narrow) {
+                vin = vcur;
+                ldin = n;
+            } else {
+                vin = V + (int64_t)j * n;
+                ldin = lds;
+            }
+            precond<R>(G, ops, vin, ldin, z, n, na, W.slot_op, grp, gmax, zfac, yfac, uvec, sd, st, W.act);
             matvec<R>(G, ops, z, nullptr, w, n, na, W.slot_op, 0, T, st, W.act);
             {
                 // classical Gram-Schmidt: the j+1 basis vectors read twice, w read twice and written once
-                Scope sc(P, sizeof(R) == 4 ? "gs_f32" : "gs_f64", st, (double)ns * sizeof(cx<R>) * n * (2.0 * (j + 1) + 3));
-                launch_dots<R>(V, n, lds, j + 1, w, n, n, ns, S.active, W.partial, nch, st);
+                Scope sc(P, narrow ? "gs_f32_b16" : sizeof(R) == 4 ? "gs_f32" : "gs_f64", st,
+                         (double)ns * n * (2.0 * (j + 1) * sizeof(B) + 3.0 * sizeof(cx<R>)));
+                launch_dots<R, B>(V, n, lds, j + 1, w, n, n, ns, S.active, W.partial, nch, st, vs);
                 launch_reduce(W.partial, nch, j + 1, ns, S.active, S.hvec, S.ldh, 0, st);
-                launch_update<R>(V, n, lds, j + 1, S.hvec, S.ldh, w, n, n, ns, S.active, W.partial, nch, -1, st);
+                launch_update<R, B>(V, n, lds, j + 1, S.hvec, S.ldh, w, n, n, ns, S.active, W.partial, nch, -1, st, vs);
                 launch_reduce(W.partial, nch, 0, ns, S.active, S.hn2, 1, 0, st);
                 launch_dgks(S, j, st);
             }
             {
                 Scope sc(P, "gs_reorth", st);
-                launch_dots<R>(V, n, lds, j + 1, w, n, n, ns, S.reorth, W.partial, nch, st);
+                launch_dots<R, B>(V, n, lds, j + 1, w, n, n, ns, S.reorth, W.partial, nch, st, vs);
                 launch_reduce(W.partial, nch, j + 1, ns, S.reorth, S.h2vec, S.ldh, 0, st);
-                launch_update<R>(V, n, lds, j + 1, S.h2vec, S.ldh, w, n, n, ns, S.reorth, W.partial, nch, -1, st);
+                launch_update<R, B>(V, n, lds, j + 1, S.h2vec, S.ldh, w, n, n, ns, S.reorth, W.partial, nch, -1, st, vs);
                 launch_reduce(W.partial, nch, 0, ns, S.reorth, S.hn2b, 1, 0, st);
             }
             {
                 Scope sc(P, "gmres_small", st);
                 launch_givens(S, j, st);
-                if (j + 1 < m) launch_scale<R>(ST, j, n, st);
+                if (j + 1 < m) launch_scale<R, B>(ST, j, n, st);
             }
             GT_CUDA(cudaMemcpyAsync(W.act_host, S.active, ns * sizeof(int), cudaMemcpyDeviceToHost, st));
             GT_CUDA(cudaStreamSynchronize(st));
@@ -629,8 +653,8 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
         }
         GT_CUDA(cudaMemsetAsync(w, 0, (size_t)ns * n * sizeof(cx<R>), st));
         {
-            Scope sc(P, "combine", st, (double)ns * sizeof(cx<R>) * n * (jdone + 2.0));
-            launch_update<R>(V, n, lds, jdone, S.y, S.ldh, w, n, n, ns, nullptr, nullptr, nch, 1, st);
+            Scope sc(P, "combine", st, (double)ns * n * (jdone * sizeof(B) + 2.0 * sizeof(cx<R>)));
+            launch_update<R, B>(V, n, lds, jdone, S.y, S.ldh, w, n, n, ns, nullptr, nullptr, nch, 1, st, vs);
         }
         act.resize(ns);
         for (int q = 0; q < ns; ++q) act[q] = q;
@@ -697,6 +721,8 @@ static int run_solve(gt_geometry* G, gt_operators* ops, int ncol, const int* col
     for (int c = 0; c < ncol; ++c)
         if (col_op[c] < 0 || col_op[c] >= ops->nops) throw Invalid("column operator index out of range");
     if (o.precision == 1) return solve_impl<double>(G, ops, ncol, col_op, o, its, res, st);
+    if (o.precision == 2) return solve_impl<float, h16c>(G, ops, ncol, col_op, o, its, res, st);
+    if (o.precision != 0) throw Invalid("precision must be 0, 1 or 2");
     return solve_impl<float>(G, ops, ncol, col_op, o, its, res, st);
 }
 
@@ -938,6 +964,11 @@ int gt_operators_create(gt_geometry* G, int32_t n_ops, const double* omega, cons
     O->zcap = p.upload(reinterpret_cast<const c64*>(zcap), (size_t)n_ops * g.np);
     O->zbr = p.upload(reinterpret_cast<const c64*>(zbr), (size_t)n_ops * g.nbr);
     O->tab = p.upload(reinterpret_cast<const c64*>(table), (size_t)n_ops * g.ntab);
+    {
+        std::vector<c32> t32((size_t)n_ops * g.ntab);
+        for (size_t q = 0; q < t32.size(); ++q) t32[q] = mk<float>((float)table[2 * q], (float)table[2 * q + 1]);
+        O->tab32 = p.upload(t32.data(), t32.size());
+    }
     cudaStream_t st = 0;
     const Fronts& F = G->F;
     Pool tmp;
@@ -1007,7 +1038,7 @@ int gt_solve_device(gt_geometry* G, gt_operators* ops, int32_t n_cols, const int
     if (!G || !ops || !opts || n_cols < 1) throw Invalid("bad arguments");
     std::lock_guard<std::mutex> lk(G->lock);
     cudaStream_t st = (cudaStream_t)stream;
-    ensure_ws(G, n_cols, opts->restart, opts->precision == 1 ? 1 : 0, std::max(1, opts->outer_k));
+    ensure_ws(G, n_cols, opts->restart, opts->precision, std::max(1, opts->outer_k));
     Workspace& W = *G->ws;
     GT_CUDA(cudaMemcpyAsync(W.b64, rhs_device, (size_t)n_cols * G->geo.n * sizeof(c64), cudaMemcpyDeviceToDevice, st));
     int rc = run_solve(G, ops, n_cols, col_op, opts, its_out, resid_out, st);
@@ -1024,7 +1055,7 @@ int gt_solve(gt_geometry* G, gt_operators* ops, int32_t n_cols, const int32_t* c
     if (!G || !ops || !opts || n_cols < 1 || !rhs || !x_out) throw Invalid("bad arguments");
     std::lock_guard<std::mutex> lk(G->lock);
     cudaStream_t st = (cudaStream_t)stream;
-    ensure_ws(G, n_cols, opts->restart, opts->precision == 1 ? 1 : 0, std::max(1, opts->outer_k));
+    ensure_ws(G, n_cols, opts->restart, opts->precision, std::max(1, opts->outer_k));
     Workspace& W = *G->ws;
     const int64_t nc = G->n_compact;
     Pool tmp;

@@ -2,6 +2,7 @@
 // (float for the inner iterations, double for residuals and factorisation), error plumbing.
 #pragma once
 #include <cuda_runtime.h>
+#include <cuda_fp16.h>
 #include <stdint.h>
 #include <atomic>
 #include <string>

@@ -7,6 +7,7 @@
 // order: results are reproducible).  The Hessenberg column, its Givens rotations and the least-squares
 // right-hand side live on the device in FP64 (peec.py:3160-3184); so does the decision that a slot's cycle
 // has converged.
+#include <type_traits>
 #include "kernels.h"
 #include "solver.h"
 
@@ -17,17 +18,26 @@ template <typename R> __device__ __forceinline__ R shfl_sum(R v) {
     return v;
 }
 
+// basis entries: loads and stores of cx<R> or of FP16 pairs
+template <typename R> __device__ __forceinline__ cx<R> bload(const cx<R>* p) { return *p; }
+__device__ __forceinline__ c32 bload(const h16c* p) {
+    const float2 f = __half22float2(p->v);
+    return mk<float>(f.x, f.y);
+}
+template <typename R> __device__ __forceinline__ void bstore(cx<R>* p, cx<R> v) { *p = v; }
+__device__ __forceinline__ void bstore(h16c* p, c32 v) { p->v = __floats2half2_rn(v.re, v.im); }
+
 constexpr int DOT_THREADS = 256;
 constexpr int DOT_EPT = 8;
 constexpr int DOT_CHUNK = DOT_THREADS * DOT_EPT;
 constexpr int MAXV = 256;
 
 // partial[(slot * nchunk + chunk) * (nv + 1) + i] = sum over the chunk of conj(V_i) w, i < nv; index nv: |w|^2
-template <typename R>
-__global__ void __launch_bounds__(DOT_THREADS) dots_kernel(const cx<R>* __restrict__ V, int64_t ldv, int64_t lds, int nv,
+template <typename R, typename B>
+__global__ void __launch_bounds__(DOT_THREADS) dots_kernel(const B* __restrict__ V, int64_t ldv, int64_t lds, int nv,
                                                            const cx<R>* __restrict__ w, int64_t ldw, int64_t n,
                                                            const int* __restrict__ active, c64* __restrict__ partial,
-                                                           int nchunk) {
+                                                           int nchunk, R vs) {
     __shared__ c64 red[DOT_THREADS / 32][MAXV + 1];
     const int slot = blockIdx.y;
     if (active && !active[slot]) return;
@@ -42,20 +52,20 @@ __global__ void __launch_bounds__(DOT_THREADS) dots_kernel(const cx<R>* __restri
         wv[e] = q < n ? w[(int64_t)slot * ldw + q] : zero<R>();
         nrm += norm2(wv[e]);
     }
-    const cx<R>* Vs = V + (int64_t)slot * lds;
+    const B* Vs = V + (int64_t)slot * lds;
     for (int i = 0; i < nv; ++i) {
-        const cx<R>* Vi = Vs + (int64_t)i * ldv;
+        const B* Vi = Vs + (int64_t)i * ldv;
         R ar = 0, ai = 0;
 #pragma unroll
         for (int e = 0; e < DOT_EPT; ++e) {
             int64_t q = base + e * DOT_THREADS + tid;
-            cx<R> v = q < n ? Vi[q] : zero<R>();
+            cx<R> v = q < n ? bload(Vi + q) : zero<R>();
             ar += v.re * wv[e].re + v.im * wv[e].im;
             ai += v.re * wv[e].im - v.im * wv[e].re;
         }
         ar = shfl_sum(ar);
         ai = shfl_sum(ai);
-        if (lane == 0) red[warp][i] = mk<double>(ar, ai);
+        if (lane == 0) red[warp][i] = mk<double>((double)ar * vs, (double)ai * vs);
     }
     nrm = shfl_sum(nrm);
     if (lane == 0) red[warp][nv] = mk<double>(nrm, 0.0);
@@ -67,10 +77,11 @@ __global__ void __launch_bounds__(DOT_THREADS) dots_kernel(const cx<R>* __restri
     }
 }
 
-template <typename R>
-void launch_dots(const cx<R>* V, int64_t ldv, int64_t lds, int nv, const cx<R>* w, int64_t ldw, int64_t n, int nslot,
-                 const int* active, c64* partial, int nchunk, cudaStream_t st) {
-    dots_kernel<R><<<dim3(nchunk, nslot), DOT_THREADS, 0, st>>>(V, ldv, lds, nv, w, ldw, n, active, partial, nchunk);
+template <typename R, typename B>
+void launch_dots(const B* V, int64_t ldv, int64_t lds, int nv, const cx<R>* w, int64_t ldw, int64_t n, int nslot,
+                 const int* active, c64* partial, int nchunk, cudaStream_t st, R vs) {
+    dots_kernel<R, B><<<dim3(nchunk, nslot), DOT_THREADS, 0, st>>>(V, ldv, lds, nv, w, ldw, n, active, partial, nchunk,
+                                                                    vs);
     GT_LAUNCH_CHECK();
 }
 
@@ -94,12 +105,12 @@ void launch_reduce(const c64* partial, int nchunk, int nv, int nslot, const int*
 }
 
 // w += sign * sum_i h_i V_i (sign -1: Gram-Schmidt; +1: the cycle's combination); partial |w|^2 per chunk
-template <typename R>
-__global__ void __launch_bounds__(DOT_THREADS) update_kernel(const cx<R>* __restrict__ V, int64_t ldv, int64_t lds,
+template <typename R, typename B>
+__global__ void __launch_bounds__(DOT_THREADS) update_kernel(const B* __restrict__ V, int64_t ldv, int64_t lds,
                                                              int nv, const c64* __restrict__ h, int ldh,
                                                              cx<R>* __restrict__ w, int64_t ldw, int64_t n,
                                                              const int* __restrict__ active, c64* __restrict__ partial,
-                                                             int nchunk, int sign) {
+                                                             int nchunk, int sign, R vs) {
     __shared__ cx<R> hs[MAXV];
     __shared__ double red[DOT_THREADS / 32];
     const int slot = blockIdx.y;
@@ -107,7 +118,7 @@ __global__ void __launch_bounds__(DOT_THREADS) update_kernel(const cx<R>* __rest
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int i = tid; i < nv; i += DOT_THREADS) {
         c64 v = h[(int64_t)slot * ldh + i];
-        hs[i] = mk<R>(R(sign * v.re), R(sign * v.im));
+        hs[i] = mk<R>(R(sign * v.re * vs), R(sign * v.im * vs));
     }
     __syncthreads();
     const int64_t base = (int64_t)blockIdx.x * DOT_CHUNK;
@@ -117,14 +128,14 @@ __global__ void __launch_bounds__(DOT_THREADS) update_kernel(const cx<R>* __rest
         int64_t q = base + e * DOT_THREADS + tid;
         acc[e] = q < n ? w[(int64_t)slot * ldw + q] : zero<R>();
     }
-    const cx<R>* Vs = V + (int64_t)slot * lds;
+    const B* Vs = V + (int64_t)slot * lds;
     for (int i = 0; i < nv; ++i) {
         const cx<R> hi = hs[i];
-        const cx<R>* Vi = Vs + (int64_t)i * ldv;
+        const B* Vi = Vs + (int64_t)i * ldv;
 #pragma unroll
         for (int e = 0; e < DOT_EPT; ++e) {
             int64_t q = base + e * DOT_THREADS + tid;
-            if (q < n) acc[e] += hi * Vi[q];
+            if (q < n) acc[e] += hi * bload(Vi + q);
         }
     }
     R nrm = 0;
@@ -146,18 +157,20 @@ __global__ void __launch_bounds__(DOT_THREADS) update_kernel(const cx<R>* __rest
     }
 }
 
-template <typename R>
-void launch_update(const cx<R>* V, int64_t ldv, int64_t lds, int nv, const c64* h, int ldh, cx<R>* w, int64_t ldw,
-                   int64_t n, int nslot, const int* active, c64* partial, int nchunk, int sign, cudaStream_t st) {
-    update_kernel<R><<<dim3(nchunk, nslot), DOT_THREADS, 0, st>>>(V, ldv, lds, nv, h, ldh, w, ldw, n, active, partial,
-                                                                   nchunk, sign);
+template <typename R, typename B>
+void launch_update(const B* V, int64_t ldv, int64_t lds, int nv, const c64* h, int ldh, cx<R>* w, int64_t ldw,
+                   int64_t n, int nslot, const int* active, c64* partial, int nchunk, int sign, cudaStream_t st, R vs) {
+    update_kernel<R, B><<<dim3(nchunk, nslot), DOT_THREADS, 0, st>>>(V, ldv, lds, nv, h, ldh, w, ldw, n, active,
+                                                                      partial, nchunk, sign, vs);
     GT_LAUNCH_CHECK();
 }
 
-template void launch_dots<float>(const c32*, int64_t, int64_t, int, const c32*, int64_t, int64_t, int, const int*, c64*, int, cudaStream_t);
-template void launch_dots<double>(const c64*, int64_t, int64_t, int, const c64*, int64_t, int64_t, int, const int*, c64*, int, cudaStream_t);
-template void launch_update<float>(const c32*, int64_t, int64_t, int, const c64*, int, c32*, int64_t, int64_t, int, const int*, c64*, int, int, cudaStream_t);
-template void launch_update<double>(const c64*, int64_t, int64_t, int, const c64*, int, c64*, int64_t, int64_t, int, const int*, c64*, int, int, cudaStream_t);
+template void launch_dots<float, c32>(const c32*, int64_t, int64_t, int, const c32*, int64_t, int64_t, int, const int*, c64*, int, cudaStream_t, float);
+template void launch_dots<float, h16c>(const h16c*, int64_t, int64_t, int, const c32*, int64_t, int64_t, int, const int*, c64*, int, cudaStream_t, float);
+template void launch_dots<double, c64>(const c64*, int64_t, int64_t, int, const c64*, int64_t, int64_t, int, const int*, c64*, int, cudaStream_t, double);
+template void launch_update<float, c32>(const c32*, int64_t, int64_t, int, const c64*, int, c32*, int64_t, int64_t, int, const int*, c64*, int, int, cudaStream_t, float);
+template void launch_update<float, h16c>(const h16c*, int64_t, int64_t, int, const c64*, int, c32*, int64_t, int64_t, int, const int*, c64*, int, int, cudaStream_t, float);
+template void launch_update<double, c64>(const c64*, int64_t, int64_t, int, const c64*, int, c64*, int64_t, int64_t, int, const int*, c64*, int, int, cudaStream_t, double);
 
 // ------------------------------------------------------------------------------------------ per-slot scalars
 // After the first Gram-Schmidt pass: hvec[0..j] = h, hvec[j+1] = |w_before|^2; hn2 = |w_after|^2 (reduced
@@ -229,15 +242,28 @@ __global__ void givens_kernel(GmresState s, int j) {
     s.resid_est[slot] = res;
 }
 
-template <typename R>
-__global__ void scale_kernel(GmresStateT<R> s, int j, int64_t n) {
+// store v (a basis vector, unscaled) at p[q]; with a narrower basis type also the stored value, unscaled,
+// to vc[q] (the vector the next product is applied to)
+template <typename R, typename B>
+__device__ __forceinline__ void put_basis(const GmresStateT<R, B>& s, B* p, cx<R>* vc, int64_t q, cx<R> v) {
+    if constexpr (std::is_same<B, cx<R>>::value) {
+        p[q] = v;
+    } else {
+        bstore(p + q, s.scale * v);
+        vc[q] = (R(1) / s.scale) * bload(p + q);
+    }
+}
+
+template <typename R, typename B>
+__global__ void scale_kernel(GmresStateT<R, B> s, int j, int64_t n) {
     const int slot = blockIdx.y;
     if (!s.active[slot]) return;
     const R f = R(s.inv_hn[slot]);
     const cx<R>* w = s.w + (int64_t)slot * s.ldv;
-    cx<R>* v = s.V + (int64_t)slot * s.lds + (int64_t)(j + 1) * s.ldv;
+    B* v = s.V + (int64_t)slot * s.lds + (int64_t)(j + 1) * s.ldv;
+    cx<R>* vc = s.vcur ? s.vcur + (int64_t)slot * s.ldv : nullptr;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
-        v[q] = f * w[q];
+        put_basis(s, v, vc, q, f * w[q]);
 }
 
 // y = R^-1 g over the slot's k = it columns (back substitution, FP64)
@@ -258,16 +284,17 @@ __global__ void hsolve_kernel(GmresState s) {
 }
 
 // a slot's cycle starts from r / rho: V_0 = r / rho, g = (1, 0, ...), rotations cleared
-template <typename R>
-__global__ void init_cycle_kernel(GmresStateT<R> s, const c64* __restrict__ r, int64_t ldr, const int* __restrict__ slot_col,
+template <typename R, typename B>
+__global__ void init_cycle_kernel(GmresStateT<R, B> s, const c64* __restrict__ r, int64_t ldr, const int* __restrict__ slot_col,
                                   const double* __restrict__ rho, int64_t n) {
     const int slot = blockIdx.y;
     const int col = slot_col[slot];
     const double inv = rho[col] > 0 ? 1.0 / rho[col] : 0.0;
-    cx<R>* v = s.V + (int64_t)slot * s.lds;
+    B* v = s.V + (int64_t)slot * s.lds;
+    cx<R>* vc = s.vcur ? s.vcur + (int64_t)slot * s.ldv : nullptr;
     const c64* rc = r + (int64_t)col * ldr;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
-        v[q] = cvt<R>(inv * rc[q]);
+        put_basis(s, v, vc, q, cvt<R>(inv * rc[q]));
 }
 
 __global__ void init_state_kernel(GmresState s, const int* __restrict__ slot_col, const double* __restrict__ rho,
@@ -363,21 +390,21 @@ void launch_givens(const GmresState& s, int j, cudaStream_t st) {
     givens_kernel<<<ceil_div(s.nslot, 64), 64, 0, st>>>(s, j);
     GT_LAUNCH_CHECK();
 }
-template <typename R>
-void launch_scale(const GmresStateT<R>& s, int j, int64_t n, cudaStream_t st) {
+template <typename R, typename B>
+void launch_scale(const GmresStateT<R, B>& s, int j, int64_t n, cudaStream_t st) {
     int blocks = (int)std::min<int64_t>((n + 255) / 256, 1024);
-    scale_kernel<R><<<dim3(blocks, s.nslot), 256, 0, st>>>(s, j, n);
+    scale_kernel<R, B><<<dim3(blocks, s.nslot), 256, 0, st>>>(s, j, n);
     GT_LAUNCH_CHECK();
 }
 void launch_hsolve(const GmresState& s, cudaStream_t st) {
     hsolve_kernel<<<ceil_div(s.nslot, 64), 64, 0, st>>>(s);
     GT_LAUNCH_CHECK();
 }
-template <typename R>
-void launch_init_cycle(const GmresStateT<R>& s, const c64* r, int64_t ldr, const int* slot_col, const double* rho,
+template <typename R, typename B>
+void launch_init_cycle(const GmresStateT<R, B>& s, const c64* r, int64_t ldr, const int* slot_col, const double* rho,
                        int64_t n, cudaStream_t st) {
     int blocks = (int)std::min<int64_t>((n + 255) / 256, 1024);
-    init_cycle_kernel<R><<<dim3(blocks, s.nslot), 256, 0, st>>>(s, r, ldr, slot_col, rho, n);
+    init_cycle_kernel<R, B><<<dim3(blocks, s.nslot), 256, 0, st>>>(s, r, ldr, slot_col, rho, n);
     GT_LAUNCH_CHECK();
 }
 void launch_init_state(const GmresState& s, const int* slot_col, const double* rho, const double* bnorm, double tol,
@@ -412,10 +439,12 @@ void launch_sqrt_norms(const c64* nrm2, int ld, int n, double* out, cudaStream_t
     GT_LAUNCH_CHECK();
 }
 
-template void launch_scale<float>(const GmresStateT<float>&, int, int64_t, cudaStream_t);
-template void launch_scale<double>(const GmresStateT<double>&, int, int64_t, cudaStream_t);
-template void launch_init_cycle<float>(const GmresStateT<float>&, const c64*, int64_t, const int*, const double*, int64_t, cudaStream_t);
-template void launch_init_cycle<double>(const GmresStateT<double>&, const c64*, int64_t, const int*, const double*, int64_t, cudaStream_t);
+template void launch_scale<float, c32>(const GmresStateT<float, c32>&, int, int64_t, cudaStream_t);
+template void launch_scale<float, h16c>(const GmresStateT<float, h16c>&, int, int64_t, cudaStream_t);
+template void launch_scale<double, c64>(const GmresStateT<double, c64>&, int, int64_t, cudaStream_t);
+template void launch_init_cycle<float, c32>(const GmresStateT<float, c32>&, const c64*, int64_t, const int*, const double*, int64_t, cudaStream_t);
+template void launch_init_cycle<float, h16c>(const GmresStateT<float, h16c>&, const c64*, int64_t, const int*, const double*, int64_t, cudaStream_t);
+template void launch_init_cycle<double, c64>(const GmresStateT<double, c64>&, const c64*, int64_t, const int*, const double*, int64_t, cudaStream_t);
 template void launch_refine<float>(c64*, int64_t, const c32*, int64_t, const int*, const double*, int64_t, int, cudaStream_t);
 template void launch_refine<double>(c64*, int64_t, const c64*, int64_t, const int*, const double*, int64_t, int, cudaStream_t);
 

@@ -54,10 +54,10 @@ void launch_tail(const Geo& g, const cx<R>* x, const cx<R>* rhs, cx<R>* out, int
 // sd (zero at nodes that are not kept), out = [D^-1 (r_1 + Ar y); y]
 template <typename R>
 void launch_pc_node(const Geo& g, const cx<R>* r, int64_t ld, cx<R>* sd, int ncol, const int* col_op,
-                    const c64* tab, const int* col_list, cudaStream_t st);
+                    const cx<R>* tab, const int* col_list, cudaStream_t st);
 template <typename R>
 void launch_pc_strip(const Geo& g, const cx<R>* r, int64_t ldr, const cx<R>* sd, cx<R>* out, int64_t ldo, int ncol,
-                     const int* col_op, const c64* tab, const int* col_list, cudaStream_t st);
+                     const int* col_op, const cx<R>* tab, const int* col_list, cudaStream_t st);
 
 // compact <-> dense
 void launch_scatter(const int64_t* c2d, int64_t ncomp, const c64* in, int64_t ldin, c64* out, int64_t ldout, int ncol,
@@ -123,13 +123,20 @@ void launch_bwd_level(const Fronts& F, const int64_t* front_list, int nf_level, 
                       cudaStream_t st);
 
 // --- Krylov vector work (batched, one basis per slot)
-template <typename R>
-void launch_dots(const cx<R>* V, int64_t ldv, int64_t lds, int nv, const cx<R>* w, int64_t ldw, int64_t n, int nslot,
-                 const int* active, c64* partial, int nchunk, cudaStream_t st);
+// A basis entry stored in FP16 (real and imaginary halves), scaled by the basis scale so that the entries
+// of a unit vector of length n sit near 1, inside FP16's normal range.
+struct h16c {
+    __half2 v;
+};
+// Basis vectors are stored as B (cx<R>, or h16c for R = float) times the scale; vs = 1 / scale undoes it.
+template <typename R, typename B>
+void launch_dots(const B* V, int64_t ldv, int64_t lds, int nv, const cx<R>* w, int64_t ldw, int64_t n, int nslot,
+                 const int* active, c64* partial, int nchunk, cudaStream_t st, R vs = R(1));
 void launch_reduce(const c64* partial, int nchunk, int nv, int nslot, const int* active, c64* out, int ldo, int mode,
                    cudaStream_t st);
-template <typename R>
-void launch_update(const cx<R>* V, int64_t ldv, int64_t lds, int nv, const c64* h, int ldh, cx<R>* w, int64_t ldw,
-                   int64_t n, int nslot, const int* active, c64* partial, int nchunk, int sign, cudaStream_t st);
+template <typename R, typename B>
+void launch_update(const B* V, int64_t ldv, int64_t lds, int nv, const c64* h, int ldh, cx<R>* w, int64_t ldw,
+                   int64_t n, int nslot, const int* active, c64* partial, int nchunk, int sign, cudaStream_t st,
+                   R vs = R(1));
 
 }  // namespace gt

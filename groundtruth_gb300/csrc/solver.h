@@ -25,21 +25,23 @@ struct GmresState {
     double* resid_est; // [slot]
 };
 
-template <typename R> struct GmresStateT {
+template <typename R, typename B = cx<R>> struct GmresStateT {
     int nslot;
     int* active;
     double* inv_hn;
-    cx<R>* V;          // [slot][m+1][ldv]
+    B* V;              // [slot][m+1][ldv], times scale
     cx<R>* w;          // [slot][ldv]
     int64_t ldv, lds;
+    R scale;           // the basis scale (1 unless B is a narrower type than cx<R>)
+    cx<R>* vcur;       // [slot][ldv]: the newest basis vector as stored, unscaled (B != cx<R> only)
 };
 
 void launch_dgks(const GmresState& s, int j, cudaStream_t st);
 void launch_givens(const GmresState& s, int j, cudaStream_t st);
-template <typename R> void launch_scale(const GmresStateT<R>& s, int j, int64_t n, cudaStream_t st);
+template <typename R, typename B> void launch_scale(const GmresStateT<R, B>& s, int j, int64_t n, cudaStream_t st);
 void launch_hsolve(const GmresState& s, cudaStream_t st);
-template <typename R>
-void launch_init_cycle(const GmresStateT<R>& s, const c64* r, int64_t ldr, const int* slot_col, const double* rho,
+template <typename R, typename B>
+void launch_init_cycle(const GmresStateT<R, B>& s, const c64* r, int64_t ldr, const int* slot_col, const double* rho,
                        int64_t n, cudaStream_t st);
 void launch_init_state(const GmresState& s, const int* slot_col, const double* rho, const double* bnorm, double tol,
                        double inner_tol, cudaStream_t st);

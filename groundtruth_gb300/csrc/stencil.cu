@@ -26,210 +26,283 @@ __device__ __forceinline__ int seg_of(const Geo& g, int64_t pos, int64_t nX, int
     return 4;
 }
 
-// D^-1 applied to the strips at one position: strip of sheet k, orientation o, with the vector u over the
-// sheets present (code)
-template <typename R>
-__device__ __forceinline__ cx<R> dinv_strip(const c64* tab, int S, int o, int code, int k, const cx<R>* u) {
-    const int NC = 1 << S;
-    const c64* T = tab + (((int64_t)o * NC + code) * S + k) * S;
-    cx<R> acc = zero<R>();
-    for (int l = 0; l < S; ++l)
-        if ((code >> l) & 1) acc += cvt<R>(T[l]) * u[l];
-    return acc;
-}
-
-template <typename R>
-__device__ __forceinline__ cx<R> load_or0(const cx<R>* p, bool ok) { return ok ? *p : zero<R>(); }
-
 }  // namespace
 
+// blockIdx.y selects the part: 0 nodes (sheet k, row i), 1 capacitances (pair p, row i), 2 branches and the
+// padding between segments.  The strips are written by the FFT pass.
 template <typename R>
-__global__ void tail_kernel(Geo g, const cx<R>* __restrict__ x, const cx<R>* __restrict__ rhs, cx<R>* __restrict__ out,
-                            int64_t ld, const int* __restrict__ col_op, const c64* __restrict__ zcap,
-                            const c64* __restrict__ zbr, int mode, const int* __restrict__ col_list) {
-    const int col = col_list ? col_list[blockIdx.y] : blockIdx.y;
+__global__ void __launch_bounds__(256) tail_kernel(Geo g, const cx<R>* __restrict__ x, const cx<R>* __restrict__ rhs,
+                                                   cx<R>* __restrict__ out, int64_t ld, const int* __restrict__ col_op,
+                                                   const c64* __restrict__ zcap, const c64* __restrict__ zbr, int mode,
+                                                   const int* __restrict__ col_list) {
+    const int col = col_list ? col_list[blockIdx.z] : blockIdx.z;
     const int op = col_op ? col_op[col] : 0;
-    const int64_t nX = (int64_t)g.S * (g.nx - 1) * g.ny, nY = (int64_t)g.S * g.nx * (g.ny - 1);
+    const int S = g.S, nx = g.nx, ny = g.ny, nxy = nx * ny;
     const cx<R>* xc = x + (int64_t)col * ld;
-    for (int64_t pos = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; pos < g.n; pos += (int64_t)gridDim.x * blockDim.x) {
-        int seg = seg_of(g, pos, nX, nY);
-        if (seg == 0 || seg == 1) continue;         // strips: written by the FFT pass
-        cx<R> y = zero<R>();
-        if (seg >= 2 && g.mask[pos]) {
-            const cx<R>* V = xc + g.off_v;
-            if (seg == 2) {
-                int64_t q = pos - g.off_c;
-                int p = int(q / ((int64_t)g.nx * g.ny));
-                int64_t ij = q - (int64_t)p * g.nx * g.ny;
-                int u = g.pair_layers[2 * p], l = g.pair_layers[2 * p + 1];
-                y = cvt<R>(zcap[(int64_t)op * g.np + p]) * xc[pos] - (V[(int64_t)u * g.nx * g.ny + ij] - V[(int64_t)l * g.nx * g.ny + ij]);
-            } else if (seg == 3) {
-                int b = int(pos - g.off_b);
-                y = cvt<R>(zbr[(int64_t)op * g.nbr + b]) * xc[pos] - (V[g.branch_nodes[2 * b]] - V[g.branch_nodes[2 * b + 1]]);
-            } else {
-                int64_t node = pos - g.off_v;
-                int k = int(node / ((int64_t)g.nx * g.ny));
-                int64_t ij = node - (int64_t)k * g.nx * g.ny;
-                int i = int(ij / g.ny), j = int(ij - (int64_t)i * g.ny);
-                const cx<R>* X = xc + g.off_x + (int64_t)k * (g.nx - 1) * g.ny;
-                const cx<R>* Y = xc + g.off_y + (int64_t)k * g.nx * (g.ny - 1);
-                cx<R> s = zero<R>();
-                if (i < g.nx - 1) s += X[(int64_t)i * g.ny + j];
-                if (i > 0) s -= X[(int64_t)(i - 1) * g.ny + j];
-                if (j < g.ny - 1) s += Y[(int64_t)i * (g.ny - 1) + j];
-                if (j > 0) s -= Y[(int64_t)i * (g.ny - 1) + j - 1];
-                for (int p = 0; p < g.np; ++p) {
-                    int u = g.pair_layers[2 * p], l = g.pair_layers[2 * p + 1];
-                    if (u == k) s += xc[g.off_c + (int64_t)p * g.nx * g.ny + ij];
-                    if (l == k) s -= xc[g.off_c + (int64_t)p * g.nx * g.ny + ij];
-                }
-                for (int e = g.node_br_ptr[node]; e < g.node_br_ptr[node + 1]; ++e) {
-                    int b = g.node_br_idx[e];
-                    if (b > 0) s += xc[g.off_b + b - 1];
-                    else s -= xc[g.off_b - b - 1];
-                }
-                y = s;
+    const cx<R>* V = xc + g.off_v;
+    const cx<R>* bc = rhs ? rhs + (int64_t)col * ld : nullptr;
+    cx<R>* oc = out + (int64_t)col * ld;
+    const int part = blockIdx.y, bx = blockIdx.x;
+    auto put = [&](int64_t pos, cx<R> y) { oc[pos] = mode == 1 ? bc[pos] - y : y; };
+    if (part == 0) {
+        // node (KCL) rows: I_x(k,i,j) - I_x(k,i-1,j) + I_y(k,i,j) - I_y(k,i,j-1) + caps + branches
+        const int k = bx / nx, i = bx - k * nx;
+        if (k >= S) return;
+        const cx<R>* X = xc + g.off_x + (int64_t)k * (nx - 1) * ny;
+        const cx<R>* Y = xc + g.off_y + (int64_t)k * nx * (ny - 1);
+        for (int j = threadIdx.x; j < ny; j += blockDim.x) {
+            const int ij = i * ny + j, node = k * nxy + ij;
+            const int64_t pos = g.off_v + node;
+            if (!g.mask[pos]) {
+                oc[pos] = zero<R>();
+                continue;
             }
-            if (mode == 1) y = rhs[(int64_t)col * ld + pos] - y;
+            cx<R> s = zero<R>();
+            if (i < nx - 1) s += X[i * ny + j];
+            if (i > 0) s -= X[(i - 1) * ny + j];
+            if (j < ny - 1) s += Y[i * (ny - 1) + j];
+            if (j > 0) s -= Y[i * (ny - 1) + j - 1];
+            for (int p = 0; p < g.np; ++p) {
+                const int u = g.pair_layers[2 * p], l = g.pair_layers[2 * p + 1];
+                if (u == k) s += xc[g.off_c + (int64_t)p * nxy + ij];
+                if (l == k) s -= xc[g.off_c + (int64_t)p * nxy + ij];
+            }
+            for (int e = g.node_br_ptr[node]; e < g.node_br_ptr[node + 1]; ++e) {
+                const int b = g.node_br_idx[e];
+                if (b > 0) s += xc[g.off_b + b - 1];
+                else s -= xc[g.off_b - b - 1];
+            }
+            put(pos, s);
         }
-        out[(int64_t)col * ld + pos] = y;
+    } else if (part == 1) {
+        // capacitance rows: z_cap I_c - (V[upper] - V[lower])
+        const int p = bx / nx, i = bx - p * nx;
+        if (p >= g.np) return;
+        const int u = g.pair_layers[2 * p], l = g.pair_layers[2 * p + 1];
+        const cx<R> zc = cvt<R>(zcap[(int64_t)op * g.np + p]);
+        for (int j = threadIdx.x; j < ny; j += blockDim.x) {
+            const int ij = i * ny + j;
+            const int64_t pos = g.off_c + (int64_t)p * nxy + ij;
+            if (!g.mask[pos]) {
+                oc[pos] = zero<R>();
+                continue;
+            }
+            put(pos, zc * xc[pos] - (V[u * nxy + ij] - V[l * nxy + ij]));
+        }
+    } else {
+        // branch rows z_br I_b - (V[a] - V[b]); padding zero
+        const int64_t nX = (int64_t)S * (nx - 1) * ny, nY = (int64_t)S * nx * (ny - 1);
+        const int64_t gap[5][2] = {{g.off_x + nX, g.off_y}, {g.off_y + nY, g.off_c},
+                                   {g.off_c + (int64_t)g.np * nxy, g.off_b}, {g.off_b + g.nbr, g.off_v},
+                                   {g.off_v + (int64_t)S * nxy, g.n}};
+        const int tid = bx * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+        for (int b = tid; b < g.nbr; b += nth) {
+            const int64_t pos = g.off_b + b;
+            if (!g.mask[pos]) {
+                oc[pos] = zero<R>();
+                continue;
+            }
+            put(pos, cvt<R>(zbr[(int64_t)op * g.nbr + b]) * xc[pos] - (V[g.branch_nodes[2 * b]] - V[g.branch_nodes[2 * b + 1]]));
+        }
+        for (int q = 0; q < 5; ++q)
+            for (int64_t pos = gap[q][0] + tid; pos < gap[q][1]; pos += nth) oc[pos] = zero<R>();
     }
 }
 
 template <typename R>
 void launch_tail(const Geo& g, const cx<R>* x, const cx<R>* rhs, cx<R>* out, int64_t ld, int ncol, const int* col_op,
                  const c64* zcap, const c64* zbr, int mode, const int* col_list, cudaStream_t st) {
-    int64_t items = g.n;
-    int blocks = (int)std::min<int64_t>((items + 255) / 256, 4096);
-    tail_kernel<R><<<dim3(blocks, ncol), 256, 0, st>>>(g, x, rhs, out, ld, col_op, zcap, zbr, mode, col_list);
+    const dim3 grid(std::max(g.nx * std::max(g.np, g.S), 1), 3, ncol);
+    tail_kernel<R><<<grid, 256, 0, st>>>(g, x, rhs, out, ld, col_op, zcap, zbr, mode, col_list);
     GT_LAUNCH_CHECK();
 }
 
-// s[perm[node]] = r_V[node] - (Ar^T D^-1 r_1)[node] for every kept node
-template <typename R>
-__global__ void pc_node_kernel(Geo g, const cx<R>* __restrict__ r, int64_t ld, cx<R>* __restrict__ sd,
-                               const int* __restrict__ col_op, const c64* __restrict__ tab, const int* __restrict__ col_list) {
+// D^-1 of the strips at one grid position applied to the S-vector u (sheets present: code); out[k] for the
+// sheets k present.  T: the table of the position's orientation.
+constexpr int SHEETS_MAX = 8;
+template <typename R, int MAXS>
+__device__ __forceinline__ void dinv_apply(const cx<R>* __restrict__ T, int S, int code, const cx<R>* u, cx<R>* out) {
+    const cx<R>* B = T + (int64_t)code * S * S;
+#pragma unroll
+    for (int k = 0; k < MAXS; ++k) {
+        out[k] = zero<R>();
+        if (k >= S || !((code >> k) & 1)) continue;
+#pragma unroll
+        for (int l = 0; l < MAXS; ++l)
+            if (l < S && ((code >> l) & 1)) out[k] += B[k * S + l] * u[l];
+    }
+}
+
+// s = r_V - Ar^T D^-1 r_1 at every kept node, written in node order (sd).  One block per grid row i and
+// column; a thread takes the S nodes of one position (i, j): the strips on either side of it are loaded once
+// for all sheets.
+template <typename R, int MAXS>
+__global__ void __launch_bounds__(256) pc_node_kernel(Geo g, const cx<R>* __restrict__ r, int64_t ld, cx<R>* __restrict__ sd,
+                                                      const int* __restrict__ col_op, const cx<R>* __restrict__ tab,
+                                                      const int* __restrict__ col_list) {
     const int col = col_list ? col_list[blockIdx.y] : blockIdx.y;
     const int op = col_op ? col_op[col] : 0;
-    const c64* T = tab + (int64_t)op * g.ntab;
+    const int S = g.S, nx = g.nx, ny = g.ny, nxy = nx * ny, NC = 1 << S;
+    const cx<R>* T = tab + (int64_t)op * g.ntab;
     const cx<R>* rc = r + (int64_t)col * ld;
-    const int S = g.S, nx = g.nx, ny = g.ny;
-    const int64_t nxy = (int64_t)nx * ny;
-    for (int64_t node = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; node < S * nxy; node += (int64_t)gridDim.x * blockDim.x) {
-        if (!g.mask[g.off_v + node]) continue;
-        int k = int(node / nxy);
-        int64_t ij = node - k * nxy;
-        int i = int(ij / ny), j = int(ij - (int64_t)i * ny);
-        cx<R> u[8];
-        cx<R> kcl = zero<R>();
-        // x strips (k,i,j) [a end] and (k,i-1,j) [b end]
-        for (int side = 0; side < 2; ++side) {
-            int ii = i - side;
-            if (ii < 0 || ii >= nx - 1) continue;
-            int code = g.code_x[(int64_t)ii * ny + j];
-            if (!((code >> k) & 1)) continue;
-            for (int l = 0; l < S; ++l)
-                u[l] = ((code >> l) & 1) ? rc[g.off_x + ((int64_t)l * (nx - 1) + ii) * ny + j] : zero<R>();
-            cx<R> t = dinv_strip<R>(T, S, 0, code, k, u);
-            if (side == 0) kcl += t; else kcl -= t;
+    const cx<R>* X = rc + g.off_x;
+    const cx<R>* Y = rc + g.off_y;
+    cx<R>* sc = sd + (int64_t)col * S * nxy;
+    const int i = blockIdx.x;
+    for (int j = threadIdx.x; j < ny; j += blockDim.x) {
+        const int ij = i * ny + j;
+        cx<R> kcl[MAXS], u[4][MAXS], t[MAXS];
+        int code[4], pq[4];
+#pragma unroll
+        for (int k = 0; k < MAXS; ++k) kcl[k] = zero<R>();
+        // x strips (., i, j) [their a end] and (., i-1, j) [b end]; y strips (., i, j) and (., i, j-1):
+        // all codes, then all strip loads, then the products
+#pragma unroll
+        for (int side = 0; side < 4; ++side) {
+            const bool xo = side < 2;
+            const int ii = xo ? i - side : i, jj = xo ? j : j - (side - 2);
+            const bool ok = xo ? (ii >= 0 && ii < nx - 1) : (jj >= 0 && jj < ny - 1);
+            pq[side] = xo ? ii * ny + jj : ii * (ny - 1) + jj;
+            code[side] = ok ? (xo ? g.code_x[pq[side]] : g.code_y[pq[side]]) : 0;
         }
-        for (int side = 0; side < 2; ++side) {
-            int jj = j - side;
-            if (jj < 0 || jj >= ny - 1) continue;
-            int code = g.code_y[(int64_t)i * (ny - 1) + jj];
-            if (!((code >> k) & 1)) continue;
-            for (int l = 0; l < S; ++l)
-                u[l] = ((code >> l) & 1) ? rc[g.off_y + ((int64_t)l * nx + i) * (ny - 1) + jj] : zero<R>();
-            cx<R> t = dinv_strip<R>(T, S, 1, code, k, u);
-            if (side == 0) kcl += t; else kcl -= t;
+#pragma unroll
+        for (int side = 0; side < 4; ++side) {
+            const bool xo = side < 2;
+            const int lstride = xo ? (nx - 1) * ny : nx * (ny - 1);
+            const cx<R>* base = xo ? X : Y;
+#pragma unroll
+            for (int l = 0; l < MAXS; ++l)
+                u[side][l] = (l < S && ((code[side] >> l) & 1)) ? base[(int64_t)l * lstride + pq[side]] : zero<R>();
+        }
+#pragma unroll
+        for (int side = 0; side < 4; ++side) {
+            if (!code[side]) continue;
+            dinv_apply<R, MAXS>(T + (int64_t)(side < 2 ? 0 : 1) * NC * S * S, S, code[side], u[side], t);
+            const bool plus = (side & 1) == 0;
+#pragma unroll
+            for (int k = 0; k < MAXS; ++k)
+                if (k < S) kcl[k] = plus ? kcl[k] + t[k] : kcl[k] - t[k];
         }
         for (int p = 0; p < g.np; ++p) {
-            int up = g.pair_layers[2 * p], lo = g.pair_layers[2 * p + 1];
-            if (up != k && lo != k) continue;
-            int64_t pos = g.off_c + p * nxy + ij;
+            const int up = g.pair_layers[2 * p], lo = g.pair_layers[2 * p + 1];
+            const int64_t pos = g.off_c + (int64_t)p * nxy + ij;
             if (!g.mask[pos]) continue;
-            cx<R> t = cvt<R>(T[g.tab_cap0 + p]) * rc[pos];
-            if (up == k) kcl += t; else kcl -= t;
+            const cx<R> v = T[g.tab_cap0 + p] * rc[pos];
+#pragma unroll
+            for (int k = 0; k < MAXS; ++k) {
+                if (k == up) kcl[k] += v;
+                if (k == lo) kcl[k] -= v;
+            }
         }
-        for (int e = g.node_br_ptr[node]; e < g.node_br_ptr[node + 1]; ++e) {
-            int b = g.node_br_idx[e];
-            int bb = (b > 0 ? b : -b) - 1;
-            cx<R> t = cvt<R>(T[g.tab_br0 + bb]) * rc[g.off_b + bb];
-            if (b > 0) kcl += t; else kcl -= t;
+#pragma unroll
+        for (int k = 0; k < MAXS; ++k) {
+            if (k >= S) break;
+            const int node = k * nxy + ij;
+            if (!g.mask[g.off_v + node]) continue;
+            cx<R> acc = kcl[k];
+            for (int e = g.node_br_ptr[node]; e < g.node_br_ptr[node + 1]; ++e) {
+                const int bq = g.node_br_idx[e];
+                const int bb = (bq > 0 ? bq : -bq) - 1;
+                const cx<R> v = T[g.tab_br0 + bb] * rc[g.off_b + bb];
+                acc = bq > 0 ? acc + v : acc - v;
+            }
+            sc[node] = rc[g.off_v + node] - acc;
         }
-        sd[(int64_t)col * S * nxy + node] = rc[g.off_v + node] - kcl;
     }
 }
 
 template <typename R>
-void launch_pc_node(const Geo& g, const cx<R>* r, int64_t ld, cx<R>* sd, int ncol, const int* col_op, const c64* tab,
+void launch_pc_node(const Geo& g, const cx<R>* r, int64_t ld, cx<R>* sd, int ncol, const int* col_op, const cx<R>* tab,
                     const int* col_list, cudaStream_t st) {
-    int64_t items = (int64_t)g.S * g.nx * g.ny;
-    int blocks = (int)std::min<int64_t>((items + 255) / 256, 4096);
-    pc_node_kernel<R><<<dim3(blocks, ncol), 256, 0, st>>>(g, r, ld, sd, col_op, tab, col_list);
+    if (g.S > SHEETS_MAX) throw CudaError{cudaErrorInvalidValue, "more sheets than the stencil kernels take"};
+    const dim3 grid(g.nx, ncol);
+    if (g.S <= 2) pc_node_kernel<R, 2><<<grid, 256, 0, st>>>(g, r, ld, sd, col_op, tab, col_list);
+    else if (g.S <= 4) pc_node_kernel<R, 4><<<grid, 256, 0, st>>>(g, r, ld, sd, col_op, tab, col_list);
+    else pc_node_kernel<R, 8><<<grid, 256, 0, st>>>(g, r, ld, sd, col_op, tab, col_list);
     GT_LAUNCH_CHECK();
 }
 
-// out = [D^-1 (r_1 + Ar y); y] over the whole dense vector (padding written zero)
-template <typename R>
-__global__ void pc_strip_kernel(Geo g, const cx<R>* __restrict__ r, int64_t ldr, const cx<R>* __restrict__ sd,
-                                cx<R>* __restrict__ out, int64_t ldo, const int* __restrict__ col_op,
-                                const c64* __restrict__ tab, const int* __restrict__ col_list) {
-    const int col = col_list ? col_list[blockIdx.y] : blockIdx.y;
+// out = [D^-1 (r_1 + Ar y); y] over the whole dense vector (padding written zero).  blockIdx.y selects the
+// part: 0 x strips (block per row i), 1 y strips (row i), 2 capacitances (pair p, row i), 3 nodes (sheet k,
+// row i), 4 branches and the padding between segments.  A strip thread takes all sheets of its position.
+template <typename R, int MAXS>
+__global__ void __launch_bounds__(256) pc_strip_kernel(Geo g, const cx<R>* __restrict__ r, int64_t ldr,
+                                                       const cx<R>* __restrict__ sd, cx<R>* __restrict__ out, int64_t ldo,
+                                                       const int* __restrict__ col_op, const cx<R>* __restrict__ tab,
+                                                       const int* __restrict__ col_list) {
+    const int col = col_list ? col_list[blockIdx.z] : blockIdx.z;
     const int op = col_op ? col_op[col] : 0;
-    const c64* T = tab + (int64_t)op * g.ntab;
+    const int S = g.S, nx = g.nx, ny = g.ny, nxy = nx * ny, NC = 1 << S;
+    const cx<R>* T = tab + (int64_t)op * g.ntab;
     const cx<R>* rc = r + (int64_t)col * ldr;
-    const cx<R>* yc = sd + (int64_t)col * g.S * g.nx * g.ny;
-    const int S = g.S, nx = g.nx, ny = g.ny;
-    const int64_t nxy = (int64_t)nx * ny;
-    const int64_t nX = (int64_t)S * (nx - 1) * ny, nY = (int64_t)S * nx * (ny - 1);
-    auto yv = [&](int64_t node) -> cx<R> { return yc[node]; };     // zero at nodes that are not kept
-    for (int64_t pos = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; pos < g.n; pos += (int64_t)gridDim.x * blockDim.x) {
-        int seg = seg_of(g, pos, nX, nY);
-        cx<R> o = zero<R>();
-        if (seg >= 0 && g.mask[pos]) {
-            if (seg == 0 || seg == 1) {
-                int64_t q = pos - (seg == 0 ? g.off_x : g.off_y);
-                int n0 = seg == 0 ? nx - 1 : nx, n1 = seg == 0 ? ny : ny - 1;
-                int k = int(q / ((int64_t)n0 * n1));
-                int64_t ij = q - (int64_t)k * n0 * n1;
-                int i = int(ij / n1), j = int(ij - (int64_t)i * n1);
-                int code = (seg == 0 ? g.code_x : g.code_y)[ij];
-                int di = seg == 0, dj = seg == 1;
-                int64_t segoff = seg == 0 ? g.off_x : g.off_y;
-                cx<R> u[8];
-                for (int l = 0; l < S; ++l) {
-                    if ((code >> l) & 1) {
-                        int64_t na = (int64_t)l * nxy + (int64_t)i * ny + j;
-                        int64_t nb = na + (int64_t)di * ny + dj;
-                        u[l] = rc[segoff + (int64_t)l * n0 * n1 + ij] + (yv(na) - yv(nb));
-                    } else {
-                        u[l] = zero<R>();
-                    }
-                }
-                o = dinv_strip<R>(T, S, seg, code, k, u);
-            } else if (seg == 2) {
-                int64_t q = pos - g.off_c;
-                int p = int(q / nxy);
-                int64_t ij = q - (int64_t)p * nxy;
-                int up = g.pair_layers[2 * p], lo = g.pair_layers[2 * p + 1];
-                o = cvt<R>(T[g.tab_cap0 + p]) * (rc[pos] + (yv(up * nxy + ij) - yv(lo * nxy + ij)));
-            } else if (seg == 3) {
-                int b = int(pos - g.off_b);
-                o = cvt<R>(T[g.tab_br0 + b]) * (rc[pos] + (yv(g.branch_nodes[2 * b]) - yv(g.branch_nodes[2 * b + 1])));
-            } else {
-                o = yv(pos - g.off_v);
-            }
+    const cx<R>* yc = sd + (int64_t)col * S * nxy;       // zero at nodes that are not kept
+    cx<R>* oc = out + (int64_t)col * ldo;
+    const int part = blockIdx.y, bx = blockIdx.x;
+    if (part <= 1) {
+        const bool xo = part == 0;
+        const int i = bx;
+        if (i >= (xo ? nx - 1 : nx)) return;
+        const int n1 = xo ? ny : ny - 1, lstride = (xo ? nx - 1 : nx) * n1;
+        const int64_t seg = xo ? g.off_x : g.off_y;
+        const uint8_t* codes = xo ? g.code_x : g.code_y;
+        const int dn = xo ? ny : 1;                          // node b = node a + dn
+        for (int j = threadIdx.x; j < n1; j += blockDim.x) {
+            const int pq = i * n1 + j, na = i * ny + j;
+            const int code = codes[pq];
+            cx<R> u[MAXS], t[MAXS];
+#pragma unroll
+            for (int l = 0; l < MAXS; ++l)
+                u[l] = (l < S && ((code >> l) & 1))
+                           ? rc[seg + (int64_t)l * lstride + pq] + (yc[l * nxy + na] - yc[l * nxy + na + dn])
+                           : zero<R>();
+            dinv_apply<R, MAXS>(T + (int64_t)(xo ? 0 : 1) * NC * S * S, S, code, u, t);
+#pragma unroll
+            for (int k = 0; k < MAXS; ++k)
+                if (k < S) oc[seg + (int64_t)k * lstride + pq] = t[k];      // zero where the strip is absent
         }
-        out[(int64_t)col * ldo + pos] = o;
+    } else if (part == 2) {
+        const int p = bx / nx, i = bx - p * nx;
+        if (p >= g.np) return;
+        const int up = g.pair_layers[2 * p], lo = g.pair_layers[2 * p + 1];
+        const cx<R> zc = T[g.tab_cap0 + p];
+        for (int j = threadIdx.x; j < ny; j += blockDim.x) {
+            const int ij = i * ny + j;
+            const int64_t pos = g.off_c + (int64_t)p * nxy + ij;
+            oc[pos] = g.mask[pos] ? zc * (rc[pos] + (yc[up * nxy + ij] - yc[lo * nxy + ij])) : zero<R>();
+        }
+    } else if (part == 3) {
+        const int k = bx / nx, i = bx - k * nx;
+        if (k >= S) return;
+        for (int j = threadIdx.x; j < ny; j += blockDim.x) {
+            const int node = k * nxy + i * ny + j;
+            oc[g.off_v + node] = yc[node];
+        }
+    } else {
+        // branches, then the padding: [off_x + nX, off_y), [off_y + nY, off_c), [off_c + np nxy, off_b),
+        // [off_b + nbr, off_v), [off_v + S nxy, n)
+        const int64_t nX = (int64_t)S * (nx - 1) * ny, nY = (int64_t)S * nx * (ny - 1);
+        const int64_t gap[5][2] = {{g.off_x + nX, g.off_y}, {g.off_y + nY, g.off_c},
+                                   {g.off_c + (int64_t)g.np * nxy, g.off_b}, {g.off_b + g.nbr, g.off_v},
+                                   {g.off_v + (int64_t)S * nxy, g.n}};
+        const int tid = bx * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+        for (int b = tid; b < g.nbr; b += nth) {
+            const int64_t pos = g.off_b + b;
+            oc[pos] = g.mask[pos] ? T[g.tab_br0 + b] * (rc[pos] + (yc[g.branch_nodes[2 * b]] - yc[g.branch_nodes[2 * b + 1]]))
+                                  : zero<R>();
+        }
+        for (int q = 0; q < 5; ++q)
+            for (int64_t pos = gap[q][0] + tid; pos < gap[q][1]; pos += nth) oc[pos] = zero<R>();
     }
 }
 
 template <typename R>
 void launch_pc_strip(const Geo& g, const cx<R>* r, int64_t ldr, const cx<R>* sd, cx<R>* out, int64_t ldo, int ncol,
-                     const int* col_op, const c64* tab, const int* col_list, cudaStream_t st) {
-    int blocks = (int)std::min<int64_t>((g.n + 255) / 256, 4096);
-    pc_strip_kernel<R><<<dim3(blocks, ncol), 256, 0, st>>>(g, r, ldr, sd, out, ldo, col_op, tab, col_list);
+                     const int* col_op, const cx<R>* tab, const int* col_list, cudaStream_t st) {
+    if (g.S > SHEETS_MAX) throw CudaError{cudaErrorInvalidValue, "more sheets than the stencil kernels take"};
+    const dim3 grid(std::max(g.nx * std::max(g.np, g.S), 1), 5, ncol);
+    if (g.S <= 2) pc_strip_kernel<R, 2><<<grid, 256, 0, st>>>(g, r, ldr, sd, out, ldo, col_op, tab, col_list);
+    else if (g.S <= 4) pc_strip_kernel<R, 4><<<grid, 256, 0, st>>>(g, r, ldr, sd, out, ldo, col_op, tab, col_list);
+    else pc_strip_kernel<R, 8><<<grid, 256, 0, st>>>(g, r, ldr, sd, out, ldo, col_op, tab, col_list);
     GT_LAUNCH_CHECK();
 }
 
@@ -263,9 +336,9 @@ void launch_gather(const int64_t* c2d, int64_t ncomp, const c64* in, int64_t ldi
 
 template void launch_tail<float>(const Geo&, const c32*, const c32*, c32*, int64_t, int, const int*, const c64*, const c64*, int, const int*, cudaStream_t);
 template void launch_tail<double>(const Geo&, const c64*, const c64*, c64*, int64_t, int, const int*, const c64*, const c64*, int, const int*, cudaStream_t);
-template void launch_pc_node<float>(const Geo&, const c32*, int64_t, c32*, int, const int*, const c64*, const int*, cudaStream_t);
+template void launch_pc_node<float>(const Geo&, const c32*, int64_t, c32*, int, const int*, const c32*, const int*, cudaStream_t);
 template void launch_pc_node<double>(const Geo&, const c64*, int64_t, c64*, int, const int*, const c64*, const int*, cudaStream_t);
-template void launch_pc_strip<float>(const Geo&, const c32*, int64_t, const c32*, c32*, int64_t, int, const int*, const c64*, const int*, cudaStream_t);
+template void launch_pc_strip<float>(const Geo&, const c32*, int64_t, const c32*, c32*, int64_t, int, const int*, const c32*, const int*, cudaStream_t);
 template void launch_pc_strip<double>(const Geo&, const c64*, int64_t, const c64*, c64*, int64_t, int, const int*, const c64*, const int*, cudaStream_t);
 
 }  // namespace gt

@@ -41,6 +41,17 @@ class GeometryDesc(C.Structure):
                 ("sterm_coef", DP)]
 
 
+PRECISIONS = {"mixed": 0, "fp64": 1, "mixed16": 2}
+
+
+def _precision(name: str) -> int:
+    """gt_solve_opts.precision: "mixed" FP32 inner GMRES + FP64 outer, "fp64" all FP64, "mixed16" as "mixed"
+    with the Krylov basis stored in FP16."""
+    if name not in PRECISIONS:
+        raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
+    return PRECISIONS[name]
+
+
 class SolveOpts(C.Structure):
     _fields_ = [("tol", C.c_double), ("restart", C.c_int32), ("max_its", C.c_int32), ("inner_tol", C.c_double),
                 ("precision", C.c_int32), ("max_outer", C.c_int32), ("reorth", C.c_double), ("outer_k", C.c_int32)]
@@ -163,7 +174,7 @@ class Geometry:
         ncol = len(idx)
         its = np.zeros(ncol, np.int32)
         res = np.zeros(ncol)
-        o = SolveOpts(tol, restart, max_its, inner_tol, 1 if precision == "fp64" else 0, max_outer, reorth, outer_k)
+        o = SolveOpts(tol, restart, max_its, inner_tol, _precision(precision), max_outer, reorth, outer_k)
         rc = self.lib.gt_solve_device(self.h, obj.h, ncol, _ptr(idx, C.c_int32), P(rhs_ptr), C.byref(o), P(x_ptr),
                                       _ptr(its, C.c_int32), _ptr(res, C.c_double), P(stream))
         if rc not in (GT_OK, GT_NOT_CONVERGED):
@@ -242,7 +253,7 @@ def solve(geom: Geometry, ops: list, rhs: np.ndarray, tol: float, restart: int =
     x = np.zeros_like(rhs)
     its = np.zeros(ncol, np.int32)
     res = np.zeros(ncol)
-    o = SolveOpts(tol, restart, max_its, inner_tol, 1 if precision == "fp64" else 0, max_outer, reorth, outer_k)
+    o = SolveOpts(tol, restart, max_its, inner_tol, _precision(precision), max_outer, reorth, outer_k)
     rc = lib.gt_solve(geom.h, obj.h, ncol, _ptr(idx, C.c_int32), _ptr(rhs.view(np.float64), C.c_double), C.byref(o),
                       _ptr(x.view(np.float64), C.c_double), _ptr(its, C.c_int32), _ptr(res, C.c_double), None)
     if rc not in (GT_OK, GT_NOT_CONVERGED):

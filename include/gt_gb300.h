@@ -81,7 +81,8 @@ typedef struct gt_solve_opts {
     int32_t restart;        /* inner GMRES cycle length */
     int32_t max_its;        /* total inner iterations allowed per column */
     double inner_tol;       /* relative residual reduction each inner FP32 cycle aims at */
-    int32_t precision;      /* 0: FP32 inner GMRES + FP64 refinement, 1: all FP64 (plain drop-in) */
+    int32_t precision;      /* 0: FP32 inner GMRES + FP64 refinement, 1: all FP64 (plain drop-in), 2: as 0 with
+                               the inner Krylov basis stored in FP16 (half the Gram-Schmidt traffic) */
     int32_t max_outer;      /* refinement steps */
     double reorth;          /* DGKS: re-orthogonalise when ||w|| fell below reorth x its norm before the first
                                Gram-Schmidt pass (0.7: the reference's rule, peec.py:3156; 0: never) */

@@ -65,7 +65,7 @@ def test_fp32_preconditioner(case):
     assert rel(y, z["prod_precond"]) < 1e-3
 
 
-@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("precision", ["mixed", "mixed16", "fp64"])
 def test_solves_match_reference(case, precision):
     """Every (net, frequency) of the fixture in one batch; rtol 1e-10 like the reference run.  Both stop at a
     backward error of 1e-10, so the solutions agree to within the conditioning times that."""
