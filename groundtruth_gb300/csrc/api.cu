@@ -357,7 +357,7 @@ static void precond(gt_geometry* G, gt_operators* ops, const cx<R>* r, int64_t l
     const double panel = (double)grp.ngroup * es * G->F.panel_total;
     {
         Scope s(P, "pc_node", st, nslot * es * (nXYC + nodes + nfac));
-        launch_pc_node<R>(G->geo, r, ldr, sd, nslot, slot_op, tab_of<R>(ops), col_list, st);
+        launch_pc_node<R>(G->geo, r, ldr, yfac, nslot, slot_op, tab_of<R>(ops), col_list, st);
     }
     const cx<R>* pan = panel_of<R>(ops);
     const int nlev = (int)G->level_ptr.size() - 1;
@@ -368,7 +368,7 @@ static void precond(gt_geometry* G, gt_operators* ops, const cx<R>* r, int64_t l
             Scope sl(P->levels ? P : nullptr, (std::string(sizeof(R) == 4 ? "fwd_f32.L" : "fwd_f64.L") +
                                                std::to_string(h)).c_str(), st, grp.ngroup * es * G->level_panel[h]);
             launch_fwd_level<R>(G->F, G->d_order + G->level_ptr[h], nf, G->level_maxnf[h], G->level_maxnown[h], pan,
-                                dinv_of<R>(ops), sd, zfac, uvec, yfac, grp, gmax, st);
+                                dinv_of<R>(ops), yfac, zfac, uvec, yfac, grp, gmax, st);
         }
     }
     {

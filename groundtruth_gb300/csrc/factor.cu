@@ -229,45 +229,69 @@ __device__ __forceinline__ void lds2(const c64* p, c64& a, c64& b) {
     b = p[1];
 }
 
-// acc[c] += l[kk] * x[k_kk][c] for LB terms, x k-major ([k][GMAXC]); kidx[kk]: the terms' rows of x
+// acc[c] += a * x[c] over all GMAXC columns of one k-major shared row x (unused columns hold zeros)
 template <typename R>
-__device__ __forceinline__ void mac_batch(cx<R>* acc, const cx<R>* l, const cx<R>* x, const int* kidx, int gc) {
+__device__ __forceinline__ void mac_row(cx<R>* acc, cx<R> a, const cx<R>* x) {
 #pragma unroll
-    for (int kk = 0; kk < LB; ++kk) {
-        const cx<R>* xk = x + kidx[kk] * GMAXC;
-#pragma unroll
-        for (int c2 = 0; c2 < GMAXC / 2; ++c2) {
-            if (2 * c2 >= gc) break;
-            cx<R> a, b;
-            lds2(xk + 2 * c2, a, b);
-            acc[2 * c2] += l[kk] * a;
-            acc[2 * c2 + 1] += l[kk] * b;
-        }
+    for (int c2 = 0; c2 < GMAXC / 2; ++c2) {
+        cx<R> u, v;
+        lds2(x + 2 * c2, u, v);
+        acc[2 * c2] += a * u;
+        acc[2 * c2 + 1] += a * v;
     }
 }
 
-// The forward rows of front f for a group: own rows of w (node-ordered s plus the children's updates)
+// acc[c] += sum_{t < cnt} A[t * lda] x[t * xs + c]: A a strided run of panel elements (part of one row or
+// column of a front's panel), x the matching k-major shared rows.  The first LB elements were loaded into
+// l ahead of time (prefetch_run, issued before the shared rows were staged); LB loads in flight after that.
+template <typename R>
+__device__ __forceinline__ void prefetch_run(const cx<R>* __restrict__ A, int lda, int cnt, cx<R>* l) {
+#pragma unroll
+    for (int u = 0; u < LB; ++u) l[u] = u < cnt ? A[u * lda] : zero<R>();
+}
+
+template <typename R>
+__device__ __forceinline__ void sweep(const cx<R>* __restrict__ A, int lda, const cx<R>* x, int xs, int cnt,
+                                      const cx<R>* l0, cx<R>* acc) {
+#pragma unroll
+    for (int u = 0; u < LB; ++u)
+        if (u < cnt) mac_row<R>(acc, l0[u], x + u * xs);
+    A += LB * lda;
+    x += LB * xs;
+    int t = LB;
+    for (; t + LB <= cnt; t += LB) {
+        cx<R> l[LB];
+#pragma unroll
+        for (int u = 0; u < LB; ++u) l[u] = A[u * lda];
+#pragma unroll
+        for (int u = 0; u < LB; ++u) mac_row<R>(acc, l[u], x + u * xs);
+        A += LB * lda;
+        x += LB * xs;
+    }
+    for (; t < cnt; ++t) {
+        mac_row<R>(acc, *A, x);
+        A += lda;
+        x += xs;
+    }
+}
+
+// The forward rows of front f for a group: own rows of w (s in factor order plus the children's updates)
 // into ws (k-major, ldw = GMAXC) and boundary rows r0 <= p < r1 into wt ([c][TR]).  Loads are issued four
 // at a time per thread ahead of their stores.
 template <typename R>
-__device__ __forceinline__ void fwd_gather(const Fronts& F, int f, const int* gs, int gc, const cx<R>* __restrict__ sd,
+__device__ __forceinline__ void fwd_gather(const Fronts& F, int f, const int* gs, int gc, const cx<R>* __restrict__ sf,
                                            const cx<R>* __restrict__ uvec, cx<R>* ws, cx<R>* wt, int TR, int r0, int r1) {
     const int nown = (int)F.nown[f];
     const int64_t own0 = F.own_start[f];
     const int tid = threadIdx.x, nth = blockDim.x;
     const int tot = gc * nown;
+    for (int q = tot + tid; q < GMAXC * nown; q += nth) ws[(q % nown) * GMAXC + q / nown] = zero<R>();
     for (int q0 = tid; q0 < tot; q0 += 4 * nth) {
-        int64_t node[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int q = min(q0 + u * nth, tot - 1), r = q % nown;
-            node[u] = F.iperm[own0 + r];
-        }
         cx<R> v[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             const int q = min(q0 + u * nth, tot - 1), c = q / nown;
-            v[u] = sd[(int64_t)gs[c] * F.nnode + node[u]];
+            v[u] = sf[(int64_t)gs[c] * F.nfac + own0 + (q - c * nown)];
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
@@ -307,8 +331,8 @@ __device__ __forceinline__ void fwd_gather(const Fronts& F, int f, const int* gs
 // order), the children's updates of the boundary rows to the front's own update-vector slots.
 template <typename R>
 __global__ void __launch_bounds__(256) fwd_assemble_kernel(Fronts F, const int64_t* __restrict__ front_list,
-                                                           const cx<R>* __restrict__ sd, cx<R>* __restrict__ uvec,
-                                                           cx<R>* __restrict__ wasm, Groups G, int ldw, int TR) {
+                                                           const cx<R>* sf, cx<R>* __restrict__ uvec, cx<R>* wasm,
+                                                           Groups G, int ldw, int TR) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<R>* ws = reinterpret_cast<cx<R>*>(smem_raw);   // [k][GMAXC]
     cx<R>* wt = ws + GMAXC * ldw;                      // [c][TR] boundary rows
@@ -320,7 +344,7 @@ __global__ void __launch_bounds__(256) fwd_assemble_kernel(Fronts F, const int64
     const int64_t own0 = F.own_start[f];
     for (int q = threadIdx.x; q < GMAXC * TR; q += blockDim.x) wt[q] = zero<R>();
     __syncthreads();
-    fwd_gather<R>(F, f, gs, gc, sd, uvec, ws, wt, TR, nown, nf);
+    fwd_gather<R>(F, f, gs, gc, sf, uvec, ws, wt, TR, nown, nf);
     for (int q = threadIdx.x; q < gc * nown; q += blockDim.x) {
         const int c = q / nown, r = q - c * nown;
         wasm[(int64_t)gs[c] * F.nfac + own0 + r] = ws[r * GMAXC + c];
@@ -333,11 +357,11 @@ __global__ void __launch_bounds__(256) fwd_assemble_kernel(Fronts F, const int64
 
 // pre: the front was assembled by fwd_assemble_kernel (own rows in wasm, boundary rows in uvec)
 template <typename R>
-__global__ void __launch_bounds__(SOLVE_THREADS) fwd_gemv_kernel(Fronts F, const int64_t* __restrict__ front_list, int nblk,
+__global__ void __launch_bounds__(SOLVE_THREADS, 2) fwd_gemv_kernel(Fronts F, const int64_t* __restrict__ front_list, int nblk,
                                                                  int rt, int kseg, const cx<R>* __restrict__ panel,
-                                                                 const cx<R>* __restrict__ dinv, const cx<R>* __restrict__ sd,
+                                                                 const cx<R>* __restrict__ dinv, const cx<R>* sf,
                                                                  cx<R>* __restrict__ z, cx<R>* __restrict__ uvec,
-                                                                 const cx<R>* __restrict__ wasm, Groups G, int ldw, int pre) {
+                                                                 const cx<R>* wasm, Groups G, int ldw, int pre) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int TR = 32 * rt;
     cx<R>* ws = reinterpret_cast<cx<R>*>(smem_raw);   // [k][GMAXC] own rows of w
@@ -354,10 +378,21 @@ __global__ void __launch_bounds__(SOLVE_THREADS) fwd_gemv_kernel(Fronts F, const
     const int gc = G.gptr[g + 1] - G.gptr[g], op = G.op[g];
     const int64_t own0 = F.own_start[f];
     const int tid = threadIdx.x, nth = blockDim.x;
+    const cx<R>* __restrict__ P = panel + (int64_t)op * F.panel_total + F.panel_off[f];
+    const int lane = tid & 31, warp = tid >> 5;
+    const int tile = warp % rt, seg = warp / rt;
+    const int rl = tile * 32 + lane, r = r0 + rl;
+    // the tile's rows need columns k < min(nown, last row + 1) (P is zero above its diagonal)
+    const int kmax = min(nown, r0 + tile * 32 + 32);
+    const int ks = (kmax + kseg - 1) / kseg;
+    const int k0 = min(kmax, seg * ks), k1 = min(kmax, k0 + ks);
+    const bool valid = r < r1;
+    // lanes past the block's rows sweep its last row (results dropped)
+    const cx<R>* A = P + (int64_t)k0 * nf + min(r, r1 - 1);
     if (pre) {
-        for (int q = tid; q < gc * nown; q += nth) {
+        for (int q = tid; q < GMAXC * nown; q += nth) {
             const int c = q / nown, r = q - c * nown;
-            ws[r * GMAXC + c] = wasm[(int64_t)gs[c] * F.nfac + own0 + r];
+            ws[r * GMAXC + c] = c < gc ? wasm[(int64_t)gs[c] * F.nfac + own0 + r] : zero<R>();
         }
         for (int q = tid; q < GMAXC * TR; q += nth) {
             const int c = q / TR, rr = q - c * TR, row = r0 + rr;
@@ -368,31 +403,14 @@ __global__ void __launch_bounds__(SOLVE_THREADS) fwd_gemv_kernel(Fronts F, const
     } else {
         for (int q = tid; q < GMAXC * TR; q += nth) wt[q] = zero<R>();
         __syncthreads();
-        fwd_gather<R>(F, f, gs, gc, sd, uvec, ws, wt, TR, r0, r1);
+        fwd_gather<R>(F, f, gs, gc, sf, uvec, ws, wt, TR, r0, r1);
     }
-    const cx<R>* __restrict__ P = panel + (int64_t)op * F.panel_total + F.panel_off[f];
-    const int lane = tid & 31, warp = tid >> 5;
-    const int tile = warp % rt, seg = warp / rt;
-    const int rl = tile * 32 + lane, r = r0 + rl;
-    // the tile's rows need columns k < min(nown, last row + 1) (P is zero above its diagonal)
-    const int kmax = min(nown, r0 + tile * 32 + 32);
-    const int ks = (kmax + kseg - 1) / kseg;
-    const int k0 = min(kmax, seg * ks), k1 = min(kmax, k0 + ks);
-    const bool valid = r < r1;
+    cx<R> l0[LB];
+    prefetch_run<R>(A, nf, k1 - k0, l0);
     cx<R> acc[GMAXC];
 #pragma unroll
     for (int c = 0; c < GMAXC; ++c) acc[c] = zero<R>();
-    for (int k8 = k0; k8 < k1; k8 += LB) {
-        cx<R> l[LB];
-        int kidx[LB];
-#pragma unroll
-        for (int kk = 0; kk < LB; ++kk) {
-            const int k = k8 + kk;
-            l[kk] = (valid && k < k1) ? P[(int64_t)k * nf + r] : zero<R>();
-            kidx[kk] = min(k, k1 - 1);
-        }
-        mac_batch<R>(acc, l, ws, kidx, gc);
-    }
+    sweep<R>(A, nf, ws + k0 * GMAXC, GMAXC, k1 - k0, l0, acc);
     if (kseg > 1) {
 #pragma unroll
         for (int c = 0; c < GMAXC; ++c)
@@ -422,12 +440,13 @@ __global__ void __launch_bounds__(SOLVE_THREADS) fwd_gemv_kernel(Fronts F, const
 }
 
 template <typename R>
-__global__ void __launch_bounds__(SOLVE_THREADS) bwd_gemv_kernel(Fronts F, const int64_t* __restrict__ front_list, int nblk,
-                                                                 int ct, int iseg, const cx<R>* __restrict__ panel_rm,
+__global__ void __launch_bounds__(SOLVE_THREADS, 2) bwd_gemv_kernel(Fronts F, const int64_t* __restrict__ front_list, int nblk,
+                                                                 int ct, int iseg, int cw,
+                                                                 const cx<R>* __restrict__ panel_rm,
                                                                  const cx<R>* __restrict__ z, cx<R>* __restrict__ y,
                                                                  cx<R>* __restrict__ sd, Groups G, int ldv) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int TC = 32 * ct;
+    const int TC = cw * ct;       // a tile: cw columns, its warp's 32 / cw lane groups take alternate rows
     cx<R>* v = reinterpret_cast<cx<R>*>(smem_raw);    // [i - kb0][GMAXC]: rows kb0 .. nf of [z_own; y_bnd]
     cx<R>* red = v + GMAXC * ldv;                      // [seg][c][TC]
     const int b = blockIdx.x % nblk, rest = blockIdx.x / nblk;
@@ -442,7 +461,26 @@ __global__ void __launch_bounds__(SOLVE_THREADS) bwd_gemv_kernel(Fronts F, const
     const int64_t own0 = F.own_start[f];
     const int64_t* bnd = F.bnd_idx + F.bnd_ptr[f];
     const int tid = threadIdx.x, nth = blockDim.x;
+    const cx<R>* __restrict__ P = panel_rm + (int64_t)op * F.panel_total + F.panel_off[f];   // (nf x nown) row-major
+    const int lane = tid & 31, warp = tid >> 5;
+    const int nph = 32 / cw, ph = lane / cw;
+    const int tile = warp % ct, seg = warp / ct;
+    const int kl = tile * cw + (lane - ph * cw), k = kb0 + kl;
+    // the tile's columns need rows i >= its first column (P is zero above its diagonal)
+    const int it0 = min(nf, kb0 + tile * cw);
+    const int is = (nf - it0 + iseg - 1) / iseg;
+    const int i0 = min(nf, it0 + seg * is), i1 = min(nf, i0 + is);
+    const int cnt = max(0, (i1 - i0 - ph + nph - 1) / nph);
+    const bool valid = k < kb1;
+    // lanes past the block's columns sweep its last column (results dropped)
+    const cx<R>* A = P + (int64_t)(i0 + ph) * nown + min(k, kb1 - 1);
+    cx<R> l0[LB];
+    prefetch_run<R>(A, nph * nown, cnt, l0);
     const int nv = nf - kb0, tot = gc * nv;
+    for (int q = gc * nv + tid; q < GMAXC * nv; q += nth) {
+        const int c = q / nv;
+        v[(q - c * nv) * GMAXC + c] = zero<R>();
+    }
     for (int q0 = tid; q0 < tot; q0 += 4 * nth) {
         int64_t src[4];
 #pragma unroll
@@ -463,33 +501,21 @@ __global__ void __launch_bounds__(SOLVE_THREADS) bwd_gemv_kernel(Fronts F, const
         }
     }
     __syncthreads();
-    const cx<R>* __restrict__ P = panel_rm + (int64_t)op * F.panel_total + F.panel_off[f];   // (nf x nown) row-major
-    const int lane = tid & 31, warp = tid >> 5;
-    const int tile = warp % ct, seg = warp / ct;
-    const int kl = tile * 32 + lane, k = kb0 + kl;
-    // the tile's columns need rows i >= its first column (P is zero above its diagonal)
-    const int it0 = min(nf, kb0 + tile * 32);
-    const int is = (nf - it0 + iseg - 1) / iseg;
-    const int i0 = min(nf, it0 + seg * is), i1 = min(nf, i0 + is);
-    const bool valid = k < kb1;
     cx<R> acc[GMAXC];
 #pragma unroll
     for (int c = 0; c < GMAXC; ++c) acc[c] = zero<R>();
-    for (int i8 = i0; i8 < i1; i8 += LB) {
-        cx<R> l[LB];
-        int kidx[LB];
+    sweep<R>(A, nph * nown, v + (i0 + ph - kb0) * GMAXC, nph * GMAXC, cnt, l0, acc);
+    if (nph == 2) {
 #pragma unroll
-        for (int ii = 0; ii < LB; ++ii) {
-            const int i = i8 + ii;
-            l[ii] = (valid && i < i1) ? P[(int64_t)i * nown + k] : zero<R>();
-            kidx[ii] = min(i, i1 - 1) - kb0;
+        for (int c = 0; c < GMAXC; ++c) {
+            acc[c].re += __shfl_xor_sync(0xffffffffu, acc[c].re, 16);
+            acc[c].im += __shfl_xor_sync(0xffffffffu, acc[c].im, 16);
         }
-        mac_batch<R>(acc, l, v, kidx, gc);
     }
     if (iseg > 1) {
 #pragma unroll
         for (int c = 0; c < GMAXC; ++c)
-            if (c < gc) red[(seg * GMAXC + c) * TC + kl] = acc[c];
+            if (c < gc && ph == 0) red[(seg * GMAXC + c) * TC + kl] = acc[c];
         __syncthreads();
         for (int q = tid; q < gc * TC; q += nth) {
             const int c = q / TC, kk = q - c * TC;
@@ -499,7 +525,7 @@ __global__ void __launch_bounds__(SOLVE_THREADS) bwd_gemv_kernel(Fronts F, const
             y[(int64_t)gs[c] * F.nfac + own0 + kb0 + kk] = s;
             sd[(int64_t)gs[c] * F.nnode + F.iperm[own0 + kb0 + kk]] = s;
         }
-    } else if (valid) {
+    } else if (valid && ph == 0) {
         const int64_t node = F.iperm[own0 + k];
 #pragma unroll
         for (int c = 0; c < GMAXC; ++c)
@@ -525,7 +551,7 @@ static void solve_shape(int ntask, int ntile, int inner, int& per_blk, int& nseg
 
 template <typename R>
 void launch_fwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, int max_nown,
-                      const cx<R>* panel, const cx<R>* dinv, const cx<R>* sd, cx<R>* z, cx<R>* uvec, cx<R>* wasm,
+                      const cx<R>* panel, const cx<R>* dinv, const cx<R>* sf, cx<R>* z, cx<R>* uvec, cx<R>* wasm,
                       const Groups& G, int gmax, cudaStream_t st) {
     if (gmax > GMAXC) throw CudaError{cudaErrorInvalidValue, "column group larger than the solve kernels take"};
     const int ntask = nf_level * G.ngroup;
@@ -538,12 +564,12 @@ void launch_fwd_level(const Fronts& F, const int64_t* front_list, int nf_level, 
         const int TRa = std::max(max_nf - 1, 1);
         const size_t sa = (size_t)GMAXC * (ldw + TRa) * sizeof(cx<R>);
         smem_attr<R>((const void*)fwd_assemble_kernel<R>, sa);
-        fwd_assemble_kernel<R><<<ntask, 256, sa, st>>>(F, front_list, sd, uvec, wasm, G, ldw, TRa);
+        fwd_assemble_kernel<R><<<ntask, 256, sa, st>>>(F, front_list, sf, uvec, wasm, G, ldw, TRa);
         GT_LAUNCH_CHECK();
     }
     const size_t sm = (size_t)GMAXC * (ldw + 32 * rt + (kseg > 1 ? kseg * 32 * rt : 0)) * sizeof(cx<R>);
     smem_attr<R>((const void*)fwd_gemv_kernel<R>, sm);
-    fwd_gemv_kernel<R><<<ntask * nblk, 32 * rt * kseg, sm, st>>>(F, front_list, nblk, rt, kseg, panel, dinv, sd, z, uvec,
+    fwd_gemv_kernel<R><<<ntask * nblk, 32 * rt * kseg, sm, st>>>(F, front_list, nblk, rt, kseg, panel, dinv, sf, z, uvec,
                                                                 wasm, G, ldw, pre);
     GT_LAUNCH_CHECK();
 }
@@ -554,14 +580,16 @@ void launch_bwd_level(const Fronts& F, const int64_t* front_list, int nf_level, 
                       cudaStream_t st) {
     if (gmax > GMAXC) throw CudaError{cudaErrorInvalidValue, "column group larger than the solve kernels take"};
     const int ntask = nf_level * G.ngroup;
-    const int ntile = ceil_div(max_nown, 32);
+    // tiles of 16 columns (two lane groups on alternate rows) where they waste fewer lanes than 32
+    const int cw = ceil_div(max_nown, 16) * 16 - max_nown < ceil_div(max_nown, 32) * 32 - max_nown ? 16 : 32;
+    const int ntile = ceil_div(max_nown, cw);
     int ct, iseg;
     solve_shape(ntask, ntile, max_nf, ct, iseg);
     const int nblk = ceil_div(ntile, ct), ldv = std::max(max_nf, 1);
-    const size_t sm = (size_t)GMAXC * (ldv + (iseg > 1 ? iseg * 32 * ct : 0)) * sizeof(cx<R>);
+    const size_t sm = (size_t)GMAXC * (ldv + (iseg > 1 ? iseg * cw * ct : 0)) * sizeof(cx<R>);
     smem_attr<R>((const void*)bwd_gemv_kernel<R>, sm);
-    bwd_gemv_kernel<R><<<ntask * nblk, 32 * ct * iseg, sm, st>>>(F, front_list, nblk, ct, iseg, panel_rm, z, y, sd, G,
-                                                                 ldv);
+    bwd_gemv_kernel<R><<<ntask * nblk, 32 * ct * iseg, sm, st>>>(F, front_list, nblk, ct, iseg, cw, panel_rm, z, y, sd,
+                                                                 G, ldv);
     GT_LAUNCH_CHECK();
 }
 

@@ -50,8 +50,8 @@ template <typename R>
 void launch_tail(const Geo& g, const cx<R>* x, const cx<R>* rhs, cx<R>* out, int64_t ld, int ncol, const int* col_op,
                  const c64* zcap, const c64* zbr, int mode, const int* col_list, cudaStream_t st);
 
-// preconditioner: s = r_V - Ar^T D^-1 r_1 into node order (sd [col][S*nx*ny]); then, with y in node order in
-// sd (zero at nodes that are not kept), out = [D^-1 (r_1 + Ar y); y]
+// preconditioner: s = r_V - Ar^T D^-1 r_1 into factor order (sd [col][nfac]); then, with y in node order in
+// sd [col][S*nx*ny] (zero at nodes that are not kept), out = [D^-1 (r_1 + Ar y); y]
 template <typename R>
 void launch_pc_node(const Geo& g, const cx<R>* r, int64_t ld, cx<R>* sd, int ncol, const int* col_op,
                     const cx<R>* tab, const int* col_list, cudaStream_t st);
@@ -110,12 +110,12 @@ struct Groups {
     const int* gslot;
     const int* op;
 };
-// forward: own rows from s in node order (sd), results to z (factor order) and the update vectors (wasm:
-// factor-ordered scratch for fronts assembled ahead of a split product);
+// forward: own rows from s in factor order (sf), results to z (factor order) and the update vectors (wasm:
+// factor-ordered scratch for fronts assembled ahead of a split product, may be sf itself);
 // backward: reads z and the ancestors' y, writes y (factor order) and sd (node order)
 template <typename R>
 void launch_fwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, int max_nown,
-                      const cx<R>* panel, const cx<R>* dinv, const cx<R>* sd, cx<R>* z, cx<R>* uvec, cx<R>* wasm,
+                      const cx<R>* panel, const cx<R>* dinv, const cx<R>* sf, cx<R>* z, cx<R>* uvec, cx<R>* wasm,
                       const Groups& G, int gmax, cudaStream_t st);
 template <typename R>
 void launch_bwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, int max_nown,

@@ -133,7 +133,7 @@ __device__ __forceinline__ void dinv_apply(const cx<R>* __restrict__ T, int S, i
     }
 }
 
-// s = r_V - Ar^T D^-1 r_1 at every kept node, written in node order (sd).  One block per grid row i and
+// s = r_V - Ar^T D^-1 r_1 at every kept node, written in factor order (sf[col][nfac], through perm).  One block per grid row i and
 // column; a thread takes the S nodes of one position (i, j): the strips on either side of it are loaded once
 // for all sheets.
 template <typename R, int MAXS>
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(256) pc_node_kernel(Geo g, const cx<R>* __rest
     const cx<R>* rc = r + (int64_t)col * ld;
     const cx<R>* X = rc + g.off_x;
     const cx<R>* Y = rc + g.off_y;
-    cx<R>* sc = sd + (int64_t)col * S * nxy;
+    cx<R>* sc = sd + (int64_t)col * g.nfac;
     const int i = blockIdx.x;
     for (int j = threadIdx.x; j < ny; j += blockDim.x) {
         const int ij = i * ny + j;
@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(256) pc_node_kernel(Geo g, const cx<R>* __rest
                 const cx<R> v = T[g.tab_br0 + bb] * rc[g.off_b + bb];
                 acc = bq > 0 ? acc + v : acc - v;
             }
-            sc[node] = rc[g.off_v + node] - acc;
+            sc[g.perm[node]] = rc[g.off_v + node] - acc;
         }
     }
 }
