@@ -53,7 +53,31 @@ __global__ void __launch_bounds__(DOT_THREADS) dots_kernel(const B* __restrict__
         nrm += norm2(wv[e]);
     }
     const B* Vs = V + (int64_t)slot * lds;
-    for (int i = 0; i < nv; ++i) {
+    int i = 0;
+    // full chunks: UN basis vectors' loads in flight together (FP32 arithmetic; FP64 keeps one)
+    constexpr int UN = sizeof(R) == 4 ? 2 : 1;
+    if (base + DOT_CHUNK <= n) {
+        for (; i + UN <= nv; i += UN) {
+            cx<R> v[UN][DOT_EPT];
+#pragma unroll
+            for (int u = 0; u < UN; ++u)
+#pragma unroll
+                for (int e = 0; e < DOT_EPT; ++e) v[u][e] = bload(Vs + (int64_t)(i + u) * ldv + base + e * DOT_THREADS + tid);
+#pragma unroll
+            for (int u = 0; u < UN; ++u) {
+                R ar = 0, ai = 0;
+#pragma unroll
+                for (int e = 0; e < DOT_EPT; ++e) {
+                    ar += v[u][e].re * wv[e].re + v[u][e].im * wv[e].im;
+                    ai += v[u][e].re * wv[e].im - v[u][e].im * wv[e].re;
+                }
+                ar = shfl_sum(ar);
+                ai = shfl_sum(ai);
+                if (lane == 0) red[warp][i + u] = mk<double>((double)ar * vs, (double)ai * vs);
+            }
+        }
+    }
+    for (; i < nv; ++i) {
         const B* Vi = Vs + (int64_t)i * ldv;
         R ar = 0, ai = 0;
 #pragma unroll
@@ -129,7 +153,25 @@ __global__ void __launch_bounds__(DOT_THREADS) update_kernel(const B* __restrict
         acc[e] = q < n ? w[(int64_t)slot * ldw + q] : zero<R>();
     }
     const B* Vs = V + (int64_t)slot * lds;
-    for (int i = 0; i < nv; ++i) {
+    int i = 0;
+    // full chunks: UN basis vectors' loads in flight together (FP32 arithmetic; FP64 keeps one)
+    constexpr int UN = sizeof(R) == 4 ? 4 : 1;
+    if (base + DOT_CHUNK <= n) {
+        for (; i + UN <= nv; i += UN) {
+            cx<R> v[UN][DOT_EPT];
+#pragma unroll
+            for (int u = 0; u < UN; ++u)
+#pragma unroll
+                for (int e = 0; e < DOT_EPT; ++e) v[u][e] = bload(Vs + (int64_t)(i + u) * ldv + base + e * DOT_THREADS + tid);
+#pragma unroll
+            for (int u = 0; u < UN; ++u) {
+                const cx<R> hi = hs[i + u];
+#pragma unroll
+                for (int e = 0; e < DOT_EPT; ++e) acc[e] += hi * v[u][e];
+            }
+        }
+    }
+    for (; i < nv; ++i) {
         const cx<R> hi = hs[i];
         const B* Vi = Vs + (int64_t)i * ldv;
 #pragma unroll

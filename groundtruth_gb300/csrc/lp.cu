@@ -24,25 +24,28 @@ __global__ void __launch_bounds__(1024) lp_pass_a(const cx<R>* __restrict__ x, i
                           int rows, const cx<R>* __restrict__ tw, cx<R>* __restrict__ T, const int* __restrict__ col_list) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw);
-    const int stride = srow(P1);
+    const int P = PL ? PL : P1;                  // compile-time when specialised
+    const int stride = srow(P);
     const int i0 = blockIdx.x * rows;
     const int s = blockIdx.y;
     const int col = col_list ? col_list[blockIdx.z] : blockIdx.z;
     const cx<R>* xs = x + (int64_t)col * ldx + off + (int64_t)s * n0 * n1;
-    for (int idx = threadIdx.x; idx < rows * P1; idx += blockDim.x) {
-        int r = idx / P1, j = idx - r * P1;
-        int i = i0 + r;
-        buf[r * stride + spad(j)] = (i < n0 && j < n1) ? xs[(int64_t)i * n1 + j] : zero<R>();
+    // each team loads, transforms and keeps its own row
+    const int team = P / 8;
+    const int r = threadIdx.x / team, t = threadIdx.x - r * team;
+    const int i = i0 + r;
+    if (r < rows) {
+        cx<R>* row = buf + r * stride;
+        for (int j = t; j < P; j += team) row[spad(j)] = (i < n0 && j < n1) ? xs[(int64_t)i * n1 + j] : zero<R>();
     }
     __syncthreads();
-    const int team = P1 / 8;
-    const int r = threadIdx.x / team, t = threadIdx.x - r * team;
-    fft_row_t<R, false, PL>(buf + r * stride, r < rows, P1, tw, team, t);
-    cx<R>* Ts = T + ((int64_t)blockIdx.z * S + s) * (int64_t)P1 * n0;
-    for (int idx = threadIdx.x; idx < rows * P1; idx += blockDim.x) {
-        int c = idx / rows, rr = idx - c * rows;
-        int i = i0 + rr;
-        if (i < n0) Ts[(int64_t)c * n0 + i] = buf[rr * stride + spad(c)];
+    fft_row_t<R, false, PL>(buf + r * stride, r < rows, P, tw, team, t);
+    // written transposed: rows (a power of two) consecutive entries per frequency column
+    cx<R>* Ts = T + ((int64_t)blockIdx.z * S + s) * (int64_t)P * n0;
+    const int lr = __ffs(rows) - 1;
+    for (int idx = threadIdx.x; idx < rows * P; idx += blockDim.x) {
+        const int c = idx >> lr, rr = idx & (rows - 1);
+        if (i0 + rr < n0) Ts[(int64_t)c * n0 + i0 + rr] = buf[rr * stride + spad(c)];
     }
 }
 
@@ -51,27 +54,28 @@ __global__ void __launch_bounds__(1024) lp_pass_b(int S, int n0, int P0, int P1,
                           const cx<R>* __restrict__ tw, cx<R>* __restrict__ T) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw);
-    const int stride = srow(P0);
+    const int P = PL ? PL : P0;                  // compile-time when specialised
+    const int stride = srow(P);
     const int c = blockIdx.x;
     const int b0 = blockIdx.y * bt;
     const int nb = min(bt, ncol - b0);
     const int nrows = nb * S;
-    for (int idx = threadIdx.x; idx < nrows * P0; idx += blockDim.x) {
-        int row = idx / P0, p = idx - row * P0;
-        int b = row / S, s = row - b * S;
-        buf[row * stride + spad(p)] = p < n0 ? T[(((int64_t)(b0 + b) * S + s) * P1 + c) * n0 + p] : zero<R>();
-    }
-    __syncthreads();
-    const int team = P0 / 8;
+    // each team loads, transforms and stores its own row (column b, sheet s)
+    const int team = P / 8;
     const int row = threadIdx.x / team, t = threadIdx.x - row * team;
-    fft_row_t<R, false, PL>(buf + row * stride, row < nrows, P0, tw, team, t);
+    const int rb = row / S, rs = row - rb * S;
+    cx<R>* Trow = T + (((int64_t)(b0 + rb) * S + rs) * P1 + c) * n0;
+    if (row < nrows)
+        for (int p = t; p < P; p += team) buf[row * stride + spad(p)] = p < n0 ? Trow[p] : zero<R>();
+    __syncthreads();
+    fft_row_t<R, false, PL>(buf + row * stride, row < nrows, P, tw, team, t);
     // spectrum multiply-add over sheets, one (column, pixel) per thread iteration
-    const int Q0 = P0 / 2 + 1;
+    const int Q0 = P / 2 + 1;
     const int q1 = min(c, P1 - c);
     const R* Kc = spec + (int64_t)q1 * Q0 * S * S;
-    for (int idx = threadIdx.x; idx < nb * P0; idx += blockDim.x) {
-        int b = idx / P0, p = idx - b * P0;
-        int q0 = min(p, P0 - p);
+    for (int idx = threadIdx.x; idx < nb * P; idx += blockDim.x) {
+        const int b = idx / P, p = idx - b * P;
+        const int q0 = min(p, P - p);
         const R* K = Kc + (int64_t)q0 * S * S;
         cx<R> u[MAXS];
 #pragma unroll
@@ -93,12 +97,9 @@ __global__ void __launch_bounds__(1024) lp_pass_b(int S, int n0, int P0, int P1,
         }
     }
     __syncthreads();
-    fft_row_t<R, true, PL>(buf + row * stride, row < nrows, P0, tw, team, t);
-    for (int idx = threadIdx.x; idx < nrows * n0; idx += blockDim.x) {
-        int rr = idx / n0, p = idx - rr * n0;
-        int b = rr / S, s = rr - b * S;
-        T[(((int64_t)(b0 + b) * S + s) * P1 + c) * n0 + p] = buf[rr * stride + spad(p)];
-    }
+    fft_row_t<R, true, PL>(buf + row * stride, row < nrows, P, tw, team, t);
+    if (row < nrows)
+        for (int p = t; p < n0; p += team) Trow[p] = buf[row * stride + spad(p)];
 }
 
 // mode 0: out = R_t x + j w L - (V[a] - V[b]); 1: out = rhs - (that); 2: out = L
@@ -111,30 +112,32 @@ __global__ void __launch_bounds__(1024) lp_pass_c(const cx<R>* __restrict__ T, c
                           const int* __restrict__ col_list) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw);
-    const int stride = srow(P1);
+    const int P = PL ? PL : P1;                  // compile-time when specialised
+    const int stride = srow(P);
     const int i0 = blockIdx.x * rows;
     const int s = blockIdx.y;
     const int col = col_list ? col_list[blockIdx.z] : blockIdx.z;
-    const cx<R>* Ts = T + ((int64_t)blockIdx.z * S + s) * (int64_t)P1 * n0;
-    for (int idx = threadIdx.x; idx < rows * P1; idx += blockDim.x) {
-        int c = idx / rows, rr = idx - c * rows;
-        int i = i0 + rr;
+    const cx<R>* Ts = T + ((int64_t)blockIdx.z * S + s) * (int64_t)P * n0;
+    const int lr = __ffs(rows) - 1;
+    for (int idx = threadIdx.x; idx < rows * P; idx += blockDim.x) {
+        const int c = idx >> lr, rr = idx & (rows - 1);
+        const int i = i0 + rr;
         buf[rr * stride + spad(c)] = i < n0 ? Ts[(int64_t)c * n0 + i] : zero<R>();
     }
     __syncthreads();
-    const int team = P1 / 8;
+    const int team = P / 8;
     const int r = threadIdx.x / team, t = threadIdx.x - r * team;
-    fft_row_t<R, true, PL>(buf + r * stride, r < rows, P1, tw, team, t);
+    fft_row_t<R, true, PL>(buf + r * stride, r < rows, P, tw, team, t);
     const int op = col_op ? col_op[col] : 0;
     const R w = omega ? R(omega[op]) : R(0);
     const cx<R> z = zs ? cvt<R>(zs[(int64_t)op * S + s]) : zero<R>();
     const int64_t base = (int64_t)col * ld;
-    for (int idx = threadIdx.x; idx < rows * n1; idx += blockDim.x) {
-        int rr = idx / n1, j = idx - rr * n1;
-        int i = i0 + rr;
-        if (i >= n0) continue;
+    // each team finishes its own row
+    const int i = i0 + r;
+    if (r >= rows || i >= n0) return;
+    for (int j = t; j < n1; j += team) {
         int64_t pos = off + ((int64_t)s * n0 + i) * n1 + j;
-        cx<R> L = buf[rr * stride + spad(j)];
+        cx<R> L = buf[r * stride + spad(j)];
         cx<R> y;
         if (mode == 2) {
             y = mask[pos] ? L : zero<R>();
@@ -162,6 +165,7 @@ template <typename R>
 void lp_shapes(const LpArgs<R>& a, int* rows_out, int* bt_out) {
     const int teamA = a.P1 / 8, teamB = a.P0 / 8;
     int rows = a.rows > 0 ? a.rows : 4;
+    while (rows & (rows - 1)) rows &= rows - 1;     // the row passes index rows by shifts: a power of two
     while (rows > 1 && (rows * teamA > 1024 || (size_t)rows * srow(a.P1) * sizeof(cx<R>) > 160 * 1024)) rows /= 2;
     int bt = a.bt > 0 ? a.bt : 2;
     while (bt > 1 && (bt * a.S * teamB > 1024 || (size_t)bt * a.S * srow(a.P0) * sizeof(cx<R>) > 160 * 1024)) bt /= 2;
