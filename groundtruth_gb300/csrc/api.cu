@@ -612,12 +612,17 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
             }
             precond<R>(G, ops, vin, ldin, z, n, na, W.slot_op, grp, gmax, zfac, yfac, uvec, sd, st, W.act);
             matvec<R>(G, ops, z, nullptr, w, n, na, W.slot_op, 0, T, st, W.act);
+            // classical Gram-Schmidt: the dot products read the j+1 basis vectors and w; the update reads
+            // them again, reads w and writes it
             {
-                // classical Gram-Schmidt: the j+1 basis vectors read twice, w read twice and written once
-                Scope sc(P, narrow ? "gs_f32_b16" : sizeof(R) == 4 ? "gs_f32" : "gs_f64", st,
-                         (double)ns * n * (2.0 * (j + 1) * sizeof(B) + 3.0 * sizeof(cx<R>)));
+                Scope sc(P, narrow ? "gs_dots_f32_b16" : sizeof(R) == 4 ? "gs_dots_f32" : "gs_dots_f64", st,
+                         (double)ns * n * ((j + 1.0) * sizeof(B) + sizeof(cx<R>)));
                 launch_dots<R, B>(V, n, lds, j + 1, w, n, n, ns, S.active, W.partial, nch, st, vs);
                 launch_reduce(W.partial, nch, j + 1, ns, S.active, S.hvec, S.ldh, 0, st);
+            }
+            {
+                Scope sc(P, narrow ? "gs_update_f32_b16" : sizeof(R) == 4 ? "gs_update_f32" : "gs_update_f64", st,
+                         (double)ns * n * ((j + 1.0) * sizeof(B) + 2.0 * sizeof(cx<R>)));
                 launch_update<R, B>(V, n, lds, j + 1, S.hvec, S.ldh, w, n, n, ns, S.active, W.partial, nch, -1, st, vs);
                 launch_reduce(W.partial, nch, 0, ns, S.active, S.hn2, 1, 0, st);
                 launch_dgks(S, j, st);

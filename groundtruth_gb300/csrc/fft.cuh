@@ -77,6 +77,42 @@ template <typename R, bool INV> __device__ __forceinline__ void dft8(cx<R>* v) {
     v[7] = e[3] - o3;
 }
 
+// the same transforms when the upper half of the inputs is zero (v[RAD/2 ..] not read)
+template <typename R, bool INV> __device__ __forceinline__ void dft4_h(cx<R>* v) {
+    const cx<R> a = v[0], b = v[1], jb = mj<R, INV>(v[1]);
+    v[0] = a + b;
+    v[1] = a + jb;
+    v[2] = a - b;
+    v[3] = a - jb;
+}
+
+template <typename R, bool INV> __device__ __forceinline__ void dft8_h(cx<R>* v) {
+    const R h = FftConst<R>::h;
+    cx<R> e[4] = {v[0], v[2], zero<R>(), zero<R>()};
+    cx<R> o[4] = {v[1], v[3], zero<R>(), zero<R>()};
+    dft4_h<R, INV>(e);
+    dft4_h<R, INV>(o);
+    cx<R> o1 = INV ? mk<R>(h * (o[1].re - o[1].im), h * (o[1].re + o[1].im))
+                   : mk<R>(h * (o[1].re + o[1].im), h * (o[1].im - o[1].re));
+    cx<R> o2 = mj<R, INV>(o[2]);
+    cx<R> o3 = INV ? mk<R>(-h * (o[3].re + o[3].im), h * (o[3].re - o[3].im))
+                   : mk<R>(h * (o[3].im - o[3].re), -h * (o[3].re + o[3].im));
+    v[0] = e[0] + o[0];
+    v[4] = e[0] - o[0];
+    v[1] = e[1] + o1;
+    v[5] = e[1] - o1;
+    v[2] = e[2] + o2;
+    v[6] = e[2] - o2;
+    v[3] = e[3] + o3;
+    v[7] = e[3] - o3;
+}
+
+template <typename R, bool INV, int RAD> __device__ __forceinline__ void dftr_h(cx<R>* v) {
+    if constexpr (RAD == 2) v[1] = v[0];
+    else if constexpr (RAD == 4) dft4_h<R, INV>(v);
+    else dft8_h<R, INV>(v);
+}
+
 template <typename R, bool INV, int RAD> __device__ __forceinline__ void dftr(cx<R>* v) {
     if constexpr (RAD == 2) dft2<R, INV>(v);
     else if constexpr (RAD == 3) dft3<R, INV>(v);
@@ -144,20 +180,24 @@ __device__ void fft_row(cx<R>* row, bool active, int P, const cx<R>* __restrict_
 
 
 // --- the same transform with the length known at compile time: every stride, plan step and index
-// division constant-folds (the runtime form above serves the lengths without a specialisation)
-template <typename R, bool INV, int RAD, int P, int NS>
+// division constant-folds (the runtime form above serves the lengths without a specialisation).
+// Pruning for the zero-padded convolution (P a power of two): HIN, the row's upper half is zero on input
+// (the first stage reads only j + r P/RAD with r < RAD/2); HOUT, only the lower half of the output is
+// wanted (the last stage, whose outputs are j + r P/RAD, computes and stores r < RAD/2 only).
+template <typename R, bool INV, int RAD, int P, int NS, bool HIN, bool HOUT>
 __device__ __forceinline__ void fft_stage_c(cx<R>* row, bool active, const cx<R>* __restrict__ tw, int t) {
     constexpr int TEAM = P / 8;
     constexpr int NB = (8 + RAD - 1) / RAD;
     constexpr int NBF = P / RAD;
     constexpr int STRIDE = P / (NS * RAD);
+    constexpr int RIN = HIN ? RAD / 2 : RAD, ROUT = HOUT ? RAD / 2 : RAD;
     cx<R> v[NB][RAD];
 #pragma unroll
     for (int q = 0; q < NB; ++q) {
         const int j = t + q * TEAM;
         if (active && j < NBF) {
 #pragma unroll
-            for (int r = 0; r < RAD; ++r) v[q][r] = row[spad(j + r * NBF)];
+            for (int r = 0; r < RIN; ++r) v[q][r] = row[spad(j + r * NBF)];
         }
     }
     __syncthreads();
@@ -174,30 +214,32 @@ __device__ __forceinline__ void fft_stage_c(cx<R>* row, bool active, const cx<R>
                     v[q][r] = v[q][r] * w;
                 }
             }
-            dftr<R, INV, RAD>(v[q]);
+            if constexpr (HIN) dftr_h<R, INV, RAD>(v[q]);
+            else dftr<R, INV, RAD>(v[q]);
             const int base = (j / NS) * NS * RAD + k;
 #pragma unroll
-            for (int r = 0; r < RAD; ++r) row[spad(base + r * NS)] = v[q][r];
+            for (int r = 0; r < ROUT; ++r) row[spad(base + r * NS)] = v[q][r];
         }
     }
     __syncthreads();
 }
 
-template <typename R, bool INV, int P, int NS>
+template <typename R, bool INV, int P, int NS, bool HIN, bool HOUT>
 __device__ __forceinline__ void fft_stages_c(cx<R>* row, bool active, const cx<R>* __restrict__ tw, int t) {
     constexpr int REST = P / NS;
     if constexpr (REST > 1) {
         constexpr int RAD = (NS == 1 && P % 3 == 0) ? 3 : (REST % 8 == 0 ? 8 : REST);
-        fft_stage_c<R, INV, RAD, P, NS>(row, active, tw, t);
-        fft_stages_c<R, INV, P, NS * RAD>(row, active, tw, t);
+        constexpr bool first = NS == 1, last = REST == RAD, pow2 = (P & (P - 1)) == 0;
+        fft_stage_c<R, INV, RAD, P, NS, HIN && first && pow2, HOUT && last && pow2>(row, active, tw, t);
+        fft_stages_c<R, INV, P, NS * RAD, HIN, HOUT>(row, active, tw, t);
     }
 }
 
-// P = 0: the runtime form with length p
-template <typename R, bool INV, int P>
+// P = 0: the runtime form with length p (no pruning).  HIN / HOUT as for fft_stage_c.
+template <typename R, bool INV, int P, bool HIN = false, bool HOUT = false>
 __device__ __forceinline__ void fft_row_t(cx<R>* row, bool active, int p, const cx<R>* __restrict__ tw, int team, int t) {
     if constexpr (P == 0) fft_row<R, INV>(row, active, p, tw, team, t);
-    else fft_stages_c<R, INV, P, 1>(row, active, tw, t);
+    else fft_stages_c<R, INV, P, 1, HIN, HOUT>(row, active, tw, t);
 }
 
 }  // namespace gt

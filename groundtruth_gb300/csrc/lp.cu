@@ -3,7 +3,9 @@
 // the strip rows of _HostMath.matvec, peec.py:3043-3062).
 //
 // An orientation's currents are a grid (S, n0, n1) of the dense vector; the FFT grid is (P0, P1) with
-// P >= 2n - 1 per axis, so the circular convolution equals the linear one on the grid.
+// P >= 2n - 1 per axis, so the circular convolution equals the linear one on the grid.  P is even, so
+// n <= P / 2: forward transforms see a zero upper half and inverse ones are read in their lower half only
+// (the pruned stages of fft.cuh).
 //   pass A  row FFTs (length P1) of the n0 rows, zero padded; written transposed T[col][s][c][i]
 //   pass B  per pixel column c: column FFTs (length P0) of all sheets, the per-pixel S x S real spectrum
 //           multiply-add (the quadrant mirrored: K(p0, p1) = Kq(min(p0, P0-p0), min(p1, P1-p1))), inverse
@@ -39,7 +41,7 @@ __global__ void __launch_bounds__(1024) lp_pass_a(const cx<R>* __restrict__ x, i
         for (int j = t; j < P; j += team) row[spad(j)] = (i < n0 && j < n1) ? xs[(int64_t)i * n1 + j] : zero<R>();
     }
     __syncthreads();
-    fft_row_t<R, false, PL>(buf + r * stride, r < rows, P, tw, team, t);
+    fft_row_t<R, false, PL, true, false>(buf + r * stride, r < rows, P, tw, team, t);
     // written transposed: rows (a power of two) consecutive entries per frequency column
     cx<R>* Ts = T + ((int64_t)blockIdx.z * S + s) * (int64_t)P * n0;
     const int lr = __ffs(rows) - 1;
@@ -68,7 +70,7 @@ __global__ void __launch_bounds__(1024) lp_pass_b(int S, int n0, int P0, int P1,
     if (row < nrows)
         for (int p = t; p < P; p += team) buf[row * stride + spad(p)] = p < n0 ? Trow[p] : zero<R>();
     __syncthreads();
-    fft_row_t<R, false, PL>(buf + row * stride, row < nrows, P, tw, team, t);
+    fft_row_t<R, false, PL, true, false>(buf + row * stride, row < nrows, P, tw, team, t);
     // spectrum multiply-add over sheets, one (column, pixel) per thread iteration
     const int Q0 = P / 2 + 1;
     const int q1 = min(c, P1 - c);
@@ -97,7 +99,7 @@ __global__ void __launch_bounds__(1024) lp_pass_b(int S, int n0, int P0, int P1,
         }
     }
     __syncthreads();
-    fft_row_t<R, true, PL>(buf + row * stride, row < nrows, P, tw, team, t);
+    fft_row_t<R, true, PL, false, true>(buf + row * stride, row < nrows, P, tw, team, t);
     if (row < nrows)
         for (int p = t; p < n0; p += team) Trow[p] = buf[row * stride + spad(p)];
 }
@@ -127,7 +129,7 @@ __global__ void __launch_bounds__(1024) lp_pass_c(const cx<R>* __restrict__ T, c
     __syncthreads();
     const int team = P / 8;
     const int r = threadIdx.x / team, t = threadIdx.x - r * team;
-    fft_row_t<R, true, PL>(buf + r * stride, r < rows, P, tw, team, t);
+    fft_row_t<R, true, PL, false, true>(buf + r * stride, r < rows, P, tw, team, t);
     const int op = col_op ? col_op[col] : 0;
     const R w = omega ? R(omega[op]) : R(0);
     const cx<R> z = zs ? cvt<R>(zs[(int64_t)op * S + s]) : zero<R>();
