@@ -436,7 +436,7 @@ static void ensure_ws(gt_geometry* G, int ncol, int m, int prec, int kmax) {
     W.rho = p.alloc<double>(ncol);
     W.bnorm = p.alloc<double>(ncol);
     const int nch = nchunks(n);
-    W.npart = p.alloc<c64>((size_t)ncol * nch);
+    W.npart = p.alloc<c64>((size_t)ncol * std::max(nch, update_chunks(n)));
     W.npart_k = p.alloc<c64>((size_t)ncol * nch * (kmax + 2));
     W.nred = p.alloc<c64>(ncol);
     W.V = p.alloc<unsigned char>((size_t)ncol * (m + 1) * n * eb);
@@ -509,7 +509,7 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
     Workspace& W = *G->ws;
     const int64_t n = G->geo.n;
     const int m = o.restart;
-    const int nch = nchunks(n);
+    const int nch = nchunks(n), nchu = update_chunks(n);
     Profiler* P = &G->prof;
     GT_CUDA(cudaMemcpyAsync(W.col_op, h_col_op, ncol * sizeof(int), cudaMemcpyHostToDevice, st));
     GT_CUDA(cudaMemsetAsync(W.x64, 0, (size_t)ncol * n * sizeof(c64), st));
@@ -623,16 +623,16 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
             {
                 Scope sc(P, narrow ? "gs_update_f32_b16" : sizeof(R) == 4 ? "gs_update_f32" : "gs_update_f64", st,
                          (double)ns * n * ((j + 1.0) * sizeof(B) + 2.0 * sizeof(cx<R>)));
-                launch_update<R, B>(V, n, lds, j + 1, S.hvec, S.ldh, w, n, n, ns, S.active, W.partial, nch, -1, st, vs);
-                launch_reduce(W.partial, nch, 0, ns, S.active, S.hn2, 1, 0, st);
+                launch_update<R, B>(V, n, lds, j + 1, S.hvec, S.ldh, w, n, n, ns, S.active, W.partial, -1, st, vs);
+                launch_reduce(W.partial, nchu, 0, ns, S.active, S.hn2, 1, 0, st);
                 launch_dgks(S, j, st);
             }
             {
                 Scope sc(P, "gs_reorth", st);
                 launch_dots<R, B>(V, n, lds, j + 1, w, n, n, ns, S.reorth, W.partial, nch, st, vs);
                 launch_reduce(W.partial, nch, j + 1, ns, S.reorth, S.h2vec, S.ldh, 0, st);
-                launch_update<R, B>(V, n, lds, j + 1, S.h2vec, S.ldh, w, n, n, ns, S.reorth, W.partial, nch, -1, st, vs);
-                launch_reduce(W.partial, nch, 0, ns, S.reorth, S.hn2b, 1, 0, st);
+                launch_update<R, B>(V, n, lds, j + 1, S.h2vec, S.ldh, w, n, n, ns, S.reorth, W.partial, -1, st, vs);
+                launch_reduce(W.partial, nchu, 0, ns, S.reorth, S.hn2b, 1, 0, st);
             }
             {
                 Scope sc(P, "gmres_small", st);
@@ -659,7 +659,7 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
         GT_CUDA(cudaMemsetAsync(w, 0, (size_t)ns * n * sizeof(cx<R>), st));
         {
             Scope sc(P, "combine", st, (double)ns * n * (jdone * sizeof(B) + 2.0 * sizeof(cx<R>)));
-            launch_update<R, B>(V, n, lds, jdone, S.y, S.ldh, w, n, n, ns, nullptr, nullptr, nch, 1, st, vs);
+            launch_update<R, B>(V, n, lds, jdone, S.y, S.ldh, w, n, n, ns, nullptr, nullptr, 1, st, vs);
         }
         act.resize(ns);
         for (int q = 0; q < ns; ++q) act[q] = q;
@@ -684,18 +684,19 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
             if (k > 0) {
                 launch_dots<double>(W.gQ, ldk, n, k, Qk, n, n, ncol, W.colact, W.npart_k, nch, st);
                 launch_reduce(W.npart_k, nch, k, ncol, W.colact, W.gbeta, K + 1, 0, st);
-                launch_update<double>(W.gQ, ldk, n, k, W.gbeta, K + 1, Qk, n, n, ncol, W.colact, W.npart, nch, -1, st);
-                launch_update<double>(W.gP, ldk, n, k, W.gbeta, K + 1, Pk, n, n, ncol, W.colact, nullptr, nch, -1, st);
+                launch_update<double>(W.gQ, ldk, n, k, W.gbeta, K + 1, Qk, n, n, ncol, W.colact, W.npart, -1, st);
+                launch_update<double>(W.gP, ldk, n, k, W.gbeta, K + 1, Pk, n, n, ncol, W.colact, nullptr, -1, st);
+                launch_reduce(W.npart, nchu, 0, ncol, W.colact, W.gnu2, 1, 0, st);
             } else {
                 launch_dots<double>(Qk, 0, n, 0, Qk, n, n, ncol, W.colact, W.npart, nch, st);
+                launch_reduce(W.npart, nch, 0, ncol, W.colact, W.gnu2, 1, 0, st);
             }
-            launch_reduce(W.npart, nch, 0, ncol, W.colact, W.gnu2, 1, 0, st);
             launch_gcr_scale(Pk, Qk, n, W.gnu2, W.colact, n, ncol, st);
             launch_dots<double>(Qk, 0, n, 1, W.r64, n, n, ncol, W.colact, W.npart_k, nch, st);
             launch_reduce(W.npart_k, nch, 1, ncol, W.colact, W.galpha, 2, 0, st);
-            launch_update<double>(Pk, 0, n, 1, W.galpha, 2, W.x64, n, n, ncol, W.colact, nullptr, nch, 1, st);
-            launch_update<double>(Qk, 0, n, 1, W.galpha, 2, W.r64, n, n, ncol, W.colact, W.npart, nch, -1, st);
-            launch_reduce(W.npart, nch, 0, ncol, W.colact, W.nred, 1, 0, st);
+            launch_update<double>(Pk, 0, n, 1, W.galpha, 2, W.x64, n, n, ncol, W.colact, nullptr, 1, st);
+            launch_update<double>(Qk, 0, n, 1, W.galpha, 2, W.r64, n, n, ncol, W.colact, W.npart, -1, st);
+            launch_reduce(W.npart, nchu, 0, ncol, W.colact, W.nred, 1, 0, st);
             launch_sqrt_norms_active(W.nred, 1, ncol, W.colact, W.rho, st);
         }
         ++k;

@@ -30,6 +30,11 @@ __device__ __forceinline__ void bstore(h16c* p, c32 v) { p->v = __floats2half2_r
 constexpr int DOT_THREADS = 256;
 constexpr int DOT_EPT = 8;
 constexpr int DOT_CHUNK = DOT_THREADS * DOT_EPT;
+// the update keeps fewer elements per thread (more blocks resident, several basis vectors in flight)
+constexpr int UPD_EPT = 4;
+constexpr int UPD_CHUNK = DOT_THREADS * UPD_EPT;
+
+int update_chunks(int64_t n) { return (int)((n + UPD_CHUNK - 1) / UPD_CHUNK); }
 constexpr int MAXV = 256;
 
 // partial[(slot * nchunk + chunk) * (nv + 1) + i] = sum over the chunk of conj(V_i) w, i < nv; index nv: |w|^2
@@ -128,7 +133,8 @@ void launch_reduce(const c64* partial, int nchunk, int nv, int nslot, const int*
     GT_LAUNCH_CHECK();
 }
 
-// w += sign * sum_i h_i V_i (sign -1: Gram-Schmidt; +1: the cycle's combination); partial |w|^2 per chunk
+// w += sign * sum_i h_i V_i (sign -1: Gram-Schmidt; +1: the cycle's combination); partial |w|^2 per chunk of
+// UPD_CHUNK elements (nchunk = update_chunks(n))
 template <typename R, typename B>
 __global__ void __launch_bounds__(DOT_THREADS) update_kernel(const B* __restrict__ V, int64_t ldv, int64_t lds,
                                                              int nv, const c64* __restrict__ h, int ldh,
@@ -145,10 +151,10 @@ __global__ void __launch_bounds__(DOT_THREADS) update_kernel(const B* __restrict
         hs[i] = mk<R>(R(sign * v.re * vs), R(sign * v.im * vs));
     }
     __syncthreads();
-    const int64_t base = (int64_t)blockIdx.x * DOT_CHUNK;
-    cx<R> acc[DOT_EPT];
+    const int64_t base = (int64_t)blockIdx.x * UPD_CHUNK;
+    cx<R> acc[UPD_EPT];
 #pragma unroll
-    for (int e = 0; e < DOT_EPT; ++e) {
+    for (int e = 0; e < UPD_EPT; ++e) {
         int64_t q = base + e * DOT_THREADS + tid;
         acc[e] = q < n ? w[(int64_t)slot * ldw + q] : zero<R>();
     }
@@ -156,18 +162,18 @@ __global__ void __launch_bounds__(DOT_THREADS) update_kernel(const B* __restrict
     int i = 0;
     // full chunks: UN basis vectors' loads in flight together (FP32 arithmetic; FP64 keeps one)
     constexpr int UN = sizeof(R) == 4 ? 4 : 1;
-    if (base + DOT_CHUNK <= n) {
+    if (base + UPD_CHUNK <= n) {
         for (; i + UN <= nv; i += UN) {
-            cx<R> v[UN][DOT_EPT];
+            cx<R> v[UN][UPD_EPT];
 #pragma unroll
             for (int u = 0; u < UN; ++u)
 #pragma unroll
-                for (int e = 0; e < DOT_EPT; ++e) v[u][e] = bload(Vs + (int64_t)(i + u) * ldv + base + e * DOT_THREADS + tid);
+                for (int e = 0; e < UPD_EPT; ++e) v[u][e] = bload(Vs + (int64_t)(i + u) * ldv + base + e * DOT_THREADS + tid);
 #pragma unroll
             for (int u = 0; u < UN; ++u) {
                 const cx<R> hi = hs[i + u];
 #pragma unroll
-                for (int e = 0; e < DOT_EPT; ++e) acc[e] += hi * v[u][e];
+                for (int e = 0; e < UPD_EPT; ++e) acc[e] += hi * v[u][e];
             }
         }
     }
@@ -175,14 +181,14 @@ __global__ void __launch_bounds__(DOT_THREADS) update_kernel(const B* __restrict
         const cx<R> hi = hs[i];
         const B* Vi = Vs + (int64_t)i * ldv;
 #pragma unroll
-        for (int e = 0; e < DOT_EPT; ++e) {
+        for (int e = 0; e < UPD_EPT; ++e) {
             int64_t q = base + e * DOT_THREADS + tid;
             if (q < n) acc[e] += hi * bload(Vi + q);
         }
     }
     R nrm = 0;
 #pragma unroll
-    for (int e = 0; e < DOT_EPT; ++e) {
+    for (int e = 0; e < UPD_EPT; ++e) {
         int64_t q = base + e * DOT_THREADS + tid;
         if (q < n) {
             w[(int64_t)slot * ldw + q] = acc[e];
@@ -201,7 +207,8 @@ __global__ void __launch_bounds__(DOT_THREADS) update_kernel(const B* __restrict
 
 template <typename R, typename B>
 void launch_update(const B* V, int64_t ldv, int64_t lds, int nv, const c64* h, int ldh, cx<R>* w, int64_t ldw,
-                   int64_t n, int nslot, const int* active, c64* partial, int nchunk, int sign, cudaStream_t st, R vs) {
+                   int64_t n, int nslot, const int* active, c64* partial, int sign, cudaStream_t st, R vs) {
+    const int nchunk = update_chunks(n);
     update_kernel<R, B><<<dim3(nchunk, nslot), DOT_THREADS, 0, st>>>(V, ldv, lds, nv, h, ldh, w, ldw, n, active,
                                                                       partial, nchunk, sign, vs);
     GT_LAUNCH_CHECK();
@@ -210,9 +217,9 @@ void launch_update(const B* V, int64_t ldv, int64_t lds, int nv, const c64* h, i
 template void launch_dots<float, c32>(const c32*, int64_t, int64_t, int, const c32*, int64_t, int64_t, int, const int*, c64*, int, cudaStream_t, float);
 template void launch_dots<float, h16c>(const h16c*, int64_t, int64_t, int, const c32*, int64_t, int64_t, int, const int*, c64*, int, cudaStream_t, float);
 template void launch_dots<double, c64>(const c64*, int64_t, int64_t, int, const c64*, int64_t, int64_t, int, const int*, c64*, int, cudaStream_t, double);
-template void launch_update<float, c32>(const c32*, int64_t, int64_t, int, const c64*, int, c32*, int64_t, int64_t, int, const int*, c64*, int, int, cudaStream_t, float);
-template void launch_update<float, h16c>(const h16c*, int64_t, int64_t, int, const c64*, int, c32*, int64_t, int64_t, int, const int*, c64*, int, int, cudaStream_t, float);
-template void launch_update<double, c64>(const c64*, int64_t, int64_t, int, const c64*, int, c64*, int64_t, int64_t, int, const int*, c64*, int, int, cudaStream_t, double);
+template void launch_update<float, c32>(const c32*, int64_t, int64_t, int, const c64*, int, c32*, int64_t, int64_t, int, const int*, c64*, int, cudaStream_t, float);
+template void launch_update<float, h16c>(const h16c*, int64_t, int64_t, int, const c64*, int, c32*, int64_t, int64_t, int, const int*, c64*, int, cudaStream_t, float);
+template void launch_update<double, c64>(const c64*, int64_t, int64_t, int, const c64*, int, c64*, int64_t, int64_t, int, const int*, c64*, int, cudaStream_t, double);
 
 // ------------------------------------------------------------------------------------------ per-slot scalars
 // After the first Gram-Schmidt pass: hvec[0..j] = h, hvec[j+1] = |w_before|^2; hn2 = |w_after|^2 (reduced

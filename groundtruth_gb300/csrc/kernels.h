@@ -134,9 +134,10 @@ void launch_dots(const B* V, int64_t ldv, int64_t lds, int nv, const cx<R>* w, i
                  const int* active, c64* partial, int nchunk, cudaStream_t st, R vs = R(1));
 void launch_reduce(const c64* partial, int nchunk, int nv, int nslot, const int* active, c64* out, int ldo, int mode,
                    cudaStream_t st);
+// partial (if not null): |w|^2 per update chunk, update_chunks(n) per slot
+int update_chunks(int64_t n);
 template <typename R, typename B>
 void launch_update(const B* V, int64_t ldv, int64_t lds, int nv, const c64* h, int ldh, cx<R>* w, int64_t ldw,
-                   int64_t n, int nslot, const int* active, c64* partial, int nchunk, int sign, cudaStream_t st,
-                   R vs = R(1));
+                   int64_t n, int nslot, const int* active, c64* partial, int sign, cudaStream_t st, R vs = R(1));
 
 }  // namespace gt
