@@ -328,13 +328,25 @@ static void matvec(gt_geometry* G, gt_operators* ops, const cx<R>* x, const cx<R
         if (G->o[k].rows[pr] == 0 && ncol >= 8 && mode != 2) tune_lp<R>(G->o[k], a, pr, st);
         a.rows = o.rows[pr];
         a.bt = o.bt[pr];
-        // algorithmic bytes: x, V and out over the strips, the intermediate grid written by pass A, read and
-        // written by pass B, read by pass C, the spectrum once per column group of pass B
-        const double es = sizeof(cx<R>), plane = (double)a.S * o.n0 * o.n1;
-        const double bytes = ncol * es * (3 * plane + 4.0 * a.S * o.n0 * o.P1) +
-                             std::ceil(ncol / 8.0) * sizeof(R) * a.S * a.S * (o.P0 / 2 + 1) * (o.P1 / 2 + 1);
-        Scope s(P, sizeof(R) == 4 ? "lp_fft_f32" : "lp_fft_f64", st, bytes);
-        launch_lp<R>(a, st);
+        // algorithmic bytes per pass: A reads the strips and writes the intermediate grid; B reads and writes
+        // the grid and reads the spectrum once per column group; C reads the grid, the strips and V and
+        // writes out
+        const double es = sizeof(cx<R>), plane = (double)a.S * o.n0 * o.n1, grid = (double)a.S * o.n0 * o.P1;
+        const bool f32 = sizeof(R) == 4;
+        {
+            Scope s(P, f32 ? "lp_a_f32" : "lp_a_f64", st, ncol * es * (plane + grid));
+            launch_lp_pass<R>(a, 0, st);
+        }
+        {
+            Scope s(P, f32 ? "lp_b_f32" : "lp_b_f64", st,
+                    ncol * es * 2.0 * grid +
+                        std::ceil(ncol / 8.0) * sizeof(R) * a.S * a.S * (o.P0 / 2 + 1) * (o.P1 / 2 + 1));
+            launch_lp_pass<R>(a, 1, st);
+        }
+        {
+            Scope s(P, f32 ? "lp_c_f32" : "lp_c_f64", st, ncol * es * (grid + 2.0 * plane));
+            launch_lp_pass<R>(a, 2, st);
+        }
     }
     if (mode != 2) {
         const double nXY = (double)(G->geo.off_c - G->geo.off_x);

@@ -41,6 +41,8 @@ template <typename R> struct LpArgs {
 };
 
 template <typename R> void launch_lp(const LpArgs<R>& a, cudaStream_t st);
+// one of the three passes (0: row FFTs, 1: column FFTs + spectrum, 2: inverse row FFTs + epilogue)
+template <typename R> void launch_lp_pass(const LpArgs<R>& a, int pass, cudaStream_t st);
 // the launch shapes launch_lp would use for these arguments
 template <typename R> void lp_shapes(const LpArgs<R>& a, int* rows, int* bt);
 

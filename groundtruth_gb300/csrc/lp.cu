@@ -209,33 +209,44 @@ static void launch_c(const LpArgs<R>& a, int rows, cudaStream_t st) {
 }
 
 template <typename R>
-void launch_lp(const LpArgs<R>& a, cudaStream_t st) {
+void launch_lp_pass(const LpArgs<R>& a, int pass, cudaStream_t st) {
     int rows, bt;
     lp_shapes<R>(a, &rows, &bt);
-    switch (a.P1) {
+    if (pass == 0) {
+        switch (a.P1) {
 #define GT_CASE(L) \
     case L: launch_a<R, L>(a, rows, st); break;
-        GT_LP_LENGTHS(GT_CASE)
+            GT_LP_LENGTHS(GT_CASE)
 #undef GT_CASE
-        default: launch_a<R, 0>(a, rows, st);
-    }
-    switch (a.P0) {
+            default: launch_a<R, 0>(a, rows, st);
+        }
+    } else if (pass == 1) {
+        switch (a.P0) {
 #define GT_CASE(L) \
     case L: launch_b<R, L>(a, bt, st); break;
-        GT_LP_LENGTHS(GT_CASE)
+            GT_LP_LENGTHS(GT_CASE)
 #undef GT_CASE
-        default: launch_b<R, 0>(a, bt, st);
-    }
-    switch (a.P1) {
+            default: launch_b<R, 0>(a, bt, st);
+        }
+    } else {
+        switch (a.P1) {
 #define GT_CASE(L) \
     case L: launch_c<R, L>(a, rows, st); break;
-        GT_LP_LENGTHS(GT_CASE)
+            GT_LP_LENGTHS(GT_CASE)
 #undef GT_CASE
-        default: launch_c<R, 0>(a, rows, st);
+            default: launch_c<R, 0>(a, rows, st);
+        }
     }
 }
 
+template <typename R>
+void launch_lp(const LpArgs<R>& a, cudaStream_t st) {
+    for (int pass = 0; pass < 3; ++pass) launch_lp_pass<R>(a, pass, st);
+}
+
 template void launch_lp<float>(const LpArgs<float>&, cudaStream_t);
+template void launch_lp_pass<float>(const LpArgs<float>&, int, cudaStream_t);
+template void launch_lp_pass<double>(const LpArgs<double>&, int, cudaStream_t);
 template void launch_lp<double>(const LpArgs<double>&, cudaStream_t);
 template void lp_shapes<float>(const LpArgs<float>&, int*, int*);
 template void lp_shapes<double>(const LpArgs<double>&, int*, int*);
