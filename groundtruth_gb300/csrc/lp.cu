@@ -104,6 +104,152 @@ __global__ void __launch_bounds__(1024) lp_pass_b(int S, int n0, int P0, int P1,
         for (int p = t; p < n0; p += team) Trow[p] = buf[row * stride + spad(p)];
 }
 
+// Pass B for P a power of 8 (all stages radix 8) with the spectrum multiply fused in registers.  A team of
+// P / 8 threads takes one column b and all S sheets of it; thread t owns butterfly t of every stage.  The
+// forward transform's last stage leaves thread t holding the pixels t + r P/8 (r < 8), exactly the inputs of
+// the inverse transform's first stage, so the S x S multiply-add runs on registers between the two.  The
+// first forward stage reads the (half-empty) column straight from T, the last inverse stage writes its lower
+// half straight back; the stages between alternate two shared buffers (one barrier per stage).
+__host__ __device__ constexpr int lp_srow(int P) { return P + (P >> 5) + 1; }
+
+template <typename R, bool INV, int P, int NS, int S>
+__device__ __forceinline__ void b8_stage(const cx<R>* src, cx<R>* dst, int t, const cx<R>* __restrict__ tw) {
+    constexpr int NBF = P / 8, STRIDE = P / (NS * 8), ST = lp_srow(P);
+    const int k = t % NS;
+    const int base = (t / NS) * NS * 8 + k;
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        cx<R> v[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[r] = src[s * ST + spad(t + r * NBF)];
+        if (k) {
+#pragma unroll
+            for (int r = 1; r < 8; ++r) {
+                cx<R> w = tw[k * r * STRIDE];
+                if (INV) w.im = -w.im;
+                v[r] = v[r] * w;
+            }
+        }
+        dft8<R, INV>(v);
+#pragma unroll
+        for (int r = 0; r < 8; ++r) dst[s * ST + spad(base + r * NS)] = v[r];
+    }
+}
+
+// the stages with NS0 <= NS < NSEND, from buffer `cur` on; returns the buffer holding the result
+template <typename R, bool INV, int P, int NS, int NSEND, int S>
+__device__ __forceinline__ int b8_stages(cx<R>* b0, cx<R>* b1, int cur, int t, const cx<R>* __restrict__ tw) {
+    if constexpr (NS < NSEND) {
+        b8_stage<R, INV, P, NS, S>(cur ? b1 : b0, cur ? b0 : b1, t, tw);
+        __syncthreads();
+        return b8_stages<R, INV, P, NS * 8, NSEND, S>(b0, b1, 1 - cur, t, tw);
+    } else {
+        return cur;
+    }
+}
+
+template <typename R, int P, int S>
+__global__ void __launch_bounds__(512) lp_pass_b8(int n0, int P1, int ncol, int bt, const R* __restrict__ spec,
+                                                  const cx<R>* __restrict__ tw, cx<R>* __restrict__ T) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int TEAM = P / 8, NBF = P / 8, ST = lp_srow(P), Q0 = P / 2 + 1;
+    const int c = blockIdx.x;
+    const int tb = threadIdx.x / TEAM, t = threadIdx.x % TEAM;
+    const int b = blockIdx.y * bt + tb;
+    const bool act = b < ncol;
+    cx<R>* b0 = reinterpret_cast<cx<R>*>(smem_raw) + tb * S * ST;
+    cx<R>* b1 = reinterpret_cast<cx<R>*>(smem_raw) + (bt + tb) * S * ST;
+    cx<R>* Trow = T + ((int64_t)min(b, ncol - 1) * S * P1 + c) * n0;      // sheet s at + s * P1 * n0
+    cx<R> v[S][8];
+    // forward stage 1 (NS = 1) from T: inputs t + r P/8, the upper half zero
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int p = t + r * NBF;
+            v[s][r] = (act && p < n0) ? Trow[(int64_t)s * P1 * n0 + p] : zero<R>();
+        }
+        dft8_h<R, false>(v[s]);
+#pragma unroll
+        for (int r = 0; r < 8; ++r) b0[s * ST + spad(t * 8 + r)] = v[s][r];
+    }
+    __syncthreads();
+    int cur = b8_stages<R, false, P, 8, P / 8, S>(b0, b1, 0, t, tw);
+    // forward last stage (NS = P/8): pixels t + r P/8 stay in registers
+    {
+        const cx<R>* src = cur ? b1 : b0;
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+#pragma unroll
+            for (int r = 0; r < 8; ++r) v[s][r] = src[s * ST + spad(t + r * NBF)];
+            if (t) {
+#pragma unroll
+                for (int r = 1; r < 8; ++r) v[s][r] = v[s][r] * tw[t * r];
+            }
+            dft8<R, false>(v[s]);
+        }
+    }
+    // spectrum multiply-add over sheets at pixel (p, c), K(p, c) = Kq(min(p, P-p), min(c, P1-c))
+    {
+        const R* Kc = spec + (int64_t)min(c, P1 - c) * Q0 * S * S;
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const int p = t + r * NBF;
+            const R* K = Kc + (int64_t)min(p, P - p) * S * S;
+            cx<R> u[S];
+#pragma unroll
+            for (int s = 0; s < S; ++s) u[s] = v[s][r];
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+                cx<R> acc = zero<R>();
+#pragma unroll
+                for (int q = 0; q < S; ++q) {
+                    const R kk = __ldg(K + s * S + q);
+                    acc.re += kk * u[q].re;
+                    acc.im += kk * u[q].im;
+                }
+                v[s][r] = acc;
+            }
+        }
+    }
+    // inverse stage 1 (NS = 1) on the registers, into the buffer the last forward stage did not read
+    {
+        cx<R>* dst = cur ? b0 : b1;
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            dft8<R, true>(v[s]);
+#pragma unroll
+            for (int r = 0; r < 8; ++r) dst[s * ST + spad(t * 8 + r)] = v[s][r];
+        }
+    }
+    __syncthreads();
+    cur = b8_stages<R, true, P, 8, P / 8, S>(b0, b1, 1 - cur, t, tw);
+    // inverse last stage (NS = P/8): the lower half (r < 4) straight to T
+    {
+        const cx<R>* src = cur ? b1 : b0;
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            cx<R> w8[8];
+#pragma unroll
+            for (int r = 0; r < 8; ++r) w8[r] = src[s * ST + spad(t + r * NBF)];
+            if (t) {
+#pragma unroll
+                for (int r = 1; r < 8; ++r) {
+                    cx<R> w = tw[t * r];
+                    w.im = -w.im;
+                    w8[r] = w8[r] * w;
+                }
+            }
+            dft8<R, true>(w8);
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int p = t + r * NBF;
+                if (act && p < n0) Trow[(int64_t)s * P1 * n0 + p] = w8[r];
+            }
+        }
+    }
+}
+
 // mode 0: out = R_t x + j w L - (V[a] - V[b]); 1: out = rhs - (that); 2: out = L
 template <typename R, int PL>
 __global__ void __launch_bounds__(1024) lp_pass_c(const cx<R>* __restrict__ T, const cx<R>* __restrict__ x, const cx<R>* __restrict__ rhs,
@@ -158,6 +304,7 @@ __global__ void __launch_bounds__(1024) lp_pass_c(const cx<R>* __restrict__ T, c
 }
 
 // ------------------------------------------------------------------------------------------ launchers
+template <typename R> static bool b8_fits(const LpArgs<R>& a);
 template <typename R>
 static void set_smem(const void* fn, size_t bytes) {
     if (bytes > 48 * 1024) GT_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
@@ -170,7 +317,10 @@ void lp_shapes(const LpArgs<R>& a, int* rows_out, int* bt_out) {
     while (rows & (rows - 1)) rows &= rows - 1;     // the row passes index rows by shifts: a power of two
     while (rows > 1 && (rows * teamA > 1024 || (size_t)rows * srow(a.P1) * sizeof(cx<R>) > 160 * 1024)) rows /= 2;
     int bt = a.bt > 0 ? a.bt : 2;
-    while (bt > 1 && (bt * a.S * teamB > 1024 || (size_t)bt * a.S * srow(a.P0) * sizeof(cx<R>) > 160 * 1024)) bt /= 2;
+    const size_t nbuf = b8_fits(a) ? 2 : 1;       // the fused column pass double-buffers its rows
+    const int per_col = b8_fits(a) ? teamB : a.S * teamB;
+    while (bt > 1 && (bt * per_col > 512 * (b8_fits(a) ? 1 : 2) ||
+                      nbuf * bt * a.S * srow(a.P0) * sizeof(cx<R>) > 160 * 1024)) bt /= 2;
     *rows_out = rows;
     *bt_out = bt;
 }
@@ -188,8 +338,30 @@ static void launch_a(const LpArgs<R>& a, int rows, cudaStream_t st) {
     GT_LAUNCH_CHECK();
 }
 
+template <typename R, int P, int S>
+static void launch_b8(const LpArgs<R>& a, int bt, cudaStream_t st) {
+    const size_t sm = (size_t)2 * bt * S * lp_srow(P) * sizeof(cx<R>);
+    set_smem<R>((const void*)lp_pass_b8<R, P, S>, sm);
+    lp_pass_b8<R, P, S><<<dim3(a.P1, ceil_div(a.ncol, bt)), bt * (P / 8), sm, st>>>(a.n0, a.P1, a.ncol, bt, a.spec, a.tw0,
+                                                                                  a.T);
+    GT_LAUNCH_CHECK();
+}
+
+// the fused column pass applies for these lengths and sheet counts
+template <typename R> static bool b8_fits(const LpArgs<R>& a) { return (a.P0 == 64 || a.P0 == 512) && a.S >= 1 && a.S <= 4; }
+
 template <typename R, int PB>
 static void launch_b(const LpArgs<R>& a, int bt, cudaStream_t st) {
+    if constexpr (PB == 64 || PB == 512) {
+        if (b8_fits(a)) {
+            switch (a.S) {
+                case 1: launch_b8<R, PB, 1>(a, bt, st); return;
+                case 2: launch_b8<R, PB, 2>(a, bt, st); return;
+                case 3: launch_b8<R, PB, 3>(a, bt, st); return;
+                default: launch_b8<R, PB, 4>(a, bt, st); return;
+            }
+        }
+    }
     size_t smB = (size_t)bt * a.S * srow(a.P0) * sizeof(cx<R>);
     dim3 gB(a.P1, ceil_div(a.ncol, bt));
     set_smem<R>((const void*)lp_pass_b<R, PB>, smB);
