@@ -250,6 +250,143 @@ __global__ void __launch_bounds__(512) lp_pass_b8(int n0, int P1, int ncol, int 
     }
 }
 
+// Row passes for P a power of 8: the first stage of pass A reads the strip row straight from x, the last
+// stage of pass C feeds the epilogue from registers; stages alternate two shared buffers.
+template <typename R, int P>
+__global__ void __launch_bounds__(1024) lp_pass_a8(const cx<R>* __restrict__ x, int64_t ldx, int64_t off, int S, int n0,
+                                                   int n1, int rows, const cx<R>* __restrict__ tw, cx<R>* __restrict__ T,
+                                                   const int* __restrict__ col_list) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int TEAM = P / 8, NBF = P / 8, ST = lp_srow(P);
+    cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw);
+    const int i0 = blockIdx.x * rows;
+    const int s = blockIdx.y;
+    const int col = col_list ? col_list[blockIdx.z] : blockIdx.z;
+    const int tr = threadIdx.x / TEAM, t = threadIdx.x % TEAM;
+    const int i = i0 + tr;
+    cx<R>* b0 = buf + tr * ST;
+    cx<R>* b1 = buf + (rows + tr) * ST;
+    const cx<R>* xrow = x + (int64_t)col * ldx + off + ((int64_t)s * n0 + min(i, n0 - 1)) * n1;
+    {
+        cx<R> v[8];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int j = t + r * NBF;
+            v[r] = (i < n0 && j < n1) ? xrow[j] : zero<R>();
+        }
+        dft8_h<R, false>(v);
+#pragma unroll
+        for (int r = 0; r < 8; ++r) b0[spad(t * 8 + r)] = v[r];
+    }
+    __syncthreads();
+    const int cur = b8_stages<R, false, P, 8, P / 8, 1>(b0, b1, 0, t, tw);
+    // last stage: natural order into the other buffer, then the transposed store
+    {
+        const cx<R>* src = cur ? b1 : b0;
+        cx<R>* dst = cur ? b0 : b1;
+        cx<R> v[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[r] = src[spad(t + r * NBF)];
+        if (t) {
+#pragma unroll
+            for (int r = 1; r < 8; ++r) v[r] = v[r] * tw[t * r];
+        }
+        dft8<R, false>(v);
+#pragma unroll
+        for (int r = 0; r < 8; ++r) dst[spad(t + r * NBF)] = v[r];
+    }
+    __syncthreads();
+    const cx<R>* res = buf + (cur ? 0 : rows) * ST;
+    cx<R>* Ts = T + ((int64_t)blockIdx.z * S + s) * (int64_t)P * n0;
+    const int lr = __ffs(rows) - 1;
+    for (int idx = threadIdx.x; idx < rows * P; idx += blockDim.x) {
+        const int c = idx >> lr, rr = idx & (rows - 1);
+        if (i0 + rr < n0) Ts[(int64_t)c * n0 + i0 + rr] = res[rr * ST + spad(c)];
+    }
+}
+
+template <typename R, int P>
+__global__ void __launch_bounds__(1024) lp_pass_c8(const cx<R>* __restrict__ T, const cx<R>* __restrict__ x,
+                                                   const cx<R>* __restrict__ rhs, cx<R>* __restrict__ out, int64_t ld,
+                                                   int64_t off, int64_t off_v, int S, int n0, int n1, int nx, int ny,
+                                                   int di, int dj, int rows, const cx<R>* __restrict__ tw,
+                                                   const uint8_t* __restrict__ mask, const int* __restrict__ col_op,
+                                                   const double* __restrict__ omega, const c64* __restrict__ zs, int mode,
+                                                   const int* __restrict__ col_list) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int TEAM = P / 8, NBF = P / 8, ST = lp_srow(P);
+    cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw);
+    const int i0 = blockIdx.x * rows;
+    const int s = blockIdx.y;
+    const int col = col_list ? col_list[blockIdx.z] : blockIdx.z;
+    const cx<R>* Ts = T + ((int64_t)blockIdx.z * S + s) * (int64_t)P * n0;
+    const int lr = __ffs(rows) - 1;
+    for (int idx = threadIdx.x; idx < rows * P; idx += blockDim.x) {
+        const int c = idx >> lr, rr = idx & (rows - 1);
+        const int i = i0 + rr;
+        buf[rr * ST + spad(c)] = i < n0 ? Ts[(int64_t)c * n0 + i] : zero<R>();
+    }
+    __syncthreads();
+    const int tr = threadIdx.x / TEAM, t = threadIdx.x % TEAM;
+    cx<R>* b0 = buf + tr * ST;
+    cx<R>* b1 = buf + (rows + tr) * ST;
+    // first inverse stage (NS = 1) from the natural-order row into the second buffer
+    {
+        cx<R> v[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[r] = b0[spad(t + r * NBF)];
+        dft8<R, true>(v);
+#pragma unroll
+        for (int r = 0; r < 8; ++r) b1[spad(t * 8 + r)] = v[r];
+    }
+    __syncthreads();
+    const int cur = b8_stages<R, true, P, 8, P / 8, 1>(b0, b1, 1, t, tw);
+    cx<R> L[4];
+    {
+        const cx<R>* src = cur ? b1 : b0;
+        cx<R> v[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[r] = src[spad(t + r * NBF)];
+        if (t) {
+#pragma unroll
+            for (int r = 1; r < 8; ++r) {
+                cx<R> w = tw[t * r];
+                w.im = -w.im;
+                v[r] = v[r] * w;
+            }
+        }
+        dft8<R, true>(v);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) L[r] = v[r];
+    }
+    const int i = i0 + tr;
+    if (tr >= rows || i >= n0) return;
+    const int op = col_op ? col_op[col] : 0;
+    const R w = omega ? R(omega[op]) : R(0);
+    const cx<R> z = zs ? cvt<R>(zs[(int64_t)op * S + s]) : zero<R>();
+    const int64_t base = (int64_t)col * ld;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int j = t + r * NBF;
+        if (j >= n1) continue;
+        const int64_t pos = off + ((int64_t)s * n0 + i) * n1 + j;
+        cx<R> y;
+        if (mode == 2) {
+            y = mask[pos] ? L[r] : zero<R>();
+        } else if (!mask[pos]) {
+            y = zero<R>();
+        } else {
+            const cx<R> xv = x[base + pos];
+            const int64_t va = off_v + ((int64_t)s * nx + i) * ny + j;
+            const int64_t vb = va + (int64_t)di * ny + dj;
+            const cx<R> dv = x[base + va] - x[base + vb];
+            y = z * xv + w * jmul(L[r]) - dv;
+            if (mode == 1) y = rhs[base + pos] - y;
+        }
+        out[base + pos] = y;
+    }
+}
+
 // mode 0: out = R_t x + j w L - (V[a] - V[b]); 1: out = rhs - (that); 2: out = L
 template <typename R, int PL>
 __global__ void __launch_bounds__(1024) lp_pass_c(const cx<R>* __restrict__ T, const cx<R>* __restrict__ x, const cx<R>* __restrict__ rhs,
@@ -315,7 +452,8 @@ void lp_shapes(const LpArgs<R>& a, int* rows_out, int* bt_out) {
     const int teamA = a.P1 / 8, teamB = a.P0 / 8;
     int rows = a.rows > 0 ? a.rows : 4;
     while (rows & (rows - 1)) rows &= rows - 1;     // the row passes index rows by shifts: a power of two
-    while (rows > 1 && (rows * teamA > 1024 || (size_t)rows * srow(a.P1) * sizeof(cx<R>) > 160 * 1024)) rows /= 2;
+    const size_t nbufA = (a.P1 == 64 || a.P1 == 512) ? 2 : 1;   // the power-of-8 row passes double-buffer
+    while (rows > 1 && (rows * teamA > 1024 || nbufA * rows * srow(a.P1) * sizeof(cx<R>) > 160 * 1024)) rows /= 2;
     int bt = a.bt > 0 ? a.bt : 2;
     const size_t nbuf = b8_fits(a) ? 2 : 1;       // the fused column pass double-buffers its rows
     const int per_col = b8_fits(a) ? teamB : a.S * teamB;
@@ -330,6 +468,14 @@ void lp_shapes(const LpArgs<R>& a, int* rows_out, int* bt_out) {
 
 template <typename R, int PA>
 static void launch_a(const LpArgs<R>& a, int rows, cudaStream_t st) {
+    if constexpr (PA == 64 || PA == 512) {
+        const size_t sm = (size_t)2 * rows * lp_srow(PA) * sizeof(cx<R>);
+        set_smem<R>((const void*)lp_pass_a8<R, PA>, sm);
+        lp_pass_a8<R, PA><<<dim3(ceil_div(a.n0, rows), a.S, a.ncol), rows * (PA / 8), sm, st>>>(
+            a.x, a.ld, a.off, a.S, a.n0, a.n1, rows, a.tw1, a.T, a.col_list);
+        GT_LAUNCH_CHECK();
+        return;
+    }
     size_t smA = (size_t)rows * srow(a.P1) * sizeof(cx<R>);
     dim3 gA(ceil_div(a.n0, rows), a.S, a.ncol);
     set_smem<R>((const void*)lp_pass_a<R, PA>, smA);
@@ -371,6 +517,15 @@ static void launch_b(const LpArgs<R>& a, int bt, cudaStream_t st) {
 
 template <typename R, int PA>
 static void launch_c(const LpArgs<R>& a, int rows, cudaStream_t st) {
+    if constexpr (PA == 64 || PA == 512) {
+        const size_t sm = (size_t)2 * rows * lp_srow(PA) * sizeof(cx<R>);
+        set_smem<R>((const void*)lp_pass_c8<R, PA>, sm);
+        lp_pass_c8<R, PA><<<dim3(ceil_div(a.n0, rows), a.S, a.ncol), rows * (PA / 8), sm, st>>>(
+            a.T, a.x, a.rhs, a.out, a.ld, a.off, a.off_v, a.S, a.n0, a.n1, a.nx, a.ny, a.di, a.dj, rows, a.tw1, a.mask,
+            a.col_op, a.omega, a.zs, a.mode, a.col_list);
+        GT_LAUNCH_CHECK();
+        return;
+    }
     size_t smA = (size_t)rows * srow(a.P1) * sizeof(cx<R>);
     dim3 gA(ceil_div(a.n0, rows), a.S, a.ncol);
     set_smem<R>((const void*)lp_pass_c<R, PA>, smA);
