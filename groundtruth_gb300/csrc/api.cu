@@ -199,6 +199,26 @@ struct gt_geometry {
     std::unique_ptr<Workspace> ws;
     Profiler prof;
     std::mutex lock;
+    // the triangular sweeps of independent column groups run on these streams side by side, so that one
+    // group's elimination level overlaps another's
+    static constexpr int NSUB = 4;
+    cudaStream_t sub[NSUB]{};
+    cudaEvent_t fork{}, join[NSUB]{};
+    void make_streams() {
+        if (fork) return;
+        GT_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+        for (int k = 0; k < NSUB; ++k) {
+            GT_CUDA(cudaStreamCreateWithFlags(&sub[k], cudaStreamNonBlocking));
+            GT_CUDA(cudaEventCreateWithFlags(&join[k], cudaEventDisableTiming));
+        }
+    }
+    ~gt_geometry() {
+        for (int k = 0; k < NSUB; ++k) {
+            if (sub[k]) cudaStreamDestroy(sub[k]);
+            if (join[k]) cudaEventDestroy(join[k]);
+        }
+        if (fork) cudaEventDestroy(fork);
+    }
 };
 
 struct gt_operators {
@@ -373,6 +393,32 @@ static void precond(gt_geometry* G, gt_operators* ops, const cx<R>* r, int64_t l
     }
     const cx<R>* pan = panel_of<R>(ops);
     const int nlev = (int)G->level_ptr.size() - 1;
+    const int nsub = P->levels ? 1 : std::min(gt_geometry::NSUB, grp.ngroup);
+    if (nsub > 1) {
+        // forward and backward sweeps per stream, each on a share of the column groups
+        Scope s(P, sizeof(R) == 4 ? "fwdbwd_f32" : "fwdbwd_f64", st,
+                2 * panel + nslot * es * (4 * nfac + 2.0 * G->F.vec_total));
+        G->make_streams();
+        GT_CUDA(cudaEventRecord(G->fork, st));
+        for (int k = 0; k < nsub; ++k) {
+            cudaStream_t sk = G->sub[k];
+            GT_CUDA(cudaStreamWaitEvent(sk, G->fork, 0));
+            const int g0 = (int)((int64_t)k * grp.ngroup / nsub), g1 = (int)((int64_t)(k + 1) * grp.ngroup / nsub);
+            const Groups gk{g1 - g0, grp.gptr + g0, grp.gslot, grp.op + g0};
+            for (int h = 0; h < nlev; ++h) {
+                const int nf = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);
+                launch_fwd_level<R>(G->F, G->d_order + G->level_ptr[h], nf, G->level_maxnf[h], G->level_maxnown[h],
+                                    pan, dinv_of<R>(ops), yfac, zfac, uvec, yfac, gk, gmax, sk);
+            }
+            for (int h = nlev - 1; h >= 0; --h) {
+                const int nf = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);
+                launch_bwd_level<R>(G->F, G->d_order + G->level_ptr[h], nf, G->level_maxnf[h], G->level_maxnown[h],
+                                    panel_rm_of<R>(ops), zfac, yfac, sd, gk, gmax, sk);
+            }
+            GT_CUDA(cudaEventRecord(G->join[k], sk));
+            GT_CUDA(cudaStreamWaitEvent(st, G->join[k], 0));
+        }
+    } else {
     {
         Scope s(P, sizeof(R) == 4 ? "fwd_f32" : "fwd_f64", st, panel + nslot * es * (2 * nfac + 2.0 * G->F.vec_total));
         for (int h = 0; h < nlev; ++h) {
@@ -392,6 +438,7 @@ static void precond(gt_geometry* G, gt_operators* ops, const cx<R>* r, int64_t l
             launch_bwd_level<R>(G->F, G->d_order + G->level_ptr[h], nf, G->level_maxnf[h], G->level_maxnown[h],
                                 panel_rm_of<R>(ops), zfac, yfac, sd, grp, gmax, st);
         }
+    }
     }
     {
         Scope s(P, "pc_strip", st, nslot * es * (2 * n + nfac));
