@@ -14,6 +14,10 @@
 
 namespace gt {
 
+// grid rows per block of the stencil kernels (fewer, fuller blocks)
+constexpr int RPB = 8;
+constexpr int RPB_NODE = 2;     // pc_node's threads carry more work per row
+
 namespace {
 
 __device__ __forceinline__ int seg_of(const Geo& g, int64_t pos, int64_t nX, int64_t nY) {
@@ -42,12 +46,12 @@ __global__ void __launch_bounds__(256) tail_kernel(Geo g, const cx<R>* __restric
     const cx<R>* V = xc + g.off_v;
     const cx<R>* bc = rhs ? rhs + (int64_t)col * ld : nullptr;
     cx<R>* oc = out + (int64_t)col * ld;
-    const int part = blockIdx.y, bx = blockIdx.x;
+    const int part = blockIdx.y;
     auto put = [&](int64_t pos, cx<R> y) { oc[pos] = mode == 1 ? bc[pos] - y : y; };
-    if (part == 0) {
+    if (part == 0) for (int bx = blockIdx.x * RPB; bx < blockIdx.x * RPB + RPB; ++bx) {
         // node (KCL) rows: I_x(k,i,j) - I_x(k,i-1,j) + I_y(k,i,j) - I_y(k,i,j-1) + caps + branches
         const int k = bx / nx, i = bx - k * nx;
-        if (k >= S) return;
+        if (k >= S) break;
         const cx<R>* X = xc + g.off_x + (int64_t)k * (nx - 1) * ny;
         const cx<R>* Y = xc + g.off_y + (int64_t)k * nx * (ny - 1);
         for (int j = threadIdx.x; j < ny; j += blockDim.x) {
@@ -74,10 +78,10 @@ __global__ void __launch_bounds__(256) tail_kernel(Geo g, const cx<R>* __restric
             }
             put(pos, s);
         }
-    } else if (part == 1) {
+    } else if (part == 1) for (int bx = blockIdx.x * RPB; bx < blockIdx.x * RPB + RPB; ++bx) {
         // capacitance rows: z_cap I_c - (V[upper] - V[lower])
         const int p = bx / nx, i = bx - p * nx;
-        if (p >= g.np) return;
+        if (p >= g.np) break;
         const int u = g.pair_layers[2 * p], l = g.pair_layers[2 * p + 1];
         const cx<R> zc = cvt<R>(zcap[(int64_t)op * g.np + p]);
         for (int j = threadIdx.x; j < ny; j += blockDim.x) {
@@ -95,7 +99,7 @@ __global__ void __launch_bounds__(256) tail_kernel(Geo g, const cx<R>* __restric
         const int64_t gap[5][2] = {{g.off_x + nX, g.off_y}, {g.off_y + nY, g.off_c},
                                    {g.off_c + (int64_t)g.np * nxy, g.off_b}, {g.off_b + g.nbr, g.off_v},
                                    {g.off_v + (int64_t)S * nxy, g.n}};
-        const int tid = bx * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+        const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
         for (int b = tid; b < g.nbr; b += nth) {
             const int64_t pos = g.off_b + b;
             if (!g.mask[pos]) {
@@ -112,7 +116,7 @@ __global__ void __launch_bounds__(256) tail_kernel(Geo g, const cx<R>* __restric
 template <typename R>
 void launch_tail(const Geo& g, const cx<R>* x, const cx<R>* rhs, cx<R>* out, int64_t ld, int ncol, const int* col_op,
                  const c64* zcap, const c64* zbr, int mode, const int* col_list, cudaStream_t st) {
-    const dim3 grid(std::max(g.nx * std::max(g.np, g.S), 1), 3, ncol);
+    const dim3 grid(std::max(ceil_div((int64_t)g.nx * std::max(g.np, g.S), RPB), 1), 3, ncol);
     tail_kernel<R><<<grid, 256, 0, st>>>(g, x, rhs, out, ld, col_op, zcap, zbr, mode, col_list);
     GT_LAUNCH_CHECK();
 }
@@ -148,7 +152,7 @@ __global__ void __launch_bounds__(256) pc_node_kernel(Geo g, const cx<R>* __rest
     const cx<R>* X = rc + g.off_x;
     const cx<R>* Y = rc + g.off_y;
     cx<R>* sc = sd + (int64_t)col * g.nfac;
-    const int i = blockIdx.x;
+    for (int i = blockIdx.x * RPB_NODE; i < min(nx, blockIdx.x * RPB_NODE + RPB_NODE); ++i)
     for (int j = threadIdx.x; j < ny; j += blockDim.x) {
         const int ij = i * ny + j;
         cx<R> kcl[MAXS], u[4][MAXS], t[MAXS];
@@ -215,7 +219,7 @@ template <typename R>
 void launch_pc_node(const Geo& g, const cx<R>* r, int64_t ld, cx<R>* sd, int ncol, const int* col_op, const cx<R>* tab,
                     const int* col_list, cudaStream_t st) {
     if (g.S > SHEETS_MAX) throw CudaError{cudaErrorInvalidValue, "more sheets than the stencil kernels take"};
-    const dim3 grid(g.nx, ncol);
+    const dim3 grid(ceil_div(g.nx, RPB_NODE), ncol);
     if (g.S <= 2) pc_node_kernel<R, 2><<<grid, 256, 0, st>>>(g, r, ld, sd, col_op, tab, col_list);
     else if (g.S <= 4) pc_node_kernel<R, 4><<<grid, 256, 0, st>>>(g, r, ld, sd, col_op, tab, col_list);
     else pc_node_kernel<R, 8><<<grid, 256, 0, st>>>(g, r, ld, sd, col_op, tab, col_list);
@@ -237,11 +241,11 @@ __global__ void __launch_bounds__(256) pc_strip_kernel(Geo g, const cx<R>* __res
     const cx<R>* rc = r + (int64_t)col * ldr;
     const cx<R>* yc = sd + (int64_t)col * S * nxy;       // zero at nodes that are not kept
     cx<R>* oc = out + (int64_t)col * ldo;
-    const int part = blockIdx.y, bx = blockIdx.x;
-    if (part <= 1) {
+    const int part = blockIdx.y;
+    if (part <= 1) for (int bx = blockIdx.x * RPB; bx < blockIdx.x * RPB + RPB; ++bx) {
         const bool xo = part == 0;
         const int i = bx;
-        if (i >= (xo ? nx - 1 : nx)) return;
+        if (i >= (xo ? nx - 1 : nx)) break;
         const int n1 = xo ? ny : ny - 1, lstride = (xo ? nx - 1 : nx) * n1;
         const int64_t seg = xo ? g.off_x : g.off_y;
         const uint8_t* codes = xo ? g.code_x : g.code_y;
@@ -260,9 +264,9 @@ __global__ void __launch_bounds__(256) pc_strip_kernel(Geo g, const cx<R>* __res
             for (int k = 0; k < MAXS; ++k)
                 if (k < S) oc[seg + (int64_t)k * lstride + pq] = t[k];      // zero where the strip is absent
         }
-    } else if (part == 2) {
+    } else if (part == 2) for (int bx = blockIdx.x * RPB; bx < blockIdx.x * RPB + RPB; ++bx) {
         const int p = bx / nx, i = bx - p * nx;
-        if (p >= g.np) return;
+        if (p >= g.np) break;
         const int up = g.pair_layers[2 * p], lo = g.pair_layers[2 * p + 1];
         const cx<R> zc = T[g.tab_cap0 + p];
         for (int j = threadIdx.x; j < ny; j += blockDim.x) {
@@ -270,9 +274,9 @@ __global__ void __launch_bounds__(256) pc_strip_kernel(Geo g, const cx<R>* __res
             const int64_t pos = g.off_c + (int64_t)p * nxy + ij;
             oc[pos] = g.mask[pos] ? zc * (rc[pos] + (yc[up * nxy + ij] - yc[lo * nxy + ij])) : zero<R>();
         }
-    } else if (part == 3) {
+    } else if (part == 3) for (int bx = blockIdx.x * RPB; bx < blockIdx.x * RPB + RPB; ++bx) {
         const int k = bx / nx, i = bx - k * nx;
-        if (k >= S) return;
+        if (k >= S) break;
         for (int j = threadIdx.x; j < ny; j += blockDim.x) {
             const int node = k * nxy + i * ny + j;
             oc[g.off_v + node] = yc[node];
@@ -284,7 +288,7 @@ __global__ void __launch_bounds__(256) pc_strip_kernel(Geo g, const cx<R>* __res
         const int64_t gap[5][2] = {{g.off_x + nX, g.off_y}, {g.off_y + nY, g.off_c},
                                    {g.off_c + (int64_t)g.np * nxy, g.off_b}, {g.off_b + g.nbr, g.off_v},
                                    {g.off_v + (int64_t)S * nxy, g.n}};
-        const int tid = bx * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+        const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
         for (int b = tid; b < g.nbr; b += nth) {
             const int64_t pos = g.off_b + b;
             oc[pos] = g.mask[pos] ? T[g.tab_br0 + b] * (rc[pos] + (yc[g.branch_nodes[2 * b]] - yc[g.branch_nodes[2 * b + 1]]))
@@ -299,7 +303,7 @@ template <typename R>
 void launch_pc_strip(const Geo& g, const cx<R>* r, int64_t ldr, const cx<R>* sd, cx<R>* out, int64_t ldo, int ncol,
                      const int* col_op, const cx<R>* tab, const int* col_list, cudaStream_t st) {
     if (g.S > SHEETS_MAX) throw CudaError{cudaErrorInvalidValue, "more sheets than the stencil kernels take"};
-    const dim3 grid(std::max(g.nx * std::max(g.np, g.S), 1), 5, ncol);
+    const dim3 grid(std::max(ceil_div((int64_t)g.nx * std::max(g.np, g.S), RPB), 1), 5, ncol);
     if (g.S <= 2) pc_strip_kernel<R, 2><<<grid, 256, 0, st>>>(g, r, ldr, sd, out, ldo, col_op, tab, col_list);
     else if (g.S <= 4) pc_strip_kernel<R, 4><<<grid, 256, 0, st>>>(g, r, ldr, sd, out, ldo, col_op, tab, col_list);
     else pc_strip_kernel<R, 8><<<grid, 256, 0, st>>>(g, r, ldr, sd, out, ldo, col_op, tab, col_list);
