@@ -285,22 +285,26 @@ def run_gpu(args):
                   for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
 
     # e2e through the C ABI from host buffers: factorise all frequencies + solve + copy out, every step
-    e2e_t = []
+    e2e_t, e2e_parts = [], []
     for k in range(0 if args.no_e2e else max(1, min(args.steps, 2))):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         data = [st._freq_tables(f) for f in freqs]
+        t1 = time.perf_counter()
         ops2 = native.Operators(st.handle, freqs, data)
+        t2 = time.perf_counter()
         xh, its2, res2, ok2 = native.solve(st.handle, [(ops2, q) for (_, q) in cols], rhs_c, args.tol, restart=args.restart,
                                            inner_tol=args.inner_tol, max_its=args.max_its, reorth=args.reorth,
                                            outer_k=args.outer_k, precision=args.precision)
         e2e_t.append(time.perf_counter() - t0)
+        e2e_parts.append({"tables_s": round(t1 - t0, 3), "operators_s": round(t2 - t1, 3),
+                          "solve_s": round(e2e_t[-1] - t2 + t0, 3)})
         del ops2
     e2e = None
     if e2e_t:
         e2e = {"value": world * ncol / float(np.median(e2e_t)), "unit": "solves/s",
                "h2d_bytes_per_step": int(rhs_c.nbytes + sum(sum(np.asarray(a).nbytes for a in d) for d in data)),
-               "d2h_bytes_per_step": int(xh.nbytes)}
+               "d2h_bytes_per_step": int(xh.nbytes), "parts": e2e_parts[-1]}
 
     # plain all-FP64 GPU comparator: one column at a time, FP64 GMRES, same preconditioner
     plain = None

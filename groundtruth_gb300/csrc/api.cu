@@ -1047,19 +1047,35 @@ int gt_operators_create(gt_geometry* G, int32_t n_ops, const double* omega, cons
     O->panel64_rm = p.alloc<c64>((size_t)n_ops * F.panel_total);
     O->dinv64 = p.alloc<c64>((size_t)n_ops * F.nfac);
     O->dinv32 = p.alloc<c32>((size_t)n_ops * F.nfac);
-    launch_assemble_s(G->d_sterm_ptr, G->d_sterm_tab, G->d_sterm_coef, F.nsv, O->tab, g.ntab, svals, n_ops, st);
+    Profiler* P = &G->prof;
+    {
+        Scope sc(P, "factor_assemble", st);
+        launch_assemble_s(G->d_sterm_ptr, G->d_sterm_tab, G->d_sterm_coef, F.nsv, O->tab, g.ntab, svals, n_ops, st);
+    }
     const int nlev = (int)G->level_ptr.size() - 1;
     for (int h = 0; h < nlev; ++h) {
         int nfl = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);
+        Scope sc(P, P->levels ? ("factor.L" + std::to_string(h)).c_str() : "factor_levels", st);
         launch_factor_level(F, G->d_order + G->level_ptr[h], nfl, G->level_maxnf[h], svals, O->panel64, upd, n_ops, status, st);
     }
     int max_nown = 1;
     for (int h = 0; h < nlev; ++h) max_nown = std::max(max_nown, G->level_maxnown[h]);
-    launch_invert_own(F, O->panel64, max_nown, n_ops, st);
-    launch_bnd_inv(F, O->panel64, max_nown, n_ops, st);
-    launch_panel_convert(F, O->panel64, O->panel32, O->panel32_rm, O->panel64_rm, O->dinv64, O->dinv32, n_ops, st);
+    {
+        Scope sc(P, "factor_invert", st);
+        launch_invert_own(F, O->panel64, max_nown, n_ops, st);
+    }
+    {
+        Scope sc(P, "factor_bnd_inv", st);
+        launch_bnd_inv(F, O->panel64, G->max_nf, n_ops, st);
+    }
+    {
+        Scope sc(P, "factor_convert", st);
+        launch_panel_convert(F, O->panel64, O->panel32, O->panel32_rm, O->panel64_rm, O->dinv64, O->dinv32, n_ops, st);
+    }
     int h_status = 0;
     GT_CUDA(cudaMemcpy(&h_status, status, sizeof(int), cudaMemcpyDeviceToHost));
+    GT_CUDA(cudaStreamSynchronize(st));
+    P->flush();
     if (h_status) throw Invalid("the Schur complement has a zero or non-finite pivot (a piece of copper with no "
                                 "path to its reference node?)");
     *out = O.release();

@@ -103,68 +103,74 @@ void launch_factor_level(const Fronts& F, const int64_t* front_list, int nf_leve
     GT_LAUNCH_CHECK();
 }
 
-// Selective inversion: each front's own block (unit lower triangular, D on the diagonal kept as is) replaced
-// in place by its inverse, so that the solves need no sequential sweep through it.  Column k of the inverse,
-// from the last: X[i, k] = -L[i, k] - sum_{k < m < i} X[i, m] L[m, k] (i > k); the columns m > k are already
-// inverted and column k of L is saved in shared memory before it is overwritten.  FP64.
-__global__ void invert_own_kernel(Fronts F, c64* __restrict__ panel) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    c64* lk = reinterpret_cast<c64*>(smem_raw);
-    const int f = blockIdx.x;
-    const int op = blockIdx.y;
+// Selective inversion: the inverse X of each front's own block (unit lower triangular; D on the diagonal
+// kept as is), FP64.  Rows are independent: X[i, k] = -(L[i, k] + sum_{k < m < i} X[i, m] L[m, k]) for k
+// descending.  X[i, k] is written to the unused upper triangle, transposed (position (k, i)), so the factor's
+// lower triangle stays intact while other rows read it; panel_convert moves X into place.  One thread per
+// row, rows of large fronts over several blocks, no barriers.
+constexpr int INV_ROWS = 128;
+__global__ void __launch_bounds__(INV_ROWS) invert_own_kernel(Fronts F, c64* __restrict__ panel, int nchunk) {
+    const int f = blockIdx.x / nchunk, chunk = blockIdx.x - f * nchunk, op = blockIdx.y;
     const int nown = (int)F.nown[f], nf = nown + (int)F.nbnd[f];
+    if (chunk * INV_ROWS >= nown) return;
+    const int i = chunk * INV_ROWS + threadIdx.x;
     c64* L = panel + (int64_t)op * F.panel_total + F.panel_off[f];
-    for (int k = nown - 2; k >= 0; --k) {
-        for (int m = k + 1 + threadIdx.x; m < nown; m += blockDim.x) lk[m] = L[(int64_t)k * nf + m];
-        __syncthreads();
-        for (int i = k + 1 + threadIdx.x; i < nown; i += blockDim.x) {
-            c64 acc = mk<double>(-lk[i].re, -lk[i].im);
-            for (int m = k + 1; m < i; ++m) acc -= L[(int64_t)m * nf + i] * lk[m];
-            L[(int64_t)k * nf + i] = acc;
-        }
-        __syncthreads();
+    const int kmax = min(nown, chunk * INV_ROWS + INV_ROWS) - 2;   // the block's largest row - 1
+    c64* Xi = L + (int64_t)min(i, nown - 1) * nf;                   // X[i, m] at Xi[m], m < i
+    for (int k = kmax; k >= 0; --k) {
+        if (k >= i || i >= nown) continue;
+        c64 acc = L[(int64_t)k * nf + i];
+        const c64* Lk = L + (int64_t)k * nf;
+        for (int m = k + 1; m < i; ++m) acc += Xi[m] * Lk[m];
+        Xi[k] = mk<double>(-acc.re, -acc.im);
     }
 }
 
 void launch_invert_own(const Fronts& F, c64* panel, int max_nown, int nops, cudaStream_t st) {
-    const size_t sm = (size_t)std::max(max_nown, 1) * sizeof(c64);
-    if (sm > 48 * 1024) GT_CUDA(cudaFuncSetAttribute((const void*)invert_own_kernel,
-                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    invert_own_kernel<<<dim3(F.nfront, nops), 256, sm, st>>>(F, panel);
+    const int nchunk = std::max(1, ceil_div(max_nown, INV_ROWS));
+    invert_own_kernel<<<dim3(F.nfront * nchunk, nops), INV_ROWS, 0, st>>>(F, panel, nchunk);
     GT_LAUNCH_CHECK();
 }
 
-// Boundary rows of each front replaced by M = -L_bnd Linv_own (in place, FP64), column by column with k
-// ascending: column k of M needs the factor's boundary columns >= k, which are still unchanged.
-__global__ void bnd_inv_kernel(Fronts F, c64* __restrict__ panel) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    c64* lk = reinterpret_cast<c64*>(smem_raw);
-    const int f = blockIdx.x, op = blockIdx.y;
+// Boundary rows of each front replaced by M = -L_bnd Linv_own (in place, FP64; after invert_own_kernel,
+// Linv read from the upper triangle).  Every boundary row is independent: M[j, k] = -(L[j, k] + sum_{m > k} L[j, m] Linv[m, k]) for k ascending reads only entries
+// m > k of its own row, which are still the factor's.  One thread per row (rows of a warp consecutive, so
+// the row loads coalesce and the Linv loads broadcast); the rows of large fronts spread over many blocks.
+constexpr int BND_ROWS = 128;
+__global__ void __launch_bounds__(BND_ROWS) bnd_inv_kernel(Fronts F, c64* __restrict__ panel, int nchunk) {
+    const int f = blockIdx.x / nchunk, chunk = blockIdx.x - f * nchunk, op = blockIdx.y;
     const int nown = (int)F.nown[f], nbnd = (int)F.nbnd[f], nf = nown + nbnd;
-    if (nbnd == 0) return;
+    const int j = nown + chunk * BND_ROWS + threadIdx.x;
+    if (chunk * BND_ROWS >= nbnd) return;
     c64* L = panel + (int64_t)op * F.panel_total + F.panel_off[f];
+    const bool act = j < nf;
+    const int jr = act ? j : nf - 1;
     for (int k = 0; k < nown; ++k) {
-        for (int m = k + 1 + threadIdx.x; m < nown; m += blockDim.x) lk[m] = L[(int64_t)k * nf + m];
-        __syncthreads();
-        for (int j = nown + threadIdx.x; j < nf; j += blockDim.x) {
-            c64 acc = L[(int64_t)k * nf + j];
-            for (int m = k + 1; m < nown; ++m) acc += L[(int64_t)m * nf + j] * lk[m];
-            L[(int64_t)k * nf + j] = mk<double>(-acc.re, -acc.im);
+        c64 acc = L[(int64_t)k * nf + jr];
+        // Linv[m, k] (m > k) is held transposed at position (k, m): L[m * nf + k]
+        int m = k + 1;
+        for (; m + 4 <= nown; m += 4) {
+            const c64 a0 = L[(int64_t)m * nf + jr], a1 = L[(int64_t)(m + 1) * nf + jr];
+            const c64 a2 = L[(int64_t)(m + 2) * nf + jr], a3 = L[(int64_t)(m + 3) * nf + jr];
+            acc += a0 * L[(int64_t)m * nf + k];
+            acc += a1 * L[(int64_t)(m + 1) * nf + k];
+            acc += a2 * L[(int64_t)(m + 2) * nf + k];
+            acc += a3 * L[(int64_t)(m + 3) * nf + k];
         }
-        __syncthreads();
+        for (; m < nown; ++m) acc += L[(int64_t)m * nf + jr] * L[(int64_t)m * nf + k];
+        if (act) L[(int64_t)k * nf + j] = mk<double>(-acc.re, -acc.im);
     }
 }
 
-void launch_bnd_inv(const Fronts& F, c64* panel, int max_nown, int nops, cudaStream_t st) {
-    const size_t sm = (size_t)std::max(max_nown, 1) * sizeof(c64);
-    if (sm > 48 * 1024) GT_CUDA(cudaFuncSetAttribute((const void*)bnd_inv_kernel,
-                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    bnd_inv_kernel<<<dim3(F.nfront, nops), 256, sm, st>>>(F, panel);
+void launch_bnd_inv(const Fronts& F, c64* panel, int max_nbnd, int nops, cudaStream_t st) {
+    const int nchunk = std::max(1, ceil_div(max_nbnd, BND_ROWS));
+    bnd_inv_kernel<<<dim3(F.nfront * nchunk, nops), BND_ROWS, 0, st>>>(F, panel, nchunk);
     GT_LAUNCH_CHECK();
 }
 
-// Finish the solve panels: the own block gets an explicit unit diagonal and zeros above it (the pivots go
-// to dinv as 1/D), and the FP32 column-major, FP32 / FP64 row-major copies are written.
+// Finish the solve panels: the own block gets its inverse below an explicit unit diagonal (moved from the
+// upper triangle, which becomes zero; the pivots go to dinv as 1/D), and the FP32 column-major, FP32 / FP64
+// row-major copies are written.
 __global__ void panel_convert_kernel(Fronts F, c64* __restrict__ p64, c32* __restrict__ p32, c32* __restrict__ r32,
                                      c64* __restrict__ r64, c64* __restrict__ d64, c32* __restrict__ d32) {
     const int f = blockIdx.x;
@@ -174,17 +180,23 @@ __global__ void panel_convert_kernel(Fronts F, c64* __restrict__ p64, c32* __res
     const int64_t dbase = (int64_t)op * F.nfac + F.own_start[f];
     for (int64_t q = threadIdx.x; q < (int64_t)nf * nown; q += blockDim.x) {
         int k = int(q / nf), i = int(q - (int64_t)k * nf);      // column-major element (i, k)
+        if (i < k) continue;                                     // the upper triangle: with its partner below
         c64 v = p64[base + q];
-        if (i < nown && i <= k) {
-            if (i == k) {
-                const c64 dv = cdiv(mk<double>(1.0, 0.0), v);
-                d64[dbase + i] = dv;
-                d32[dbase + i] = cvt<float>(dv);
-                v = mk<double>(1.0, 0.0);
-            } else {
-                v = zero<double>();
-            }
+        if (i == k) {
+            const c64 dv = cdiv(mk<double>(1.0, 0.0), v);
+            d64[dbase + i] = dv;
+            d32[dbase + i] = cvt<float>(dv);
+            v = mk<double>(1.0, 0.0);
             p64[base + q] = v;
+        } else if (i < nown) {
+            // X[i, k] from its transposed position (k, i), which becomes zero
+            const int64_t qt = (int64_t)i * nf + k;
+            v = p64[base + qt];
+            p64[base + q] = v;
+            p64[base + qt] = zero<double>();
+            p32[base + qt] = zero<float>();
+            r32[base + (int64_t)k * nown + i] = zero<float>();
+            r64[base + (int64_t)k * nown + i] = zero<double>();
         }
         p32[base + q] = cvt<float>(v);
         r32[base + (int64_t)i * nown + k] = cvt<float>(v);
