@@ -571,16 +571,22 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
     const int nch = nchunks(n), nchu = update_chunks(n);
     Profiler* P = &G->prof;
     GT_CUDA(cudaMemcpyAsync(W.col_op, h_col_op, ncol * sizeof(int), cudaMemcpyHostToDevice, st));
-    GT_CUDA(cudaMemsetAsync(W.x64, 0, (size_t)ncol * n * sizeof(c64), st));
     GT_CUDA(cudaMemsetAsync(W.its_col, 0, ncol * sizeof(int), st));
-    GT_CUDA(cudaMemcpyAsync(W.r64, W.b64, (size_t)ncol * n * sizeof(c64), cudaMemcpyDeviceToDevice, st));
     norms64(G, W.b64, n, ncol, W.bnorm, st);
-    GT_CUDA(cudaMemcpyAsync(W.rho, W.bnorm, ncol * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    if (o.use_guess) {
+        // x holds the starting points: r = b - K x in FP64
+        matvec<double>(G, ops, W.x64, W.b64, W.r64, n, ncol, W.col_op, 1, W.T64, st);
+        norms64(G, W.r64, n, ncol, W.rho, st);
+    } else {
+        GT_CUDA(cudaMemsetAsync(W.x64, 0, (size_t)ncol * n * sizeof(c64), st));
+        GT_CUDA(cudaMemcpyAsync(W.r64, W.b64, (size_t)ncol * n * sizeof(c64), cudaMemcpyDeviceToDevice, st));
+        GT_CUDA(cudaMemcpyAsync(W.rho, W.bnorm, ncol * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    }
     std::vector<double> h_bnorm(ncol), h_rho(ncol);
     std::vector<int> h_its(ncol, 0);
     GT_CUDA(cudaMemcpyAsync(h_bnorm.data(), W.bnorm, ncol * sizeof(double), cudaMemcpyDeviceToHost, st));
+    GT_CUDA(cudaMemcpyAsync(h_rho.data(), W.rho, ncol * sizeof(double), cudaMemcpyDeviceToHost, st));
     GT_CUDA(cudaStreamSynchronize(st));
-    h_rho = h_bnorm;
     const int gmax = group_max(G, sizeof(cx<R>));
     B* V = static_cast<B*>(W.V);
     cx<R>* vcur = narrow ? static_cast<cx<R>*>(W.vcur) : nullptr;
@@ -1122,6 +1128,8 @@ int gt_solve_device(gt_geometry* G, gt_operators* ops, int32_t n_cols, const int
     ensure_ws(G, n_cols, opts->restart, opts->precision, std::max(1, opts->outer_k));
     Workspace& W = *G->ws;
     GT_CUDA(cudaMemcpyAsync(W.b64, rhs_device, (size_t)n_cols * G->geo.n * sizeof(c64), cudaMemcpyDeviceToDevice, st));
+    if (opts->use_guess)
+        GT_CUDA(cudaMemcpyAsync(W.x64, x_device, (size_t)n_cols * G->geo.n * sizeof(c64), cudaMemcpyDeviceToDevice, st));
     int rc = run_solve(G, ops, n_cols, col_op, opts, its_out, resid_out, st);
     GT_CUDA(cudaMemcpyAsync(x_device, W.x64, (size_t)n_cols * G->geo.n * sizeof(c64), cudaMemcpyDeviceToDevice, st));
     GT_CUDA(cudaStreamSynchronize(st));
@@ -1144,6 +1152,11 @@ int gt_solve(gt_geometry* G, gt_operators* ops, int32_t n_cols, const int32_t* c
     GT_CUDA(cudaMemcpyAsync(d_c, rhs, (size_t)n_cols * nc * sizeof(c64), cudaMemcpyHostToDevice, st));
     GT_CUDA(cudaMemsetAsync(W.b64, 0, (size_t)n_cols * G->geo.n * sizeof(c64), st));
     launch_scatter(G->d_c2d, nc, d_c, nc, W.b64, G->geo.n, n_cols, st);
+    if (opts->use_guess) {
+        GT_CUDA(cudaMemcpyAsync(d_c, x_out, (size_t)n_cols * nc * sizeof(c64), cudaMemcpyHostToDevice, st));
+        GT_CUDA(cudaMemsetAsync(W.x64, 0, (size_t)n_cols * G->geo.n * sizeof(c64), st));
+        launch_scatter(G->d_c2d, nc, d_c, nc, W.x64, G->geo.n, n_cols, st);
+    }
     int rc = run_solve(G, ops, n_cols, col_op, opts, its_out, resid_out, st);
     launch_gather(G->d_c2d, nc, W.x64, G->geo.n, d_c, nc, n_cols, st);
     GT_CUDA(cudaMemcpyAsync(x_out, d_c, (size_t)n_cols * nc * sizeof(c64), cudaMemcpyDeviceToHost, st));

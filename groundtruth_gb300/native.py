@@ -54,7 +54,8 @@ def _precision(name: str) -> int:
 
 class SolveOpts(C.Structure):
     _fields_ = [("tol", C.c_double), ("restart", C.c_int32), ("max_its", C.c_int32), ("inner_tol", C.c_double),
-                ("precision", C.c_int32), ("max_outer", C.c_int32), ("reorth", C.c_double), ("outer_k", C.c_int32)]
+                ("precision", C.c_int32), ("max_outer", C.c_int32), ("reorth", C.c_double), ("outer_k", C.c_int32),
+                ("use_guess", C.c_int32)]
 
 
 def load():
@@ -174,7 +175,7 @@ class Geometry:
         ncol = len(idx)
         its = np.zeros(ncol, np.int32)
         res = np.zeros(ncol)
-        o = SolveOpts(tol, restart, max_its, inner_tol, _precision(precision), max_outer, reorth, outer_k)
+        o = SolveOpts(tol, restart, max_its, inner_tol, _precision(precision), max_outer, reorth, outer_k, 0)
         rc = self.lib.gt_solve_device(self.h, obj.h, ncol, _ptr(idx, C.c_int32), P(rhs_ptr), C.byref(o), P(x_ptr),
                                       _ptr(its, C.c_int32), _ptr(res, C.c_double), P(stream))
         if rc not in (GT_OK, GT_NOT_CONVERGED):
@@ -244,16 +245,20 @@ def _ops_and_index(ops: list):
 
 def solve(geom: Geometry, ops: list, rhs: np.ndarray, tol: float, restart: int = 50, max_its: int = 2000,
           inner_tol: float = 1e-5, precision: str = "mixed", max_outer: int = 40, reorth: float = 0.7,
-          outer_k: int = 8):
-    """rhs: (ncol, n_compact) complex in the reference's order.  Returns (x, its, resid, converged)."""
+          outer_k: int = 8, x0: np.ndarray | None = None):
+    """rhs: (ncol, n_compact) complex in the reference's order; x0: optional starting points (same shape).
+    Returns (x, its, resid, converged)."""
     lib = geom.lib
     obj, idx = _ops_and_index(ops)
     rhs = np.ascontiguousarray(rhs, np.complex128)
     ncol = rhs.shape[0]
-    x = np.zeros_like(rhs)
+    x = np.zeros_like(rhs) if x0 is None else np.array(x0, np.complex128, order="C", copy=True)
+    if x.shape != rhs.shape:
+        raise ValueError("x0 must have the shape of rhs")
     its = np.zeros(ncol, np.int32)
     res = np.zeros(ncol)
-    o = SolveOpts(tol, restart, max_its, inner_tol, _precision(precision), max_outer, reorth, outer_k)
+    o = SolveOpts(tol, restart, max_its, inner_tol, _precision(precision), max_outer, reorth, outer_k,
+                  0 if x0 is None else 1)
     rc = lib.gt_solve(geom.h, obj.h, ncol, _ptr(idx, C.c_int32), _ptr(rhs.view(np.float64), C.c_double), C.byref(o),
                       _ptr(x.view(np.float64), C.c_double), _ptr(its, C.c_int32), _ptr(res, C.c_double), None)
     if rc not in (GT_OK, GT_NOT_CONVERGED):

@@ -345,5 +345,99 @@ def small_stack3(seed: int = 9) -> Board:
                  tol=1e-10, restart=50)
 
 
+def random_board(seed: int, side=(24, 48), n_layers=(2, 6), n_nets=(1, 2), n_freq: int = 2, slots: bool = False,
+                 cut_max: int = 8) -> Board:
+    """A seeded board drawn like the uneven-batch workload (sides, pitch, 2-6 plane layers with gaps
+    U[0.1, 1.5] mm, 0-8 polygon cut-outs of 3-8 vertices per layer, stitching vias at a Poisson density of
+    0-4 per cm2, random-walk nets, log-spaced frequencies in [1 MHz, 1 GHz]), with the raster sides drawn from
+    `side` (small enough for the FP64 oracle); `slots`: also one straight slot per layer (the largest
+    instance's layers).  The nets' return nodes are on the top plane and connected there."""
+    rng = np.random.default_rng(seed)
+    nx, ny = (int(rng.integers(side[0], side[1] + 1)) for _ in range(2))
+    d = float(rng.uniform(0.2, 0.5)) * 1e-3
+    t = 35e-6
+    nl = int(rng.integers(n_layers[0], n_layers[1] + 1))
+    zs = [0.0]
+    for _ in range(nl - 1):
+        zs.append(zs[-1] - (float(rng.uniform(0.1, 1.5)) * 1e-3 + t))
+    W, H = (nx - 1) * d, (ny - 1) * d
+    layers = []
+    for k, z in enumerate(zs):
+        cuts = []
+        for _ in range(int(rng.integers(0, cut_max + 1))):
+            c = np.array([rng.uniform(0.15, 0.85) * W, rng.uniform(0.15, 0.85) * H])
+            nv = int(rng.integers(3, 9))
+            ang = np.sort(rng.uniform(0, 2 * math.pi, nv))
+            rad = rng.uniform(0.03, 0.09, nv) * min(W, H)
+            cuts.append(c + np.stack([rad * np.cos(ang), rad * np.sin(ang)], 1))
+        if slots:
+            cuts.append(rect_polygon(rng.uniform(0.3, 0.7) * W, rng.uniform(0.3, 0.7) * H, 0.5 * min(W, H),
+                                     2.2 * d, rng.uniform(0, math.pi)))
+        layers.append(_full_layer(f"L{k}", z, t, nx, ny, d, cuts))
+    branches = []
+    lam = float(rng.uniform(0.0, 4.0)) * (W * H * 1e4)          # vias on the board (density per cm2)
+    for _ in range(int(rng.poisson(lam))):
+        i, j = int(rng.integers(1, nx - 1)), int(rng.integers(1, ny - 1))
+        k0, k1 = sorted(int(v) for v in rng.choice(nl, 2, replace=False))
+        if layers[k0].node[i, j] and layers[k1].node[i, j]:
+            length = abs(zs[k0] - zs[k1])
+            branches.append(BranchSpec((k0, i, j), (k1, i, j), length / (SIGMA_CU * math.pi * 2 * 1.5e-4 * 25e-6),
+                                       2e-10 * length / 1e-3, 0.0, "via", 1.5e-4))
+    z_face, z_sig = 0.5 * t, 0.15e-3 + t
+    top = layers[0].node
+    lab = _labels(top, layers[0].xb, layers[0].yb)
+    nets = []
+    for _ in range(int(rng.integers(n_nets[0], n_nets[1] + 1))):
+        for _try in range(200):
+            s = (int(rng.integers(2, nx - 2)), int(rng.integers(2, ny - 2)))
+            e = (int(rng.integers(2, nx - 2)), int(rng.integers(2, ny - 2)))
+            if top[s] and top[e] and lab[s] == lab[e] and abs(s[0] - e[0]) + abs(s[1] - e[1]) > min(nx, ny) // 3:
+                break
+        else:
+            raise RuntimeError("no connected pair of return nodes on the top plane")
+        mid = ((s[0] + e[0]) // 2, (s[1] + e[1]) // 2)
+        cells = _manhattan_walk(rng, s, mid, e, int(rng.integers(4, 12)), 2, nx - 3, ny - 3)
+        pts = [(c[0] * d, c[1] * d) for c in cells]
+        nets.append(Net(_segments(pts, z_sig, z_face, 0.15e-3), (0, *s), (0, *e)))
+    freqs = np.sort(np.exp(rng.uniform(math.log(1e6), math.log(1e9), n_freq)))
+    return Board(f"random_{seed}", d, nx, ny, layers, [], branches, nets, freqs, precond="diag", tol=1e-10,
+                 restart=50)
+
+
+def six_sheet(seed: int = 21) -> Board:
+    """The largest instance's shape at oracle size: six plane layers, cut-outs and a slot on every layer."""
+    return random_board(seed, side=(28, 40), n_layers=(6, 6), n_nets=(1, 2), slots=True, cut_max=3)
+
+
+def _labels(mask: np.ndarray, xb: np.ndarray, yb: np.ndarray) -> np.ndarray:
+    """Connected components of a layer's nodes joined by its x / y strips; -1 off copper."""
+    lab = -np.ones(mask.shape, np.int64)
+    nxx, nyy = mask.shape
+    cur = 0
+    for i0 in range(nxx):
+        for j0 in range(nyy):
+            if not mask[i0, j0] or lab[i0, j0] >= 0:
+                continue
+            stack = [(i0, j0)]
+            lab[i0, j0] = cur
+            while stack:
+                i, j = stack.pop()
+                nbrs = []
+                if i + 1 < nxx and xb[i, j]:
+                    nbrs.append((i + 1, j))
+                if i > 0 and xb[i - 1, j]:
+                    nbrs.append((i - 1, j))
+                if j + 1 < nyy and yb[i, j]:
+                    nbrs.append((i, j + 1))
+                if j > 0 and yb[i, j - 1]:
+                    nbrs.append((i, j - 1))
+                for a, b in nbrs:
+                    if mask[a, b] and lab[a, b] < 0:
+                        lab[a, b] = cur
+                        stack.append((a, b))
+            cur += 1
+    return lab
+
+
 WORKLOADS = {"plain_plane": plain_plane, "slotted_pair": slotted_pair, "small_pair": small_pair,
-             "small_stack3": small_stack3}
+             "small_stack3": small_stack3, "six_sheet": six_sheet}

@@ -88,6 +88,8 @@ typedef struct gt_solve_opts {
                                Gram-Schmidt pass (0.7: the reference's rule, peec.py:3156; 0: never) */
     int32_t outer_k;        /* FP64 outer GCR directions kept (each cycle's correction orthogonalised against
                                the previous ones; 1: a plain refinement step with the optimal step length) */
+    int32_t use_guess;      /* nonzero: x holds each column's starting point on entry (the warm start x0 of
+                               peec.py:2570-2578); the solve starts from r = b - K x0 in FP64 */
 } gt_solve_opts;
 
 /* Library version (major*10000 + minor*100 + patch). */

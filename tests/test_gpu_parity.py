@@ -80,3 +80,20 @@ def test_solves_match_reference(case, precision):
             assert abs(sol.Z_loop - Zr) <= 1e-8 * abs(Zr), (k, q, sol.Z_loop, Zr)
             assert rel(sol.m, z[f"m{k}_{q}"]) < 1e-7
             assert sol.residual <= board.tol
+
+
+def test_warm_start_guess(case):
+    """peec.py:2570-2578: a guess spanning the solution starts the solve there; a poor one is ignored."""
+    name, z, board, st, routes = case
+    f = float(board.freqs[0])
+    r = routes[0]
+    Ib, V, its, x = st.solve(f, r.rhs_top(f), r.J(), tol=board.tol)[:4]
+    Ib2, V2, its2, x2 = st.solve(f, r.rhs_top(f), r.J(), tol=board.tol, guess=[x])[:4]
+    assert its2 == 0 and rel(x2, x) < 1e-9
+    rng = np.random.default_rng(3)
+    noisy = x * (1 + 1e-3 * rng.standard_normal(len(x)))
+    Ib3, V3, its3, x3 = st.solve(f, r.rhs_top(f), r.J(), tol=board.tol, guess=[noisy])[:4]
+    assert its3 < its and rel(x3, x) < 1e-7
+    junk = rng.standard_normal(len(x)) * np.linalg.norm(x)
+    Ib4, V4, its4, x4 = st.solve(f, r.rhs_top(f), r.J(), tol=board.tol, guess=[junk])[:4]
+    assert rel(x4, x) < 1e-7

@@ -1,0 +1,38 @@
+"""Parity of the CUDA path with the FP64 oracle on seeded boards drawn like the uneven-batch workload (2-6
+plane layers, polygon cut-outs, stitching vias, non-square rasters) and on a six-layer stack with a slot on
+every layer (the largest instance's shape), at sizes the oracle solves in seconds.  Needs a GPU."""
+import numpy as np
+import pytest
+
+from groundtruth_gb300 import stack as gs, synth
+from test_oracle_golden import oracle_routes, oracle_stack
+
+pytestmark = pytest.mark.gpu
+BOARDS = [("random", 31), ("random", 32), ("random", 33), ("random", 34), ("six_sheet", 21)]
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.fixture(scope="module", params=BOARDS, ids=[f"{k}{s}" for k, s in BOARDS])
+def case(request):
+    kind, seed = request.param
+    board = synth.six_sheet(seed) if kind == "six_sheet" else synth.random_board(seed)
+    ost = oracle_stack(board)
+    oroutes = oracle_routes(ost, board)
+    st, routes = gs.from_board(board)
+    return board, ost, oroutes, st, routes
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_solves_match_oracle(case, precision):
+    board, ost, oroutes, st, routes = case
+    sols = gs.solve_many(routes, list(board.freqs), tol=board.tol, precision=precision)
+    for k, per in enumerate(sols):
+        for q, sol in enumerate(per):
+            ref = oroutes[k].solve(float(board.freqs[q]), tol=board.tol)
+            Ib = ref["x"][: ost.nb]
+            assert rel(np.concatenate([sol.I_x[tuple(st.xa.T)], sol.I_y[tuple(st.ya.T)]]), Ib[: ost.ns]) < 1e-7
+            assert abs(sol.Z_loop - ref["Z_loop"]) <= 1e-8 * abs(ref["Z_loop"]), (k, q, sol.Z_loop, ref["Z_loop"])
+            assert sol.residual <= board.tol
