@@ -184,14 +184,25 @@ def run_gpu(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    from groundtruth_gb300 import native, stack as gs, synth
+    from groundtruth_gb300 import greens, native, stack as gs, synth
 
     board = synth.slotted_pair()
     if args.nets:
         board.nets = board.nets[: args.nets]
     if args.freqs:
         board.freqs = board.freqs[:: args.freqs]
+    t_setup = time.perf_counter()
     st, routes = gs.from_board(board)
+    t_setup = time.perf_counter() - t_setup
+    # psi of every strip per net on the device (the right-hand sides' setup), beside the host restatement
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for net in board.nets:
+        st.handle.strip_coupling(st.zs, st.ts, st.d, net.segments, st.ns)
+    psi_dev = (time.perf_counter() - t0) / len(board.nets)
+    t0 = time.perf_counter()
+    greens.strip_coupling(board.nets[0].segments, [st.xa, st.ya], st.d, st.zs, st.ts)
+    psi_host = time.perf_counter() - t0
     lib = st.handle.lib
     freqs = list(board.freqs)
     cols = [(k, q) for k in range(len(routes)) for q in range(len(freqs))]
@@ -338,6 +349,8 @@ def run_gpu(args):
                 "roofline": {"bound": "hbm", "kernel": top, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                              "frac": round(ach / peak, 4), "peak_kind": peak_kind, "traffic": traffic,
                              "algorithmic_bytes_per_launch": round(per_launch)},
+                "setup": {"stack_and_routes_s": round(t_setup, 3), "psi_device_ms_per_net": round(psi_dev * 1e3, 2),
+                          "psi_host_ms_per_net": round(psi_host * 1e3, 1)},
                 "kernel_families": per_family,
                 **({"solve_levels": levels} if levels else {}),
                 "e2e": e2e, "gpu_launches": launches // max(args.steps, 1) * args.steps,

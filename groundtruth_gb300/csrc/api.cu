@@ -190,7 +190,7 @@ struct gt_geometry {
     std::vector<double> level_panel;   // panel entries (sum of nf x nown) of each level
     int max_nf = 0;
     int64_t* d_order = nullptr;
-    int64_t n_compact = 0;
+    int64_t n_compact = 0, n_strips = 0;
     int64_t* d_c2d = nullptr;
     int64_t* d_sterm_ptr = nullptr;
     int* d_sterm_tab = nullptr;
@@ -921,6 +921,9 @@ int gt_geometry_create(const gt_geometry_desc* d, gt_geometry** out) {
     if (g.tab_br0 + d->n_branches != d->n_table) throw Invalid("admittance table length mismatch");
     G->n_compact = d->n_compact;
     G->d_c2d = p.upload(d->compact_to_dense, d->n_compact);
+    // the strips lead the compact order (x strips, y strips)
+    G->n_strips = 0;
+    while (G->n_strips < d->n_compact && d->compact_to_dense[G->n_strips] < d->off_c) ++G->n_strips;
     // FFT orientations
     const double* specs[2] = {d->spectrum_x, d->spectrum_y};
     for (int k = 0; k < 2; ++k) {
@@ -1237,6 +1240,28 @@ int gt_apply(gt_geometry* G, gt_operators* ops, int32_t kind, int32_t precision,
     launch_gather(G->d_c2d, nc, yout, n, d_c, nc, n_cols, st);
     GT_CUDA(cudaMemcpyAsync(y, d_c, (size_t)n_cols * nc * sizeof(c64), cudaMemcpyDeviceToHost, st));
     GT_CUDA(cudaStreamSynchronize(st));
+    return GT_OK;
+    GT_GUARD_END
+}
+
+int gt_strip_coupling(gt_geometry* G, const double* sheet_z, const double* sheet_t, double pitch, int32_t n_seg,
+                      const double* segments, double* psi, int64_t* n_strips) {
+    GT_GUARD_BEGIN
+    if (!G || !sheet_z || !sheet_t || !psi || n_seg < 0 || (n_seg > 0 && !segments) || !(pitch > 0))
+        throw Invalid("bad arguments");
+    std::lock_guard<std::mutex> lk(G->lock);
+    const int64_t ns = G->n_strips;
+    if (n_strips) *n_strips = ns;
+    Pool tmp;
+    const int S = G->geo.S;
+    double* dz = tmp.upload(sheet_z, S);
+    double* dt = tmp.upload(sheet_t, S);
+    double* dseg = n_seg ? tmp.upload(segments, (size_t)n_seg * 8) : nullptr;
+    double* dpsi = tmp.alloc<double>(std::max<int64_t>(ns, 1));
+    cudaStream_t st = 0;
+    if (n_seg == 0) GT_CUDA(cudaMemsetAsync(dpsi, 0, std::max<int64_t>(ns, 1) * sizeof(double), st));
+    else launch_strip_coupling(G->geo, G->d_c2d, ns, dz, dt, pitch, dseg, n_seg, dpsi, st);
+    GT_CUDA(cudaMemcpy(psi, dpsi, ns * sizeof(double), cudaMemcpyDeviceToHost));
     return GT_OK;
     GT_GUARD_END
 }

@@ -61,6 +61,10 @@ template <typename R>
 void launch_pc_strip(const Geo& g, const cx<R>* r, int64_t ldr, const cx<R>* sd, cx<R>* out, int64_t ldo, int ncol,
                      const int* col_op, const cx<R>* tab, const int* col_list, cudaStream_t st);
 
+// psi of the first ns compact entries (the strips): segments [nseg][8] (a, b, width, current), device FP64
+void launch_strip_coupling(const Geo& g, const int64_t* c2d, int64_t ns, const double* sheet_z, const double* sheet_t,
+                           double d, const double* segs, int nseg, double* psi, cudaStream_t st);
+
 // compact <-> dense
 void launch_scatter(const int64_t* c2d, int64_t ncomp, const c64* in, int64_t ldin, c64* out, int64_t ldout, int ncol,
                     cudaStream_t st);

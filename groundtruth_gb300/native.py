@@ -84,6 +84,7 @@ def load():
     lib.gt_to_compact.argtypes = [P, C.c_int32, P, DP, P]
     lib.gt_apply.argtypes = [P, P, C.c_int32, C.c_int32, C.c_int32, I32P, DP, DP, P]
     lib.gt_profile.argtypes = [P, C.c_char_p, C.c_int32, DP, DP, I32P, C.c_int32]
+    lib.gt_strip_coupling.argtypes = [P, DP, DP, C.c_double, C.c_int32, DP, DP, C.POINTER(C.c_int64)]
     lib.gt_lp_product_noalloc.argtypes = [P, C.c_int32, P, P, P]
     if lib.gt_device_count() < 1:
         raise RuntimeError("no CUDA device is visible: the groundtruth_gb300 solver runs on the GPU only")
@@ -192,6 +193,21 @@ class Geometry:
         check(self.lib, self.lib.gt_to_compact(self.h, ncol, P(dense_ptr), _ptr(out.view(np.float64), C.c_double),
                                                P(stream)), "gt_to_compact")
         return out
+
+    def strip_coupling(self, sheet_z: np.ndarray, sheet_t: np.ndarray, pitch: float, segments: np.ndarray,
+                       n_strips: int) -> np.ndarray:
+        """psi of every strip on the device (gt_strip_coupling); segments (n, 8) rows (a, b, width, current)."""
+        z = np.ascontiguousarray(sheet_z, np.float64)
+        t = np.ascontiguousarray(sheet_t, np.float64)
+        seg = np.ascontiguousarray(np.asarray(segments, np.float64).reshape(-1, 8))
+        psi = np.zeros(max(n_strips, 1))
+        ns = C.c_int64(0)
+        check(self.lib, self.lib.gt_strip_coupling(self.h, _ptr(z, C.c_double), _ptr(t, C.c_double), float(pitch),
+                                                   len(seg), _ptr(seg, C.c_double), _ptr(psi, C.c_double),
+                                                   C.byref(ns)), "gt_strip_coupling")
+        if ns.value != n_strips:
+            raise RuntimeError(f"strip count mismatch: device {ns.value}, host {n_strips}")
+        return psi[:n_strips]
 
     def profile(self, on: bool | None = None, levels: bool = False) -> dict:
         """Toggle (on=True/False: reset; levels: time each elimination level too) or read

@@ -402,6 +402,10 @@ class PlaneStack:
 
     # ------------------------------------------------------------------ coupling to a signal path
     def strip_coupling(self, segments: np.ndarray) -> np.ndarray:
+        """psi of every strip (peec.py:2615-2656): on the device for a device stack (gt_strip_coupling), the
+        host restatement otherwise."""
+        if self.handle is not None:
+            return self.handle.strip_coupling(self.zs, self.ts, self.d, segments, self.ns)
         px, py = greens.strip_coupling(segments, [self.xa, self.ya], self.d, self.zs, self.ts)
         return np.concatenate([px, py])
 

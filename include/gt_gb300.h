@@ -149,6 +149,14 @@ int gt_apply(gt_geometry* g, gt_operators* ops, int32_t kind, int32_t precision,
  * the reference: it is an addition of this library. */
 int gt_lp_product_noalloc(gt_geometry* g, int32_t n_cols, const void* x_device, void* y_device, void* stream);
 
+/* psi of every strip (the flux per ampere of a signal path along it; peec.py:2615-2656 with
+ * kernel.py:297-312), FP64 on the device, in the reference's strip order (x strips then y strips, the first
+ * n_strips entries of the compact order).  sheet_z / sheet_t: [n_sheets] each sheet's face z (m) and copper
+ * thickness (m); pitch in m; segments: [n_seg][8] rows (ax, ay, az, bx, by, bz, width, current) in host memory;
+ * psi: [n_strips] host output.  Returns n_strips in *n_strips. */
+int gt_strip_coupling(gt_geometry* g, const double* sheet_z, const double* sheet_t, double pitch, int32_t n_seg,
+                      const double* segments, double* psi, int64_t* n_strips);
+
 /* Per-kernel-family timing of the solves on this geometry, by CUDA events on the launch stream.
  * names == NULL and cap == -2: reset and switch timing on; cap == -3: the same, with each elimination level
  * of the triangular solves also timed as a family of its own ("fwd_f32.L<h>"); cap == -1: switch it off.

@@ -97,3 +97,16 @@ def test_warm_start_guess(case):
     junk = rng.standard_normal(len(x)) * np.linalg.norm(x)
     Ib4, V4, its4, x4 = st.solve(f, r.rhs_top(f), r.J(), tol=board.tol, guess=[junk])[:4]
     assert rel(x4, x) < 1e-7
+
+
+def test_strip_coupling_on_device(case):
+    """psi of every strip on the device against the reference's own (fixture) and the host restatement."""
+    name, z, board, st, routes = case
+    from groundtruth_gb300 import greens
+    for k, net in enumerate(board.nets):
+        dev = st.handle.strip_coupling(st.zs, st.ts, st.d, net.segments, st.ns)
+        px, py = greens.strip_coupling(net.segments, [st.xa, st.ya], st.d, st.zs, st.ts)
+        host = np.concatenate([px, py])
+        assert rel(dev, host) < 1e-12, k
+        if f"psi{k}" in z.files:
+            assert rel(dev, z[f"psi{k}"][: st.ns]) < 1e-12, k
