@@ -1266,6 +1266,35 @@ int gt_strip_coupling(gt_geometry* G, const double* sheet_z, const double* sheet
     GT_GUARD_END
 }
 
+int gt_node_field(gt_geometry* G, int32_t n_cols, const void* x_device, double pitch, void* kx_device,
+                  void* ky_device, void* stream) {
+    GT_GUARD_BEGIN
+    if (!G || n_cols < 1 || !x_device || !kx_device || !ky_device || !(pitch > 0)) throw Invalid("bad arguments");
+    std::lock_guard<std::mutex> lk(G->lock);
+    cudaStream_t st = (cudaStream_t)stream;
+    launch_node_field(G->geo, static_cast<const c64*>(x_device), G->geo.n, n_cols, pitch, static_cast<c64*>(kx_device),
+                      static_cast<c64*>(ky_device), st);
+    GT_CUDA(cudaStreamSynchronize(st));
+    return GT_OK;
+    GT_GUARD_END
+}
+
+int gt_moment(gt_geometry* G, int32_t n_cols, const void* x_device, const double* sheet_z, double pitch, double* m,
+              void* stream) {
+    GT_GUARD_BEGIN
+    if (!G || n_cols < 1 || !x_device || !sheet_z || !m || !(pitch > 0)) throw Invalid("bad arguments");
+    std::lock_guard<std::mutex> lk(G->lock);
+    cudaStream_t st = (cudaStream_t)stream;
+    Pool tmp;
+    double* dz = tmp.upload(sheet_z, G->geo.S);
+    c64* dm = tmp.alloc<c64>((size_t)n_cols * 3);
+    launch_moment(G->geo, static_cast<const c64*>(x_device), G->geo.n, n_cols, dz, pitch, dm, st);
+    GT_CUDA(cudaStreamSynchronize(st));
+    GT_CUDA(cudaMemcpy(m, dm, (size_t)n_cols * 3 * sizeof(c64), cudaMemcpyDeviceToHost));
+    return GT_OK;
+    GT_GUARD_END
+}
+
 int gt_profile(gt_geometry* G, char* names, int32_t names_cap, double* ms, double* bytes, int32_t* launches,
                int32_t cap) {
     if (!G) return 0;

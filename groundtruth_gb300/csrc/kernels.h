@@ -65,6 +65,11 @@ void launch_pc_strip(const Geo& g, const cx<R>* r, int64_t ldr, const cx<R>* sd,
 void launch_strip_coupling(const Geo& g, const int64_t* c2d, int64_t ns, const double* sheet_z, const double* sheet_t,
                            double d, const double* segs, int nseg, double* psi, cudaStream_t st);
 
+// post-solve outputs from dense FP64 solutions [col][ld]: node fields kx / ky [col][S][nx][ny]; moments [col][3]
+void launch_node_field(const Geo& g, const c64* x, int64_t ld, int ncol, double d, c64* kx, c64* ky, cudaStream_t st);
+void launch_moment(const Geo& g, const c64* x, int64_t ld, int ncol, const double* zs, double d, c64* m,
+                   cudaStream_t st);
+
 // compact <-> dense
 void launch_scatter(const int64_t* c2d, int64_t ncomp, const c64* in, int64_t ldin, c64* out, int64_t ldout, int ncol,
                     cudaStream_t st);

@@ -85,6 +85,8 @@ def load():
     lib.gt_apply.argtypes = [P, P, C.c_int32, C.c_int32, C.c_int32, I32P, DP, DP, P]
     lib.gt_profile.argtypes = [P, C.c_char_p, C.c_int32, DP, DP, I32P, C.c_int32]
     lib.gt_strip_coupling.argtypes = [P, DP, DP, C.c_double, C.c_int32, DP, DP, C.POINTER(C.c_int64)]
+    lib.gt_node_field.argtypes = [P, C.c_int32, P, C.c_double, P, P, P]
+    lib.gt_moment.argtypes = [P, C.c_int32, P, DP, C.c_double, DP, P]
     lib.gt_lp_product_noalloc.argtypes = [P, C.c_int32, P, P, P]
     if lib.gt_device_count() < 1:
         raise RuntimeError("no CUDA device is visible: the groundtruth_gb300 solver runs on the GPU only")
@@ -208,6 +210,19 @@ class Geometry:
         if ns.value != n_strips:
             raise RuntimeError(f"strip count mismatch: device {ns.value}, host {n_strips}")
         return psi[:n_strips]
+
+    def node_field(self, n_cols: int, x_ptr: int, pitch: float, kx_ptr: int, ky_ptr: int, stream: int = 0):
+        """gt_node_field on dense device solutions (pointers)."""
+        check(self.lib, self.lib.gt_node_field(self.h, n_cols, P(x_ptr), float(pitch), P(kx_ptr), P(ky_ptr),
+                                               P(stream)), "gt_node_field")
+
+    def moment(self, n_cols: int, x_ptr: int, sheet_z: np.ndarray, pitch: float, stream: int = 0) -> np.ndarray:
+        """gt_moment on dense device solutions: the plane's part of m per column, (n_cols, 3) complex."""
+        z = np.ascontiguousarray(sheet_z, np.float64)
+        m = np.zeros((n_cols, 3), np.complex128)
+        check(self.lib, self.lib.gt_moment(self.h, n_cols, P(x_ptr), _ptr(z, C.c_double), float(pitch),
+                                           _ptr(m.view(np.float64), C.c_double), P(stream)), "gt_moment")
+        return m
 
     def profile(self, on: bool | None = None, levels: bool = False) -> dict:
         """Toggle (on=True/False: reset; levels: time each elimination level too) or read

@@ -106,6 +106,32 @@ class Solution:
     def L_loop(self) -> float:
         return self.Z_loop.imag / (2 * math.pi * self.f)
 
+    def node_field(self, k: int, d_mm: float, copper: bool = False) -> tuple:
+        """Complex (Kx, Ky) at the nodes of layer k in A/m per A (peec.py:1151-1203): each node averages the
+        strips of each direction that touch it and carry current, per cell width.  copper=True needs the
+        narrow-strip widths of the exact-copper raster, which this build does not model."""
+        if copper:
+            raise NotImplementedError("per-copper-width fields need the exact-copper raster")
+        d = d_mm * 1e-3
+        Ix, Iy = self.I_x[k], self.I_y[k]
+        nx, ny = self.V.shape[1:]
+        kx, ky = np.zeros((nx, ny), complex), np.zeros((nx, ny), complex)
+        cx, cy = np.zeros((nx, ny)), np.zeros((nx, ny))
+        kx[:-1, :] += Ix
+        kx[1:, :] += Ix
+        cx[:-1, :] += Ix != 0
+        cx[1:, :] += Ix != 0
+        ky[:, :-1] += Iy
+        ky[:, 1:] += Iy
+        cy[:, :-1] += Iy != 0
+        cy[:, 1:] += Iy != 0
+        return kx / np.maximum(cx, 1) / d, ky / np.maximum(cy, 1) / d
+
+    def sheet_current(self, k: int, d_mm: float, copper: bool = False) -> np.ndarray:
+        """|K| at the nodes of layer k (peec.py:1205-1208)."""
+        kx, ky = self.node_field(k, d_mm, copper)
+        return np.sqrt(np.abs(kx) ** 2 + np.abs(ky) ** 2)
+
 
 def freq_key(f: float) -> float:
     """f to 12 significant digits (peec.py:2292-2296, 3264-3267)."""

@@ -157,6 +157,18 @@ int gt_lp_product_noalloc(gt_geometry* g, int32_t n_cols, const void* x_device, 
 int gt_strip_coupling(gt_geometry* g, const double* sheet_z, const double* sheet_t, double pitch, int32_t n_seg,
                       const double* segments, double* psi, int64_t* n_strips);
 
+/* Outputs of dense FP64 device solutions x [n_cols][n_dense] (as gt_solve_device writes them), on the device.
+ * gt_node_field: (Kx, Ky) at every node of every sheet in A/m per A (Solution.node_field, peec.py:1151-1203,
+ * copper=False): each node averages the strips of each direction that touch it and carry current, over the
+ * pitch; kx, ky: device [n_cols][n_sheets][nx][ny] complex128.
+ * gt_moment: the plane's part of the magnetic moment m = 1/2 sum r x I dl (strips, plane-pair capacitances,
+ * branches; PlaneStack.moment, peec.py:2668-2700) per column; the signal segments' own part is the caller's;
+ * sheet_z: [n_sheets] host; m: [n_cols][3] complex128 host. */
+int gt_node_field(gt_geometry* g, int32_t n_cols, const void* x_device, double pitch, void* kx_device,
+                  void* ky_device, void* stream);
+int gt_moment(gt_geometry* g, int32_t n_cols, const void* x_device, const double* sheet_z, double pitch, double* m,
+              void* stream);
+
 /* Per-kernel-family timing of the solves on this geometry, by CUDA events on the launch stream.
  * names == NULL and cap == -2: reset and switch timing on; cap == -3: the same, with each elimination level
  * of the triangular solves also timed as a family of its own ("fwd_f32.L<h>"); cap == -1: switch it off.

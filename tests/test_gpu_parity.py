@@ -110,3 +110,29 @@ def test_strip_coupling_on_device(case):
         assert rel(dev, host) < 1e-12, k
         if f"psi{k}" in z.files:
             assert rel(dev, z[f"psi{k}"][: st.ns]) < 1e-12, k
+
+
+def test_outputs_on_device(case):
+    """Node fields and the plane's moment from a dense device solution against the host formulas."""
+    import torch
+    name, z, board, st, routes = case
+    f = float(board.freqs[0])
+    r = routes[0]
+    Ib, V, its, x = st.solve(f, r.rhs_top(f), r.J(), tol=board.tol)[:4]
+    X = torch.zeros((1, st.handle.n_dense), dtype=torch.complex128, device="cuda")
+    st.handle.to_dense(x[None, :], X.data_ptr(), 0)
+    kx = torch.zeros((1, st.N, st.nx, st.ny), dtype=torch.complex128, device="cuda")
+    ky = torch.zeros_like(kx)
+    st.handle.node_field(1, X.data_ptr(), st.d, kx.data_ptr(), ky.data_ptr())
+    I_x = np.zeros((st.N, st.nx - 1, st.ny), complex)
+    I_y = np.zeros((st.N, st.nx, st.ny - 1), complex)
+    I_x[tuple(st.xa.T)] = Ib[: st.nxb]
+    I_y[tuple(st.ya.T)] = Ib[st.nxb: st.ns]
+    sol = gs.Solution(f, I_x, I_y, np.zeros((st.N, st.nx, st.ny), complex), Ib[st.ns + st.ncap:], 0j,
+                      np.zeros(3, complex), its)
+    for k in range(st.N):
+        hx, hy = sol.node_field(k, st.d * 1e3)
+        assert rel(kx[0, k].cpu().numpy(), hx) < 1e-13 and rel(ky[0, k].cpu().numpy(), hy) < 1e-13
+    m_dev = st.handle.moment(1, X.data_ptr(), st.zs, st.d)[0]
+    m_host = st.moment(np.zeros((0, 8)), Ib)
+    assert rel(m_dev, m_host) < 1e-12
