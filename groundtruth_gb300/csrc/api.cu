@@ -1295,6 +1295,18 @@ int gt_moment(gt_geometry* G, int32_t n_cols, const void* x_device, const double
     GT_GUARD_END
 }
 
+int gt_kernel_spectrum(int32_t n_axial, int32_t n_lateral, double d, double dz, int32_t P0, int32_t P1,
+                       const double* near, int32_t n_near, double* quad) {
+    GT_GUARD_BEGIN
+    if (n_axial < 1 || n_lateral < 1 || !(d > 0) || !(dz >= 0) || !near || n_near < 1 || !quad)
+        throw Invalid("bad arguments");
+    if (!good_fft_size(P0) || !good_fft_size(P1) || P0 < 2 * n_axial - 1 || P1 < 2 * n_lateral - 1)
+        throw Invalid("FFT sizes must be 2^a or 3*2^a (a >= 3) and cover 2n - 1");
+    kernel_spectrum(n_axial, n_lateral, d, dz, P0, P1, near, n_near, quad);
+    return GT_OK;
+    GT_GUARD_END
+}
+
 int gt_profile(gt_geometry* G, char* names, int32_t names_cap, double* ms, double* bytes, int32_t* launches,
                int32_t cap) {
     if (!G) return 0;

@@ -70,6 +70,10 @@ void launch_node_field(const Geo& g, const c64* x, int64_t ld, int ncol, double 
 void launch_moment(const Geo& g, const c64* x, int64_t ld, int ncol, const double* zs, double d, c64* m,
                    cudaStream_t st);
 
+// the real (P0/2+1) x (P1/2+1) spectrum quadrant of a strip kernel (host in / out, device work)
+void kernel_spectrum(int na, int nl, double d, double dz, int P0, int P1, const double* near_h, int nnear,
+                     double* quad_h);
+
 // compact <-> dense
 void launch_scatter(const int64_t* c2d, int64_t ncomp, const c64* in, int64_t ldin, c64* out, int64_t ldout, int ncol,
                     cudaStream_t st);

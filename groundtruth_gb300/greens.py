@@ -97,6 +97,16 @@ def strip_kernel(n_axial: int, n_lateral: int, d: float, dz: float) -> np.ndarra
     return K
 
 
+def near_values(n_axial: int, n_lateral: int, d: float, dz: float) -> np.ndarray:
+    """(NEAR+1, NEAR+1) tape-integrated mutual inductances at the nearest offsets (kernel.py:287-294); offsets
+    beyond the grid are zero."""
+    out = np.zeros((NEAR + 1, NEAR + 1))
+    for oa in range(min(NEAR, n_axial - 1) + 1):
+        for ol in range(min(NEAR, n_lateral - 1) + 1):
+            out[oa, ol] = tape_mutual(d, d, d, oa * d, ol * d, dz)
+    return out
+
+
 def spectrum_quadrant(K: np.ndarray, P0: int, P1: int) -> np.ndarray:
     """Real (P0//2+1, P1//2+1) quadrant of the DFT of the centred even kernel wrapped onto a P0 x P1 torus."""
     Z = np.zeros((P0, P1))

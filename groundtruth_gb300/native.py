@@ -86,6 +86,8 @@ def load():
     lib.gt_profile.argtypes = [P, C.c_char_p, C.c_int32, DP, DP, I32P, C.c_int32]
     lib.gt_strip_coupling.argtypes = [P, DP, DP, C.c_double, C.c_int32, DP, DP, C.POINTER(C.c_int64)]
     lib.gt_node_field.argtypes = [P, C.c_int32, P, C.c_double, P, P, P]
+    lib.gt_kernel_spectrum.argtypes = [C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_int32, C.c_int32, DP,
+                                       C.c_int32, DP]
     lib.gt_moment.argtypes = [P, C.c_int32, P, DP, C.c_double, DP, P]
     lib.gt_lp_product_noalloc.argtypes = [P, C.c_int32, P, P, P]
     if lib.gt_device_count() < 1:
@@ -295,6 +297,18 @@ def solve(geom: Geometry, ops: list, rhs: np.ndarray, tol: float, restart: int =
     if rc not in (GT_OK, GT_NOT_CONVERGED):
         check(lib, rc, "gt_solve")
     return x, its, res, res <= tol
+
+
+def kernel_spectrum(n_axial: int, n_lateral: int, d: float, dz: float, P0: int, P1: int,
+                    near: np.ndarray) -> np.ndarray:
+    """The strip kernel's real spectrum quadrant (P0/2+1, P1/2+1) computed on the device (gt_kernel_spectrum);
+    near: (n, n) tape-integrated values at the nearest offsets."""
+    lib = load()
+    nr = np.ascontiguousarray(near, np.float64)
+    out = np.zeros((P0 // 2 + 1, P1 // 2 + 1))
+    check(lib, lib.gt_kernel_spectrum(int(n_axial), int(n_lateral), float(d), float(dz), int(P0), int(P1),
+                                      _ptr(nr, C.c_double), nr.shape[0], _ptr(out, C.c_double)), "gt_kernel_spectrum")
+    return out
 
 
 def apply(geom: Geometry, obj: Operators, kind: str, x: np.ndarray, op_index, precision: str = "fp64") -> np.ndarray:

@@ -156,6 +156,7 @@ class PlaneStack:
             if l.grid.wx is not None or l.grid.wy is not None:
                 raise NotImplementedError("strips narrower than the pitch (Grid.wx/wy) are not modelled")
         self.lib = native.load() if _device else None
+        self._device = bool(_device)
         self.layers = list(layers)
         self.N = self.n_sheets = len(layers)
         self.nx, self.ny = g0.nx, g0.ny
@@ -218,7 +219,16 @@ class PlaneStack:
         for s in range(S):
             for t in range(s, S):
                 dz = greens.round12(self.face_gap(s, t))
-                if dz not in cache:
+                if dz not in cache and self._device:
+                    # on the device (gt_kernel_spectrum): the centre is the nearest tape value, the sums the
+                    # spectra's DC terms
+                    from . import native
+                    nxv, nyv = greens.near_values(nx - 1, ny, d, dz), greens.near_values(ny - 1, nx, d, dz)
+                    px, py = self.P["x"], self.P["y"]
+                    qxq = native.kernel_spectrum(nx - 1, ny, d, dz, px[0], px[1], nxv)
+                    qyq = native.kernel_spectrum(ny - 1, nx, d, dz, py[1], py[0], nyv).T
+                    cache[dz] = (qxq.T, qyq.T, float(nxv[0, 0]), float(qxq[0, 0]), float(qyq[0, 0]))
+                elif dz not in cache:
                     kx = greens.strip_kernel(nx - 1, ny, d, dz)
                     ky = greens.strip_kernel(ny - 1, nx, d, dz).T
                     cache[dz] = (greens.spectrum_quadrant(kx, *self.P["x"]).T, greens.spectrum_quadrant(ky, *self.P["y"]).T,

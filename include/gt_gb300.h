@@ -169,6 +169,14 @@ int gt_node_field(gt_geometry* g, int32_t n_cols, const void* x_device, double p
 int gt_moment(gt_geometry* g, int32_t n_cols, const void* x_device, const double* sheet_z, double pitch, double* m,
               void* stream);
 
+/* The real (P0/2+1) x (P1/2+1) quadrant of the spectrum of the partial-inductance kernel between square
+ * strips of pitch d (m) on sheets dz (m) apart, over (2 n_axial - 1) x (2 n_lateral - 1) grid offsets wrapped
+ * onto a P0 x P1 torus (peec.py:3276-3306, 3362-3371; kernel.py:170-176, 268-294), FP64 on the current
+ * device.  near: [n_near][n_near] the tape-integrated values at the nearest offsets |axial|, |lateral| < n_near
+ * (host); quad: host output, row-major [P0/2+1][P1/2+1].  P0, P1: 2^a or 3*2^a with a >= 3. */
+int gt_kernel_spectrum(int32_t n_axial, int32_t n_lateral, double d, double dz, int32_t P0, int32_t P1,
+                       const double* near, int32_t n_near, double* quad);
+
 /* Per-kernel-family timing of the solves on this geometry, by CUDA events on the launch stream.
  * names == NULL and cap == -2: reset and switch timing on; cap == -3: the same, with each elimination level
  * of the triangular solves also timed as a family of its own ("fwd_f32.L<h>"); cap == -1: switch it off.

@@ -136,3 +136,15 @@ def test_outputs_on_device(case):
     m_dev = st.handle.moment(1, X.data_ptr(), st.zs, st.d)[0]
     m_host = st.moment(np.zeros((0, 8)), Ib)
     assert rel(m_dev, m_host) < 1e-12
+
+
+@pytest.mark.parametrize("shape", [(39, 36, 0.5e-3, 0.0), (39, 36, 0.5e-3, 0.2e-3), (255, 256, 0.25e-3, 1.07e-3),
+                                   (29, 44, 0.4e-3, 0.335e-3)])
+def test_kernel_spectrum_on_device(shape):
+    """The strip kernel's spectrum quadrant on the device against the host FFT of the host kernel."""
+    from groundtruth_gb300 import greens
+    na, nl, d, dz = shape
+    P0, P1 = greens.fft_size(2 * na - 1), greens.fft_size(2 * nl - 1)
+    host = greens.spectrum_quadrant(greens.strip_kernel(na, nl, d, dz), P0, P1)
+    dev = native.kernel_spectrum(na, nl, d, dz, P0, P1, greens.near_values(na, nl, d, dz))
+    assert np.max(np.abs(dev - host)) <= 1e-12 * np.max(np.abs(host))
