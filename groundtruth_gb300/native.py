@@ -278,14 +278,21 @@ def _ops_and_index(ops: list):
 
 def solve(geom: Geometry, ops: list, rhs: np.ndarray, tol: float, restart: int = 50, max_its: int = 2000,
           inner_tol: float = 1e-5, precision: str = "mixed", max_outer: int = 40, reorth: float = 0.7,
-          outer_k: int = 8, x0: np.ndarray | None = None):
-    """rhs: (ncol, n_compact) complex in the reference's order; x0: optional starting points (same shape).
+          outer_k: int = 8, x0: np.ndarray | None = None, out: np.ndarray | None = None):
+    """rhs: (ncol, n_compact) complex in the reference's order; x0: optional starting points (same shape);
+    out: optional C-contiguous complex128 array of that shape to receive x (e.g. page-locked host memory).
     Returns (x, its, resid, converged)."""
     lib = geom.lib
     obj, idx = _ops_and_index(ops)
     rhs = np.ascontiguousarray(rhs, np.complex128)
     ncol = rhs.shape[0]
-    x = np.zeros_like(rhs) if x0 is None else np.array(x0, np.complex128, order="C", copy=True)
+    if out is not None:
+        if out.shape != rhs.shape or out.dtype != np.complex128 or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous complex128 array of the shape of rhs")
+        x = out
+        x[...] = 0 if x0 is None else x0
+    else:
+        x = np.zeros_like(rhs) if x0 is None else np.array(x0, np.complex128, order="C", copy=True)
     if x.shape != rhs.shape:
         raise ValueError("x0 must have the shape of rhs")
     its = np.zeros(ncol, np.int32)
