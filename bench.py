@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--freqs", type=int, default=0, help="use only every k-th frequency (0: all)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "mixed16"],
                     help="inner GMRES: FP32 with an FP32 (mixed) or FP16 (mixed16) Krylov basis")
+    ap.add_argument("--borrow", action="store_true",
+                    help="precondition every other frequency with its neighbour's factorisation (half the LDL^T)")
     ap.add_argument("--levels", action="store_true",
                     help="also time each elimination level of the triangular solves (key 'solve_levels')")
     return ap.parse_args()
@@ -215,7 +217,7 @@ def run_gpu(args):
     # operators (factorised Schur complements at every frequency), timed on their own
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    ops = st.factorise(freqs, together=True)
+    ops = st.factorise(freqs, together=True, borrow=args.borrow)
     torch.cuda.synchronize()
     factor_s = time.perf_counter() - t0
     obj = ops[0][0]
@@ -310,7 +312,7 @@ def run_gpu(args):
         t0 = time.perf_counter()
         data = [st._freq_tables(f) for f in freqs]
         t1 = time.perf_counter()
-        ops2 = native.Operators(st.handle, freqs, data)
+        ops2 = native.Operators(st.handle, freqs, data, gs.borrow_plan(freqs) if args.borrow else None)
         t2 = time.perf_counter()
         xh, its2, res2, ok2 = native.solve(st.handle, [(ops2, q) for (_, q) in cols], rhs_pin, args.tol,
                                            restart=args.restart, inner_tol=args.inner_tol, max_its=args.max_its,

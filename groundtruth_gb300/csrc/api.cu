@@ -161,6 +161,7 @@ struct Workspace {
     c64* partial = nullptr;
     GmresState st{};
     int *slot_col = nullptr, *slot_op = nullptr, *g_ptr = nullptr, *g_slot = nullptr, *g_op = nullptr, *col_op = nullptr;
+    int* slot_pc = nullptr;      // each slot's factorisation (the preconditioner's tables, panels and pivots)
     int* act = nullptr;
     int* act_host = nullptr;
     // outer GCR: directions P (corrections) and Q = K P, per column, k-major; step sizes; active columns
@@ -224,6 +225,10 @@ struct gt_geometry {
 struct gt_operators {
     gt_geometry* g = nullptr;
     int nops = 0;
+    // the factorisations: nfact of them; operator q is preconditioned by factorisation fslot[q] (its own, or
+    // one borrowed from another operator); the tables, panels and pivots below are per factorisation
+    int nfact = 0;
+    std::vector<int> fslot;
     Pool pool;
     double* omega = nullptr;
     c64 *zs = nullptr, *zcap = nullptr, *zbr = nullptr, *tab = nullptr;
@@ -532,6 +537,7 @@ static void ensure_ws(gt_geometry* G, int ncol, int m, int prec, int kmax) {
     s.resid_est = p.alloc<double>(ncol);
     W.slot_col = p.alloc<int>(ncol);
     W.slot_op = p.alloc<int>(ncol);
+    W.slot_pc = p.alloc<int>(ncol);
     W.g_ptr = p.alloc<int>(ncol + 1);
     W.g_slot = p.alloc<int>(ncol);
     W.g_op = p.alloc<int>(ncol);
@@ -600,9 +606,9 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
     cx<R>* uvec = static_cast<cx<R>*>(W.uvec);
     cx<R>* sd = static_cast<cx<R>*>(W.sd);
     const int64_t lds = (int64_t)(m + 1) * n;
-    std::vector<int> slot_col, slot_op, gptr, gslot, gop, act;
+    std::vector<int> slot_col, slot_op, slot_pc, gptr, gslot, gop, act;
     auto upload_groups = [&](const std::vector<int>& slots) {
-        make_groups(slots, slot_op, gmax, gptr, gslot, gop);
+        make_groups(slots, slot_pc, gmax, gptr, gslot, gop);
         GT_CUDA(cudaMemcpyAsync(W.act, slots.data(), slots.size() * sizeof(int), cudaMemcpyHostToDevice, st));
         GT_CUDA(cudaMemcpyAsync(W.g_ptr, gptr.data(), gptr.size() * sizeof(int), cudaMemcpyHostToDevice, st));
         GT_CUDA(cudaMemcpyAsync(W.g_slot, gslot.data(), gslot.size() * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -638,12 +644,21 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
             pick();
         }
         if (slot_col.empty()) break;
-        std::stable_sort(slot_col.begin(), slot_col.end(), [&](int a, int b) { return h_col_op[a] < h_col_op[b]; });
+        // slots sorted by factorisation, then operator: the columns sharing a factor read it together
+        std::stable_sort(slot_col.begin(), slot_col.end(), [&](int a, int b) {
+            const int fa = ops->fslot[h_col_op[a]], fb = ops->fslot[h_col_op[b]];
+            return fa != fb ? fa < fb : h_col_op[a] < h_col_op[b];
+        });
         const int ns = (int)slot_col.size();
         slot_op.resize(ns);
-        for (int s = 0; s < ns; ++s) slot_op[s] = h_col_op[slot_col[s]];
+        slot_pc.resize(ns);
+        for (int s = 0; s < ns; ++s) {
+            slot_op[s] = h_col_op[slot_col[s]];
+            slot_pc[s] = ops->fslot[slot_op[s]];
+        }
         GT_CUDA(cudaMemcpyAsync(W.slot_col, slot_col.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
         GT_CUDA(cudaMemcpyAsync(W.slot_op, slot_op.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
+        GT_CUDA(cudaMemcpyAsync(W.slot_pc, slot_pc.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
         act.resize(ns);
         for (int q = 0; q < ns; ++q) act[q] = q;
         std::vector<int> its_slot(ns);
@@ -675,7 +690,7 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
                 vin = V + (int64_t)j * n;
                 ldin = lds;
             }
-            precond<R>(G, ops, vin, ldin, z, n, na, W.slot_op, grp, gmax, zfac, yfac, uvec, sd, st, W.act);
+            precond<R>(G, ops, vin, ldin, z, n, na, W.slot_pc, grp, gmax, zfac, yfac, uvec, sd, st, W.act);
             matvec<R>(G, ops, z, nullptr, w, n, na, W.slot_op, 0, T, st, W.act);
             // classical Gram-Schmidt: the dot products read the j+1 basis vectors and w; the update reads
             // them again, reads w and writes it
@@ -729,7 +744,7 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
         act.resize(ns);
         for (int q = 0; q < ns; ++q) act[q] = q;
         grp = upload_groups(act);
-        precond<R>(G, ops, w, n, z, n, ns, W.slot_op, grp, gmax, zfac, yfac, uvec, sd, st, W.act);
+        precond<R>(G, ops, w, n, z, n, ns, W.slot_pc, grp, gmax, zfac, yfac, uvec, sd, st, W.act);
         // GCR step in FP64: p = the cycle's correction, q = K p, both orthogonalised against the directions
         // held (q orthonormal); then x += alpha p, r -= alpha q with alpha = q^H r
         if (k == K) k = 0;
@@ -1025,6 +1040,12 @@ void gt_geometry_free(gt_geometry* g) {
 
 int gt_operators_create(gt_geometry* G, int32_t n_ops, const double* omega, const double* zs, const double* zcap,
                         const double* zbr, const double* table, gt_operators** out) {
+    return gt_operators_create_shared(G, n_ops, omega, zs, zcap, zbr, table, nullptr, out);
+}
+
+int gt_operators_create_shared(gt_geometry* G, int32_t n_ops, const double* omega, const double* zs,
+                               const double* zcap, const double* zbr, const double* table, const int32_t* factor_of,
+                               gt_operators** out) {
     GT_GUARD_BEGIN
     if (!G || !out || n_ops < 1) throw Invalid("bad arguments");
     std::lock_guard<std::mutex> lk(G->lock);
@@ -1033,16 +1054,39 @@ int gt_operators_create(gt_geometry* G, int32_t n_ops, const double* omega, cons
     O->nops = n_ops;
     Pool& p = O->pool;
     const Geo& g = G->geo;
+    // which operators are factorised (their own) and which factorisation each one uses
+    std::vector<int> own;
+    O->fslot.assign(n_ops, -1);
+    for (int q = 0; q < n_ops; ++q) {
+        const int src = factor_of ? factor_of[q] : q;
+        if (src < 0 || src >= n_ops || (factor_of && factor_of[src] != src))
+            throw Invalid("factor_of must name operators that use their own factorisation");
+        if (src == q) {
+            O->fslot[q] = (int)own.size();
+            own.push_back(q);
+        }
+    }
+    for (int q = 0; q < n_ops; ++q)
+        if (O->fslot[q] < 0) O->fslot[q] = O->fslot[factor_of[q]];
+    const int nf_ops = O->nfact = (int)own.size();
     O->omega = p.upload(omega, n_ops);
     O->zs = p.upload(reinterpret_cast<const c64*>(zs), (size_t)n_ops * g.S);
     O->zcap = p.upload(reinterpret_cast<const c64*>(zcap), (size_t)n_ops * g.np);
     O->zbr = p.upload(reinterpret_cast<const c64*>(zbr), (size_t)n_ops * g.nbr);
-    O->tab = p.upload(reinterpret_cast<const c64*>(table), (size_t)n_ops * g.ntab);
     {
-        std::vector<c32> t32((size_t)n_ops * g.ntab);
-        for (size_t q = 0; q < t32.size(); ++q) t32[q] = mk<float>((float)table[2 * q], (float)table[2 * q + 1]);
+        // the admittance tables of the factorised operators (the preconditioner's D^-1 and the Schur values)
+        std::vector<c64> t64((size_t)nf_ops * g.ntab);
+        std::vector<c32> t32(t64.size());
+        for (int f = 0; f < nf_ops; ++f)
+            for (int e = 0; e < g.ntab; ++e) {
+                const size_t src = ((size_t)own[f] * g.ntab + e) * 2, dst = (size_t)f * g.ntab + e;
+                t64[dst] = mk<double>(table[src], table[src + 1]);
+                t32[dst] = mk<float>((float)table[src], (float)table[src + 1]);
+            }
+        O->tab = p.upload(t64.data(), t64.size());
         O->tab32 = p.upload(t32.data(), t32.size());
     }
+    n_ops = nf_ops;        // the factorisation below runs over the factorised operators
     cudaStream_t st = 0;
     const Fronts& F = G->F;
     Pool tmp;
@@ -1186,10 +1230,12 @@ int gt_apply(gt_geometry* G, gt_operators* ops, int32_t kind, int32_t precision,
     GT_CUDA(cudaMemsetAsync(xin, 0, (size_t)n_cols * n * sizeof(c64), st));
     GT_CUDA(cudaMemsetAsync(yout, 0, (size_t)n_cols * n * sizeof(c64), st));
     launch_scatter(G->d_c2d, nc, d_c, nc, xin, n, n_cols, st);
-    std::vector<int> h_op(col_op, col_op + n_cols);
-    // kind 1 groups columns by operator: require them sorted
+    std::vector<int> h_op(col_op, col_op + n_cols), h_pc(n_cols);
+    for (int c = 0; c < n_cols; ++c) h_pc[c] = ops->fslot[h_op[c]];
+    int* d_pc = tmp.upload(h_pc.data(), n_cols);
+    // kind 1 groups columns by factorisation: require them sorted
     for (int c = 1; c < n_cols; ++c)
-        if (kind == 1 && h_op[c] < h_op[c - 1]) throw Invalid("preconditioner columns must be sorted by operator");
+        if (kind == 1 && h_pc[c] < h_pc[c - 1]) throw Invalid("preconditioner columns must be sorted by operator");
     auto run = [&](auto tag) {
         using R = decltype(tag);
         cx<R>* xi;
@@ -1214,7 +1260,7 @@ int gt_apply(gt_geometry* G, gt_operators* ops, int32_t kind, int32_t precision,
             std::vector<int> gptr, gslot, gop, all(n_cols);
             for (int c = 0; c < n_cols; ++c) all[c] = c;
             const int gmax = group_max(G, sizeof(cx<R>));
-            make_groups(all, h_op, gmax, gptr, gslot, gop);
+            make_groups(all, h_pc, gmax, gptr, gslot, gop);
             int* g0 = tmp.upload(gptr.data(), gptr.size());
             int* g1 = tmp.upload(gslot.data(), gslot.size());
             int* g2 = tmp.upload(gop.data(), gop.size());
@@ -1224,7 +1270,7 @@ int gt_apply(gt_geometry* G, gt_operators* ops, int32_t kind, int32_t precision,
             cx<R>* uv = tmp.alloc<cx<R>>((size_t)n_cols * std::max<int64_t>(G->F.vec_total, 1));
             cx<R>* sdv = tmp.alloc<cx<R>>((size_t)n_cols * G->F.nnode);
             GT_CUDA(cudaMemsetAsync(sdv, 0, (size_t)n_cols * G->F.nnode * sizeof(cx<R>), st));
-            precond<R>(G, ops, xi, n, yo, n, n_cols, d_op, grp, gmax, zf, yf, uv, sdv, st);
+            precond<R>(G, ops, xi, n, yo, n, n_cols, d_pc, grp, gmax, zf, yf, uv, sdv, st);
         }
         if constexpr (sizeof(R) == 4) {
             std::vector<c32> h32((size_t)n_cols * n);

@@ -86,6 +86,7 @@ def load():
     lib.gt_profile.argtypes = [P, C.c_char_p, C.c_int32, DP, DP, I32P, C.c_int32]
     lib.gt_strip_coupling.argtypes = [P, DP, DP, C.c_double, C.c_int32, DP, DP, C.POINTER(C.c_int64)]
     lib.gt_node_field.argtypes = [P, C.c_int32, P, C.c_double, P, P, P]
+    lib.gt_operators_create_shared.argtypes = [P, C.c_int32, DP, DP, DP, DP, DP, I32P, C.POINTER(P)]
     lib.gt_kernel_spectrum.argtypes = [C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_int32, C.c_int32, DP,
                                        C.c_int32, DP]
     lib.gt_moment.argtypes = [P, C.c_int32, P, DP, C.c_double, DP, P]
@@ -245,7 +246,9 @@ class Geometry:
 class Operators:
     """Factorised Schur complements at several frequencies (gt_operators_create)."""
 
-    def __init__(self, geom: Geometry, keys: list, data: list):
+    def __init__(self, geom: Geometry, keys: list, data: list, factor_of=None):
+        """factor_of: optional per-operator index of the operator whose factorisation preconditions it
+        (gt_operators_create_shared); None: every operator its own."""
         lib = geom.lib
         self.geom = geom
         w = np.array([x[0] for x in data], np.float64)
@@ -255,9 +258,13 @@ class Operators:
         tab = np.ascontiguousarray(np.stack([x[4] for x in data]).astype(np.complex128))
         self._keep = (zs, zc, zb, tab)
         h = P()
-        check(lib, lib.gt_operators_create(geom.h, len(data), _ptr(w, C.c_double), _ptr(zs.view(np.float64), C.c_double),
-                                           _ptr(zc.view(np.float64), C.c_double), _ptr(zb.view(np.float64), C.c_double),
-                                           _ptr(tab.view(np.float64), C.c_double), C.byref(h)), "gt_operators_create")
+        fo = None if factor_of is None else np.ascontiguousarray(factor_of, np.int32)
+        self.factor_of = fo
+        check(lib, lib.gt_operators_create_shared(
+            geom.h, len(data), _ptr(w, C.c_double), _ptr(zs.view(np.float64), C.c_double),
+            _ptr(zc.view(np.float64), C.c_double), _ptr(zb.view(np.float64), C.c_double),
+            _ptr(tab.view(np.float64), C.c_double), None if fo is None else _ptr(fo, C.c_int32), C.byref(h)),
+            "gt_operators_create_shared")
         self.h = h
         self.keys = list(keys)
 

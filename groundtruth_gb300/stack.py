@@ -133,6 +133,27 @@ class Solution:
         return np.sqrt(np.abs(kx) ** 2 + np.abs(ky) ** 2)
 
 
+PRECOND_REUSE = 0.25      # peec.py: the log-frequency window a factorisation may serve
+
+
+def borrow_plan(keys: list) -> list:
+    """For each frequency, the index of the frequency whose factorisation preconditions it: along the sorted
+    sweep every other frequency borrows the factorisation next below it when that one is within PRECOND_REUSE
+    (|ln f / f_lu|) and lends to no one else yet (peec.py:2227-2343 decides borrowing between rounds; within one
+    batch this halves the factorisations of a sweep whose frequencies are close)."""
+    order = sorted(range(len(keys)), key=lambda q: keys[q])
+    plan = list(range(len(keys)))
+    last_own, lent = None, False
+    for q in order:
+        if last_own is not None and not lent and keys[last_own] > 0 and keys[q] > 0 \
+                and abs(math.log(keys[q] / keys[last_own])) < PRECOND_REUSE:
+            plan[q] = last_own
+            lent = True
+        else:
+            last_own, lent = q, False
+    return plan
+
+
 def freq_key(f: float) -> float:
     """f to 12 significant digits (peec.py:2292-2296, 3264-3267)."""
     return float(f"{float(f):.12g}")
@@ -363,20 +384,22 @@ class PlaneStack:
         op = self.factorise([key])[0]
         return op
 
-    def factorise(self, freqs, together: bool = False) -> list:
+    def factorise(self, freqs, together: bool = False, borrow: bool = False) -> list:
         """Factorise the Schur complement at each frequency key on the device (one batched launch per
         elimination level); returns the cached operators [(Operators, index)].  together: all of them in one
-        Operators object (what a batched solve needs), refactorising cached ones that live elsewhere."""
+        Operators object (what a batched solve needs), refactorising cached ones that live elsewhere.
+        borrow: let a frequency be preconditioned by a neighbouring one's factorisation (borrow_plan)."""
         from . import native
         keys = [freq_key(f) for f in freqs]
         todo = [k for k in dict.fromkeys(keys) if k not in self._ops]
-        if together and not todo and len({id(self._ops[k][0]) for k in keys}) > 1:
+        if together and not todo and (len({id(self._ops[k][0]) for k in keys}) > 1 or
+                                      any((self._ops[k][0].factor_of is not None) != borrow for k in keys)):
             todo = list(dict.fromkeys(keys))
         elif together and todo and len(todo) < len(set(keys)):
             todo = list(dict.fromkeys(keys))
         if todo:
             data = [self._freq_tables(k) for k in todo]
-            ops = native.Operators(self.handle, todo, data)
+            ops = native.Operators(self.handle, todo, data, borrow_plan(todo) if borrow else None)
             with self._lock:
                 for n, k in enumerate(todo):
                     self._ops[k] = (ops, n)
@@ -397,11 +420,11 @@ class PlaneStack:
 
     def solve_batch(self, freqs, rhs_tops, Js, tol: float = 1e-5, max_cycles: int = 8, guesses=None,
                     restart: int = 50, max_its: int = 2000, inner_tol: float = 1e-5, precision: str = "mixed",
-                    reorth: float = 0.7):
+                    reorth: float = 0.7, borrow: bool = False):
         """Many columns (frequency, right-hand side) in one device run: returns [(Ib, V, its, x)]."""
         from . import native
         ncol = len(freqs)
-        ops = self.factorise(freqs, together=True)
+        ops = self.factorise(freqs, together=True, borrow=borrow)
         rhs = np.stack([self.rhs_vector(r, j) for r, j in zip(rhs_tops, Js)])
         x0 = self._warm_start(ops, rhs, guesses) if guesses is not None else None
         x, its, res, ok = native.solve(self.handle, ops, rhs, tol=tol, restart=restart, max_its=max_its,

@@ -110,6 +110,14 @@ void gt_geometry_free(gt_geometry* g);
  * the capacitance / branch impedances; table[n_ops*n_table] the admittance table D^-1 draws from. */
 int gt_operators_create(gt_geometry* g, int32_t n_ops, const double* omega, const double* zs,
                         const double* zcap, const double* zbr, const double* table, gt_operators** out);
+/* As gt_operators_create, with preconditioners shared between operators: factor_of[q] (0..n_ops-1) names the
+ * operator whose Schur factorisation and D^-1 blocks precondition operator q; an operator so named must be its
+ * own (factor_of[factor_of[q]] == factor_of[q]), and only those are factorised.  The system at q is q's own
+ * (a borrowed preconditioner: PlaneStack.operator / _lend, peec.py:2227-2343).  factor_of NULL: every operator
+ * its own. */
+int gt_operators_create_shared(gt_geometry* g, int32_t n_ops, const double* omega, const double* zs,
+                               const double* zcap, const double* zbr, const double* table, const int32_t* factor_of,
+                               gt_operators** out);
 void gt_operators_free(gt_operators* ops);
 
 /* Solve n_cols columns K x = rhs (peec.py:2560-2607): col_op[n_cols] the operator of each column,

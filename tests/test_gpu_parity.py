@@ -148,3 +148,18 @@ def test_kernel_spectrum_on_device(shape):
     host = greens.spectrum_quadrant(greens.strip_kernel(na, nl, d, dz), P0, P1)
     dev = native.kernel_spectrum(na, nl, d, dz, P0, P1, greens.near_values(na, nl, d, dz))
     assert np.max(np.abs(dev - host)) <= 1e-12 * np.max(np.abs(host))
+
+
+def test_solves_with_borrowed_preconditioners(case):
+    """Every other frequency preconditioned by its neighbour's factorisation (gt_operators_create_shared): the
+    same solutions, the system always at the column's own frequency."""
+    name, z, board, st, routes = case
+    freqs = list(board.freqs)
+    if len(freqs) < 2 or gs.borrow_plan(freqs) == list(range(len(freqs))):
+        freqs = [freqs[0], freqs[0] * 1.2]
+    sols = gs.solve_many(routes, freqs, tol=board.tol, borrow=True)
+    ref = gs.solve_many(routes, freqs, tol=board.tol)
+    for per, per_ref in zip(sols, ref):
+        for sol, r in zip(per, per_ref):
+            assert sol.residual <= board.tol
+            assert abs(sol.Z_loop - r.Z_loop) <= 1e-8 * abs(r.Z_loop)
