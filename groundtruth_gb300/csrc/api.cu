@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <complex>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -197,6 +198,11 @@ struct gt_geometry {
     int* d_sterm_tab = nullptr;
     double* d_sterm_coef = nullptr;
     int64_t maxT = 0;  // largest S * P1 * n0 of the two orientations
+    // the last n_lowrank branches are left out of the S-term map: a derived stack whose operators come from
+    // gt_operators_derive (its base's factorisations plus a low-rank update)
+    int n_lowrank = 0;
+    std::vector<int> h_branch_nodes;
+    uint64_t fsig = 0;  // signature of the factor structure (ordering, fronts, panel layout)
     std::unique_ptr<Workspace> ws;
     Profiler prof;
     std::mutex lock;
@@ -240,6 +246,17 @@ struct gt_operators {
     c32* panel32_rm = nullptr;
     c64* dinv64 = nullptr;
     c32* dinv32 = nullptr;
+    std::vector<int> own;        // the operator whose frequency each factorisation was made at
+    // a derived set (gt_operators_derive): the panels and pivots above are its base's; nlow branches beyond the
+    // base's are added by the Woodbury identity with W = S^-1 U (node order) and Minv = (Z + U^T W)^-1 per
+    // factorisation
+    const gt_operators* base = nullptr;
+    int nlow = 0;
+    int* low_ends = nullptr;     // [2 nlow] dense node index of each added branch's ends
+    c64* low_w64 = nullptr;      // [nfact][nlow][nnode]
+    c32* low_w32 = nullptr;
+    c64* low_m64 = nullptr;      // [nfact][nlow][nlow]
+    c32* low_m32 = nullptr;
 };
 
 namespace gt {
@@ -270,6 +287,12 @@ template <> const c64* tab_of<double>(const gt_operators* ops) { return ops->tab
 template <typename R> static const cx<R>* dinv_of(const gt_operators* ops);
 template <> const c32* dinv_of<float>(const gt_operators* ops) { return ops->dinv32; }
 template <> const c64* dinv_of<double>(const gt_operators* ops) { return ops->dinv64; }
+template <typename R> static const cx<R>* low_w_of(const gt_operators* ops);
+template <> const c32* low_w_of<float>(const gt_operators* ops) { return ops->low_w32; }
+template <> const c64* low_w_of<double>(const gt_operators* ops) { return ops->low_w64; }
+template <typename R> static const cx<R>* low_m_of(const gt_operators* ops);
+template <> const c32* low_m_of<float>(const gt_operators* ops) { return ops->low_m32; }
+template <> const c64* low_m_of<double>(const gt_operators* ops) { return ops->low_m64; }
 
 static bool good_fft_size(int P) {
     if (P < 8) return false;
@@ -444,6 +467,12 @@ static void precond(gt_geometry* G, gt_operators* ops, const cx<R>* r, int64_t l
                                 panel_rm_of<R>(ops), zfac, yfac, sd, grp, gmax, st);
         }
     }
+    }
+    if (ops->nlow) {
+        // the derived stack's added branches: y -= W Minv U^T y (the coefficients in zfac, free after the sweeps)
+        Scope s(P, "lowrank", st, nslot * es * (double)G->F.nnode * (ops->nlow + 2));
+        launch_lowrank<R>(sd, G->F.nnode, nslot, ops->nlow, ops->low_ends, low_w_of<R>(ops), low_m_of<R>(ops), slot_op,
+                          col_list, zfac, G->F.nfac, st);
     }
     {
         Scope s(P, "pc_strip", st, nslot * es * (2 * n + nfac));
@@ -1023,6 +1052,39 @@ int gt_geometry_create(const gt_geometry_desc* d, gt_geometry** out) {
         G->level_maxnown.push_back(mo);
         G->max_nf = std::max(G->max_nf, mx);
     }
+    if (d->n_lowrank < 0 || d->n_lowrank > d->n_branches || d->n_lowrank > LOWRANK_MAX)
+        throw Invalid("n_lowrank must be in 0 .. min(n_branches, 64)");
+    G->n_lowrank = d->n_lowrank;
+    G->h_branch_nodes.assign(d->branch_nodes, d->branch_nodes + 2 * d->n_branches);
+    {
+        // FNV-1a over everything that fixes where a factor entry lives
+        uint64_t h = 1469598103934665603ull;
+        auto mix = [&](const int64_t* a, int64_t len) {
+            for (int64_t i = 0; i < len; ++i) {
+                uint64_t v = (uint64_t)a[i];
+                for (int b = 0; b < 8; ++b) {
+                    h ^= (v >> (8 * b)) & 0xff;
+                    h *= 1099511628211ull;
+                }
+            }
+        };
+        const int64_t sizes[5] = {d->n_factor, d->panel_total, d->upd_total, d->vec_total, (int64_t)nf};
+        mix(sizes, 5);
+        mix(d->perm, nn);
+        mix(d->level_ptr, d->n_levels + 1);
+        mix(d->front_order, nf);
+        mix(d->own_start, nf);
+        mix(d->nown, nf);
+        mix(d->nbnd, nf);
+        mix(d->bnd_ptr, nf + 1);
+        mix(d->bnd_idx, d->bnd_ptr[nf]);
+        mix(d->child_ptr, nf + 1);
+        mix(d->child_idx, d->child_ptr[nf]);
+        mix(d->panel_off, nf);
+        mix(d->upd_off, nf);
+        mix(d->vec_off, nf);
+        G->fsig = h;
+    }
     G->d_sterm_ptr = p.upload(d->sterm_ptr, d->n_svalues + 1);
     G->d_sterm_tab = p.upload(d->sterm_tab, d->sterm_ptr[d->n_svalues]);
     G->d_sterm_coef = p.upload(d->sterm_coef, d->sterm_ptr[d->n_svalues]);
@@ -1048,6 +1110,9 @@ int gt_operators_create_shared(gt_geometry* G, int32_t n_ops, const double* omeg
                                gt_operators** out) {
     GT_GUARD_BEGIN
     if (!G || !out || n_ops < 1) throw Invalid("bad arguments");
+    if (G->n_lowrank)
+        throw Invalid("the geometry's last branches are a low-rank update of a base: make its operators with "
+                      "gt_operators_derive");
     std::lock_guard<std::mutex> lk(G->lock);
     std::unique_ptr<gt_operators> O(new gt_operators());
     O->g = G;
@@ -1069,6 +1134,7 @@ int gt_operators_create_shared(gt_geometry* G, int32_t n_ops, const double* omeg
     for (int q = 0; q < n_ops; ++q)
         if (O->fslot[q] < 0) O->fslot[q] = O->fslot[factor_of[q]];
     const int nf_ops = O->nfact = (int)own.size();
+    O->own = own;
     O->omega = p.upload(omega, n_ops);
     O->zs = p.upload(reinterpret_cast<const c64*>(zs), (size_t)n_ops * g.S);
     O->zcap = p.upload(reinterpret_cast<const c64*>(zcap), (size_t)n_ops * g.np);
@@ -1131,6 +1197,169 @@ int gt_operators_create_shared(gt_geometry* G, int32_t n_ops, const double* omeg
     P->flush();
     if (h_status) throw Invalid("the Schur complement has a zero or non-finite pivot (a piece of copper with no "
                                 "path to its reference node?)");
+    *out = O.release();
+    return GT_OK;
+    GT_GUARD_END
+}
+
+int gt_operators_derive(gt_geometry* G, const gt_operators* base, int32_t n_ops, const double* omega, const double* zs,
+                        const double* zcap, const double* zbr, const double* table, gt_operators** out) {
+    GT_GUARD_BEGIN
+    if (!G || !base || !out || n_ops < 1) throw Invalid("bad arguments");
+    const gt_geometry* BG = base->g;
+    if (base->nlow) throw Invalid("the base is itself derived: derive from its base with all the added branches");
+    const int k = G->n_lowrank;
+    if (k < 1) throw Invalid("the geometry adds no branches (n_lowrank 0)");
+    const Geo& g = G->geo;
+    const Geo& bg = BG->geo;
+    if (g.S != bg.S || g.nx != bg.nx || g.ny != bg.ny || g.np != bg.np || g.sheet != bg.sheet ||
+        g.nbr != bg.nbr + k || G->fsig != BG->fsig || G->F.nfac != BG->F.nfac || G->F.nnode != BG->F.nnode)
+        throw Invalid("the geometry is not the base's plus its n_lowrank last branches");
+    for (int e = 0; e < 2 * bg.nbr; ++e)
+        if (G->h_branch_nodes[e] != BG->h_branch_nodes[e]) throw Invalid("the base's branches must lead the geometry's");
+    if (n_ops != base->nops) throw Invalid("n_ops must equal the base's operator count");
+    if (k > G->F.nfac) throw Invalid("more added branches than kept nodes");
+    std::lock_guard<std::mutex> lk(G->lock);
+    std::unique_ptr<gt_operators> O(new gt_operators());
+    O->g = G;
+    O->nops = n_ops;
+    O->nfact = base->nfact;
+    O->fslot = base->fslot;
+    O->own = base->own;
+    O->base = base;
+    Pool& p = O->pool;
+    const int nf = O->nfact;
+    O->omega = p.upload(omega, n_ops);
+    O->zs = p.upload(reinterpret_cast<const c64*>(zs), (size_t)n_ops * g.S);
+    O->zcap = p.upload(reinterpret_cast<const c64*>(zcap), (size_t)n_ops * g.np);
+    O->zbr = p.upload(reinterpret_cast<const c64*>(zbr), (size_t)n_ops * g.nbr);
+    {
+        // D^-1 of the derived stack at each factorisation's frequency (the added branches' admittances too)
+        std::vector<c64> t64((size_t)nf * g.ntab);
+        std::vector<c32> t32(t64.size());
+        for (int f = 0; f < nf; ++f)
+            for (int e = 0; e < g.ntab; ++e) {
+                const size_t src = ((size_t)O->own[f] * g.ntab + e) * 2, dst = (size_t)f * g.ntab + e;
+                t64[dst] = mk<double>(table[src], table[src + 1]);
+                t32[dst] = mk<float>((float)table[src], (float)table[src + 1]);
+            }
+        O->tab = p.upload(t64.data(), t64.size());
+        O->tab32 = p.upload(t32.data(), t32.size());
+    }
+    O->panel64 = base->panel64;
+    O->panel32 = base->panel32;
+    O->panel64_rm = base->panel64_rm;
+    O->panel32_rm = base->panel32_rm;
+    O->dinv64 = base->dinv64;
+    O->dinv32 = base->dinv32;
+    O->nlow = k;
+    const std::vector<int> ends(G->h_branch_nodes.begin() + 2 * bg.nbr, G->h_branch_nodes.end());
+    O->low_ends = p.upload(ends.data(), ends.size());
+    const int64_t nnode = G->F.nnode, nfac = G->F.nfac, ntot = (int64_t)nf * k;
+    O->low_w64 = p.alloc<c64>((size_t)ntot * nnode);
+    O->low_w32 = p.alloc<c32>((size_t)ntot * nnode);
+    cudaStream_t st = 0;
+    Profiler* P = &G->prof;
+    {
+        // W = S^-1 U: the base's FP64 sweeps on U e_j, column c = f k + j, in batches
+        Scope sc(P, "lowrank_make", st);
+        const int gmax = group_max(G, sizeof(c64));
+        const int bc = (int)std::min<int64_t>(ntot, 64);
+        Pool tmp;
+        c64* sv = tmp.alloc<c64>((size_t)bc * nfac);
+        c64* zv = tmp.alloc<c64>((size_t)bc * nfac);
+        c64* uv = tmp.alloc<c64>((size_t)bc * std::max<int64_t>(G->F.vec_total, 1));
+        int* d_gptr = tmp.alloc<int>(bc + 1);
+        int* d_gslot = tmp.alloc<int>(bc);
+        int* d_gop = tmp.alloc<int>(bc);
+        const int nlev = (int)G->level_ptr.size() - 1;
+        for (int64_t c0 = 0; c0 < ntot; c0 += bc) {
+            const int nc = (int)std::min<int64_t>(bc, ntot - c0);
+            c64* wout = O->low_w64 + c0 * nnode;
+            GT_CUDA(cudaMemsetAsync(sv, 0, (size_t)nc * nfac * sizeof(c64), st));
+            GT_CUDA(cudaMemsetAsync(wout, 0, (size_t)nc * nnode * sizeof(c64), st));
+            launch_lowrank_rhs(sv, nfac, (int)c0, nc, k, O->low_ends, g.perm, st);
+            std::vector<int> slots(nc), sfact(nc), gptr, gslot, gop;
+            for (int q = 0; q < nc; ++q) {
+                slots[q] = q;
+                sfact[q] = (int)((c0 + q) / k);
+            }
+            make_groups(slots, sfact, gmax, gptr, gslot, gop);
+            GT_CUDA(cudaMemcpy(d_gptr, gptr.data(), gptr.size() * sizeof(int), cudaMemcpyHostToDevice));
+            GT_CUDA(cudaMemcpy(d_gslot, gslot.data(), gslot.size() * sizeof(int), cudaMemcpyHostToDevice));
+            GT_CUDA(cudaMemcpy(d_gop, gop.data(), gop.size() * sizeof(int), cudaMemcpyHostToDevice));
+            const Groups grp{(int)gop.size(), d_gptr, d_gslot, d_gop};
+            for (int h = 0; h < nlev; ++h) {
+                const int nfl = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);
+                launch_fwd_level<double>(G->F, G->d_order + G->level_ptr[h], nfl, G->level_maxnf[h],
+                                         G->level_maxnown[h], base->panel64, base->dinv64, sv, zv, uv, sv, grp, gmax, st);
+            }
+            for (int h = nlev - 1; h >= 0; --h) {
+                const int nfl = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);
+                launch_bwd_level<double>(G->F, G->d_order + G->level_ptr[h], nfl, G->level_maxnf[h],
+                                         G->level_maxnown[h], base->panel64_rm, zv, sv, wout, grp, gmax, st);
+            }
+            GT_CUDA(cudaStreamSynchronize(st));   // the group tables are reused by the next batch
+        }
+        // U^T W to the host; Minv = (diag(z) + U^T W)^-1 per factorisation at its frequency
+        c64* gbuf = tmp.alloc<c64>((size_t)ntot * k);
+        launch_lowrank_gather(O->low_w64, nnode, (int)ntot, k, O->low_ends, gbuf, st);
+        std::vector<c64> hg((size_t)ntot * k);
+        GT_CUDA(cudaMemcpy(hg.data(), gbuf, hg.size() * sizeof(c64), cudaMemcpyDeviceToHost));
+        std::vector<c64> m64((size_t)nf * k * k);
+        std::vector<c32> m32(m64.size());
+        std::vector<std::complex<double>> A((size_t)k * k), X((size_t)k * k);
+        for (int f = 0; f < nf; ++f) {
+            const int q = O->own[f];
+            for (int i = 0; i < k; ++i)
+                for (int j = 0; j < k; ++j) {
+                    const c64 v = hg[((size_t)f * k + j) * k + i];
+                    A[(size_t)i * k + j] = {v.re, v.im};
+                }
+            for (int i = 0; i < k; ++i) {
+                const size_t zi = ((size_t)q * g.nbr + bg.nbr + i) * 2;
+                A[(size_t)i * k + i] += std::complex<double>(zbr[zi], zbr[zi + 1]);
+            }
+            // Gauss-Jordan with partial pivoting
+            for (size_t e = 0; e < X.size(); ++e) X[e] = (e / k == e % k) ? 1.0 : 0.0;
+            for (int c = 0; c < k; ++c) {
+                int piv = c;
+                for (int r = c + 1; r < k; ++r)
+                    if (std::abs(A[(size_t)r * k + c]) > std::abs(A[(size_t)piv * k + c])) piv = r;
+                const std::complex<double> pv = A[(size_t)piv * k + c];
+                if (!(std::abs(pv) > 0) || !std::isfinite(std::abs(pv)))
+                    throw Invalid("the low-rank branch update is singular");
+                if (piv != c)
+                    for (int j = 0; j < k; ++j) {
+                        std::swap(A[(size_t)piv * k + j], A[(size_t)c * k + j]);
+                        std::swap(X[(size_t)piv * k + j], X[(size_t)c * k + j]);
+                    }
+                const std::complex<double> inv = 1.0 / pv;
+                for (int j = 0; j < k; ++j) {
+                    A[(size_t)c * k + j] *= inv;
+                    X[(size_t)c * k + j] *= inv;
+                }
+                for (int r = 0; r < k; ++r) {
+                    if (r == c) continue;
+                    const std::complex<double> fct = A[(size_t)r * k + c];
+                    if (fct == 0.0) continue;
+                    for (int j = 0; j < k; ++j) {
+                        A[(size_t)r * k + j] -= fct * A[(size_t)c * k + j];
+                        X[(size_t)r * k + j] -= fct * X[(size_t)c * k + j];
+                    }
+                }
+            }
+            for (size_t e = 0; e < X.size(); ++e) {
+                m64[(size_t)f * k * k + e] = mk<double>(X[e].real(), X[e].imag());
+                m32[(size_t)f * k * k + e] = mk<float>((float)X[e].real(), (float)X[e].imag());
+            }
+        }
+        O->low_m64 = p.upload(m64.data(), m64.size());
+        O->low_m32 = p.upload(m32.data(), m32.size());
+        launch_lowrank_to32(O->low_w64, O->low_w32, ntot * nnode, st);
+        GT_CUDA(cudaStreamSynchronize(st));
+    }
+    P->flush();
     *out = O.release();
     return GT_OK;
     GT_GUARD_END

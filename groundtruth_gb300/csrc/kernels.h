@@ -137,6 +137,20 @@ void launch_bwd_level(const Fronts& F, const int64_t* front_list, int nf_level, 
                       const cx<R>* panel_rm, const cx<R>* z, cx<R>* y, cx<R>* sd, const Groups& G, int gmax,
                       cudaStream_t st);
 
+// --- low-rank branch update of a factorised Schur complement (woodbury.cu)
+constexpr int LOWRANK_MAX = 64;      // branches one derived operator set may add
+// y (node order, sd [col][nnode]) -= W Minv (U^T y) per column: W [fact][k][nnode], Minv [fact][k][k],
+// col_fact[col] the factorisation; cbuf [col][ldc] scratch for the k coefficients
+template <typename R>
+void launch_lowrank(cx<R>* sd, int64_t nnode, int ncol, int k, const int* ends, const cx<R>* w, const cx<R>* minv,
+                    const int* col_fact, const int* col_list, cx<R>* cbuf, int64_t ldc, cudaStream_t st);
+// U e_j in factor order for the columns c0 .. c0+ncol of (factorisation, branch) pairs (j = c mod k)
+void launch_lowrank_rhs(c64* s, int64_t nfac, int c0, int ncol, int k, const int* ends, const int64_t* perm,
+                        cudaStream_t st);
+// U^T W entries g[c][i] of ncol node-ordered columns
+void launch_lowrank_gather(const c64* w, int64_t nnode, int ncol, int k, const int* ends, c64* g, cudaStream_t st);
+void launch_lowrank_to32(const c64* a, c32* b, int64_t n, cudaStream_t st);
+
 // --- Krylov vector work (batched, one basis per slot)
 // A basis entry stored in FP16 (real and imaginary halves), scaled by the basis scale so that the entries
 // of a unit vector of length n sit near 1, inside FP16's normal range.

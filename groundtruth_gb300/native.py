@@ -38,7 +38,7 @@ class GeometryDesc(C.Structure):
                 ("panel_total", C.c_int64), ("upd_total", C.c_int64), ("vec_total", C.c_int64),
                 ("ent_ptr", I64P), ("ent_row", I32P), ("ent_col", I32P), ("ent_s", I64P),
                 ("n_svalues", C.c_int64), ("n_table", C.c_int32), ("sterm_ptr", I64P), ("sterm_tab", I32P),
-                ("sterm_coef", DP)]
+                ("sterm_coef", DP), ("n_lowrank", C.c_int32)]
 
 
 PRECISIONS = {"mixed": 0, "fp64": 1, "mixed16": 2}
@@ -86,6 +86,7 @@ def load():
     lib.gt_profile.argtypes = [P, C.c_char_p, C.c_int32, DP, DP, I32P, C.c_int32]
     lib.gt_strip_coupling.argtypes = [P, DP, DP, C.c_double, C.c_int32, DP, DP, C.POINTER(C.c_int64)]
     lib.gt_node_field.argtypes = [P, C.c_int32, P, C.c_double, P, P, P]
+    lib.gt_operators_derive.argtypes = [P, P, C.c_int32, DP, DP, DP, DP, DP, C.POINTER(P)]
     lib.gt_operators_create_shared.argtypes = [P, C.c_int32, DP, DP, DP, DP, DP, I32P, C.POINTER(P)]
     lib.gt_kernel_spectrum.argtypes = [C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_int32, C.c_int32, DP,
                                        C.c_int32, DP]
@@ -162,6 +163,7 @@ class Geometry:
         d.sterm_ptr = _ptr(arr(M.indptr, np.int64), C.c_int64)
         d.sterm_tab = _ptr(arr(M.indices, np.int32), C.c_int32)
         d.sterm_coef = _ptr(arr(M.data, np.float64), C.c_double)
+        d.n_lowrank = int(getattr(st, "n_lowrank", 0))
         h = P()
         check(lib, lib.gt_geometry_create(C.byref(d), C.byref(h)), "gt_geometry_create")
         self.h = h
@@ -246,9 +248,11 @@ class Geometry:
 class Operators:
     """Factorised Schur complements at several frequencies (gt_operators_create)."""
 
-    def __init__(self, geom: Geometry, keys: list, data: list, factor_of=None):
+    def __init__(self, geom: Geometry, keys: list, data: list, factor_of=None, base: "Operators | None" = None):
         """factor_of: optional per-operator index of the operator whose factorisation preconditions it
-        (gt_operators_create_shared); None: every operator its own."""
+        (gt_operators_create_shared); None: every operator its own.  base: the base stack's operators at the
+        same keys, for a derived geometry (gt_operators_derive: the base's factorisations plus a low-rank
+        update for the added branches); kept alive as long as these."""
         lib = geom.lib
         self.geom = geom
         w = np.array([x[0] for x in data], np.float64)
@@ -258,13 +262,20 @@ class Operators:
         tab = np.ascontiguousarray(np.stack([x[4] for x in data]).astype(np.complex128))
         self._keep = (zs, zc, zb, tab)
         h = P()
-        fo = None if factor_of is None else np.ascontiguousarray(factor_of, np.int32)
-        self.factor_of = fo
-        check(lib, lib.gt_operators_create_shared(
-            geom.h, len(data), _ptr(w, C.c_double), _ptr(zs.view(np.float64), C.c_double),
-            _ptr(zc.view(np.float64), C.c_double), _ptr(zb.view(np.float64), C.c_double),
-            _ptr(tab.view(np.float64), C.c_double), None if fo is None else _ptr(fo, C.c_int32), C.byref(h)),
-            "gt_operators_create_shared")
+        self.base = base
+        args = (_ptr(w, C.c_double), _ptr(zs.view(np.float64), C.c_double), _ptr(zc.view(np.float64), C.c_double),
+                _ptr(zb.view(np.float64), C.c_double), _ptr(tab.view(np.float64), C.c_double))
+        if base is not None:
+            if list(keys) != base.keys:
+                raise ValueError("derived operators take the base's keys, in its order")
+            self.factor_of = base.factor_of
+            check(lib, lib.gt_operators_derive(geom.h, base.h, len(data), *args, C.byref(h)), "gt_operators_derive")
+        else:
+            fo = None if factor_of is None else np.ascontiguousarray(factor_of, np.int32)
+            self.factor_of = fo
+            check(lib, lib.gt_operators_create_shared(geom.h, len(data), *args,
+                                                      None if fo is None else _ptr(fo, C.c_int32), C.byref(h)),
+                  "gt_operators_create_shared")
         self.h = h
         self.keys = list(keys)
 

@@ -19,6 +19,7 @@ layer raises NotImplementedError) and full-width strips (grids without wx/wy wid
 """
 from __future__ import annotations
 
+import copy
 import math
 import threading
 from collections import OrderedDict
@@ -33,6 +34,7 @@ from . import greens, layout
 SIGMA_CU = 5.8e7
 SCREEN_MIN_NODES = 16
 OPERATOR_CACHE = 64           # factorised frequencies kept on the device per stack
+LOWRANK_MAX = 64              # branches a derived stack may add to its base (gt_operators_derive)
 
 
 class SolverError(RuntimeError):
@@ -127,10 +129,23 @@ class Solution:
         cy[:, 1:] += Iy != 0
         return kx / np.maximum(cx, 1) / d, ky / np.maximum(cy, 1) / d
 
+    def state_for(self, stack: "PlaneStack") -> np.ndarray:
+        """The solver's unknown vector [branch currents; kept node potentials] of this solution on `stack`, the
+        stack it was solved on, rebuilt from the currents and potentials kept here (peec.py:1127-1145; a warm
+        start for a derived stack through map_state)."""
+        strips = np.concatenate([self.I_x[tuple(stack.xa.T)], self.I_y[tuple(stack.ya.T)]])
+        Ib = np.concatenate([strips, self.I_cap, self.I_branch])
+        return np.concatenate([Ib, self.V[np.nonzero(stack.node)][stack.keep]])
+
     def sheet_current(self, k: int, d_mm: float, copper: bool = False) -> np.ndarray:
         """|K| at the nodes of layer k (peec.py:1205-1208)."""
         kx, ky = self.node_field(k, d_mm, copper)
         return np.sqrt(np.abs(kx) ** 2 + np.abs(ky) ** 2)
+
+
+def native_geometry(st):
+    from . import native
+    return native.Geometry(st)
 
 
 PRECOND_REUSE = 0.25      # peec.py: the log-frequency window a factorisation may serve
@@ -178,6 +193,9 @@ class PlaneStack:
                 raise NotImplementedError("strips narrower than the pitch (Grid.wx/wy) are not modelled")
         self.lib = native.load() if _device else None
         self._device = bool(_device)
+        self.screen, self.leaf = screen, leaf
+        self._base: Optional[PlaneStack] = None
+        self.n_lowrank = 0
         self.layers = list(layers)
         self.N = self.n_sheets = len(layers)
         self.nx, self.ny = g0.nx, g0.ny
@@ -204,7 +222,7 @@ class PlaneStack:
         self._schur_structure(leaf)
         self._lock = threading.Lock()
         self._ops: OrderedDict = OrderedDict()
-        self.handle = native.Geometry(self) if _device else None
+        self.handle = native_geometry(self) if _device else None
 
     # ------------------------------------------------------------------ construction
     def _check_screen(self, screen: bool):
@@ -342,6 +360,70 @@ class PlaneStack:
         M.eliminate_zeros()
         self.sterm = M
 
+    # ------------------------------------------------------------------ derived stacks
+    def node_id(self, node) -> int:
+        """The node number of (layer, i, j), -1 when it is not on copper (peec.py:1864-1869)."""
+        k, i, j = (int(v) for v in node)
+        if not (0 <= k < self.N and 0 <= i < self.nx and 0 <= j < self.ny):
+            return -1
+        return int(self.nid[k, i, j])
+
+    def with_branches(self, extra: list) -> "PlaneStack":
+        """This stack plus a few branches (candidate vias, parts), peec.py:1871-1912.  Shares the grids, the
+        kernel spectra and the Schur structure; its solves reuse this stack's factorisations through a low-rank
+        (Woodbury) update of the Schur complement (gt_operators_derive).  Branches with an end off copper or
+        both ends on one node are dropped; none left: this stack.  A branch that joins two pieces of copper
+        changes the reference nodes: a stack of its own.  A derived stack of a derived stack derives from the
+        first base with all the added branches (the same system and preconditioner)."""
+        extra = [b for b in extra if self.node_id(b.a) >= 0 and self.node_id(b.b) >= 0
+                 and tuple(b.a) != tuple(b.b)]
+        if not extra:
+            return self
+        a = np.array([self.node_id(b.a) for b in extra])
+        b = np.array([self.node_id(b.b) for b in extra])
+        branches = self.branches + extra
+        root = self._base if self._base is not None else self
+        if np.any(self.full_label[a] != self.full_label[b]) or len(branches) - root.nbr > LOWRANK_MAX:
+            return PlaneStack(self.layers, branches, self.pairs, self.sigma, self.precond_mode, self.screen,
+                              leaf=self.leaf, _device=self._device)
+        t, kept = layout.topology([l.grid.node for l in root.layers], [l.grid.xb for l in root.layers],
+                                  [l.grid.yb for l in root.layers], root.d,
+                                  [(p.upper, p.lower, p.c_per_area, p.tan_delta) for p in root.pairs],
+                                  [(br.a, br.b) for br in branches])
+        if len(kept) != len(branches) or not np.array_equal(t.keep, root.keep):
+            raise RuntimeError("a derived stack must keep its base's nodes")
+        # a shallow copy shares the grids, spectra, symbolic analysis and S-term map (which covers the base's
+        # branches only); the branch list, numbering of the unknowns and the caches are its own
+        new = copy.copy(root)
+        new.top = t
+        new.branches_all = new.branches = branches
+        new.nbr, new.nb = t.nbr, t.nb
+        new.full_label, new.cond_label = t.full_label, t.cond_label
+        new.dense = layout.dense_layout(t)
+        new.n_table = root.tab_br0 + t.nbr
+        new.n_lowrank = t.nbr - root.nbr
+        new._base = root
+        new._lock = threading.Lock()
+        new._ops = OrderedDict()
+        new.handle = native_geometry(new) if root._device else None
+        return new
+
+    def map_state(self, x: Optional[np.ndarray], stack: "PlaneStack") -> Optional[np.ndarray]:
+        """A solution vector of `stack` in this stack's unknowns (a warm start), peec.py:1914-1923: the same
+        stack, or one whose branches lead this one's on the same base, whose added branches start with zero
+        current; None otherwise."""
+        if x is None:
+            return None
+        if stack is self:
+            return x
+        root = self._base if self._base is not None else self
+        sroot = stack._base if stack._base is not None else stack
+        n = len(stack.branches)
+        if sroot is root and n <= len(self.branches) and all(p is q for p, q in zip(stack.branches, self.branches)) \
+                and len(x) == stack.nb + int(stack.keep.sum()):
+            return np.concatenate([x[: stack.nb], np.zeros(self.nb - stack.nb, complex), x[stack.nb:]])
+        return None
+
     # ------------------------------------------------------------------ per-frequency data
     def _freq_tables(self, f: float):
         """(omega, sheet impedances (S,), cap impedances (npairs,), branch impedances (nbr,), admittance
@@ -391,6 +473,8 @@ class PlaneStack:
         borrow: let a frequency be preconditioned by a neighbouring one's factorisation (borrow_plan)."""
         from . import native
         keys = [freq_key(f) for f in freqs]
+        if self._base is not None:
+            return self._factorise_derived(keys, borrow)
         todo = [k for k in dict.fromkeys(keys) if k not in self._ops]
         if together and not todo and (len({id(self._ops[k][0]) for k in keys}) > 1 or
                                       any((self._ops[k][0].factor_of is not None) != borrow for k in keys)):
@@ -403,6 +487,24 @@ class PlaneStack:
             with self._lock:
                 for n, k in enumerate(todo):
                     self._ops[k] = (ops, n)
+                while len(self._ops) > max(OPERATOR_CACHE, len(keys)):
+                    self._ops.popitem(last=False)
+        return [self._ops[k] for k in keys]
+
+    def _factorise_derived(self, keys: list, borrow: bool) -> list:
+        """A derived stack's operators: its base's factorisations of the keys (made there if need be) with the
+        low-rank update for the added branches (peec.py:2354-2377), one set per base operator set."""
+        from . import native
+        bops = self._base.factorise(keys, together=True, borrow=borrow)
+        bobj = bops[0][0]
+        with self._lock:
+            cached = all(k in self._ops and self._ops[k][0].base is bobj for k in keys)
+        if not cached:
+            data = [self._freq_tables(k) for k in bobj.keys]
+            dobj = native.Operators(self.handle, bobj.keys, data, base=bobj)
+            with self._lock:
+                for n, k in enumerate(bobj.keys):
+                    self._ops[k] = (dobj, n)
                 while len(self._ops) > max(OPERATOR_CACHE, len(keys)):
                     self._ops.popitem(last=False)
         return [self._ops[k] for k in keys]
@@ -468,10 +570,11 @@ class PlaneStack:
         px, py = greens.strip_coupling(segments, [self.xa, self.ya], self.d, self.zs, self.ts)
         return np.concatenate([px, py])
 
-    def branch_coupling(self, segments: np.ndarray) -> np.ndarray:
+    def branch_coupling(self, segments: np.ndarray, start: int = 0) -> np.ndarray:
+        """psi of the branches from `start` on: a via's barrel couples to the trace's vertical segments."""
         vert = [s for s in segments if abs(s[5] - s[2]) > 0 and np.linalg.norm(s[3:5] - s[0:2]) < 1e-12]
-        out = np.zeros(self.nbr)
-        for n, b in enumerate(self.branches):
+        out = np.zeros(self.nbr - start)
+        for n, b in enumerate(self.branches[start:]):
             if b.kind == "via" and vert:
                 pa, pb = self.pos(b.a), self.pos(b.b)
                 out[n] = sum(s[7] * greens.segment_mutual(s[0:3], s[3:6], pa, pb, b.radius) for s in vert)
@@ -511,10 +614,15 @@ class RouteExcitation:
     (peec.py:2703-2817)."""
 
     def __init__(self, stack: PlaneStack, trace: list, inject_driver=None, inject_receiver=None,
-                 trace_thickness: float = 35e-6, injections: Optional[list] = None):
+                 trace_thickness: float = 35e-6, strip_psi: Optional[np.ndarray] = None,
+                 branch_psi: Optional[np.ndarray] = None, injections: Optional[list] = None):
+        """strip_psi / branch_psi: the coupling of the same loop computed on another stack with the same strips
+        (a derived stack: RouteExcitation.on), reused; branches beyond branch_psi are coupled here."""
         self.stack = stack
         self.trace = trace
         self.trace_t = trace_thickness
+        self.inject = (inject_driver, inject_receiver)
+        self.extra = list(injections or [])
         self.segments = np.array([[*s.a, *s.b, s.width, s.i] for s in trace], float).reshape(-1, 8)
         terms = []
         if inject_driver is not None:
@@ -539,10 +647,18 @@ class RouteExcitation:
                 raise SolverError("receiver return node is not connected to the driver's return node")
             raise SolverError("the injected currents do not balance on every connected piece of copper")
         self.injections = ids
-        self.strip_psi = stack.strip_coupling(self.segments)
-        self.branch_psi = stack.branch_coupling(self.segments)
+        self.strip_psi = stack.strip_coupling(self.segments) if strip_psi is None else strip_psi
+        bp = np.zeros(0) if branch_psi is None else np.asarray(branch_psi, float)
+        if len(bp) < stack.nbr:
+            bp = np.concatenate([bp, stack.branch_coupling(self.segments, start=len(bp))])
+        self.branch_psi = bp[: stack.nbr]
         self.psi = np.concatenate([self.strip_psi, np.zeros(stack.ncap), self.branch_psi])
         self.L_trace = greens.trace_self(self.segments, trace_thickness) if len(trace) else 0.0
+
+    def on(self, stack: PlaneStack) -> "RouteExcitation":
+        """The same loop on a derived stack (with_branches), its strip coupling reused (peec.py:2771-2774)."""
+        return RouteExcitation(stack, self.trace, *self.inject, self.trace_t, self.strip_psi, self.branch_psi,
+                               self.extra)
 
     def J(self) -> np.ndarray:
         J = np.zeros(self.stack.n_nodes)

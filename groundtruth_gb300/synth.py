@@ -439,5 +439,38 @@ def _labels(mask: np.ndarray, xb: np.ndarray, yb: np.ndarray) -> np.ndarray:
     return lab
 
 
+def what_if_branches(board: Board, seed: int, n_via: int = 2, n_part: int = 1) -> list:
+    """A what-if edit's added branches (the serving workload's "add 1-4 vias" / "move a decoupling part"):
+    n_via stitching vias and n_part decoupling parts (ESR 20 mohm, ESL 0.5 nH, 100 nF) between two sheets at
+    seeded positions where both sheets have copper and the two nodes already lie on one connected piece
+    (through the plane pair or other branches), so the base's reference nodes stay."""
+    from . import layout
+    rng = np.random.default_rng(seed)
+    t, _ = layout.topology([l.node for l in board.layers], [l.xb for l in board.layers],
+                           [l.yb for l in board.layers], board.d,
+                           [(p.upper, p.lower, p.c_per_area, p.tan_delta) for p in board.pairs],
+                           [(b.a, b.b) for b in board.branches])
+    S = len(board.layers)
+    out, taken = [], {(b.a, b.b) for b in board.branches}
+    for n in range(200 * (n_via + n_part)):
+        if len(out) == n_via + n_part:
+            break
+        k0 = int(rng.integers(0, S - 1))
+        k1 = int(rng.integers(k0 + 1, S))
+        i, j = int(rng.integers(1, board.nx - 1)), int(rng.integers(1, board.ny - 1))
+        a, b = (k0, i, j), (k1, i, j)
+        na, nb = int(t.nid[a]), int(t.nid[b])
+        if na < 0 or nb < 0 or t.full_label[na] != t.full_label[nb] or (a, b) in taken:
+            continue
+        taken.add((a, b))
+        length = abs(board.layers[k0].z - board.layers[k1].z)
+        if len(out) < n_via:
+            out.append(BranchSpec(a, b, length / (SIGMA_CU * math.pi * 2 * 1.5e-4 * 25e-6), 2e-10 * length / 1e-3,
+                                  0.0, "via", 1.5e-4))
+        else:
+            out.append(BranchSpec(a, b, 0.02, 0.5e-9, 100e-9, "part"))
+    return out
+
+
 WORKLOADS = {"plain_plane": plain_plane, "slotted_pair": slotted_pair, "small_pair": small_pair,
              "small_stack3": small_stack3, "six_sheet": six_sheet}

@@ -74,6 +74,10 @@ typedef struct gt_geometry_desc {
     const int64_t* sterm_ptr;           /* [n_svalues+1] CSR: S value = sum coef * table[tab] */
     const int32_t* sterm_tab;
     const double* sterm_coef;
+    /* A derived stack (PlaneStack.with_branches, peec.py:1871-1912): the last n_lowrank (0..64) branches are
+     * left out of the S-term map, whose Schur structure is its base's; its operators come from
+     * gt_operators_derive.  0 for every other geometry. */
+    int32_t n_lowrank;
 } gt_geometry_desc;
 
 typedef struct gt_solve_opts {
@@ -118,6 +122,15 @@ int gt_operators_create(gt_geometry* g, int32_t n_ops, const double* omega, cons
 int gt_operators_create_shared(gt_geometry* g, int32_t n_ops, const double* omega, const double* zs,
                                const double* zcap, const double* zbr, const double* table, const int32_t* factor_of,
                                gt_operators** out);
+/* Operators of a derived geometry (n_lowrank > 0) from its base's (peec.py:2345-2377): operator q is the
+ * base's operator q with the added branches, preconditioned by the base's factorisation of q plus the
+ * Woodbury identity for the added branches (S' = S + U diag(1/z) U^T; only an n_lowrank x n_lowrank matrix
+ * per factorisation is inverted).  Arguments as gt_operators_create for the derived geometry (zbr and table
+ * with its branches), n_ops equal to the base's.  The base's factor panels are shared, not copied: free the
+ * derived operators before the base's. */
+int gt_operators_derive(gt_geometry* g, const gt_operators* base, int32_t n_ops, const double* omega,
+                        const double* zs, const double* zcap, const double* zbr, const double* table,
+                        gt_operators** out);
 void gt_operators_free(gt_operators* ops);
 
 /* Solve n_cols columns K x = rhs (peec.py:2560-2607): col_op[n_cols] the operator of each column,

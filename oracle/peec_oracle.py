@@ -17,6 +17,7 @@ covers (one current sheet per layer, full-width strips: no face sheets and no na
 * system product / preconditioner               src/groundtruth/solver/peec.py:3043-3083
 * restarted GMRES (CGS + DGKS, Givens)          src/groundtruth/solver/peec.py:3093-3224
 * solve driver                                  src/groundtruth/solver/peec.py:2560-2607
+* derived stacks (added branches, Woodbury)     src/groundtruth/solver/peec.py:1871-1923, 2354-2377
 * excitation, coupling, moment, loop impedance  src/groundtruth/solver/peec.py:2615-2817, 3227-3250
 
 Parity of this restatement is pinned by ``tests/golden/*.npz``, produced by the reference itself
@@ -24,6 +25,7 @@ Parity of this restatement is pinned by ``tests/golden/*.npz``, produced by the 
 """
 from __future__ import annotations
 
+import copy
 import math
 from dataclasses import dataclass, field
 from typing import Callable, Optional
@@ -408,8 +410,35 @@ class OracleStack:
         self.pairs = list(pairs or [])
         self.precond_mode = precond
         self.sheet_t = np.array([l.thickness for l in layers], float)
+        self._base: Optional[OracleStack] = None
         self._topology(list(branches or []))
         self._kernels()
+
+    def with_branches(self, extra: list) -> "OracleStack":
+        """This stack plus a few branches (peec.py:1871-1912): a shallow copy sharing the grids and kernels with
+        its own incidence; its operators update the base's factorisation (operator below).  A branch joining
+        two pieces of copper: a stack of its own."""
+        extra = [b for b in extra if self.nid[b.a] >= 0 and self.nid[b.b] >= 0 and b.a != b.b]
+        if not extra:
+            return self
+        a = np.array([self.nid[b.a] for b in extra])
+        b = np.array([self.nid[b.b] for b in extra])
+        if np.any(self.full_label[a] != self.full_label[b]):
+            return OracleStack(self.layers, self.d, self.branches + extra, self.pairs, self.sigma, self.precond_mode)
+        new = copy.copy(self)
+        new._topology(self.branches + extra)
+        new._base = self
+        return new
+
+    def map_state(self, x: Optional[np.ndarray], stack: "OracleStack") -> Optional[np.ndarray]:
+        """A solution of the base in this stack's unknowns, the added branches at zero (peec.py:1914-1923)."""
+        if x is None:
+            return None
+        if stack is self:
+            return x
+        if self._base is stack and len(x) == stack.nb + stack.Ar.shape[1]:
+            return np.concatenate([x[: stack.nb], np.zeros(self.nb - stack.nb, complex), x[stack.nb:]])
+        return None
 
     # -- topology (peec.py:1596-1656, 1845-1862)
     def _topology(self, branches):
@@ -587,6 +616,20 @@ class OracleStack:
         f = cache_value(f)
         w, R_strip, z_tail = self.impedances(f)
         Dinv = self.admittance(w, R_strip, z_tail)
+        if self._base is not None:
+            # a derived stack: S = S_base + U diag(1/z_new) U^T, solved by the Woodbury identity on the base's
+            # factorisation (peec.py:2354-2377); only a k x k matrix is inverted
+            bop = self._base.operator(f)
+            k0 = self._base.nb
+            U = self.ArT[:, k0:].toarray()
+            SiU = bop["solve_S"](U.astype(complex))
+            small_inv = np.linalg.inv(np.diag(z_tail[k0 - self.ns:]) + U.T @ SiU)
+
+            def solve_S(v, b=bop["solve_S"], SiU=SiU, Ut=U.T, small_inv=small_inv):
+                y = b(v)
+                return y - SiU @ (small_inv @ (Ut @ y))
+            return {"f": f, "w": w, "R_strip": R_strip, "z_tail": z_tail, "Dinv": Dinv, "S": None,
+                    "solve_S": solve_S}
         S = (self.ArT @ Dinv @ self.Ar).tocsc()
         lu = splu(S, permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=LU_PIVOT_THRESHOLD,
                   options={"SymmetricMode": True})

@@ -16,6 +16,9 @@ The reference's solver module imports shapely at module level but uses it only t
 * per net and frequency the solve at rtol = board.tol with GMRES(board.restart): unknown vector, its,
   Z_loop, magnetic moment, psi
 
+``small_pair_derived.npz`` holds the same for small_pair plus a what-if edit's branches on a derived stack
+(PlaneStack.with_branches), including solves warm-started from the base's solutions.
+
 ``--full`` additionally runs the 256 x 256 slotted plane pair (a few nets x frequencies, minutes per solve)
 and stores only its scalar outputs (Z_loop, its, current norms).
 """
@@ -104,6 +107,45 @@ def record(peec, board: synth.Board, solve: bool = True) -> dict:
     return out
 
 
+def record_derived(peec, board: synth.Board, seed: int) -> dict:
+    """The same board plus a what-if edit's branches (synth.what_if_branches) on a derived stack
+    (PlaneStack.with_branches: the base's factorisation with a Woodbury update): its operator's products on a
+    seeded vector at the first frequency, and per net and frequency the cold solve and the solve warm-started
+    from the base's solution (map_state)."""
+    peec.gmres_restart = lambda n, r=board.restart: r
+    peec.PlaneStack.solve.__defaults__ = (board.tol, 8, None)
+    st, routes = build_reference(peec, board)
+    extra = synth.what_if_branches(board, seed)
+    branches = [peec.Branch(b.a, b.b, (lambda f, b=b: b.z(f)), f"x{n}", b.kind, b.radius) for n, b in enumerate(extra)]
+    dst = st.with_branches(branches)
+    assert dst._base is st, "the edit must make a derived stack"
+    out = {f"board_{k}": v for k, v in board.to_arrays().items()}
+    out["extra"] = np.array([[*b.a, *b.b, b.R, b.L, b.C, b.kind == "via", b.radius] for b in extra], float)
+    out.update(nb=np.int64(dst.nb), nbr=np.int64(dst.nbr))
+    f0 = float(board.freqs[0])
+    op = dst.operator(f0)
+    rng = np.random.default_rng(321)
+    n = dst.nb + dst.Ar.shape[1]
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    host = peec._HostMath(dst)
+    out.update(prod_x=x, prod_matvec=host.matvec(op, x), prod_precond=host.precond(op, x))
+    for k, r in enumerate(routes):
+        rd = r.on(dst)
+        out[f"psi{k}"] = rd.psi
+        for q, f in enumerate(board.freqs):
+            base = r.solve(float(f))
+            cold = rd.solve(float(f))
+            warm = rd.solve(float(f), guess=[dst.map_state(base.state_for(st), st)])
+            out[f"Z{k}_{q}"] = np.complex128(cold.Z_loop)
+            out[f"x{k}_{q}"] = cold.state_for(dst)
+            out[f"its{k}_{q}"] = np.int64(cold.iterations)
+            out[f"Zwarm{k}_{q}"] = np.complex128(warm.Z_loop)
+            out[f"itswarm{k}_{q}"] = np.int64(warm.iterations)
+            print(f"  {board.name}+edit net {k} f {f:.4g}: its {cold.iterations} (warm {warm.iterations}) "
+                  f"Z {cold.Z_loop:.6g}", flush=True)
+    return out
+
+
 def kernel_functions(kernel) -> dict:
     """Point values of the reference's Green's-function helpers."""
     rng = np.random.default_rng(7)
@@ -124,8 +166,13 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", required=True)
     ap.add_argument("--full", action="store_true")
+    ap.add_argument("--derived-only", action="store_true", help="only the derived-stack fixture")
     args = ap.parse_args()
     peec, kernel = import_reference(args.reference)
+    print("small_pair_derived", flush=True)
+    np.savez_compressed(HERE / "small_pair_derived.npz", **record_derived(peec, synth.small_pair(), seed=11))
+    if args.derived_only:
+        return
     np.savez_compressed(HERE / "kernel_functions.npz", **kernel_functions(kernel))
     for name in ("small_pair", "small_stack3", "plain_plane"):
         board = synth.WORKLOADS[name]()

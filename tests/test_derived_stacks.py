@@ -1,0 +1,151 @@
+"""Derived stacks (PlaneStack.with_branches: a what-if edit's added branches on a base's factorisation, updated
+by the Woodbury identity; peec.py:1871-1923, 2354-2377) on the CPU: the oracle's restatement against the
+reference's own derived-stack outputs (tests/golden/small_pair_derived.npz), the Woodbury update against a
+fresh factorisation of the whole stack, and the host side of the GPU build's derived stacks (branch filtering,
+unknown numbering, warm-start mapping) without a device."""
+import numpy as np
+import pytest
+
+from groundtruth_gb300 import stack as gs, synth
+from oracle import peec_oracle as po
+from test_oracle_golden import load, oracle_routes, oracle_stack
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(np.asarray(b)), 1e-300)
+
+
+def extra_of(z):
+    """The edit's branches as synth.BranchSpec rows (a, b, R, L, C, is_via, radius)."""
+    out = []
+    for r in z["extra"]:
+        a, b = tuple(int(v) for v in r[0:3]), tuple(int(v) for v in r[3:6])
+        out.append(synth.BranchSpec(a, b, float(r[6]), float(r[7]), float(r[8]), "via" if r[9] else "part",
+                                    float(r[10])))
+    return out
+
+
+@pytest.fixture(scope="module")
+def derived():
+    z, board = load("small_pair_derived")
+    extra = extra_of(z)
+    ost = oracle_stack(board)
+    odst = ost.with_branches([po.OBranch(b.a, b.b, b.R, b.L, b.C, b.kind, b.radius) for b in extra])
+    return z, board, extra, ost, odst
+
+
+def test_fixture_edit_is_the_seeded_one(derived):
+    z, board, extra, ost, odst = derived
+    again = synth.what_if_branches(board, seed=11)
+    assert [(b.a, b.b, b.kind) for b in again] == [(b.a, b.b, b.kind) for b in extra]
+
+
+def test_oracle_derived_stack_is_derived(derived):
+    z, board, extra, ost, odst = derived
+    assert odst._base is ost
+    assert odst.nb == int(z["nb"]) and odst.nbr == int(z["nbr"])
+    assert np.array_equal(odst.keep, ost.keep)
+
+
+def test_oracle_derived_products_match_reference(derived):
+    z, board, extra, ost, odst = derived
+    op = odst.operator(float(board.freqs[0]))
+    assert rel(odst.matvec(op, z["prod_x"]), z["prod_matvec"]) < 1e-12
+    assert rel(odst.precond(op, z["prod_x"]), z["prod_precond"]) < 1e-10
+
+
+def test_woodbury_equals_fresh_factorisation(derived):
+    """The update is exact: the derived stack's preconditioner is the whole stack's own."""
+    z, board, extra, ost, odst = derived
+    full = po.OracleStack(ost.layers, ost.d, ost.branches + list(odst.branches[ost.nbr:]), ost.pairs, ost.sigma,
+                          ost.precond_mode)
+    assert full._base is None and full.nb == odst.nb
+    for f in board.freqs:
+        a, b = odst.operator(float(f)), full.operator(float(f))
+        assert rel(odst.precond(a, z["prod_x"]), full.precond(b, z["prod_x"])) < 1e-10
+
+
+def test_oracle_derived_solves_match_reference(derived):
+    z, board, extra, ost, odst = derived
+    routes = oracle_routes(odst, board)
+    for k, r in enumerate(routes):
+        assert rel(r.psi, z[f"psi{k}"]) < 1e-12
+        q = 1
+        ref = r.solve(float(board.freqs[q]), tol=board.tol)
+        assert abs(ref["Z_loop"] - z[f"Z{k}_{q}"]) <= 1e-8 * abs(z[f"Z{k}_{q}"])
+        assert rel(ref["x"][: odst.nb], z[f"x{k}_{q}"][: odst.nb]) < 1e-7
+
+
+def test_oracle_map_state(derived):
+    z, board, extra, ost, odst = derived
+    x = np.arange(ost.nb + int(ost.keep.sum())).astype(complex)
+    y = odst.map_state(x, ost)
+    assert len(y) == odst.nb + int(odst.keep.sum())
+    assert np.array_equal(y[: ost.nb], x[: ost.nb]) and not y[ost.nb: odst.nb].any()
+    assert np.array_equal(y[odst.nb:], x[ost.nb:])
+
+
+# ---------------------------------------------------------------------------------------- host side of the build
+def host_stack(board):
+    return gs.from_board(board, _device=False)[0]
+
+
+def branches_of(extra):
+    return [gs.Branch(b.a, b.b, b.z, f"x{n}", b.kind, b.radius) for n, b in enumerate(extra)]
+
+
+def test_with_branches_numbering(derived):
+    z, board, extra, ost, odst = derived
+    st = host_stack(board)
+    dst = st.with_branches(branches_of(extra))
+    assert dst._base is st and dst.n_lowrank == len(extra)
+    assert dst.nb == int(z["nb"]) and dst.nbr == int(z["nbr"])
+    assert np.array_equal(dst.keep, st.keep) and dst.sym is st.sym and dst.spectrum is st.spectrum
+    # the dense layout gains the branches; the strips, caps and nodes keep their places
+    assert dst.dense.off_b == st.dense.off_b and dst.dense.n >= st.dense.n
+    c2d_base, c2d = st.dense.compact_to_dense, dst.dense.compact_to_dense
+    assert np.array_equal(c2d[: st.nb], c2d_base[: st.nb])
+    assert np.array_equal(c2d[dst.nb:] - dst.dense.off_v, c2d_base[st.nb:] - st.dense.off_v)
+    # the admittance table grows by the added branches; the S-term map stays the base's
+    assert dst.n_table == st.n_table + len(extra) and dst.sterm is st.sterm
+    w, zs, zcap, zbr, tab = dst._freq_tables(1e8)
+    assert np.allclose(tab[dst.tab_br0 + st.nbr:], [1.0 / b.z(1e8) for b in extra])
+
+
+def test_with_branches_filters_and_chains(derived):
+    z, board, extra, ost, odst = derived
+    st = host_stack(board)
+    assert st.with_branches([]) is st
+    off = gs.Branch((0, 0, 0), (0, 0, 0), lambda f: 1.0)                 # both ends on one node
+    outside = gs.Branch((0, 1, 1), (1, board.nx + 3, 1), lambda f: 1.0)  # an end off the grid
+    assert st.with_branches([off, outside]) is st
+    b = branches_of(extra)
+    d1 = st.with_branches(b[:1])
+    d2 = d1.with_branches(b[1:])
+    assert d2._base is st and d2.n_lowrank == len(extra)              # derived from the first base
+    x1 = np.arange(d1.nb + int(d1.keep.sum())).astype(complex)
+    y = d2.map_state(x1, d1)
+    assert len(y) == d2.nb + int(d2.keep.sum()) and not y[d1.nb: d2.nb].any()
+    assert d2.map_state(x1, st) is None                                # not st's vector length
+
+
+def test_with_branches_joining_copper_makes_a_stack():
+    """Two sheets with no plane pair and no branch are separate pieces: a via between them changes the
+    reference nodes, so the result is a stack of its own (peec.py:1880-1882)."""
+    b = synth.small_pair()
+    b.pairs, b.branches = [], []
+    st = host_stack(b)
+    via = gs.Branch((0, 20, 3), (1, 20, 3), lambda f: 1e-3 + 0j, "v", "via")
+    assert st.full_label[st.node_id((0, 20, 3))] != st.full_label[st.node_id((1, 20, 3))]
+    new = st.with_branches([via])
+    assert new is not st and new._base is None and new.nbr == 1
+    assert int(new.keep.sum()) == int(st.keep.sum()) + 1
+
+
+def test_route_on_derived_reuses_strip_coupling(derived):
+    z, board, extra, ost, odst = derived
+    st, routes = gs.from_board(board, _device=False)
+    dst = st.with_branches(branches_of(extra))
+    r = routes[0].on(dst)
+    assert r.strip_psi is routes[0].strip_psi
+    assert len(r.psi) == dst.nb and rel(r.psi, z["psi0"]) < 1e-12
