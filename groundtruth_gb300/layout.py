@@ -368,17 +368,24 @@ def symbolic(t: Topology, S_pattern: sp.csr_matrix, leaf: int = 48) -> Symbolic:
     erow = np.empty(len(s_row), np.int64)
     in_own = s_row < own_start[ef] + nown[ef]
     erow[in_own] = s_row[in_own] - own_start[ef[in_own]]
-    out = ~in_own
-    for f in np.unique(ef[out]):
-        sel = np.flatnonzero(out & (ef == f))
-        erow[sel] = nown[f] + np.searchsorted(bnd[f], s_row[sel])
+    # boundary rows: the entries below each front's own block, grouped by front (one sort, no per-front scan)
+    oi = np.flatnonzero(~in_own)
+    of = ef[oi]
+    so = np.argsort(of, kind="stable")
+    oi, of = oi[so], of[so]
+    cut = np.flatnonzero(np.diff(of)) + 1
+    for s0, s1 in zip(np.concatenate([[0], cut]), np.concatenate([cut, [len(oi)]])):
+        if s1 <= s0:
+            continue
+        f = of[s0]
+        sel = oi[s0:s1]
+        pos = np.searchsorted(bnd[f], s_row[sel])
+        if np.any(pos >= nbnd[f]) or not np.array_equal(bnd[f][pos], s_row[sel]):
+            raise AssertionError("symbolic: an entry of S is not on its front's boundary")
+        erow[sel] = nown[f] + pos
     nfe = (nown + nbnd)[ef]
     if len(erow) and (erow.min() < 0 or np.any(erow >= nfe) or np.any(erow < ecol)):
         raise AssertionError("symbolic: an entry of S falls outside its front")
-    for f in np.unique(ef[out]):
-        sel = np.flatnonzero(out & (ef == f))
-        if not np.array_equal(bnd[f][erow[sel] - nown[f]], s_row[sel]):
-            raise AssertionError("symbolic: an entry of S is not on its front's boundary")
     eo = np.argsort(ef, kind="stable")
     ent_ptr = np.searchsorted(ef[eo], np.arange(nfront + 1)).astype(np.int64)
     return Symbolic(n, perm, iperm, own_start, nown, nbnd, bnd_ptr, bnd_idx, parent, height, order.astype(np.int64),

@@ -439,6 +439,55 @@ def _labels(mask: np.ndarray, xb: np.ndarray, yb: np.ndarray) -> np.ndarray:
     return lab
 
 
+def what_if_base(n: int = 512, d_mm: float = 0.2, n_nets: int = 12, n_freq: int = 16, seed: int = 4,
+                 slot: bool = True, n_decap: int = 8) -> Board:
+    """The interactive what-if workload's base board: 4-layer Sig/GND/PWR/Sig at d_mm pitch, the GND/PWR pair
+    solved (sheet preconditioner), PWR split into two islands by a 1 mm gap across the board, a seeded 1 mm
+    GND slot across 60 % of the board (slot=False: the same board with the slot filled, the "toggle the slot"
+    edit), n_decap decoupling parts between GND and the PWR islands and n_nets random-walk nets on the top
+    signal layer returning in GND; n_freq log-spaced frequencies in [1 MHz, 1 GHz]."""
+    rng = np.random.default_rng(seed)
+    d = d_mm * 1e-3
+    t = 35e-6
+    side = (n - 1) * d
+    length = 0.6 * n * d
+    cx, cy = side * rng.uniform(0.4, 0.6), side * rng.uniform(0.4, 0.6)
+    ang = rng.uniform(0, math.pi)
+    cut = rect_polygon(cx, cy, length, 1e-3, ang)
+    gnd = _full_layer("GND", 0.0, t, n, n, d, [cut] if slot else [])
+    split_at = side * rng.uniform(0.35, 0.65)
+    gap = np.array([[split_at - 0.5e-3, -d], [split_at + 0.5e-3, -d], [split_at + 0.5e-3, side + d],
+                    [split_at - 0.5e-3, side + d]])
+    pwr = _full_layer("PWR", -(0.2e-3 + t), t, n, n, d, [gap])
+    pair = Pair(0, 1, EPS0 * 4.3 / 0.2e-3, 0.02)
+    branches = []
+    while len(branches) < n_decap:
+        i, j = int(rng.integers(4, n - 4)), int(rng.integers(4, n - 4))
+        if gnd.node[i, j] and pwr.node[i, j]:
+            branches.append(BranchSpec((0, i, j), (1, i, j), 0.02, 0.5e-9, 100e-9, "part"))
+    z_face, z_sig = 0.5 * t, 0.15e-3 + t
+    u = np.array([math.cos(ang), math.sin(ang)])
+    v = np.array([-u[1], u[0]])
+    margin = max(4, n // 32)
+    nets = []
+    for _ in range(n_nets):
+        for _ in range(1000):
+            s = np.array([cx, cy]) + rng.uniform(-0.35, 0.35) * length * u - rng.uniform(0.15, 0.4) * side * v
+            e = np.array([cx, cy]) + rng.uniform(-0.35, 0.35) * length * u + rng.uniform(0.15, 0.4) * side * v
+            m = np.array([cx, cy]) + rng.uniform(-0.3, 0.3) * length * u
+            cs, ce, cm = (np.round(p / d).astype(int) for p in (s, e, m))
+            ok = all(margin <= c[0] < n - margin and margin <= c[1] < n - margin for c in (cs, ce, cm))
+            if ok and gnd.node[cs[0], cs[1]] and gnd.node[ce[0], ce[1]]:
+                break
+        cells = _manhattan_walk(rng, cs, cm, ce, int(rng.integers(20, 61)), margin, n - 1 - margin, n - 1 - margin)
+        pts = [(c[0] * d, c[1] * d) for c in cells]
+        nets.append(Net(_segments(pts, z_sig, z_face, 0.15e-3), (0, int(cs[0]), int(cs[1])),
+                        (0, int(ce[0]), int(ce[1]))))
+    freqs = np.logspace(6, 9, n_freq)
+    return Board("what_if_base", d, n, n, [gnd, pwr], [pair], branches, nets, freqs, precond="sheet", tol=1e-5,
+                 restart=50)
+
+
 def what_if_branches(board: Board, seed: int, n_via: int = 2, n_part: int = 1) -> list:
     """A what-if edit's added branches (the serving workload's "add 1-4 vias" / "move a decoupling part"):
     n_via stitching vias and n_part decoupling parts (ESR 20 mohm, ESL 0.5 nH, 100 nF) between two sheets at
