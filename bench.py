@@ -60,6 +60,12 @@ def parse():
                     help="precondition every other frequency with its neighbour's factorisation (half the LDL^T)")
     ap.add_argument("--levels", action="store_true",
                     help="also time each elimination level of the triangular solves (key 'solve_levels')")
+    ap.add_argument("--workload", default="slotted_pair", choices=["slotted_pair", "what_if"],
+                    help="what_if: latency of interactive edits (added vias / decoupling parts) on a solved "
+                         "512 x 512 board, warm-started derived stacks (a line of its own, not the headline)")
+    ap.add_argument("--requests", type=int, default=24, help="what_if: timed edits")
+    ap.add_argument("--rate", type=float, default=200.0, help="what_if: Poisson arrival rate (edits/s) of the queue")
+    ap.add_argument("--max-cols", type=int, default=32, help="what_if: columns per device batch")
     return ap.parse_args()
 
 
@@ -371,9 +377,90 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+# ------------------------------------------------------------------------------------------ what-if edits
+def run_what_if(args):
+    """Interactive edits on a solved board: each request adds 1-4 stitching vias (70 %) or one decoupling
+    part and re-solves 1-8 nets at 1-16 of the base's frequencies on a derived stack (the base's
+    factorisations plus a low-rank update), warm-started from the base's solutions.  Requests run one after
+    another; their service times also drive a FIFO queue with Poisson arrivals at --rate."""
+    import torch
+    from groundtruth_gb300 import stack as gs, synth, whatif
+    rank = int(os.environ.get("RANK", 0))
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    rng = np.random.default_rng(2024 + rank)
+    t0 = time.perf_counter()
+    board = synth.what_if_base()
+    st, routes = gs.from_board(board)
+    setup_s = time.perf_counter() - t0
+    wi = whatif.WhatIf(st, routes, board.freqs, tol=board.tol, max_cols=args.max_cols, restart=args.restart,
+                       inner_tol=args.inner_tol, reorth=args.reorth, max_its=args.max_its)
+    base_s = wi.baseline()
+    n_base = len(routes) * len(board.freqs)
+    reqs = []
+    for r in range(args.warmup + args.requests):
+        vias = rng.random() < 0.7
+        extra = synth.what_if_branches(board, seed=1000 + r, n_via=int(rng.integers(1, 5)) if vias else 0,
+                                       n_part=0 if vias else 1)
+        nets = sorted(int(k) for k in rng.choice(len(routes), size=int(rng.integers(1, 9)), replace=False))
+        fq = sorted(int(q) for q in rng.choice(len(board.freqs), size=int(rng.integers(1, 17)), replace=False))
+        reqs.append(([gs.Branch(b.a, b.b, b.z, f"edit{r}_{n}", b.kind, b.radius) for n, b in enumerate(extra)],
+                     nets, [float(board.freqs[q]) for q in fq]))
+    from groundtruth_gb300 import native
+    lib = native.load()
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", 0)))
+    service, cols, its, parts, worst, l0 = [], [], [], [], 0.0, 0
+    for r, (br, nets, fq) in enumerate(reqs):
+        if r == args.warmup:
+            clocks.start()
+            l0 = lib.gt_launch_count()
+        res = wi.evaluate(br, nets, fq)
+        if r < args.warmup:
+            continue
+        service.append(res.seconds)
+        cols.append(len(res.solutions))
+        its += res.iterations
+        parts.append(res.parts)
+        worst = max(worst, max(s.residual for s in res.solutions.values()))
+    launches = int(lib.gt_launch_count() - l0)
+    ck = clocks.stop()
+    sv = np.array(service)
+    # FIFO single server, Poisson arrivals
+    arr = np.cumsum(np.random.default_rng(7).exponential(1.0 / args.rate, len(sv)))
+    fin, lat = 0.0, []
+    for a, s in zip(arr, sv):
+        fin = max(a, fin) + s
+        lat.append(fin - a)
+    ms = lambda x: round(float(x) * 1e3, 2)
+    line = {
+        "metric": "what-if edit latency (p50)", "value": ms(np.median(sv)), "unit": "ms", "n_gpus": 1,
+        "higher_is_better": False, "impl": "gb300", "dtype": "c64 inner / c128 outer", "data": "synthetic",
+        "config": {"workload": f"what_if_base {board.nx}x{board.ny} @{board.d * 1e3:g}mm GND slot + split PWR, "
+                               f"{len(routes)} nets x {len(board.freqs)} freqs; edits: 1-4 vias | 1 decap, "
+                               "1-8 nets x 1-16 freqs, warm-started", "tol": board.tol, "max_cols": args.max_cols},
+        "requests": len(sv), "warmup": args.warmup, "p50_ms": ms(np.median(sv)), "p99_ms": ms(np.quantile(sv, 0.99)),
+        "mean_ms": ms(sv.mean()), "max_ms": ms(sv.max()), "columns_per_request": float(np.mean(cols)),
+        "solves_per_s": round(float(sum(cols) / sv.sum()), 2),
+        "sustainable_edits_per_s": round(float(1.0 / sv.mean()), 3),
+        "queue": {"rate_per_s": args.rate, "stable": bool(args.rate * sv.mean() < 1.0),
+                  "p50_ms": ms(np.median(lat)), "p99_ms": ms(np.quantile(lat, 0.99))},
+        "iterations_mean": round(float(np.mean(its)), 1), "max_residual": worst,
+        "parts_median_s": {k: round(float(np.median([p[k] for p in parts])), 4) for k in parts[0]},
+        "setup": {"stack_and_routes_s": round(setup_s, 2), "baseline_s": round(base_s, 2),
+                  "baseline_solves_per_s": round(n_base / base_s, 2)},
+        "clocks": ck, "gpu_launches": launches,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.workload == "what_if":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the headline workload only"}))
+            return
+        run_what_if(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

@@ -480,12 +480,16 @@ static void precond(gt_geometry* G, gt_operators* ops, const cx<R>* r, int64_t l
     }
 }
 
+// the solve kernels hold a front's rows for 8 columns plus up to 16 warps' partial sums in shared memory
+static bool solve_fits(const gt_geometry* G, size_t elem) {
+    return (size_t)(G->max_nf + 16 * 32) * 8 * elem <= 220 * 1024;
+}
+
 static int group_max(const gt_geometry* G, size_t elem) {
-    // the solve kernels hold a front's rows for 8 columns plus up to 16 warps' partial sums in shared memory
-    if ((size_t)(G->max_nf + 16 * 32) * 8 * elem > 220 * 1024)
-        throw Invalid("a front is too large for the triangular-solve kernels' shared memory");
+    if (!solve_fits(G, elem)) throw Invalid("a front is too large for the triangular-solve kernels' shared memory");
     return 8;
 }
+
 
 // the listed slots (sorted by operator) -> groups of <= gmax slots sharing one operator:
 // group g holds gslot[gptr[g] .. gptr[g+1])
@@ -502,6 +506,52 @@ static void make_groups(const std::vector<int>& slots, const std::vector<int>& s
         gptr.push_back((int)gslot.size());
         op.push_back(slot_op[slots[s]]);
         s = e;
+    }
+}
+
+// W = S^-1 U for a derived operator set: the base's sweeps (precision R) on U e_j, column c = f k + j of
+// the nf factorisations' k added branches, in batches; w: [nf k][nnode] node order
+template <typename R>
+static void lowrank_w(gt_geometry* G, const gt_operators* base, int nf, int k, const int* ends, cx<R>* w,
+                      cudaStream_t st) {
+    const int64_t nnode = G->F.nnode, nfac = G->F.nfac, ntot = (int64_t)nf * k;
+    const int gmax = group_max(G, sizeof(cx<R>));
+    const int bc = (int)std::min<int64_t>(ntot, 64);
+    Pool tmp;
+    cx<R>* sv = tmp.alloc<cx<R>>((size_t)bc * nfac);
+    cx<R>* zv = tmp.alloc<cx<R>>((size_t)bc * nfac);
+    cx<R>* uv = tmp.alloc<cx<R>>((size_t)bc * std::max<int64_t>(G->F.vec_total, 1));
+    int* d_gptr = tmp.alloc<int>(bc + 1);
+    int* d_gslot = tmp.alloc<int>(bc);
+    int* d_gop = tmp.alloc<int>(bc);
+    const int nlev = (int)G->level_ptr.size() - 1;
+    for (int64_t c0 = 0; c0 < ntot; c0 += bc) {
+        const int nc = (int)std::min<int64_t>(bc, ntot - c0);
+        cx<R>* wout = w + c0 * nnode;
+        GT_CUDA(cudaMemsetAsync(sv, 0, (size_t)nc * nfac * sizeof(cx<R>), st));
+        GT_CUDA(cudaMemsetAsync(wout, 0, (size_t)nc * nnode * sizeof(cx<R>), st));
+        launch_lowrank_rhs<R>(sv, nfac, (int)c0, nc, k, ends, G->geo.perm, st);
+        std::vector<int> slots(nc), sfact(nc), gptr, gslot, gop;
+        for (int q = 0; q < nc; ++q) {
+            slots[q] = q;
+            sfact[q] = (int)((c0 + q) / k);
+        }
+        make_groups(slots, sfact, gmax, gptr, gslot, gop);
+        GT_CUDA(cudaMemcpy(d_gptr, gptr.data(), gptr.size() * sizeof(int), cudaMemcpyHostToDevice));
+        GT_CUDA(cudaMemcpy(d_gslot, gslot.data(), gslot.size() * sizeof(int), cudaMemcpyHostToDevice));
+        GT_CUDA(cudaMemcpy(d_gop, gop.data(), gop.size() * sizeof(int), cudaMemcpyHostToDevice));
+        const Groups grp{(int)gop.size(), d_gptr, d_gslot, d_gop};
+        for (int h = 0; h < nlev; ++h) {
+            const int nfl = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);
+            launch_fwd_level<R>(G->F, G->d_order + G->level_ptr[h], nfl, G->level_maxnf[h], G->level_maxnown[h],
+                                panel_of<R>(base), dinv_of<R>(base), sv, zv, uv, sv, grp, gmax, st);
+        }
+        for (int h = nlev - 1; h >= 0; --h) {
+            const int nfl = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);
+            launch_bwd_level<R>(G->F, G->d_order + G->level_ptr[h], nfl, G->level_maxnf[h], G->level_maxnown[h],
+                                panel_rm_of<R>(base), zv, sv, wout, grp, gmax, st);
+        }
+        GT_CUDA(cudaStreamSynchronize(st));   // the group tables are reused by the next batch
     }
 }
 
@@ -1255,51 +1305,23 @@ int gt_operators_derive(gt_geometry* G, const gt_operators* base, int32_t n_ops,
     O->nlow = k;
     const std::vector<int> ends(G->h_branch_nodes.begin() + 2 * bg.nbr, G->h_branch_nodes.end());
     O->low_ends = p.upload(ends.data(), ends.size());
-    const int64_t nnode = G->F.nnode, nfac = G->F.nfac, ntot = (int64_t)nf * k;
+    const int64_t nnode = G->F.nnode, ntot = (int64_t)nf * k;
     O->low_w64 = p.alloc<c64>((size_t)ntot * nnode);
     O->low_w32 = p.alloc<c32>((size_t)ntot * nnode);
     cudaStream_t st = 0;
     Profiler* P = &G->prof;
     {
-        // W = S^-1 U: the base's FP64 sweeps on U e_j, column c = f k + j, in batches
+        // W = S^-1 U by the base's FP64 sweeps; where the largest front is too large for the FP64 solve kernels
+        // (which then serve no FP64 solve of this geometry either), by the FP32 sweeps the mixed-precision
+        // solves use
         Scope sc(P, "lowrank_make", st);
-        const int gmax = group_max(G, sizeof(c64));
-        const int bc = (int)std::min<int64_t>(ntot, 64);
         Pool tmp;
-        c64* sv = tmp.alloc<c64>((size_t)bc * nfac);
-        c64* zv = tmp.alloc<c64>((size_t)bc * nfac);
-        c64* uv = tmp.alloc<c64>((size_t)bc * std::max<int64_t>(G->F.vec_total, 1));
-        int* d_gptr = tmp.alloc<int>(bc + 1);
-        int* d_gslot = tmp.alloc<int>(bc);
-        int* d_gop = tmp.alloc<int>(bc);
-        const int nlev = (int)G->level_ptr.size() - 1;
-        for (int64_t c0 = 0; c0 < ntot; c0 += bc) {
-            const int nc = (int)std::min<int64_t>(bc, ntot - c0);
-            c64* wout = O->low_w64 + c0 * nnode;
-            GT_CUDA(cudaMemsetAsync(sv, 0, (size_t)nc * nfac * sizeof(c64), st));
-            GT_CUDA(cudaMemsetAsync(wout, 0, (size_t)nc * nnode * sizeof(c64), st));
-            launch_lowrank_rhs(sv, nfac, (int)c0, nc, k, O->low_ends, g.perm, st);
-            std::vector<int> slots(nc), sfact(nc), gptr, gslot, gop;
-            for (int q = 0; q < nc; ++q) {
-                slots[q] = q;
-                sfact[q] = (int)((c0 + q) / k);
-            }
-            make_groups(slots, sfact, gmax, gptr, gslot, gop);
-            GT_CUDA(cudaMemcpy(d_gptr, gptr.data(), gptr.size() * sizeof(int), cudaMemcpyHostToDevice));
-            GT_CUDA(cudaMemcpy(d_gslot, gslot.data(), gslot.size() * sizeof(int), cudaMemcpyHostToDevice));
-            GT_CUDA(cudaMemcpy(d_gop, gop.data(), gop.size() * sizeof(int), cudaMemcpyHostToDevice));
-            const Groups grp{(int)gop.size(), d_gptr, d_gslot, d_gop};
-            for (int h = 0; h < nlev; ++h) {
-                const int nfl = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);
-                launch_fwd_level<double>(G->F, G->d_order + G->level_ptr[h], nfl, G->level_maxnf[h],
-                                         G->level_maxnown[h], base->panel64, base->dinv64, sv, zv, uv, sv, grp, gmax, st);
-            }
-            for (int h = nlev - 1; h >= 0; --h) {
-                const int nfl = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);
-                launch_bwd_level<double>(G->F, G->d_order + G->level_ptr[h], nfl, G->level_maxnf[h],
-                                         G->level_maxnown[h], base->panel64_rm, zv, sv, wout, grp, gmax, st);
-            }
-            GT_CUDA(cudaStreamSynchronize(st));   // the group tables are reused by the next batch
+        if (solve_fits(G, sizeof(c64))) {
+            lowrank_w<double>(G, base, nf, k, O->low_ends, O->low_w64, st);
+            launch_lowrank_to32(O->low_w64, O->low_w32, ntot * nnode, st);
+        } else {
+            lowrank_w<float>(G, base, nf, k, O->low_ends, O->low_w32, st);
+            launch_lowrank_to64(O->low_w32, O->low_w64, ntot * nnode, st);
         }
         // U^T W to the host; Minv = (diag(z) + U^T W)^-1 per factorisation at its frequency
         c64* gbuf = tmp.alloc<c64>((size_t)ntot * k);
@@ -1356,7 +1378,6 @@ int gt_operators_derive(gt_geometry* G, const gt_operators* base, int32_t n_ops,
         }
         O->low_m64 = p.upload(m64.data(), m64.size());
         O->low_m32 = p.upload(m32.data(), m32.size());
-        launch_lowrank_to32(O->low_w64, O->low_w32, ntot * nnode, st);
         GT_CUDA(cudaStreamSynchronize(st));
     }
     P->flush();

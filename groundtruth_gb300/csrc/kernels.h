@@ -145,11 +145,13 @@ template <typename R>
 void launch_lowrank(cx<R>* sd, int64_t nnode, int ncol, int k, const int* ends, const cx<R>* w, const cx<R>* minv,
                     const int* col_fact, const int* col_list, cx<R>* cbuf, int64_t ldc, cudaStream_t st);
 // U e_j in factor order for the columns c0 .. c0+ncol of (factorisation, branch) pairs (j = c mod k)
-void launch_lowrank_rhs(c64* s, int64_t nfac, int c0, int ncol, int k, const int* ends, const int64_t* perm,
+template <typename R>
+void launch_lowrank_rhs(cx<R>* s, int64_t nfac, int c0, int ncol, int k, const int* ends, const int64_t* perm,
                         cudaStream_t st);
 // U^T W entries g[c][i] of ncol node-ordered columns
 void launch_lowrank_gather(const c64* w, int64_t nnode, int ncol, int k, const int* ends, c64* g, cudaStream_t st);
 void launch_lowrank_to32(const c64* a, c32* b, int64_t n, cudaStream_t st);
+void launch_lowrank_to64(const c32* a, c64* b, int64_t n, cudaStream_t st);
 
 // --- Krylov vector work (batched, one basis per slot)
 // A basis entry stored in FP16 (real and imaginary halves), scaled by the basis scale so that the entries

@@ -69,15 +69,16 @@ void launch_lowrank(cx<R>* sd, int64_t nnode, int ncol, int k, const int* ends, 
 // right-hand sides U e_j in factor order: column c = f * k + j (of the batch starting at c0) gets +1 at the
 // factor index of branch j's end a and -1 at that of end b (ends that are not kept get nothing); s is zero
 // on entry
-__global__ void lowrank_rhs_kernel(c64* __restrict__ s, int64_t nfac, int c0, int ncol, int k,
+template <typename R>
+__global__ void lowrank_rhs_kernel(cx<R>* __restrict__ s, int64_t nfac, int c0, int ncol, int k,
                                    const int* __restrict__ ends, const int64_t* __restrict__ perm) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= ncol) return;
     const int j = (c0 + q) % k;
     const int64_t fa = perm[ends[2 * j]], fb = perm[ends[2 * j + 1]];
-    c64* sc = s + (int64_t)q * nfac;
-    if (fa >= 0) sc[fa] += mk<double>(1.0, 0.0);
-    if (fb >= 0) sc[fb] -= mk<double>(1.0, 0.0);
+    cx<R>* sc = s + (int64_t)q * nfac;
+    if (fa >= 0) sc[fa] = mk<R>(R(1), R(0));
+    if (fb >= 0) sc[fb] = mk<R>(R(-1), R(0));
 }
 
 // U^T W: g[c][i] = W_c[a_i] - W_c[b_i] for the ncol columns of w (node order) of one batch
@@ -90,16 +91,20 @@ __global__ void lowrank_gather_kernel(const c64* __restrict__ w, int64_t nnode, 
     g[q] = wc[ends[2 * i]] - wc[ends[2 * i + 1]];
 }
 
-__global__ void lowrank_to32_kernel(const c64* __restrict__ a, c32* __restrict__ b, int64_t n) {
+template <typename D, typename S>
+__global__ void lowrank_convert_kernel(const cx<S>* __restrict__ a, cx<D>* __restrict__ b, int64_t n) {
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
-        b[q] = cvt<float>(a[q]);
+        b[q] = cvt<D>(a[q]);
 }
 
-void launch_lowrank_rhs(c64* s, int64_t nfac, int c0, int ncol, int k, const int* ends, const int64_t* perm,
+template <typename R>
+void launch_lowrank_rhs(cx<R>* s, int64_t nfac, int c0, int ncol, int k, const int* ends, const int64_t* perm,
                         cudaStream_t st) {
-    lowrank_rhs_kernel<<<(ncol + 127) / 128, 128, 0, st>>>(s, nfac, c0, ncol, k, ends, perm);
+    lowrank_rhs_kernel<R><<<(ncol + 127) / 128, 128, 0, st>>>(s, nfac, c0, ncol, k, ends, perm);
     GT_LAUNCH_CHECK();
 }
+template void launch_lowrank_rhs<float>(c32*, int64_t, int, int, int, const int*, const int64_t*, cudaStream_t);
+template void launch_lowrank_rhs<double>(c64*, int64_t, int, int, int, const int*, const int64_t*, cudaStream_t);
 
 void launch_lowrank_gather(const c64* w, int64_t nnode, int ncol, int k, const int* ends, c64* g, cudaStream_t st) {
     lowrank_gather_kernel<<<(ncol * k + 127) / 128, 128, 0, st>>>(w, nnode, ncol, k, ends, g);
@@ -107,7 +112,12 @@ void launch_lowrank_gather(const c64* w, int64_t nnode, int ncol, int k, const i
 }
 
 void launch_lowrank_to32(const c64* a, c32* b, int64_t n, cudaStream_t st) {
-    lowrank_to32_kernel<<<(int)std::min<int64_t>((n + 255) / 256, 1216), 256, 0, st>>>(a, b, n);
+    lowrank_convert_kernel<float, double><<<(int)std::min<int64_t>((n + 255) / 256, 1216), 256, 0, st>>>(a, b, n);
+    GT_LAUNCH_CHECK();
+}
+
+void launch_lowrank_to64(const c32* a, c64* b, int64_t n, cudaStream_t st) {
+    lowrank_convert_kernel<double, float><<<(int)std::min<int64_t>((n + 255) / 256, 1216), 256, 0, st>>>(a, b, n);
     GT_LAUNCH_CHECK();
 }
 

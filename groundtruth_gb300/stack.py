@@ -543,21 +543,29 @@ class PlaneStack:
 
     def _warm_start(self, ops, rhs: np.ndarray, guesses) -> Optional[np.ndarray]:
         """Starting points from guess vectors (peec.py:2570-2578): per column x0 = G c with c minimising
-        ||K G c - b|| (one FP64 device product per guess vector), kept where it lowers the residual below 0.9 of
-        ||b||; None when no column has one."""
+        ||K G c - b|| (the FP64 device products of every column's guess vectors in one batch), kept where it
+        lowers the residual below 0.9 of ||b||; None when no column has one."""
         from . import native
+        vecs, owner, idx = [], [], []
+        for c, guess in enumerate(guesses):
+            for g in (guess or []):
+                if g is not None and len(g) == rhs.shape[1] and np.any(g):
+                    vecs.append(np.asarray(g, complex))
+                    owner.append(c)
+                    idx.append(ops[c][1])
+        if not vecs:
+            return None
+        obj = ops[0][0]
+        KG_all = native.apply(self.handle, obj, "matvec", np.stack(vecs), np.array(idx, np.int32), "fp64")
+        owner = np.array(owner)
         x0 = np.zeros_like(rhs)
         used = False
-        for c, guess in enumerate(guesses):
-            G = [np.asarray(g, complex) for g in (guess or []) if g is not None and len(g) == rhs.shape[1]
-                 and np.any(g)]
-            if not G:
-                continue
-            obj, k = ops[c]
-            KG = native.apply(self.handle, obj, "matvec", np.stack(G), k, "fp64").T
+        for c in np.unique(owner):
+            sel = np.flatnonzero(owner == c)
+            KG = KG_all[sel].T
             coef, *_ = np.linalg.lstsq(KG, rhs[c], rcond=None)
             if np.linalg.norm(rhs[c] - KG @ coef) < 0.9 * np.linalg.norm(rhs[c]):
-                x0[c] = np.stack(G, axis=1) @ coef
+                x0[c] = np.stack([vecs[q] for q in sel], axis=1) @ coef
                 used = True
         return x0 if used else None
 
