@@ -444,7 +444,8 @@ def run_what_if(args):
         "queue": {"rate_per_s": args.rate, "stable": bool(args.rate * sv.mean() < 1.0),
                   "p50_ms": ms(np.median(lat)), "p99_ms": ms(np.quantile(lat, 0.99))},
         "iterations_mean": round(float(np.mean(its)), 1), "max_residual": worst,
-        "parts_median_s": {k: round(float(np.median([p[k] for p in parts])), 4) for k in parts[0]},
+        "cold_redo_columns": int(sum(p["cold_redo"] for p in parts)),
+        "parts_median_s": {k: round(float(np.median([p[k] for p in parts])), 4) for k in parts[0] if k != "cold_redo"},
         "setup": {"stack_and_routes_s": round(setup_s, 2), "baseline_s": round(base_s, 2),
                   "baseline_solves_per_s": round(n_base / base_s, 2)},
         "clocks": ck, "gpu_launches": launches,

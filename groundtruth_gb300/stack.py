@@ -522,8 +522,10 @@ class PlaneStack:
 
     def solve_batch(self, freqs, rhs_tops, Js, tol: float = 1e-5, max_cycles: int = 8, guesses=None,
                     restart: int = 50, max_its: int = 2000, inner_tol: float = 1e-5, precision: str = "mixed",
-                    reorth: float = 0.7, borrow: bool = False):
-        """Many columns (frequency, right-hand side) in one device run: returns [(Ib, V, its, x)]."""
+                    reorth: float = 0.7, borrow: bool = False, failed: Optional[list] = None):
+        """Many columns (frequency, right-hand side) in one device run: returns [(Ib, V, its, x, residual)].
+        A column that misses tol raises SolverError, or, when a list is passed as `failed`, has its index
+        appended there (its entry holds the best solution found)."""
         from . import native
         ncol = len(freqs)
         ops = self.factorise(freqs, together=True, borrow=borrow)
@@ -534,8 +536,10 @@ class PlaneStack:
         out = []
         for c in range(ncol):
             if not ok[c]:
-                raise SolverError(f"GMRES did not converge at {freqs[c]:.4g} Hz ({its[c]} iterations, "
-                                  f"residual {res[c]:.3g})")
+                if failed is None:
+                    raise SolverError(f"GMRES did not converge at {freqs[c]:.4g} Hz ({its[c]} iterations, "
+                                      f"residual {res[c]:.3g})")
+                failed.append(c)
             V = np.zeros(self.n_nodes, complex)
             V[self.keep] = x[c, self.nb:]
             out.append((x[c, : self.nb], V, int(its[c]), x[c], float(res[c])))

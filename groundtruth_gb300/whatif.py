@@ -4,7 +4,15 @@ and 452-465, on PlaneStack.with_branches, peec.py:1871-1923).
 The base board is solved once per net and frequency.  Each edit (added stitching vias, an added decoupling part)
 becomes a derived stack that reuses the base's factorisations through a low-rank (Woodbury) update, and its
 solves start from the base's solutions mapped onto the derived stack's unknowns (the new branches at zero
-current), all columns of an edit in as few device batches as the device memory budget allows."""
+current), all columns of an edit in as few device batches as the device memory budget allows.
+
+The inner iterations run in FP32.  An edit that shorts a weakly coupled piece of copper (a via from a plane
+island to ground at low frequency) removes, through the low-rank update, a potential mode that the base's
+FP32 solve carries at up to 10^6 times the size of what remains; the remainder then drowns in FP32 rounding
+when the Krylov space starts from the warm start's residual (concentrated on the new branches), and such a
+solve stagnates.  Warm-started columns therefore run under an iteration budget (a multiple of the base
+solve's count), and the columns that miss it are solved again from zero, which converges like a fresh
+factorisation of the edited board."""
 from __future__ import annotations
 
 import time
@@ -28,32 +36,46 @@ class WhatIf:
     frequencies the base is solved at (edits pick from them, so the base's factorisations serve every edit)."""
 
     def __init__(self, stack: gs.PlaneStack, routes: list, freqs, tol: float = 1e-5, max_cols: int = 32,
-                 **solve_kw):
+                 warm_budget: float = 2.0, **solve_kw):
         self.stack = stack
         self.routes = list(routes)
         self.freqs = [float(f) for f in freqs]
         self.tol = tol
         self.max_cols = max_cols
+        self.warm_budget = warm_budget
         self.kw = solve_kw
         self.base: dict = {}
 
-    def _solve(self, stack, routes: dict, cols: list, guesses=None) -> list:
-        """Columns [(net, f)] on `stack` in batches of max_cols; returns their Solutions in order."""
-        out = []
+    def _solve(self, stack, routes: dict, cols: list, guesses=None, budget=None) -> tuple:
+        """Columns [(net, f)] on `stack` in batches of max_cols; returns (their Solutions in order, the
+        indices of the warm-started columns that missed their budget and were solved again from zero)."""
+        out, redo = [], []
         for c0 in range(0, len(cols), self.max_cols):
             part = cols[c0: c0 + self.max_cols]
-            g = None if guesses is None else guesses[c0: c0 + self.max_cols]
+            kw = dict(self.kw)
+            failed = None
+            if guesses is not None and budget is not None:
+                kw["max_its"] = int(max(budget[c] for c in part))
+                failed = []
+            g = None if guesses is None else [guesses[c0 + q] for q in range(len(part))]
             res = stack.solve_batch([f for _, f in part], [routes[k].rhs_top(f) for k, f in part],
-                                    [routes[k].J() for k, _ in part], tol=self.tol, guesses=g, **self.kw)
+                                    [routes[k].J() for k, _ in part], tol=self.tol, guesses=g, failed=failed, **kw)
+            if failed:
+                again = stack.solve_batch([part[q][1] for q in failed], [routes[part[q][0]].rhs_top(part[q][1])
+                                                                         for q in failed],
+                                          [routes[part[q][0]].J() for q in failed], tol=self.tol, **self.kw)
+                for q, r in zip(failed, again):
+                    res[q] = (r[0], r[1], r[2] + res[q][2], r[3], r[4])
+                redo += [c0 + q for q in failed]
             out += [routes[k].solution(f, Ib, V, its, r) for (k, f), (Ib, V, its, x, r) in zip(part, res)]
-        return out
+        return out, redo
 
     def baseline(self) -> float:
         """Solve every net at every frequency on the base stack; returns the seconds it took."""
         t0 = time.perf_counter()
         self.stack.factorise(self.freqs, together=True)
         cols = [(k, f) for k in range(len(self.routes)) for f in self.freqs]
-        sols = self._solve(self.stack, dict(enumerate(self.routes)), cols)
+        sols, _ = self._solve(self.stack, dict(enumerate(self.routes)), cols)
         self.base = dict(zip(cols, sols))
         return time.perf_counter() - t0
 
@@ -70,7 +92,9 @@ class WhatIf:
         guesses = [[dst.map_state(self.base[c].state_for(self.stack), self.stack)] for c in cols]
         dst.factorise([f for _, f in cols], together=True)
         t2 = time.perf_counter()
-        sols = self._solve(dst, droutes, cols, guesses)
+        budget = {c: self.warm_budget * self.base[c].iterations + self.kw.get("restart", 50) for c in cols}
+        sols, redo = self._solve(dst, droutes, cols, guesses, budget)
         t3 = time.perf_counter()
         return EditResult(dict(zip(cols, sols)), t3 - t0, [s.iterations for s in sols],
-                          {"derive_stack_s": t1 - t0, "operators_s": t2 - t1, "solve_s": t3 - t2})
+                          {"derive_stack_s": t1 - t0, "operators_s": t2 - t1, "solve_s": t3 - t2,
+                           "cold_redo": len(redo)})

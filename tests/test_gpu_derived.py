@@ -89,3 +89,19 @@ def test_derived_of_derived_matches_whole_stack_oracle(case):
     sol = routes[1].on(d2).solve(f, tol=board.tol)
     ref = oroute.solve(f, tol=board.tol)
     assert abs(sol.Z_loop - ref["Z_loop"]) <= 1e-8 * abs(ref["Z_loop"])
+
+
+def test_what_if_service(case):
+    """The what-if service (whatif.WhatIf): a solved base, one edit on two nets at two frequencies, warm
+    started from the base's solutions; the same answers as the reference's derived stack."""
+    from groundtruth_gb300 import whatif
+    z, board, extra, st, routes, dst = case
+    wi = whatif.WhatIf(st, routes, board.freqs, tol=board.tol)
+    wi.baseline()
+    res = wi.evaluate(branches_of(extra), [0, 1], [float(board.freqs[1]), float(board.freqs[2])])
+    for (k, f), sol in res.solutions.items():
+        q = [float(v) for v in board.freqs].index(f)
+        ref = z[f"Z{k}_{q}"]
+        assert abs(sol.Z_loop - ref) <= 1e-8 * abs(ref), (k, q)
+        assert sol.residual <= board.tol
+    assert res.parts["cold_redo"] == 0
