@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--requests", type=int, default=24, help="what_if: timed edits")
     ap.add_argument("--rate", type=float, default=200.0, help="what_if: Poisson arrival rate (edits/s) of the queue")
     ap.add_argument("--max-cols", type=int, default=32, help="what_if: columns per device batch")
+    ap.add_argument("--what-if-method", default="bordered", choices=["bordered", "derived"],
+                    help="what_if: compose from base solves (bordered) or solve every column on the derived stack")
     return ap.parse_args()
 
 
@@ -380,9 +382,9 @@ def run_gpu(args):
 # ------------------------------------------------------------------------------------------ what-if edits
 def run_what_if(args):
     """Interactive edits on a solved board: each request adds 1-4 stitching vias (70 %) or one decoupling
-    part and re-solves 1-8 nets at 1-16 of the base's frequencies on a derived stack (the base's
-    factorisations plus a low-rank update), warm-started from the base's solutions.  Requests run one after
-    another; their service times also drive a FIFO queue with Poisson arrivals at --rate."""
+    part and answers 1-8 nets at 1-16 of the base's frequencies (whatif.WhatIf: composed from base solves of
+    the new branches' injections, or solved on the derived stack).  Requests run one after another; their
+    service times also drive a FIFO queue with Poisson arrivals at --rate."""
     import torch
     from groundtruth_gb300 import stack as gs, synth, whatif
     rank = int(os.environ.get("RANK", 0))
@@ -392,7 +394,8 @@ def run_what_if(args):
     board = synth.what_if_base()
     st, routes = gs.from_board(board)
     setup_s = time.perf_counter() - t0
-    wi = whatif.WhatIf(st, routes, board.freqs, tol=board.tol, max_cols=args.max_cols, restart=args.restart,
+    wi = whatif.WhatIf(st, routes, board.freqs, tol=board.tol, max_cols=args.max_cols, method=args.what_if_method,
+                       restart=args.restart,
                        inner_tol=args.inner_tol, reorth=args.reorth, max_its=args.max_its)
     base_s = wi.baseline()
     n_base = len(routes) * len(board.freqs)
@@ -436,7 +439,7 @@ def run_what_if(args):
         "higher_is_better": False, "impl": "gb300", "dtype": "c64 inner / c128 outer", "data": "synthetic",
         "config": {"workload": f"what_if_base {board.nx}x{board.ny} @{board.d * 1e3:g}mm GND slot + split PWR, "
                                f"{len(routes)} nets x {len(board.freqs)} freqs; edits: 1-4 vias | 1 decap, "
-                               "1-8 nets x 1-16 freqs, warm-started", "tol": board.tol, "max_cols": args.max_cols},
+                               "1-8 nets x 1-16 freqs", "tol": board.tol, "max_cols": args.max_cols},
         "requests": len(sv), "warmup": args.warmup, "p50_ms": ms(np.median(sv)), "p99_ms": ms(np.quantile(sv, 0.99)),
         "mean_ms": ms(sv.mean()), "max_ms": ms(sv.max()), "columns_per_request": float(np.mean(cols)),
         "solves_per_s": round(float(sum(cols) / sv.sum()), 2),
@@ -444,8 +447,10 @@ def run_what_if(args):
         "queue": {"rate_per_s": args.rate, "stable": bool(args.rate * sv.mean() < 1.0),
                   "p50_ms": ms(np.median(lat)), "p99_ms": ms(np.quantile(lat, 0.99))},
         "iterations_mean": round(float(np.mean(its)), 1), "max_residual": worst,
+        "method": args.what_if_method,
         "cold_redo_columns": int(sum(p["cold_redo"] for p in parts)),
-        "parts_median_s": {k: round(float(np.median([p[k] for p in parts])), 4) for k in parts[0] if k != "cold_redo"},
+        "border_columns": int(sum(p.get("border_columns", 0) for p in parts)),
+        "parts_median_s": {k: round(float(np.median([p[k] for p in parts])), 4) for k in parts[0] if k.endswith("_s")},
         "setup": {"stack_and_routes_s": round(setup_s, 2), "baseline_s": round(base_s, 2),
                   "baseline_solves_per_s": round(n_base / base_s, 2)},
         "clocks": ck, "gpu_launches": launches,

@@ -368,13 +368,14 @@ class PlaneStack:
             return -1
         return int(self.nid[k, i, j])
 
-    def with_branches(self, extra: list) -> "PlaneStack":
+    def with_branches(self, extra: list, device: Optional[bool] = None) -> "PlaneStack":
         """This stack plus a few branches (candidate vias, parts), peec.py:1871-1912.  Shares the grids, the
         kernel spectra and the Schur structure; its solves reuse this stack's factorisations through a low-rank
         (Woodbury) update of the Schur complement (gt_operators_derive).  Branches with an end off copper or
         both ends on one node are dropped; none left: this stack.  A branch that joins two pieces of copper
         changes the reference nodes: a stack of its own.  A derived stack of a derived stack derives from the
-        first base with all the added branches (the same system and preconditioner)."""
+        first base with all the added branches (the same system and preconditioner).  device=False: the host
+        side only (numbering, couplings, outputs), without a device geometry."""
         extra = [b for b in extra if self.node_id(b.a) >= 0 and self.node_id(b.b) >= 0
                  and tuple(b.a) != tuple(b.b)]
         if not extra:
@@ -385,7 +386,7 @@ class PlaneStack:
         root = self._base if self._base is not None else self
         if np.any(self.full_label[a] != self.full_label[b]) or len(branches) - root.nbr > LOWRANK_MAX:
             return PlaneStack(self.layers, branches, self.pairs, self.sigma, self.precond_mode, self.screen,
-                              leaf=self.leaf, _device=self._device)
+                              leaf=self.leaf, _device=self._device if device is None else bool(device))
         t, kept = layout.topology([l.grid.node for l in root.layers], [l.grid.xb for l in root.layers],
                                   [l.grid.yb for l in root.layers], root.d,
                                   [(p.upper, p.lower, p.c_per_area, p.tan_delta) for p in root.pairs],
@@ -405,7 +406,8 @@ class PlaneStack:
         new._base = root
         new._lock = threading.Lock()
         new._ops = OrderedDict()
-        new.handle = native_geometry(new) if root._device else None
+        new._device = root._device if device is None else bool(device) and root._device
+        new.handle = native_geometry(new) if new._device else None
         return new
 
     def map_state(self, x: Optional[np.ndarray], stack: "PlaneStack") -> Optional[np.ndarray]:
@@ -582,11 +584,13 @@ class PlaneStack:
         px, py = greens.strip_coupling(segments, [self.xa, self.ya], self.d, self.zs, self.ts)
         return np.concatenate([px, py])
 
-    def branch_coupling(self, segments: np.ndarray, start: int = 0) -> np.ndarray:
-        """psi of the branches from `start` on: a via's barrel couples to the trace's vertical segments."""
+    def branch_coupling(self, segments: np.ndarray, start: int = 0, branches: Optional[list] = None) -> np.ndarray:
+        """psi of the branches from `start` on (or of `branches`): a via's barrel couples to the trace's
+        vertical segments."""
         vert = [s for s in segments if abs(s[5] - s[2]) > 0 and np.linalg.norm(s[3:5] - s[0:2]) < 1e-12]
-        out = np.zeros(self.nbr - start)
-        for n, b in enumerate(self.branches[start:]):
+        brs = self.branches[start:] if branches is None else list(branches)
+        out = np.zeros(len(brs))
+        for n, b in enumerate(brs):
             if b.kind == "via" and vert:
                 pa, pb = self.pos(b.a), self.pos(b.b)
                 out[n] = sum(s[7] * greens.segment_mutual(s[0:3], s[3:6], pa, pb, b.radius) for s in vert)

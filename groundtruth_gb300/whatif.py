@@ -1,18 +1,27 @@
 """Interactive what-if edits on a solved board (GroundTruth: the fix search's candidate solves, suggest.py:318-325
 and 452-465, on PlaneStack.with_branches, peec.py:1871-1923).
 
-The base board is solved once per net and frequency.  Each edit (added stitching vias, an added decoupling part)
-becomes a derived stack that reuses the base's factorisations through a low-rank (Woodbury) update, and its
-solves start from the base's solutions mapped onto the derived stack's unknowns (the new branches at zero
-current), all columns of an edit in as few device batches as the device memory budget allows.
+The base board is solved once per net and frequency.  An edit adds k branches (stitching vias, a decoupling
+part) without joining separate pieces of copper.  Two ways to answer it:
 
-The inner iterations run in FP32.  An edit that shorts a weakly coupled piece of copper (a via from a plane
-island to ground at low frequency) removes, through the low-rank update, a potential mode that the base's
-FP32 solve carries at up to 10^6 times the size of what remains; the remainder then drowns in FP32 rounding
-when the Krylov space starts from the warm start's residual (concentrated on the new branches), and such a
-solve stagnates.  Warm-started columns therefore run under an iteration budget (a multiple of the base
-solve's count), and the columns that miss it are solved again from zero, which converges like a fresh
-factorisation of the edited board."""
+* "bordered" (default): the edited system is the base system bordered by the k new branch currents,
+      [K  F] [x]   [b    ]      F = the new branches' injections into the KCL rows,
+      [G  Z] [i] = [b_new],     G x = -(V_a - V_b) across each new branch, Z = diag(z_new),
+  so x = x_base - X_F i with X_F = K^-1 F (k solves of the base system per frequency, shared by every net)
+  and i = (Z - G X_F)^-1 (b_new - G x_base), a k x k system per column.  Every device solve is a base solve
+  with the base's own preconditioner; an edit costs k columns per frequency instead of one per net and
+  frequency.  The edited residual is r' = r_base - r_F i on the base rows and zero on the new ones, so
+  ||r'|| <= ||r_base|| + sum |i_j| ||r_F,j||, a bound known on the host; the base is solved to half the
+  tolerance and X_F to border_tol times it, and a column whose bound still misses the tolerance is solved on
+  the derived stack from the composed solution.
+* "derived": the derived stack (the base's factorisations plus a low-rank update of the Schur complement)
+  solves every column, warm-started from the base's solution (the reference's way).  Its inner iterations
+  run in FP32: an edit that shorts a weakly coupled piece of copper (a via from a plane island to ground at
+  low frequency) removes, through the update, a potential mode that the base's FP32 sweeps carry at up to
+  10^6 times the size of what remains, and a solve whose Krylov space starts from the warm start's residual
+  (concentrated on the new branches) can stagnate in FP32 rounding.  Warm-started columns therefore run under
+  an iteration budget (a multiple of the base solve's count) and are solved again from zero when they miss it.
+"""
 from __future__ import annotations
 
 import time
@@ -36,17 +45,29 @@ class WhatIf:
     frequencies the base is solved at (edits pick from them, so the base's factorisations serve every edit)."""
 
     def __init__(self, stack: gs.PlaneStack, routes: list, freqs, tol: float = 1e-5, max_cols: int = 32,
-                 warm_budget: float = 2.0, **solve_kw):
+                 method: str = "bordered", warm_budget: float = 2.0, border_tol: float = 1e-2, **solve_kw):
+        if method not in ("bordered", "derived"):
+            raise ValueError("method must be 'bordered' or 'derived'")
         self.stack = stack
         self.routes = list(routes)
         self.freqs = [float(f) for f in freqs]
         self.tol = tol
         self.max_cols = max_cols
+        self.method = method
+        self.border_tol = border_tol
         self.warm_budget = warm_budget
         self.kw = solve_kw
         self.base: dict = {}
 
-    def _solve(self, stack, routes: dict, cols: list, guesses=None, budget=None) -> tuple:
+    def _raw(self, stack, freqs: list, rhs_tops: list, Js: list, tol: float) -> list:
+        """solve_batch in batches of max_cols: [(Ib, V, its, x, residual)]."""
+        out = []
+        for c0 in range(0, len(freqs), self.max_cols):
+            sl = slice(c0, c0 + self.max_cols)
+            out += stack.solve_batch(freqs[sl], rhs_tops[sl], Js[sl], tol=tol, **self.kw)
+        return out
+
+    def _solve(self, stack, routes: dict, cols: list, guesses=None, budget=None, tol=None) -> tuple:
         """Columns [(net, f)] on `stack` in batches of max_cols; returns (their Solutions in order, the
         indices of the warm-started columns that missed their budget and were solved again from zero)."""
         out, redo = [], []
@@ -58,12 +79,13 @@ class WhatIf:
                 kw["max_its"] = int(max(budget[c] for c in part))
                 failed = []
             g = None if guesses is None else [guesses[c0 + q] for q in range(len(part))]
+            tol = self.tol if tol is None else tol
             res = stack.solve_batch([f for _, f in part], [routes[k].rhs_top(f) for k, f in part],
-                                    [routes[k].J() for k, _ in part], tol=self.tol, guesses=g, failed=failed, **kw)
+                                    [routes[k].J() for k, _ in part], tol=tol, guesses=g, failed=failed, **kw)
             if failed:
                 again = stack.solve_batch([part[q][1] for q in failed], [routes[part[q][0]].rhs_top(part[q][1])
                                                                          for q in failed],
-                                          [routes[part[q][0]].J() for q in failed], tol=self.tol, **self.kw)
+                                          [routes[part[q][0]].J() for q in failed], tol=tol, **self.kw)
                 for q, r in zip(failed, again):
                     res[q] = (r[0], r[1], r[2] + res[q][2], r[3], r[4])
                 redo += [c0 + q for q in failed]
@@ -75,15 +97,97 @@ class WhatIf:
         t0 = time.perf_counter()
         self.stack.factorise(self.freqs, together=True)
         cols = [(k, f) for k in range(len(self.routes)) for f in self.freqs]
-        sols, _ = self._solve(self.stack, dict(enumerate(self.routes)), cols)
+        tol = self.tol * (0.5 if self.method == "bordered" else 1.0)
+        sols, _ = self._solve(self.stack, dict(enumerate(self.routes)), cols, tol=tol)
         self.base = dict(zip(cols, sols))
         return time.perf_counter() - t0
 
     def evaluate(self, branches: list, nets, freqs) -> EditResult:
         """The base plus `branches`, solved for the given nets (indices) at the given frequencies (a subset of
-        the base's), warm-started from the base's solutions."""
+        the base's)."""
         if not self.base:
             raise RuntimeError("solve the baseline first")
+        st = self.stack
+        keep = [b for b in branches if st.node_id(b.a) >= 0 and st.node_id(b.b) >= 0 and tuple(b.a) != tuple(b.b)]
+        joins = any(st.full_label[st.node_id(b.a)] != st.full_label[st.node_id(b.b)] for b in keep)
+        if self.method == "bordered" and keep and not joins:
+            return self._bordered(keep, nets, freqs)
+        return self._derived(branches, nets, freqs)
+
+    def _bordered(self, extra: list, nets, freqs) -> EditResult:
+        t0 = time.perf_counter()
+        st = self.stack
+        dst = st.with_branches(extra, device=False)
+        droutes = {k: self.routes[k].on(dst) for k in nets}
+        nb, k, n_nodes = st.nb, len(extra), st.n_nodes
+        kept = np.full(n_nodes, -1, np.int64)
+        kept[np.flatnonzero(st.keep)] = np.arange(int(st.keep.sum()))
+        na = np.array([st.node_id(b.a) for b in extra])
+        nbn = np.array([st.node_id(b.b) for b in extra])
+        ka, kb = kept[na], kept[nbn]
+        freqs = [float(f) for f in freqs]
+        t1 = time.perf_counter()
+        # X_F: the base system's response to each new branch's unit injection (+1 at a, -1 at b), per frequency
+        fcols = [(f, j) for f in freqs for j in range(k)]
+        Js = []
+        for f, j in fcols:
+            J = np.zeros(n_nodes)
+            J[na[j]] += 1.0
+            J[nbn[j]] -= 1.0
+            Js.append(J)
+        raw = self._raw(st, [f for f, _ in fcols], [np.zeros(nb, complex)] * len(fcols), Js,
+                        self.tol * self.border_tol)
+        XF = {c: r[3] for c, r in zip(fcols, raw)}
+        rF = {c: r[4] * np.sqrt(2.0) for c, r in zip(fcols, raw)}      # ||F_j|| = sqrt 2
+        t2 = time.perf_counter()
+
+        def across(v, idx):                    # v at kept indices idx, zero where a node is not kept
+            return np.where(idx >= 0, v[np.maximum(idx, 0)], 0.0)
+
+        sols, redo_cols, redo_x0 = {}, [], []
+        for f in freqs:
+            X = np.stack([XF[(f, j)] for j in range(k)], axis=1)         # (nb + n_keep, k)
+            VF = X[nb:]
+            # U^T V_F: row i = V_F at branch i's end a minus at end b (k x k)
+            UtVF = (np.where(ka[:, None] >= 0, VF[np.maximum(ka, 0)], 0.0)
+                    - np.where(kb[:, None] >= 0, VF[np.maximum(kb, 0)], 0.0))
+            Sigma = np.diag([complex(b.z(f)) for b in extra]) + UtVF
+            rFf = np.array([rF[(f, j)] for j in range(k)])
+            for net in nets:
+                base = self.base[(net, f)]
+                xb = base.state_for(st)
+                r = droutes[net]
+                top = r.rhs_top(f)
+                b_new = top[nb: nb + k]
+                Vb = xb[nb:]
+                i_new = np.linalg.solve(Sigma, b_new + (across(Vb, ka) - across(Vb, kb)))
+                x = np.concatenate([xb[:nb] - X[:nb] @ i_new, i_new, Vb - VF @ i_new])
+                bb = np.linalg.norm(np.concatenate([self.routes[net].rhs_top(f),
+                                                    self.routes[net].J()[st.keep]]))
+                bd = np.linalg.norm(np.concatenate([top, r.J()[st.keep]]))
+                bound = (base.residual * bb + float(np.abs(i_new) @ rFf)) / bd
+                V = np.zeros(n_nodes, complex)
+                V[st.keep] = x[nb + k:]
+                sols[(net, f)] = r.solution(f, x[: nb + k], V, 0, bound)
+                if not bound <= self.tol:
+                    redo_cols.append((net, f))
+                    redo_x0.append(x)
+        t3 = time.perf_counter()
+        if redo_cols:
+            # columns whose bound misses the tolerance: the derived stack, from the composed solution
+            ddst = st.with_branches(extra)
+            drr = {net: self.routes[net].on(ddst) for net in nets}
+            out, _ = self._solve(ddst, drr, redo_cols, [[x] for x in redo_x0],
+                                 {c: self.warm_budget * self.base[c].iterations + self.kw.get("restart", 50)
+                                  for c in redo_cols})
+            sols.update(zip(redo_cols, out))
+        t4 = time.perf_counter()
+        cols = [(net, f) for net in nets for f in freqs]
+        return EditResult({c: sols[c] for c in cols}, t4 - t0, [r[2] for r in raw],
+                          {"derive_stack_s": t1 - t0, "border_solve_s": t2 - t1, "compose_s": t3 - t2,
+                           "redo_s": t4 - t3, "border_columns": len(fcols), "cold_redo": len(redo_cols)})
+
+    def _derived(self, branches: list, nets, freqs) -> EditResult:
         t0 = time.perf_counter()
         dst = self.stack.with_branches(branches)
         droutes = {k: self.routes[k].on(dst) for k in nets}

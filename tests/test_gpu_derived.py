@@ -105,3 +105,24 @@ def test_what_if_service(case):
         assert abs(sol.Z_loop - ref) <= 1e-8 * abs(ref), (k, q)
         assert sol.residual <= board.tol
     assert res.parts["cold_redo"] == 0
+
+
+@pytest.mark.parametrize("method", ["bordered", "derived"])
+def test_what_if_methods_agree_with_oracle_whole_stack(case, method):
+    """Both ways of answering an edit give the whole edited board's solution (oracle, factorised afresh)."""
+    from groundtruth_gb300 import whatif
+    z, board, extra, st, routes, dst = case
+    more = synth.what_if_branches(board, seed=13, n_via=3, n_part=1)
+    whole = synth.Board.from_arrays(board.to_arrays())
+    whole.branches = list(board.branches) + list(more)
+    ost = oracle_stack(whole)
+    oroutes = oracle_routes(ost, whole)
+    wi = whatif.WhatIf(st, routes, board.freqs, tol=board.tol, method=method)
+    wi.baseline()
+    res = wi.evaluate(branches_of(more), [0, 1], [float(f) for f in board.freqs])
+    for (k, f), sol in res.solutions.items():
+        ref = oroutes[k].solve(f, tol=board.tol)
+        assert abs(sol.Z_loop - ref["Z_loop"]) <= 1e-8 * abs(ref["Z_loop"]), (method, k, f)
+        assert sol.residual <= board.tol
+    if method == "bordered":
+        assert res.parts["border_columns"] == len(more) * len(board.freqs)
