@@ -24,18 +24,43 @@ part) without joining separate pieces of copper.  Two ways to answer it:
 """
 from __future__ import annotations
 
+import math
 import time
 from dataclasses import dataclass, field
+from typing import Callable
 
 import numpy as np
 
-from . import stack as gs
+from . import greens, stack as gs
+
+
+@dataclass
+class EditColumn:
+    """One (net, frequency) answer of an edit: the loop impedance, moment and FP64 residual (for the bordered
+    way a rigorous upper bound), and the full solution on demand (``solution()``: currents, potentials)."""
+    f: float
+    Z_loop: complex
+    m: np.ndarray
+    residual: float
+    iterations: int
+    make: Callable = field(repr=False, default=None)
+
+    @property
+    def L_loop(self) -> float:
+        return self.Z_loop.imag / (2 * math.pi * self.f)
+
+    def solution(self) -> gs.Solution:
+        return self.make()
+
+
+def _column(sol: gs.Solution) -> EditColumn:
+    return EditColumn(sol.f, sol.Z_loop, sol.m, sol.residual, sol.iterations, lambda: sol)
 
 
 @dataclass
 class EditResult:
-    solutions: dict                     # (net, frequency) -> stack.Solution
-    seconds: float                      # wall time of the edit, derived stack to the last solution on the host
+    solutions: dict                     # (net, frequency) -> EditColumn
+    seconds: float                      # wall time of the edit, derived stack to the last answer on the host
     iterations: list = field(default_factory=list)
     parts: dict = field(default_factory=dict)
 
@@ -69,8 +94,10 @@ class WhatIf:
 
     def _solve(self, stack, routes: dict, cols: list, guesses=None, budget=None, tol=None) -> tuple:
         """Columns [(net, f)] on `stack` in batches of max_cols; returns (their Solutions in order, the
-        indices of the warm-started columns that missed their budget and were solved again from zero)."""
-        out, redo = [], []
+        indices of the warm-started columns that missed their budget and were solved again from zero, the
+        solution vectors in the reference's unknown order)."""
+        out, redo, xs = [], [], []
+        tol = self.tol if tol is None else tol
         for c0 in range(0, len(cols), self.max_cols):
             part = cols[c0: c0 + self.max_cols]
             kw = dict(self.kw)
@@ -79,7 +106,6 @@ class WhatIf:
                 kw["max_its"] = int(max(budget[c] for c in part))
                 failed = []
             g = None if guesses is None else [guesses[c0 + q] for q in range(len(part))]
-            tol = self.tol if tol is None else tol
             res = stack.solve_batch([f for _, f in part], [routes[k].rhs_top(f) for k, f in part],
                                     [routes[k].J() for k, _ in part], tol=tol, guesses=g, failed=failed, **kw)
             if failed:
@@ -90,21 +116,27 @@ class WhatIf:
                     res[q] = (r[0], r[1], r[2] + res[q][2], r[3], r[4])
                 redo += [c0 + q for q in failed]
             out += [routes[k].solution(f, Ib, V, its, r) for (k, f), (Ib, V, its, x, r) in zip(part, res)]
-        return out, redo
+            xs += [r[3] for r in res]
+        return out, redo, xs
 
     def baseline(self) -> float:
         """Solve every net at every frequency on the base stack; returns the seconds it took."""
         t0 = time.perf_counter()
-        self.stack.factorise(self.freqs, together=True)
+        st = self.stack
+        st.factorise(self.freqs, together=True)
         cols = [(k, f) for k in range(len(self.routes)) for f in self.freqs]
         tol = self.tol * (0.5 if self.method == "bordered" else 1.0)
-        sols, _ = self._solve(self.stack, dict(enumerate(self.routes)), cols, tol=tol)
+        sols, _, xs = self._solve(st, dict(enumerate(self.routes)), cols, tol=tol)
         self.base = dict(zip(cols, sols))
+        self.base_x = dict(zip(cols, xs))
+        self.base_bnorm = {(k, f): float(np.linalg.norm(st.rhs_vector(self.routes[k].rhs_top(f), self.routes[k].J())))
+                           for k, f in cols}
+        self.base_psi_ib = {(k, f): complex(np.dot(self.routes[k].psi, x[: st.nb])) for (k, f), x in zip(cols, xs)}
         return time.perf_counter() - t0
 
     def evaluate(self, branches: list, nets, freqs) -> EditResult:
-        """The base plus `branches`, solved for the given nets (indices) at the given frequencies (a subset of
-        the base's)."""
+        """The base plus `branches`, answered for the given nets (indices) at the given frequencies (a subset
+        of the base's)."""
         if not self.base:
             raise RuntimeError("solve the baseline first")
         st = self.stack
@@ -125,6 +157,7 @@ class WhatIf:
         na = np.array([st.node_id(b.a) for b in extra])
         nbn = np.array([st.node_id(b.b) for b in extra])
         ka, kb = kept[na], kept[nbn]
+        arm = np.array([0.5 * np.cross(st.pos(b.a), st.pos(b.b)) for b in extra])        # (k, 3)
         freqs = [float(f) for f in freqs]
         t1 = time.perf_counter()
         # X_F: the base system's response to each new branch's unit injection (+1 at a, -1 at b), per frequency
@@ -141,49 +174,53 @@ class WhatIf:
         rF = {c: r[4] * np.sqrt(2.0) for c, r in zip(fcols, raw)}      # ||F_j|| = sqrt 2
         t2 = time.perf_counter()
 
-        def across(v, idx):                    # v at kept indices idx, zero where a node is not kept
-            return np.where(idx >= 0, v[np.maximum(idx, 0)], 0.0)
+        def at(v, idx):                        # rows of v at kept indices idx, zero where a node is not kept
+            return np.where((idx >= 0).reshape((-1,) + (1,) * (v.ndim - 1)), v[np.maximum(idx, 0)], 0.0)
 
-        sols, redo_cols, redo_x0 = {}, [], []
+        cols_out, redo_cols, redo_x0 = {}, [], []
         for f in freqs:
+            w = 2 * math.pi * f
             X = np.stack([XF[(f, j)] for j in range(k)], axis=1)         # (nb + n_keep, k)
-            VF = X[nb:]
-            # U^T V_F: row i = V_F at branch i's end a minus at end b (k x k)
-            UtVF = (np.where(ka[:, None] >= 0, VF[np.maximum(ka, 0)], 0.0)
-                    - np.where(kb[:, None] >= 0, VF[np.maximum(kb, 0)], 0.0))
-            Sigma = np.diag([complex(b.z(f)) for b in extra]) + UtVF
+            XI, VF = X[:nb], X[nb:]
+            Sigma = np.diag([complex(b.z(f)) for b in extra]) + at(VF, ka) - at(VF, kb)
             rFf = np.array([rF[(f, j)] for j in range(k)])
+            MX = np.stack([st.moment(np.zeros((0, 8)), XI[:, j]) for j in range(k)], axis=1)   # (3, k)
             for net in nets:
-                base = self.base[(net, f)]
-                xb = base.state_for(st)
+                c = (net, f)
+                base, xb, r0 = self.base[c], self.base_x[c], self.routes[net]
                 r = droutes[net]
-                top = r.rhs_top(f)
-                b_new = top[nb: nb + k]
+                psi_new = r.psi[nb: nb + k]
+                b_new = -1j * w * psi_new
                 Vb = xb[nb:]
-                i_new = np.linalg.solve(Sigma, b_new + (across(Vb, ka) - across(Vb, kb)))
-                x = np.concatenate([xb[:nb] - X[:nb] @ i_new, i_new, Vb - VF @ i_new])
-                bb = np.linalg.norm(np.concatenate([self.routes[net].rhs_top(f),
-                                                    self.routes[net].J()[st.keep]]))
-                bd = np.linalg.norm(np.concatenate([top, r.J()[st.keep]]))
-                bound = (base.residual * bb + float(np.abs(i_new) @ rFf)) / bd
-                V = np.zeros(n_nodes, complex)
-                V[st.keep] = x[nb + k:]
-                sols[(net, f)] = r.solution(f, x[: nb + k], V, 0, bound)
+                i_new = np.linalg.solve(Sigma, b_new + at(Vb, ka) - at(Vb, kb))
+                psi_ib = self.base_psi_ib[c] - (r0.psi @ XI) @ i_new + psi_new @ i_new
+                v_inj = sum(a * (at(Vb, kept[[n]])[0] - at(VF, kept[[n]])[0] @ i_new) for n, a in r.injections)
+                Z = complex(greens.trace_resistance(r.segments, f, st.sigma, r.trace_t) + v_inj
+                            + 1j * w * (r.L_trace + psi_ib))
+                m = base.m - MX @ i_new + arm.T @ i_new
+                bb = self.base_bnorm[c]
+                bound = (base.residual * bb + float(np.abs(i_new) @ rFf)) / math.sqrt(bb * bb + float(np.vdot(b_new, b_new).real))
+
+                def make(f=f, r=r, xb=xb, XI=XI, VF=VF, i_new=i_new, bound=bound):
+                    V = np.zeros(n_nodes, complex)
+                    V[st.keep] = xb[nb:] - VF @ i_new
+                    return r.solution(f, np.concatenate([xb[:nb] - XI @ i_new, i_new]), V, 0, bound)
+                cols_out[c] = EditColumn(f, Z, m, bound, 0, make)
                 if not bound <= self.tol:
-                    redo_cols.append((net, f))
-                    redo_x0.append(x)
+                    redo_cols.append(c)
+                    redo_x0.append(np.concatenate([xb[:nb] - XI @ i_new, i_new, Vb - VF @ i_new]))
         t3 = time.perf_counter()
         if redo_cols:
             # columns whose bound misses the tolerance: the derived stack, from the composed solution
             ddst = st.with_branches(extra)
             drr = {net: self.routes[net].on(ddst) for net in nets}
-            out, _ = self._solve(ddst, drr, redo_cols, [[x] for x in redo_x0],
-                                 {c: self.warm_budget * self.base[c].iterations + self.kw.get("restart", 50)
-                                  for c in redo_cols})
-            sols.update(zip(redo_cols, out))
+            out, _, _ = self._solve(ddst, drr, redo_cols, [[x] for x in redo_x0],
+                                    {c: self.warm_budget * self.base[c].iterations + self.kw.get("restart", 50)
+                                     for c in redo_cols})
+            cols_out.update((c, _column(sol)) for c, sol in zip(redo_cols, out))
         t4 = time.perf_counter()
         cols = [(net, f) for net in nets for f in freqs]
-        return EditResult({c: sols[c] for c in cols}, t4 - t0, [r[2] for r in raw],
+        return EditResult({c: cols_out[c] for c in cols}, t4 - t0, [r[2] for r in raw],
                           {"derive_stack_s": t1 - t0, "border_solve_s": t2 - t1, "compose_s": t3 - t2,
                            "redo_s": t4 - t3, "border_columns": len(fcols), "cold_redo": len(redo_cols)})
 
@@ -193,12 +230,12 @@ class WhatIf:
         droutes = {k: self.routes[k].on(dst) for k in nets}
         t1 = time.perf_counter()
         cols = [(k, float(f)) for k in nets for f in freqs]
-        guesses = [[dst.map_state(self.base[c].state_for(self.stack), self.stack)] for c in cols]
+        guesses = [[dst.map_state(self.base_x[c], self.stack)] for c in cols]
         dst.factorise([f for _, f in cols], together=True)
         t2 = time.perf_counter()
         budget = {c: self.warm_budget * self.base[c].iterations + self.kw.get("restart", 50) for c in cols}
-        sols, redo = self._solve(dst, droutes, cols, guesses, budget)
+        sols, redo, _ = self._solve(dst, droutes, cols, guesses, budget)
         t3 = time.perf_counter()
-        return EditResult(dict(zip(cols, sols)), t3 - t0, [s.iterations for s in sols],
+        return EditResult({c: _column(sol) for c, sol in zip(cols, sols)}, t3 - t0, [s.iterations for s in sols],
                           {"derive_stack_s": t1 - t0, "operators_s": t2 - t1, "solve_s": t3 - t2,
                            "cold_redo": len(redo)})

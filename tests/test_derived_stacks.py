@@ -149,3 +149,47 @@ def test_route_on_derived_reuses_strip_coupling(derived):
     r = routes[0].on(dst)
     assert r.strip_psi is routes[0].strip_psi
     assert len(r.psi) == dst.nb and rel(r.psi, z["psi0"]) < 1e-12
+
+
+class _OracleBacked:
+    """A host-only PlaneStack whose solves run on the oracle (FP64 CPU): the what-if composition's host
+    arithmetic tested without a device."""
+
+    def __init__(self, st, ost):
+        self.st, self.ost = st, ost
+
+    def solve_batch(self, freqs, rhs_tops, Js, tol=1e-5, guesses=None, failed=None, **kw):
+        out = []
+        for f, top, J in zip(freqs, rhs_tops, Js):
+            Ib, V, its, x = self.ost.solve(f, np.asarray(top, complex), np.asarray(J, float), tol=tol)
+            rhs = self.st.rhs_vector(top, J)
+            res = np.linalg.norm(rhs - self.ost.matvec(self.ost.operator(f), x)) / np.linalg.norm(rhs)
+            out.append((Ib, V, its, x, res))
+        return out
+
+
+def test_bordered_edit_composition_on_cpu(derived):
+    """whatif.WhatIf's bordered way (base solves of the new branches' injections, k x k solve per column)
+    with the oracle as the solver: loop impedance, moment, currents and the residual bound against the oracle's
+    solve of the whole edited board."""
+    from groundtruth_gb300 import whatif
+    z, board, extra, ost, odst = derived
+    st, routes = gs.from_board(board, _device=False)
+    backed = _OracleBacked(st, ost)
+    st.factorise = lambda *a, **k: None
+    st.solve_batch = backed.solve_batch
+    wi = whatif.WhatIf(st, routes, board.freqs[:2], tol=1e-9, method="bordered")
+    wi.baseline()
+    res = wi.evaluate(branches_of(extra), [0, 1], [float(board.freqs[1])])
+    assert res.parts["border_columns"] == len(extra) and res.parts["cold_redo"] == 0
+    oroutes = oracle_routes(odst, board)
+    f = float(board.freqs[1])
+    for k in (0, 1):
+        col = res.solutions[(k, f)]
+        ref = oroutes[k].solve(f, tol=1e-12)
+        assert abs(col.Z_loop - ref["Z_loop"]) <= 1e-7 * abs(ref["Z_loop"])
+        assert np.linalg.norm(col.m - ref["m"]) <= 1e-6 * np.linalg.norm(ref["m"])
+        assert col.residual <= 1e-9
+        sol = col.solution()
+        x = sol.state_for(st.with_branches(branches_of(extra)))
+        assert rel(x[: odst.nb], ref["x"][: odst.nb]) < 1e-6
