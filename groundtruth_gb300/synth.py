@@ -96,6 +96,9 @@ class Layer:
     node: np.ndarray
     xb: np.ndarray
     yb: np.ndarray
+    # strips narrower than the pitch (the reference Grid's wx / wy, ox / oy, rx / ry: width and centre offset as
+    # fractions of the pitch, the resistance's width; None: every strip full and centred)
+    widths: Optional[dict] = None
 
 
 @dataclass
@@ -164,6 +167,9 @@ class Board:
                "branch_rlc": np.array([[b.R, b.L, b.C, b.radius] for b in self.branches], float).reshape(-1, 4),
                "branch_via": np.array([b.kind == "via" for b in self.branches], bool),
                "net_count": np.int64(len(self.nets))}
+        for k, l in enumerate(self.layers):
+            for key, v in (l.widths or {}).items():
+                out[f"layer{k}_{key}"] = np.asarray(v, float)
         for n, net in enumerate(self.nets):
             out[f"net{n}_seg"] = net.segments
             out[f"net{n}_ends"] = np.array([*net.driver, *net.receiver], np.int64)
@@ -174,6 +180,10 @@ class Board:
     def from_arrays(a) -> "Board":
         layers = [Layer(f"L{k}", float(a["layer_z"][k]), float(a["layer_t"][k]), a["layer_node"][k].astype(bool),
                         a["layer_xb"][k].astype(bool), a["layer_yb"][k].astype(bool)) for k in range(len(a["layer_z"]))]
+        files = a.files if hasattr(a, "files") else list(a.keys())
+        for k, l in enumerate(layers):
+            w = {key: np.asarray(a[f"layer{k}_{key}"], float) for key in WIDTH_KEYS if f"layer{k}_{key}" in files}
+            l.widths = w or None
         pairs = [Pair(int(p[0]), int(p[1]), float(p[2]), float(p[3])) for p in a["pairs"]]
         branches = [BranchSpec(tuple(int(v) for v in ab[:3]), tuple(int(v) for v in ab[3:]), float(r[0]), float(r[1]),
                                float(r[2]), "via" if via else "part", float(r[3]))
@@ -439,6 +449,57 @@ def _labels(mask: np.ndarray, xb: np.ndarray, yb: np.ndarray) -> np.ndarray:
     return lab
 
 
+WIDTH_KEYS = ("wx", "wy", "ox", "oy", "rx", "ry")
+
+
+def necked_pair(seed: int = 17) -> Board:
+    """A plane pair (40 x 36 at 0.5 mm) whose PWR plane has an island joined to the rest by a neck narrower
+    than the pitch, with seeded narrow, off-centre and series-narrowed strips along the moat (the exact-copper
+    raster's wx / wy, ox / oy, rx / ry), a decoupling part on the island and two nets crossing the GND slot."""
+    rng = np.random.default_rng(seed)
+    b = small_pair(seed=5)
+    b.name = "necked_pair"
+    pwr = b.layers[1]
+    node = pwr.node.copy()
+    i0, i1, j0, j1 = 25, 37, 21, 33                 # the moat: one cell wide around the island
+    node[i0, j0:j1 + 1] = False
+    node[i1, j0:j1 + 1] = False
+    node[i0:i1 + 1, j0] = False
+    node[i0:i1 + 1, j1] = False
+    node[i0, 26:28] = True                          # the neck through the moat's left side
+    xb = node[:-1, :] & node[1:, :]
+    yb = node[:, :-1] & node[:, 1:]
+    nx, ny = node.shape
+    wx, wy = np.ones((nx - 1, ny)), np.ones((nx, ny - 1))
+    ox, oy = np.zeros((nx - 1, ny)), np.zeros((nx, ny - 1))
+    rx, ry = np.zeros((nx - 1, ny)), np.zeros((nx, ny - 1))
+    for i in (i0 - 1, i0):                          # the neck's x strips: 0.35-0.45 of the pitch
+        for j in (26, 27):
+            wx[i, j] = rng.uniform(0.35, 0.45)
+            ox[i, j] = 0.1 if j == 26 else -0.1
+    wy[i0, 26] = 0.5
+    rx[i0 - 1, 26] = 0.8 * wx[i0 - 1, 26]           # a change of width along the strip, in series
+    rx[i0, 27] = 0.9 * wx[i0, 27]
+    # strips along the moat's outside: partly covered borders
+    edge_y = [(i0 - 1, j) for j in range(j0, j1) if yb[i0 - 1, j] and j not in (25, 26, 27)]
+    for q in rng.choice(len(edge_y), size=min(8, len(edge_y)), replace=False):
+        i, j = edge_y[q]
+        wy[i, j] = rng.uniform(0.55, 0.95)
+        oy[i, j] = rng.uniform(-0.5, 0.5) * (1 - wy[i, j])
+    edge_x = [(i, j0 - 1) for i in range(i0, i1) if xb[i, j0 - 1]]
+    for q in rng.choice(len(edge_x), size=min(4, len(edge_x)), replace=False):
+        i, j = edge_x[q]
+        wx[i, j] = rng.uniform(0.6, 0.95)
+        ox[i, j] = rng.uniform(-0.5, 0.5) * (1 - wx[i, j])
+    ry[i0 - 1, j0 + 2] = 0.7 if yb[i0 - 1, j0 + 2] else 0.0
+    b.layers[1] = Layer(pwr.name, pwr.z, pwr.thickness, node, xb, yb,
+                        {"wx": wx, "wy": wy, "ox": ox, "oy": oy, "rx": rx, "ry": ry})
+    # the decoupling part moves onto the island (the small pair's other branches stay)
+    b.branches = [BranchSpec((0, 30, 27), (1, 30, 27), 0.02, 0.5e-9, 100e-9, "part")] + b.branches[1:]
+    b.freqs = np.array([1e6, 1e8, 1e9])
+    return b
+
+
 def what_if_base(n: int = 512, d_mm: float = 0.2, n_nets: int = 12, n_freq: int = 16, seed: int = 4,
                  slot: bool = True, n_decap: int = 8) -> Board:
     """The interactive what-if workload's base board: 4-layer Sig/GND/PWR/Sig at d_mm pitch, the GND/PWR pair
@@ -522,4 +583,4 @@ def what_if_branches(board: Board, seed: int, n_via: int = 2, n_part: int = 1) -
 
 
 WORKLOADS = {"plain_plane": plain_plane, "slotted_pair": slotted_pair, "small_pair": small_pair,
-             "small_stack3": small_stack3, "six_sheet": six_sheet}
+             "small_stack3": small_stack3, "six_sheet": six_sheet, "necked_pair": necked_pair}

@@ -5,7 +5,7 @@ This module is the checker, never the product: only ``tests/``, ``__graft_entry_
 CUDA library under ``groundtruth_gb300/`` and fails loudly when that library is missing.
 
 It restates, in plain numpy/scipy FP64, the algorithm of GroundTruth's solver for the scope the GPU build
-covers (one current sheet per layer, full-width strips: no face sheets and no narrow-strip corrections):
+covers (one current sheet per layer, no face sheets):
 
 * partial inductances and the strip kernel      src/groundtruth/solver/kernel.py:165-294
 * slab impedance / skin thickness               src/groundtruth/solver/kernel.py:23-75
@@ -18,6 +18,7 @@ covers (one current sheet per layer, full-width strips: no face sheets and no na
 * restarted GMRES (CGS + DGKS, Givens)          src/groundtruth/solver/peec.py:3093-3224
 * solve driver                                  src/groundtruth/solver/peec.py:2560-2607
 * derived stacks (added branches, Woodbury)     src/groundtruth/solver/peec.py:1871-1923, 2354-2377
+* strips narrower than the pitch (dL, M_near)   src/groundtruth/solver/peec.py:1732-1820, 2129-2132, 3309-3342
 * excitation, coupling, moment, loop impedance  src/groundtruth/solver/peec.py:2615-2817, 3227-3250
 
 Parity of this restatement is pinned by ``tests/golden/*.npz``, produced by the reference itself
@@ -346,6 +347,34 @@ def gmres(op: Callable, b: np.ndarray, tol: float, max_cycles: int = 8, restart:
     return x, its, bool(np.linalg.norm(r) <= tol * bnorm)
 
 
+NEAR_AXIAL = 2      # peec.py:3325: side-by-side partial strips corrected up to this many strips along
+
+
+def narrow_self(d: float, phi, t):
+    """The partial self inductance a strip d long and phi*d wide adds to the full square strip's: the numeric
+    flat-strip integral's change plus the thickness change of the GMD formula (peec.py:3309-3322)."""
+    phi, t = np.asarray(phi, float), np.asarray(t, float)
+
+    def thick(w):
+        return filament_mutual(d, 0.0, GMD_FLAT * w) - filament_mutual(d, 0.0, GMD_FLAT * (w + t))
+    return strip_self_numeric(d, phi * d) - strip_self_numeric(d, d) - thick(phi * d) + thick(d)
+
+
+def side_mutual(length: float, wa, wb, gap, steps=0.0, n: int = 8) -> np.ndarray:
+    """Mutual inductance of two flat coplanar parallel strips (widths wa, wb, centre distance gap, `steps`
+    lengths apart along them; fractions of `length`): the mean of n x n filament mutuals, touching filaments a
+    filament's GMD apart (peec.py:3328-3341)."""
+    wa, wb, gap, steps = (np.atleast_1d(v) for v in np.broadcast_arrays(*(np.asarray(v, float) for v in
+                                                                            (wa, wb, gap, steps))))
+    wa, wb, gap = wa * length, wb * length, gap * length
+    u = (np.arange(n) + 0.5) / n - 0.5
+    ya = wa[:, None, None] * u[None, :, None]
+    yb = gap[:, None, None] + wb[:, None, None] * u[None, None, :]
+    rho = np.maximum(np.abs(yb - ya), GMD_FLAT * np.maximum(wa, wb)[:, None, None] / n)
+    axial = np.broadcast_to((steps * length)[:, None, None], rho.shape)
+    return filament_mutual(length, axial, rho).mean(axis=(1, 2))
+
+
 # ----------------------------------------------------------------------------------------------- problem
 @dataclass
 class OLayer:
@@ -355,6 +384,7 @@ class OLayer:
     node: np.ndarray
     xb: np.ndarray
     yb: np.ndarray
+    widths: Optional[dict] = None     # the grid's wx / wy, ox / oy, rx / ry (peec.py:213-220); None: full strips
 
 
 @dataclass
@@ -413,6 +443,70 @@ class OracleStack:
         self._base: Optional[OracleStack] = None
         self._topology(list(branches or []))
         self._kernels()
+        self._widths()
+
+    # -- strips narrower than the pitch (peec.py:1732-1820, 3309-3342)
+    def _widths(self):
+        """strip_width, r_width (ns), dL (ns or None) and M_near (sparse ns x ns or None): peec.py:1732-1820."""
+        def gather(key, idx, shape, default):
+            if len(idx) == 0:
+                return np.zeros(0)
+            if all((l.widths or {}).get(key) is None for l in self.layers):
+                return np.full(len(idx), default)
+            w = np.stack([np.asarray(l.widths[key], float) if (l.widths or {}).get(key) is not None
+                          else np.full(shape, default) for l in self.layers])
+            return w[tuple(idx.T)]
+        sx, sy = (self.nx - 1, self.ny), (self.nx, self.ny - 1)
+        w = np.concatenate([gather("wx", self.xa, sx, 1.0), gather("wy", self.ya, sy, 1.0)])
+        ok = w > 0
+        self.strip_width = np.where(ok, w, 1.0)
+        rw = np.concatenate([gather("rx", self.xa, sx, 0.0), gather("ry", self.ya, sy, 0.0)])
+        self.r_width = np.where(ok & (rw > 0), rw, self.strip_width)
+        self.r_uniform = not np.any(self.r_width != 1.0)
+        off = np.where(ok, np.concatenate([gather("ox", self.xa, sx, 0.0), gather("oy", self.ya, sy, 0.0)]), 0.0)
+        self.dL = self.M_near = None
+        narrow = self.strip_width < 1.0
+        if not np.any(narrow):
+            return
+        d = self.d
+        t = self.sheet_t[np.concatenate([self.xa[:, 0], self.ya[:, 0]])]
+        dL = np.zeros(self.ns)
+        keys, inv = np.unique(np.round(np.column_stack([self.strip_width[narrow], t[narrow]]), 12), axis=0,
+                              return_inverse=True)
+        dL[narrow] = narrow_self(d, keys[:, 0], keys[:, 1])[np.ravel(inv)]
+        self.dL = dL
+        rows, cols, steps = [], [], []
+        for idx, shape, lo, axis in ((self.xa, sx, 0, 2), (self.ya, sy, self.nxb, 1)):
+            if len(idx) == 0:
+                continue
+            at = -np.ones((self.N, *shape), np.int64)
+            at[tuple(idx.T)] = lo + np.arange(len(idx))
+            n_ax = shape[0] if axis == 2 else shape[1]
+            for k in range(-NEAR_AXIAL, NEAR_AXIAL + 1):
+                if abs(k) >= n_ax:
+                    continue
+                ax_a = slice(max(-k, 0), n_ax - max(k, 0))
+                ax_b = slice(max(k, 0), n_ax - max(-k, 0))
+                a = at[:, ax_a, :-1] if axis == 2 else at[:, :-1, ax_a]
+                b = at[:, ax_b, 1:] if axis == 2 else at[:, 1:, ax_b]
+                both = (a >= 0) & (b >= 0)
+                a, b = a[both], b[both]
+                part = narrow[a] | narrow[b]
+                rows.append(a[part])
+                cols.append(b[part])
+                steps.append(np.full(int(part.sum()), abs(k)))
+        a, b = np.concatenate(rows), np.concatenate(cols)
+        if len(a) == 0:
+            return
+        k = np.concatenate(steps)
+        wa, wb = self.strip_width[a], self.strip_width[b]
+        gap = 1.0 + off[b] - off[a]
+        keys, inv = np.unique(np.round(np.column_stack([wa, wb, gap, k]), 9), axis=0, return_inverse=True)
+        ones = np.ones(len(keys))
+        dM = (side_mutual(d, keys[:, 0], keys[:, 1], keys[:, 2], keys[:, 3])
+              - side_mutual(d, ones, ones, ones, keys[:, 3]))[np.ravel(inv)]
+        M = sp.coo_matrix((dM, (a, b)), shape=(self.ns, self.ns))
+        self.M_near = (M + M.T).tocsr()
 
     def with_branches(self, extra: list) -> "OracleStack":
         """This stack plus a few branches (peec.py:1871-1912): a shallow copy sharing the grids and kernels with
@@ -576,13 +670,18 @@ class OracleStack:
                     G[t] += self._full(orient, t, s) * F[s]
             Y = ifft2(G, axes=(1, 2), workers=-1, overwrite_x=True)
             out[lo:hi] = Y[tuple(idx.T)]
+        if self.dL is not None:             # strips narrower than the pitch (peec.py:2129-2132)
+            out += self.dL * I_s
+            if self.M_near is not None:
+                out += self.M_near @ I_s
         return out
 
     # -- operators (peec.py:2150-2178, 2345-2511)
     def impedances(self, f: float):
         w = 2 * math.pi * f
         zs = np.array([complex(slab_impedance(l.thickness, f, self.sigma)) for l in self.layers])
-        R_strip = np.concatenate([zs[self.xa[:, 0]], zs[self.ya[:, 0]]]) if self.ns else np.zeros(0, complex)
+        R_strip = (np.concatenate([zs[self.xa[:, 0]], zs[self.ya[:, 0]]]) / self.r_width if self.ns
+                   else np.zeros(0, complex))
         if self.ncap:
             C, tand = self.cap[:, 4], self.cap[:, 5]
             z_cap = 1.0 / (w * C * tand + 1j * w * C) if w > 0 else np.full(self.ncap, 1e18 + 0j)
@@ -592,7 +691,9 @@ class OracleStack:
         return w, R_strip, np.concatenate([z_cap, z_br])
 
     def admittance(self, w, R_strip, z_tail) -> sp.csr_matrix:
-        d = np.concatenate([1.0 / (R_strip + 1j * w * self.L_self), 1.0 / z_tail])
+        """peec.py:2465-2511 (no face sheets)."""
+        L_own = self.L_self if self.dL is None else self.L_self + self.dL
+        d = np.concatenate([1.0 / (R_strip + 1j * w * L_own), 1.0 / z_tail])
         if not self.blocks:
             return sp.diags(d).tocsr()
         rows, cols, vals = [np.arange(self.nb)], [np.arange(self.nb)], [d]
@@ -600,9 +701,15 @@ class OracleStack:
         for strips, layers, orient in self.blocks:
             B = (self.B_x if orient == "x" else self.B_y)[np.ix_(layers, layers)]
             m = len(layers)
-            R = np.diag([R_strip[strips[0, k]] for k in range(m)]).astype(complex)
-            Zi = np.linalg.inv(R + 1j * w * B)
-            Zi = np.broadcast_to(Zi.ravel(), (len(strips), m * m)).ravel()
+            if self.dL is None and self.r_uniform:       # every position alike: one inverse
+                R = np.diag([R_strip[strips[0, k]] for k in range(m)]).astype(complex)
+                Zi = np.linalg.inv(R + 1j * w * B)
+                Zi = np.broadcast_to(Zi.ravel(), (len(strips), m * m)).ravel()
+            else:                                           # each position its own R and self inductance
+                Z = np.broadcast_to(1j * w * B, (len(strips), m, m)).copy()
+                Z[:, np.arange(m), np.arange(m)] += R_strip[strips] + (
+                    0.0 if self.dL is None else 1j * w * self.dL[strips])
+                Zi = np.linalg.inv(Z).ravel()
             rows.append(np.repeat(strips, m, axis=1).ravel())
             cols.append(np.tile(strips, (1, m)).ravel())
             vals.append(Zi)

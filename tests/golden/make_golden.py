@@ -16,6 +16,8 @@ The reference's solver module imports shapely at module level but uses it only t
 * per net and frequency the solve at rtol = board.tol with GMRES(board.restart): unknown vector, its,
   Z_loop, magnetic moment, psi
 
+``necked_pair.npz`` holds the same records for a plane pair with strips narrower than the pitch (an island on
+a neck; the grids' wx / wy, ox / oy, rx / ry), plus the reference's strip widths, dL and M_near.
 ``small_pair_derived.npz`` holds the same for small_pair plus a what-if edit's branches on a derived stack
 (PlaneStack.with_branches), including solves warm-started from the base's solutions.
 
@@ -47,7 +49,8 @@ def import_reference(root: str):
 
 
 def build_reference(peec, board: synth.Board):
-    grids = [peec.Grid(0.0, 0.0, board.d * 1e3, board.nx, board.ny, l.node.copy(), l.xb.copy(), l.yb.copy())
+    grids = [peec.Grid(0.0, 0.0, board.d * 1e3, board.nx, board.ny, l.node.copy(), l.xb.copy(), l.yb.copy(),
+                       **{k: np.array(v, float) for k, v in (l.widths or {}).items()})
              for l in board.layers]
     layers = [peec.PlaneLayer(l.name, l.z, g, l.thickness) for l, g in zip(board.layers, grids)]
     branches = [peec.Branch(b.a, b.b, (lambda f, b=b: b.z(f)), f"br{n}", b.kind, b.radius)
@@ -77,6 +80,10 @@ def record(peec, board: synth.Board, solve: bool = True) -> dict:
                ns=np.int64(st.ns), ncap=np.int64(st.ncap), nbr=np.int64(st.nbr), cap=st.cap)
     if getattr(st, "B_x", None) is not None:
         out.update(B_x=st.B_x, B_y=st.B_y)
+    if getattr(st, "dL", None) is not None:          # strips narrower than the pitch
+        out.update(strip_width=st.strip_width, r_width=st.r_width, dL=st.dL)
+        if st.M_near is not None:
+            out["M_near_ij"], out["M_near"] = coo(st.M_near)
     f0 = float(board.freqs[0])
     op = st.operator(f0)
     out.update(op_f=np.float64(f0), op_R=op.R_strip, op_z=op.z_tail)
@@ -167,8 +174,13 @@ def main():
     ap.add_argument("--reference", required=True)
     ap.add_argument("--full", action="store_true")
     ap.add_argument("--derived-only", action="store_true", help="only the derived-stack fixture")
+    ap.add_argument("--narrow-only", action="store_true", help="only the narrow-strip board's fixture")
     args = ap.parse_args()
     peec, kernel = import_reference(args.reference)
+    print("necked_pair", flush=True)
+    np.savez_compressed(HERE / "necked_pair.npz", **record(peec, synth.necked_pair()))
+    if args.narrow_only:
+        return
     print("small_pair_derived", flush=True)
     np.savez_compressed(HERE / "small_pair_derived.npz", **record_derived(peec, synth.small_pair(), seed=11))
     if args.derived_only:

@@ -13,7 +13,7 @@ from groundtruth_gb300 import synth
 from oracle import peec_oracle as po
 
 GOLD = Path(__file__).resolve().parent / "golden"
-CASES = ["small_pair", "small_stack3", "plain_plane"]
+CASES = ["small_pair", "small_stack3", "plain_plane", "necked_pair"]
 
 
 def load(name):
@@ -23,7 +23,7 @@ def load(name):
 
 
 def oracle_stack(board):
-    layers = [po.OLayer(l.z, l.thickness, l.node, l.xb, l.yb) for l in board.layers]
+    layers = [po.OLayer(l.z, l.thickness, l.node, l.xb, l.yb, l.widths) for l in board.layers]
     pairs = [po.OPair(p.upper, p.lower, p.c_per_area, p.tan_delta) for p in board.pairs]
     branches = [po.OBranch(b.a, b.b, b.R, b.L, b.C, b.kind, b.radius) for b in board.branches]
     return po.OracleStack(layers, board.d, branches, pairs, board.sigma, board.precond)
@@ -110,3 +110,16 @@ def test_coupling_and_solves_match_reference(case):
             assert abs(sol["Z_loop"] - z[f"Z{k}_{q}"]) <= 1e-8 * abs(z[f"Z{k}_{q}"]), (k, f)
             assert rel(sol["m"], z[f"m{k}_{q}"]) < 1e-7
             assert abs(sol["its"] - int(z[f"its{k}_{q}"])) <= 2
+
+
+def test_narrow_strip_corrections_match_reference():
+    """Strips narrower than the pitch (peec.py:1732-1820): widths, resistance widths, the self-inductance
+    change dL and the side-by-side mutual changes M_near equal the reference's."""
+    import scipy.sparse as sp
+    z, board = load("necked_pair")
+    st = oracle_stack(board)
+    assert np.array_equal(st.strip_width, z["strip_width"]) and np.array_equal(st.r_width, z["r_width"])
+    assert (st.strip_width < 1).sum() > 0 and rel(st.dL, z["dL"]) < 1e-12
+    ij = z["M_near_ij"]
+    ref = sp.coo_matrix((z["M_near"], (ij[0], ij[1])), shape=(st.ns, st.ns)).tocsr()
+    assert st.M_near.nnz == ref.nnz and abs(st.M_near - ref).max() <= 1e-12 * abs(ref).max()
