@@ -18,7 +18,7 @@ ROOT = HERE.parent
 SRC = HERE / "csrc"
 OUT = HERE / "libgtgb300.so"
 OBJ = HERE / "_build"
-UNITS = ["api.cu", "lp.cu", "stencil.cu", "factor.cu", "gmres.cu", "noalloc.cu", "coupling.cu", "outputs.cu", "spectra.cu", "woodbury.cu"]
+UNITS = ["api.cu", "lp.cu", "stencil.cu", "factor.cu", "gmres.cu", "noalloc.cu", "coupling.cu", "outputs.cu", "spectra.cu", "woodbury.cu", "narrow.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", f"-I{ROOT / 'include'}",
          "-Xptxas", "-warn-spills"]

@@ -201,6 +201,7 @@ struct gt_geometry {
     // the last n_lowrank branches are left out of the S-term map: a derived stack whose operators come from
     // gt_operators_derive (its base's factorisations plus a low-rank update)
     int n_lowrank = 0;
+    Narrow narrow{};
     std::vector<int> h_branch_nodes;
     uint64_t fsig = 0;  // signature of the factor structure (ordering, fronts, panel layout)
     std::unique_ptr<Workspace> ws;
@@ -401,6 +402,10 @@ static void matvec(gt_geometry* G, gt_operators* ops, const cx<R>* x, const cx<R
         Scope s(P, sizeof(R) == 4 ? "tail_f32" : "tail_f64", st,
                 ncol * (double)sizeof(cx<R>) * (2.0 * (G->geo.n - nXY) + nXY));
         launch_tail<R>(G->geo, x, rhs, out, ld, ncol, col_op, ops->zcap, ops->zbr, mode, col_list, st);
+    }
+    if (G->narrow.nrow) {
+        Scope s(P, "narrow", st);
+        launch_narrow<R>(G->narrow, x, out, ld, ncol, G->geo.S, col_op, ops->omega, ops->zs, mode, col_list, st);
     }
 }
 
@@ -924,6 +929,8 @@ void lp_with_scratch(gt_geometry* G, int ncol, const c64* x, c64* y, void* scrat
         a.mode = 2;
         launch_lp<double>(a, st);
     }
+    if (G->narrow.nrow)
+        launch_narrow<double>(G->narrow, x, y, G->geo.n, ncol, G->geo.S, nullptr, nullptr, nullptr, 2, nullptr, st);
 }
 
 }  // namespace gt
@@ -1010,9 +1017,40 @@ int gt_geometry_create(const gt_geometry_desc* d, gt_geometry** out) {
     g.perm = p.upload(d->perm, nn);
     g.nfac = d->n_factor;
     g.ntab = d->n_table;
-    g.tab_cap0 = 2 * (1 << S) * S * S;
+    if (d->n_override < 0) throw Invalid("n_override must not be negative");
+    g.tab_ovr0 = 2 * (1 << S) * S * S;
+    g.tab_cap0 = g.tab_ovr0 + d->n_override * S * S;
     g.tab_br0 = g.tab_cap0 + d->n_pairs;
     if (g.tab_br0 + d->n_branches != d->n_table) throw Invalid("admittance table length mismatch");
+    g.ovr_x = g.ovr_y = nullptr;
+    if (d->n_override > 0) {
+        if (!d->override_x || !d->override_y) throw Invalid("override positions missing");
+        for (size_t q = 0; q < (size_t)(nx - 1) * ny; ++q)
+            if (d->override_x[q] >= d->n_override) throw Invalid("override index out of range");
+        for (size_t q = 0; q < (size_t)nx * (ny - 1); ++q)
+            if (d->override_y[q] >= d->n_override) throw Invalid("override index out of range");
+        g.ovr_x = p.upload(d->override_x, (size_t)(nx - 1) * ny);
+        g.ovr_y = p.upload(d->override_y, (size_t)nx * (ny - 1));
+    }
+    if (d->n_narrow > 0) {
+        const int64_t nr = d->n_narrow, ne = d->narrow_ptr[nr];
+        for (int64_t q = 0; q < nr; ++q) {
+            if (d->narrow_pos[q] < d->off_x || d->narrow_pos[q] >= d->off_c || d->narrow_sheet[q] < 0 ||
+                d->narrow_sheet[q] >= S)
+                throw Invalid("narrow strip row out of range");
+        }
+        for (int64_t e = 0; e < ne; ++e)
+            if (d->narrow_col[e] < d->off_x || d->narrow_col[e] >= d->off_c) throw Invalid("narrow strip column out of range");
+        Narrow& nw = G->narrow;
+        nw.nrow = nr;
+        nw.pos = p.upload(d->narrow_pos, nr);
+        nw.sheet = p.upload(d->narrow_sheet, nr);
+        nw.rdelta = p.upload(d->narrow_rdelta, nr);
+        nw.dl = p.upload(d->narrow_dl, nr);
+        nw.ptr = p.upload(d->narrow_ptr, nr + 1);
+        nw.col = p.upload(d->narrow_col, std::max<int64_t>(ne, 1));
+        nw.val = p.upload(d->narrow_val, std::max<int64_t>(ne, 1));
+    }
     G->n_compact = d->n_compact;
     G->d_c2d = p.upload(d->compact_to_dense, d->n_compact);
     // the strips lead the compact order (x strips, y strips)

@@ -18,7 +18,29 @@ struct Geo {
     const int64_t* perm;         // dense node -> factor index or -1
     int64_t nfac;
     int ntab, tab_cap0, tab_br0;
+    // positions whose strips are not all full width (their own S x S blocks of D^-1 at tab_ovr0 + idx S S):
+    // per x / y strip position the block index or -1 (null: none)
+    const int* ovr_x;
+    const int* ovr_y;
+    int tab_ovr0;
 };
+
+// The narrow strips' corrections to the system product (narrow.cu): rows at dense positions pos[q] of sheet
+// sheet[q], resistance factor rdelta = 1/width - 1, self-inductance change dl (H), and the mutual changes
+// M[q, col[e]] = val[e] (H) for e in ptr[q] .. ptr[q+1]
+struct Narrow {
+    int64_t nrow = 0;
+    const int64_t* pos = nullptr;
+    const int* sheet = nullptr;
+    const double* rdelta = nullptr;
+    const double* dl = nullptr;
+    const int64_t* ptr = nullptr;
+    const int64_t* col = nullptr;
+    const double* val = nullptr;
+};
+template <typename R>
+void launch_narrow(const Narrow& nw, const cx<R>* x, cx<R>* out, int64_t ld, int ncol, int S, const int* col_op,
+                   const double* omega, const c64* zs, int mode, const int* col_list, cudaStream_t st);
 
 template <typename R> struct LpArgs {
     const cx<R>* x;

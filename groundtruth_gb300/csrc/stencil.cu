@@ -122,11 +122,11 @@ void launch_tail(const Geo& g, const cx<R>* x, const cx<R>* rhs, cx<R>* out, int
 }
 
 // D^-1 of the strips at one grid position applied to the S-vector u (sheets present: code); out[k] for the
-// sheets k present.  T: the table of the position's orientation.
+// sheets k present.  B: the position's S x S block (by its sheet code from the orientation's table, or the
+// position's own where its strips are not all full width).
 constexpr int SHEETS_MAX = 8;
 template <typename R, int MAXS>
-__device__ __forceinline__ void dinv_apply(const cx<R>* __restrict__ T, int S, int code, const cx<R>* u, cx<R>* out) {
-    const cx<R>* B = T + (int64_t)code * S * S;
+__device__ __forceinline__ void dinv_apply(const cx<R>* __restrict__ B, int S, int code, const cx<R>* u, cx<R>* out) {
 #pragma unroll
     for (int k = 0; k < MAXS; ++k) {
         out[k] = zero<R>();
@@ -181,7 +181,11 @@ __global__ void __launch_bounds__(256) pc_node_kernel(Geo g, const cx<R>* __rest
 #pragma unroll
         for (int side = 0; side < 4; ++side) {
             if (!code[side]) continue;
-            dinv_apply<R, MAXS>(T + (int64_t)(side < 2 ? 0 : 1) * NC * S * S, S, code[side], u[side], t);
+            const int* ovr = side < 2 ? g.ovr_x : g.ovr_y;
+            const int ob = ovr ? ovr[pq[side]] : -1;
+            dinv_apply<R, MAXS>(ob >= 0 ? T + g.tab_ovr0 + (int64_t)ob * S * S
+                                        : T + ((int64_t)(side < 2 ? 0 : 1) * NC + code[side]) * S * S,
+                                S, code[side], u[side], t);
             const bool plus = (side & 1) == 0;
 #pragma unroll
             for (int k = 0; k < MAXS; ++k)
@@ -259,7 +263,11 @@ __global__ void __launch_bounds__(256) pc_strip_kernel(Geo g, const cx<R>* __res
                 u[l] = (l < S && ((code >> l) & 1))
                            ? rc[seg + (int64_t)l * lstride + pq] + (yc[l * nxy + na] - yc[l * nxy + na + dn])
                            : zero<R>();
-            dinv_apply<R, MAXS>(T + (int64_t)(xo ? 0 : 1) * NC * S * S, S, code, u, t);
+            const int* ovr = xo ? g.ovr_x : g.ovr_y;
+            const int ob = ovr ? ovr[pq] : -1;
+            dinv_apply<R, MAXS>(ob >= 0 ? T + g.tab_ovr0 + (int64_t)ob * S * S
+                                        : T + ((int64_t)(xo ? 0 : 1) * NC + code) * S * S,
+                                S, code, u, t);
 #pragma unroll
             for (int k = 0; k < MAXS; ++k)
                 if (k < S) oc[seg + (int64_t)k * lstride + pq] = t[k];      // zero where the strip is absent

@@ -7,6 +7,7 @@ per-iteration work is in the CUDA library.  The formulas are GroundTruth's:
 * filament mutual inductance (Neumann, closed form)      src/groundtruth/solver/kernel.py:165-176
 * flat-tape mutual by the width-difference integral       src/groundtruth/solver/kernel.py:219-265
 * strip self inductance (numeric) / GMD formula           src/groundtruth/solver/kernel.py:179-206
+* narrow strips' self / side-by-side mutual changes      src/groundtruth/solver/peec.py:3309-3342
 * strip kernel: filaments far, tapes for |offset| <= 4    src/groundtruth/solver/kernel.py:268-294
 * one-face slab impedance, Dowell skin thickness          src/groundtruth/solver/kernel.py:23-75
 * vector potential of a filament, segment mutual          src/groundtruth/solver/kernel.py:297-337
@@ -80,6 +81,45 @@ def tape_mutual(length, wa, wb, axial, lateral, dz) -> float:
 
 def strip_self(length: float, width: float, thickness: float = 0.0) -> float:
     return float(filament_mutual(length, np.array(0.0), np.array(GMD_FLAT * (width + thickness))))
+
+
+def strip_self_numeric(length: float, width):
+    """A flat strip's partial self inductance as the mean filament mutual over its width pairs, by a graded
+    Gauss rule toward the coincident pair (kernel.py:187-206).  width may be an array."""
+    s, ws = _graded(0.0, 1.0, 0.0, PANELS, ORDER)
+    w = np.atleast_1d(np.asarray(width, float)).ravel()
+    u = w[:, None] * s[None, :]
+    out = 2.0 * (filament_mutual(length, 0.0, u) * ((1.0 - s) * ws)[None, :]).sum(axis=1)
+    return float(out[0]) if np.ndim(width) == 0 else out.reshape(np.shape(width))
+
+
+NEAR_AXIAL = 2      # peec.py:3325: side-by-side partial strips corrected up to this many strips along
+
+
+def narrow_self(d: float, phi, t):
+    """The partial self inductance a strip d long and phi*d wide (copper t thick) adds to the full square
+    strip's (peec.py:3309-3322): the numeric flat-strip integral's change and the GMD formula's thickness
+    change."""
+    phi, t = np.asarray(phi, float), np.asarray(t, float)
+
+    def thick(w):
+        return filament_mutual(d, 0.0, GMD_FLAT * w) - filament_mutual(d, 0.0, GMD_FLAT * (w + t))
+    return strip_self_numeric(d, phi * d) - strip_self_numeric(d, d) - thick(phi * d) + thick(d)
+
+
+def side_mutual(length: float, wa, wb, gap, steps=0.0, n: int = 8) -> np.ndarray:
+    """Mutual inductance of two flat coplanar parallel strips, widths wa and wb, centres gap apart across them
+    and `steps` lengths apart along them (fractions of `length`): the mean of n x n filament mutuals, touching
+    filaments a filament's GMD apart (peec.py:3328-3341)."""
+    wa, wb, gap, steps = (np.atleast_1d(v) for v in np.broadcast_arrays(*(np.asarray(v, float) for v in
+                                                                            (wa, wb, gap, steps))))
+    wa, wb, gap = wa * length, wb * length, gap * length
+    u = (np.arange(n) + 0.5) / n - 0.5
+    ya = wa[:, None, None] * u[None, :, None]
+    yb = gap[:, None, None] + wb[:, None, None] * u[None, None, :]
+    rho = np.maximum(np.abs(yb - ya), GMD_FLAT * np.maximum(wa, wb)[:, None, None] / n)
+    axial = np.broadcast_to((steps * length)[:, None, None], rho.shape)
+    return filament_mutual(length, axial, rho).mean(axis=(1, 2))
 
 
 def strip_kernel(n_axial: int, n_lateral: int, d: float, dz: float) -> np.ndarray:

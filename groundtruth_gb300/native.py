@@ -38,7 +38,10 @@ class GeometryDesc(C.Structure):
                 ("panel_total", C.c_int64), ("upd_total", C.c_int64), ("vec_total", C.c_int64),
                 ("ent_ptr", I64P), ("ent_row", I32P), ("ent_col", I32P), ("ent_s", I64P),
                 ("n_svalues", C.c_int64), ("n_table", C.c_int32), ("sterm_ptr", I64P), ("sterm_tab", I32P),
-                ("sterm_coef", DP), ("n_lowrank", C.c_int32)]
+                ("sterm_coef", DP), ("n_lowrank", C.c_int32),
+                ("n_override", C.c_int32), ("override_x", I32P), ("override_y", I32P),
+                ("n_narrow", C.c_int64), ("narrow_pos", I64P), ("narrow_sheet", I32P), ("narrow_rdelta", DP),
+                ("narrow_dl", DP), ("narrow_ptr", I64P), ("narrow_col", I64P), ("narrow_val", DP)]
 
 
 PRECISIONS = {"mixed": 0, "fp64": 1, "mixed16": 2}
@@ -164,6 +167,20 @@ class Geometry:
         d.sterm_tab = _ptr(arr(M.indices, np.int32), C.c_int32)
         d.sterm_coef = _ptr(arr(M.data, np.float64), C.c_double)
         d.n_lowrank = int(getattr(st, "n_lowrank", 0))
+        d.n_override = int(st.n_override)
+        if st.n_override:
+            d.override_x = _ptr(arr(st.override["x"].reshape(-1), np.int32), C.c_int32)
+            d.override_y = _ptr(arr(st.override["y"].reshape(-1), np.int32), C.c_int32)
+        nr = st.narrow_rows
+        d.n_narrow = len(nr["pos"])
+        if d.n_narrow:
+            d.narrow_pos = _ptr(arr(nr["pos"], np.int64), C.c_int64)
+            d.narrow_sheet = _ptr(arr(nr["sheet"], np.int32), C.c_int32)
+            d.narrow_rdelta = _ptr(arr(nr["rdelta"], np.float64), C.c_double)
+            d.narrow_dl = _ptr(arr(nr["dl"], np.float64), C.c_double)
+            d.narrow_ptr = _ptr(arr(nr["ptr"], np.int64), C.c_int64)
+            d.narrow_col = _ptr(arr(nr["col"] if len(nr["col"]) else np.zeros(1), np.int64), C.c_int64)
+            d.narrow_val = _ptr(arr(nr["val"] if len(nr["val"]) else np.zeros(1), np.float64), C.c_double)
         h = P()
         check(lib, lib.gt_geometry_create(C.byref(d), C.byref(h)), "gt_geometry_create")
         self.h = h

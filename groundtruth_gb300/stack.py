@@ -15,7 +15,8 @@ does the once-per-geometry index work (``layout``) and FP64 kernels (``greens``)
 per-frequency impedance tables.
 
 Scope: one current sheet per layer (``screen`` face sheets are not modelled: a stack that would split a
-layer raises NotImplementedError) and full-width strips (grids without wx/wy widths).
+layer raises NotImplementedError); strips narrower than the pitch (the grids' wx / wy, ox / oy, rx / ry) are
+modelled as the reference does (resistance over the width, dL, M_near, per-position preconditioner blocks).
 """
 from __future__ import annotations
 
@@ -52,8 +53,12 @@ class Grid:
     node: np.ndarray
     xb: np.ndarray
     yb: np.ndarray
-    wx: Optional[np.ndarray] = None
+    wx: Optional[np.ndarray] = None      # (nx-1, ny) copper width of each x strip, a fraction of d (None: full)
     wy: Optional[np.ndarray] = None
+    ox: Optional[np.ndarray] = None      # where that copper's centre lies across the strip, a fraction of d
+    oy: Optional[np.ndarray] = None
+    rx: Optional[np.ndarray] = None      # the width the strip's resistance takes (None / 0: its width)
+    ry: Optional[np.ndarray] = None
 
 
 @dataclass
@@ -189,8 +194,6 @@ class PlaneStack:
         for l in layers:
             if (l.grid.nx, l.grid.ny, l.grid.d) != (g0.nx, g0.ny, g0.d):
                 raise SolverError("all layers must share one grid")
-            if l.grid.wx is not None or l.grid.wy is not None:
-                raise NotImplementedError("strips narrower than the pitch (Grid.wx/wy) are not modelled")
         self.lib = native.load() if _device else None
         self._device = bool(_device)
         self.screen, self.leaf = screen, leaf
@@ -219,6 +222,7 @@ class PlaneStack:
         self.full_label, self.cond_label = t.full_label, t.cond_label
         self.dense = layout.dense_layout(t)
         self._kernels()
+        self._widths()
         self._schur_structure(leaf)
         self._lock = threading.Lock()
         self._ops: OrderedDict = OrderedDict()
@@ -288,6 +292,98 @@ class PlaneStack:
         if self.precond_mode == "sheet" and S > 1:
             self.B = {"x": greens.sheet_blocks(self.L_self, centre, sx), "y": greens.sheet_blocks(self.L_self, centre, sy)}
 
+    def _widths(self):
+        """Strips narrower than the pitch (peec.py:1732-1820): strip_width and r_width per strip (fractions of
+        the pitch), dL (the self-inductance change, None when every strip is full) and M_near (sparse side-by-side
+        mutual changes); then the device's view of them: the strip positions whose D^-1 blocks are their own
+        (override), and the rows of the system product's corrections."""
+        t, S = self.top, self.N
+        sx, sy = (self.nx - 1, self.ny), (self.nx, self.ny - 1)
+
+        def gather(attr, idx, shape, default):
+            if len(idx) == 0:
+                return np.zeros(0)
+            if all(getattr(l.grid, attr, None) is None for l in self.layers):
+                return np.full(len(idx), default)
+            w = np.stack([np.asarray(getattr(l.grid, attr), float) if getattr(l.grid, attr, None) is not None
+                          else np.full(shape, default) for l in self.layers])
+            return w[tuple(idx.T)]
+        w = np.concatenate([gather("wx", t.xa, sx, 1.0), gather("wy", t.ya, sy, 1.0)])
+        ok = w > 0
+        self.strip_width = np.where(ok, w, 1.0)
+        rw = np.concatenate([gather("rx", t.xa, sx, 0.0), gather("ry", t.ya, sy, 0.0)])
+        self.r_width = np.where(ok & (rw > 0), rw, self.strip_width)
+        off = np.where(ok, np.concatenate([gather("ox", t.xa, sx, 0.0), gather("oy", t.ya, sy, 0.0)]), 0.0)
+        self.dL = self.M_near = None
+        narrow = self.strip_width < 1.0
+        if np.any(narrow):
+            th = self.ts[np.concatenate([t.xa[:, 0], t.ya[:, 0]])]
+            dL = np.zeros(self.ns)
+            keys, inv = np.unique(np.round(np.column_stack([self.strip_width[narrow], th[narrow]]), 12), axis=0,
+                                  return_inverse=True)
+            dL[narrow] = greens.narrow_self(self.d, keys[:, 0], keys[:, 1])[np.ravel(inv)]
+            self.dL = dL
+            rows, cols, steps = [], [], []
+            for idx, shape, lo, axis in ((t.xa, sx, 0, 2), (t.ya, sy, self.nxb, 1)):
+                if len(idx) == 0:
+                    continue
+                at = -np.ones((S, *shape), np.int64)
+                at[tuple(idx.T)] = lo + np.arange(len(idx))
+                n_ax = shape[0] if axis == 2 else shape[1]
+                for k in range(-greens.NEAR_AXIAL, greens.NEAR_AXIAL + 1):
+                    if abs(k) >= n_ax:
+                        continue
+                    ax_a = slice(max(-k, 0), n_ax - max(k, 0))
+                    ax_b = slice(max(k, 0), n_ax - max(-k, 0))
+                    a = at[:, ax_a, :-1] if axis == 2 else at[:, :-1, ax_a]
+                    b = at[:, ax_b, 1:] if axis == 2 else at[:, 1:, ax_b]
+                    both = (a >= 0) & (b >= 0)
+                    a, b = a[both], b[both]
+                    part = narrow[a] | narrow[b]
+                    rows.append(a[part])
+                    cols.append(b[part])
+                    steps.append(np.full(int(part.sum()), abs(k)))
+            a, b = np.concatenate(rows), np.concatenate(cols)
+            if len(a):
+                k = np.concatenate(steps)
+                wa, wb = self.strip_width[a], self.strip_width[b]
+                gap = 1.0 + off[b] - off[a]
+                keys, inv = np.unique(np.round(np.column_stack([wa, wb, gap, k]), 9), axis=0, return_inverse=True)
+                one = np.ones(len(keys))
+                dM = (greens.side_mutual(self.d, keys[:, 0], keys[:, 1], keys[:, 2], keys[:, 3])
+                      - greens.side_mutual(self.d, one, one, one, keys[:, 3]))[np.ravel(inv)]
+                M = sp.coo_matrix((dM, (a, b)), shape=(self.ns, self.ns))
+                self.M_near = (M + M.T).tocsr()
+        # the device's view: positions with a strip that is not a full square get their own D^-1 block
+        odd = (self.strip_width != 1.0) | (self.r_width != 1.0)
+        if self.dL is not None:
+            odd |= self.dL != 0
+        self.override = {"x": -np.ones(sx, np.int32), "y": -np.ones(sy, np.int32)}
+        self.override_pos = []            # (orientation 0 / 1, i, j) per override block
+        for o, (name, idx, lo) in enumerate((("x", t.xa, 0), ("y", t.ya, self.nxb))):
+            if len(idx) == 0:
+                continue
+            sel = odd[lo: lo + len(idx)]
+            pos = np.unique(idx[sel][:, 1:], axis=0)
+            for i, j in pos:
+                self.override[name][i, j] = len(self.override_pos)
+                self.override_pos.append((o, int(i), int(j)))
+        self.n_override = len(self.override_pos)
+        # correction rows: strips with a resistance factor, a self change or side-by-side changes
+        rows = np.flatnonzero(odd | (np.diff(self.M_near.indptr) > 0 if self.M_near is not None
+                                     else np.zeros(self.ns, bool)))
+        c2d = self.dense.compact_to_dense
+        M = self.M_near[rows] if self.M_near is not None else sp.csr_matrix((len(rows), max(self.ns, 1)))
+        self.narrow_rows = {
+            "pos": c2d[rows].astype(np.int64),
+            "sheet": np.concatenate([t.xa[:, 0], t.ya[:, 0]])[rows].astype(np.int32) if len(rows) else np.zeros(0, np.int32),
+            "rdelta": 1.0 / self.r_width[rows] - 1.0,
+            "dl": self.dL[rows] if self.dL is not None else np.zeros(len(rows)),
+            "ptr": M.indptr.astype(np.int64),
+            "col": c2d[M.indices].astype(np.int64),
+            "val": M.data.astype(np.float64),
+        }
+
     def _schur_structure(self, leaf: int):
         """S = Ar^T D^-1 Ar as a linear map of the per-frequency admittance table, and its symbolic analysis."""
         t, S, nx, ny = self.top, self.N, self.nx, self.ny
@@ -298,7 +394,8 @@ class PlaneStack:
         for k in range(S):
             self.code["x"] |= (t.xb[k].astype(np.uint8) << k)
             self.code["y"] |= (t.yb[k].astype(np.uint8) << k)
-        self.tab_cap0 = 2 * ncode * S * S
+        self.tab_ovr0 = 2 * ncode * S * S
+        self.tab_cap0 = self.tab_ovr0 + self.n_override * S * S
         self.tab_br0 = self.tab_cap0 + len(t.pair_layers)
         self.n_table = self.tab_br0 + self.nbr
         kept_of_nid = -np.ones(t.n_nodes, np.int64)
@@ -327,7 +424,8 @@ class PlaneStack:
                 else:                              # blocks: every strip present at the same position
                     ll = np.full(len(k), l)
                     sel = (code >> l) & 1 == 1
-                tab = ((o * ncode + code) * S + k) * S + ll
+                ovr = self.override["x" if o == 0 else "y"][i, j].astype(np.int64)
+                tab = np.where(ovr >= 0, self.tab_ovr0 + (ovr * S + k) * S + ll, ((o * ncode + code) * S + k) * S + ll)
                 e1 = (ends1[0][sel], ends1[1][sel])
                 e2 = (t.nid[ll[sel], i[sel], j[sel]], t.nid[ll[sel], i[sel] + di, j[sel] + dj])
                 add(e1, e2, tab[sel])
@@ -453,9 +551,37 @@ class PlaneStack:
                     for k in lay:
                         blk[k, k] = dself[k]
                 tab[(o * ncode + code) * S * S: (o * ncode + code + 1) * S * S] = blk.ravel()
+        if self.n_override:
+            self._override_blocks(tab, w, zs, dself)
         tab[self.tab_cap0: self.tab_br0] = 1.0 / zcap if len(pl) else []
         tab[self.tab_br0:] = 1.0 / zbr if self.nbr else []
         return w, zs, zcap, zbr, tab
+
+    def _override_blocks(self, tab: np.ndarray, w: float, zs: np.ndarray, dself: np.ndarray):
+        """D^-1 blocks of the positions whose strips are not all full squares (peec.py:2480-2509: each such
+        position its own R / width and self inductance + dL; a sheet block where two or more strips share it)."""
+        t, S = self.top, self.N
+        sidx = {}
+        for name, idx, lo in (("x", t.xa, 0), ("y", t.ya, self.nxb)):
+            a = -np.ones((S, *self.override[name].shape), np.int64)
+            if len(idx):
+                a[tuple(idx.T)] = lo + np.arange(len(idx))
+            sidx[name] = a
+        dL = self.dL if self.dL is not None else np.zeros(self.ns)
+        for q, (o, i, j) in enumerate(self.override_pos):
+            name = "xy"[o]
+            strips = sidx[name][:, i, j]
+            lay = [k for k in range(S) if strips[k] >= 0]
+            st_ = strips[lay]
+            R = zs[lay] / self.r_width[st_]
+            blk = np.zeros((S, S), complex)
+            if self.sheet and len(lay) >= 2:
+                Z = 1j * w * self.B[name][np.ix_(lay, lay)] + np.diag(R + 1j * w * dL[st_])
+                blk[np.ix_(lay, lay)] = np.linalg.inv(Z)
+            else:
+                for k, sq, r in zip(lay, st_, R):
+                    blk[k, k] = 1.0 / (r + 1j * w * (self.L_self + dL[sq]))
+            tab[self.tab_ovr0 + q * S * S: self.tab_ovr0 + (q + 1) * S * S] = blk.ravel()
 
     def operator(self, f: float):
         """The device operator (factorised Schur complement) at f's key, made once and cached."""
@@ -717,7 +843,8 @@ def solve_many(excitations: list, freqs, tol: float = 1e-5, **kw) -> list:
 
 def from_board(board, _device: bool = True):
     """A PlaneStack and its RouteExcitations for a ``synth.Board`` (the workloads' boards)."""
-    grids = [Grid(0.0, 0.0, board.d * 1e3, board.nx, board.ny, l.node, l.xb, l.yb) for l in board.layers]
+    grids = [Grid(0.0, 0.0, board.d * 1e3, board.nx, board.ny, l.node, l.xb, l.yb, **(l.widths or {}))
+             for l in board.layers]
     layers = [PlaneLayer(l.name, l.z, g, l.thickness) for l, g in zip(board.layers, grids)]
     branches = [Branch(b.a, b.b, b.z, f"br{n}", b.kind, b.radius) for n, b in enumerate(board.branches)]
     pairs = [PlanePair(p.upper, p.lower, p.c_per_area, p.tan_delta) for p in board.pairs]

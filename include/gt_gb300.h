@@ -78,6 +78,24 @@ typedef struct gt_geometry_desc {
      * left out of the S-term map, whose Schur structure is its base's; its operators come from
      * gt_operators_derive.  0 for every other geometry. */
     int32_t n_lowrank;
+    /* Strips narrower than the pitch (PlaneStack._widths, peec.py:1732-1820); all zero / NULL when every strip
+     * is full width.  n_override positions have their own S x S blocks of D^-1 in the admittance table, right
+     * after the code blocks (before the capacitances); override_x / override_y: [(nx-1)*ny] / [nx*(ny-1)] the
+     * block index of each strip position or -1.  The system product's corrections, per row q (n_narrow rows):
+     * dense position narrow_pos, sheet narrow_sheet, resistance factor narrow_rdelta = 1/width - 1, self
+     * inductance change narrow_dl (H) and mutual changes narrow_val (H) with the dense columns narrow_col of
+     * entries narrow_ptr[q] .. narrow_ptr[q+1] (the side-by-side neighbours, M_near). */
+    int32_t n_override;
+    const int32_t* override_x;
+    const int32_t* override_y;
+    int64_t n_narrow;
+    const int64_t* narrow_pos;
+    const int32_t* narrow_sheet;
+    const double* narrow_rdelta;
+    const double* narrow_dl;
+    const int64_t* narrow_ptr;
+    const int64_t* narrow_col;
+    const double* narrow_val;
 } gt_geometry_desc;
 
 typedef struct gt_solve_opts {
