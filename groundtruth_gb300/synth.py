@@ -152,6 +152,7 @@ class Board:
     tol: float = 1e-10
     restart: int = 50
     sigma: float = SIGMA_CU
+    screen: bool = False          # split layers with copper above and below into two face sheets
 
     # -- flat arrays (fixtures, the C-ABI) -----------------------------------------------------------
     def to_arrays(self) -> dict:
@@ -166,7 +167,7 @@ class Board:
                "branch_ab": np.array([[*b.a, *b.b] for b in self.branches], np.int64).reshape(-1, 6),
                "branch_rlc": np.array([[b.R, b.L, b.C, b.radius] for b in self.branches], float).reshape(-1, 4),
                "branch_via": np.array([b.kind == "via" for b in self.branches], bool),
-               "net_count": np.int64(len(self.nets))}
+               "net_count": np.int64(len(self.nets)), "screen": np.bool_(self.screen)}
         for k, l in enumerate(self.layers):
             for key, v in (l.widths or {}).items():
                 out[f"layer{k}_{key}"] = np.asarray(v, float)
@@ -195,7 +196,7 @@ class Board:
                             tuple(int(v) for v in e[3:]), float(a[f"net{n}_trace_t"])))
         return Board(str(a["name"]), float(a["d"]), int(a["nx"]), int(a["ny"]), layers, pairs, branches, nets,
                      np.asarray(a["freqs"], float), str(a["precond"]), float(a["tol"]), int(a["restart"]),
-                     float(a["sigma"]))
+                     float(a["sigma"]), bool(a["screen"]) if "screen" in files else False)
 
 
 def _full_layer(name, z, t, nx, ny, d, cutouts=()):
@@ -452,6 +453,16 @@ def _labels(mask: np.ndarray, xb: np.ndarray, yb: np.ndarray) -> np.ndarray:
 WIDTH_KEYS = ("wx", "wy", "ox", "oy", "rx", "ry")
 
 
+def faces_stack3(precond: str = "diag") -> Board:
+    """small_stack3 with screening on: its middle plane has copper above and below, so it is split into two
+    face sheets (PlaneStack._faces, peec.py:1658-1697): four current sheets on three layers."""
+    b = small_stack3()
+    b.name = f"faces_stack3_{precond}"
+    b.precond = precond
+    b.screen = True
+    return b
+
+
 def necked_pair(seed: int = 17) -> Board:
     """A plane pair (40 x 36 at 0.5 mm) whose PWR plane has an island joined to the rest by a neck narrower
     than the pitch, with seeded narrow, off-centre and series-narrowed strips along the moat (the exact-copper
@@ -583,4 +594,5 @@ def what_if_branches(board: Board, seed: int, n_via: int = 2, n_part: int = 1) -
 
 
 WORKLOADS = {"plain_plane": plain_plane, "slotted_pair": slotted_pair, "small_pair": small_pair,
-             "small_stack3": small_stack3, "six_sheet": six_sheet, "necked_pair": necked_pair}
+             "small_stack3": small_stack3, "six_sheet": six_sheet, "necked_pair": necked_pair,
+             "faces_stack3": faces_stack3}

@@ -347,6 +347,37 @@ def gmres(op: Callable, b: np.ndarray, tol: float, max_cycles: int = 8, restart:
     return x, its, bool(np.linalg.norm(r) <= tol * bnorm)
 
 
+SCREEN_MIN_NODES = 16   # peec.py: a layer with this many nodes under copper above and below is split into faces
+
+
+def slab_modes(t, f, sigma, free_space: bool = False):
+    """(zs, zd) of a slab t thick in units of 1/(sigma t): u coth(u/2) and u tanh(u/2), u = (1 + j) t / delta; with
+    free_space the difference mode beside the free space between two face sheets, u^2 tanh(u/2) / (u - 2 tanh(u/2));
+    thin foils (t / delta < 0.1) by their series (kernel.py:130-152)."""
+    t = np.asarray(t, float)
+    f = np.asarray(f, float)
+    with np.errstate(divide="ignore", over="ignore", invalid="ignore"):
+        delta = 1.0 / np.sqrt(np.pi * np.maximum(f, 1e-300) * MU0 * sigma)
+        x = np.where(f > 0, t / delta, 0.0)
+        u = (1 + 1j) * x
+        th = np.tanh(np.where(x > 0, (1 + 1j) * np.minimum(x, 60.0), 1.0) / 2)
+        small = x < 0.1
+        zs = np.where(small, 2.0 + x ** 4 / 90.0 + 1j * (x ** 2 / 3.0 - x ** 6 / 1890.0), u / th)
+        if free_space:
+            zd = np.where(small, 6.0 + x ** 4 / 350.0 + 1j * x ** 2 / 5.0, u * u * th / (u - 2.0 * th))
+        else:
+            zd = np.where(small, x ** 4 / 6.0 + 1j * (x ** 2 - x ** 6 / 30.0), u * th)
+    return zs, zd
+
+
+def face_sheet_impedance(t, f, sigma):
+    """(z_self, z_mutual) per square of a slab's two face sheets t apart with free space between them
+    (kernel.py:102-127)."""
+    t = np.asarray(t, float)
+    zs, zdm = slab_modes(t, f, sigma, free_space=True)
+    return 0.5 * (zs + zdm) / (sigma * t), 0.5 * (zs - zdm) / (sigma * t)
+
+
 NEAR_AXIAL = 2      # peec.py:3325: side-by-side partial strips corrected up to this many strips along
 
 
@@ -428,7 +459,7 @@ class OracleStack:
     """Everything of peec.PlaneStack the scope needs: topology, kernels, per-frequency operators, products."""
 
     def __init__(self, layers: list, d: float, branches=None, pairs=None, sigma: float = SIGMA_CU,
-                 precond: str = "diag"):
+                 precond: str = "diag", screen: bool = False):
         if precond not in ("diag", "sheet"):
             raise ValueError("precond must be 'diag' or 'sheet'")
         self.layers = list(layers)
@@ -439,11 +470,66 @@ class OracleStack:
         self.sigma = sigma
         self.pairs = list(pairs or [])
         self.precond_mode = precond
-        self.sheet_t = np.array([l.thickness for l in layers], float)
+        self.screen = screen
+        self.layer_t = np.array([l.thickness for l in layers], float)
         self._base: Optional[OracleStack] = None
         self._topology(list(branches or []))
         self._kernels()
         self._widths()
+
+    # -- face sheets of screened layers (peec.py:1658-1723)
+    def _faces(self, node: np.ndarray):
+        """twin_parent, n_sheets, sheet_layer, sheet_z, sheet_t (peec.py:1658-1697)."""
+        N = self.N
+        t = self.layer_t
+        twins = []
+        if self.screen and N >= 3:
+            for k in range(N):
+                above = np.zeros(node.shape[1:], bool)
+                below = np.zeros(node.shape[1:], bool)
+                for m in range(N):
+                    if self.zs[m] > self.zs[k]:
+                        above |= node[m]
+                    elif self.zs[m] < self.zs[k]:
+                        below |= node[m]
+                if int(np.count_nonzero(node[k] & above & below)) >= SCREEN_MIN_NODES:
+                    twins.append(k)
+        self.twin_parent = np.array(twins, np.int64)
+        self.n_sheets = N + len(twins)
+        self.sheet_layer = np.concatenate([np.arange(N), self.twin_parent]).astype(np.int64)
+        z = self.zs.copy()
+        st = t.copy()
+        z[twins] = self.zs[twins] + 0.5 * t[twins]
+        st[twins] = 0.0
+        self.sheet_z = np.concatenate([z, self.zs[twins] - 0.5 * t[twins]])
+        self.sheet_t = np.concatenate([st, np.zeros(len(twins))])
+
+    def _twins(self):
+        """tw_a / tw_b: each split layer's upper-face strips and the twin's (peec.py:1699-1716)."""
+        N = self.N
+        a, b = [], []
+        for xb, lo in ((self.xb, 0), (self.yb, self.nxb)):
+            per = np.count_nonzero(xb.reshape(self.n_sheets, -1), axis=1)
+            start = lo + np.concatenate([[0], np.cumsum(per)[:-1]])
+            for m, p in enumerate(self.twin_parent):
+                a.append(start[p] + np.arange(per[p]))
+                b.append(start[N + m] + np.arange(per[p]))
+        self.tw_a = np.concatenate(a).astype(np.int64) if a else np.zeros(0, np.int64)
+        self.tw_b = np.concatenate(b).astype(np.int64) if b else np.zeros(0, np.int64)
+
+    def layer_index(self, orient: str) -> np.ndarray:
+        """The orientation's strips as (layer, i, j) rows (peec.py:1718-1729)."""
+        idx = (self.xa if orient == "x" else self.ya).copy()
+        idx[:, 0] = self.sheet_layer[idx[:, 0]]
+        return idx
+
+    def sheet_of_strip(self, strips: np.ndarray) -> np.ndarray:
+        strips = np.asarray(strips, np.int64)
+        out = np.empty(len(strips), np.int64)
+        x = strips < self.nxb
+        out[x] = self.xa[strips[x], 0]
+        out[~x] = self.ya[strips[~x] - self.nxb, 0]
+        return out
 
     # -- strips narrower than the pitch (peec.py:1732-1820, 3309-3342)
     def _widths(self):
@@ -457,19 +543,20 @@ class OracleStack:
                           else np.full(shape, default) for l in self.layers])
             return w[tuple(idx.T)]
         sx, sy = (self.nx - 1, self.ny), (self.nx, self.ny - 1)
-        w = np.concatenate([gather("wx", self.xa, sx, 1.0), gather("wy", self.ya, sy, 1.0)])
+        lx, ly = self.layer_index("x"), self.layer_index("y")
+        w = np.concatenate([gather("wx", lx, sx, 1.0), gather("wy", ly, sy, 1.0)])
         ok = w > 0
         self.strip_width = np.where(ok, w, 1.0)
-        rw = np.concatenate([gather("rx", self.xa, sx, 0.0), gather("ry", self.ya, sy, 0.0)])
+        rw = np.concatenate([gather("rx", lx, sx, 0.0), gather("ry", ly, sy, 0.0)])
         self.r_width = np.where(ok & (rw > 0), rw, self.strip_width)
         self.r_uniform = not np.any(self.r_width != 1.0)
-        off = np.where(ok, np.concatenate([gather("ox", self.xa, sx, 0.0), gather("oy", self.ya, sy, 0.0)]), 0.0)
+        off = np.where(ok, np.concatenate([gather("ox", lx, sx, 0.0), gather("oy", ly, sy, 0.0)]), 0.0)
         self.dL = self.M_near = None
         narrow = self.strip_width < 1.0
         if not np.any(narrow):
             return
         d = self.d
-        t = self.sheet_t[np.concatenate([self.xa[:, 0], self.ya[:, 0]])]
+        t = self.layer_t[np.concatenate([lx[:, 0], ly[:, 0]])]
         dL = np.zeros(self.ns)
         keys, inv = np.unique(np.round(np.column_stack([self.strip_width[narrow], t[narrow]]), 12), axis=0,
                               return_inverse=True)
@@ -479,7 +566,7 @@ class OracleStack:
         for idx, shape, lo, axis in ((self.xa, sx, 0, 2), (self.ya, sy, self.nxb, 1)):
             if len(idx) == 0:
                 continue
-            at = -np.ones((self.N, *shape), np.int64)
+            at = -np.ones((self.n_sheets, *shape), np.int64)
             at[tuple(idx.T)] = lo + np.arange(len(idx))
             n_ax = shape[0] if axis == 2 else shape[1]
             for k in range(-NEAR_AXIAL, NEAR_AXIAL + 1):
@@ -497,6 +584,7 @@ class OracleStack:
                 steps.append(np.full(int(part.sum()), abs(k)))
         a, b = np.concatenate(rows), np.concatenate(cols)
         if len(a) == 0:
+            self._twin_corrections()
             return
         k = np.concatenate(steps)
         wa, wb = self.strip_width[a], self.strip_width[b]
@@ -507,6 +595,19 @@ class OracleStack:
               - side_mutual(d, ones, ones, ones, keys[:, 3]))[np.ravel(inv)]
         M = sp.coo_matrix((dM, (a, b)), shape=(self.ns, self.ns))
         self.M_near = (M + M.T).tocsr()
+        self._twin_corrections()
+
+    def _twin_corrections(self):
+        """A split layer's faces share their copper's narrow-width corrections (peec.py:1822-1843)."""
+        if self.dL is None or not len(self.tw_b):
+            return
+        n = self.ns
+        pairs = np.concatenate([self.tw_a, self.tw_b]), np.concatenate([self.tw_b, self.tw_a])
+        extra = sp.coo_matrix((np.concatenate([self.dL[self.tw_a], self.dL[self.tw_b]]), pairs), shape=(n, n))
+        if self.M_near is not None:
+            swap = sp.coo_matrix((np.ones(len(pairs[0])), pairs), shape=(n, n)).tocsr()
+            extra = extra + self.M_near @ swap
+        self.M_near = ((self.M_near if self.M_near is not None else 0) + extra).tocsr()
 
     def with_branches(self, extra: list) -> "OracleStack":
         """This stack plus a few branches (peec.py:1871-1912): a shallow copy sharing the grids and kernels with
@@ -538,8 +639,11 @@ class OracleStack:
     def _topology(self, branches):
         node = np.stack([l.node for l in self.layers])
         self.node = node
-        self.xb = np.stack([l.xb for l in self.layers]) & node[:, :-1, :] & node[:, 1:, :]
-        self.yb = np.stack([l.yb for l in self.layers]) & node[:, :, :-1] & node[:, :, 1:]
+        xb = np.stack([l.xb for l in self.layers]) & node[:, :-1, :] & node[:, 1:, :]
+        yb = np.stack([l.yb for l in self.layers]) & node[:, :, :-1] & node[:, :, 1:]
+        self._faces(node)
+        self.xb = np.concatenate([xb, xb[self.twin_parent]]) if len(self.twin_parent) else xb
+        self.yb = np.concatenate([yb, yb[self.twin_parent]]) if len(self.twin_parent) else yb
         self.nid = -np.ones(node.shape, np.int64)
         idx = np.nonzero(node)
         self.nid[idx] = np.arange(len(idx[0]))
@@ -547,6 +651,7 @@ class OracleStack:
         self.xa, self.ya = np.argwhere(self.xb), np.argwhere(self.yb)
         self.nxb, self.nyb = len(self.xa), len(self.ya)
         self.ns = self.nxb + self.nyb
+        self._twins()
         cap = []
         cell = self.d ** 2
         for p in self.pairs:
@@ -562,7 +667,7 @@ class OracleStack:
         self.nbr = len(self.branches)
         self.nb = self.ns + self.ncap + self.nbr
         cu = self.cap[:, :4].astype(np.int64)
-        xa, ya = self.xa, self.ya
+        xa, ya = self.layer_index("x"), self.layer_index("y")       # a strip joins its layer's nodes
         self.a_nodes = np.concatenate([self.nid[tuple(xa.T)], self.nid[tuple(ya.T)], self.nid[cu[:, 0], cu[:, 2], cu[:, 3]],
                                        np.array([self.nid[b.a] for b in self.branches], np.int64)]).astype(np.int64)
         self.b_nodes = np.concatenate([self.nid[xa[:, 0], xa[:, 1] + 1, xa[:, 2]], self.nid[ya[:, 0], ya[:, 1], ya[:, 2] + 1],
@@ -586,14 +691,15 @@ class OracleStack:
         self.ArT = self.Ar.T.tocsr()
 
     def face_gap(self, s: int, t: int) -> float:
-        """peec.py:1926-1933 (one sheet per layer)."""
+        """The distance between the faces sheets s and t turn to each other (peec.py:1926-1933)."""
         if s == t:
             return 0.0
-        return max(abs(self.zs[s] - self.zs[t]) - 0.5 * (self.sheet_t[s] + self.sheet_t[t]), 1e-6)
+        return max(abs(self.sheet_z[s] - self.sheet_z[t]) - 0.5 * (self.sheet_t[s] + self.sheet_t[t]), 1e-6)
 
     # -- kernels (peec.py:1941-1988)
     def _kernels(self):
-        nx, ny, d, N = self.nx, self.ny, self.d, self.N
+        """Spectra for every sheet pair, the self term and the 'sheet' blocks (peec.py:1941-2028)."""
+        nx, ny, d, N = self.nx, self.ny, self.d, self.n_sheets
         self.Px = (next_fast_len(2 * (nx - 1) - 1), next_fast_len(2 * ny - 1))
         self.Py = (next_fast_len(2 * nx - 1), next_fast_len(2 * (ny - 1) - 1))
         Kx = np.empty((self.Px[0] // 2 + 1, self.Px[1] // 2 + 1, N, N))
@@ -614,14 +720,49 @@ class OracleStack:
         self.Kq = {"x": Kx, "y": Ky}
         self.centre, self.sum_x, self.sum_y = centre, sum_x, sum_y
         self.blocks = []
-        if self.precond_mode == "sheet" and N > 1:
-            self.B_x = sheet_blocks(self.L_self, centre, sum_x)
-            self.B_y = sheet_blocks(self.L_self, centre, sum_y)
+        if self.precond_mode == "sheet" and self.N > 1:
+            self.B_x = self._sheet_block(centre, sum_x)
+            self.B_y = self._sheet_block(centre, sum_y)
             self._block_layout()
+        elif len(self.twin_parent):
+            # 'diag' with split layers: each face pair at a position is a 2 x 2 block (peec.py:1979-1987)
+            B = np.diag(np.full(N, self.L_self))
+            for m, p in enumerate(self.twin_parent):
+                B[p, self.N + m] = B[self.N + m, p] = centre[p, self.N + m]
+            self.B_x = self.B_y = B
+            self._twin_blocks()
+
+    def _sheet_block(self, centre: np.ndarray, sums: np.ndarray) -> np.ndarray:
+        """'sheet' blocks made over the layers, a split layer's twin taking its layer's row and column with the
+        faces' own difference L_self - M_twin kept (peec.py:1989-2010)."""
+        N = self.N
+        B = sheet_blocks(self.L_self, centre[:N, :N], sums[:N, :N])
+        if not len(self.twin_parent):
+            return B
+        lay = self.sheet_layer
+        full = B[np.ix_(lay, lay)].copy()
+        for m, p in enumerate(self.twin_parent):
+            tw = N + m
+            gap = max(self.L_self - centre[p, tw], 0.0)
+            for j in range(self.n_sheets):
+                if lay[j] == p and j != tw:
+                    full[tw, j] = full[j, tw] = B[p, p] - gap
+        return full
+
+    def _twin_blocks(self):
+        """peec.py:2012-2021."""
+        N = self.N
+        nx_a = self.tw_a < self.nxb
+        for m, p in enumerate(self.twin_parent):
+            mine = self.sheet_of_strip(self.tw_b) == N + m
+            for orient, sel in (("x", nx_a), ("y", ~nx_a)):
+                pick = mine & sel
+                if pick.any():
+                    self.blocks.append((np.column_stack([self.tw_a[pick], self.tw_b[pick]]), [int(p), N + m], orient))
 
     def _block_layout(self):
         """peec.py:2032-2052."""
-        S = self.N
+        S = self.n_sheets
         for idx, mask, off, orient in ((self.xa, self.xb, 0, "x"), (self.ya, self.yb, self.nxb, "y")):
             if len(idx) == 0:
                 continue
@@ -656,7 +797,7 @@ class OracleStack:
     # -- L_p product (peec.py:2054-2135; FFTs on all host cores as fft_workers() = -1, peec.py:136-138)
     def Lp_matvec(self, I_s: np.ndarray) -> np.ndarray:
         out = np.empty(self.ns, complex)
-        S = self.N
+        S = self.n_sheets
         for orient, idx, lo, hi, shape, P in (("x", self.xa, 0, self.nxb, (S, self.nx - 1, self.ny), self.Px),
                                               ("y", self.ya, self.nxb, self.ns, (S, self.nx, self.ny - 1), self.Py)):
             if hi <= lo:
@@ -680,8 +821,13 @@ class OracleStack:
     def impedances(self, f: float):
         w = 2 * math.pi * f
         zs = np.array([complex(slab_impedance(l.thickness, f, self.sigma)) for l in self.layers])
-        R_strip = (np.concatenate([zs[self.xa[:, 0]], zs[self.ya[:, 0]]]) / self.r_width if self.ns
+        lay = self.sheet_layer
+        R_strip = (np.concatenate([zs[lay[self.xa[:, 0]]], zs[lay[self.ya[:, 0]]]]) / self.r_width if self.ns
                    else np.zeros(0, complex))
+        if len(self.tw_b):           # a split layer's face strips: the face pair's own impedance (peec.py:2161-2166)
+            z_self = np.asarray(face_sheet_impedance(self.layer_t, f, self.sigma)[0])
+            for tw in (self.tw_a, self.tw_b):
+                R_strip[tw] = z_self[lay[self.sheet_of_strip(tw)]] / self.r_width[tw]
         if self.ncap:
             C, tand = self.cap[:, 4], self.cap[:, 5]
             z_cap = 1.0 / (w * C * tand + 1j * w * C) if w > 0 else np.full(self.ncap, 1e18 + 0j)
@@ -690,25 +836,47 @@ class OracleStack:
         z_br = np.array([b.z(f) for b in self.branches], complex)
         return w, R_strip, np.concatenate([z_cap, z_br])
 
-    def admittance(self, w, R_strip, z_tail) -> sp.csr_matrix:
-        """peec.py:2465-2511 (no face sheets)."""
+    def twin_z(self, f: float) -> Optional[np.ndarray]:
+        """The face coupling impedance per twin pair: z_mutual of the face pair / the strip's width
+        (peec.py:2186-2197); None without split layers."""
+        if not len(self.tw_b):
+            return None
+        z_mut = np.asarray(face_sheet_impedance(self.layer_t, f, self.sigma)[1])
+        return z_mut[self.sheet_layer[self.sheet_of_strip(self.tw_b)]] / self.r_width[self.tw_b]
+
+    def admittance(self, w, R_strip, z_tail, Z12=None) -> sp.csr_matrix:
+        """peec.py:2465-2511."""
         L_own = self.L_self if self.dL is None else self.L_self + self.dL
         d = np.concatenate([1.0 / (R_strip + 1j * w * L_own), 1.0 / z_tail])
         if not self.blocks:
             return sp.diags(d).tocsr()
+        z12 = None
+        if Z12 is not None:
+            z12 = np.zeros(self.ns, complex)
+            z12[self.tw_b] = Z12
         rows, cols, vals = [np.arange(self.nb)], [np.arange(self.nb)], [d]
         in_block = np.zeros(self.nb, bool)
         for strips, layers, orient in self.blocks:
             B = (self.B_x if orient == "x" else self.B_y)[np.ix_(layers, layers)]
             m = len(layers)
+            faces = [(layers.index(int(self.sheet_layer[s])), k) for k, s in enumerate(layers)
+                     if s >= self.N and int(self.sheet_layer[s]) in layers] if z12 is not None else []
             if self.dL is None and self.r_uniform:       # every position alike: one inverse
                 R = np.diag([R_strip[strips[0, k]] for k in range(m)]).astype(complex)
+                for ia, ib in faces:
+                    R[ia, ib] = R[ib, ia] = z12[strips[0, ib]]
                 Zi = np.linalg.inv(R + 1j * w * B)
                 Zi = np.broadcast_to(Zi.ravel(), (len(strips), m * m)).ravel()
             else:                                           # each position its own R and self inductance
                 Z = np.broadcast_to(1j * w * B, (len(strips), m, m)).copy()
                 Z[:, np.arange(m), np.arange(m)] += R_strip[strips] + (
                     0.0 if self.dL is None else 1j * w * self.dL[strips])
+                for ia, ib in faces:
+                    cross = z12[strips[:, ib]]
+                    if self.dL is not None:
+                        cross = cross + 1j * w * self.dL[strips[:, ib]]
+                    Z[:, ia, ib] += cross
+                    Z[:, ib, ia] += cross
                 Zi = np.linalg.inv(Z).ravel()
             rows.append(np.repeat(strips, m, axis=1).ravel())
             cols.append(np.tile(strips, (1, m)).ravel())
@@ -722,7 +890,8 @@ class OracleStack:
         """The system data and the SuperLU-factorised Schur complement at f (own factorisation, no borrowing)."""
         f = cache_value(f)
         w, R_strip, z_tail = self.impedances(f)
-        Dinv = self.admittance(w, R_strip, z_tail)
+        Z12 = self.twin_z(f)
+        Dinv = self.admittance(w, R_strip, z_tail, Z12)
         if self._base is not None:
             # a derived stack: S = S_base + U diag(1/z_new) U^T, solved by the Woodbury identity on the base's
             # factorisation (peec.py:2354-2377); only a k x k matrix is inverted
@@ -736,11 +905,12 @@ class OracleStack:
                 y = b(v)
                 return y - SiU @ (small_inv @ (Ut @ y))
             return {"f": f, "w": w, "R_strip": R_strip, "z_tail": z_tail, "Dinv": Dinv, "S": None,
-                    "solve_S": solve_S}
+                    "solve_S": solve_S, "Z12": Z12}
         S = (self.ArT @ Dinv @ self.Ar).tocsc()
         lu = splu(S, permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=LU_PIVOT_THRESHOLD,
                   options={"SymmetricMode": True})
-        return {"f": f, "w": w, "R_strip": R_strip, "z_tail": z_tail, "Dinv": Dinv, "S": S, "solve_S": lu.solve}
+        return {"f": f, "w": w, "R_strip": R_strip, "z_tail": z_tail, "Dinv": Dinv, "S": S, "solve_S": lu.solve,
+                "Z12": Z12}
 
     def matvec(self, op: dict, x: np.ndarray) -> np.ndarray:
         """[Z I - Ar V; Ar^T I] (peec.py:3043-3062)."""
@@ -748,6 +918,9 @@ class OracleStack:
         Ib = x[:nb]
         top = np.empty(nb, complex)
         top[:ns] = op["R_strip"] * Ib[:ns] + 1j * op["w"] * self.Lp_matvec(Ib[:ns])
+        if op.get("Z12") is not None:         # a split layer's faces: the slab two-port's coupling
+            top[self.tw_a] += op["Z12"] * Ib[self.tw_b]
+            top[self.tw_b] += op["Z12"] * Ib[self.tw_a]
         top[ns:] = op["z_tail"] * Ib[ns:]
         top -= self.Ar @ x[nb:]
         return np.concatenate([top, self.ArT @ Ib])
@@ -789,7 +962,7 @@ class OracleStack:
                 continue
             k, i, j = idx[:, 0], idx[:, 1], idx[:, 2]
             centres = np.stack([i * d + (d / 2 if axis == 0 else 0.0), j * d + (d / 2 if axis == 1 else 0.0),
-                                self.zs[k]], axis=1)
+                                self.sheet_z[k]], axis=1)
             acc = np.zeros(len(idx))
             half = 0.5 * self.sheet_t[k]
             for s in horiz:
@@ -798,7 +971,7 @@ class OracleStack:
                 if abs(ab[axis]) < 1e-15 * L:
                     continue
                 zseg = 0.5 * (s.a[2] + s.b[2])
-                centres[:, 2] = self.zs[k] + np.where(zseg > self.zs[k], half, -half)
+                centres[:, 2] = self.sheet_z[k] + np.where(zseg > self.sheet_z[k], half, -half)
                 rho_min = max(0.5 * s.width, 1e-7)
                 a_c = segment_vector_potential(s.a, s.b, centres, rho_min)
                 near = dist_to_segment(centres, s.a, s.b) < 3 * d + 2 * s.width
@@ -833,11 +1006,11 @@ class OracleStack:
         d = self.d
         Ix, Iy = Ib[: self.nxb], Ib[self.nxb: self.ns]
         k, _, j = self.xa.T if self.nxb else (np.zeros(0, int),) * 3
-        z = self.zs[k]
+        z = self.sheet_z[k]
         m[1] += 0.5 * np.sum(z * d * Ix)
         m[2] += 0.5 * np.sum(-(j * d) * d * Ix)
         k, i, _ = self.ya.T if self.nyb else (np.zeros(0, int),) * 3
-        z = self.zs[k]
+        z = self.sheet_z[k]
         m[0] += 0.5 * np.sum(-z * d * Iy)
         m[2] += 0.5 * np.sum((i * d) * d * Iy)
         I_cap = Ib[self.ns: self.ns + self.ncap]
@@ -912,8 +1085,9 @@ class OracleRoute:
         w = 2 * math.pi * f
         I_x = np.zeros((st.N, st.nx - 1, st.ny), complex)
         I_y = np.zeros((st.N, st.nx, st.ny - 1), complex)
-        I_x[tuple(st.xa.T)] = Ib[: st.nxb]
-        I_y[tuple(st.ya.T)] = Ib[st.nxb: st.ns]
+        # per layer: a split layer's two faces added (peec.py:2796-2803)
+        np.add.at(I_x, tuple(st.layer_index("x").T), Ib[: st.nxb])
+        np.add.at(I_y, tuple(st.layer_index("y").T), Ib[st.nxb: st.ns])
         Vg = np.zeros((st.N, st.nx, st.ny), complex)
         Vg[np.nonzero(st.node)] = V[: st.n_grid]
         v_inj = sum(amps * V[n] for n, amps in self.injections)

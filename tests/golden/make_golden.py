@@ -18,6 +18,9 @@ The reference's solver module imports shapely at module level but uses it only t
 
 ``necked_pair.npz`` holds the same records for a plane pair with strips narrower than the pitch (an island on
 a neck; the grids' wx / wy, ox / oy, rx / ry), plus the reference's strip widths, dL and M_near.
+``faces_stack3_diag.npz`` / ``faces_stack3_sheet.npz``: three planes with screening on (the middle one split
+into two face sheets, PlaneStack._faces), with either preconditioner, plus the sheets' layers, heights and twin
+pairs and the face coupling Z12.
 ``small_pair_derived.npz`` holds the same for small_pair plus a what-if edit's branches on a derived stack
 (PlaneStack.with_branches), including solves warm-started from the base's solutions.
 
@@ -56,7 +59,7 @@ def build_reference(peec, board: synth.Board):
     branches = [peec.Branch(b.a, b.b, (lambda f, b=b: b.z(f)), f"br{n}", b.kind, b.radius)
                 for n, b in enumerate(board.branches)]
     pairs = [peec.PlanePair(p.upper, p.lower, p.c_per_area, p.tan_delta) for p in board.pairs]
-    st = peec.PlaneStack(layers, branches, pairs, board.sigma, precond=board.precond, screen=False)
+    st = peec.PlaneStack(layers, branches, pairs, board.sigma, precond=board.precond, screen=board.screen)
     routes = []
     for net in board.nets:
         trace = [peec.TraceSegment(s[0:3].copy(), s[3:6].copy(), float(s[6]), float(s[7])) for s in net.segments]
@@ -80,6 +83,9 @@ def record(peec, board: synth.Board, solve: bool = True) -> dict:
                ns=np.int64(st.ns), ncap=np.int64(st.ncap), nbr=np.int64(st.nbr), cap=st.cap)
     if getattr(st, "B_x", None) is not None:
         out.update(B_x=st.B_x, B_y=st.B_y)
+    if len(getattr(st, "twin_parent", [])):          # split layers: face sheets
+        out.update(n_sheets=np.int64(st.n_sheets), sheet_layer=st.sheet_layer, twin_parent=st.twin_parent,
+                   tw_a=st.tw_a, tw_b=st.tw_b, sheet_z=st.sheet_z, sheet_t=st.sheet_t)
     if getattr(st, "dL", None) is not None:          # strips narrower than the pitch
         out.update(strip_width=st.strip_width, r_width=st.r_width, dL=st.dL)
         if st.M_near is not None:
@@ -87,6 +93,8 @@ def record(peec, board: synth.Board, solve: bool = True) -> dict:
     f0 = float(board.freqs[0])
     op = st.operator(f0)
     out.update(op_f=np.float64(f0), op_R=op.R_strip, op_z=op.z_tail)
+    if getattr(op, "Z12", None) is not None:
+        out["op_Z12"] = op.Z12
     out["op_Dinv_ij"], out["op_Dinv"] = coo(op.Dinv)
     S = (st.ArT @ op.Dinv @ st.Ar)
     out["op_S_ij"], out["op_S"] = coo(S)
@@ -175,8 +183,14 @@ def main():
     ap.add_argument("--full", action="store_true")
     ap.add_argument("--derived-only", action="store_true", help="only the derived-stack fixture")
     ap.add_argument("--narrow-only", action="store_true", help="only the narrow-strip board's fixture")
+    ap.add_argument("--faces-only", action="store_true", help="only the face-sheet boards' fixtures")
     args = ap.parse_args()
     peec, kernel = import_reference(args.reference)
+    for pc in ("diag", "sheet"):
+        print(f"faces_stack3_{pc}", flush=True)
+        np.savez_compressed(HERE / f"faces_stack3_{pc}.npz", **record(peec, synth.faces_stack3(pc)))
+    if args.faces_only:
+        return
     print("necked_pair", flush=True)
     np.savez_compressed(HERE / "necked_pair.npz", **record(peec, synth.necked_pair()))
     if args.narrow_only:

@@ -13,7 +13,7 @@ from groundtruth_gb300 import synth
 from oracle import peec_oracle as po
 
 GOLD = Path(__file__).resolve().parent / "golden"
-CASES = ["small_pair", "small_stack3", "plain_plane", "necked_pair"]
+CASES = ["small_pair", "small_stack3", "plain_plane", "necked_pair", "faces_stack3_diag", "faces_stack3_sheet"]
 
 
 def load(name):
@@ -26,7 +26,7 @@ def oracle_stack(board):
     layers = [po.OLayer(l.z, l.thickness, l.node, l.xb, l.yb, l.widths) for l in board.layers]
     pairs = [po.OPair(p.upper, p.lower, p.c_per_area, p.tan_delta) for p in board.pairs]
     branches = [po.OBranch(b.a, b.b, b.R, b.L, b.C, b.kind, b.radius) for b in board.branches]
-    return po.OracleStack(layers, board.d, branches, pairs, board.sigma, board.precond)
+    return po.OracleStack(layers, board.d, branches, pairs, board.sigma, board.precond, board.screen)
 
 
 def oracle_routes(st, board):
@@ -123,3 +123,15 @@ def test_narrow_strip_corrections_match_reference():
     ij = z["M_near_ij"]
     ref = sp.coo_matrix((z["M_near"], (ij[0], ij[1])), shape=(st.ns, st.ns)).tocsr()
     assert st.M_near.nnz == ref.nnz and abs(st.M_near - ref).max() <= 1e-12 * abs(ref).max()
+
+
+@pytest.mark.parametrize("name", ["faces_stack3_diag", "faces_stack3_sheet"])
+def test_face_sheets_match_reference(name):
+    """Screened layers split into two face sheets (peec.py:1658-1716, 2186-2197): the sheets, their layers and
+    heights, the twin strip pairs and the face coupling equal the reference's."""
+    z, board = load(name)
+    st = oracle_stack(board)
+    assert st.n_sheets == int(z["n_sheets"]) and np.array_equal(st.sheet_layer, z["sheet_layer"])
+    assert np.array_equal(st.tw_a, z["tw_a"]) and np.array_equal(st.tw_b, z["tw_b"])
+    assert np.allclose(st.sheet_z, z["sheet_z"], rtol=0, atol=1e-15) and np.array_equal(st.sheet_t, z["sheet_t"])
+    assert rel(st.twin_z(float(z["op_f"])), z["op_Z12"]) < 1e-13
