@@ -201,6 +201,7 @@ struct gt_geometry {
     // the last n_lowrank branches are left out of the S-term map: a derived stack whose operators come from
     // gt_operators_derive (its base's factorisations plus a low-rank update)
     int n_lowrank = 0;
+    int ntw = 0;                 // split layers (face couplings per operator)
     Narrow narrow{};
     std::vector<int> h_branch_nodes;
     uint64_t fsig = 0;  // signature of the factor structure (ordering, fronts, panel layout)
@@ -239,6 +240,7 @@ struct gt_operators {
     Pool pool;
     double* omega = nullptr;
     c64 *zs = nullptr, *zcap = nullptr, *zbr = nullptr, *tab = nullptr;
+    c64* zmut = nullptr;         // [op][ntw] the split layers' face couplings
     c32* tab32 = nullptr;        // the admittance table rounded to FP32 (the FP32 preconditioner's stencils)
     // per front P = [Linv_own; -L_bnd Linv_own] (nf x nown) and the pivot reciprocals dinv ([op][nfac])
     c64* panel64 = nullptr;      // column-major per front (forward solves)
@@ -261,6 +263,20 @@ struct gt_operators {
 };
 
 namespace gt {
+
+// the operators' sheet impedances [op][S] and, with face sheets, the face couplings [op][ntw] from the host's
+// zs [op][S + ntw]
+static void upload_zs(gt_operators* O, const gt_geometry* G, const double* zs, int n_ops) {
+    const int S = G->geo.S, ntw = G->ntw, ld = S + ntw;
+    std::vector<c64> a((size_t)n_ops * S), b((size_t)n_ops * std::max(ntw, 1));
+    for (int q = 0; q < n_ops; ++q) {
+        for (int k = 0; k < S; ++k) a[(size_t)q * S + k] = mk<double>(zs[2 * ((size_t)q * ld + k)], zs[2 * ((size_t)q * ld + k) + 1]);
+        for (int m = 0; m < ntw; ++m)
+            b[(size_t)q * ntw + m] = mk<double>(zs[2 * ((size_t)q * ld + S + m)], zs[2 * ((size_t)q * ld + S + m) + 1]);
+    }
+    O->zs = O->pool.upload(a.data(), a.size());
+    O->zmut = O->pool.upload(b.data(), b.size());
+}
 
 static int status_of(const CudaError& e) {
     set_error(std::string(cudaGetErrorString(e.code)) + " (" + e.where + ")");
@@ -373,6 +389,7 @@ static void matvec(gt_geometry* G, gt_operators* ops, const cx<R>* x, const cx<R
         a.zs = ops->zs;
         a.mode = mode;
         a.col_list = col_list;
+        a.sheet_layer = G->geo.NL < G->geo.S ? G->geo.sheet_layer : nullptr;
         const int pr = sizeof(R) == 8;
         if (G->o[k].rows[pr] == 0 && ncol >= 8 && mode != 2) tune_lp<R>(G->o[k], a, pr, st);
         a.rows = o.rows[pr];
@@ -405,7 +422,8 @@ static void matvec(gt_geometry* G, gt_operators* ops, const cx<R>* x, const cx<R
     }
     if (G->narrow.nrow) {
         Scope s(P, "narrow", st);
-        launch_narrow<R>(G->narrow, x, out, ld, ncol, G->geo.S, col_op, ops->omega, ops->zs, mode, col_list, st);
+        launch_narrow<R>(G->narrow, x, out, ld, ncol, G->geo.S, col_op, ops->omega, ops->zs, ops->zmut, mode,
+                         col_list, st);
     }
 }
 
@@ -930,7 +948,8 @@ void lp_with_scratch(gt_geometry* G, int ncol, const c64* x, c64* y, void* scrat
         launch_lp<double>(a, st);
     }
     if (G->narrow.nrow)
-        launch_narrow<double>(G->narrow, x, y, G->geo.n, ncol, G->geo.S, nullptr, nullptr, nullptr, 2, nullptr, st);
+        launch_narrow<double>(G->narrow, x, y, G->geo.n, ncol, G->geo.S, nullptr, nullptr, nullptr, nullptr, 2,
+                              nullptr, st);
 }
 
 }  // namespace gt
@@ -980,8 +999,21 @@ int gt_geometry_create(const gt_geometry_desc* d, gt_geometry** out) {
     Pool& p = G->pool;
     Geo& g = G->geo;
     const int S = d->n_sheets, nx = d->nx, ny = d->ny;
-    const int64_t nn = (int64_t)S * nx * ny;
+    const int NL = d->n_layers > 0 ? d->n_layers : S;
+    if (NL > S || (NL < S && !d->sheet_layer)) throw Invalid("n_layers must not exceed n_sheets; sheet_layer needed");
+    const int64_t nn = (int64_t)NL * nx * ny;
     g.S = S;
+    g.NL = NL;
+    {
+        std::vector<int> sl(S);
+        for (int k = 0; k < S; ++k) {
+            sl[k] = d->sheet_layer && NL < S ? d->sheet_layer[k] : k;
+            if (sl[k] < 0 || sl[k] >= NL) throw Invalid("sheet_layer out of range");
+        }
+        g.sheet_layer = p.upload(sl.data(), sl.size());
+    }
+    if (d->n_twins < 0 || d->n_twins != S - NL) throw Invalid("n_twins must be n_sheets - n_layers");
+    G->ntw = d->n_twins;
     g.nx = nx;
     g.ny = ny;
     g.np = d->n_pairs;
@@ -1050,6 +1082,18 @@ int gt_geometry_create(const gt_geometry_desc* d, gt_geometry** out) {
         nw.ptr = p.upload(d->narrow_ptr, nr + 1);
         nw.col = p.upload(d->narrow_col, std::max<int64_t>(ne, 1));
         nw.val = p.upload(d->narrow_val, std::max<int64_t>(ne, 1));
+        if (d->narrow_partner) {
+            for (int64_t q = 0; q < nr; ++q) {
+                const int64_t pp = d->narrow_partner[q];
+                if (pp >= 0 && (pp < d->off_x || pp >= d->off_c || d->narrow_twin[q] < 0 ||
+                                d->narrow_twin[q] >= d->n_twins))
+                    throw Invalid("face partner out of range");
+            }
+            nw.partner = p.upload(d->narrow_partner, nr);
+            nw.twin = p.upload(d->narrow_twin, nr);
+            nw.tw_fac = p.upload(d->narrow_twfac, nr);
+            nw.ntw = d->n_twins;
+        }
     }
     G->n_compact = d->n_compact;
     G->d_c2d = p.upload(d->compact_to_dense, d->n_compact);
@@ -1224,7 +1268,7 @@ int gt_operators_create_shared(gt_geometry* G, int32_t n_ops, const double* omeg
     const int nf_ops = O->nfact = (int)own.size();
     O->own = own;
     O->omega = p.upload(omega, n_ops);
-    O->zs = p.upload(reinterpret_cast<const c64*>(zs), (size_t)n_ops * g.S);
+    upload_zs(O.get(), G, zs, n_ops);
     O->zcap = p.upload(reinterpret_cast<const c64*>(zcap), (size_t)n_ops * g.np);
     O->zbr = p.upload(reinterpret_cast<const c64*>(zbr), (size_t)n_ops * g.nbr);
     {
@@ -1318,7 +1362,7 @@ int gt_operators_derive(gt_geometry* G, const gt_operators* base, int32_t n_ops,
     Pool& p = O->pool;
     const int nf = O->nfact;
     O->omega = p.upload(omega, n_ops);
-    O->zs = p.upload(reinterpret_cast<const c64*>(zs), (size_t)n_ops * g.S);
+    upload_zs(O.get(), G, zs, n_ops);
     O->zcap = p.upload(reinterpret_cast<const c64*>(zcap), (size_t)n_ops * g.np);
     O->zbr = p.upload(reinterpret_cast<const c64*>(zbr), (size_t)n_ops * g.nbr);
     {
@@ -1604,6 +1648,7 @@ int gt_node_field(gt_geometry* G, int32_t n_cols, const void* x_device, double p
                   void* ky_device, void* stream) {
     GT_GUARD_BEGIN
     if (!G || n_cols < 1 || !x_device || !kx_device || !ky_device || !(pitch > 0)) throw Invalid("bad arguments");
+    if (G->geo.NL != G->geo.S) throw Invalid("node fields of face sheets are summed per layer on the host");
     std::lock_guard<std::mutex> lk(G->lock);
     cudaStream_t st = (cudaStream_t)stream;
     launch_node_field(G->geo, static_cast<const c64*>(x_device), G->geo.n, n_cols, pitch, static_cast<c64*>(kx_device),
@@ -1617,6 +1662,7 @@ int gt_moment(gt_geometry* G, int32_t n_cols, const void* x_device, const double
               void* stream) {
     GT_GUARD_BEGIN
     if (!G || n_cols < 1 || !x_device || !sheet_z || !m || !(pitch > 0)) throw Invalid("bad arguments");
+    if (G->geo.NL != G->geo.S) throw Invalid("the moment of face sheets is taken on the host");
     std::lock_guard<std::mutex> lk(G->lock);
     cudaStream_t st = (cudaStream_t)stream;
     Pool tmp;

@@ -7,6 +7,8 @@ namespace gt {
 // The geometry as the kernels see it (device pointers, sizes).
 struct Geo {
     int S, nx, ny, np, nbr, sheet;
+    int NL;                      // node layers (S minus the split layers' lower-face sheets)
+    const int* sheet_layer;      // [S] the layer whose nodes each sheet's strips join
     int64_t n, off_x, off_y, off_c, off_b, off_v;
     const uint8_t* mask;
     const uint8_t* code_x;
@@ -37,10 +39,17 @@ struct Narrow {
     const int64_t* ptr = nullptr;
     const int64_t* col = nullptr;
     const double* val = nullptr;
+    // a split layer's face strips: the partner face's strip (dense position, -1: none), the split layer's index
+    // into the per-operator face couplings and the factor 1 / width: out[p] += z_mut fac x[partner]
+    const int64_t* partner = nullptr;
+    const int* twin = nullptr;
+    const double* tw_fac = nullptr;
+    int ntw = 0;
 };
 template <typename R>
 void launch_narrow(const Narrow& nw, const cx<R>* x, cx<R>* out, int64_t ld, int ncol, int S, const int* col_op,
-                   const double* omega, const c64* zs, int mode, const int* col_list, cudaStream_t st);
+                   const double* omega, const c64* zs, const c64* zmut, int mode, const int* col_list,
+                   cudaStream_t st);
 
 template <typename R> struct LpArgs {
     const cx<R>* x;
@@ -58,6 +67,7 @@ template <typename R> struct LpArgs {
     const c64* zs;
     int mode;
     const int* col_list;
+    const int* sheet_layer;   // [S] node layer of each sheet's strips (null: the sheet itself)
     int rows;              // rows per block of the row passes (0: default)
     int bt;                // columns per block of the column pass (0: default)
 };

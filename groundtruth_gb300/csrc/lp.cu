@@ -312,7 +312,7 @@ __global__ void __launch_bounds__(1024) lp_pass_c8(const cx<R>* __restrict__ T, 
                                                    int di, int dj, int rows, const cx<R>* __restrict__ tw,
                                                    const uint8_t* __restrict__ mask, const int* __restrict__ col_op,
                                                    const double* __restrict__ omega, const c64* __restrict__ zs, int mode,
-                                                   const int* __restrict__ col_list) {
+                                                   const int* __restrict__ col_list, const int* __restrict__ sheet_layer) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int TEAM = P / 8, NBF = P / 8, ST = lp_srow(P);
     cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw);
@@ -365,6 +365,7 @@ __global__ void __launch_bounds__(1024) lp_pass_c8(const cx<R>* __restrict__ T, 
     const R w = omega ? R(omega[op]) : R(0);
     const cx<R> z = zs ? cvt<R>(zs[(int64_t)op * S + s]) : zero<R>();
     const int64_t base = (int64_t)col * ld;
+    const int layer = sheet_layer ? sheet_layer[s] : s;     // the nodes a face sheet's strips join
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
         const int j = t + r * NBF;
@@ -377,7 +378,7 @@ __global__ void __launch_bounds__(1024) lp_pass_c8(const cx<R>* __restrict__ T, 
             y = zero<R>();
         } else {
             const cx<R> xv = x[base + pos];
-            const int64_t va = off_v + ((int64_t)s * nx + i) * ny + j;
+            const int64_t va = off_v + ((int64_t)layer * nx + i) * ny + j;
             const int64_t vb = va + (int64_t)di * ny + dj;
             const cx<R> dv = x[base + va] - x[base + vb];
             y = z * xv + w * jmul(L[r]) - dv;
@@ -394,7 +395,7 @@ __global__ void __launch_bounds__(1024) lp_pass_c(const cx<R>* __restrict__ T, c
                           int nx, int ny, int di, int dj, int P1, int rows, const cx<R>* __restrict__ tw,
                           const uint8_t* __restrict__ mask, const int* __restrict__ col_op,
                           const double* __restrict__ omega, const c64* __restrict__ zs, int mode,
-                          const int* __restrict__ col_list) {
+                          const int* __restrict__ col_list, const int* __restrict__ sheet_layer) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw);
     const int P = PL ? PL : P1;                  // compile-time when specialised
@@ -420,6 +421,7 @@ __global__ void __launch_bounds__(1024) lp_pass_c(const cx<R>* __restrict__ T, c
     // each team finishes its own row
     const int i = i0 + r;
     if (r >= rows || i >= n0) return;
+    const int layer = sheet_layer ? sheet_layer[s] : s;
     for (int j = t; j < n1; j += team) {
         int64_t pos = off + ((int64_t)s * n0 + i) * n1 + j;
         cx<R> L = buf[r * stride + spad(j)];
@@ -430,7 +432,7 @@ __global__ void __launch_bounds__(1024) lp_pass_c(const cx<R>* __restrict__ T, c
             y = zero<R>();
         } else {
             cx<R> xv = x[base + pos];
-            int64_t va = off_v + ((int64_t)s * nx + i) * ny + j;
+            int64_t va = off_v + ((int64_t)layer * nx + i) * ny + j;
             int64_t vb = va + (int64_t)di * ny + dj;
             cx<R> dv = x[base + va] - x[base + vb];
             y = z * xv + w * jmul(L) - dv;
@@ -522,7 +524,7 @@ static void launch_c(const LpArgs<R>& a, int rows, cudaStream_t st) {
         set_smem<R>((const void*)lp_pass_c8<R, PA>, sm);
         lp_pass_c8<R, PA><<<dim3(ceil_div(a.n0, rows), a.S, a.ncol), rows * (PA / 8), sm, st>>>(
             a.T, a.x, a.rhs, a.out, a.ld, a.off, a.off_v, a.S, a.n0, a.n1, a.nx, a.ny, a.di, a.dj, rows, a.tw1, a.mask,
-            a.col_op, a.omega, a.zs, a.mode, a.col_list);
+            a.col_op, a.omega, a.zs, a.mode, a.col_list, a.sheet_layer);
         GT_LAUNCH_CHECK();
         return;
     }
@@ -531,7 +533,7 @@ static void launch_c(const LpArgs<R>& a, int rows, cudaStream_t st) {
     set_smem<R>((const void*)lp_pass_c<R, PA>, smA);
     lp_pass_c<R, PA><<<gA, rows * (a.P1 / 8), smA, st>>>(a.T, a.x, a.rhs, a.out, a.ld, a.off, a.off_v, a.S, a.n0, a.n1,
                                                           a.nx, a.ny, a.di, a.dj, a.P1, rows, a.tw1, a.mask, a.col_op,
-                                                          a.omega, a.zs, a.mode, a.col_list);
+                                                          a.omega, a.zs, a.mode, a.col_list, a.sheet_layer);
     GT_LAUNCH_CHECK();
 }
 

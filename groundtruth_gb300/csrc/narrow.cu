@@ -3,7 +3,9 @@
 // treat every strip as a full square; the few strips whose copper is narrower (a neck, a partly covered
 // border) get their corrections here, after the passes, as a sparse row list:
 //     out[p] += z_k (1/w_p - 1) x[p] + j omega (dL_p x[p] + sum_q M[p,q] x[q])      (system product)
-// with the sign flipped for a residual (rhs - K x) and without the resistance and j omega for L_p alone.
+// with the sign flipped for a residual (rhs - K x) and without the resistance and j omega for L_p alone.  The
+// same rows carry a split layer's face coupling (PlaneStack._twin_z, peec.py:2186-2197; the product's
+// top[tw_a] += Z12 I[tw_b] and back, peec.py:3054-3056): out[p] += z_mut / width x[partner].
 #include "kernels.h"
 
 namespace gt {
@@ -13,7 +15,8 @@ template <typename R>
 __global__ void __launch_bounds__(128) narrow_kernel(Narrow nw, const cx<R>* __restrict__ x, cx<R>* __restrict__ out,
                                                     int64_t ld, int S, const int* __restrict__ col_op,
                                                     const double* __restrict__ omega, const c64* __restrict__ zs,
-                                                    int mode, const int* __restrict__ col_list) {
+                                                    const c64* __restrict__ zmut, int mode,
+                                                    const int* __restrict__ col_list) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nw.nrow) return;
     const int col = col_list ? col_list[blockIdx.y] : blockIdx.y;
@@ -28,6 +31,8 @@ __global__ void __launch_bounds__(128) narrow_kernel(Narrow nw, const cx<R>* __r
     } else {
         const cx<R> z = cvt<R>(zs[(int64_t)op * S + nw.sheet[q]]);
         y = R(nw.rdelta[q]) * (z * xc[p]) + R(omega[op]) * jmul(acc);
+        if (nw.partner && nw.partner[q] >= 0)       // the face coupling of a split layer's two strips
+            y += R(nw.tw_fac[q]) * (cvt<R>(zmut[(int64_t)op * nw.ntw + nw.twin[q]]) * xc[nw.partner[q]]);
         if (mode == 1) y = zero<R>() - y;
     }
     out[(int64_t)col * ld + p] += y;
@@ -35,16 +40,17 @@ __global__ void __launch_bounds__(128) narrow_kernel(Narrow nw, const cx<R>* __r
 
 template <typename R>
 void launch_narrow(const Narrow& nw, const cx<R>* x, cx<R>* out, int64_t ld, int ncol, int S, const int* col_op,
-                   const double* omega, const c64* zs, int mode, const int* col_list, cudaStream_t st) {
+                   const double* omega, const c64* zs, const c64* zmut, int mode, const int* col_list,
+                   cudaStream_t st) {
     if (nw.nrow == 0 || ncol < 1) return;
     narrow_kernel<R><<<dim3((unsigned)((nw.nrow + 127) / 128), ncol), 128, 0, st>>>(nw, x, out, ld, S, col_op, omega,
-                                                                                   zs, mode, col_list);
+                                                                                   zs, zmut, mode, col_list);
     GT_LAUNCH_CHECK();
 }
 
 template void launch_narrow<float>(const Narrow&, const c32*, c32*, int64_t, int, int, const int*, const double*,
-                                   const c64*, int, const int*, cudaStream_t);
+                                   const c64*, const c64*, int, const int*, cudaStream_t);
 template void launch_narrow<double>(const Narrow&, const c64*, c64*, int64_t, int, int, const int*, const double*,
-                                    const c64*, int, const int*, cudaStream_t);
+                                    const c64*, const c64*, int, const int*, cudaStream_t);
 
 }  // namespace gt

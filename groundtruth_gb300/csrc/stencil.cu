@@ -49,11 +49,10 @@ __global__ void __launch_bounds__(256) tail_kernel(Geo g, const cx<R>* __restric
     const int part = blockIdx.y;
     auto put = [&](int64_t pos, cx<R> y) { oc[pos] = mode == 1 ? bc[pos] - y : y; };
     if (part == 0) for (int bx = blockIdx.x * RPB; bx < blockIdx.x * RPB + RPB; ++bx) {
-        // node (KCL) rows: I_x(k,i,j) - I_x(k,i-1,j) + I_y(k,i,j) - I_y(k,i,j-1) + caps + branches
+        // node (KCL) rows: I_x(k,i,j) - I_x(k,i-1,j) + I_y(k,i,j) - I_y(k,i,j-1) + caps + branches, the strips of
+        // every sheet on layer k (a split layer's two faces)
         const int k = bx / nx, i = bx - k * nx;
-        if (k >= S) break;
-        const cx<R>* X = xc + g.off_x + (int64_t)k * (nx - 1) * ny;
-        const cx<R>* Y = xc + g.off_y + (int64_t)k * nx * (ny - 1);
+        if (k >= g.NL) break;
         for (int j = threadIdx.x; j < ny; j += blockDim.x) {
             const int ij = i * ny + j, node = k * nxy + ij;
             const int64_t pos = g.off_v + node;
@@ -62,10 +61,15 @@ __global__ void __launch_bounds__(256) tail_kernel(Geo g, const cx<R>* __restric
                 continue;
             }
             cx<R> s = zero<R>();
-            if (i < nx - 1) s += X[i * ny + j];
-            if (i > 0) s -= X[(i - 1) * ny + j];
-            if (j < ny - 1) s += Y[i * (ny - 1) + j];
-            if (j > 0) s -= Y[i * (ny - 1) + j - 1];
+            for (int sh = g.NL == S ? k : 0; sh < (g.NL == S ? k + 1 : S); ++sh) {
+                if (g.sheet_layer[sh] != k) continue;
+                const cx<R>* X = xc + g.off_x + (int64_t)sh * (nx - 1) * ny;
+                const cx<R>* Y = xc + g.off_y + (int64_t)sh * nx * (ny - 1);
+                if (i < nx - 1) s += X[i * ny + j];
+                if (i > 0) s -= X[(i - 1) * ny + j];
+                if (j < ny - 1) s += Y[i * (ny - 1) + j];
+                if (j > 0) s -= Y[i * (ny - 1) + j - 1];
+            }
             for (int p = 0; p < g.np; ++p) {
                 const int u = g.pair_layers[2 * p], l = g.pair_layers[2 * p + 1];
                 if (u == k) s += xc[g.off_c + (int64_t)p * nxy + ij];
@@ -98,7 +102,7 @@ __global__ void __launch_bounds__(256) tail_kernel(Geo g, const cx<R>* __restric
         const int64_t nX = (int64_t)S * (nx - 1) * ny, nY = (int64_t)S * nx * (ny - 1);
         const int64_t gap[5][2] = {{g.off_x + nX, g.off_y}, {g.off_y + nY, g.off_c},
                                    {g.off_c + (int64_t)g.np * nxy, g.off_b}, {g.off_b + g.nbr, g.off_v},
-                                   {g.off_v + (int64_t)S * nxy, g.n}};
+                                   {g.off_v + (int64_t)g.NL * nxy, g.n}};
         const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
         for (int b = tid; b < g.nbr; b += nth) {
             const int64_t pos = g.off_b + b;
@@ -187,9 +191,20 @@ __global__ void __launch_bounds__(256) pc_node_kernel(Geo g, const cx<R>* __rest
                                         : T + ((int64_t)(side < 2 ? 0 : 1) * NC + code[side]) * S * S,
                                 S, code[side], u[side], t);
             const bool plus = (side & 1) == 0;
+            if (g.NL == S) {
 #pragma unroll
-            for (int k = 0; k < MAXS; ++k)
-                if (k < S) kcl[k] = plus ? kcl[k] + t[k] : kcl[k] - t[k];
+                for (int k = 0; k < MAXS; ++k)
+                    if (k < S) kcl[k] = plus ? kcl[k] + t[k] : kcl[k] - t[k];
+            } else {
+#pragma unroll
+                for (int k = 0; k < MAXS; ++k) {
+                    if (k >= S) continue;
+                    const int L = g.sheet_layer[k];      // a face sheet's strips join its layer's nodes
+#pragma unroll
+                    for (int m = 0; m < MAXS; ++m)
+                        if (m == L) kcl[m] = plus ? kcl[m] + t[k] : kcl[m] - t[k];
+                }
+            }
         }
         for (int p = 0; p < g.np; ++p) {
             const int up = g.pair_layers[2 * p], lo = g.pair_layers[2 * p + 1];
@@ -204,7 +219,7 @@ __global__ void __launch_bounds__(256) pc_node_kernel(Geo g, const cx<R>* __rest
         }
 #pragma unroll
         for (int k = 0; k < MAXS; ++k) {
-            if (k >= S) break;
+            if (k >= g.NL) break;
             const int node = k * nxy + ij;
             if (!g.mask[g.off_v + node]) continue;
             cx<R> acc = kcl[k];
@@ -243,7 +258,7 @@ __global__ void __launch_bounds__(256) pc_strip_kernel(Geo g, const cx<R>* __res
     const int S = g.S, nx = g.nx, ny = g.ny, nxy = nx * ny, NC = 1 << S;
     const cx<R>* T = tab + (int64_t)op * g.ntab;
     const cx<R>* rc = r + (int64_t)col * ldr;
-    const cx<R>* yc = sd + (int64_t)col * S * nxy;       // zero at nodes that are not kept
+    const cx<R>* yc = sd + (int64_t)col * g.NL * nxy;    // zero at nodes that are not kept
     cx<R>* oc = out + (int64_t)col * ldo;
     const int part = blockIdx.y;
     if (part <= 1) for (int bx = blockIdx.x * RPB; bx < blockIdx.x * RPB + RPB; ++bx) {
@@ -261,7 +276,8 @@ __global__ void __launch_bounds__(256) pc_strip_kernel(Geo g, const cx<R>* __res
 #pragma unroll
             for (int l = 0; l < MAXS; ++l)
                 u[l] = (l < S && ((code >> l) & 1))
-                           ? rc[seg + (int64_t)l * lstride + pq] + (yc[l * nxy + na] - yc[l * nxy + na + dn])
+                           ? rc[seg + (int64_t)l * lstride + pq] +
+                                 (yc[g.sheet_layer[l] * nxy + na] - yc[g.sheet_layer[l] * nxy + na + dn])
                            : zero<R>();
             const int* ovr = xo ? g.ovr_x : g.ovr_y;
             const int ob = ovr ? ovr[pq] : -1;
@@ -284,7 +300,7 @@ __global__ void __launch_bounds__(256) pc_strip_kernel(Geo g, const cx<R>* __res
         }
     } else if (part == 3) for (int bx = blockIdx.x * RPB; bx < blockIdx.x * RPB + RPB; ++bx) {
         const int k = bx / nx, i = bx - k * nx;
-        if (k >= S) break;
+        if (k >= g.NL) break;
         for (int j = threadIdx.x; j < ny; j += blockDim.x) {
             const int node = k * nxy + i * ny + j;
             oc[g.off_v + node] = yc[node];
@@ -295,7 +311,7 @@ __global__ void __launch_bounds__(256) pc_strip_kernel(Geo g, const cx<R>* __res
         const int64_t nX = (int64_t)S * (nx - 1) * ny, nY = (int64_t)S * nx * (ny - 1);
         const int64_t gap[5][2] = {{g.off_x + nX, g.off_y}, {g.off_y + nY, g.off_c},
                                    {g.off_c + (int64_t)g.np * nxy, g.off_b}, {g.off_b + g.nbr, g.off_v},
-                                   {g.off_v + (int64_t)S * nxy, g.n}};
+                                   {g.off_v + (int64_t)g.NL * nxy, g.n}};
         const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
         for (int b = tid; b < g.nbr; b += nth) {
             const int64_t pos = g.off_b + b;

@@ -170,6 +170,22 @@ def slab_impedance(t, f, sigma):
     return complex(out) if out.ndim == 0 else out
 
 
+def face_sheet_impedance(t, f, sigma):
+    """(z_self, z_mutual) per square of a slab's two face sheets t apart with free space between them: the sum
+    mode u coth(u/2) and the difference mode beside the free space u^2 tanh(u/2) / (u - 2 tanh(u/2)), in units of
+    1/(sigma t), u = (1 + j) t / delta, thin foils (t / delta < 0.1) by their series (kernel.py:102-152)."""
+    t = np.asarray(t, float)
+    with np.errstate(divide="ignore", over="ignore", invalid="ignore"):
+        delta = 1.0 / np.sqrt(np.pi * max(f, 1e-300) * MU0 * sigma)
+        x = t / delta if f > 0 else np.zeros_like(t)
+        u = (1 + 1j) * x
+        th = np.tanh(np.where(x > 0, (1 + 1j) * np.minimum(x, 60.0), 1.0) / 2)
+        small = x < 0.1
+        zs = np.where(small, 2.0 + x ** 4 / 90.0 + 1j * (x ** 2 / 3.0 - x ** 6 / 1890.0), u / th)
+        zd = np.where(small, 6.0 + x ** 4 / 350.0 + 1j * x ** 2 / 5.0, u * u * th / (u - 2.0 * th))
+    return 0.5 * (zs + zd) / (sigma * t), 0.5 * (zs - zd) / (sigma * t)
+
+
 def skin_thickness(t, f, sigma):
     t = np.asarray(t, float)
     f = np.asarray(f, float)

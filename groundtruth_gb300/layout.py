@@ -37,13 +37,13 @@ def _align(n: int) -> int:
 
 @dataclass
 class Topology:
-    S: int
+    S: int                    # current sheets (the layers, then the lower faces of split layers)
     nx: int
     ny: int
-    node: np.ndarray          # (S, nx, ny) bool
-    xb: np.ndarray            # (S, nx-1, ny) bool (strip and both end nodes)
+    node: np.ndarray          # (NL, nx, ny) bool, per layer
+    xb: np.ndarray            # (S, nx-1, ny) bool (strip and both end nodes), per sheet
     yb: np.ndarray
-    nid: np.ndarray           # (S, nx, ny) int64, -1 off copper
+    nid: np.ndarray           # (NL, nx, ny) int64, -1 off copper
     xa: np.ndarray            # (nxb, 3)
     ya: np.ndarray
     cap: np.ndarray           # (ncap, 6): upper, lower, i, j, C, tan_delta
@@ -55,6 +55,11 @@ class Topology:
     cond_label: np.ndarray
     full_label: np.ndarray
     keep: np.ndarray          # (n_nodes,) bool
+    sheet_layer: np.ndarray = None   # (S,) each sheet's layer (its strips join that layer's nodes)
+
+    @property
+    def NL(self):
+        return self.node.shape[0]
 
     @property
     def n_nodes(self):
@@ -85,13 +90,21 @@ class Topology:
         return int(self.keep.sum())
 
 
-def topology(node_masks, xb_masks, yb_masks, d: float, pairs: list, branch_nodes: list) -> tuple:
-    """The reference's numbering.  pairs: [(upper, lower, c_per_area, tan_delta)]; branch_nodes: [((k,i,j),
-    (k,i,j))].  Returns (Topology, indices of the branches kept: both ends on copper and different)."""
+def topology(node_masks, xb_masks, yb_masks, d: float, pairs: list, branch_nodes: list, twin_parent=()) -> tuple:
+    """The reference's numbering (peec.py:1596-1656).  pairs: [(upper, lower, c_per_area, tan_delta)];
+    branch_nodes: [((k,i,j), (k,i,j))]; twin_parent: the split layers, whose lower-face sheets (numbered after the
+    layers) have the layer's strips on the layer's nodes.  Returns (Topology, indices of the branches kept: both
+    ends on copper and different)."""
     node = np.stack(node_masks).astype(bool)
-    S, nx, ny = node.shape
+    NL, nx, ny = node.shape
+    twin_parent = np.asarray(twin_parent, np.int64)
     xb = np.stack(xb_masks).astype(bool) & node[:, :-1, :] & node[:, 1:, :]
     yb = np.stack(yb_masks).astype(bool) & node[:, :, :-1] & node[:, :, 1:]
+    if len(twin_parent):
+        xb = np.concatenate([xb, xb[twin_parent]])
+        yb = np.concatenate([yb, yb[twin_parent]])
+    sheet_layer = np.concatenate([np.arange(NL), twin_parent]).astype(np.int64)
+    S = NL + len(twin_parent)
     nid = -np.ones(node.shape, np.int64)
     idx = np.nonzero(node)
     nid[idx] = np.arange(len(idx[0]))
@@ -117,8 +130,10 @@ def topology(node_masks, xb_masks, yb_masks, d: float, pairs: list, branch_nodes
             ab.append((na, nbb))
     ab = np.array(ab, np.int64).reshape(-1, 2)
     cu = cap[:, :4].astype(np.int64)
-    a_nodes = np.concatenate([nid[tuple(xa.T)], nid[tuple(ya.T)], nid[cu[:, 0], cu[:, 2], cu[:, 3]], ab[:, 0]]).astype(np.int64)
-    b_nodes = np.concatenate([nid[xa[:, 0], xa[:, 1] + 1, xa[:, 2]], nid[ya[:, 0], ya[:, 1], ya[:, 2] + 1],
+    lx, ly = sheet_layer[xa[:, 0]], sheet_layer[ya[:, 0]]          # a strip joins its layer's nodes
+    a_nodes = np.concatenate([nid[lx, xa[:, 1], xa[:, 2]], nid[ly, ya[:, 1], ya[:, 2]],
+                              nid[cu[:, 0], cu[:, 2], cu[:, 3]], ab[:, 0]]).astype(np.int64)
+    b_nodes = np.concatenate([nid[lx, xa[:, 1] + 1, xa[:, 2]], nid[ly, ya[:, 1], ya[:, 2] + 1],
                               nid[cu[:, 1], cu[:, 2], cu[:, 3]], ab[:, 1]]).astype(np.int64)
     ns = len(xa) + len(ya)
     cond = np.ones(len(a_nodes), bool)
@@ -131,7 +146,8 @@ def topology(node_masks, xb_masks, yb_masks, d: float, pairs: list, branch_nodes
     keep = np.ones(n, bool)
     keep[first] = False
     top = Topology(S, nx, ny, node, xb, yb, nid, xa, ya, cap, np.array(pl, np.int64).reshape(-1, 2),
-                   np.array(cmask, bool).reshape(-1, nx, ny), ab, a_nodes, b_nodes, cond_label, full_label, keep)
+                   np.array(cmask, bool).reshape(-1, nx, ny), ab, a_nodes, b_nodes, cond_label, full_label, keep,
+                   sheet_layer)
     return top, kept
 
 
@@ -150,7 +166,7 @@ class Dense:
 
 def dense_layout(t: Topology) -> Dense:
     S, nx, ny = t.S, t.nx, t.ny
-    nX, nY, nV = S * (nx - 1) * ny, S * nx * (ny - 1), S * nx * ny
+    nX, nY, nV = S * (nx - 1) * ny, S * nx * (ny - 1), t.NL * nx * ny
     nC = len(t.pair_layers) * nx * ny
     off_x = 0
     off_y = _align(off_x + nX)
@@ -307,7 +323,7 @@ def symbolic(t: Topology, S_pattern: sp.csr_matrix, leaf: int = 48) -> Symbolic:
     n = len(key)
     fac_of_kept = np.empty(n, np.int64)
     fac_of_kept[key] = np.arange(n)
-    perm = -np.ones(t.S * nxy, np.int64)
+    perm = -np.ones(t.NL * nxy, np.int64)
     perm[kept_dense] = fac_of_kept
     iperm = kept_dense[key]
     counts = np.bincount(owner, minlength=nfront)

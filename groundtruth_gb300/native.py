@@ -41,7 +41,9 @@ class GeometryDesc(C.Structure):
                 ("sterm_coef", DP), ("n_lowrank", C.c_int32),
                 ("n_override", C.c_int32), ("override_x", I32P), ("override_y", I32P),
                 ("n_narrow", C.c_int64), ("narrow_pos", I64P), ("narrow_sheet", I32P), ("narrow_rdelta", DP),
-                ("narrow_dl", DP), ("narrow_ptr", I64P), ("narrow_col", I64P), ("narrow_val", DP)]
+                ("narrow_dl", DP), ("narrow_ptr", I64P), ("narrow_col", I64P), ("narrow_val", DP),
+                ("n_layers", C.c_int32), ("sheet_layer", I32P), ("n_twins", C.c_int32),
+                ("narrow_partner", I64P), ("narrow_twin", I32P), ("narrow_twfac", DP)]
 
 
 PRECISIONS = {"mixed": 0, "fp64": 1, "mixed16": 2}
@@ -181,6 +183,13 @@ class Geometry:
             d.narrow_ptr = _ptr(arr(nr["ptr"], np.int64), C.c_int64)
             d.narrow_col = _ptr(arr(nr["col"] if len(nr["col"]) else np.zeros(1), np.int64), C.c_int64)
             d.narrow_val = _ptr(arr(nr["val"] if len(nr["val"]) else np.zeros(1), np.float64), C.c_double)
+            if len(st.tw_b):
+                d.narrow_partner = _ptr(arr(nr["partner"], np.int64), C.c_int64)
+                d.narrow_twin = _ptr(arr(nr["twin"], np.int32), C.c_int32)
+                d.narrow_twfac = _ptr(arr(nr["tw_fac"], np.float64), C.c_double)
+        d.n_layers = st.N
+        d.sheet_layer = _ptr(arr(st.sheet_layer, np.int32), C.c_int32)
+        d.n_twins = len(st.twin_parent)
         h = P()
         check(lib, lib.gt_geometry_create(C.byref(d), C.byref(h)), "gt_geometry_create")
         self.h = h

@@ -14,8 +14,8 @@ Everything per iteration runs in the CUDA library (``groundtruth_gb300/csrc``) t
 does the once-per-geometry index work (``layout``) and FP64 kernels (``greens``), and the cheap
 per-frequency impedance tables.
 
-Scope: one current sheet per layer (``screen`` face sheets are not modelled: a stack that would split a
-layer raises NotImplementedError); strips narrower than the pitch (the grids' wx / wy, ox / oy, rx / ry) are
+Scope: the reference's current sheets (a layer with copper above and below is split into two face sheets when
+``screen``); strips narrower than the pitch (the grids' wx / wy, ox / oy, rx / ry) are
 modelled as the reference does (resistance over the width, dL, M_near, per-position preconditioner blocks).
 """
 from __future__ import annotations
@@ -108,6 +108,7 @@ class Solution:
     iterations: int
     I_cap: np.ndarray = field(default_factory=lambda: np.zeros(0, complex))
     residual: float = 0.0          # final relative FP64 residual ||b - K x|| / ||b||
+    I_twin: Optional[np.ndarray] = None   # (2, pairs) a split layer's upper- and lower-face strip currents
 
     @property
     def L_loop(self) -> float:
@@ -138,7 +139,13 @@ class Solution:
         """The solver's unknown vector [branch currents; kept node potentials] of this solution on `stack`, the
         stack it was solved on, rebuilt from the currents and potentials kept here (peec.py:1127-1145; a warm
         start for a derived stack through map_state)."""
-        strips = np.concatenate([self.I_x[tuple(stack.xa.T)], self.I_y[tuple(stack.ya.T)]])
+        strips = np.concatenate([self.I_x[tuple(stack.layer_index("x").T)], self.I_y[tuple(stack.layer_index("y").T)]])
+        if len(stack.tw_b):
+            # a split layer's faces: I_x / I_y hold their sum (peec.py:1135-1140)
+            if self.I_twin is not None and self.I_twin.shape[1] == len(stack.tw_b):
+                strips[stack.tw_a], strips[stack.tw_b] = self.I_twin
+            else:
+                strips[stack.tw_b] = 0.0
         Ib = np.concatenate([strips, self.I_cap, self.I_branch])
         return np.concatenate([Ib, self.V[np.nonzero(stack.node)][stack.keep]])
 
@@ -200,7 +207,7 @@ class PlaneStack:
         self._base: Optional[PlaneStack] = None
         self.n_lowrank = 0
         self.layers = list(layers)
-        self.N = self.n_sheets = len(layers)
+        self.N = len(layers)
         self.nx, self.ny = g0.nx, g0.ny
         self.d = g0.d * 1e-3
         self.zs = np.array([l.z for l in layers], float)
@@ -208,18 +215,19 @@ class PlaneStack:
         self.sigma = sigma
         self.precond_mode = precond
         self.pairs = list(capacitance or [])
-        self._check_screen(screen)
+        self._faces(np.stack([l.grid.node for l in layers]).astype(bool), screen)
         self.branches_all = list(branches or [])
         t, kept = layout.topology([l.grid.node for l in layers], [l.grid.xb for l in layers],
                                   [l.grid.yb for l in layers], self.d,
                                   [(p.upper, p.lower, p.c_per_area, p.tan_delta) for p in self.pairs],
-                                  [(b.a, b.b) for b in self.branches_all])
+                                  [(b.a, b.b) for b in self.branches_all], self.twin_parent)
         self.top = t
         self.branches = [self.branches_all[k] for k in kept]
         self.node, self.nid, self.xa, self.ya, self.keep = t.node, t.nid, t.xa, t.ya, t.keep
         self.nxb, self.nyb, self.ns, self.ncap, self.nbr, self.nb = t.nxb, len(t.ya), t.ns, t.ncap, t.nbr, t.nb
         self.n_nodes = self.n_grid = t.n_nodes
         self.full_label, self.cond_label = t.full_label, t.cond_label
+        self._twins()
         self.dense = layout.dense_layout(t)
         self._kernels()
         self._widths()
@@ -229,30 +237,71 @@ class PlaneStack:
         self.handle = native_geometry(self) if _device else None
 
     # ------------------------------------------------------------------ construction
-    def _check_screen(self, screen: bool):
-        if not screen or self.N < 3:
-            return
-        node = np.stack([l.grid.node for l in self.layers])
-        for k in range(self.N):
-            above = np.zeros(node.shape[1:], bool)
-            below = np.zeros(node.shape[1:], bool)
-            for m in range(self.N):
-                if self.zs[m] > self.zs[k]:
-                    above |= node[m]
-                elif self.zs[m] < self.zs[k]:
-                    below |= node[m]
-            if int(np.count_nonzero(node[k] & above & below)) >= SCREEN_MIN_NODES:
-                raise NotImplementedError("a layer with copper above and below (screen=True) needs face sheets, "
-                                          "which this build does not model; pass screen=False")
+    def _faces(self, node: np.ndarray, screen: bool):
+        """The current sheets (peec.py:1658-1697): one per layer, and a second for each layer with copper of other
+        layers above and below at SCREEN_MIN_NODES or more of its nodes (when `screen`): such a layer is split into
+        its two faces, its own sheet at the upper face and the twin (numbered after the layers) at the lower one,
+        both with all its strips on its nodes.  Sets twin_parent, n_sheets, sheet_layer, sheet_z (the height each
+        sheet's current stands at) and sheet_t (the copper face_gap takes off: 0 for a face sheet)."""
+        N = self.N
+        twins = []
+        if screen and N >= 3:
+            for k in range(N):
+                above = np.zeros(node.shape[1:], bool)
+                below = np.zeros(node.shape[1:], bool)
+                for m in range(N):
+                    if self.zs[m] > self.zs[k]:
+                        above |= node[m]
+                    elif self.zs[m] < self.zs[k]:
+                        below |= node[m]
+                if int(np.count_nonzero(node[k] & above & below)) >= SCREEN_MIN_NODES:
+                    twins.append(k)
+        self.twin_parent = np.array(twins, np.int64)
+        self.n_sheets = N + len(twins)
+        self.sheet_layer = np.concatenate([np.arange(N), self.twin_parent]).astype(np.int64)
+        z, st = self.zs.copy(), self.ts.copy()
+        z[twins] = self.zs[twins] + 0.5 * self.ts[twins]
+        st[twins] = 0.0
+        self.sheet_z = np.concatenate([z, self.zs[twins] - 0.5 * self.ts[twins]])
+        self.sheet_t = np.concatenate([st, np.zeros(len(twins))])
+
+    def _twins(self):
+        """tw_a / tw_b: the strips of each split layer's upper face and of its twin, pairwise (peec.py:1699-1716),
+        and each strip's twin-pair index (tw_of, -1 for a one-sheet layer's strip)."""
+        N, t = self.N, self.top
+        a, b = [], []
+        for xb, lo in ((t.xb, 0), (t.yb, self.nxb)):
+            per = np.count_nonzero(xb.reshape(self.n_sheets, -1), axis=1)
+            start = lo + np.concatenate([[0], np.cumsum(per)[:-1]])
+            for m, p in enumerate(self.twin_parent):
+                a.append(start[p] + np.arange(per[p]))
+                b.append(start[N + m] + np.arange(per[p]))
+        self.tw_a = np.concatenate(a).astype(np.int64) if a else np.zeros(0, np.int64)
+        self.tw_b = np.concatenate(b).astype(np.int64) if b else np.zeros(0, np.int64)
+
+    def sheet_of_strip(self, strips: np.ndarray) -> np.ndarray:
+        strips = np.asarray(strips, np.int64)
+        out = np.empty(len(strips), np.int64)
+        x = strips < self.nxb
+        out[x] = self.xa[strips[x], 0]
+        out[~x] = self.ya[strips[~x] - self.nxb, 0]
+        return out
+
+    def layer_index(self, orient: str) -> np.ndarray:
+        """The orientation's strips as (layer, i, j) rows (peec.py:1718-1729)."""
+        idx = (self.xa if orient == "x" else self.ya).copy()
+        idx[:, 0] = self.sheet_layer[idx[:, 0]]
+        return idx
 
     def face_gap(self, s: int, t: int) -> float:
+        """The distance between the faces sheets s and t turn to each other (peec.py:1926-1933)."""
         if s == t:
             return 0.0
-        return max(abs(self.zs[s] - self.zs[t]) - 0.5 * (self.ts[s] + self.ts[t]), 1e-6)
+        return max(abs(self.sheet_z[s] - self.sheet_z[t]) - 0.5 * (self.sheet_t[s] + self.sheet_t[t]), 1e-6)
 
     def _kernels(self):
         """Strip kernels per sheet pair and their spectra at this build's FFT sizes (peec.py:1941-1988)."""
-        nx, ny, S = self.nx, self.ny, self.N
+        nx, ny, S = self.nx, self.ny, self.n_sheets
         d = greens.round12(self.d)
         self.P = {"x": (greens.fft_size(2 * (nx - 1) - 1), greens.fft_size(2 * ny - 1)),
                   "y": (greens.fft_size(2 * nx - 1), greens.fft_size(2 * (ny - 1) - 1))}
@@ -289,16 +338,76 @@ class PlaneStack:
         self.spectrum = {o: np.ascontiguousarray(spec[o] / (self.P[o][0] * self.P[o][1])) for o in "xy"}
         self.centre, self.sum_x, self.sum_y = centre, sx, sy
         self.B = None
-        if self.precond_mode == "sheet" and S > 1:
-            self.B = {"x": greens.sheet_blocks(self.L_self, centre, sx), "y": greens.sheet_blocks(self.L_self, centre, sy)}
+        self.twin_diag = False
+        if self.precond_mode == "sheet" and self.N > 1:
+            self.B = {"x": self._sheet_block(centre, sx), "y": self._sheet_block(centre, sy)}
+        elif len(self.twin_parent):
+            # 'diag' with split layers: each face pair at a position is a 2 x 2 block with their own and mutual
+            # partial inductance (peec.py:1979-1987)
+            B = np.diag(np.full(S, self.L_self))
+            for m, p in enumerate(self.twin_parent):
+                B[p, self.N + m] = B[self.N + m, p] = centre[p, self.N + m]
+            self.B = {"x": B, "y": B}
+            self.twin_diag = True
+
+    def _sheet_block(self, centre: np.ndarray, sums: np.ndarray) -> np.ndarray:
+        """The 'sheet' block over every sheet: made over the layers, a split layer's twin taking its layer's row
+        and column, the two faces keeping their own difference L_self - M_twin (peec.py:1989-2010)."""
+        N = self.N
+        B = greens.sheet_blocks(self.L_self, centre[:N, :N], sums[:N, :N])
+        if not len(self.twin_parent):
+            return B
+        lay = self.sheet_layer
+        full = B[np.ix_(lay, lay)].copy()
+        for m, p in enumerate(self.twin_parent):
+            tw = N + m
+            gap = max(self.L_self - centre[p, tw], 0.0)
+            for j in range(self.n_sheets):
+                if lay[j] == p and j != tw:
+                    full[tw, j] = full[j, tw] = B[p, p] - gap
+        return full
+
+    def _dinv_block(self, name: str, lay: list, R: np.ndarray, dl: np.ndarray, z12: dict, w: float) -> np.ndarray:
+        """D^-1 of the strips at one position (peec.py:2465-2511): present sheets `lay`, their impedances R and
+        self-inductance changes dl, the face couplings z12 {twin sheet: coupling} -> the S x S block.  A 'sheet'
+        block over all present sheets, a 2 x 2 block per face pair ('diag' with split layers), else diagonal."""
+        S, N = self.n_sheets, self.N
+        blk = np.zeros((S, S), complex)
+        if self.B is not None and not self.twin_diag and len(lay) >= 2:
+            groups = [list(range(len(lay)))]
+        elif self.twin_diag:
+            groups, used = [], set()
+            for q, k in enumerate(lay):
+                if k >= N and int(self.sheet_layer[k]) in lay:
+                    qa = lay.index(int(self.sheet_layer[k]))
+                    groups.append([qa, q])
+                    used |= {qa, q}
+            groups += [[q] for q in range(len(lay)) if q not in used]
+        else:
+            groups = [[q] for q in range(len(lay))]
+        for g in groups:
+            sh = [lay[q] for q in g]
+            if len(g) == 1:
+                blk[sh[0], sh[0]] = 1.0 / (R[g[0]] + 1j * w * (self.L_self + dl[g[0]]))
+                continue
+            Z = 1j * w * self.B[name][np.ix_(sh, sh)] + np.diag(R[g] + 1j * w * dl[g])
+            for ib, k in enumerate(sh):
+                if k >= N and int(self.sheet_layer[k]) in sh:
+                    ia = sh.index(int(self.sheet_layer[k]))
+                    cross = z12[k] + 1j * w * dl[g[ib]] * (self.dL is not None)
+                    Z[ia, ib] += cross
+                    Z[ib, ia] += cross
+            blk[np.ix_(sh, sh)] = np.linalg.inv(Z)
+        return blk
 
     def _widths(self):
         """Strips narrower than the pitch (peec.py:1732-1820): strip_width and r_width per strip (fractions of
         the pitch), dL (the self-inductance change, None when every strip is full) and M_near (sparse side-by-side
         mutual changes); then the device's view of them: the strip positions whose D^-1 blocks are their own
         (override), and the rows of the system product's corrections."""
-        t, S = self.top, self.N
+        t, S = self.top, self.n_sheets
         sx, sy = (self.nx - 1, self.ny), (self.nx, self.ny - 1)
+        lx, ly = self.layer_index("x"), self.layer_index("y")      # a face sheet has its layer's copper
 
         def gather(attr, idx, shape, default):
             if len(idx) == 0:
@@ -308,16 +417,16 @@ class PlaneStack:
             w = np.stack([np.asarray(getattr(l.grid, attr), float) if getattr(l.grid, attr, None) is not None
                           else np.full(shape, default) for l in self.layers])
             return w[tuple(idx.T)]
-        w = np.concatenate([gather("wx", t.xa, sx, 1.0), gather("wy", t.ya, sy, 1.0)])
+        w = np.concatenate([gather("wx", lx, sx, 1.0), gather("wy", ly, sy, 1.0)])
         ok = w > 0
         self.strip_width = np.where(ok, w, 1.0)
-        rw = np.concatenate([gather("rx", t.xa, sx, 0.0), gather("ry", t.ya, sy, 0.0)])
+        rw = np.concatenate([gather("rx", lx, sx, 0.0), gather("ry", ly, sy, 0.0)])
         self.r_width = np.where(ok & (rw > 0), rw, self.strip_width)
-        off = np.where(ok, np.concatenate([gather("ox", t.xa, sx, 0.0), gather("oy", t.ya, sy, 0.0)]), 0.0)
+        off = np.where(ok, np.concatenate([gather("ox", lx, sx, 0.0), gather("oy", ly, sy, 0.0)]), 0.0)
         self.dL = self.M_near = None
         narrow = self.strip_width < 1.0
         if np.any(narrow):
-            th = self.ts[np.concatenate([t.xa[:, 0], t.ya[:, 0]])]
+            th = self.ts[np.concatenate([lx[:, 0], ly[:, 0]])]
             dL = np.zeros(self.ns)
             keys, inv = np.unique(np.round(np.column_stack([self.strip_width[narrow], th[narrow]]), 12), axis=0,
                                   return_inverse=True)
@@ -354,6 +463,16 @@ class PlaneStack:
                       - greens.side_mutual(self.d, one, one, one, keys[:, 3]))[np.ravel(inv)]
                 M = sp.coo_matrix((dM, (a, b)), shape=(self.ns, self.ns))
                 self.M_near = (M + M.T).tocsr()
+            if len(self.tw_b):
+                # a split layer's faces share their copper's corrections (peec.py:1822-1843)
+                n = self.ns
+                pairs = np.concatenate([self.tw_a, self.tw_b]), np.concatenate([self.tw_b, self.tw_a])
+                extra = sp.coo_matrix((np.concatenate([self.dL[self.tw_a], self.dL[self.tw_b]]), pairs),
+                                      shape=(n, n))
+                if self.M_near is not None:
+                    swap = sp.coo_matrix((np.ones(len(pairs[0])), pairs), shape=(n, n)).tocsr()
+                    extra = extra + self.M_near @ swap
+                self.M_near = ((self.M_near if self.M_near is not None else 0) + extra).tocsr()
         # the device's view: positions with a strip that is not a full square get their own D^-1 block
         odd = (self.strip_width != 1.0) | (self.r_width != 1.0)
         if self.dL is not None:
@@ -369,9 +488,17 @@ class PlaneStack:
                 self.override[name][i, j] = len(self.override_pos)
                 self.override_pos.append((o, int(i), int(j)))
         self.n_override = len(self.override_pos)
-        # correction rows: strips with a resistance factor, a self change or side-by-side changes
-        rows = np.flatnonzero(odd | (np.diff(self.M_near.indptr) > 0 if self.M_near is not None
-                                     else np.zeros(self.ns, bool)))
+        # correction rows: strips with a resistance factor, a self change, side-by-side changes or a face partner
+        partner = -np.ones(self.ns, np.int64)
+        partner[self.tw_a], partner[self.tw_b] = self.tw_b, self.tw_a
+        twin = -np.ones(self.ns, np.int64)
+        tw_fac = np.zeros(self.ns)
+        if len(self.tw_b):
+            m = self.sheet_of_strip(self.tw_b) - self.N
+            twin[self.tw_a], twin[self.tw_b] = m, m
+            tw_fac[self.tw_a] = tw_fac[self.tw_b] = 1.0 / self.r_width[self.tw_b]
+        rows = np.flatnonzero(odd | (partner >= 0) | (np.diff(self.M_near.indptr) > 0 if self.M_near is not None
+                                                       else np.zeros(self.ns, bool)))
         c2d = self.dense.compact_to_dense
         M = self.M_near[rows] if self.M_near is not None else sp.csr_matrix((len(rows), max(self.ns, 1)))
         self.narrow_rows = {
@@ -382,13 +509,17 @@ class PlaneStack:
             "ptr": M.indptr.astype(np.int64),
             "col": c2d[M.indices].astype(np.int64),
             "val": M.data.astype(np.float64),
+            "partner": np.where(partner[rows] >= 0, c2d[np.maximum(partner[rows], 0)], -1).astype(np.int64),
+            "twin": np.maximum(twin[rows], 0).astype(np.int32),
+            "tw_fac": tw_fac[rows],
         }
 
     def _schur_structure(self, leaf: int):
         """S = Ar^T D^-1 Ar as a linear map of the per-frequency admittance table, and its symbolic analysis."""
-        t, S, nx, ny = self.top, self.N, self.nx, self.ny
+        t, S, nx, ny = self.top, self.n_sheets, self.nx, self.ny
         nxy = nx * ny
         self.sheet = self.B is not None
+        lay = self.sheet_layer
         ncode = 1 << S
         self.code = {"x": np.zeros((nx - 1, ny), np.uint8), "y": np.zeros((nx, ny - 1), np.uint8)}
         for k in range(S):
@@ -415,19 +546,21 @@ class PlaneStack:
                 continue
             k, i, j = idx[:, 0], idx[:, 1], idx[:, 2]
             code = self.code["x" if o == 0 else "y"][i, j].astype(np.int64)
-            ends1 = (t.nid[k, i, j], t.nid[k, i + di, j + dj])
+            ends1 = (t.nid[lay[k], i, j], t.nid[lay[k], i + di, j + dj])     # a strip joins its layer's nodes
             partners = range(S) if self.sheet else [None]
             for l in partners:
                 if l is None:                      # diagonal D: each strip with itself
                     ll = k
                     sel = np.ones(len(k), bool)
-                else:                              # blocks: every strip present at the same position
-                    ll = np.full(len(k), l)
+                else:                              # blocks: every strip present at the same position (with split
+                    ll = np.full(len(k), l)        # layers under 'diag': only a face pair)
                     sel = (code >> l) & 1 == 1
+                    if self.twin_diag:
+                        sel &= lay[k] == lay[l]
                 ovr = self.override["x" if o == 0 else "y"][i, j].astype(np.int64)
                 tab = np.where(ovr >= 0, self.tab_ovr0 + (ovr * S + k) * S + ll, ((o * ncode + code) * S + k) * S + ll)
                 e1 = (ends1[0][sel], ends1[1][sel])
-                e2 = (t.nid[ll[sel], i[sel], j[sel]], t.nid[ll[sel], i[sel] + di, j[sel] + dj])
+                e2 = (t.nid[lay[ll[sel]], i[sel], j[sel]], t.nid[lay[ll[sel]], i[sel] + di, j[sel] + dj])
                 add(e1, e2, tab[sel])
         cu = t.cap[:, :4].astype(np.int64)
         if len(cu):
@@ -488,7 +621,7 @@ class PlaneStack:
         t, kept = layout.topology([l.grid.node for l in root.layers], [l.grid.xb for l in root.layers],
                                   [l.grid.yb for l in root.layers], root.d,
                                   [(p.upper, p.lower, p.c_per_area, p.tan_delta) for p in root.pairs],
-                                  [(br.a, br.b) for br in branches])
+                                  [(br.a, br.b) for br in branches], root.twin_parent)
         if len(kept) != len(branches) or not np.array_equal(t.keep, root.keep):
             raise RuntimeError("a derived stack must keep its base's nodes")
         # a shallow copy shares the grids, spectra, symbolic analysis and S-term map (which covers the base's
@@ -526,11 +659,20 @@ class PlaneStack:
 
     # ------------------------------------------------------------------ per-frequency data
     def _freq_tables(self, f: float):
-        """(omega, sheet impedances (S,), cap impedances (npairs,), branch impedances (nbr,), admittance
-        table (n_table,)) at f: peec.py:2150-2178 and 2465-2511 restated over the table."""
+        """(omega, per operator the sheet impedances (S,) then the split layers' face couplings (n_twins,), cap
+        impedances (npairs,), branch impedances (nbr,), admittance table (n_table,)) at f: peec.py:2150-2197 and
+        2465-2511 restated over the table."""
         w = 2 * math.pi * f
-        S = self.N
-        zs = np.array([complex(greens.slab_impedance(l.thickness, f, self.sigma)) for l in self.layers])
+        S, N = self.n_sheets, self.N
+        zl = np.array([complex(greens.slab_impedance(l.thickness, f, self.sigma)) for l in self.layers])
+        zsh = zl[self.sheet_layer]                         # a sheet's impedance per square
+        zm = np.zeros(len(self.twin_parent), complex)
+        if len(self.twin_parent):
+            # a split layer's two faces: the face pair's own impedance and their coupling (peec.py:2161-2166)
+            zself, zmut = greens.face_sheet_impedance(self.ts, f, self.sigma)
+            for m, p in enumerate(self.twin_parent):
+                zsh[p] = zsh[N + m] = zself[p]
+                zm[m] = zmut[p]
         pl = self.top.pair_layers
         C = np.array([p.c_per_area for p in self.pairs]) * self.d ** 2
         tand = np.array([p.tan_delta for p in self.pairs])
@@ -538,29 +680,22 @@ class PlaneStack:
         zbr = np.array([complex(b.z(f)) for b in self.branches], complex)
         ncode = 1 << S
         tab = np.zeros(self.n_table, complex)
-        dself = 1.0 / (zs + 1j * w * self.L_self)
+        z12 = {N + m: zm[m] for m in range(len(zm))}
         for o, name in enumerate("xy"):
             for code in range(1, ncode):
                 lay = [k for k in range(S) if code >> k & 1]
-                blk = np.zeros((S, S), complex)
-                if self.sheet and len(lay) >= 2:
-                    Bo = self.B[name][np.ix_(lay, lay)]
-                    Zi = np.linalg.inv(np.diag(zs[lay]) + 1j * w * Bo)
-                    blk[np.ix_(lay, lay)] = Zi
-                else:
-                    for k in lay:
-                        blk[k, k] = dself[k]
+                blk = self._dinv_block(name, lay, zsh[lay], np.zeros(len(lay)), z12, w)
                 tab[(o * ncode + code) * S * S: (o * ncode + code + 1) * S * S] = blk.ravel()
         if self.n_override:
-            self._override_blocks(tab, w, zs, dself)
+            self._override_blocks(tab, w, zsh, zm)
         tab[self.tab_cap0: self.tab_br0] = 1.0 / zcap if len(pl) else []
         tab[self.tab_br0:] = 1.0 / zbr if self.nbr else []
-        return w, zs, zcap, zbr, tab
+        return w, np.concatenate([zsh, zm]), zcap, zbr, tab
 
-    def _override_blocks(self, tab: np.ndarray, w: float, zs: np.ndarray, dself: np.ndarray):
+    def _override_blocks(self, tab: np.ndarray, w: float, zsh: np.ndarray, zm: np.ndarray):
         """D^-1 blocks of the positions whose strips are not all full squares (peec.py:2480-2509: each such
-        position its own R / width and self inductance + dL; a sheet block where two or more strips share it)."""
-        t, S = self.top, self.N
+        position its own R / width and self inductance + dL, a face pair's coupling / width)."""
+        t, S, N = self.top, self.n_sheets, self.N
         sidx = {}
         for name, idx, lo in (("x", t.xa, 0), ("y", t.ya, self.nxb)):
             a = -np.ones((S, *self.override[name].shape), np.int64)
@@ -573,14 +708,9 @@ class PlaneStack:
             strips = sidx[name][:, i, j]
             lay = [k for k in range(S) if strips[k] >= 0]
             st_ = strips[lay]
-            R = zs[lay] / self.r_width[st_]
-            blk = np.zeros((S, S), complex)
-            if self.sheet and len(lay) >= 2:
-                Z = 1j * w * self.B[name][np.ix_(lay, lay)] + np.diag(R + 1j * w * dL[st_])
-                blk[np.ix_(lay, lay)] = np.linalg.inv(Z)
-            else:
-                for k, sq, r in zip(lay, st_, R):
-                    blk[k, k] = 1.0 / (r + 1j * w * (self.L_self + dL[sq]))
+            R = zsh[lay] / self.r_width[st_]
+            z12 = {k: zm[k - N] / self.r_width[strips[k]] for k in lay if k >= N}
+            blk = self._dinv_block(name, lay, R, dL[st_], z12, w)
             tab[self.tab_ovr0 + q * S * S: self.tab_ovr0 + (q + 1) * S * S] = blk.ravel()
 
     def operator(self, f: float):
@@ -706,8 +836,8 @@ class PlaneStack:
         """psi of every strip (peec.py:2615-2656): on the device for a device stack (gt_strip_coupling), the
         host restatement otherwise."""
         if self.handle is not None:
-            return self.handle.strip_coupling(self.zs, self.ts, self.d, segments, self.ns)
-        px, py = greens.strip_coupling(segments, [self.xa, self.ya], self.d, self.zs, self.ts)
+            return self.handle.strip_coupling(self.sheet_z, self.sheet_t, self.d, segments, self.ns)
+        px, py = greens.strip_coupling(segments, [self.xa, self.ya], self.d, self.sheet_z, self.sheet_t)
         return np.concatenate([px, py])
 
     def branch_coupling(self, segments: np.ndarray, start: int = 0, branches: Optional[list] = None) -> np.ndarray:
@@ -733,11 +863,11 @@ class PlaneStack:
             m += 0.5 * s[7] * np.cross(s[0:3], s[3:6])
         d = self.d
         Ix, Iy = Ib[: self.nxb], Ib[self.nxb: self.ns]
-        k, _, j = self.xa.T
-        m[1] += 0.5 * np.sum(self.zs[k] * d * Ix)
+        k, _, j = self.xa.T                         # each strip at its sheet's height
+        m[1] += 0.5 * np.sum(self.sheet_z[k] * d * Ix)
         m[2] += 0.5 * np.sum(-(j * d) * d * Ix)
         k, i, _ = self.ya.T
-        m[0] += 0.5 * np.sum(-self.zs[k] * d * Iy)
+        m[0] += 0.5 * np.sum(-self.sheet_z[k] * d * Iy)
         m[2] += 0.5 * np.sum((i * d) * d * Iy)
         I_cap = Ib[self.ns: self.ns + self.ncap]
         if len(I_cap):
@@ -816,15 +946,17 @@ class RouteExcitation:
         w = 2 * math.pi * f
         I_x = np.zeros((st.N, st.nx - 1, st.ny), complex)
         I_y = np.zeros((st.N, st.nx, st.ny - 1), complex)
-        I_x[tuple(st.xa.T)] = Ib[: st.nxb]
-        I_y[tuple(st.ya.T)] = Ib[st.nxb: st.ns]
+        # per layer: a split layer's two faces added (peec.py:2796-2803)
+        np.add.at(I_x, tuple(st.layer_index("x").T), Ib[: st.nxb])
+        np.add.at(I_y, tuple(st.layer_index("y").T), Ib[st.nxb: st.ns])
         Vg = np.zeros((st.N, st.nx, st.ny), complex)
         Vg[np.nonzero(st.node)] = V[: st.n_grid]
         v_inj = sum(a * V[n] for n, a in self.injections)
         Z = complex(greens.trace_resistance(self.segments, f, st.sigma, self.trace_t) + v_inj
                     + 1j * w * (self.L_trace + np.dot(self.psi, Ib)))
         return Solution(f, I_x, I_y, Vg, Ib[st.ns + st.ncap:].copy(), Z, st.moment(self.segments, Ib), its,
-                        Ib[st.ns: st.ns + st.ncap].copy(), res)
+                        Ib[st.ns: st.ns + st.ncap].copy(), res,
+                        np.stack([Ib[st.tw_a], Ib[st.tw_b]]) if len(st.tw_b) else None)
 
     def solve(self, f: float, guess=None, tol: float = 1e-5) -> Solution:
         Ib, V, its, x = self.stack.solve(f, self.rhs_top(f), self.J(), tol=tol, guess=guess)[:4]
@@ -848,7 +980,8 @@ def from_board(board, _device: bool = True):
     layers = [PlaneLayer(l.name, l.z, g, l.thickness) for l, g in zip(board.layers, grids)]
     branches = [Branch(b.a, b.b, b.z, f"br{n}", b.kind, b.radius) for n, b in enumerate(board.branches)]
     pairs = [PlanePair(p.upper, p.lower, p.c_per_area, p.tan_delta) for p in board.pairs]
-    st = PlaneStack(layers, branches, pairs, board.sigma, precond=board.precond, screen=False, _device=_device)
+    st = PlaneStack(layers, branches, pairs, board.sigma, precond=board.precond, screen=board.screen,
+                    _device=_device)
     routes = []
     for net in board.nets:
         trace = [TraceSegment(s[0:3].copy(), s[3:6].copy(), float(s[6]), float(s[7])) for s in net.segments]

@@ -96,6 +96,17 @@ typedef struct gt_geometry_desc {
     const int64_t* narrow_ptr;
     const int64_t* narrow_col;
     const double* narrow_val;
+    /* Face sheets of screened layers (PlaneStack._faces / _twins, peec.py:1658-1716): n_layers node layers
+     * (0: as many as sheets) and each sheet's layer sheet_layer[n_sheets] (the lower faces of the n_twins split
+     * layers follow the layers).  The V segment holds n_layers x nx x ny nodes.  Rows of the narrow list with
+     * narrow_partner >= 0 add the face coupling z_mut(narrow_twin) * narrow_twfac * x[narrow_partner]; the
+     * operators' zs then carry, per operator, the n_sheets sheet impedances followed by the n_twins couplings. */
+    int32_t n_layers;
+    const int32_t* sheet_layer;
+    int32_t n_twins;
+    const int64_t* narrow_partner;
+    const int32_t* narrow_twin;
+    const double* narrow_twfac;
 } gt_geometry_desc;
 
 typedef struct gt_solve_opts {
@@ -128,7 +139,7 @@ int gt_geometry_create(const gt_geometry_desc* desc, gt_geometry** out);
 void gt_geometry_free(gt_geometry* g);
 
 /* Factorise the Schur complement at n_ops frequencies (peec.py:2345-2445, 2465-2511):
- * omega[n_ops]; zs[n_ops*S] sheet impedances per square; zcap[n_ops*n_pairs] and zbr[n_ops*n_branches]
+ * omega[n_ops]; zs[n_ops*(S + n_twins)] sheet impedances per square (then the face couplings, with face sheets); zcap[n_ops*n_pairs] and zbr[n_ops*n_branches]
  * the capacitance / branch impedances; table[n_ops*n_table] the admittance table D^-1 draws from. */
 int gt_operators_create(gt_geometry* g, int32_t n_ops, const double* omega, const double* zs,
                         const double* zcap, const double* zbr, const double* table, gt_operators** out);

@@ -7,7 +7,7 @@ from groundtruth_gb300 import native, stack as gs
 from test_oracle_golden import load
 
 pytestmark = pytest.mark.gpu
-CASES = ["small_pair", "small_stack3", "plain_plane", "necked_pair"]
+CASES = ["small_pair", "small_stack3", "plain_plane", "necked_pair", "faces_stack3_diag", "faces_stack3_sheet"]
 
 
 def rel(a, b):
