@@ -210,10 +210,10 @@ def run_gpu(args):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for net in board.nets:
-        st.handle.strip_coupling(st.zs, st.ts, st.d, net.segments, st.ns)
+        st.handle.strip_coupling(st.sheet_z, st.sheet_t, st.d, net.segments, st.ns)
     psi_dev = (time.perf_counter() - t0) / len(board.nets)
     t0 = time.perf_counter()
-    greens.strip_coupling(board.nets[0].segments, [st.xa, st.ya], st.d, st.zs, st.ts)
+    greens.strip_coupling(board.nets[0].segments, [st.xa, st.ya], st.d, st.sheet_z, st.sheet_t)
     psi_host = time.perf_counter() - t0
     lib = st.handle.lib
     freqs = list(board.freqs)
