@@ -86,3 +86,28 @@ def test_excitation_matches_reference(case):
     for k, r in enumerate(routes):
         assert rel(r.psi, z[f"psi{k}"]) < 1e-13
         assert r.L_trace == pytest.approx(float(z[f"Ltrace{k}"]), rel=1e-13)
+
+
+@pytest.mark.parametrize("name", ["small_pair", "necked_pair", "faces_stack3_diag", "faces_stack3_sheet"])
+def test_schur_values_and_impedances_match_reference(name):
+    """The per-frequency admittance table through the S-term map gives the reference's own Schur complement
+    (narrow strips' own blocks, split layers' face blocks included), and the table's impedances its R_strip and
+    face coupling Z12."""
+    z, board = load(name)
+    st, routes = gs.from_board(board, _device=False)
+    for k in ("xa", "ya", "keep", "a_nodes", "b_nodes"):
+        assert np.array_equal(getattr(st.top, k), z[k]), k
+    f = float(z["op_f"])
+    w, zs, zcap, zbr, tab = st._freq_tables(f)
+    sym = st.sym
+    ij = z["op_S_ij"]
+    S_ref = sp.coo_matrix((z["op_S"], (ij[0], ij[1])), shape=(sym.n, sym.n)).tocsr()
+    fac = sym.perm[np.flatnonzero(st.top.node.ravel())[st.top.keep]]
+    P = sp.coo_matrix((np.ones(sym.n), (fac, np.arange(sym.n))), shape=(sym.n, sym.n)).tocsr()
+    ref = np.asarray((P @ S_ref @ P.T).tocsr()[sym.s_row, sym.s_col]).ravel()
+    assert np.abs(st.sterm @ tab - ref).max() <= 1e-14 * np.abs(ref).max()
+    R = zs[: st.n_sheets][np.concatenate([st.xa[:, 0], st.ya[:, 0]])] / st.r_width
+    assert rel(R, z["op_R"]) < 1e-14
+    if "op_Z12" in z.files:
+        Z12 = zs[st.n_sheets:][st.sheet_of_strip(st.tw_b) - st.N] / st.r_width[st.tw_b]
+        assert rel(Z12, z["op_Z12"]) < 1e-14
