@@ -453,6 +453,32 @@ def _labels(mask: np.ndarray, xb: np.ndarray, yb: np.ndarray) -> np.ndarray:
 WIDTH_KEYS = ("wx", "wy", "ox", "oy", "rx", "ry")
 
 
+def necked_faces(seed: int = 23) -> Board:
+    """faces_stack3 ('sheet' preconditioner) with strips narrower than the pitch on the split middle layer and
+    on the top one: the split layer's faces share their copper's corrections (PlaneStack._twin_corrections,
+    peec.py:1822-1843) and its face blocks carry them (peec.py:2497-2503)."""
+    rng = np.random.default_rng(seed)
+    b = faces_stack3("sheet")
+    b.name = "necked_faces"
+    for k in (0, 1):
+        l = b.layers[k]
+        nx, ny = l.node.shape
+        wx, wy = np.ones((nx - 1, ny)), np.ones((nx, ny - 1))
+        ox, oy = np.zeros((nx - 1, ny)), np.zeros((nx, ny - 1))
+        rx, ry = np.zeros((nx - 1, ny)), np.zeros((nx, ny - 1))
+        xs, ys = np.argwhere(l.xb), np.argwhere(l.yb)
+        for (i, j) in xs[rng.choice(len(xs), size=10, replace=False)]:
+            wx[i, j] = rng.uniform(0.3, 0.9)
+            ox[i, j] = rng.uniform(-0.5, 0.5) * (1 - wx[i, j])
+        for (i, j) in ys[rng.choice(len(ys), size=10, replace=False)]:
+            wy[i, j] = rng.uniform(0.3, 0.9)
+            oy[i, j] = rng.uniform(-0.5, 0.5) * (1 - wy[i, j])
+        i, j = xs[0]
+        rx[i, j] = 0.8 * wx[i, j] if wx[i, j] < 1 else 0.7
+        l.widths = {"wx": wx, "wy": wy, "ox": ox, "oy": oy, "rx": rx, "ry": ry}
+    return b
+
+
 def faces_stack3(precond: str = "diag") -> Board:
     """small_stack3 with screening on: its middle plane has copper above and below, so it is split into two
     face sheets (PlaneStack._faces, peec.py:1658-1697): four current sheets on three layers."""
@@ -595,4 +621,4 @@ def what_if_branches(board: Board, seed: int, n_via: int = 2, n_part: int = 1) -
 
 WORKLOADS = {"plain_plane": plain_plane, "slotted_pair": slotted_pair, "small_pair": small_pair,
              "small_stack3": small_stack3, "six_sheet": six_sheet, "necked_pair": necked_pair,
-             "faces_stack3": faces_stack3}
+             "faces_stack3": faces_stack3, "necked_faces": necked_faces}

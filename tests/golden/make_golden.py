@@ -20,7 +20,8 @@ The reference's solver module imports shapely at module level but uses it only t
 a neck; the grids' wx / wy, ox / oy, rx / ry), plus the reference's strip widths, dL and M_near.
 ``faces_stack3_diag.npz`` / ``faces_stack3_sheet.npz``: three planes with screening on (the middle one split
 into two face sheets, PlaneStack._faces), with either preconditioner, plus the sheets' layers, heights and twin
-pairs and the face coupling Z12.
+pairs and the face coupling Z12; ``necked_faces.npz`` the sheet-preconditioned one with narrow strips on the
+split layer and the top one (the faces' shared corrections).
 ``small_pair_derived.npz`` holds the same for small_pair plus a what-if edit's branches on a derived stack
 (PlaneStack.with_branches), including solves warm-started from the base's solutions.
 
@@ -189,6 +190,8 @@ def main():
     for pc in ("diag", "sheet"):
         print(f"faces_stack3_{pc}", flush=True)
         np.savez_compressed(HERE / f"faces_stack3_{pc}.npz", **record(peec, synth.faces_stack3(pc)))
+    print("necked_faces", flush=True)
+    np.savez_compressed(HERE / "necked_faces.npz", **record(peec, synth.necked_faces()))
     if args.faces_only:
         return
     print("necked_pair", flush=True)

@@ -7,7 +7,8 @@ from groundtruth_gb300 import native, stack as gs
 from test_oracle_golden import load
 
 pytestmark = pytest.mark.gpu
-CASES = ["small_pair", "small_stack3", "plain_plane", "necked_pair", "faces_stack3_diag", "faces_stack3_sheet"]
+CASES = ["small_pair", "small_stack3", "plain_plane", "necked_pair", "faces_stack3_diag", "faces_stack3_sheet",
+         "necked_faces"]
 
 
 def rel(a, b):

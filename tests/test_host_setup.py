@@ -88,7 +88,7 @@ def test_excitation_matches_reference(case):
         assert r.L_trace == pytest.approx(float(z[f"Ltrace{k}"]), rel=1e-13)
 
 
-@pytest.mark.parametrize("name", ["small_pair", "necked_pair", "faces_stack3_diag", "faces_stack3_sheet"])
+@pytest.mark.parametrize("name", ["small_pair", "necked_pair", "faces_stack3_diag", "faces_stack3_sheet", "necked_faces"])
 def test_schur_values_and_impedances_match_reference(name):
     """The per-frequency admittance table through the S-term map gives the reference's own Schur complement
     (narrow strips' own blocks, split layers' face blocks included), and the table's impedances its R_strip and

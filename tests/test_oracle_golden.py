@@ -13,7 +13,8 @@ from groundtruth_gb300 import synth
 from oracle import peec_oracle as po
 
 GOLD = Path(__file__).resolve().parent / "golden"
-CASES = ["small_pair", "small_stack3", "plain_plane", "necked_pair", "faces_stack3_diag", "faces_stack3_sheet"]
+CASES = ["small_pair", "small_stack3", "plain_plane", "necked_pair", "faces_stack3_diag", "faces_stack3_sheet",
+         "necked_faces"]
 
 
 def load(name):
