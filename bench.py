@@ -381,8 +381,8 @@ def run_gpu(args):
 
 # ------------------------------------------------------------------------------------------ what-if edits
 def run_what_if(args):
-    """Interactive edits on a solved board: each request adds 1-4 stitching vias (70 %) or one decoupling
-    part and answers 1-8 nets at 1-16 of the base's frequencies (whatif.WhatIf: composed from base solves of
+    """Interactive edits on a solved board: each request adds 1-4 stitching vias (60 %), adds a decoupling part
+    (20 %) or moves one (20 %: removed, added elsewhere) and answers 1-8 nets at 1-16 of the base's frequencies (whatif.WhatIf: composed from base solves of
     the new branches' injections, or solved on the derived stack).  Requests run one after another; their
     service times also drive a FIFO queue with Poisson arrivals at --rate."""
     import torch
@@ -401,22 +401,24 @@ def run_what_if(args):
     n_base = len(routes) * len(board.freqs)
     reqs = []
     for r in range(args.warmup + args.requests):
-        vias = rng.random() < 0.7
+        u = rng.random()            # 60 % add 1-4 vias, 20 % add a decoupling part, 20 % move one
+        vias = u < 0.6
         extra = synth.what_if_branches(board, seed=1000 + r, n_via=int(rng.integers(1, 5)) if vias else 0,
                                        n_part=0 if vias else 1)
+        remove = [int(rng.integers(0, st.nbr))] if u >= 0.8 and st.nbr else []
         nets = sorted(int(k) for k in rng.choice(len(routes), size=int(rng.integers(1, 9)), replace=False))
         fq = sorted(int(q) for q in rng.choice(len(board.freqs), size=int(rng.integers(1, 17)), replace=False))
         reqs.append(([gs.Branch(b.a, b.b, b.z, f"edit{r}_{n}", b.kind, b.radius) for n, b in enumerate(extra)],
-                     nets, [float(board.freqs[q]) for q in fq]))
+                     nets, [float(board.freqs[q]) for q in fq], remove))
     from groundtruth_gb300 import native
     lib = native.load()
     clocks = Clocks(int(os.environ.get("LOCAL_RANK", 0)))
     service, cols, its, parts, worst, l0 = [], [], [], [], 0.0, 0
-    for r, (br, nets, fq) in enumerate(reqs):
+    for r, (br, nets, fq, remove) in enumerate(reqs):
         if r == args.warmup:
             clocks.start()
             l0 = lib.gt_launch_count()
-        res = wi.evaluate(br, nets, fq)
+        res = wi.evaluate(br, nets, fq, remove=remove)
         if r < args.warmup:
             continue
         service.append(res.seconds)
@@ -438,7 +440,7 @@ def run_what_if(args):
         "metric": "what-if edit latency (p50)", "value": ms(np.median(sv)), "unit": "ms", "n_gpus": 1,
         "higher_is_better": False, "impl": "gb300", "dtype": "c64 inner / c128 outer", "data": "synthetic",
         "config": {"workload": f"what_if_base {board.nx}x{board.ny} @{board.d * 1e3:g}mm GND slot + split PWR, "
-                               f"{len(routes)} nets x {len(board.freqs)} freqs; edits: 1-4 vias | 1 decap, "
+                               f"{len(routes)} nets x {len(board.freqs)} freqs; edits: 1-4 vias | add 1 decap | move 1 decap, "
                                "1-8 nets x 1-16 freqs", "tol": board.tol, "max_cols": args.max_cols},
         "requests": len(sv), "warmup": args.warmup, "p50_ms": ms(np.median(sv)), "p99_ms": ms(np.quantile(sv, 0.99)),
         "mean_ms": ms(sv.mean()), "max_ms": ms(sv.max()), "columns_per_request": float(np.mean(cols)),

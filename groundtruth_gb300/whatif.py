@@ -2,7 +2,8 @@
 and 452-465, on PlaneStack.with_branches, peec.py:1871-1923).
 
 The base board is solved once per net and frequency.  An edit adds k branches (stitching vias, a decoupling
-part) without joining separate pieces of copper.  Two ways to answer it:
+part; a part moved elsewhere is its removal, a parallel branch of the opposite impedance, plus its addition)
+without joining separate pieces of copper.  Two ways to answer it:
 
 * "bordered" (default): the edited system is the base system bordered by the k new branch currents,
       [K  F] [x]   [b    ]      F = the new branches' injections into the KCL rows,
@@ -134,12 +135,18 @@ class WhatIf:
         self.base_psi_ib = {(k, f): complex(np.dot(self.routes[k].psi, x[: st.nb])) for (k, f), x in zip(cols, xs)}
         return time.perf_counter() - t0
 
-    def evaluate(self, branches: list, nets, freqs) -> EditResult:
-        """The base plus `branches`, answered for the given nets (indices) at the given frequencies (a subset
-        of the base's)."""
+    def evaluate(self, branches: list, nets, freqs, remove=()) -> EditResult:
+        """The base plus `branches` and without the base's branches numbered in `remove` (a moved part: removed
+        and added elsewhere), answered for the given nets (indices) at the given frequencies (a subset of the
+        base's).  A removed branch is cancelled by a parallel one of the opposite impedance and the same coupling
+        to the signal path: the pair's net current is zero, so the edited system's solution is the one without
+        the branch (its unknowns keep the pair)."""
         if not self.base:
             raise RuntimeError("solve the baseline first")
         st = self.stack
+        branches = list(branches) + [
+            gs.Branch(st.branches[q].a, st.branches[q].b, (lambda f, z=st.branches[q].z: -z(f)),
+                      f"-{st.branches[q].name}", st.branches[q].kind, st.branches[q].radius) for q in remove]
         keep = [b for b in branches if st.node_id(b.a) >= 0 and st.node_id(b.b) >= 0 and tuple(b.a) != tuple(b.b)]
         joins = any(st.full_label[st.node_id(b.a)] != st.full_label[st.node_id(b.b)] for b in keep)
         if self.method == "bordered" and keep and not joins:

@@ -193,3 +193,26 @@ def test_bordered_edit_composition_on_cpu(derived):
         sol = col.solution()
         x = sol.state_for(st.with_branches(branches_of(extra)))
         assert rel(x[: odst.nb], ref["x"][: odst.nb]) < 1e-6
+
+
+def test_moved_part_composition_on_cpu(derived):
+    """A moved decoupling part (removed at its place, added at another) through the bordered composition equals
+    the oracle's solve of the board with the part moved."""
+    from groundtruth_gb300 import whatif
+    z, board, extra, ost, odst = derived
+    st, routes = gs.from_board(board, _device=False)
+    backed = _OracleBacked(st, ost)
+    st.factorise = lambda *a, **k: None
+    st.solve_batch = backed.solve_batch
+    wi = whatif.WhatIf(st, routes, board.freqs[1:2], tol=1e-9)
+    wi.baseline()
+    decap = board.branches[0]
+    moved = synth.BranchSpec((0, 30, 10), (1, 30, 10), decap.R, decap.L, decap.C, decap.kind, decap.radius)
+    res = wi.evaluate(branches_of([moved]), [0], [float(board.freqs[1])], remove=[0])
+    whole = synth.Board.from_arrays(board.to_arrays())
+    whole.branches = [moved] + list(board.branches[1:])
+    wst = oracle_stack(whole)
+    ref = oracle_routes(wst, whole)[0].solve(float(board.freqs[1]), tol=1e-12)
+    col = res.solutions[(0, float(board.freqs[1]))]
+    assert abs(col.Z_loop - ref["Z_loop"]) <= 1e-7 * abs(ref["Z_loop"])
+    assert np.linalg.norm(col.m - ref["m"]) <= 1e-6 * np.linalg.norm(ref["m"])
