@@ -126,3 +126,23 @@ def test_what_if_methods_agree_with_oracle_whole_stack(case, method):
         assert sol.residual <= board.tol
     if method == "bordered":
         assert res.parts["border_columns"] == len(more) * len(board.freqs)
+
+
+@pytest.mark.parametrize("method", ["bordered", "derived"])
+def test_moved_part_matches_oracle(case, method):
+    """A decoupling part moved elsewhere (removed and added) answered on the device equals the oracle's solve of
+    the board with the part moved."""
+    from groundtruth_gb300 import whatif
+    z, board, extra, st, routes, dst = case
+    decap = board.branches[0]
+    moved = synth.BranchSpec((0, 30, 10), (1, 30, 10), decap.R, decap.L, decap.C, decap.kind, decap.radius)
+    whole = synth.Board.from_arrays(board.to_arrays())
+    whole.branches = [moved] + list(board.branches[1:])
+    oroutes = oracle_routes(oracle_stack(whole), whole)
+    wi = whatif.WhatIf(st, routes, board.freqs, tol=board.tol, method=method)
+    wi.baseline()
+    f = float(board.freqs[1])
+    res = wi.evaluate(branches_of([moved]), [0, 1], [f], remove=[0])
+    for k in (0, 1):
+        ref = oroutes[k].solve(f, tol=board.tol)
+        assert abs(res.solutions[(k, f)].Z_loop - ref["Z_loop"]) <= 1e-8 * abs(ref["Z_loop"]), (method, k)
