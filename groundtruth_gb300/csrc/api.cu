@@ -1094,6 +1094,11 @@ int gt_geometry_create(const gt_geometry_desc* d, gt_geometry** out) {
             nw.tw_fac = p.upload(d->narrow_twfac, nr);
             nw.ntw = d->n_twins;
         }
+        if (d->narrow_rre) {
+            if (!d->narrow_twre) throw Invalid("narrow_rre needs narrow_twre");
+            nw.rre = p.upload(d->narrow_rre, nr);
+            nw.twre = p.upload(d->narrow_twre, nr);
+        }
     }
     G->n_compact = d->n_compact;
     G->d_c2d = p.upload(d->compact_to_dense, d->n_compact);

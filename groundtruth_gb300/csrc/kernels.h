@@ -45,6 +45,9 @@ struct Narrow {
     const int* twin = nullptr;
     const double* tw_fac = nullptr;
     int ntw = 0;
+    // resistance factors (null: none): out[p] += rre Re(z) x[p] + twre Re(z_mut) x[partner]
+    const double* rre = nullptr;
+    const double* twre = nullptr;
 };
 template <typename R>
 void launch_narrow(const Narrow& nw, const cx<R>* x, cx<R>* out, int64_t ld, int ncol, int S, const int* col_op,

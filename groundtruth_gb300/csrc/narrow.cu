@@ -31,8 +31,12 @@ __global__ void __launch_bounds__(128) narrow_kernel(Narrow nw, const cx<R>* __r
     } else {
         const cx<R> z = cvt<R>(zs[(int64_t)op * S + nw.sheet[q]]);
         y = R(nw.rdelta[q]) * (z * xc[p]) + R(omega[op]) * jmul(acc);
-        if (nw.partner && nw.partner[q] >= 0)       // the face coupling of a split layer's two strips
-            y += R(nw.tw_fac[q]) * (cvt<R>(zmut[(int64_t)op * nw.ntw + nw.twin[q]]) * xc[nw.partner[q]]);
+        if (nw.rre) y += (R(nw.rre[q]) * z.re) * xc[p];           // a resistance factor: the real part only
+        if (nw.partner && nw.partner[q] >= 0) {     // the face coupling of a split layer's two strips
+            const cx<R> zm = cvt<R>(zmut[(int64_t)op * nw.ntw + nw.twin[q]]);
+            y += R(nw.tw_fac[q]) * (zm * xc[nw.partner[q]]);
+            if (nw.twre) y += (R(nw.twre[q]) * zm.re) * xc[nw.partner[q]];
+        }
         if (mode == 1) y = zero<R>() - y;
     }
     out[(int64_t)col * ld + p] += y;

@@ -43,7 +43,8 @@ class GeometryDesc(C.Structure):
                 ("n_narrow", C.c_int64), ("narrow_pos", I64P), ("narrow_sheet", I32P), ("narrow_rdelta", DP),
                 ("narrow_dl", DP), ("narrow_ptr", I64P), ("narrow_col", I64P), ("narrow_val", DP),
                 ("n_layers", C.c_int32), ("sheet_layer", I32P), ("n_twins", C.c_int32),
-                ("narrow_partner", I64P), ("narrow_twin", I32P), ("narrow_twfac", DP)]
+                ("narrow_partner", I64P), ("narrow_twin", I32P), ("narrow_twfac", DP),
+                ("narrow_rre", DP), ("narrow_twre", DP)]
 
 
 PRECISIONS = {"mixed": 0, "fp64": 1, "mixed16": 2}
@@ -183,6 +184,9 @@ class Geometry:
             d.narrow_ptr = _ptr(arr(nr["ptr"], np.int64), C.c_int64)
             d.narrow_col = _ptr(arr(nr["col"] if len(nr["col"]) else np.zeros(1), np.int64), C.c_int64)
             d.narrow_val = _ptr(arr(nr["val"] if len(nr["val"]) else np.zeros(1), np.float64), C.c_double)
+            if np.any(nr["rre"] != 0) or np.any(nr["twre"] != 0):
+                d.narrow_rre = _ptr(arr(nr["rre"], np.float64), C.c_double)
+                d.narrow_twre = _ptr(arr(nr["twre"], np.float64), C.c_double)
             if len(st.tw_b):
                 d.narrow_partner = _ptr(arr(nr["partner"], np.int64), C.c_int64)
                 d.narrow_twin = _ptr(arr(nr["twin"], np.int32), C.c_int32)

@@ -230,7 +230,9 @@ class PlaneStack:
         self._twins()
         self.dense = layout.dense_layout(t)
         self._kernels()
+        self.r_scale = self.branch_scale = None
         self._widths()
+        self._corrections()
         self._schur_structure(leaf)
         self._lock = threading.Lock()
         self._ops: OrderedDict = OrderedDict()
@@ -473,8 +475,15 @@ class PlaneStack:
                     swap = sp.coo_matrix((np.ones(len(pairs[0])), pairs), shape=(n, n)).tocsr()
                     extra = extra + self.M_near @ swap
                 self.M_near = ((self.M_near if self.M_near is not None else 0) + extra).tocsr()
-        # the device's view: positions with a strip that is not a full square get their own D^-1 block
-        odd = (self.strip_width != 1.0) | (self.r_width != 1.0)
+
+    def _corrections(self):
+        """The device's view of the strips that are not full squares (narrow, a resistance width or factor):
+        the positions whose D^-1 blocks are their own (override) and the rows of the system product's corrections
+        (with a split layer's face partners)."""
+        t = self.top
+        sx, sy = (self.nx - 1, self.ny), (self.nx, self.ny - 1)
+        sc = self.r_scale if self.r_scale is not None else np.ones(self.ns)
+        odd = (self.strip_width != 1.0) | (self.r_width != 1.0) | (sc != 1.0)
         if self.dL is not None:
             odd |= self.dL != 0
         self.override = {"x": -np.ones(sx, np.int32), "y": -np.ones(sy, np.int32)}
@@ -493,10 +502,12 @@ class PlaneStack:
         partner[self.tw_a], partner[self.tw_b] = self.tw_b, self.tw_a
         twin = -np.ones(self.ns, np.int64)
         tw_fac = np.zeros(self.ns)
+        pair_sc = np.ones(self.ns)        # a face pair's coupling takes its lower strip's factor (peec.py:2196)
         if len(self.tw_b):
             m = self.sheet_of_strip(self.tw_b) - self.N
             twin[self.tw_a], twin[self.tw_b] = m, m
             tw_fac[self.tw_a] = tw_fac[self.tw_b] = 1.0 / self.r_width[self.tw_b]
+            pair_sc[self.tw_a] = pair_sc[self.tw_b] = sc[self.tw_b]
         rows = np.flatnonzero(odd | (partner >= 0) | (np.diff(self.M_near.indptr) > 0 if self.M_near is not None
                                                        else np.zeros(self.ns, bool)))
         c2d = self.dense.compact_to_dense
@@ -512,9 +523,12 @@ class PlaneStack:
             "partner": np.where(partner[rows] >= 0, c2d[np.maximum(partner[rows], 0)], -1).astype(np.int64),
             "twin": np.maximum(twin[rows], 0).astype(np.int32),
             "tw_fac": tw_fac[rows],
+            # a resistance factor scales the real part only: R = (Re z sc + j Im z) / w
+            "rre": (sc[rows] - 1.0) / self.r_width[rows],
+            "twre": (pair_sc[rows] - 1.0) * tw_fac[rows],
         }
 
-    def _schur_structure(self, leaf: int):
+    def _schur_structure(self, leaf: int, sym=None):
         """S = Ar^T D^-1 Ar as a linear map of the per-frequency admittance table, and its symbolic analysis."""
         t, S, nx, ny = self.top, self.n_sheets, self.nx, self.ny
         nxy = nx * ny
@@ -574,7 +588,7 @@ class PlaneStack:
         n = t.n_keep
         pattern = sp.coo_matrix((np.ones(len(U)), (U, Vv)), shape=(n, n)).tocsr()
         pattern = ((pattern + pattern.T) != 0).astype(np.float64)
-        self.sym = layout.symbolic(t, pattern, leaf)
+        self.sym = sym if sym is not None else layout.symbolic(t, pattern, leaf)
         sym = self.sym
         # kept index -> factor index
         node_dense = np.flatnonzero(t.node.ravel())
@@ -678,6 +692,8 @@ class PlaneStack:
         tand = np.array([p.tan_delta for p in self.pairs])
         zcap = 1.0 / (w * C * tand + 1j * w * C) if w > 0 else np.full(len(pl), 1e18 + 0j)
         zbr = np.array([complex(b.z(f)) for b in self.branches], complex)
+        if self.branch_scale is not None and len(zbr):   # a branch's resistance only (its inductance stays)
+            zbr = zbr.real * self.branch_scale[: len(zbr)] + 1j * zbr.imag
         ncode = 1 << S
         tab = np.zeros(self.n_table, complex)
         z12 = {N + m: zm[m] for m in range(len(zm))}
@@ -708,10 +724,36 @@ class PlaneStack:
             strips = sidx[name][:, i, j]
             lay = [k for k in range(S) if strips[k] >= 0]
             st_ = strips[lay]
-            R = zsh[lay] / self.r_width[st_]
-            z12 = {k: zm[k - N] / self.r_width[strips[k]] for k in lay if k >= N}
+            sc = self.r_scale[st_] if self.r_scale is not None else np.ones(len(st_))
+            R = (zsh[lay].real * sc + 1j * zsh[lay].imag) / self.r_width[st_]
+            z12 = {}
+            for k in lay:
+                if k >= N:
+                    sk = self.r_scale[strips[k]] if self.r_scale is not None else 1.0
+                    z12[k] = (zm[k - N].real * sk + 1j * zm[k - N].imag) / self.r_width[strips[k]]
             blk = self._dinv_block(name, lay, R, dL[st_], z12, w)
             tab[self.tab_ovr0 + q * S * S: self.tab_ovr0 + (q + 1) * S * S] = blk.ravel()
+
+    def set_resistance_scale(self, strips: Optional[np.ndarray] = None, branches: Optional[np.ndarray] = None):
+        """Scale the strips' resistances (one factor per strip, x strips then y strips) and the branches' (their
+        real part), e.g. by 1 + alpha (T - 20 C) for copper at its temperature; None: as built
+        (peec.py:2199-2216).  The factorisations made before are dropped; the device geometry is rebuilt with
+        the scaled strips' own preconditioner blocks and correction rows."""
+        r = None if strips is None else np.asarray(strips, float)
+        b = None if branches is None else np.asarray(branches, float)
+        if r is not None and len(r) != self.ns:
+            raise ValueError(f"{len(r)} strip factors for {self.ns} strips")
+        if b is not None and len(b) != len(self.branches):
+            raise ValueError(f"{len(b)} branch factors for {len(self.branches)} branches")
+        if self._base is not None:
+            raise ValueError("scale the base stack's resistances, then derive")
+        with self._lock:
+            self.r_scale, self.branch_scale = r, b
+            self._corrections()
+            self._schur_structure(self.leaf, sym=self.sym)
+            self._ops.clear()
+            if self._device:
+                self.handle = native_geometry(self)
 
     def operator(self, f: float):
         """The device operator (factorised Schur complement) at f's key, made once and cached."""

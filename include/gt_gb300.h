@@ -107,6 +107,11 @@ typedef struct gt_geometry_desc {
     const int64_t* narrow_partner;
     const int32_t* narrow_twin;
     const double* narrow_twfac;
+    /* Resistance factors (PlaneStack.set_resistance_scale, peec.py:2199-2216), NULL when none: per row the real
+     * part's extra factor of the strip's own impedance (narrow_rre = (scale - 1) / width) and of its face
+     * coupling (narrow_twre). */
+    const double* narrow_rre;
+    const double* narrow_twre;
 } gt_geometry_desc;
 
 typedef struct gt_solve_opts {

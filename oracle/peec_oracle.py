@@ -473,6 +473,7 @@ class OracleStack:
         self.screen = screen
         self.layer_t = np.array([l.thickness for l in layers], float)
         self._base: Optional[OracleStack] = None
+        self.r_scale = self.branch_scale = None
         self._topology(list(branches or []))
         self._kernels()
         self._widths()
@@ -828,13 +829,28 @@ class OracleStack:
             z_self = np.asarray(face_sheet_impedance(self.layer_t, f, self.sigma)[0])
             for tw in (self.tw_a, self.tw_b):
                 R_strip[tw] = z_self[lay[self.sheet_of_strip(tw)]] / self.r_width[tw]
+        if self.r_scale is not None and self.ns:       # the resistance only; the internal inductance stays
+            R_strip = R_strip.real * self.r_scale + 1j * R_strip.imag
         if self.ncap:
             C, tand = self.cap[:, 4], self.cap[:, 5]
             z_cap = 1.0 / (w * C * tand + 1j * w * C) if w > 0 else np.full(self.ncap, 1e18 + 0j)
         else:
             z_cap = np.zeros(0, complex)
         z_br = np.array([b.z(f) for b in self.branches], complex)
+        if self.branch_scale is not None and len(z_br):
+            z_br = z_br.real * self.branch_scale + 1j * z_br.imag
         return w, R_strip, np.concatenate([z_cap, z_br])
+
+    def set_resistance_scale(self, strips=None, branches=None):
+        """Scale the strips' resistances (one factor per strip) and the branches' (their real parts), e.g. copper
+        at its temperature; None: as built (peec.py:2199-2216)."""
+        self.r_scale = None if strips is None else np.asarray(strips, float)
+        self.branch_scale = None if branches is None else np.asarray(branches, float)
+        if self.r_scale is not None and len(self.r_scale) != self.ns:
+            raise ValueError(f"{len(self.r_scale)} strip factors for {self.ns} strips")
+        if self.branch_scale is not None and len(self.branch_scale) != len(self.branches):
+            raise ValueError(f"{len(self.branch_scale)} branch factors for {len(self.branches)} branches")
+        self.r_uniform = not np.any(self.r_width != 1.0) and self.r_scale is None
 
     def twin_z(self, f: float) -> Optional[np.ndarray]:
         """The face coupling impedance per twin pair: z_mutual of the face pair / the strip's width
@@ -842,7 +858,10 @@ class OracleStack:
         if not len(self.tw_b):
             return None
         z_mut = np.asarray(face_sheet_impedance(self.layer_t, f, self.sigma)[1])
-        return z_mut[self.sheet_layer[self.sheet_of_strip(self.tw_b)]] / self.r_width[self.tw_b]
+        z12 = z_mut[self.sheet_layer[self.sheet_of_strip(self.tw_b)]] / self.r_width[self.tw_b]
+        if self.r_scale is not None:
+            z12 = z12.real * self.r_scale[self.tw_b] + 1j * z12.imag
+        return z12
 
     def admittance(self, w, R_strip, z_tail, Z12=None) -> sp.csr_matrix:
         """peec.py:2465-2511."""

@@ -22,6 +22,8 @@ a neck; the grids' wx / wy, ox / oy, rx / ry), plus the reference's strip widths
 into two face sheets, PlaneStack._faces), with either preconditioner, plus the sheets' layers, heights and twin
 pairs and the face coupling Z12; ``necked_faces.npz`` the sheet-preconditioned one with narrow strips on the
 split layer and the top one (the faces' shared corrections).
+``necked_pair_scaled.npz`` / ``faces_stack3_sheet_scaled.npz``: those boards with seeded resistance factors on
+every strip and branch (PlaneStack.set_resistance_scale): products and solves.
 ``small_pair_derived.npz`` holds the same for small_pair plus a what-if edit's branches on a derived stack
 (PlaneStack.with_branches), including solves warm-started from the base's solutions.
 
@@ -162,6 +164,36 @@ def record_derived(peec, board: synth.Board, seed: int) -> dict:
     return out
 
 
+def record_scaled(peec, board: synth.Board, seed: int) -> dict:
+    """The board with seeded resistance factors on every strip (1.0-1.4) and branch (PlaneStack.
+    set_resistance_scale): the operator's products at the first frequency and the solves."""
+    rng = np.random.default_rng(seed)
+    peec.gmres_restart = lambda n, r=board.restart: r
+    peec.PlaneStack.solve.__defaults__ = (board.tol, 8, None)
+    st, routes = build_reference(peec, board)
+    rs, bs = rng.uniform(1.0, 1.4, st.ns), rng.uniform(1.0, 1.4, st.nbr)
+    st.set_resistance_scale(rs, bs)
+    out = {f"board_{k}": v for k, v in board.to_arrays().items()}
+    out.update(r_scale=rs, branch_scale=bs)
+    f0 = float(board.freqs[0])
+    op = st.operator(f0)
+    out.update(op_f=np.float64(f0), op_R=op.R_strip, op_z=op.z_tail)
+    if getattr(op, "Z12", None) is not None:
+        out["op_Z12"] = op.Z12
+    rng2 = np.random.default_rng(123)
+    n = st.nb + st.Ar.shape[1]
+    x = rng2.standard_normal(n) + 1j * rng2.standard_normal(n)
+    host = peec._HostMath(st)
+    out.update(prod_x=x, prod_matvec=host.matvec(op, x), prod_precond=host.precond(op, x))
+    for k, r in enumerate(routes):
+        for q, f in enumerate(board.freqs):
+            sol = r.solve(float(f))
+            out[f"Z{k}_{q}"] = np.complex128(sol.Z_loop)
+            out[f"x{k}_{q}"] = sol.state_for(st)
+            print(f"  {board.name} scaled net {k} f {f:.4g}: its {sol.iterations} Z {sol.Z_loop:.6g}", flush=True)
+    return out
+
+
 def kernel_functions(kernel) -> dict:
     """Point values of the reference's Green's-function helpers."""
     rng = np.random.default_rng(7)
@@ -192,6 +224,10 @@ def main():
         np.savez_compressed(HERE / f"faces_stack3_{pc}.npz", **record(peec, synth.faces_stack3(pc)))
     print("necked_faces", flush=True)
     np.savez_compressed(HERE / "necked_faces.npz", **record(peec, synth.necked_faces()))
+    for name in ("necked_pair", "faces_stack3_sheet"):
+        board = synth.WORKLOADS[name]() if name != "faces_stack3_sheet" else synth.faces_stack3("sheet")
+        print(f"{name}_scaled", flush=True)
+        np.savez_compressed(HERE / f"{name}_scaled.npz", **record_scaled(peec, board, seed=31))
     if args.faces_only:
         return
     print("necked_pair", flush=True)

@@ -170,3 +170,21 @@ def test_solves_with_borrowed_preconditioners(case):
         for sol, r in zip(per, per_ref):
             assert sol.residual <= board.tol
             assert abs(sol.Z_loop - r.Z_loop) <= 1e-8 * abs(r.Z_loop)
+
+
+@pytest.mark.parametrize("name", ["necked_pair_scaled", "faces_stack3_sheet_scaled"])
+def test_resistance_scale_on_device(name):
+    """PlaneStack.set_resistance_scale (peec.py:2199-2216) on the device: products, preconditioner and solves
+    against the reference's scaled stack."""
+    z, board = load(name)
+    st, routes = gs.from_board(board)
+    st.set_resistance_scale(z["r_scale"], z["branch_scale"])
+    obj, k = _op(st, float(z["op_f"]))
+    assert rel(native.apply(st.handle, obj, "matvec", z["prod_x"], k, "fp64")[0], z["prod_matvec"]) < 1e-12
+    assert rel(native.apply(st.handle, obj, "precond", z["prod_x"], k, "fp64")[0], z["prod_precond"]) < 1e-9
+    sols = gs.solve_many(routes, list(board.freqs), tol=board.tol)
+    for kk, per in enumerate(sols):
+        for q, sol in enumerate(per):
+            Zr = complex(z[f"Z{kk}_{q}"])
+            assert abs(sol.Z_loop - Zr) <= 1e-8 * abs(Zr), (kk, q)
+            assert sol.residual <= board.tol

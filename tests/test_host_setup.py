@@ -111,3 +111,26 @@ def test_schur_values_and_impedances_match_reference(name):
     if "op_Z12" in z.files:
         Z12 = zs[st.n_sheets:][st.sheet_of_strip(st.tw_b) - st.N] / st.r_width[st.tw_b]
         assert rel(Z12, z["op_Z12"]) < 1e-14
+
+
+@pytest.mark.parametrize("name", ["necked_pair_scaled", "faces_stack3_sheet_scaled"])
+def test_resistance_scale_tables(name):
+    """set_resistance_scale on the host side: the scaled strips' own D^-1 blocks through the S-term map give
+    the (pinned) oracle's Schur complement, the scaled impedances the reference's R_strip and branch z."""
+    z, board = load(name)
+    st, routes = gs.from_board(board, _device=False)
+    st.set_resistance_scale(z["r_scale"], z["branch_scale"])
+    ost = oracle_stack(board)
+    ost.set_resistance_scale(z["r_scale"], z["branch_scale"])
+    f = float(z["op_f"])
+    op = ost.operator(f)
+    w, zs, zcap, zbr, tab = st._freq_tables(f)
+    sym = st.sym
+    fac = sym.perm[np.flatnonzero(st.top.node.ravel())[st.top.keep]]
+    P = sp.coo_matrix((np.ones(sym.n), (fac, np.arange(sym.n))), shape=(sym.n, sym.n)).tocsr()
+    ref = np.asarray((P @ op["S"].tocsr() @ P.T).tocsr()[sym.s_row, sym.s_col]).ravel()
+    assert np.abs(st.sterm @ tab - ref).max() <= 1e-13 * np.abs(ref).max()
+    assert rel(zbr, z["op_z"][st.ncap:]) < 1e-14
+    nr = st.narrow_rows
+    sc = z["r_scale"]
+    assert np.count_nonzero(nr["rre"]) == np.count_nonzero((sc != 1.0))

@@ -136,3 +136,18 @@ def test_face_sheets_match_reference(name):
     assert np.array_equal(st.tw_a, z["tw_a"]) and np.array_equal(st.tw_b, z["tw_b"])
     assert np.allclose(st.sheet_z, z["sheet_z"], rtol=0, atol=1e-15) and np.array_equal(st.sheet_t, z["sheet_t"])
     assert rel(st.twin_z(float(z["op_f"])), z["op_Z12"]) < 1e-13
+
+
+@pytest.mark.parametrize("name", ["necked_pair_scaled", "faces_stack3_sheet_scaled"])
+def test_resistance_scale_matches_reference(name):
+    """PlaneStack.set_resistance_scale (peec.py:2199-2216): strips' and branches' resistances scaled, their
+    internal inductance kept; the preconditioner then takes every position on its own."""
+    z, board = load(name)
+    st = oracle_stack(board)
+    st.set_resistance_scale(z["r_scale"], z["branch_scale"])
+    op = st.operator(float(z["op_f"]))
+    assert rel(op["R_strip"], z["op_R"]) < 1e-14 and rel(op["z_tail"], z["op_z"]) < 1e-14
+    assert rel(st.matvec(op, z["prod_x"]), z["prod_matvec"]) < 1e-12
+    assert rel(st.precond(op, z["prod_x"]), z["prod_precond"]) < 1e-10
+    ref = oracle_routes(st, board)[0].solve(float(board.freqs[1]), tol=board.tol)
+    assert abs(ref["Z_loop"] - z["Z0_1"]) <= 1e-8 * abs(z["Z0_1"])
