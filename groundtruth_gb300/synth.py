@@ -453,6 +453,33 @@ def _labels(mask: np.ndarray, xb: np.ndarray, yb: np.ndarray) -> np.ndarray:
 WIDTH_KEYS = ("wx", "wy", "ox", "oy", "rx", "ry")
 
 
+def microstrip(slot: float = 0.0, edge_split: bool = False, full_cut: bool = False, f=(1e8,)) -> Board:
+    """A 40 x 20 mm plane (35 um copper at z = 0) on 0.25 mm pitch under a 0.2 mm trace 0.5 mm above it, from
+    (5, 10) to (35, 10) mm, dropping to the plane at both ends (the reference's analytic cases, tests/
+    test_solver.py:19-30): slot = a 1 mm wide slot of that length (mm) across the trace at x = 20 mm;
+    edge_split = a 1 mm cut from y = 4 mm to the plane's edge; full_cut = a cut across the whole plane."""
+    d, t, H, W = 0.25e-3, 35e-6, 0.5e-3, 0.2e-3
+    nx, ny = 161, 81
+    outline = np.array([[0.0, 0.0], [40e-3, 0.0], [40e-3, 20e-3], [0.0, 20e-3]])
+    cuts = []
+
+    def box(x0, y0, x1, y1):
+        return np.array([[x0, y0], [x1, y0], [x1, y1], [x0, y1]]) * 1e-3
+    if slot:
+        cuts.append(box(19.5, 10 - slot / 2, 20.5, 10 + slot / 2))
+    if edge_split:
+        cuts.append(box(19.5, 4, 20.5, 20.1))
+    if full_cut:
+        cuts.append(box(19.5, -1, 20.5, 21))
+    node, xb, yb = raster_layer(nx, ny, d, outline, cuts)
+    layer = Layer("GND", 0.0, t, node, xb, yb)
+    i0, i1, j = 20, 140, 40
+    pts = [(i0 * d, j * d), (i1 * d, j * d)]
+    net = Net(_segments(pts, H, 0.0, W), (0, i0, j), (0, i1, j))
+    return Board("microstrip", d, nx, ny, [layer], nets=[net], freqs=np.asarray(f, float), precond="diag",
+                 tol=1e-5, restart=50)
+
+
 def necked_faces(seed: int = 23) -> Board:
     """faces_stack3 ('sheet' preconditioner) with strips narrower than the pitch on the split middle layer and
     on the top one: the split layer's faces share their copper's corrections (PlaneStack._twin_corrections,
