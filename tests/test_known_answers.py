@@ -100,3 +100,71 @@ def test_fully_cut_plane_is_refused():
         oracle_routes(oracle_stack(b), b)
     with pytest.raises(gs.SolverError):
         gs.from_board(b, _device=False)
+
+
+def _tape_integral(length, wa, wb, axial, lateral, dz):
+    """The two tapes' mutual inductance by adaptive quadrature of the width-difference integral (independent of
+    the panel rules under test)."""
+    from scipy.integrate import quad
+
+    def f(v):
+        over = min(0.5 * wa, v + 0.5 * wb) - max(-0.5 * wa, v - 0.5 * wb)
+        return max(over, 0.0) * float(greens.filament_mutual(length, axial, math.hypot(lateral + v, dz)))
+    h, k = 0.5 * (wa + wb), 0.5 * abs(wa - wb)
+    pts = sorted({-h, -k, k, h} | ({-lateral} if -h < -lateral < h else set()))
+    return sum(quad(f, p, q, limit=400, epsabs=0, epsrel=1e-12)[0] for p, q in zip(pts[:-1], pts[1:]) if q > p) / (wa * wb)
+
+
+@pytest.mark.parametrize("case", [(1, 1, 0, 0, 0), (1, 1, 1, 0, 0), (1, 1, 0, 1, 0), (1, 1, 0, 0, 0.05),
+                                  (1, 1, 1, 1, 0.02), (0.3, 1, 0, 0.6, 0), (0.1, 0.7, 2, 0.4, 0.001)])
+def test_tape_mutual_is_the_integral(case):
+    """test_numerics_audit.py:311-322: the tapes' near-field mutual and the strip's self term equal the integral
+    to 1e-9 (host setup and oracle)."""
+    d = 0.5e-3
+    wa, wb, a, lat, dz = (v * d for v in case)
+    ref = _tape_integral(d, wa, wb, a, lat, dz)
+    for mod in (greens, po):
+        assert mod.tape_mutual(d, wa, wb, a, lat, dz) == pytest.approx(ref, rel=1e-9)
+        assert float(mod.strip_self_numeric(d, d)) == pytest.approx(_tape_integral(d, d, d, 0, 0, 0), rel=1e-9)
+
+
+@pytest.mark.parametrize("ratio, tol", [(2.0, 0.006), (10.0, 0.002), (20.0, 0.002)])
+def test_plane_pair_sheet_inductance_is_mu0_dz(ratio, tol):
+    """test_numerics_audit.py:325-339: opposite uniform currents on two planes dz apart have mu0 dz of loop
+    inductance per square, 2 sum(K(0) - K(dz)) over a 41 x 41 plane, however thin the gap."""
+    d, n = 0.5e-3, 41
+    dz = d / ratio
+    for mod in (greens, po):
+        sheet = 2 * (mod.strip_kernel(n, n, d, 0.0) - mod.strip_kernel(n, n, d, dz)).sum()
+        assert sheet == pytest.approx(4e-7 * math.pi * dz, rel=tol)
+
+
+@pytest.mark.parametrize("t_um", [18.0, 35.0, 70.0, 105.0, 210.0])
+def test_slab_impedance_is_the_coth_form(t_um):
+    """test_plane_pair.py:84-106: the one-face slab (1 + j)/(sigma delta) coth((1 + j) t/delta) from 1 kHz to
+    20 GHz within 1e-5, its half-space limit beyond t/delta = 30 within 1e-9."""
+    sigma, mu0 = 5.8e7, 4e-7 * math.pi
+    t = t_um * 1e-6
+    for f in np.logspace(3, np.log10(2e10), 60):
+        delta = 1 / math.sqrt(math.pi * f * mu0 * sigma)
+        u = (1 + 1j) * t / delta
+        if abs(u) < 1e-3:
+            ref = (1 + u ** 2 / 3 - u ** 4 / 45 + 2 * u ** 6 / 945) / (sigma * t)
+        else:
+            ref = u * (1 + np.exp(-2 * u)) / (1 - np.exp(-2 * u)) / (sigma * t)
+        for mod in (greens, po):
+            z = complex(mod.slab_impedance(t, f, sigma))
+            assert abs(z.real / ref.real - 1) < 1e-5 and abs(z.imag / ref.imag - 1) < 1e-5, (t_um, f)
+            if t / delta > 30:
+                assert abs(z / ((1 + 1j) / (sigma * delta)) - 1) < 1e-9
+
+
+def test_oracle_gmres_solves_like_a_direct_solve():
+    """test_speed.py:18-28: restarted GMRES reaches the direct solution to 1e-8 across restarts."""
+    rng = np.random.default_rng(1)
+    n = 60
+    A = np.eye(n) * 4 + rng.standard_normal((n, n)) / np.sqrt(n) + 1j * rng.standard_normal((n, n)) / np.sqrt(n)
+    b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    x, its, ok = po.gmres(lambda v: A @ v, b, 1e-10, restart=15, max_cycles=40)
+    assert ok and its > 15
+    assert np.linalg.norm(x - np.linalg.solve(A, b)) < 1e-8 * np.linalg.norm(x)
