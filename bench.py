@@ -186,6 +186,17 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------------------------------ GPU side
+def replicas_rate(t_step: float, ncol: int, world: int, dist=None, device: str = "cuda") -> tuple:
+    """(job step time, whole-job solves/s) of `world` replicas that each solved ncol columns in t_step
+    seconds: the slowest replica's time (the max over ranks) is the job's; no data crosses between ranks."""
+    if dist is not None and world > 1:
+        import torch
+        t = torch.tensor([t_step], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_step = float(t.item())
+    return t_step, world * ncol / t_step
+
+
 def run_gpu(args):
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -261,12 +272,7 @@ def run_gpu(args):
     launches = int(lib.gt_launch_count() - l0)
     clk = clocks.stop()
     ms = [a.elapsed_time(b) for a, b in ev]
-    t_step = float(np.sum(ms)) / args.steps / 1e3
-    if dist:
-        t = torch.tensor([t_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_step = float(t.item())
-    value = world * ncol / t_step
+    t_step, value = replicas_rate(float(np.sum(ms)) / args.steps / 1e3, ncol, world, dist, "cuda")
 
     # accuracy of this run: every column's FP64 residual, and Z_loop against the reference's own full solves
     xc = st.handle.to_compact(X.data_ptr(), ncol, sptr)
