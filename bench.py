@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--requests", type=int, default=24, help="what_if: timed edits")
     ap.add_argument("--rate", type=float, default=200.0, help="what_if: Poisson arrival rate (edits/s) of the queue")
     ap.add_argument("--max-cols", type=int, default=32, help="what_if: columns per device batch")
+    ap.add_argument("--border-tol", type=float, default=1e-2,
+                    help="what_if: tolerance of the border solves relative to --tol's (bordered)")
     ap.add_argument("--what-if-method", default="bordered", choices=["bordered", "derived"],
                     help="what_if: compose from base solves (bordered) or solve every column on the derived stack")
     return ap.parse_args()
@@ -401,6 +403,7 @@ def run_what_if(args):
     st, routes = gs.from_board(board)
     setup_s = time.perf_counter() - t0
     wi = whatif.WhatIf(st, routes, board.freqs, tol=board.tol, max_cols=args.max_cols, method=args.what_if_method,
+                       border_tol=args.border_tol,
                        restart=args.restart,
                        inner_tol=args.inner_tol, reorth=args.reorth, max_its=args.max_its)
     base_s = wi.baseline()
@@ -447,7 +450,8 @@ def run_what_if(args):
         "higher_is_better": False, "impl": "gb300", "dtype": "c64 inner / c128 outer", "data": "synthetic",
         "config": {"workload": f"what_if_base {board.nx}x{board.ny} @{board.d * 1e3:g}mm GND slot + split PWR, "
                                f"{len(routes)} nets x {len(board.freqs)} freqs; edits: 1-4 vias | add 1 decap | move 1 decap, "
-                               "1-8 nets x 1-16 freqs", "tol": board.tol, "max_cols": args.max_cols},
+                               "1-8 nets x 1-16 freqs", "tol": board.tol, "max_cols": args.max_cols,
+                   "border_tol": args.border_tol},
         "requests": len(sv), "warmup": args.warmup, "p50_ms": ms(np.median(sv)), "p99_ms": ms(np.quantile(sv, 0.99)),
         "mean_ms": ms(sv.mean()), "max_ms": ms(sv.max()), "columns_per_request": float(np.mean(cols)),
         "solves_per_s": round(float(sum(cols) / sv.sum()), 2),
