@@ -66,7 +66,7 @@ def parse():
     ap.add_argument("--requests", type=int, default=24, help="what_if: timed edits")
     ap.add_argument("--rate", type=float, default=200.0, help="what_if: Poisson arrival rate (edits/s) of the queue")
     ap.add_argument("--max-cols", type=int, default=32, help="what_if: columns per device batch")
-    ap.add_argument("--border-tol", type=float, default=1e-2,
+    ap.add_argument("--border-tol", type=float, default=0.1,
                     help="what_if: tolerance of the border solves relative to --tol's (bordered)")
     ap.add_argument("--what-if-method", default="bordered", choices=["bordered", "derived"],
                     help="what_if: compose from base solves (bordered) or solve every column on the derived stack")

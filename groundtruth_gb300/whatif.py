@@ -13,7 +13,7 @@ without joining separate pieces of copper.  Two ways to answer it:
   with the base's own preconditioner; an edit costs k columns per frequency instead of one per net and
   frequency.  The edited residual is r' = r_base - r_F i on the base rows and zero on the new ones, so
   ||r'|| <= ||r_base|| + sum |i_j| ||r_F,j||, a bound known on the host; the base is solved to half the
-  tolerance and X_F to border_tol times it, and a column whose bound still misses the tolerance is solved on
+  tolerance and X_F to border_tol (0.1) times it, and a column whose bound still misses the tolerance is solved on
   the derived stack from the composed solution.
 * "derived": the derived stack (the base's factorisations plus a low-rank update of the Schur complement)
   solves every column, warm-started from the base's solution (the reference's way).  Its inner iterations
@@ -71,7 +71,7 @@ class WhatIf:
     frequencies the base is solved at (edits pick from them, so the base's factorisations serve every edit)."""
 
     def __init__(self, stack: gs.PlaneStack, routes: list, freqs, tol: float = 1e-5, max_cols: int = 32,
-                 method: str = "bordered", warm_budget: float = 2.0, border_tol: float = 1e-2, **solve_kw):
+                 method: str = "bordered", warm_budget: float = 2.0, border_tol: float = 0.1, **solve_kw):
         if method not in ("bordered", "derived"):
             raise ValueError("method must be 'bordered' or 'derived'")
         self.stack = stack
