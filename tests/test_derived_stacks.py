@@ -216,3 +216,14 @@ def test_moved_part_composition_on_cpu(derived):
     col = res.solutions[(0, float(board.freqs[1]))]
     assert abs(col.Z_loop - ref["Z_loop"]) <= 1e-7 * abs(ref["Z_loop"])
     assert np.linalg.norm(col.m - ref["m"]) <= 1e-6 * np.linalg.norm(ref["m"])
+
+
+def test_with_branches_on_a_face_sheet_stack():
+    """A derived stack of a stack with split layers keeps its sheets, twins and corrections."""
+    z, board = load("faces_stack3_sheet")
+    st = host_stack(board)
+    more = synth.what_if_branches(board, seed=5, n_via=2, n_part=1)
+    dst = st.with_branches(branches_of(more))
+    assert dst._base is st and dst.n_sheets == st.n_sheets == 4
+    assert np.array_equal(dst.tw_a, st.tw_a) and np.array_equal(dst.top.sheet_layer, st.top.sheet_layer)
+    assert dst.nb == st.nb + len(more) and np.array_equal(dst.keep, st.keep)

@@ -146,3 +146,23 @@ def test_moved_part_matches_oracle(case, method):
     for k in (0, 1):
         ref = oroutes[k].solve(f, tol=board.tol)
         assert abs(res.solutions[(k, f)].Z_loop - ref["Z_loop"]) <= 1e-8 * abs(ref["Z_loop"]), (method, k)
+
+
+@pytest.mark.parametrize("name", ["necked_pair", "faces_stack3_sheet", "necked_faces"])
+@pytest.mark.parametrize("method", ["bordered", "derived"])
+def test_edits_on_narrow_and_face_sheet_boards(name, method):
+    """Added vias and a part on boards with narrow strips and face sheets, both ways, against the oracle's
+    solve of the whole edited board."""
+    from groundtruth_gb300 import whatif
+    z, board = load(name)
+    st, routes = gs.from_board(board)
+    more = synth.what_if_branches(board, seed=5, n_via=2, n_part=1)
+    whole = synth.Board.from_arrays(board.to_arrays())
+    whole.branches = list(board.branches) + list(more)
+    oroutes = oracle_routes(oracle_stack(whole), whole)
+    wi = whatif.WhatIf(st, routes, board.freqs, tol=board.tol, method=method)
+    wi.baseline()
+    f = float(board.freqs[-1])
+    res = wi.evaluate(branches_of(more), [0], [f])
+    ref = oroutes[0].solve(f, tol=board.tol)
+    assert abs(res.solutions[(0, f)].Z_loop - ref["Z_loop"]) <= 1e-8 * abs(ref["Z_loop"]), (name, method)
