@@ -403,10 +403,9 @@ class PlaneStack:
         return blk
 
     def _widths(self):
-        """Strips narrower than the pitch (peec.py:1732-1820): strip_width and r_width per strip (fractions of
+        """Strips narrower than the pitch (peec.py:1732-1843): strip_width and r_width per strip (fractions of
         the pitch), dL (the self-inductance change, None when every strip is full) and M_near (sparse side-by-side
-        mutual changes); then the device's view of them: the strip positions whose D^-1 blocks are their own
-        (override), and the rows of the system product's corrections."""
+        mutual changes, with a split layer's faces sharing them).  _corrections makes the device's view."""
         t, S = self.top, self.n_sheets
         sx, sy = (self.nx - 1, self.ny), (self.nx, self.ny - 1)
         lx, ly = self.layer_index("x"), self.layer_index("y")      # a face sheet has its layer's copper
