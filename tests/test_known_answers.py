@@ -168,3 +168,38 @@ def test_oracle_gmres_solves_like_a_direct_solve():
     x, its, ok = po.gmres(lambda v: A @ v, b, 1e-10, restart=15, max_cycles=40)
     assert ok and its > 15
     assert np.linalg.norm(x - np.linalg.solve(A, b)) < 1e-8 * np.linalg.norm(x)
+
+
+def _dc_drop(board):
+    """The plane's DC drop between the receiver and driver nodes by a direct solve of its resistive network
+    (every strip a square of sheet resistance 1/(sigma t) between its nodes; GroundTruth's DC sheet reference,
+    tests/refsolvers.py:96-153, on the solver's own grid)."""
+    import scipy.sparse as sp
+    from scipy.sparse.linalg import spsolve
+    st = gs.from_board(board, _device=False)[0]
+    g = st.sigma * st.ts[0]
+    a, b = st.top.a_nodes[: st.ns], st.top.b_nodes[: st.ns]
+    n = st.n_nodes
+    L = sp.coo_matrix((np.concatenate([np.full(st.ns, g)] * 2 + [np.full(st.ns, -g)] * 2),
+                       (np.concatenate([a, b, a, b]), np.concatenate([a, b, b, a]))), shape=(n, n)).tocsr()
+    net = board.nets[0]
+    drv, rcv = int(st.nid[net.driver]), int(st.nid[net.receiver])
+    J = np.zeros(n)
+    J[drv], J[rcv] = -1.0, 1.0
+    keep = np.flatnonzero(st.keep)
+    V = np.zeros(n)
+    V[keep] = spsolve(L[keep][:, keep].tocsc(), J[keep])
+    return V[rcv] - V[drv]
+
+
+@pytest.mark.parametrize("solve", SOLVERS)
+def test_dc_limit_is_the_resistive_sheet(solve):
+    """At 0 Hz the solve is the plane's resistive network: the loop impedance's plane part (the injections'
+    potential difference) equals a direct solve of the sheet's conductance Laplacian."""
+    b = synth.microstrip(f=(0.0,))
+    b.tol = 1e-10
+    I_x, Z, m = solve(b, 0.0)
+    seg = b.nets[0].segments
+    r_trace = greens.trace_resistance(seg, 0.0, b.sigma, b.nets[0].trace_t)
+    assert Z.imag == pytest.approx(0.0, abs=1e-12)
+    assert Z.real - r_trace == pytest.approx(_dc_drop(b), rel=1e-8)
