@@ -79,6 +79,35 @@ class Branch:
     radius: float = 1.5e-4
 
 
+VIA_PLATING = 25e-6           # m, a via barrel's plating (peec.py:75)
+
+
+def via_impedance(length_m: float, drill_m: float, sigma: float = SIGMA_CU, filled: bool = False,
+                  plating: float = VIA_PLATING) -> Callable[[float], complex]:
+    """A plated via barrel between two layers as a branch impedance z(f) = R + j w L (peec.py:1061-1072): L the
+    partial self inductance of a filament at the barrel's radius (a thin tube's GMD), R the plating ring's (the
+    whole hole's when a pin fills it)."""
+    r = max(drill_m / 2, 5e-5)
+    length = max(length_m, 1e-6)
+    L = float(greens.filament_mutual(length, np.array(0.0), np.array(r)))
+    area = math.pi * r * r if filled else math.pi * 2 * r * plating
+    R = length / (sigma * area)
+    return lambda f, R=R, L=L: complex(R, 2 * math.pi * f * L)
+
+
+def track_impedance(length_m: float, width_m: float, thickness_m: float = 35e-6,
+                    sigma: float = SIGMA_CU) -> Callable[[float], complex]:
+    """A piece of track as a lumped branch (a bridge across another net's cells, peec.py:1075-1090): the
+    resistance over the copper's effective thickness at f (skin depth) + j w its partial self inductance."""
+    length = max(length_m, 1e-6)
+    L = greens.strip_self(length, width_m, thickness_m)
+
+    def z(f: float) -> complex:
+        t = float(greens.skin_thickness(thickness_m, f, sigma))
+        return complex(length / (sigma * width_m * t), 2 * math.pi * f * L)
+    return z
+
+
 @dataclass
 class PlanePair:
     upper: int

@@ -194,6 +194,17 @@ def record_scaled(peec, board: synth.Board, seed: int) -> dict:
     return out
 
 
+def branch_functions(peec) -> dict:
+    """The reference's via and track branch impedances at a few sizes and frequencies."""
+    f = np.logspace(3, 10, 12)
+    vias = [(1.6e-3, 0.3e-3, False), (0.2e-3, 0.2e-3, False), (1.0e-3, 0.8e-3, True), (0.0, 0.05e-3, False)]
+    tracks = [(2e-3, 0.15e-3, 35e-6), (0.5e-3, 0.4e-3, 18e-6), (5e-3, 1e-3, 70e-6)]
+    out = {"bf_f": f, "bf_via_args": np.array(vias, float), "bf_track_args": np.array(tracks, float)}
+    out["bf_via"] = np.array([[peec.via_impedance(l, dr, filled=fl)(x) for x in f] for l, dr, fl in vias])
+    out["bf_track"] = np.array([[peec.track_impedance(l, w, t)(x) for x in f] for l, w, t in tracks])
+    return out
+
+
 def kernel_functions(kernel) -> dict:
     """Point values of the reference's Green's-function helpers."""
     rng = np.random.default_rng(7)
@@ -238,7 +249,7 @@ def main():
     np.savez_compressed(HERE / "small_pair_derived.npz", **record_derived(peec, synth.small_pair(), seed=11))
     if args.derived_only:
         return
-    np.savez_compressed(HERE / "kernel_functions.npz", **kernel_functions(kernel))
+    np.savez_compressed(HERE / "kernel_functions.npz", **kernel_functions(kernel), **branch_functions(peec))
     for name in ("small_pair", "small_stack3", "plain_plane"):
         board = synth.WORKLOADS[name]()
         print(name, flush=True)

@@ -151,3 +151,17 @@ def test_resistance_scale_matches_reference(name):
     assert rel(st.precond(op, z["prod_x"]), z["prod_precond"]) < 1e-10
     ref = oracle_routes(st, board)[0].solve(float(board.freqs[1]), tol=board.tol)
     assert abs(ref["Z_loop"] - z["Z0_1"]) <= 1e-8 * abs(z["Z0_1"])
+
+
+def test_branch_impedances_match_reference():
+    """via_impedance / track_impedance (peec.py:1061-1090): the product's restatement at a few sizes and
+    frequencies equals the reference's."""
+    from groundtruth_gb300 import stack as gs
+    z = np.load(GOLD / "kernel_functions.npz")
+    f = z["bf_f"]
+    for (l, dr, fl), ref in zip(z["bf_via_args"], z["bf_via"]):
+        got = np.array([gs.via_impedance(l, dr, filled=bool(fl))(x) for x in f])
+        assert rel(got, ref) < 1e-13
+    for (l, w, t), ref in zip(z["bf_track_args"], z["bf_track"]):
+        got = np.array([gs.track_impedance(l, w, t)(x) for x in f])
+        assert rel(got, ref) < 1e-13
