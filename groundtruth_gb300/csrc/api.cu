@@ -39,9 +39,13 @@ struct Invalid : std::runtime_error {
 // Device allocations owned by an object, freed together.
 struct Pool {
     std::vector<void*> ptrs;
+    bool dry = false;      // count the bytes only (memory planning), allocate nothing
+    size_t bytes = 0;
     template <typename T> T* alloc(size_t n) {
         void* p = nullptr;
         if (n == 0) n = 1;
+        bytes += n * sizeof(T);
+        if (dry) return nullptr;
         cudaError_t e = cudaMalloc(&p, n * sizeof(T));
         if (e != cudaSuccess) throw CudaError{e, "cudaMalloc of " + std::to_string(n * sizeof(T)) + " bytes"};
         ptrs.push_back(p);
@@ -580,13 +584,27 @@ static void lowrank_w(gt_geometry* G, const gt_operators* base, int nf, int k, c
 
 static int nchunks(int64_t n) { return (int)((n + 2047) / 2048); }  // DOT_CHUNK in gmres.cu
 
+static void fill_ws(Workspace& W, gt_geometry* G, int ncol, int m, int prec, int kmax);
+
 static void ensure_ws(gt_geometry* G, int ncol, int m, int prec, int kmax) {
     auto& w = G->ws;
     if (w && w->ncol >= ncol && w->m >= m && w->prec == prec && w->kmax >= kmax) return;
     w.reset();
     cudaDeviceSynchronize();
     w.reset(new Workspace());
-    Workspace& W = *w;
+    fill_ws(*w, G, ncol, m, prec, kmax);
+}
+
+// the bytes fill_ws would allocate (nothing is allocated)
+static size_t ws_bytes(gt_geometry* G, int ncol, int m, int prec, int kmax) {
+    Workspace W;
+    W.pool.dry = true;
+    fill_ws(W, G, ncol, m, prec, kmax);
+    return W.pool.bytes;
+}
+
+static void fill_ws(Workspace& W, gt_geometry* G, int ncol, int m, int prec, int kmax) {
+    const bool dry = W.pool.dry;
     W.ncol = ncol;
     W.m = m;
     W.prec = prec;
@@ -615,7 +633,7 @@ static void ensure_ws(gt_geometry* G, int ncol, int m, int prec, int kmax) {
     W.uvec = p.alloc<unsigned char>((size_t)ncol * std::max<int64_t>(G->F.vec_total, 1) * es);
     // node-ordered s / y of the preconditioner: entries of nodes that are not kept stay zero
     W.sd = p.alloc<unsigned char>((size_t)ncol * G->F.nnode * es);
-    GT_CUDA(cudaMemset(W.sd, 0, (size_t)ncol * G->F.nnode * es));
+    if (!dry) GT_CUDA(cudaMemset(W.sd, 0, (size_t)ncol * G->F.nnode * es));
     W.partial = p.alloc<c64>((size_t)ncol * nch * (m + 2));
     GmresState& s = W.st;
     s.nslot = ncol;
@@ -644,7 +662,7 @@ static void ensure_ws(gt_geometry* G, int ncol, int m, int prec, int kmax) {
     W.g_slot = p.alloc<int>(ncol);
     W.g_op = p.alloc<int>(ncol);
     W.act = p.alloc<int>(ncol);
-    GT_CUDA(cudaMallocHost(&W.act_host, ncol * sizeof(int)));
+    if (!dry) GT_CUDA(cudaMallocHost(&W.act_host, ncol * sizeof(int)));
     W.gP = p.alloc<c64>((size_t)kmax * ncol * n);
     W.gQ = p.alloc<c64>((size_t)kmax * ncol * n);
     W.gbeta = p.alloc<c64>((size_t)ncol * (kmax + 1));
@@ -654,6 +672,7 @@ static void ensure_ws(gt_geometry* G, int ncol, int m, int prec, int kmax) {
     W.col_op = p.alloc<int>(ncol);
     W.flag_dev = p.alloc<int>(1);
     W.its_col = p.alloc<int>(ncol);
+    if (dry) return;
     GT_CUDA(cudaMallocHost(&W.flag_host, sizeof(int)));
     GT_CUDA(cudaMemset(W.V, 0, (size_t)ncol * (m + 1) * n * eb));
 }
@@ -1547,6 +1566,24 @@ int gt_solve(gt_geometry* G, gt_operators* ops, int32_t n_cols, const int32_t* c
     GT_CUDA(cudaStreamSynchronize(st));
     if (rc != GT_OK) gt::set_error("GMRES did not converge for at least one column");
     return rc;
+    GT_GUARD_END
+}
+
+int gt_memory(gt_geometry* G, int32_t n_cols, const gt_solve_opts* opts, int64_t* need, int64_t* held,
+              int64_t* free_bytes, int64_t* total_bytes) {
+    GT_GUARD_BEGIN
+    if (!G || !opts || n_cols < 1) throw Invalid("bad arguments");
+    if (opts->restart < 1 || opts->restart > 250) throw Invalid("restart must be in 1..250");
+    std::lock_guard<std::mutex> lk(G->lock);
+    // the workspace plus gt_solve's compact staging of the right-hand sides and solutions
+    const size_t ws = ws_bytes(G, n_cols, opts->restart, opts->precision, std::max(1, opts->outer_k));
+    if (need) *need = (int64_t)(ws + (size_t)n_cols * G->n_compact * sizeof(c64));
+    if (held) *held = G->ws ? (int64_t)G->ws->pool.bytes : 0;
+    size_t fr = 0, tot = 0;
+    if (free_bytes || total_bytes) GT_CUDA(cudaMemGetInfo(&fr, &tot));
+    if (free_bytes) *free_bytes = (int64_t)fr;
+    if (total_bytes) *total_bytes = (int64_t)tot;
+    return GT_OK;
     GT_GUARD_END
 }
 

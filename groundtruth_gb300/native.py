@@ -98,6 +98,8 @@ def load():
                                        C.c_int32, DP]
     lib.gt_moment.argtypes = [P, C.c_int32, P, DP, C.c_double, DP, P]
     lib.gt_lp_product_noalloc.argtypes = [P, C.c_int32, P, P, P]
+    lib.gt_memory.argtypes = [P, C.c_int32, C.POINTER(SolveOpts), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                              C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     if lib.gt_device_count() < 1:
         raise RuntimeError("no CUDA device is visible: the groundtruth_gb300 solver runs on the GPU only")
     _LIB = lib
@@ -352,6 +354,15 @@ def solve(geom: Geometry, ops: list, rhs: np.ndarray, tol: float, restart: int =
     if rc not in (GT_OK, GT_NOT_CONVERGED):
         check(lib, rc, "gt_solve")
     return x, its, res, res <= tol
+
+
+def memory(geom: Geometry, n_cols: int, restart: int = 50, precision: str = "mixed", outer_k: int = 8) -> dict:
+    """gt_memory: {"need": bytes a solve of n_cols columns allocates, "held": the geometry's workspace now,
+    "free" / "total": the device's}."""
+    o = SolveOpts(1e-5, restart, 1, 1e-5, _precision(precision), 1, 0.0, outer_k, 0)
+    v = [C.c_int64(0) for _ in range(4)]
+    check(geom.lib, geom.lib.gt_memory(geom.h, int(n_cols), C.byref(o), *(C.byref(x) for x in v)), "gt_memory")
+    return dict(zip(("need", "held", "free", "total"), (x.value for x in v)))
 
 
 def kernel_spectrum(n_axial: int, n_lateral: int, d: float, dz: float, P0: int, P1: int,

@@ -859,8 +859,14 @@ class PlaneStack:
         ops = self.factorise(freqs, together=True, borrow=borrow)
         rhs = np.stack([self.rhs_vector(r, j) for r, j in zip(rhs_tops, Js)])
         x0 = self._warm_start(ops, rhs, guesses) if guesses is not None else None
-        x, its, res, ok = native.solve(self.handle, ops, rhs, tol=tol, restart=restart, max_its=max_its,
-                                       inner_tol=inner_tol, precision=precision, reorth=reorth, x0=x0)
+        x = np.zeros_like(rhs)
+        its, res, ok = np.zeros(ncol, np.int32), np.zeros(ncol), np.zeros(ncol, bool)
+        step = self.columns_that_fit(ncol, restart, precision)
+        for c0 in range(0, ncol, step):
+            sl = slice(c0, c0 + step)
+            x[sl], its[sl], res[sl], ok[sl] = native.solve(
+                self.handle, ops[sl], rhs[sl], tol=tol, restart=restart, max_its=max_its, inner_tol=inner_tol,
+                precision=precision, reorth=reorth, x0=None if x0 is None else x0[sl])
         out = []
         for c in range(ncol):
             if not ok[c]:
@@ -872,6 +878,25 @@ class PlaneStack:
             V[self.keep] = x[c, self.nb:]
             out.append((x[c, : self.nb], V, int(its[c]), x[c], float(res[c])))
         return out
+
+    MEMORY_HEADROOM = 0.9         # of the device's free memory a solve may take
+
+    def columns_that_fit(self, ncol: int, restart: int = 50, precision: str = "mixed") -> int:
+        """How many columns one device solve takes at once (the reference's memory gate, peec.py:1388-1501):
+        all of them when their workspace fits the geometry's present one plus MEMORY_HEADROOM of the free
+        memory, else as many as fit; MemoryError when not even one does."""
+        from . import native
+        full = native.memory(self.handle, ncol, restart, precision)
+        room = full["held"] + self.MEMORY_HEADROOM * full["free"]
+        if full["need"] <= room:
+            return ncol
+        one = native.memory(self.handle, 1, restart, precision)["need"]
+        per = (full["need"] - one) / max(ncol - 1, 1)
+        fit = int((room - one) // per) + 1 if room >= one else 0
+        if fit < 1:
+            raise MemoryError(f"a solve of one column needs {one / 2**30:.1f} GiB, "
+                              f"{room / 2**30:.1f} GiB are available on the device")
+        return min(fit, ncol)
 
     def _warm_start(self, ops, rhs: np.ndarray, guesses) -> Optional[np.ndarray]:
         """Starting points from guess vectors (peec.py:2570-2578): per column x0 = G c with c minimising

@@ -174,6 +174,13 @@ void gt_operators_free(gt_operators* ops);
 int gt_solve(gt_geometry* g, gt_operators* ops, int32_t n_cols, const int32_t* col_op, const double* rhs,
              const gt_solve_opts* opts, double* x_out, int32_t* its_out, double* resid_out, void* stream);
 
+/* Device memory of solves (the reference's memory gate, peec.py:1388-1501, gpu.py:593-605): *need the bytes a
+ * gt_solve of n_cols columns with these options allocates (its workspace and the staging of the compact vectors),
+ * *held those the geometry's workspace holds now (freed before a larger one is made, reused otherwise), *free_bytes
+ * and *total_bytes the device's.  Any output pointer may be NULL. */
+int gt_memory(gt_geometry* g, int32_t n_cols, const gt_solve_opts* opts, int64_t* need, int64_t* held,
+              int64_t* free_bytes, int64_t* total_bytes);
+
 /* The same with device-resident dense vectors: rhs_device / x_device are [n_cols*n_dense] complex128 in the
  * dense layout; nothing crosses to the host but the per-column scalars. */
 int gt_solve_device(gt_geometry* g, gt_operators* ops, int32_t n_cols, const int32_t* col_op,

@@ -227,3 +227,23 @@ def test_with_branches_on_a_face_sheet_stack():
     assert dst._base is st and dst.n_sheets == st.n_sheets == 4
     assert np.array_equal(dst.tw_a, st.tw_a) and np.array_equal(dst.top.sheet_layer, st.top.sheet_layer)
     assert dst.nb == st.nb + len(more) and np.array_equal(dst.keep, st.keep)
+
+
+def test_solves_split_into_what_fits_the_device(monkeypatch):
+    """The memory gate: a batch whose workspace does not fit the free device memory is solved in parts, a
+    column that does not fit at all raises MemoryError."""
+    from groundtruth_gb300 import native
+    st = host_stack(synth.small_pair())
+    st.handle = object()
+    per, fixed = 10, 5
+
+    def fake_memory(geom, n, restart=50, precision="mixed", outer_k=8):
+        return {"need": fixed + per * n, "held": 0, "free": free[0], "total": 10 ** 6}
+    monkeypatch.setattr(native, "memory", fake_memory)
+    free = [10 ** 6]
+    assert st.columns_that_fit(40) == 40
+    free[0] = (fixed + per * 12) / st.MEMORY_HEADROOM
+    assert st.columns_that_fit(40) == 12
+    free[0] = 1
+    with pytest.raises(MemoryError):
+        st.columns_that_fit(40)

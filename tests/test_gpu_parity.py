@@ -188,3 +188,16 @@ def test_resistance_scale_on_device(name):
             Zr = complex(z[f"Z{kk}_{q}"])
             assert abs(sol.Z_loop - Zr) <= 1e-8 * abs(Zr), (kk, q)
             assert sol.residual <= board.tol
+
+
+def test_memory_gate_counts_the_workspace(case):
+    """gt_memory: a solve's bytes grow with its columns; after a solve the geometry's workspace holds what it
+    said it would need (less the compact staging)."""
+    name, z, board, st, routes = case
+    m1, m4 = native.memory(st.handle, 1), native.memory(st.handle, 4)
+    assert 0 < m1["need"] < m4["need"] and 0 < m4["free"] <= m4["total"]
+    f = float(board.freqs[0])
+    r = routes[0]
+    st.solve_batch([f] * 4, [r.rhs_top(f)] * 4, [r.J()] * 4, tol=board.tol)
+    held = native.memory(st.handle, 4)["held"]
+    assert held >= m4["need"] - 4 * st.handle.n_compact * 16
