@@ -1001,7 +1001,7 @@ class RouteExcitation:
             raise SolverError("no current is injected")
         ids = []
         for node, amps, what in terms:
-            n = int(stack.nid[tuple(node)])
+            n = stack.node_id(node)
             if n < 0:
                 raise SolverError(f"{what} is not on plane copper")
             ids.append((n, amps))

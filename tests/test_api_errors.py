@@ -1,0 +1,67 @@
+"""The Python mirror's error behaviour, as the reference's (peec.py:124-127, 1559-1593, 2199-2216, 2713-2760):
+SolverError for unsolvable models and bad injections, ValueError for malformed arguments.  Host side only."""
+import numpy as np
+import pytest
+
+from groundtruth_gb300 import stack as gs, synth
+
+
+def host(board):
+    return gs.from_board(board, _device=False)
+
+
+def test_no_layers_and_bad_preconditioner():
+    with pytest.raises(gs.SolverError):
+        gs.PlaneStack([], _device=False)
+    b = synth.small_pair()
+    st, _ = host(b)
+    with pytest.raises(ValueError):
+        gs.PlaneStack(st.layers, precond="ilu", _device=False)
+
+
+def test_layers_must_share_one_grid():
+    b = synth.small_pair()
+    st, _ = host(b)
+    g = st.layers[1].grid
+    other = gs.Grid(0.0, 0.0, g.d, g.nx - 1, g.ny, g.node[:-1], g.xb[:-1], g.yb[:-1])
+    with pytest.raises(gs.SolverError):
+        gs.PlaneStack([st.layers[0], gs.PlaneLayer("X", -1e-3, other)], _device=False)
+
+
+def test_injections_must_be_on_copper_and_balance():
+    b = synth.small_pair()
+    st, routes = host(b)
+    trace = routes[0].trace
+    hole = tuple(int(v) for v in np.argwhere(~st.node[0])[0])       # a node of the slot
+    with pytest.raises(gs.SolverError, match="not on plane copper"):
+        gs.RouteExcitation(st, trace, (0, *hole), b.nets[0].receiver)
+    with pytest.raises(gs.SolverError, match="not on plane copper"):
+        gs.RouteExcitation(st, trace, (0, st.nx + 5, 0), b.nets[0].receiver)      # off the grid
+    with pytest.raises(gs.SolverError, match="no current"):
+        gs.RouteExcitation(st, trace)
+    with pytest.raises(gs.SolverError, match="balance"):
+        gs.RouteExcitation(st, trace, injections=[(b.nets[0].driver, 1.0)])
+
+
+def test_driver_and_receiver_on_separate_copper():
+    b = synth.microstrip(full_cut=True)
+    with pytest.raises(gs.SolverError, match="not connected"):
+        host(b)
+
+
+def test_resistance_factors_must_match_the_unknowns():
+    st, _ = host(synth.small_pair())
+    with pytest.raises(ValueError):
+        st.set_resistance_scale(np.ones(st.ns - 1))
+    with pytest.raises(ValueError):
+        st.set_resistance_scale(None, np.ones(st.nbr + 1))
+
+
+def test_branches_off_copper_are_dropped():
+    b = synth.small_pair()
+    st, _ = host(b)
+    hole = tuple(int(v) for v in np.argwhere(~st.node[0])[0])
+    br = gs.Branch((0, *hole), (1, *hole), lambda f: 1.0 + 0j)
+    assert st.with_branches([br]) is st
+    new = gs.PlaneStack(st.layers, st.branches + [br], st.pairs, precond="sheet", screen=False, _device=False)
+    assert new.nbr == st.nbr
