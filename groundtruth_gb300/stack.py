@@ -60,6 +60,24 @@ class Grid:
     rx: Optional[np.ndarray] = None      # the width the strip's resistance takes (None / 0: its width)
     ry: Optional[np.ndarray] = None
 
+    def copper_area(self) -> np.ndarray:
+        """Each node's copper as a share of its cell (peec.py:257-281, without a measured area): the mean width of
+        the strips that touch it, 1 at a node of full strips or of a grid without widths, 0 off copper."""
+        out = self.node.astype(float)
+        if self.wx is None or self.wy is None:
+            return out
+        sx, nxs, sy, nys = (np.zeros(self.node.shape) for _ in range(4))
+        sx[:-1, :] += np.where(self.xb, self.wx, 0.0)
+        sx[1:, :] += np.where(self.xb, self.wx, 0.0)
+        nxs[:-1, :] += self.xb
+        nxs[1:, :] += self.xb
+        sy[:, :-1] += np.where(self.yb, self.wy, 0.0)
+        sy[:, 1:] += np.where(self.yb, self.wy, 0.0)
+        nys[:, :-1] += self.yb
+        nys[:, 1:] += self.yb
+        n = nxs + nys
+        return np.where(n > 0, (sx + sy) / np.maximum(n, 1), out)
+
 
 @dataclass
 class PlaneLayer:
@@ -138,6 +156,9 @@ class Solution:
     I_cap: np.ndarray = field(default_factory=lambda: np.zeros(0, complex))
     residual: float = 0.0          # final relative FP64 residual ||b - K x|| / ||b||
     I_twin: Optional[np.ndarray] = None   # (2, pairs) a split layer's upper- and lower-face strip currents
+    W_x: Optional[np.ndarray] = None      # per layer the strips' resistance widths (None: all full)
+    W_y: Optional[np.ndarray] = None
+    A_cu: Optional[np.ndarray] = None     # per layer each node's copper share of its cell
 
     @property
     def L_loop(self) -> float:
@@ -145,12 +166,14 @@ class Solution:
 
     def node_field(self, k: int, d_mm: float, copper: bool = False) -> tuple:
         """Complex (Kx, Ky) at the nodes of layer k in A/m per A (peec.py:1151-1203): each node averages the
-        strips of each direction that touch it and carry current, per cell width.  copper=True needs the
-        narrow-strip widths of the exact-copper raster, which this build does not model."""
-        if copper:
-            raise NotImplementedError("per-copper-width fields need the exact-copper raster")
+        strips of each direction that touch it and carry current, per cell width; copper=True per width of the
+        copper itself, the vector's length set by the touching strips' heat over the node's copper area."""
         d = d_mm * 1e-3
         Ix, Iy = self.I_x[k], self.I_y[k]
+        wx = wy = None
+        if copper and self.W_x is not None:
+            wx, wy = self.W_x[k], self.W_y[k]
+            Ix, Iy = Ix / wx, Iy / wy
         nx, ny = self.V.shape[1:]
         kx, ky = np.zeros((nx, ny), complex), np.zeros((nx, ny), complex)
         cx, cy = np.zeros((nx, ny)), np.zeros((nx, ny))
@@ -162,7 +185,24 @@ class Solution:
         ky[:, 1:] += Iy
         cy[:, :-1] += Iy != 0
         cy[:, 1:] += Iy != 0
-        return kx / np.maximum(cx, 1) / d, ky / np.maximum(cy, 1) / d
+        kx, ky = kx / np.maximum(cx, 1) / d, ky / np.maximum(cy, 1) / d
+        if not copper or self.A_cu is None:
+            return kx, ky
+        # the node's share of its strips' heat per rho / t, sum 1/2 |I|^2 / width, over its copper area
+        hx = 0.5 * np.abs(self.I_x[k]) ** 2 / (wx if wx is not None else 1.0)
+        hy = 0.5 * np.abs(self.I_y[k]) ** 2 / (wy if wy is not None else 1.0)
+        q = np.zeros((nx, ny))
+        q[:-1, :] += hx
+        q[1:, :] += hx
+        q[:, :-1] += hy
+        q[:, 1:] += hy
+        a = self.A_cu[k].astype(float)
+        mag = np.sqrt(np.where(a > 0, q / np.maximum(a, 1e-12), 0.0)) / d
+        vec = np.sqrt(np.abs(kx) ** 2 + np.abs(ky) ** 2)
+        # the mean's direction at that length; where the mean cancels, the length alone along x
+        scale = np.where(vec > 1e-9 * mag, mag / np.maximum(vec, 1e-300), 0.0)
+        alone = (vec <= 1e-9 * mag) & (mag > 0)
+        return np.where(alone, mag, kx * scale), np.where(alone, 0.0, ky * scale)
 
     def state_for(self, stack: "PlaneStack") -> np.ndarray:
         """The solver's unknown vector [branch currents; kept node potentials] of this solution on `stack`, the
@@ -262,6 +302,13 @@ class PlaneStack:
         self.r_scale = self.branch_scale = None
         self._widths()
         self._corrections()
+        # per layer the strips' resistance widths and the nodes' copper shares (Solution.node_field(copper=True))
+        self.A_cu = np.stack([l.grid.copper_area() for l in self.layers]).astype(np.float32)
+        self.W_x = self.W_y = None
+        if np.any(self.strip_width != 1.0) or np.any(self.r_width != 1.0):
+            self.W_x, self.W_y = np.ones((self.N, self.nx - 1, self.ny)), np.ones((self.N, self.nx, self.ny - 1))
+            self.W_x[tuple(self.layer_index("x").T)] = self.r_width[: self.nxb]
+            self.W_y[tuple(self.layer_index("y").T)] = self.r_width[self.nxb:]
         self._schur_structure(leaf)
         self._lock = threading.Lock()
         self._ops: OrderedDict = OrderedDict()
@@ -1051,7 +1098,7 @@ class RouteExcitation:
                     + 1j * w * (self.L_trace + np.dot(self.psi, Ib)))
         return Solution(f, I_x, I_y, Vg, Ib[st.ns + st.ncap:].copy(), Z, st.moment(self.segments, Ib), its,
                         Ib[st.ns: st.ns + st.ncap].copy(), res,
-                        np.stack([Ib[st.tw_a], Ib[st.tw_b]]) if len(st.tw_b) else None)
+                        np.stack([Ib[st.tw_a], Ib[st.tw_b]]) if len(st.tw_b) else None, st.W_x, st.W_y, st.A_cu)
 
     def solve(self, f: float, guess=None, tol: float = 1e-5) -> Solution:
         Ib, V, its, x = self.stack.solve(f, self.rhs_top(f), self.J(), tol=tol, guess=guess)[:4]

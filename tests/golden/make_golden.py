@@ -24,6 +24,8 @@ pairs and the face coupling Z12; ``necked_faces.npz`` the sheet-preconditioned o
 split layer and the top one (the faces' shared corrections).
 ``necked_pair_scaled.npz`` / ``faces_stack3_sheet_scaled.npz``: those boards with seeded resistance factors on
 every strip and branch (PlaneStack.set_resistance_scale): products and solves.
+``necked_pair_fields.npz``: the reference's current-density maps of that board's net 0 (per cell and per
+copper width, Solution.node_field).
 ``small_pair_derived.npz`` holds the same for small_pair plus a what-if edit's branches on a derived stack
 (PlaneStack.with_branches), including solves warm-started from the base's solutions.
 
@@ -205,6 +207,23 @@ def branch_functions(peec) -> dict:
     return out
 
 
+def record_fields(peec, board: synth.Board) -> dict:
+    """The reference's current-density maps (Solution.node_field, per cell and per copper width) of net 0 at
+    the board's second frequency, every layer."""
+    peec.gmres_restart = lambda n, r=board.restart: r
+    peec.PlaneStack.solve.__defaults__ = (board.tol, 8, None)
+    st, routes = build_reference(peec, board)
+    f = float(board.freqs[1])
+    sol = routes[0].solve(f)
+    out = {f"board_{k}": v for k, v in board.to_arrays().items()}
+    out.update(f=np.float64(f), x=sol.state_for(st))
+    for k in range(st.N):
+        for copper in (False, True):
+            kx, ky = sol.node_field(k, board.d * 1e3, copper=copper)
+            out[f"kx{k}_{int(copper)}"], out[f"ky{k}_{int(copper)}"] = kx, ky
+    return out
+
+
 def kernel_functions(kernel) -> dict:
     """Point values of the reference's Green's-function helpers."""
     rng = np.random.default_rng(7)
@@ -235,6 +254,8 @@ def main():
         np.savez_compressed(HERE / f"faces_stack3_{pc}.npz", **record(peec, synth.faces_stack3(pc)))
     print("necked_faces", flush=True)
     np.savez_compressed(HERE / "necked_faces.npz", **record(peec, synth.necked_faces()))
+    print("necked_pair_fields", flush=True)
+    np.savez_compressed(HERE / "necked_pair_fields.npz", **record_fields(peec, synth.necked_pair()))
     for name in ("necked_pair", "faces_stack3_sheet"):
         board = synth.WORKLOADS[name]() if name != "faces_stack3_sheet" else synth.faces_stack3("sheet")
         print(f"{name}_scaled", flush=True)

@@ -134,3 +134,18 @@ def test_resistance_scale_tables(name):
     nr = st.narrow_rows
     sc = z["r_scale"]
     assert np.count_nonzero(nr["rre"]) == np.count_nonzero((sc != 1.0))
+
+
+def test_current_density_maps_match_reference():
+    """Solution.node_field per cell width and per copper width (peec.py:1151-1203, Grid.copper_area 257-281) on
+    the reference's own solution of a board with narrow strips."""
+    z, board = load("necked_pair_fields")
+    st, routes = gs.from_board(board, _device=False)
+    x = z["x"]
+    V = np.zeros(st.n_nodes, complex)
+    V[st.keep] = x[st.nb:]
+    sol = routes[0].solution(float(z["f"]), x[: st.nb], V, 0)
+    for k in range(st.N):
+        for copper in (False, True):
+            kx, ky = sol.node_field(k, board.d * 1e3, copper=copper)
+            assert rel(kx, z[f"kx{k}_{int(copper)}"]) < 1e-12 and rel(ky, z[f"ky{k}_{int(copper)}"]) < 1e-12
