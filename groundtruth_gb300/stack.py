@@ -4,6 +4,7 @@
     PlaneStack.solve(f, rhs_top, J, tol, max_cycles, guess) -> (Ib, V, its, x)  peec.py:2513-2607
     RouteExcitation(stack, trace, inject_driver, inject_receiver, ...)       peec.py:2703-2769
     RouteExcitation.solve(f, guess) -> Solution                              peec.py:2787-2817
+    PlaneProblem / MultiPlaneProblem (one-off stack + route)                 peec.py:2820-2837
 
 with the same argument meanings, unknown numbering and error behaviour (SolverError for unsolvable models
 and non-convergence, MemoryError when the device cannot hold a model).  A batched entry point,
@@ -1103,6 +1104,24 @@ class RouteExcitation:
     def solve(self, f: float, guess=None, tol: float = 1e-5) -> Solution:
         Ib, V, its, x = self.stack.solve(f, self.rhs_top(f), self.J(), tol=tol, guess=guess)[:4]
         return self.solution(f, Ib, V, its)
+
+
+def MultiPlaneProblem(layers: list, trace: list, inject_driver: tuple, inject_receiver: tuple,
+                      branches: Optional[list] = None, sigma: float = SIGMA_CU, trace_thickness: float = 35e-6,
+                      capacitance: Optional[list] = None, _device: bool = True) -> RouteExcitation:
+    """A one-off problem: a stack plus one route (peec.py:2820-2826)."""
+    return RouteExcitation(PlaneStack(layers, branches, capacitance, sigma, _device=_device), trace, inject_driver,
+                           inject_receiver, trace_thickness)
+
+
+def PlaneProblem(grid: Grid, trace: list, inject_driver: tuple, inject_receiver: tuple,
+                 branches: Optional[list] = None, cu_thickness: float = 35e-6, sigma: float = SIGMA_CU,
+                 trace_thickness: float = 35e-6, _device: bool = True) -> RouteExcitation:
+    """A single plane at z = 0 under a trace (peec.py:2829-2837); nodes may be (i, j) or (0, i, j)."""
+    fix = lambda n: tuple(n) if len(n) == 3 else (0, *n)  # noqa: E731
+    br = [Branch(fix(b.a), fix(b.b), b.z, b.name, b.kind, b.radius) for b in (branches or [])]
+    return MultiPlaneProblem([PlaneLayer("plane", 0.0, grid, cu_thickness)], trace, fix(inject_driver),
+                             fix(inject_receiver), br, sigma, trace_thickness, _device=_device)
 
 
 def solve_many(excitations: list, freqs, tol: float = 1e-5, **kw) -> list:

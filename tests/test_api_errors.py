@@ -65,3 +65,16 @@ def test_branches_off_copper_are_dropped():
     assert st.with_branches([br]) is st
     new = gs.PlaneStack(st.layers, st.branches + [br], st.pairs, precond="sheet", screen=False, _device=False)
     assert new.nbr == st.nbr
+
+
+def test_plane_problem_builds_the_stack_and_route():
+    """PlaneProblem (peec.py:2829-2837): one plane at z = 0 under a trace, (i, j) nodes taken as layer 0."""
+    b = synth.microstrip()
+    l = b.layers[0]
+    g = gs.Grid(0.0, 0.0, b.d * 1e3, b.nx, b.ny, l.node, l.xb, l.yb)
+    net = b.nets[0]
+    trace = [gs.TraceSegment(s[0:3], s[3:6], float(s[6])) for s in net.segments]
+    pp = gs.PlaneProblem(g, trace, net.driver[1:], net.receiver[1:], _device=False)
+    st, routes = host(b)
+    assert pp.stack.nb == st.nb and pp.injections == routes[0].injections
+    assert np.allclose(pp.psi, routes[0].psi)
