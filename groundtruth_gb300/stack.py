@@ -915,6 +915,17 @@ class PlaneStack:
             x[sl], its[sl], res[sl], ok[sl] = native.solve(
                 self.handle, ops[sl], rhs[sl], tol=tol, restart=restart, max_its=max_its, inner_tol=inner_tol,
                 precision=precision, reorth=reorth, x0=None if x0 is None else x0[sl])
+        lender = getattr(ops[0][0], "factor_of", None) if borrow else None
+        lent = [c for c in range(ncol) if not ok[c] and lender is not None and lender[ops[c][1]] != ops[c][1]]
+        if lent:
+            # a borrowed preconditioner that did not get there: factorise at the columns' own frequencies and go
+            # on from their solutions so far (peec.py:2584-2595)
+            again = self.solve_batch([freqs[c] for c in lent], [rhs_tops[c] for c in lent], [Js[c] for c in lent],
+                                     tol=tol, guesses=[[x[c]] for c in lent], restart=restart, max_its=max_its,
+                                     inner_tol=inner_tol, precision=precision, reorth=reorth, borrow=False,
+                                     failed=[])
+            for c, r in zip(lent, again):
+                x[c], its[c], res[c], ok[c] = r[3], its[c] + r[2], r[4], r[4] <= tol
         out = []
         for c in range(ncol):
             if not ok[c]:

@@ -247,3 +247,38 @@ def test_solves_split_into_what_fits_the_device(monkeypatch):
     free[0] = 1
     with pytest.raises(MemoryError):
         st.columns_that_fit(40)
+
+
+def test_borrowed_columns_that_miss_get_their_own_factorisation(monkeypatch):
+    """A column whose borrowed preconditioner does not reach the tolerance is factorised at its own frequency
+    and solved on from where it got (peec.py:2584-2595); host logic with the device calls faked."""
+    from groundtruth_gb300 import native
+    st = host_stack(synth.small_pair())
+    st.handle = object()
+    freqs = [1e8, 1.1e8]
+
+    class Obj:
+        def __init__(self, keys, factor_of):
+            self.keys, self.factor_of = keys, factor_of
+    calls = []
+
+    def fake_factorise(fs, together=False, borrow=False):
+        keys = [gs.freq_key(f) for f in fs]
+        obj = Obj(keys, np.array([0] * len(keys)) if borrow and len(keys) > 1 else None)
+        return [(obj, n) for n in range(len(keys))]
+
+    def fake_solve(geom, ops, rhs, tol, x0=None, **kw):
+        obj = ops[0][0]
+        calls.append((obj.factor_of is not None, x0 is not None))
+        n = rhs.shape[0]
+        x = np.ones_like(rhs) if x0 is None else x0 + 1
+        res = np.array([1e-3 if obj.factor_of is not None and k == 1 else 1e-9 for k in range(n)])
+        return x, np.full(n, 10, np.int32), res, res <= tol
+    monkeypatch.setattr(st, "factorise", fake_factorise)
+    monkeypatch.setattr(st, "columns_that_fit", lambda n, *a: n)
+    monkeypatch.setattr(st, "_warm_start", lambda ops, rhs, guesses: np.stack([g[0] for g in guesses]))
+    monkeypatch.setattr(native, "solve", fake_solve)
+    J = np.zeros(st.n_nodes)
+    out = st.solve_batch(freqs, [np.zeros(st.nb, complex)] * 2, [J, J], tol=1e-6, borrow=True)
+    assert calls == [(True, False), (False, True)]          # the miss re-solved with its own, from its x
+    assert out[1][2] == 20 and out[1][4] <= 1e-6
