@@ -858,8 +858,10 @@ class PlaneStack:
         elif together and todo and len(todo) < len(set(keys)):
             todo = list(dict.fromkeys(keys))
         if todo:
+            plan = borrow_plan(todo) if borrow else None
+            self._admit(len(set(plan)) if plan is not None else len(todo))
             data = [self._freq_tables(k) for k in todo]
-            ops = native.Operators(self.handle, todo, data, borrow_plan(todo) if borrow else None)
+            ops = native.Operators(self.handle, todo, data, plan)
             with self._lock:
                 for n, k in enumerate(todo):
                     self._ops[k] = (ops, n)
@@ -938,7 +940,33 @@ class PlaneStack:
             out.append((x[c, : self.nb], V, int(its[c]), x[c], float(res[c])))
         return out
 
-    MEMORY_HEADROOM = 0.9         # of the device's free memory a solve may take
+    MEMORY_HEADROOM = 0.9         # of the device's free memory a solve or a factorisation may take
+
+    def factorisation_bytes(self, n_fact: int) -> int:
+        """Device bytes of n_fact factorisations (gt_operators_create_shared): each one's panels in FP64 and FP32,
+        column- and row-major, its pivots and tables, and while it is made the Schur values and update matrices."""
+        sym = self.sym
+        per = sym.panel_total * (16 + 8 + 8 + 16) + sym.n * (16 + 8) + self.n_table * (16 + 8)
+        made = self.sterm.shape[0] * 16 + max(sym.upd_total, 1) * 16
+        return int(n_fact * (per + made))
+
+    def _admit(self, n_fact: int):
+        """The memory gate for factorisations (_MemoryGate, peec.py:1442-1501): when n_fact more would not fit
+        MEMORY_HEADROOM of the free device memory, this stack's cached factorisations are dropped first; still
+        too little: MemoryError."""
+        from . import native
+        need = self.factorisation_bytes(n_fact)
+        free = native.memory(self.handle, 1)["free"]
+        if need <= self.MEMORY_HEADROOM * free:
+            return
+        with self._lock:
+            self._ops.clear()
+        import gc
+        gc.collect()
+        free = native.memory(self.handle, 1)["free"]
+        if need > self.MEMORY_HEADROOM * free:
+            raise MemoryError(f"{n_fact} factorisations need {need / 2**30:.1f} GiB, "
+                              f"{self.MEMORY_HEADROOM * free / 2**30:.1f} GiB are available on the device")
 
     def columns_that_fit(self, ncol: int, restart: int = 50, precision: str = "mixed") -> int:
         """How many columns one device solve takes at once (the reference's memory gate, peec.py:1388-1501):

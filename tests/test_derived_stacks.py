@@ -282,3 +282,22 @@ def test_borrowed_columns_that_miss_get_their_own_factorisation(monkeypatch):
     out = st.solve_batch(freqs, [np.zeros(st.nb, complex)] * 2, [J, J], tol=1e-6, borrow=True)
     assert calls == [(True, False), (False, True)]          # the miss re-solved with its own, from its x
     assert out[1][2] == 20 and out[1][4] <= 1e-6
+
+
+def test_factorisations_are_admitted_against_free_memory(monkeypatch):
+    """The memory gate for factorisations: cached ones are dropped when new ones would not fit, MemoryError
+    when they still do not."""
+    from groundtruth_gb300 import native
+    st = host_stack(synth.small_pair())
+    st.handle = object()
+    one = st.factorisation_bytes(1)
+    assert one > st.sym.panel_total * 48 and st.factorisation_bytes(4) == 4 * one
+    free = [10 * one]
+    monkeypatch.setattr(native, "memory", lambda g, n, *a, **k: {"need": 0, "held": 0, "free": free[0], "total": 0})
+    st._ops["k"] = ("cached", 0)
+    st._admit(4)
+    assert "k" in st._ops                           # fits: the cache stays
+    free[0] = 2 * one
+    with pytest.raises(MemoryError):
+        st._admit(4)
+    assert not st._ops                              # dropped before giving up
