@@ -64,9 +64,10 @@ def copper_at(px, py, outline: np.ndarray, cutouts: list) -> np.ndarray:
     return inside
 
 
-def raster_layer(nx: int, ny: int, d: float, outline: np.ndarray, cutouts: list):
+def raster_layer(nx: int, ny: int, d: float, outline: np.ndarray, cutouts: list, exact: bool = False):
     """(node, xb, yb) masks for one layer's copper by the sub=1 rules (node at (i d, j d), coordinates in
-    the same unit as d)."""
+    the same unit as d); exact=True adds the strips' widths: the share of each strip's cell border that the
+    copper covers (raster.line_cover along the borders, raster.strip_widths), as (node, xb, yb, widths)."""
     xs = np.arange(nx) * d
     ys = np.arange(ny) * d
     X, Y = np.meshgrid(xs, ys, indexing="ij")
@@ -75,7 +76,17 @@ def raster_layer(nx: int, ny: int, d: float, outline: np.ndarray, cutouts: list)
     my = copper_at(X[:, :-1], Y[:, :-1] + d / 2, outline, cutouts)
     xb = node[:-1, :] & node[1:, :] & mx
     yb = node[:, :-1] & node[:, 1:] & my
-    return node, xb, yb
+    if not exact:
+        return node, xb, yb
+    from . import raster
+    pa, pb = raster.ring_edges(outline, cutouts)
+    # an x strip (i, j) crosses the border x = (i + 1/2) d, |y - j d| <= d / 2; a y strip the border y = (j + 1/2) d
+    cx = raster.line_cover(pa[:, 0], pa[:, 1], pb[:, 0], pb[:, 1], d / 2, d, nx - 1, 0.0, d, ny) / d
+    cy = raster.line_cover(pa[:, 1], pa[:, 0], pb[:, 1], pb[:, 0], d / 2, d, ny - 1, 0.0, d, nx).T / d
+    zx, zy = np.zeros(xb.shape), np.zeros(yb.shape)
+    wx, ox = raster.strip_widths(xb, cx, zx, zx, d)
+    wy, oy = raster.strip_widths(yb, cy, zy, zy, d)
+    return node, xb, yb, {"wx": np.where(xb, wx, 1.0), "wy": np.where(yb, wy, 1.0), "ox": ox, "oy": oy}
 
 
 def rect_polygon(cx: float, cy: float, length: float, width: float, angle: float) -> np.ndarray:

@@ -41,3 +41,23 @@ def test_strip_widths_adopt_and_series_factor_match_reference():
     for ax in (0, 1):
         got = raster.series_factor(Z["sf_face"], list(Z["sf_samples"]), Z["sf_has"], ax)
         assert np.array_equal(got, Z[f"sf_{ax}"])
+
+
+def test_exact_widths_of_a_slanted_slot():
+    """A plane with a slanted slot rasterised with exact widths: full strips away from it, strips whose border
+    the slot partly covers narrower, every width in (0, 1]; the host stack models them."""
+    from groundtruth_gb300 import stack as gs, synth
+    d, n = 0.5e-3, 30
+    h = d / 2
+    outline = np.array([[-h, -h], [(n - 1) * d + h, -h], [(n - 1) * d + h, (n - 1) * d + h], [-h, (n - 1) * d + h]])
+    slot = synth.rect_polygon(7.3e-3, 7.1e-3, 9e-3, 0.8e-3, 0.5)
+    node, xb, yb, w = synth.raster_layer(n, n, d, outline, [slot], exact=True)
+    wx, wy = w["wx"][xb], w["wy"][yb]
+    assert np.all((wx > 0) & (wx <= 1)) and np.all((wy > 0) & (wy <= 1))
+    narrow = lambda w: np.count_nonzero(w < 1 - 1e-9)      # noqa: E731  (a border's sum of partial intervals)
+    assert 0 < narrow(wx) < len(wx) // 4 and narrow(wy) > 0
+    layer = synth.Layer("GND", 0.0, 35e-6, node, xb, yb, w)
+    pwr = synth._full_layer("PWR", -0.5e-3, 35e-6, n, n, d)
+    b = synth.Board("exact", d, n, n, [layer, pwr], [synth.Pair(0, 1, 7.6e-8, 0.02)], [], [], np.array([1e8]))
+    st, _ = gs.from_board(b, _device=False)
+    assert st.dL is not None and np.count_nonzero(st.dL) == narrow(st.strip_width)
