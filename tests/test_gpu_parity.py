@@ -201,3 +201,24 @@ def test_memory_gate_counts_the_workspace(case):
     st.solve_batch([f] * 4, [r.rhs_top(f)] * 4, [r.J()] * 4, tol=board.tol)
     held = native.memory(st.handle, 4)["held"]
     assert held >= m4["need"] - 4 * st.handle.n_compact * 16
+
+
+@pytest.mark.parametrize("name", ["small_pair", "necked_faces"])
+def test_not_converged_is_reported(name):
+    """Forced non-convergence, an iteration limit of 2 against a tolerance of 1e-12 (peec.py:2599-2600): a
+    SolverError naming the frequency, or, with `failed`, every column's index and its solution so far; the device
+    state stays usable and the next solve at the board's tolerance converges."""
+    z, board = load(name)
+    st, routes = gs.from_board(board)
+    r = routes[0]
+    fs = [float(f) for f in board.freqs[:2]]
+    args = (fs, [r.rhs_top(f) for f in fs], [r.J()] * len(fs))
+    with pytest.raises(gs.SolverError, match="did not converge"):
+        st.solve_batch(*args, tol=1e-12, max_its=2)
+    failed = []
+    out = st.solve_batch(*args, tol=1e-12, max_its=2, failed=failed)
+    assert failed == list(range(len(fs)))
+    assert all(np.isfinite(o[3]).all() and o[4] > 1e-12 for o in out)
+    sol = gs.solve_many(routes[:1], fs[:1], tol=board.tol)[0][0]
+    assert sol.residual <= board.tol
+    assert abs(sol.Z_loop - complex(z["Z0_0"])) <= 1e-8 * abs(complex(z["Z0_0"]))
