@@ -132,3 +132,37 @@ def test_serving_solves_survive_a_worker_killed_mid_batch(tmp_path):
         ref = routes[j["net"]].solve(float(board.freqs[j["f"]]), tol=board.tol)
         assert o.value[0] == pytest.approx(complex(ref["Z_loop"]), rel=1e-12)
         assert np.allclose(o.value[1], ref["m"], rtol=1e-12, atol=0)
+
+
+def test_solve_board_reads_the_board_and_gathers_every_net_and_frequency(monkeypatch):
+    """dispatch.solve_board's host side, in this process: the board comes back from its arrays, every net is solved
+    at every frequency in one batch, and the answers are gathered per (net, frequency).  The device solve is
+    replaced here by the oracle's."""
+    from groundtruth_gb300 import stack as gs
+    from test_oracle_golden import oracle_routes, oracle_stack
+    board = synth.small_pair()
+    host = gs.from_board
+    monkeypatch.setattr(gs, "from_board", lambda b: host(b, _device=False))
+    seen = {}
+
+    def oracle_many(routes, freqs, tol, restart):
+        seen.update(n=len(routes), freqs=list(freqs), tol=tol, restart=restart)
+        ref = oracle_routes(oracle_stack(board), board)
+        out = []
+        for r in ref:
+            row = []
+            for f in freqs:
+                o = r.solve(float(f), tol=tol)
+                row.append(gs.Solution(float(f), o["I_x"], o["I_y"], o["V"], o["I_branch"], complex(o["Z_loop"]),
+                                       np.asarray(o["m"]), int(o["its"])))
+            out.append(row)
+        return out
+    monkeypatch.setattr(gs, "solve_many", oracle_many)
+    res = dispatch.solve_board(board.to_arrays())
+    nn, nf = len(board.nets), len(board.freqs)
+    assert seen == dict(n=nn, freqs=list(board.freqs), tol=board.tol, restart=board.restart)
+    assert res["Z_loop"].shape == (nn, nf) and res["m"].shape == (nn, nf, 3)
+    assert res["iterations"].shape == (nn, nf) and res["residual"].shape == (nn, nf)
+    assert np.array_equal(res["freqs"], board.freqs)
+    ref = oracle_routes(oracle_stack(board), board)[1].solve(float(board.freqs[2]), tol=board.tol)
+    assert res["Z_loop"][1, 2] == complex(ref["Z_loop"])
