@@ -464,6 +464,26 @@ def _labels(mask: np.ndarray, xb: np.ndarray, yb: np.ndarray) -> np.ndarray:
 WIDTH_KEYS = ("wx", "wy", "ox", "oy", "rx", "ry")
 
 
+def plane_pair_line(length_mm: float, w: float = 10e-3, h: float = 0.2e-3, t: float = 35e-6, d: float = 0.4e-3,
+                    f=(1e6, 1e8)) -> Board:
+    """A parallel-plate line (the reference's plane_pair_line, tests/boardgen.py:1149-1178): two strips `w` wide
+    and `length_mm` long, copper `t` thick, `h` of dielectric between their faces (layer heights at the foils'
+    centres, h + t apart), on pitch d.  A row of ten shorts 1 mm apart across the far end (a capacitor's short
+    model: 1 uOhm, 1 fH), fed between the strips near the other end: the one net has no trace, its receiver on the
+    upper strip (+1 A in) and its driver on the lower one, so its loop impedance is the port's."""
+    nx, ny = int(round(length_mm * 1e-3 / d)), int(round(w / d))
+    node = np.ones((nx, ny), bool)
+    layers = [Layer(name, z, t, node.copy(), np.ones((nx - 1, ny), bool), np.ones((nx, ny - 1), bool))
+              for name, z in (("VDD", 0.0), ("GND", -(h + t)))]
+    n = 10
+    shorts = [BranchSpec((0, nx - 2, j), (1, nx - 2, j), 1e-6, 1e-15) for j in
+              (int((k + 0.5) * w / n / d) for k in range(n))]
+    feed = ny // 2
+    net = Net(np.zeros((0, 8)), (1, 2, feed), (0, 2, feed))
+    return Board(f"plane_pair_line{length_mm:g}", d, nx, ny, layers, branches=shorts, nets=[net],
+                 freqs=np.asarray(f, float), precond="sheet", tol=1e-8, restart=50)
+
+
 def microstrip(slot: float = 0.0, edge_split: bool = False, full_cut: bool = False, f=(1e8,)) -> Board:
     """A 40 x 20 mm plane (35 um copper at z = 0) on 0.25 mm pitch under a 0.2 mm trace 0.5 mm above it, from
     (5, 10) to (35, 10) mm, dropping to the plane at both ends (the reference's analytic cases, tests/

@@ -2,7 +2,8 @@
 restated on a 40 x 20 mm plane under a microstrip (synth.microstrip): the strip kernel's symmetry and self term,
 the return current under the trace against image theory, the loop inductance against Wheeler's formula and
 the moment against the loop's area, current spreading at low frequency, a slot's monotonic effect, a cut from
-the edge turning the loop into the board plane, and a fully cut plane refused.  Each runs on the oracle (CPU)
+the edge turning the loop into the board plane, a fully cut plane refused, a plane pair's inductance per
+length (tests/test_plane_pair.py:70-81), and the reciprocity of two loops' mutual impedance.  Each runs on the oracle (CPU)
 and, marked gpu, through the CUDA library."""
 import math
 
@@ -100,6 +101,65 @@ def test_fully_cut_plane_is_refused():
         oracle_routes(oracle_stack(b), b)
     with pytest.raises(gs.SolverError):
         gs.from_board(b, _device=False)
+
+
+@pytest.mark.parametrize("solve", SOLVERS)
+def test_plane_pair_inductance_per_length(solve):
+    """test_plane_pair.py:70-81: a parallel-plate line 10 mm wide, 0.2 mm between its 35 um foils, shorted at
+    its far end; the difference of a 40 mm and a 20 mm line is the inductance of 20 mm of line alone.  At 1 MHz
+    (skin depth 66 um > t) mu0 (h + 2t/3) / w, at 100 MHz (6.6 um) mu0 (h + delta) / w, each within -6 % / +3 %
+    (the field fringing past the edges lowers it), and the high-frequency value the lower one."""
+    mu0, sigma, h, w, t = 4e-7 * math.pi, 5.8e7, 0.2e-3, 10e-3, 35e-6
+    L = {ln: [] for ln in (20.0, 40.0)}
+    for ln in L:
+        b = synth.plane_pair_line(ln)
+        for f in b.freqs:
+            L[ln].append(solve(b, f)[1].imag / (2 * math.pi * f))
+    per = [(l40 - l20) / 20e-3 for l20, l40 in zip(L[20.0], L[40.0])]
+    low = mu0 * (h + 2 * t / 3) / w
+    high = mu0 * (h + 1 / math.sqrt(math.pi * 1e8 * mu0 * sigma)) / w
+    assert 0.94 * low < per[0] < 1.03 * low, (per[0], low)
+    assert 0.94 * high < per[1] < 1.03 * high, (per[1], high)
+    assert per[1] < per[0]
+
+
+def _two_loops_oracle(board, f):
+    st = oracle_stack(board)
+    rs = oracle_routes(st, board)
+    net = board.nets[0]
+    other = rs[1] if len(rs) > 1 else po.OracleRoute(st, [], net.driver, net.receiver)
+    out = []
+    for r in (rs[0], other):
+        Ib, V, *_ = st.solve(f, r.rhs_top(f), r.J(), tol=1e-12)
+        out.append((r.psi, r.J(), Ib, V))
+    return out
+
+
+def _two_loops_device(board, f):
+    st, routes = gs.from_board(board)
+    net = board.nets[0]
+    rs = [routes[0], routes[1] if len(routes) > 1 else gs.RouteExcitation(st, [], net.driver, net.receiver)]
+    res = st.solve_batch([f, f], [r.rhs_top(f) for r in rs], [r.J() for r in rs], tol=1e-10)
+    return [(r.psi, r.J(), o[0], o[1]) for r, o in zip(rs, res)]
+
+
+@pytest.mark.parametrize("name", ["small_pair", "necked_pair", "necked_faces", "six_sheet"])
+@pytest.mark.parametrize("solve", [pytest.param(_two_loops_oracle, id="oracle"),
+                                   pytest.param(_two_loops_device, id="gpu", marks=pytest.mark.gpu)])
+def test_mutual_impedance_is_reciprocal(solve, name):
+    """Reciprocity, a property of the system at any size (its matrix is complex symmetric: the partial
+    inductances, the narrow strips' mutual corrections and the face couplings are): the plane's part of the
+    mutual impedance of two loops, j omega psi_a . I_b + J_a . V_b, is the same both ways.  The loops are the
+    board's first two nets, or its first net and a port at the same return nodes without the trace; with plane
+    pairs, narrow strips, face sheets and six layers."""
+    board = getattr(synth, name)()
+    for f in board.freqs[:2]:
+        w = 2 * math.pi * f
+        loops = solve(board, float(f))
+        z = [[1j * w * np.dot(a[0], b[2]) + a[1] @ b[3] for b in loops] for a in loops]
+        scale = math.sqrt(abs(z[0][0] * z[1][1]))
+        assert abs(z[0][1]) > 1e-3 * scale
+        assert abs(z[0][1] - z[1][0]) <= 1e-7 * scale, (name, f)
 
 
 def _tape_integral(length, wa, wb, axial, lateral, dz):
