@@ -890,7 +890,10 @@ class PlaneStack:
     # ------------------------------------------------------------------ solves
     def solve(self, f: float, rhs_top: np.ndarray, J: np.ndarray, tol: float = 1e-5, max_cycles: int = 8,
               guess: Optional[list] = None):
-        """Solve K [I; V] = [rhs_top; J] (peec.py:2513-2607).  Returns (Ib (nb), V (n_nodes), its, x)."""
+        """Solve K [I; V] = [rhs_top; J] (peec.py:2513-2607).  Returns (Ib (nb), V (n_nodes), its, x).
+        max_cycles is taken for the reference's signature: the reference restarts GMRES max_cycles times (and
+        more while each restart still lowers the residual, peec.py:3093-3110); the device's FP64 outer
+        iteration instead stops at tol, at max_its inner iterations (solve_batch) or after 40 outer steps."""
         out = self.solve_batch([f], [np.asarray(rhs_top, complex)], [np.asarray(J, float)], tol=tol,
                                max_cycles=max_cycles, guesses=[guess])
         return out[0]

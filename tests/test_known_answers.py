@@ -220,7 +220,8 @@ def test_slab_impedance_is_the_coth_form(t_um):
 
 
 def test_oracle_gmres_solves_like_a_direct_solve():
-    """test_speed.py:18-28: restarted GMRES reaches the direct solution to 1e-8 across restarts."""
+    """test_speed.py:18-28: restarted GMRES reaches the direct solution to 1e-8 across restarts, and stops at its
+    iteration budget with the best solution so far."""
     rng = np.random.default_rng(1)
     n = 60
     A = np.eye(n) * 4 + rng.standard_normal((n, n)) / np.sqrt(n) + 1j * rng.standard_normal((n, n)) / np.sqrt(n)
@@ -228,6 +229,26 @@ def test_oracle_gmres_solves_like_a_direct_solve():
     x, its, ok = po.gmres(lambda v: A @ v, b, 1e-10, restart=15, max_cycles=40)
     assert ok and its > 15
     assert np.linalg.norm(x - np.linalg.solve(A, b)) < 1e-8 * np.linalg.norm(x)
+    D = np.arange(1.0, 201.0)                   # needs ~200 iterations: stopped at its budget, the best so far
+    x, its, ok = po.gmres(lambda v: D * v, np.ones(200, complex), 1e-10, max_its=7)
+    assert not ok and its == 7 and np.linalg.norm(D * x - 1) < np.sqrt(200)
+
+
+def test_oracle_gmres_goes_on_while_its_residual_falls():
+    """test_speed.py:31-45: restarts beyond max_cycles while each still lowers the residual, none once it
+    stalls (GMRES(4) on a cyclic shift makes no progress)."""
+    rng = np.random.default_rng(2)
+    n = 120
+    A = np.eye(n) * 3 + rng.standard_normal((n, n)) / np.sqrt(n)
+    b = rng.standard_normal(n).astype(complex)
+    _, its, ok = po.gmres(lambda v: A @ v, b, 1e-10, restart=4, max_cycles=3)
+    assert not ok and its == 12
+    x, its, ok = po.gmres(lambda v: A @ v, b, 1e-10, restart=4, max_cycles=3, extra_cycles=40)
+    assert ok and its > 12 and np.linalg.norm(A @ x - b) <= 1e-10 * np.linalg.norm(b)
+    P = np.roll(np.eye(n), 1, axis=0)
+    _, its, ok = po.gmres(lambda v: P @ v, np.eye(n)[0].astype(complex), 1e-10, restart=4, max_cycles=2,
+                          extra_cycles=40)
+    assert not ok and its <= 3 * 4
 
 
 def _dc_drop(board):
