@@ -680,3 +680,13 @@ def what_if_branches(board: Board, seed: int, n_via: int = 2, n_part: int = 1) -
 WORKLOADS = {"plain_plane": plain_plane, "slotted_pair": slotted_pair, "small_pair": small_pair,
              "small_stack3": small_stack3, "six_sheet": six_sheet, "necked_pair": necked_pair,
              "faces_stack3": faces_stack3, "necked_faces": necked_faces}
+
+# the analytic known-answer boards (the reference's tests/test_solver.py:19-88 and tests/test_plane_pair.py:19-81)
+KNOWN_BOARDS = {
+    "microstrip": lambda: microstrip(f=(1e3, 1e8)),
+    "microstrip_slot6": lambda: microstrip(slot=6.0),
+    "microstrip_slot12": lambda: microstrip(slot=12.0),
+    "microstrip_edge_split": lambda: microstrip(edge_split=True),
+    "plane_pair_line20": lambda: plane_pair_line(20.0),
+    "plane_pair_line40": lambda: plane_pair_line(40.0),
+}

@@ -29,6 +29,10 @@ copper width, Solution.node_field).
 ``small_pair_derived.npz`` holds the same for small_pair plus a what-if edit's branches on a derived stack
 (PlaneStack.with_branches), including solves warm-started from the base's solutions.
 
+``known_answers.npz``: the reference's loop impedances and moments for the known-answer boards (the
+microstrip over a 40 x 20 mm plane with and without slots or an edge cut, the parallel-plate lines 20 and 40 mm
+long; ``synth.KNOWN_BOARDS``), solved to rtol 1e-10.
+
 ``--full`` additionally runs the 256 x 256 slotted plane pair (a few nets x frequencies, minutes per solve)
 and stores only its scalar outputs (Z_loop, its, current norms).
 """
@@ -240,6 +244,29 @@ def kernel_functions(kernel) -> dict:
             "strip_kernel_6x5": kernel.strip_kernel(6, 5, 0.5e-3, 0.3e-3)}
 
 
+KNOWN_TOL = 1e-10
+
+
+def record_known(peec) -> dict:
+    """Per known-answer board and frequency the reference's Z_loop, moment and iterations at rtol KNOWN_TOL."""
+    out = {}
+    for name, make in synth.KNOWN_BOARDS.items():
+        board = make()
+        peec.gmres_restart = lambda n, r=board.restart: r
+        peec.PlaneStack.solve.__defaults__ = (KNOWN_TOL, 8, None)
+        st, routes = build_reference(peec, board)
+        out[f"{name}_freqs"] = np.asarray(board.freqs, float)
+        for q, f in enumerate(board.freqs):
+            t0 = time.perf_counter()
+            sol = routes[0].solve(float(f))
+            out[f"{name}_Z{q}"] = np.complex128(sol.Z_loop)
+            out[f"{name}_m{q}"] = np.asarray(sol.m)
+            out[f"{name}_its{q}"] = np.int64(sol.iterations)
+            print(f"  {name} f {f:.4g}: its {sol.iterations} Z {sol.Z_loop:.10g} ({time.perf_counter() - t0:.1f} s)",
+                  flush=True)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", required=True)
@@ -247,8 +274,13 @@ def main():
     ap.add_argument("--derived-only", action="store_true", help="only the derived-stack fixture")
     ap.add_argument("--narrow-only", action="store_true", help="only the narrow-strip board's fixture")
     ap.add_argument("--faces-only", action="store_true", help="only the face-sheet boards' fixtures")
+    ap.add_argument("--known-only", action="store_true", help="only the known-answer boards' scalars")
     args = ap.parse_args()
     peec, kernel = import_reference(args.reference)
+    print("known_answers", flush=True)
+    np.savez_compressed(HERE / "known_answers.npz", **record_known(peec))
+    if args.known_only:
+        return
     for pc in ("diag", "sheet"):
         print(f"faces_stack3_{pc}", flush=True)
         np.savez_compressed(HERE / f"faces_stack3_{pc}.npz", **record(peec, synth.faces_stack3(pc)))

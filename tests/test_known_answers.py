@@ -6,6 +6,7 @@ the edge turning the loop into the board plane, a fully cut plane refused, a pla
 length (tests/test_plane_pair.py:70-81), and the reciprocity of two loops' mutual impedance.  Each runs on the oracle (CPU)
 and, marked gpu, through the CUDA library."""
 import math
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -121,6 +122,22 @@ def test_plane_pair_inductance_per_length(solve):
     assert 0.94 * low < per[0] < 1.03 * low, (per[0], low)
     assert 0.94 * high < per[1] < 1.03 * high, (per[1], high)
     assert per[1] < per[0]
+
+
+@pytest.mark.parametrize("name", list(synth.KNOWN_BOARDS))
+@pytest.mark.parametrize("solve", SOLVERS)
+def test_known_answer_boards_match_the_reference(solve, name):
+    """The known-answer boards' loop impedances and moments against the reference's own solves of the same
+    boards (tests/golden/known_answers.npz), both at rtol 1e-10: Z_loop within 1e-8, m within 1e-6."""
+    ref = np.load(Path(__file__).resolve().parent / "golden" / "known_answers.npz")
+    board = synth.KNOWN_BOARDS[name]()
+    board.tol = 1e-10
+    assert np.array_equal(ref[f"{name}_freqs"], board.freqs)
+    for q, f in enumerate(board.freqs):
+        _, Z, m = solve(board, float(f))
+        Zr, mr = complex(ref[f"{name}_Z{q}"]), ref[f"{name}_m{q}"]
+        assert abs(Z - Zr) <= 1e-8 * abs(Zr), (name, f, Z, Zr)
+        assert np.linalg.norm(m - mr) <= 1e-6 * np.linalg.norm(mr), (name, f)
 
 
 def _two_loops_oracle(board, f):
