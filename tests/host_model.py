@@ -2,8 +2,9 @@
 
 It executes, with numpy, the same arithmetic the CUDA kernels do on the same uploaded arrays: the 3-pass
 FFT L_p product on this build's padded sizes, the stencil tail of the system product, the per-position
-admittance blocks, and the multifrontal LDL^T factorisation / triangular solves driven by the symbolic
-analysis.  Tests compare it with the oracle (so the arrays are right) and the GPU with it (so the kernels
+admittance blocks (with the positions' own blocks where strips are not full squares), the correction rows of
+narrow strips and split layers' face couplings (narrow.cu), current sheets mapped to node layers (face
+sheets), and the multifrontal LDL^T factorisation / triangular solves driven by the symbolic analysis.  Tests compare it with the oracle (so the arrays are right) and the GPU with it (so the kernels
 are)."""
 import numpy as np
 
@@ -13,6 +14,8 @@ class DenseModel:
         self.st = st
         t, D = st.top, st.dense
         self.S, self.nx, self.ny = t.S, t.nx, t.ny
+        self.NL = t.NL
+        self.lay = np.asarray(t.sheet_layer, np.int64)     # each current sheet's node layer
         self.D = D
         self.np_ = len(t.pair_layers)
 
@@ -28,7 +31,8 @@ class DenseModel:
         if name == "B":
             return v[..., D.off_b: D.off_b + self.st.nbr]
         if name == "V":
-            return v[..., D.off_v: D.off_v + S * nx * ny].reshape(v.shape[:-1] + (S, nx, ny))
+            NL = self.NL
+            return v[..., D.off_v: D.off_v + NL * nx * ny].reshape(v.shape[:-1] + (NL, nx, ny))
 
     def to_dense(self, x_compact):
         v = np.zeros(self.D.n, complex)
@@ -56,38 +60,47 @@ class DenseModel:
 
     # ---------------------------------------------------------------- system product
     def matvec(self, v, w, zs, zcap, zbr):
+        """zs: the sheets' impedances (S,) then the split layers' face couplings (n_twins,)."""
         st = self.st
         t = st.top
+        zsh, zm = zs[: self.S], zs[self.S:]
         out = np.zeros_like(v)
         X, Y, C, B, Vn = (self.seg(v, n) for n in "XYCBV")
         oX, oY, oC, oB, oV = (self.seg(out, n) for n in "XYCBV")
-        oX[:] = (zs[:, None, None] * X + 1j * w * self.lp(X, "x") - (Vn[:, :-1, :] - Vn[:, 1:, :])) * t.xb
-        oY[:] = (zs[:, None, None] * Y + 1j * w * self.lp(Y, "y") - (Vn[:, :, :-1] - Vn[:, :, 1:])) * t.yb
+        Vs = Vn[self.lay]                         # a sheet's strips end on its layer's nodes
+        oX[:] = (zsh[:, None, None] * X + 1j * w * self.lp(X, "x") - (Vs[:, :-1, :] - Vs[:, 1:, :])) * t.xb
+        oY[:] = (zsh[:, None, None] * Y + 1j * w * self.lp(Y, "y") - (Vs[:, :, :-1] - Vs[:, :, 1:])) * t.yb
         for p, (u, l) in enumerate(t.pair_layers):
             oC[p] = (zcap[p] * C[p] - (Vn[u] - Vn[l])) * t.cap_mask[p]
         Vf = Vn.reshape(-1)
         for n, (a, b) in enumerate(self.branch_dense()):
             oB[n] = zbr[n] * B[n] - (Vf[a] - Vf[b])
-        kcl = np.zeros_like(Vn)
-        kcl[:, :-1, :] += X
-        kcl[:, 1:, :] -= X
-        kcl[:, :, :-1] += Y
-        kcl[:, :, 1:] -= Y
-        for p, (u, l) in enumerate(t.pair_layers):
-            kcl[u] += C[p]
-            kcl[l] -= C[p]
-        kf = kcl.reshape(-1)
-        for n, (a, b) in enumerate(self.branch_dense()):
-            kf[a] += B[n]
-            kf[b] -= B[n]
-        oV[:] = kcl * self.vmask()
+        self.corrections(v, out, w, zsh, zm)
+        oV[:] = self.kcl(v)
         return out
 
+    def corrections(self, v, out, w, zsh, zm):
+        """The rows of strips that are not full squares and of face pairs (narrow.cu's system-product mode):
+        out[p] += z (1/w_p - 1) x[p] + j omega (dL_p x[p] + sum_q M[p,q] x[q]) (+ the real part's factor)
+        (+ the face coupling z_mut / width x[partner])."""
+        nr = getattr(self.st, "narrow_rows", None)
+        if nr is None:
+            return
+        for q in range(len(nr["pos"])):
+            p, s = nr["pos"][q], nr["sheet"][q]
+            lo, hi = nr["ptr"][q], nr["ptr"][q + 1]
+            acc = nr["dl"][q] * v[p] + np.dot(nr["val"][lo:hi], v[nr["col"][lo:hi]])
+            y = nr["rdelta"][q] * zsh[s] * v[p] + 1j * w * acc + nr["rre"][q] * zsh[s].real * v[p]
+            if nr["partner"][q] >= 0:
+                zq = zm[nr["twin"][q]]
+                y += (nr["tw_fac"][q] * zq + nr["twre"][q] * zq.real) * v[nr["partner"][q]]
+            out[p] += y
+
     def vmask(self):
-        m = np.zeros(self.S * self.nx * self.ny, bool)
+        m = np.zeros(self.NL * self.nx * self.ny, bool)
         node_dense = np.flatnonzero(self.st.top.node.ravel())
         m[node_dense[self.st.top.keep]] = True
-        return m.reshape(self.S, self.nx, self.ny)
+        return m.reshape(self.NL, self.nx, self.ny)
 
     def branch_dense(self):
         node_dense = np.flatnonzero(self.st.top.node.ravel())
@@ -104,6 +117,13 @@ class DenseModel:
             O = self.seg(out, name)
             code = st.code["x" if o == 0 else "y"].astype(np.int64)
             T = tab[: 2 * ncode * S * S].reshape(2, ncode, S, S)[o][code]      # (n0, n1, S, S)
+            own = st.override["x" if o == 0 else "y"] if st.n_override else None
+            if own is not None and (own >= 0).any():
+                # a position whose strips are not all full squares: its own block, over the sheets present
+                blocks = tab[st.tab_ovr0: st.tab_ovr0 + st.n_override * S * S].reshape(-1, S, S)
+                sel = own >= 0
+                bits = (code[sel][:, None] >> np.arange(S)[None, :]) & 1
+                T[sel] = blocks[own[sel]] * (bits[:, :, None] * bits[:, None, :])
             O[:] = np.einsum("ijkl,lij->kij", T, A)
         C, oC = self.seg(v, "C"), self.seg(out, "C")
         for p in range(self.np_):
@@ -115,11 +135,12 @@ class DenseModel:
         """Ar^T applied to the branch segments: the node rows (masked by the kept nodes)."""
         t = self.st.top
         X, Y, C, B = (self.seg(v, n) for n in "XYCB")
-        k = np.zeros((self.S, self.nx, self.ny), complex)
-        k[:, :-1, :] += X
-        k[:, 1:, :] -= X
-        k[:, :, :-1] += Y
-        k[:, :, 1:] -= Y
+        k = np.zeros((self.NL, self.nx, self.ny), complex)
+        for s, L in enumerate(self.lay):          # a face sheet's strips join its layer's nodes
+            k[L, :-1, :] += X[s]
+            k[L, 1:, :] -= X[s]
+            k[L, :, :-1] += Y[s]
+            k[L, :, 1:] -= Y[s]
         for p, (u, l) in enumerate(t.pair_layers):
             k[u] += C[p]
             k[l] -= C[p]
@@ -132,8 +153,9 @@ class DenseModel:
     def grad(self, Vn):
         """Ar applied to node potentials: per-branch-segment differences V[a] - V[b] (dense, unmasked)."""
         out = np.zeros(self.D.n, complex)
-        self.seg(out, "X")[:] = Vn[:, :-1, :] - Vn[:, 1:, :]
-        self.seg(out, "Y")[:] = Vn[:, :, :-1] - Vn[:, :, 1:]
+        Vs = Vn[self.lay]
+        self.seg(out, "X")[:] = Vs[:, :-1, :] - Vs[:, 1:, :]
+        self.seg(out, "Y")[:] = Vs[:, :, :-1] - Vs[:, :, 1:]
         C = self.seg(out, "C")
         for p, (u, l) in enumerate(self.st.top.pair_layers):
             C[p] = Vn[u] - Vn[l]
@@ -149,9 +171,9 @@ class DenseModel:
         s = self.seg(v, "V") - self.kcl(t1)
         s_fac = s.reshape(-1)[sym.iperm]
         y_fac = fac.solve(s_fac)
-        yv = np.zeros(self.S * self.nx * self.ny, complex)
+        yv = np.zeros(self.NL * self.nx * self.ny, complex)
         yv[sym.iperm] = y_fac
-        yv = yv.reshape(self.S, self.nx, self.ny)
+        yv = yv.reshape(self.NL, self.nx, self.ny)
         u = v + self.grad(yv)
         out = self.dinv(u, tab)
         out *= self.D.mask

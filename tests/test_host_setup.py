@@ -149,3 +149,25 @@ def test_current_density_maps_match_reference():
         for copper in (False, True):
             kx, ky = sol.node_field(k, board.d * 1e3, copper=copper)
             assert rel(kx, z[f"kx{k}_{int(copper)}"]) < 1e-12 and rel(ky, z[f"ky{k}_{int(copper)}"]) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["necked_pair", "faces_stack3_diag", "faces_stack3_sheet", "necked_faces",
+                                  "necked_pair_scaled", "faces_stack3_sheet_scaled"])
+def test_corrections_and_face_sheets_through_the_device_model(name):
+    """The arrays uploaded for strips narrower than the pitch, face sheets and resistance factors (the correction
+    rows, the positions' own D^-1 blocks, the sheets' node layers) give, through the numpy model of the device
+    algorithm, the reference's own system product (<=1e-12) and preconditioner (<=1e-9)."""
+    z, board = load(name)
+    st, routes = gs.from_board(board, _device=False)
+    if "r_scale" in z.files:
+        st.set_resistance_scale(z["r_scale"], z["branch_scale"])
+    m = DenseModel(st)
+    f = float(z["op_f"])
+    w, zs, zcap, zbr, tab = st._freq_tables(f)
+    x = m.to_dense(z["prod_x"])
+    got = m.to_compact(m.matvec(x, w, zs, zcap, zbr))
+    assert rel(got, z["prod_matvec"]) < 1e-12
+    rows = np.flatnonzero(np.isin(m.D.compact_to_dense, st.narrow_rows["pos"]))     # the corrected rows alone
+    assert len(rows) and rel(got[rows], z["prod_matvec"][rows]) < 1e-12
+    mf = Multifrontal(st, st.sterm @ tab)
+    assert rel(m.to_compact(m.precond(x, tab, mf)), z["prod_precond"]) < 1e-9
