@@ -235,3 +235,29 @@ class Multifrontal:
                 for k in range(no - 1, -1, -1):
                     z[o0 + k] -= Lp[no:, k] @ z[bnd] + Lp[k + 1: no, k] @ z[o0 + k + 1: o0 + no]
         return z
+
+
+class LowRank:
+    """A derived stack's factor (woodbury.cu, gt_operators_derive): the base's factorisation of S plus the added
+    branches' update S' = S + U diag(1/z) U^T, solved as y - W (Z + U^T W)^-1 U^T y with y = S^-1 v and
+    W = S^-1 U (U: per added branch +1 / -1 at its kept end nodes, in factor order)."""
+
+    def __init__(self, model: DenseModel, fac, zbr):
+        st = model.st
+        sym = st.sym
+        n0 = st.nbr - st.n_lowrank
+        ends = model.branch_dense()[n0:]
+        kept = model.vmask().reshape(-1)
+        self.U = np.zeros((sym.n, st.n_lowrank))
+        for k, (a, b) in enumerate(ends):
+            if kept[a]:
+                self.U[sym.perm[a], k] += 1.0
+            if kept[b]:
+                self.U[sym.perm[b], k] -= 1.0
+        self.fac = fac
+        self.W = np.stack([fac.solve(self.U[:, k].astype(complex)) for k in range(st.n_lowrank)], axis=1)
+        self.Minv = np.linalg.inv(np.diag(zbr[n0:]) + self.U.T @ self.W)
+
+    def solve(self, v):
+        y = self.fac.solve(v)
+        return y - self.W @ (self.Minv @ (self.U.T @ y))

@@ -171,3 +171,23 @@ def test_corrections_and_face_sheets_through_the_device_model(name):
     assert len(rows) and rel(got[rows], z["prod_matvec"][rows]) < 1e-12
     mf = Multifrontal(st, st.sterm @ tab)
     assert rel(m.to_compact(m.precond(x, tab, mf)), z["prod_precond"]) < 1e-9
+
+
+def test_derived_stack_through_the_device_model():
+    """A derived stack (a what-if edit's branches on the base's factorisation, PlaneStack.with_branches): its
+    system product and its preconditioner, the base's factor with the low-rank update for the added branches,
+    through the numpy model equal the reference's own derived stack's (small_pair_derived.npz)."""
+    from host_model import LowRank
+    from test_derived_stacks import extra_of
+    z, board = load("small_pair_derived")
+    st, _ = gs.from_board(board, _device=False)
+    dst = st.with_branches([gs.Branch(b.a, b.b, b.z, f"x{n}", b.kind, b.radius)
+                            for n, b in enumerate(extra_of(z))])
+    assert dst._base is st and dst.n_lowrank > 0
+    m = DenseModel(dst)
+    w, zs, zcap, zbr, tab = dst._freq_tables(float(board.freqs[0]))
+    x = m.to_dense(z["prod_x"])
+    assert rel(m.to_compact(m.matvec(x, w, zs, zcap, zbr)), z["prod_matvec"]) < 1e-12
+    base = Multifrontal(dst, dst.sterm @ tab[: st.n_table])
+    assert rel(m.to_compact(m.precond(x, tab, LowRank(m, base, zbr))), z["prod_precond"]) < 1e-9
+    assert rel(m.to_compact(m.precond(x, tab, base)), z["prod_precond"]) > 1e-3     # the update matters
