@@ -22,7 +22,7 @@
 """
 from __future__ import annotations
 
-from dataclasses import dataclass
+from dataclasses import dataclass, replace
 
 import numpy as np
 import scipy.sparse as sp
@@ -149,6 +149,27 @@ def topology(node_masks, xb_masks, yb_masks, d: float, pairs: list, branch_nodes
                    np.array(cmask, bool).reshape(-1, nx, ny), ab, a_nodes, b_nodes, cond_label, full_label, keep,
                    sheet_layer)
     return top, kept
+
+
+def add_branches(t: Topology, ab: np.ndarray) -> Topology:
+    """t with more branches between node ids ab (k, 2) inside its pieces of copper (a derived stack,
+    PlaneStack.with_branches, peec.py:1871-1912): the same strips, capacitances, nodes and reference nodes, the
+    branches' ends appended to the incidence lists and the conductor components merged, numbered as topology()
+    numbers them (connected_components: by each component's lowest node).  What topology() would give for the
+    whole branch list, without redoing the grid's work."""
+    ab = np.asarray(ab, np.int64).reshape(-1, 2)
+    if np.any(t.full_label[ab[:, 0]] != t.full_label[ab[:, 1]]):
+        raise ValueError("a branch joins two pieces of copper: the reference nodes change")
+    nc = int(t.cond_label.max()) + 1 if len(t.cond_label) else 0
+    g = sp.coo_matrix((np.ones(len(ab)), (t.cond_label[ab[:, 0]], t.cond_label[ab[:, 1]])), shape=(nc, nc))
+    _, merged = connected_components(g, directed=False)
+    lbl = merged[t.cond_label]
+    _, first = np.unique(lbl, return_index=True)
+    rank = np.empty(len(first), np.int64)
+    rank[np.argsort(first)] = np.arange(len(first))
+    return replace(t, branch_ab=np.concatenate([t.branch_ab, ab]),
+                   a_nodes=np.concatenate([t.a_nodes, ab[:, 0]]), b_nodes=np.concatenate([t.b_nodes, ab[:, 1]]),
+                   cond_label=rank[lbl].astype(t.cond_label.dtype))
 
 
 @dataclass

@@ -708,12 +708,7 @@ class PlaneStack:
         if np.any(self.full_label[a] != self.full_label[b]) or len(branches) - root.nbr > LOWRANK_MAX:
             return PlaneStack(self.layers, branches, self.pairs, self.sigma, self.precond_mode, self.screen,
                               leaf=self.leaf, _device=self._device if device is None else bool(device))
-        t, kept = layout.topology([l.grid.node for l in root.layers], [l.grid.xb for l in root.layers],
-                                  [l.grid.yb for l in root.layers], root.d,
-                                  [(p.upper, p.lower, p.c_per_area, p.tan_delta) for p in root.pairs],
-                                  [(br.a, br.b) for br in branches], root.twin_parent)
-        if len(kept) != len(branches) or not np.array_equal(t.keep, root.keep):
-            raise RuntimeError("a derived stack must keep its base's nodes")
+        t = layout.add_branches(root.top, [(self.node_id(br.a), self.node_id(br.b)) for br in branches[root.nbr:]])
         # a shallow copy shares the grids, spectra, symbolic analysis and S-term map (which covers the base's
         # branches only); the branch list, numbering of the unknowns and the caches are its own
         new = copy.copy(root)
@@ -725,6 +720,7 @@ class PlaneStack:
         new.n_table = root.tab_br0 + t.nbr
         new.n_lowrank = t.nbr - root.nbr
         new._base = root
+        new._moment_w = None
         new._lock = threading.Lock()
         new._ops = OrderedDict()
         new._device = root._device if device is None else bool(device) and root._device
@@ -1041,29 +1037,38 @@ class PlaneStack:
         k, i, j = node
         return np.array([i * self.d, j * self.d, self.zs[k]])
 
-    def moment(self, segments: np.ndarray, Ib: np.ndarray) -> np.ndarray:
-        """m = 1/2 sum r x I dl over the closed loop (peec.py:2668-2700)."""
-        m = np.zeros(3, complex)
-        for s in segments:
-            m += 0.5 * s[7] * np.cross(s[0:3], s[3:6])
+    def moment_weights(self) -> np.ndarray:
+        """(3, nb): the plane's part of the moment as a linear map of the branch currents, m = W Ib (peec.py:
+        2680-2700: each strip's 1/2 r x dl at its sheet's height, each capacitance's and lumped branch's)."""
+        W = getattr(self, "_moment_w", None)
+        if W is not None and W.shape[1] == self.nb:
+            return W
         d = self.d
-        Ix, Iy = Ib[: self.nxb], Ib[self.nxb: self.ns]
+        W = np.zeros((3, self.nb))
         k, _, j = self.xa.T                         # each strip at its sheet's height
-        m[1] += 0.5 * np.sum(self.sheet_z[k] * d * Ix)
-        m[2] += 0.5 * np.sum(-(j * d) * d * Ix)
+        W[1, : self.nxb] = 0.5 * self.sheet_z[k] * d
+        W[2, : self.nxb] = -0.5 * (j * d) * d
         k, i, _ = self.ya.T
-        m[0] += 0.5 * np.sum(-self.sheet_z[k] * d * Iy)
-        m[2] += 0.5 * np.sum((i * d) * d * Iy)
-        I_cap = Ib[self.ns: self.ns + self.ncap]
-        if len(I_cap):
+        W[0, self.nxb: self.ns] = -0.5 * self.sheet_z[k] * d
+        W[2, self.nxb: self.ns] = 0.5 * (i * d) * d
+        if self.ncap:
             cu = self.top.cap[:, :4].astype(int)
             x, y = cu[:, 2] * d, cu[:, 3] * d
             dz = self.zs[cu[:, 1]] - self.zs[cu[:, 0]]
-            m[0] += 0.5 * np.sum(y * dz * I_cap)
-            m[1] += 0.5 * np.sum(-x * dz * I_cap)
-        for b, cur in zip(self.branches, Ib[self.ns + self.ncap:]):
-            m += 0.5 * np.cross(self.pos(b.a), self.pos(b.b)) * cur
-        return m
+            W[0, self.ns: self.ns + self.ncap] = 0.5 * y * dz
+            W[1, self.ns: self.ns + self.ncap] = -0.5 * x * dz
+        for n, b in enumerate(self.branches):
+            W[:, self.ns + self.ncap + n] = 0.5 * np.cross(self.pos(b.a), self.pos(b.b))
+        self._moment_w = W
+        return W
+
+    def moment(self, segments: np.ndarray, Ib: np.ndarray) -> np.ndarray:
+        """m = 1/2 sum r x I dl over the closed loop (peec.py:2668-2700): the trace's segments, then the plane's
+        part (moment_weights)."""
+        m = np.zeros(3, complex)
+        for s in segments:
+            m += 0.5 * s[7] * np.cross(s[0:3], s[3:6])
+        return m + self.moment_weights() @ Ib
 
 
 class RouteExcitation:
@@ -1072,9 +1077,11 @@ class RouteExcitation:
 
     def __init__(self, stack: PlaneStack, trace: list, inject_driver=None, inject_receiver=None,
                  trace_thickness: float = 35e-6, strip_psi: Optional[np.ndarray] = None,
-                 branch_psi: Optional[np.ndarray] = None, injections: Optional[list] = None):
+                 branch_psi: Optional[np.ndarray] = None, injections: Optional[list] = None,
+                 _L_trace: Optional[float] = None):
         """strip_psi / branch_psi: the coupling of the same loop computed on another stack with the same strips
-        (a derived stack: RouteExcitation.on), reused; branches beyond branch_psi are coupled here."""
+        (a derived stack: RouteExcitation.on), reused; branches beyond branch_psi are coupled here.  _L_trace:
+        the trace's own inductance, when already known for the same trace."""
         self.stack = stack
         self.trace = trace
         self.trace_t = trace_thickness
@@ -1110,12 +1117,16 @@ class RouteExcitation:
             bp = np.concatenate([bp, stack.branch_coupling(self.segments, start=len(bp))])
         self.branch_psi = bp[: stack.nbr]
         self.psi = np.concatenate([self.strip_psi, np.zeros(stack.ncap), self.branch_psi])
-        self.L_trace = greens.trace_self(self.segments, trace_thickness) if len(trace) else 0.0
+        if _L_trace is not None:
+            self.L_trace = _L_trace
+        else:
+            self.L_trace = greens.trace_self(self.segments, trace_thickness) if len(trace) else 0.0
 
     def on(self, stack: PlaneStack) -> "RouteExcitation":
-        """The same loop on a derived stack (with_branches), its strip coupling reused (peec.py:2771-2774)."""
+        """The same loop on a derived stack (with_branches), its strip coupling and the trace's own inductance
+        reused (peec.py:2771-2774)."""
         return RouteExcitation(stack, self.trace, *self.inject, self.trace_t, self.strip_psi, self.branch_psi,
-                               self.extra)
+                               self.extra, _L_trace=self.L_trace)
 
     def J(self) -> np.ndarray:
         J = np.zeros(self.stack.n_nodes)

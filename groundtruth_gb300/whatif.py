@@ -58,6 +58,14 @@ def _column(sol: gs.Solution) -> EditColumn:
     return EditColumn(sol.f, sol.Z_loop, sol.m, sol.residual, sol.iterations, lambda: sol)
 
 
+def _real_times(A: np.ndarray, X: np.ndarray) -> np.ndarray:
+    """A (m, n) real times each row of X (k, n) complex, as (m, k), without casting A to complex: the rows'
+    real and imaginary parts are read in place (X's last axis contiguous)."""
+    Xv = X.view(np.float64).reshape(X.shape[0], X.shape[1], 2)
+    P = A @ Xv                                                       # (k, m, 2)
+    return (P[..., 0] + 1j * P[..., 1]).T
+
+
 @dataclass
 class EditResult:
     solutions: dict                     # (net, frequency) -> EditColumn
@@ -133,6 +141,8 @@ class WhatIf:
         self.base_bnorm = {(k, f): float(np.linalg.norm(st.rhs_vector(self.routes[k].rhs_top(f), self.routes[k].J())))
                            for k, f in cols}
         self.base_psi_ib = {(k, f): complex(np.dot(self.routes[k].psi, x[: st.nb])) for (k, f), x in zip(cols, xs)}
+        self.base_r_trace = {(k, f): float(greens.trace_resistance(self.routes[k].segments, f, st.sigma,
+                                                                   self.routes[k].trace_t)) for k, f in cols}
         return time.perf_counter() - t0
 
     def evaluate(self, branches: list, nets, freqs, remove=()) -> EditResult:
@@ -184,25 +194,28 @@ class WhatIf:
         def at(v, idx):                        # rows of v at kept indices idx, zero where a node is not kept
             return np.where((idx >= 0).reshape((-1,) + (1,) * (v.ndim - 1)), v[np.maximum(idx, 0)], 0.0)
 
+        # the real maps applied to the border solutions: the base's moment weights and the nets' couplings
+        A = np.concatenate([st.moment_weights(), np.stack([self.routes[net].psi for net in nets])])
         cols_out, redo_cols, redo_x0 = {}, [], []
         for f in freqs:
             w = 2 * math.pi * f
-            X = np.stack([XF[(f, j)] for j in range(k)], axis=1)         # (nb + n_keep, k)
-            XI, VF = X[:nb], X[nb:]
-            Sigma = np.diag([complex(b.z(f)) for b in extra]) + at(VF, ka) - at(VF, kb)
+            X = np.stack([XF[(f, j)] for j in range(k)])                  # (k, nb + n_keep), rows contiguous
+            XI, VF = X[:, :nb], X[:, nb:]
+            Sigma = np.diag([complex(b.z(f)) for b in extra]) + at(VF.T, ka) - at(VF.T, kb)
             rFf = np.array([rF[(f, j)] for j in range(k)])
-            MX = np.stack([st.moment(np.zeros((0, 8)), XI[:, j]) for j in range(k)], axis=1)   # (3, k)
-            for net in nets:
+            AX = _real_times(A, XI)
+            MX, PX = AX[:3], AX[3:]                                       # (3, k) moments, (nets, k) psi . I
+            for q, net in enumerate(nets):
                 c = (net, f)
-                base, xb, r0 = self.base[c], self.base_x[c], self.routes[net]
+                base, xb = self.base[c], self.base_x[c]
                 r = droutes[net]
                 psi_new = r.psi[nb: nb + k]
                 b_new = -1j * w * psi_new
                 Vb = xb[nb:]
                 i_new = np.linalg.solve(Sigma, b_new + at(Vb, ka) - at(Vb, kb))
-                psi_ib = self.base_psi_ib[c] - (r0.psi @ XI) @ i_new + psi_new @ i_new
-                v_inj = sum(a * (at(Vb, kept[[n]])[0] - at(VF, kept[[n]])[0] @ i_new) for n, a in r.injections)
-                Z = complex(greens.trace_resistance(r.segments, f, st.sigma, r.trace_t) + v_inj
+                psi_ib = self.base_psi_ib[c] - PX[q] @ i_new + psi_new @ i_new
+                v_inj = sum(a * (at(Vb, kept[[n]])[0] - at(VF.T, kept[[n]])[0] @ i_new) for n, a in r.injections)
+                Z = complex(self.base_r_trace[c] + v_inj
                             + 1j * w * (r.L_trace + psi_ib))
                 m = base.m - MX @ i_new + arm.T @ i_new
                 bb = self.base_bnorm[c]
@@ -210,12 +223,12 @@ class WhatIf:
 
                 def make(f=f, r=r, xb=xb, XI=XI, VF=VF, i_new=i_new, bound=bound):
                     V = np.zeros(n_nodes, complex)
-                    V[st.keep] = xb[nb:] - VF @ i_new
-                    return r.solution(f, np.concatenate([xb[:nb] - XI @ i_new, i_new]), V, 0, bound)
+                    V[st.keep] = xb[nb:] - i_new @ VF
+                    return r.solution(f, np.concatenate([xb[:nb] - i_new @ XI, i_new]), V, 0, bound)
                 cols_out[c] = EditColumn(f, Z, m, bound, 0, make)
                 if not bound <= self.tol:
                     redo_cols.append(c)
-                    redo_x0.append(np.concatenate([xb[:nb] - XI @ i_new, i_new, Vb - VF @ i_new]))
+                    redo_x0.append(np.concatenate([xb[:nb] - i_new @ XI, i_new, Vb - i_new @ VF]))
         t3 = time.perf_counter()
         if redo_cols:
             # columns whose bound misses the tolerance: the derived stack, from the composed solution

@@ -301,3 +301,43 @@ def test_factorisations_are_admitted_against_free_memory(monkeypatch):
     with pytest.raises(MemoryError):
         st._admit(4)
     assert not st._ops                              # dropped before giving up
+
+
+@pytest.mark.parametrize("name", ["small_pair", "capacitance_only", "faces_stack3", "six_sheet"])
+def test_added_branches_number_like_a_whole_topology(name):
+    """layout.add_branches (a derived stack's numbering without redoing the grid's work) gives exactly what
+    layout.topology gives for the whole branch list: incidence ends, conductor components (merged and numbered
+    by their lowest node, as connected_components numbers them), copper components and reference nodes.
+    capacitance_only: the plane pair without its branches, its planes joined by capacitance alone, so a new via
+    merges two conductor components."""
+    from groundtruth_gb300 import layout
+    board = synth.small_pair() if name in ("small_pair", "capacitance_only") else getattr(synth, name)()
+    if name == "capacitance_only":
+        board.branches = []
+    st = host_stack(board)
+    t0 = st.top
+    coords = np.argwhere(t0.node)                        # node id -> (layer, i, j)
+    rng = np.random.default_rng(7)
+    merged = False
+    for trial in range(6):
+        ab = []
+        while len(ab) < 1 + trial % 4:
+            a, b = rng.integers(0, t0.n_nodes, 2)
+            if a != b and t0.full_label[a] == t0.full_label[b]:
+                ab.append((a, b))
+        ab = np.array(ab)
+        got = layout.add_branches(t0, ab)
+        whole, kept = layout.topology([l.grid.node for l in st.layers], [l.grid.xb for l in st.layers],
+                                      [l.grid.yb for l in st.layers], st.d,
+                                      [(p.upper, p.lower, p.c_per_area, p.tan_delta) for p in st.pairs],
+                                      [(br.a, br.b) for br in st.branches]
+                                      + [(tuple(coords[a]), tuple(coords[b])) for a, b in ab], st.twin_parent)
+        assert len(kept) == st.nbr + len(ab)
+        for k in ("branch_ab", "a_nodes", "b_nodes", "cond_label", "full_label", "keep", "nid", "xa", "ya", "cap"):
+            assert np.array_equal(getattr(got, k), getattr(whole, k)), (k, trial)
+        merged |= got.cond_label.max() < t0.cond_label.max()
+    assert merged == (name == "capacitance_only")
+    other = np.flatnonzero(t0.full_label != t0.full_label[0])
+    if len(other):                                       # a branch between two pieces of copper: a stack of its own
+        with pytest.raises(ValueError):
+            layout.add_branches(t0, [(0, other[0])])
