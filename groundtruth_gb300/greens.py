@@ -19,7 +19,6 @@ convolution; the reference uses scipy's next_fast_len, peec.py:1952-1953).
 """
 from __future__ import annotations
 
-import math
 from functools import lru_cache
 
 import numpy as np

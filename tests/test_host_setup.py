@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 import scipy.sparse as sp
 
-from groundtruth_gb300 import stack as gs, synth
+from groundtruth_gb300 import stack as gs
 from oracle import peec_oracle as po
 from test_oracle_golden import load, oracle_stack
 from host_model import DenseModel, Multifrontal

@@ -3,7 +3,6 @@
 These pins are what makes the oracle trustworthy as the GPU build's checker: the restated topology and
 index work must be bit-exact, the kernels, operators and products equal to FP64 rounding, and the solves
 equal to the GMRES tolerance."""
-import math
 from pathlib import Path
 
 import numpy as np
