@@ -2,9 +2,12 @@
 that need no polygon library): how much copper crosses each cell border along scanlines, the copper area of each
 cell from its outline by Green's theorem, a strip's width and centre from those, copper of a border without a strip
 of its net moved to the nearest strip that has one, and the series factor of a narrow run whose width changes
-along its length.  Polygons are given as their edges (outlines counter-clockwise, holes clockwise: ring_edges), in
+along its length; and the walk that claims tracks' cells and strips on a layer's grid (peec.py:893-983).  Polygons are given as their edges (outlines counter-clockwise, holes clockwise: ring_edges), in
 the same length unit as the pitch."""
 from __future__ import annotations
+
+import math
+from typing import Optional
 
 import numpy as np
 
@@ -199,3 +202,94 @@ def series_factor(face, samples: list, has, axis: int) -> np.ndarray:
     out = np.ones(h.shape)
     out[h] = factor[key]
     return out if axis == 1 else out.T
+
+
+TRACK_SAMPLE = 0.4   # peec.py:939: a centreline is sampled every 0.4 pitch, so that no cell is skipped
+
+
+def _nearest_cells(u: float, v: float) -> list:
+    """The four cells around grid point (u, v) (pitch units), nearest first; ties keep the order (i0, j0),
+    (i0, j0 + 1), (i0 + 1, j0), (i0 + 1, j0 + 1)."""
+    i0, j0 = math.floor(u), math.floor(v)
+    four = [(i0, j0), (i0, j0 + 1), (i0 + 1, j0), (i0 + 1, j0 + 1)]
+    return sorted(four, key=lambda c: (c[0] - u) ** 2 + (c[1] - v) ** 2)
+
+
+def _l_path(a: tuple, b: tuple, blocked) -> list:
+    """The 4-connected cells from a (excluded) to b (included) along an L: along i first or along j first,
+    whichever crosses fewer blocked cells (along i on a tie)."""
+    di, dj = b[0] - a[0], b[1] - a[1]
+    si, sj = (di > 0) - (di < 0), (dj > 0) - (dj < 0)
+    leg_i = [(a[0] + si * n, a[1]) for n in range(1, abs(di) + 1)]
+    leg_j = [(a[0], a[1] + sj * n) for n in range(1, abs(dj) + 1)]
+    i_first = leg_i + [(b[0], c[1]) for c in leg_j]
+    j_first = leg_j + [(c[0], b[1]) for c in leg_i]
+    cost = [sum(1 for c in p if blocked(c)) for p in (i_first, j_first)]
+    return i_first if cost[0] <= cost[1] else j_first
+
+
+def rasterise_tracks(k: int, polylines, x0: float, y0: float, d: float, label: np.ndarray, seeded: np.ndarray,
+                     forced_x: np.ndarray, forced_y: np.ndarray, part: Optional[np.ndarray] = None,
+                     owners: Optional[list] = None) -> list:
+    """Tracks (polylines [(points (p, 2), width)], in the unit of x0, y0 and d) claimed on a layer's cell grid
+    for net k (GroundTruth's _rasterise_lines, peec.py:893-983); label (cells' nets, -1 free), seeded, forced_x /
+    forced_y (the widest claiming track's width per strip) and part are updated in place.
+
+    Each centreline is walked one sample every TRACK_SAMPLE pitch: at a sample the walk takes, of the four
+    cells around it (nearest first), the first that is already the track's own (net k's, and of the track's
+    piece of copper when `part` / `owners` give pieces), else the first that may be claimed (free or own), else
+    the nearest; a cell that differs from the last is reached along the L path through fewer cells that may not
+    be claimed.  Then, in walk order, free cells on the grid are claimed (and seeded); consecutive own cells one
+    step apart force their strip's width; an own cell reached across cells the track could not claim starts a
+    bridge from the last own cell: returned as (i0, j0, i1, j1, length along the track (at least d), width), a
+    lumped branch for the caller."""
+    nx, ny = label.shape
+    bridges = []
+    for n_line, (pts, width) in enumerate(polylines):
+        piece = owners[n_line] if owners is not None else None
+
+        def on_grid(c):
+            return 0 <= c[0] < nx and 0 <= c[1] < ny
+
+        def own(c):
+            return on_grid(c) and label[c] == k and (part is None or piece is None or part[c] == piece)
+
+        def claimable(c):
+            return on_grid(c) and (label[c] == -1 or own(c))
+
+        walk = []                                          # (i, j, distance along the centreline)
+        start = 0.0
+        for (ax, ay), (bx, by) in zip(pts, pts[1:]):
+            seg = math.hypot(bx - ax, by - ay)
+            for t in np.linspace(0.0, 1.0, max(int(math.ceil(seg / (TRACK_SAMPLE * d))), 1) + 1):
+                near = _nearest_cells((ax + t * (bx - ax) - x0) / d, (ay + t * (by - ay) - y0) / d)
+                cell = next((c for c in near if own(c)), None) or next((c for c in near if claimable(c)), near[0])
+                s = start + t * seg
+                if not walk:
+                    walk.append((cell[0], cell[1], s))
+                elif walk[-1][:2] != cell:
+                    walk.extend((c[0], c[1], s) for c in _l_path(walk[-1][:2], cell, lambda c: not claimable(c)))
+            start += seg
+        prev, last = None, None
+        for i, j, s in walk:
+            if not on_grid((i, j)):
+                prev = last = None
+                continue
+            if label[i, j] < 0:
+                label[i, j] = k
+                if part is not None and piece is not None:
+                    part[i, j] = piece
+                seeded[i, j] = True
+            if not own((i, j)):
+                prev = None
+                continue
+            if prev is not None:
+                tw = max(float(width), 1e-6)
+                if prev[1] == j and abs(prev[0] - i) == 1:
+                    forced_x[min(prev[0], i), j] = max(forced_x[min(prev[0], i), j], tw)
+                elif prev[0] == i and abs(prev[1] - j) == 1:
+                    forced_y[i, min(prev[1], j)] = max(forced_y[i, min(prev[1], j)], tw)
+            elif last is not None and last[:2] != (i, j):
+                bridges.append((last[0], last[1], i, j, max(s - last[2], d), float(width)))
+            prev, last = (i, j), (i, j, s)
+    return bridges

@@ -3,8 +3,9 @@
     python tests/golden/make_raster_golden.py --reference /path/to/GroundTruth
 
 Seeded polygons (as edge lists, groundtruth_gb300.raster.ring_edges) and arrays go through the reference's
-_line_cover, _cell_areas, _strip_widths, _adopt and _series_factor; inputs and outputs are stored in
-raster_functions.npz (shapely is stubbed: none of these functions calls it)."""
+_line_cover, _cell_areas, _strip_widths, _adopt and _series_factor, and seeded layers and polylines through its
+track walk _rasterise_lines; inputs and outputs are stored in raster_functions.npz (shapely is stubbed: none of
+these functions calls it)."""
 from __future__ import annotations
 
 import argparse
@@ -70,7 +71,39 @@ def main():
     for ax in (0, 1):
         out[f"sf_{ax}"] = peec._series_factor(face, samples, has_s, ax)
     out.update(sf_face=face, sf_samples=np.stack(samples), sf_has=has_s)
+    out.update(track_cases(peec, rng))
     np.savez_compressed(HERE / "raster_functions.npz", **out)
+
+
+def track_cases(peec, rng) -> dict:
+    """Seeded layers (free cells, net 2's cells in two pieces, other nets' cells) with polylines partly off the
+    grid, through the reference's _rasterise_lines without and with pieces: inputs and every updated array."""
+    out = {}
+    nx, ny, d, x0, y0, k = 30, 24, 0.5, 1.0, 2.0, 2
+    lines = []
+    for n in range(6):
+        m = int(rng.integers(2, 6))
+        pts = np.stack([rng.uniform(x0 - 1.5, x0 + nx * d + 1.0, m), rng.uniform(y0 - 1.0, y0 + ny * d + 1.5, m)], 1)
+        lines.append((pts, 0.0 if n == 2 else float(rng.uniform(0.1, 0.6))))
+    out.update(tr_pts=np.concatenate([p for p, _ in lines]), tr_ptr=np.cumsum([0] + [len(p) for p, _ in lines]),
+               tr_width=np.array([w for _, w in lines]), tr_owners=np.array([n % 2 for n in range(len(lines))]))
+    for case, pieces in (("plain", False), ("pieces", True)):
+        r = rng.random((nx, ny))
+        label = np.where(r < 0.6, -1, np.where(r < 0.8, k, rng.integers(0, 2, (nx, ny)) * 2 - 1 + (r > 0.9) * 4))
+        label = np.where(label == k, k, np.where(label < 0, -1, label))
+        part = np.where(label == k, rng.integers(0, 2, (nx, ny)), -1) if pieces else None
+        seeded = np.zeros((nx, ny), bool)
+        fx, fy = np.zeros((nx - 1, ny)), np.zeros((nx, ny - 1))
+        out.update({f"tr_{case}_label0": label.copy()})
+        if pieces:
+            out[f"tr_{case}_part0"] = part.copy()
+        br = peec._rasterise_lines(k, lines, x0, y0, d, label, seeded, fx, fy, part,
+                                   [n % 2 for n in range(len(lines))] if pieces else None)
+        out.update({f"tr_{case}_label": label, f"tr_{case}_seeded": seeded, f"tr_{case}_fx": fx,
+                    f"tr_{case}_fy": fy, f"tr_{case}_bridges": np.array(br, float).reshape(-1, 6)})
+        if pieces:
+            out[f"tr_{case}_part"] = part
+    return out
 
 
 if __name__ == "__main__":

@@ -61,3 +61,47 @@ def test_exact_widths_of_a_slanted_slot():
     b = synth.Board("exact", d, n, n, [layer, pwr], [synth.Pair(0, 1, 7.6e-8, 0.02)], [], [], np.array([1e8]))
     st, _ = gs.from_board(b, _device=False)
     assert st.dL is not None and np.count_nonzero(st.dL) == narrow(st.strip_width)
+
+
+def _lines():
+    ptr = Z["tr_ptr"]
+    return [(Z["tr_pts"][a:b], float(w)) for a, b, w in zip(ptr[:-1], ptr[1:], Z["tr_width"])]
+
+
+def test_track_walk_matches_reference():
+    """raster.rasterise_tracks against the reference's _rasterise_lines on seeded layers (free cells, the net's
+    own cells, other nets' cells) with polylines running off the grid, without and with pieces of copper: the
+    claimed labels, seeded cells, forced strip widths, pieces and bridges, bit for bit."""
+    lines = _lines()
+    for case in ("plain", "pieces"):
+        label = Z[f"tr_{case}_label0"].copy()
+        nx, ny = label.shape
+        seeded = np.zeros((nx, ny), bool)
+        fx, fy = np.zeros((nx - 1, ny)), np.zeros((nx, ny - 1))
+        part = Z[f"tr_{case}_part0"].copy() if case == "pieces" else None
+        owners = list(Z["tr_owners"]) if case == "pieces" else None
+        br = raster.rasterise_tracks(2, lines, 1.0, 2.0, 0.5, label, seeded, fx, fy, part, owners)
+        assert np.array_equal(label, Z[f"tr_{case}_label"])
+        assert np.array_equal(seeded, Z[f"tr_{case}_seeded"])
+        assert np.array_equal(fx, Z[f"tr_{case}_fx"]) and np.array_equal(fy, Z[f"tr_{case}_fy"])
+        assert np.array_equal(np.array(br, float).reshape(-1, 6), Z[f"tr_{case}_bridges"])
+        if part is not None:
+            assert np.array_equal(part, Z[f"tr_{case}_part"])
+
+
+def test_a_straight_track_on_free_cells_claims_one_row():
+    """A track along a row of free cells claims that row, forces its x strips to the track's width and needs
+    no bridge; a foreign cell in its way is walked around (the L path through fewer foreign cells)."""
+    label = -np.ones((12, 7), np.int64)
+    seeded = np.zeros(label.shape, bool)
+    fx, fy = np.zeros((11, 7)), np.zeros((12, 6))
+    br = raster.rasterise_tracks(1, [(np.array([[1.0, 3.0], [9.0, 3.0]]), 0.3)], 0.0, 0.0, 1.0, label, seeded, fx, fy)
+    assert br == [] and np.array_equal(np.flatnonzero(label[:, 3] == 1), np.arange(1, 10))
+    assert (label == 1).sum() == 9 and np.all(fx[1:9, 3] == 0.3) and not fy.any()
+    label = -np.ones((12, 7), np.int64)
+    label[5, 3] = 0                                       # another net's cell on the centreline
+    seeded[:] = False
+    fx[:], fy[:] = 0, 0
+    br = raster.rasterise_tracks(1, [(np.array([[1.0, 3.0], [9.0, 3.0]]), 0.3)], 0.0, 0.0, 1.0, label, seeded, fx, fy)
+    assert label[5, 3] == 0 and br == []                  # the walk stepped around it
+    assert (label == 1).sum() > 9 and fy.any()
