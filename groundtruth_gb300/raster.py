@@ -7,6 +7,7 @@ the same length unit as the pitch."""
 from __future__ import annotations
 
 import math
+from dataclasses import dataclass, field
 from typing import Optional
 
 import numpy as np
@@ -293,3 +294,289 @@ def rasterise_tracks(k: int, polylines, x0: float, y0: float, d: float, label: n
                 bridges.append((last[0], last[1], i, j, max(s - last[2], d), float(width)))
             prev, last = (i, j), (i, j, s)
     return bridges
+
+
+STRIP_SAMPLES = 6    # peec.py:107: lines across each strip's length where its copper's width is measured ...
+ADOPT_CELLS = 2      # peec.py:111: ... and how far a cell's copper without a node of its net goes to find one
+
+
+def _bounds(pa: np.ndarray, pb: np.ndarray) -> tuple:
+    lo = np.minimum(pa.min(axis=0), pb.min(axis=0))
+    hi = np.maximum(pa.max(axis=0), pb.max(axis=0))
+    return float(lo[0]), float(lo[1]), float(hi[0]), float(hi[1])
+
+
+def exact_copper(nets: list, label: np.ndarray, xb: np.ndarray, yb: np.ndarray, x0: float, y0: float,
+                 d: float) -> tuple:
+    """Strip widths and node areas measured on the copper itself (GroundTruth's _exact_copper, peec.py:708-771):
+    nets[k] = (pa, pb), net k's copper as oriented edges (ring_edges; None: no copper), label the cells' nets,
+    xb / yb the strips; returns (ex_x (nx-1, ny), ex_y (nx, ny-1), area (nx, ny), kx, ky): per strip the covered
+    length of the cell border it crosses over d (copper of its net on a border line where the net has no strip
+    adopted by the nearest strip within ADOPT_FACES), per node its cell's copper of its net over d^2 (adopted
+    within ADOPT_CELLS), and per strip of a lone narrow band the series factor of its width measured at
+    STRIP_SAMPLES lines along it (1 elsewhere).  Each net is worked in a window of cells around its copper."""
+    nx, ny = label.shape
+    ex_x, ex_y, area = np.zeros((nx - 1, ny)), np.zeros((nx, ny - 1)), np.zeros((nx, ny))
+    kx, ky = np.ones((nx - 1, ny)), np.ones((nx, ny - 1))
+    along_rows, along_cols = ((0, 1), (0, -1)), ((1, 0), (-1, 0))
+    q = STRIP_SAMPLES
+    for k, edges in enumerate(nets):
+        if edges is None or len(edges[0]) == 0:
+            continue
+        pa, pb = edges
+        bx0, by0, bx1, by1 = _bounds(pa, pb)
+        i0, i1 = max(int(math.floor((bx0 - x0) / d)) - 2, 0), min(int(math.ceil((bx1 - x0) / d)) + 3, nx)
+        j0, j1 = max(int(math.floor((by0 - y0) / d)) - 2, 0), min(int(math.ceil((by1 - y0) / d)) + 3, ny)
+        wi, wj = i1 - i0, j1 - j0
+        if wi < 2 or wj < 2:
+            continue
+        xa, ya, xe, ye = pa[:, 0], pa[:, 1], pb[:, 0], pb[:, 1]
+        # vertical borders x = x_i - d/2 (line m: the left border of window column m) and horizontal ones
+        # y = y_j + d/2 between window rows: the copper each cell's stretch of them holds
+        vert = line_cover(xa, ya, xe, ye, x0 + (i0 - 0.5) * d, d, wi + 1, y0 + j0 * d, d, wj)
+        horiz = line_cover(ya, xa, ye, xe, y0 + (j0 + 0.5) * d, d, wj - 1, x0 + i0 * d, d, wi).T
+        mine = label[i0:i1, j0:j1] == k
+        sx = xb[i0:i1 - 1, j0:j1] & mine[:-1, :]
+        sy = yb[i0:i1, j0:j1 - 1] & mine[:, :-1]
+        fx = adopt(vert[1:wi, :] / d, sx, along_rows, ADOPT_FACES)
+        fy = adopt(horiz / d, sy, along_cols, ADOPT_FACES)
+        ex_x[i0:i1 - 1, j0:j1] += fx
+        ex_y[i0:i1, j0:j1 - 1] += fy
+        # the width along each strip: q lines across its length at x_i + (p + 1/2) d / q
+        cut_x = (line_cover(xa, ya, xe, ye, x0 + (i0 + 0.5 / q) * d, d / q, (wi - 1) * q, y0 + j0 * d, d, wj)
+                 / d).reshape(wi - 1, q, wj)
+        cut_y = (line_cover(ya, xa, ye, xe, y0 + (j0 + 0.5 / q) * d, d / q, (wj - 1) * q, x0 + i0 * d, d, wi)
+                 / d).reshape(wj - 1, q, wi)
+        samples_x = [adopt(cut_x[:, p, :], sx, along_rows, ADOPT_FACES) for p in range(q)]
+        samples_y = [adopt(cut_y[:, p, :].T, sy, along_cols, ADOPT_FACES) for p in range(q)]
+        kx[i0:i1 - 1, j0:j1][sx] = series_factor(fx, samples_x, sx, 1)[sx]
+        ky[i0:i1, j0:j1 - 1][sy] = series_factor(fy, samples_y, sy, 0)[sy]
+        cells = cell_areas(pa, pb, x0 + (i0 - 0.5) * d, y0 + (j0 - 0.5) * d, d, wi, wj, vert[1:wi + 1, :]) / (d * d)
+        area[i0:i1, j0:j1] += adopt(np.clip(cells, 0.0, 1.0), mine, along_cols + along_rows, ADOPT_CELLS)
+    return ex_x, ex_y, area, kx, ky
+
+
+def coarse_from_fine(nets: list, x0: float, y0: float, d: float, nx: int, ny: int, s: int) -> tuple:
+    """Cells, their nets and the copper joining neighbours from a sub-grid of pitch d / s (GroundTruth's
+    _coarse_from_fine, peec.py:774-849).  nets[k] = (outline, holes) polygons of net k (None: none), points of
+    the sub-grid inside them (strictly, holes closed: synth.copper_at) take the first net that holds them.
+    Returns (label (nx, ny): each cell's net, its largest piece of one net's sub-grid copper inside the cell when
+    that spans at least s sub-grid points, else -1; cross_x (nx-1, ny) / cross_y (nx, ny-1): the fraction of
+    the s sub-grid strips across the border two cells' kept pieces join by; fill (nx, ny): the kept piece's share
+    of the cell; off_x / off_y: the crossing strips' mean position along the border from its middle, over d)."""
+    from scipy.sparse.csgraph import connected_components
+    import scipy.sparse as sp
+    from .synth import copper_at
+    df = d / s
+    mx, my = nx * s, ny * s
+    xf = x0 - d / 2 + (np.arange(mx) + 0.5) * df
+    yf = y0 - d / 2 + (np.arange(my) + 0.5) * df
+    fine = -np.ones((mx, my), np.int32)
+    for k, poly in enumerate(nets):
+        if poly is None:
+            continue
+        outline, holes = np.asarray(poly[0], float), [np.asarray(h, float) for h in poly[1]]
+        bx0, by0 = outline.min(axis=0)
+        bx1, by1 = outline.max(axis=0)
+        p0, p1 = max(int(math.floor((bx0 - xf[0]) / df)) - 1, 0), min(int(math.ceil((bx1 - xf[0]) / df)) + 2, mx)
+        q0, q1 = max(int(math.floor((by0 - yf[0]) / df)) - 1, 0), min(int(math.ceil((by1 - yf[0]) / df)) + 2, my)
+        if p0 >= p1 or q0 >= q1:
+            continue
+        X, Y = np.meshgrid(xf[p0:p1], yf[q0:q1], indexing="ij")
+        win = fine[p0:p1, q0:q1]
+        win[copper_at(X, Y, outline, holes) & (win < 0)] = k
+    same_x = (fine[:-1, :] >= 0) & (fine[:-1, :] == fine[1:, :])         # sub-grid strips within one net
+    same_y = (fine[:, :-1] >= 0) & (fine[:, :-1] == fine[:, 1:])
+    border_x = ((np.arange(mx - 1) + 1) % s == 0)[:, None]                # ... that cross a cell border
+    border_y = ((np.arange(my - 1) + 1) % s == 0)[None, :]
+    n = mx * my
+    at = np.arange(n).reshape(mx, my)
+    inner_x, inner_y = same_x & ~border_x, same_y & ~border_y           # the cells' pieces: strips inside cells
+    a = np.concatenate([at[:-1, :][inner_x], at[:, :-1][inner_y]])
+    b = np.concatenate([at[1:, :][inner_x], at[:, 1:][inner_y]])
+    _, piece = connected_components(sp.coo_matrix((np.ones(len(a), np.int8), (a, b)), shape=(n, n)), directed=False)
+    piece = piece.reshape(mx, my)
+    cell_of = (np.arange(mx) // s)[:, None] * ny + (np.arange(my) // s)[None, :]
+    cu = fine >= 0
+    pid = piece[cu]
+    size = np.bincount(pid, minlength=n)
+    p_cell, p_net = np.full(n, -1), np.full(n, -1)
+    p_cell[pid] = cell_of[cu]
+    p_net[pid] = fine[cu]
+    pieces = np.unique(pid)
+    pieces = pieces[np.lexsort((-size[pieces], p_cell[pieces]))]           # per cell, the largest piece first
+    lead = np.ones(len(pieces), bool)
+    lead[1:] = p_cell[pieces[1:]] != p_cell[pieces[:-1]]
+    kept = pieces[lead]
+    kept = kept[size[kept] >= s]
+    label = -np.ones(nx * ny, int)
+    label[p_cell[kept]] = p_net[kept]
+    fill = np.zeros(nx * ny)
+    fill[p_cell[kept]] = size[kept] / (s * s)
+    is_kept = np.zeros(n, bool)
+    is_kept[kept] = True
+    on = cu & is_kept[piece]
+    cross_x, off_x = np.zeros((nx - 1, ny)), np.zeros((nx - 1, ny))
+    fi, fj = np.nonzero(same_x & border_x & on[:-1, :] & on[1:, :])
+    np.add.at(cross_x, (fi // s, fj // s), 1.0 / s)
+    np.add.at(off_x, (fi // s, fj // s), ((fj % s + 0.5) / s - 0.5) / s)
+    cross_y, off_y = np.zeros((nx, ny - 1)), np.zeros((nx, ny - 1))
+    fi, fj = np.nonzero(same_y & border_y & on[:, :-1] & on[:, 1:])
+    np.add.at(cross_y, (fi // s, fj // s), 1.0 / s)
+    np.add.at(off_y, (fi // s, fj // s), ((fi % s + 0.5) / s - 0.5) / s)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        off_x = np.where(cross_x > 0, off_x / cross_x, 0.0)
+        off_y = np.where(cross_y > 0, off_y / cross_y, 0.0)
+    return label.reshape(nx, ny), cross_x, cross_y, fill.reshape(nx, ny), off_x, off_y
+
+
+def _covers(px, py, poly) -> np.ndarray:
+    """Points inside a polygon (outline, holes) or on its border (shapely's covers)."""
+    from .synth import polygon_contains
+    ins, on = polygon_contains(px, py, np.asarray(poly[0], float))
+    out = ins | on
+    for h in poly[1]:
+        hin, _ = polygon_contains(px, py, np.asarray(h, float))
+        out &= ~hin
+    return out
+
+
+def _inside(X, Y, pieces: list) -> np.ndarray:
+    """Points strictly inside any of the pieces (outline minus closed holes)."""
+    from .synth import copper_at
+    out = np.zeros(np.shape(X), bool)
+    for outline, holes in pieces:
+        out |= copper_at(X, Y, np.asarray(outline, float), [np.asarray(h, float) for h in holes])
+    return out
+
+
+@dataclass
+class LayerRaster:
+    """One layer's copper on a grid of pitch d (GroundTruth's Grid, peec.py:197-223, without the heat points):
+    nodes, strips, each node's net (label, -1: none), the cells' copper fraction (sub-grid only), the tracks'
+    bridges, and with a sub-grid the strips' widths, offsets and resistance widths and the nodes' areas."""
+    x0: float
+    y0: float
+    d: float
+    nx: int
+    ny: int
+    node: np.ndarray
+    xb: np.ndarray
+    yb: np.ndarray
+    label: np.ndarray
+    nets: list
+    fill: Optional[np.ndarray] = None
+    bridges: list = field(default_factory=list)
+    wx: Optional[np.ndarray] = None
+    wy: Optional[np.ndarray] = None
+    ox: Optional[np.ndarray] = None
+    oy: Optional[np.ndarray] = None
+    area: Optional[np.ndarray] = None
+    rx: Optional[np.ndarray] = None
+    ry: Optional[np.ndarray] = None
+
+    def widths(self) -> Optional[dict]:
+        """The strip widths as the solver's Grid takes them (None: every strip full)."""
+        if self.wx is None:
+            return None
+        return {"wx": self.wx, "wy": self.wy, "ox": self.ox, "oy": self.oy, "rx": self.rx, "ry": self.ry}
+
+
+def build_layer(nets: dict, bbox: tuple, d: float, seeds: Optional[dict] = None, lines: Optional[dict] = None,
+                sub: int = 1) -> LayerRaster:
+    """A layer's copper on a grid of pitch d over bbox (x0, y0, x1, y1) (GroundTruth's build_grid,
+    peec.py:329-449, heat points left out).  nets {net: [piece (outline, holes), ...]}: each net's copper as its
+    connected pieces (polygons, in the unit of d); seeds {net: [(x, y)]}: points whose nearest free node becomes
+    the net's (a via ring or pad smaller than the grid); lines {net: [(polyline, width)]}: tracks claimed by
+    rasterise_tracks.  sub = 1: a node is a net's when its point lies inside the net's copper (the first net
+    keeps it), a strip when its midpoint does too; sub > 1: cells, joins and offsets from the sub-grid
+    (coarse_from_fine, pieces kept apart), then the widths and areas from the copper itself (exact_copper,
+    strip_widths; the resistance width times the series factor).  A strip joins two nodes of one net and one
+    piece whose midpoint is that net's copper, or either of which is seeded, or that a track forces."""
+    x0, y0, x1, y1 = bbox
+    nx = max(int(math.ceil((x1 - x0) / d)) + 1, 3)
+    ny = max(int(math.ceil((y1 - y0) / d)) + 1, 3)
+    names = list(nets)
+    per_net = [list(nets[n]) for n in names]
+    fine = sub > 1
+    pieces = [(k, p) for k, ps in enumerate(per_net) for p in ps] if fine else []
+    fill = None
+    if fine:
+        part, cross_x, cross_y, fill, off_x, off_y = coarse_from_fine([p for _, p in pieces], x0, y0, d, nx, ny, sub)
+        label = np.array([k for k, _ in pieces] + [-1], int)[part]
+        mids_x = np.where(cross_x > 0, label[:-1, :], -1)
+        mids_y = np.where(cross_y > 0, label[:, :-1], -1)
+    else:
+        label = -np.ones((nx, ny), int)
+        mids_x, mids_y = np.full((nx - 1, ny), -1), np.full((nx, ny - 1), -1)
+        part = None
+        xs, ys = x0 + np.arange(nx) * d, y0 + np.arange(ny) * d
+        for k, ps in enumerate(per_net):
+            if not ps:
+                continue
+            lo = np.min([np.min(np.asarray(o, float), axis=0) for o, _ in ps], axis=0)
+            hi = np.max([np.max(np.asarray(o, float), axis=0) for o, _ in ps], axis=0)
+            i0, i1 = max(int(math.floor((lo[0] - x0) / d)) - 1, 0), min(int(math.ceil((hi[0] - x0) / d)) + 2, nx)
+            j0, j1 = max(int(math.floor((lo[1] - y0) / d)) - 1, 0), min(int(math.ceil((hi[1] - y0) / d)) + 2, ny)
+            if i0 >= i1 or j0 >= j1:
+                continue
+            X, Y = np.meshgrid(xs[i0:i1], ys[j0:j1], indexing="ij")
+            win = label[i0:i1, j0:j1]
+            win[_inside(X, Y, ps) & (win < 0)] = k
+            mx = mids_x[i0:min(i1, nx - 1), j0:j1]
+            mx[_inside(X[: mx.shape[0]] + d / 2, Y[: mx.shape[0]], ps) & (mx < 0)] = k
+            my = mids_y[i0:i1, j0:min(j1, ny - 1)]
+            my[_inside(X[:, : my.shape[1]], Y[:, : my.shape[1]] + d / 2, ps) & (my < 0)] = k
+    if part is None:
+        part = label                      # no pieces: a net is its own piece (the same array)
+
+    def piece_at(k: int, px: float, py: float) -> int:
+        """The piece of net k holding (px, py) (inside or on its border), else a new piece of its own."""
+        if not pieces:
+            return k
+        for c, (net, poly) in enumerate(pieces):
+            if net == k and poly is not None and bool(_covers(np.array([px]), np.array([py]), poly)[0]):
+                return c
+        pieces.append((k, None))
+        return len(pieces) - 1
+
+    seeded = np.zeros((nx, ny), bool)
+    for net, points in (seeds or {}).items():
+        if net not in names:
+            continue
+        k = names.index(net)
+        for px, py in points:
+            i, j = int(round((px - x0) / d)), int(round((py - y0) / d))
+            if 0 <= i < nx and 0 <= j < ny and label[i, j] < 0:
+                label[i, j] = k
+                part[i, j] = piece_at(k, px, py)
+                seeded[i, j] = True
+    forced_x, forced_y = np.zeros((nx - 1, ny)), np.zeros((nx, ny - 1))
+    bridges = []
+    for net, polylines in (lines or {}).items():
+        if net not in names:
+            continue
+        k = names.index(net)
+        owners = None
+        if pieces:
+            owners = []
+            for pts, _ in polylines:
+                (ax, ay), (bx, by) = pts[0], pts[1] if len(pts) > 1 else pts[0]
+                owners.append(piece_at(k, (ax + bx) / 2, (ay + by) / 2))
+        bridges += rasterise_tracks(k, polylines, x0, y0, d, label, seeded, forced_x, forced_y, part, owners)
+    xb = (label[:-1, :] >= 0) & (label[:-1, :] == label[1:, :]) & (part[:-1, :] == part[1:, :]) & (
+        (mids_x == label[:-1, :]) | seeded[:-1, :] | seeded[1:, :] | (forced_x > 0))
+    yb = (label[:, :-1] >= 0) & (label[:, :-1] == label[:, 1:]) & (part[:, :-1] == part[:, 1:]) & (
+        (mids_y == label[:, :-1]) | seeded[:, :-1] | seeded[:, 1:] | (forced_y > 0))
+    out = LayerRaster(x0, y0, d, nx, ny, label >= 0, xb, yb, label, names, fill, bridges)
+    if fine:
+        edges = []
+        for ps in per_net:
+            rings = [ring_edges(o, h) for o, h in ps]
+            edges.append((np.concatenate([a for a, _ in rings]), np.concatenate([b for _, b in rings]))
+                         if rings else None)
+        ex_x, ex_y, area, kx, ky = exact_copper(edges, label, xb, yb, x0, y0, d)
+        out.wx, out.ox = strip_widths(xb, cross_x, off_x, forced_x, d, ex_x)
+        out.wy, out.oy = strip_widths(yb, cross_y, off_y, forced_y, d, ex_y)
+        out.area, out.rx, out.ry = area, out.wx * kx, out.wy * ky
+    return out

@@ -595,6 +595,39 @@ def necked_pair(seed: int = 17) -> Board:
     return b
 
 
+def routed_pair(sub: int = 4) -> Board:
+    """A plane pair rasterised from polygons by raster.build_layer (GroundTruth's build_grid) at sub-grid `sub`,
+    with the copper's exact widths: a GND pour (a slanted slot, a square hole, a notched corner with a pad in it
+    joined to the pour by a 0.25 mm corridor, its track's centreline forced) over a PWR plane with a cut-out;
+    0.5 mm pitch, 40 x 36 nodes, a decoupling part and a via, two nets crossing the slot.  The copper's ragged
+    edges give strips narrower than the pitch all around (wx / wy, ox / oy, rx / ry)."""
+    from . import raster
+    d_mm, t, h = 0.5, 35e-6, 0.2e-3
+    bbox = (0.0, 0.0, 19.5, 17.5)
+    pour = (np.array([[0.2, 0.3], [19.3, 0.3], [19.3, 17.2], [4.1, 17.2], [4.1, 13.6], [1.725, 13.6],
+                      [1.725, 15.1], [2.3, 15.1], [2.3, 16.4], [0.9, 16.4], [0.9, 15.1], [1.475, 15.1],
+                      [1.475, 13.6], [0.2, 13.6]]),
+            [rect_polygon(10.0, 8.6, 8.0, 0.6, math.radians(30.0)),
+             np.array([[14.3, 3.1], [15.6, 3.1], [15.6, 4.4], [14.3, 4.4]])])
+    gnd = raster.build_layer({"GND": [pour]}, bbox, d_mm,
+                             lines={"GND": [(np.array([[1.6, 15.7], [1.6, 13.0]]), 0.25)]}, sub=sub)
+    plane = (np.array([[0.1, 0.1], [19.4, 0.1], [19.4, 17.4], [0.1, 17.4]]),
+             [np.array([[5.2, 2.3], [7.9, 2.3], [7.9, 4.1], [5.2, 4.1]])])
+    pwr = raster.build_layer({"PWR": [plane]}, bbox, d_mm, sub=sub)
+    layers = [Layer("GND", 0.0, t, gnd.node, gnd.xb, gnd.yb, gnd.widths()),
+              Layer("PWR", -(h + t), t, pwr.node, pwr.xb, pwr.yb, pwr.widths())]
+    d = d_mm * 1e-3
+    pairs = [Pair(0, 1, EPS0 * 4.4 / h)]
+    branches = [BranchSpec((0, 30, 26), (1, 30, 26), 0.02, 0.5e-9, 100e-9, "part"),
+                BranchSpec((0, 8, 30), (1, 8, 30), 1e-3, 0.3e-9, 0.0, "via", 1.5e-4)]
+    nets = []
+    for (i0, j0), (i1, j1) in (((6, 5), (32, 12)), ((12, 24), (33, 6))):
+        pts = [(i0 * d, j0 * d), (i0 * d, j1 * d), (i1 * d, j1 * d)]
+        nets.append(Net(_segments(pts, 0.3e-3, 0.0, 0.2e-3), (0, i0, j0), (0, i1, j1)))
+    return Board("routed_pair", d, gnd.nx, gnd.ny, layers, pairs, branches, nets, np.array([1e6, 1e8, 1e9]),
+                 precond="sheet", tol=1e-10, restart=50)
+
+
 def what_if_base(n: int = 512, d_mm: float = 0.2, n_nets: int = 12, n_freq: int = 16, seed: int = 4,
                  slot: bool = True, n_decap: int = 8) -> Board:
     """The interactive what-if workload's base board: 4-layer Sig/GND/PWR/Sig at d_mm pitch, the GND/PWR pair

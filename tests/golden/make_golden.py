@@ -29,6 +29,8 @@ copper width, Solution.node_field).
 ``small_pair_derived.npz`` holds the same for small_pair plus a what-if edit's branches on a derived stack
 (PlaneStack.with_branches), including solves warm-started from the base's solutions.
 
+``routed_pair.npz``: the same records for a plane pair rasterised from polygons by this build's restatement of
+the reference's build_grid (raster.build_layer, sub-grid 4, exact widths; synth.routed_pair).
 ``known_answers.npz``: the reference's loop impedances and moments for the known-answer boards (the
 microstrip over a 40 x 20 mm plane with and without slots or an edge cut, the parallel-plate lines 20 and 40 mm
 long; ``synth.KNOWN_BOARDS``), solved to rtol 1e-10.
@@ -275,8 +277,13 @@ def main():
     ap.add_argument("--narrow-only", action="store_true", help="only the narrow-strip board's fixture")
     ap.add_argument("--faces-only", action="store_true", help="only the face-sheet boards' fixtures")
     ap.add_argument("--known-only", action="store_true", help="only the known-answer boards' scalars")
+    ap.add_argument("--routed-only", action="store_true", help="only the board rasterised from polygons")
     args = ap.parse_args()
     peec, kernel = import_reference(args.reference)
+    print("routed_pair", flush=True)
+    np.savez_compressed(HERE / "routed_pair.npz", **record(peec, synth.routed_pair()))
+    if args.routed_only:
+        return
     print("known_answers", flush=True)
     np.savez_compressed(HERE / "known_answers.npz", **record_known(peec))
     if args.known_only:

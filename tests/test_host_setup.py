@@ -152,7 +152,7 @@ def test_current_density_maps_match_reference():
 
 
 @pytest.mark.parametrize("name", ["necked_pair", "faces_stack3_diag", "faces_stack3_sheet", "necked_faces",
-                                  "necked_pair_scaled", "faces_stack3_sheet_scaled"])
+                                  "necked_pair_scaled", "faces_stack3_sheet_scaled", "routed_pair"])
 def test_corrections_and_face_sheets_through_the_device_model(name):
     """The arrays uploaded for strips narrower than the pitch, face sheets and resistance factors (the correction
     rows, the positions' own D^-1 blocks, the sheets' node layers) give, through the numpy model of the device

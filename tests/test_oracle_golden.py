@@ -13,7 +13,7 @@ from oracle import peec_oracle as po
 
 GOLD = Path(__file__).resolve().parent / "golden"
 CASES = ["small_pair", "small_stack3", "plain_plane", "necked_pair", "faces_stack3_diag", "faces_stack3_sheet",
-         "necked_faces"]
+         "necked_faces", "routed_pair"]
 
 
 def load(name):
@@ -112,11 +112,12 @@ def test_coupling_and_solves_match_reference(case):
             assert abs(sol["its"] - int(z[f"its{k}_{q}"])) <= 2
 
 
-def test_narrow_strip_corrections_match_reference():
+@pytest.mark.parametrize("name", ["necked_pair", "routed_pair"])
+def test_narrow_strip_corrections_match_reference(name):
     """Strips narrower than the pitch (peec.py:1732-1820): widths, resistance widths, the self-inductance
     change dL and the side-by-side mutual changes M_near equal the reference's."""
     import scipy.sparse as sp
-    z, board = load("necked_pair")
+    z, board = load(name)
     st = oracle_stack(board)
     assert np.array_equal(st.strip_width, z["strip_width"]) and np.array_equal(st.r_width, z["r_width"])
     assert (st.strip_width < 1).sum() > 0 and rel(st.dL, z["dL"]) < 1e-12
@@ -164,3 +165,12 @@ def test_branch_impedances_match_reference():
     for (l, w, t), ref in zip(z["bf_track_args"], z["bf_track"]):
         got = np.array([gs.track_impedance(l, w, t)(x) for x in f])
         assert rel(got, ref) < 1e-13
+
+
+def test_routed_board_is_the_rasterised_one():
+    """routed_pair's fixture holds the board as raster.build_layer made it from its polygons: made again, the
+    masks and widths are the same, bit for bit."""
+    z, board = load("routed_pair")
+    again = synth.routed_pair().to_arrays()
+    for k, v in again.items():
+        assert np.array_equal(np.asarray(v), z[f"board_{k}"]), k

@@ -4,6 +4,7 @@ copper area against the polygon's own area."""
 from pathlib import Path
 
 import numpy as np
+import pytest
 
 from groundtruth_gb300 import raster
 
@@ -105,3 +106,70 @@ def test_a_straight_track_on_free_cells_claims_one_row():
     br = raster.rasterise_tracks(1, [(np.array([[1.0, 3.0], [9.0, 3.0]]), 0.3)], 0.0, 0.0, 1.0, label, seeded, fx, fy)
     assert label[5, 3] == 0 and br == []                  # the walk stepped around it
     assert (label == 1).sum() > 9 and fy.any()
+
+
+def _copper_nets():
+    nets = []
+    for k in range(3):
+        holes = [Z[f"cu_net{k}_hole{m}"] for m in range(4) if f"cu_net{k}_hole{m}" in Z.files]
+        nets.append((Z[f"cu_net{k}_outline"], holes))
+    return nets
+
+
+def test_sub_grid_rasteriser_matches_reference():
+    """raster.coarse_from_fine against the reference's _coarse_from_fine (s = 4) on a pour with holes, a slanted
+    0.3 mm track and a pad: the cells' nets, the border crossings and their offsets, the fill, bit for bit (the
+    sub-grid's point test, synth.copper_at, stood in for shapely's in the reference run)."""
+    got = raster.coarse_from_fine(_copper_nets(), 0.4, 0.3, 0.5, 44, 46, 4)
+    for g, key in zip(got, ("label", "cx", "cy", "fill", "ox", "oy")):
+        assert np.array_equal(g, Z[f"cu_{key}"]), key
+
+
+def test_exact_copper_matches_reference():
+    """raster.exact_copper against the reference's _exact_copper on the same nets and cells: strip widths, node
+    areas and the narrow track's series factors, bit for bit; the areas add up to the copper's."""
+    nets = [raster.ring_edges(o, h) for o, h in _copper_nets()]
+    got = raster.exact_copper(nets, Z["cu_label"], Z["cu_xb"], Z["cu_yb"], 0.4, 0.3, 0.5)
+    for g, key in zip(got, ("ex_x", "ex_y", "area", "kx", "ky")):
+        assert np.array_equal(g, Z[f"cu_{key}"]), key
+    assert (got[3] != 1).any()                                # the narrow track's series factors
+    copper = sum(0.5 * np.sum(pa[:, 0] * pb[:, 1] - pb[:, 0] * pa[:, 1]) for pa, pb in nets)
+    assert abs(got[2].sum() * 0.25 - copper) < 0.02 * copper  # copper of no node within reach is dropped
+
+
+def _layer_nets():
+    nets = {}
+    for name in ("GND", "SIG", "VCC"):
+        pieces = []
+        for m in range(3):
+            if f"ly_{name}_{m}_outline" not in Z.files:
+                break
+            holes = [Z[f"ly_{name}_{m}_hole{q}"] for q in range(4) if f"ly_{name}_{m}_hole{q}" in Z.files]
+            pieces.append((Z[f"ly_{name}_{m}_outline"], holes))
+        nets[name] = pieces
+    return nets
+
+
+@pytest.mark.parametrize("case, bbox, d, sub", [("s1", (0.3, 0.2, 21.0, 24.5), 0.5, 1),
+                                                ("s4", (0.3, 0.2, 21.0, 24.5), 0.5, 4),
+                                                ("s3", (-0.4, 0.9, 20.6, 22.0), 0.7, 3)])
+def test_layer_raster_matches_reference(case, bbox, d, sub):
+    """raster.build_layer against the reference's build_grid on a layer with a pour (holes), a slanted track, a
+    supply of two separate pads, seeds (one on a far empty node, one for a net the layer lacks) and tracks: nodes,
+    strips, labels and bridges at sub = 1, and at sub = 4 and 3 the fill, strip widths and offsets, node areas and
+    resistance widths, bit for bit (the reference run with the same point test, its heat points left out)."""
+    seeds = {"GND": [(4.0, 12.0), (10.1, 9.6), (2.9, 2.7)], "VCC": [(18.0, 4.0), (30.0, 30.0)], "NC": [(1.0, 1.0)]}
+    lines = {"SIG": [(np.array([[5.2, 14.3], [11.0, 16.1], [19.4, 20.2]]), 0.2)],
+             "GND": [(np.array([[3.0, 3.0], [3.0, 6.5], [6.0, 6.5]]), 0.25)],
+             "VCC": [(np.array([[2.8, 2.6], [17.9, 3.9]]), 0.3)]}
+    g = raster.build_layer(_layer_nets(), bbox, d, seeds, lines, sub)
+    for key in ("node", "xb", "yb", "label"):
+        assert np.array_equal(getattr(g, key), Z[f"ly_{case}_{key}"]), key
+    assert np.array_equal(np.array(g.bridges, float).reshape(-1, 6), Z[f"ly_{case}_bridges"])
+    for key in ("fill", "wx", "wy", "ox", "oy", "area", "rx", "ry"):
+        if sub == 1:
+            assert getattr(g, key) is None
+        else:
+            assert np.array_equal(getattr(g, key), Z[f"ly_{case}_{key}"]), key
+    if sub > 1:
+        assert set(g.widths()) == {"wx", "wy", "ox", "oy", "rx", "ry"}
