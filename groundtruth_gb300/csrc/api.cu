@@ -1073,6 +1073,14 @@ int gt_geometry_create(const gt_geometry_desc* d, gt_geometry** out) {
     g.tab_cap0 = g.tab_ovr0 + d->n_override * S * S;
     g.tab_br0 = g.tab_cap0 + d->n_pairs;
     if (g.tab_br0 + d->n_branches != d->n_table) throw Invalid("admittance table length mismatch");
+    g.cap_fill = nullptr;
+    if (d->cap_fill && d->n_pairs > 0) {
+        const size_t nc = (size_t)d->n_pairs * nx * ny;
+        for (size_t q = 0; q < nc; ++q)
+            if (d->mask[d->off_c + (int64_t)q] && !(d->cap_fill[q] > 0.0 && d->cap_fill[q] <= 1.0))
+                throw Invalid("cap_fill must be in (0, 1] at every capacitance cell");
+        g.cap_fill = p.upload(d->cap_fill, nc);
+    }
     g.ovr_x = g.ovr_y = nullptr;
     if (d->n_override > 0) {
         if (!d->override_x || !d->override_y) throw Invalid("override positions missing");

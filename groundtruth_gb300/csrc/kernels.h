@@ -25,6 +25,9 @@ struct Geo {
     const int* ovr_x;
     const int* ovr_y;
     int tab_ovr0;
+    // per capacitance cell [np][nx][ny] the share of the cell's area both planes' copper covers (a cell of
+    // admittance share / z_cap); null: every cell whole
+    const double* cap_fill;
 };
 
 // The narrow strips' corrections to the system product (narrow.cu): rows at dense positions pos[q] of sheet

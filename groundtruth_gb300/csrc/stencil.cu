@@ -95,7 +95,9 @@ __global__ void __launch_bounds__(256) tail_kernel(Geo g, const cx<R>* __restric
                 oc[pos] = zero<R>();
                 continue;
             }
-            put(pos, zc * xc[pos] - (V[u * nxy + ij] - V[l * nxy + ij]));
+            // a partly covered cell: its capacitance is the share's, its impedance z_cap / share
+            const cx<R> z = g.cap_fill ? R(1.0 / g.cap_fill[(int64_t)p * nxy + ij]) * zc : zc;
+            put(pos, z * xc[pos] - (V[u * nxy + ij] - V[l * nxy + ij]));
         }
     } else {
         // branch rows z_br I_b - (V[a] - V[b]); padding zero
@@ -210,7 +212,8 @@ __global__ void __launch_bounds__(256) pc_node_kernel(Geo g, const cx<R>* __rest
             const int up = g.pair_layers[2 * p], lo = g.pair_layers[2 * p + 1];
             const int64_t pos = g.off_c + (int64_t)p * nxy + ij;
             if (!g.mask[pos]) continue;
-            const cx<R> v = T[g.tab_cap0 + p] * rc[pos];
+            cx<R> v = T[g.tab_cap0 + p] * rc[pos];
+            if (g.cap_fill) v = R(g.cap_fill[(int64_t)p * nxy + ij]) * v;
 #pragma unroll
             for (int k = 0; k < MAXS; ++k) {
                 if (k == up) kcl[k] += v;
@@ -296,7 +299,8 @@ __global__ void __launch_bounds__(256) pc_strip_kernel(Geo g, const cx<R>* __res
         for (int j = threadIdx.x; j < ny; j += blockDim.x) {
             const int ij = i * ny + j;
             const int64_t pos = g.off_c + (int64_t)p * nxy + ij;
-            oc[pos] = g.mask[pos] ? zc * (rc[pos] + (yc[up * nxy + ij] - yc[lo * nxy + ij])) : zero<R>();
+            const cx<R> y = g.cap_fill ? R(g.cap_fill[(int64_t)p * nxy + ij]) * zc : zc;
+            oc[pos] = g.mask[pos] ? y * (rc[pos] + (yc[up * nxy + ij] - yc[lo * nxy + ij])) : zero<R>();
         }
     } else if (part == 3) for (int bx = blockIdx.x * RPB; bx < blockIdx.x * RPB + RPB; ++bx) {
         const int k = bx / nx, i = bx - k * nx;

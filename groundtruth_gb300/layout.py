@@ -56,6 +56,7 @@ class Topology:
     full_label: np.ndarray
     keep: np.ndarray          # (n_nodes,) bool
     sheet_layer: np.ndarray = None   # (S,) each sheet's layer (its strips join that layer's nodes)
+    cap_share: np.ndarray = None     # (ncap,) each capacitance cell's facing copper share (1: whole cells)
 
     @property
     def NL(self):
@@ -90,11 +91,13 @@ class Topology:
         return int(self.keep.sum())
 
 
-def topology(node_masks, xb_masks, yb_masks, d: float, pairs: list, branch_nodes: list, twin_parent=()) -> tuple:
+def topology(node_masks, xb_masks, yb_masks, d: float, pairs: list, branch_nodes: list, twin_parent=(),
+             fills=None) -> tuple:
     """The reference's numbering (peec.py:1596-1656).  pairs: [(upper, lower, c_per_area, tan_delta)];
     branch_nodes: [((k,i,j), (k,i,j))]; twin_parent: the split layers, whose lower-face sheets (numbered after the
-    layers) have the layer's strips on the layer's nodes.  Returns (Topology, indices of the branches kept: both
-    ends on copper and different)."""
+    layers) have the layer's strips on the layer's nodes; fills: per layer the cells' copper fraction (None, or
+    None for a layer: its node mask), a plane pair's cell capacitance taking the smaller of its two layers'
+    (peec.py:1622-1637).  Returns (Topology, indices of the branches kept: both ends on copper and different)."""
     node = np.stack(node_masks).astype(bool)
     NL, nx, ny = node.shape
     twin_parent = np.asarray(twin_parent, np.int64)
@@ -110,17 +113,22 @@ def topology(node_masks, xb_masks, yb_masks, d: float, pairs: list, branch_nodes
     nid[idx] = np.arange(len(idx[0]))
     n = len(idx[0])
     xa, ya = np.argwhere(xb), np.argwhere(yb)
-    caps, pl, cmask = [], [], []
+    fill = [node[k].astype(float) if fills is None or fills[k] is None else np.asarray(fills[k], float)
+            for k in range(NL)]
+    caps, pl, cmask, shares = [], [], [], []
     for (u, l, cpa, td) in pairs:
         between = np.zeros((nx, ny), bool)
         for m in range(int(u) + 1, int(l)):
             between |= node[m]
-        mask = node[int(u)] & node[int(l)] & ~between
+        full = np.minimum(fill[int(u)], fill[int(l)])
+        mask = node[int(u)] & node[int(l)] & ~between & (full > 0)
         ii, jj = np.nonzero(mask)
+        share = full[ii, jj]
         caps.append(np.column_stack([np.full(len(ii), u), np.full(len(ii), l), ii, jj,
-                                     np.full(len(ii), cpa * d * d), np.full(len(ii), td)]))
+                                     cpa * (d * d) * share, np.full(len(ii), td)]))
         pl.append((int(u), int(l)))
         cmask.append(mask)
+        shares.append(share)
     cap = np.concatenate(caps) if caps else np.zeros((0, 6))
     kept, ab = [], []
     for n_br, (a, b) in enumerate(branch_nodes):
@@ -147,7 +155,7 @@ def topology(node_masks, xb_masks, yb_masks, d: float, pairs: list, branch_nodes
     keep[first] = False
     top = Topology(S, nx, ny, node, xb, yb, nid, xa, ya, cap, np.array(pl, np.int64).reshape(-1, 2),
                    np.array(cmask, bool).reshape(-1, nx, ny), ab, a_nodes, b_nodes, cond_label, full_label, keep,
-                   sheet_layer)
+                   sheet_layer, np.concatenate(shares) if shares else np.zeros(0))
     return top, kept
 
 

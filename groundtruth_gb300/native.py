@@ -44,7 +44,7 @@ class GeometryDesc(C.Structure):
                 ("narrow_dl", DP), ("narrow_ptr", I64P), ("narrow_col", I64P), ("narrow_val", DP),
                 ("n_layers", C.c_int32), ("sheet_layer", I32P), ("n_twins", C.c_int32),
                 ("narrow_partner", I64P), ("narrow_twin", I32P), ("narrow_twfac", DP),
-                ("narrow_rre", DP), ("narrow_twre", DP)]
+                ("narrow_rre", DP), ("narrow_twre", DP), ("cap_fill", DP)]
 
 
 PRECISIONS = {"mixed": 0, "fp64": 1, "mixed16": 2}
@@ -196,6 +196,11 @@ class Geometry:
         d.n_layers = st.N
         d.sheet_layer = _ptr(arr(st.sheet_layer, np.int32), C.c_int32)
         d.n_twins = len(st.twin_parent)
+        share = t.cap_share
+        if share is not None and len(share) and np.any(share != 1.0):
+            cells = np.ones(len(t.pair_layers) * nx * ny)
+            cells[D.compact_to_dense[st.ns: st.ns + st.ncap] - D.off_c] = share
+            d.cap_fill = _ptr(arr(cells, np.float64), C.c_double)
         h = P()
         check(lib, lib.gt_geometry_create(C.byref(d), C.byref(h)), "gt_geometry_create")
         self.h = h

@@ -60,10 +60,16 @@ class Grid:
     oy: Optional[np.ndarray] = None
     rx: Optional[np.ndarray] = None      # the width the strip's resistance takes (None / 0: its width)
     ry: Optional[np.ndarray] = None
+    fill: Optional[np.ndarray] = None    # (nx, ny) each cell's copper fraction from a sub-grid (None: whole cells)
+    area: Optional[np.ndarray] = None    # (nx, ny) each node's measured copper in its cell, a fraction of d^2
+    label: Optional[np.ndarray] = None   # (nx, ny) each node's net (-1: none; None: one net)
 
     def copper_area(self) -> np.ndarray:
-        """Each node's copper as a share of its cell (peec.py:257-281, without a measured area): the mean width of
-        the strips that touch it, 1 at a node of full strips or of a grid without widths, 0 off copper."""
+        """Each node's copper as a share of its cell (peec.py:257-312), 0 off copper: without a measured area the
+        mean width of the strips that touch it (1 at a node of full strips or of a grid without widths); with one,
+        the node's run width (its x strips' mean where it has x strips on both sides and not y, and the other way
+        round, else all its strips') times the measured area over the run widths summed over its 3 x 3
+        neighbourhood of the same net, or the mean width where no measured copper is around it."""
         out = self.node.astype(float)
         if self.wx is None or self.wy is None:
             return out
@@ -77,7 +83,26 @@ class Grid:
         nys[:, :-1] += self.yb
         nys[:, 1:] += self.yb
         n = nxs + nys
-        return np.where(n > 0, (sx + sy) / np.maximum(n, 1), out)
+        mean_width = np.where(n > 0, (sx + sy) / np.maximum(n, 1), out)
+        if self.area is None:
+            return mean_width
+        along_x, along_y = nxs == 2, nys == 2
+        run = np.where(along_x & ~along_y, sx / np.maximum(nxs, 1),
+                       np.where(along_y & ~along_x, sy / np.maximum(nys, 1), mean_width))
+        a = np.where(self.node, self.area, 0.0)
+        w = np.where(self.node, run, 0.0)
+        net = np.where(self.node, self.label if self.label is not None else 0, -1)
+        tot_a, tot_w = np.zeros(a.shape), np.zeros(a.shape)
+        ni, nj = a.shape
+        for di in (-1, 0, 1):
+            for dj in (-1, 0, 1):
+                src = (slice(max(di, 0), ni + min(di, 0)), slice(max(dj, 0), nj + min(dj, 0)))
+                dst = (slice(max(-di, 0), ni + min(-di, 0)), slice(max(-dj, 0), nj + min(-dj, 0)))
+                same = (net[src] == net[dst]) & (net[dst] >= 0)
+                tot_a[dst] += np.where(same, a[src], 0.0)
+                tot_w[dst] += np.where(same, w[src], 0.0)
+        spread = np.where(tot_w > 0, w * tot_a / np.maximum(tot_w, 1e-12), 0.0)
+        return np.where(self.node, np.where(spread > 0, spread, mean_width), 0.0)
 
 
 @dataclass
@@ -290,7 +315,8 @@ class PlaneStack:
         t, kept = layout.topology([l.grid.node for l in layers], [l.grid.xb for l in layers],
                                   [l.grid.yb for l in layers], self.d,
                                   [(p.upper, p.lower, p.c_per_area, p.tan_delta) for p in self.pairs],
-                                  [(b.a, b.b) for b in self.branches_all], self.twin_parent)
+                                  [(b.a, b.b) for b in self.branches_all], self.twin_parent,
+                                  [l.grid.fill for l in layers])
         self.top = t
         self.branches = [self.branches_all[k] for k in kept]
         self.node, self.nid, self.xa, self.ya, self.keep = t.node, t.nid, t.xa, t.ya, t.keep
@@ -623,13 +649,14 @@ class PlaneStack:
         kept_of_nid[t.keep] = np.arange(t.n_keep)
         U, Vv, T, C = [], [], [], []
 
-        def add(s1_nodes, s2_nodes, tab):
-            """D^-1 entry tab between strips with ends s1 (a, b) and s2 (a, b): all (u, v) terms."""
+        def add(s1_nodes, s2_nodes, tab, scale=None):
+            """D^-1 entry tab (times scale) between strips with ends s1 (a, b) and s2 (a, b): all (u, v) terms."""
             for (u, su) in ((s1_nodes[0], 1.0), (s1_nodes[1], -1.0)):
                 for (v, sv) in ((s2_nodes[0], 1.0), (s2_nodes[1], -1.0)):
                     ku, kv = kept_of_nid[u], kept_of_nid[v]
                     ok = (ku >= 0) & (kv >= 0)
-                    U.append(ku[ok]); Vv.append(kv[ok]); T.append(tab[ok]); C.append(np.full(int(ok.sum()), su * sv))
+                    U.append(ku[ok]); Vv.append(kv[ok]); T.append(tab[ok])
+                    C.append(su * sv * scale[ok] if scale is not None else np.full(int(ok.sum()), su * sv))
 
         for o, idx, di, dj in ((0, t.xa, 1, 0), (1, t.ya, 0, 1)):
             if len(idx) == 0:
@@ -656,7 +683,8 @@ class PlaneStack:
         if len(cu):
             pidx = np.concatenate([np.full(int(t.cap_mask[p].sum()), p) for p in range(len(t.pair_layers))])
             e = (t.nid[cu[:, 0], cu[:, 2], cu[:, 3]], t.nid[cu[:, 1], cu[:, 2], cu[:, 3]])
-            add(e, e, self.tab_cap0 + pidx)
+            # a partly covered cell's admittance: the pair's whole-cell one times the facing share
+            add(e, e, self.tab_cap0 + pidx, t.cap_share if np.any(t.cap_share != 1.0) else None)
         if self.nbr:
             e = (t.branch_ab[:, 0], t.branch_ab[:, 1])
             add(e, e, self.tab_br0 + np.arange(self.nbr))
@@ -1189,8 +1217,8 @@ def solve_many(excitations: list, freqs, tol: float = 1e-5, **kw) -> list:
 
 def from_board(board, _device: bool = True):
     """A PlaneStack and its RouteExcitations for a ``synth.Board`` (the workloads' boards)."""
-    grids = [Grid(0.0, 0.0, board.d * 1e3, board.nx, board.ny, l.node, l.xb, l.yb, **(l.widths or {}))
-             for l in board.layers]
+    grids = [Grid(0.0, 0.0, board.d * 1e3, board.nx, board.ny, l.node, l.xb, l.yb, **(l.widths or {}),
+                  fill=l.fill, area=l.area, label=l.label) for l in board.layers]
     layers = [PlaneLayer(l.name, l.z, g, l.thickness) for l, g in zip(board.layers, grids)]
     branches = [Branch(b.a, b.b, b.z, f"br{n}", b.kind, b.radius) for n, b in enumerate(board.branches)]
     pairs = [PlanePair(p.upper, p.lower, p.c_per_area, p.tan_delta) for p in board.pairs]

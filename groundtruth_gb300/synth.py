@@ -110,6 +110,11 @@ class Layer:
     # strips narrower than the pitch (the reference Grid's wx / wy, ox / oy, rx / ry: width and centre offset as
     # fractions of the pitch, the resistance's width; None: every strip full and centred)
     widths: Optional[dict] = None
+    # a sub-grid raster's cells (the reference Grid's fill / area / label: each cell's copper fraction, each node's
+    # measured copper, each node's net; None: whole cells, no measured copper, one net)
+    fill: Optional[np.ndarray] = None
+    area: Optional[np.ndarray] = None
+    label: Optional[np.ndarray] = None
 
 
 @dataclass
@@ -182,6 +187,9 @@ class Board:
         for k, l in enumerate(self.layers):
             for key, v in (l.widths or {}).items():
                 out[f"layer{k}_{key}"] = np.asarray(v, float)
+            for key in CELL_KEYS:
+                if getattr(l, key) is not None:
+                    out[f"layer{k}_{key}"] = np.asarray(getattr(l, key), np.int64 if key == "label" else float)
         for n, net in enumerate(self.nets):
             out[f"net{n}_seg"] = net.segments
             out[f"net{n}_ends"] = np.array([*net.driver, *net.receiver], np.int64)
@@ -196,6 +204,9 @@ class Board:
         for k, l in enumerate(layers):
             w = {key: np.asarray(a[f"layer{k}_{key}"], float) for key in WIDTH_KEYS if f"layer{k}_{key}" in files}
             l.widths = w or None
+            for key in CELL_KEYS:
+                if f"layer{k}_{key}" in files:
+                    setattr(l, key, np.asarray(a[f"layer{k}_{key}"]))
         pairs = [Pair(int(p[0]), int(p[1]), float(p[2]), float(p[3])) for p in a["pairs"]]
         branches = [BranchSpec(tuple(int(v) for v in ab[:3]), tuple(int(v) for v in ab[3:]), float(r[0]), float(r[1]),
                                float(r[2]), "via" if via else "part", float(r[3]))
@@ -462,6 +473,7 @@ def _labels(mask: np.ndarray, xb: np.ndarray, yb: np.ndarray) -> np.ndarray:
 
 
 WIDTH_KEYS = ("wx", "wy", "ox", "oy", "rx", "ry")
+CELL_KEYS = ("fill", "area", "label")
 
 
 def plane_pair_line(length_mm: float, w: float = 10e-3, h: float = 0.2e-3, t: float = 35e-6, d: float = 0.4e-3,
@@ -600,7 +612,8 @@ def routed_pair(sub: int = 4) -> Board:
     with the copper's exact widths: a GND pour (a slanted slot, a square hole, a notched corner with a pad in it
     joined to the pour by a 0.25 mm corridor, its track's centreline forced) over a PWR plane with a cut-out;
     0.5 mm pitch, 40 x 36 nodes, a decoupling part and a via, two nets crossing the slot.  The copper's ragged
-    edges give strips narrower than the pitch all around (wx / wy, ox / oy, rx / ry)."""
+    edges give strips narrower than the pitch all around (wx / wy, ox / oy, rx / ry), cells partly covered (their
+    plane-pair capacitance the facing share) and measured node areas."""
     from . import raster
     d_mm, t, h = 0.5, 35e-6, 0.2e-3
     bbox = (0.0, 0.0, 19.5, 17.5)
@@ -614,8 +627,8 @@ def routed_pair(sub: int = 4) -> Board:
     plane = (np.array([[0.1, 0.1], [19.4, 0.1], [19.4, 17.4], [0.1, 17.4]]),
              [np.array([[5.2, 2.3], [7.9, 2.3], [7.9, 4.1], [5.2, 4.1]])])
     pwr = raster.build_layer({"PWR": [plane]}, bbox, d_mm, sub=sub)
-    layers = [Layer("GND", 0.0, t, gnd.node, gnd.xb, gnd.yb, gnd.widths()),
-              Layer("PWR", -(h + t), t, pwr.node, pwr.xb, pwr.yb, pwr.widths())]
+    layers = [Layer(name, z, t, g.node, g.xb, g.yb, g.widths(), g.fill, g.area, g.label)
+              for name, z, g in (("GND", 0.0, gnd), ("PWR", -(h + t), pwr))]
     d = d_mm * 1e-3
     pairs = [Pair(0, 1, EPS0 * 4.4 / h)]
     branches = [BranchSpec((0, 30, 26), (1, 30, 26), 0.02, 0.5e-9, 100e-9, "part"),

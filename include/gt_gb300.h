@@ -112,6 +112,11 @@ typedef struct gt_geometry_desc {
      * coupling (narrow_twre). */
     const double* narrow_rre;
     const double* narrow_twre;
+    /* Plane-pair capacitance of partly covered cells (PlaneStack.__init__'s per-cell facing area,
+     * peec.py:1622-1637: C = c_per_area d^2 min(fill_upper, fill_lower)), NULL when every cell is whole: per cell
+     * [n_pairs][nx][ny] of the C segment the covered share (> 0 where the cell has a capacitance); the cell's
+     * impedance is the operator's zcap of its pair over the share and its D^-1 entry the table's times it. */
+    const double* cap_fill;
 } gt_geometry_desc;
 
 typedef struct gt_solve_opts {

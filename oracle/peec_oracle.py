@@ -416,6 +416,7 @@ class OLayer:
     xb: np.ndarray
     yb: np.ndarray
     widths: Optional[dict] = None     # the grid's wx / wy, ox / oy, rx / ry (peec.py:213-220); None: full strips
+    fill: Optional[np.ndarray] = None  # the grid's cells' copper fraction (peec.py:211); None: the node mask
 
 
 @dataclass
@@ -653,15 +654,19 @@ class OracleStack:
         self.nxb, self.nyb = len(self.xa), len(self.ya)
         self.ns = self.nxb + self.nyb
         self._twins()
+        # a plane pair's capacitance per cell where both planes have copper and no layer between them does, over
+        # the facing copper area of the cell (peec.py:1622-1637)
         cap = []
         cell = self.d ** 2
+        fill = [l.fill if l.fill is not None else node[k].astype(float) for k, l in enumerate(self.layers)]
         for p in self.pairs:
             between = np.zeros(node.shape[1:], bool)
             for m in range(p.upper + 1, p.lower):
                 between |= node[m]
-            ii, jj = np.nonzero(node[p.upper] & node[p.lower] & ~between)
+            share = np.minimum(fill[p.upper], fill[p.lower])
+            ii, jj = np.nonzero(node[p.upper] & node[p.lower] & ~between & (share > 0))
             cap.append(np.column_stack([np.full(len(ii), p.upper), np.full(len(ii), p.lower), ii, jj,
-                                        np.full(len(ii), p.c_per_area * cell), np.full(len(ii), p.tan_delta)]))
+                                        p.c_per_area * cell * share[ii, jj], np.full(len(ii), p.tan_delta)]))
         self.cap = np.concatenate(cap) if cap else np.zeros((0, 6))
         self.ncap = len(self.cap)
         self.branches = [b for b in branches if self.nid[b.a] >= 0 and self.nid[b.b] >= 0 and b.a != b.b]

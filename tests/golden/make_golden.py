@@ -30,7 +30,8 @@ copper width, Solution.node_field).
 (PlaneStack.with_branches), including solves warm-started from the base's solutions.
 
 ``routed_pair.npz``: the same records for a plane pair rasterised from polygons by this build's restatement of
-the reference's build_grid (raster.build_layer, sub-grid 4, exact widths; synth.routed_pair).
+the reference's build_grid (raster.build_layer, sub-grid 4: exact widths, cell fills, measured node areas;
+synth.routed_pair); ``routed_pair_fields.npz`` its current-density maps.
 ``known_answers.npz``: the reference's loop impedances and moments for the known-answer boards (the
 microstrip over a 40 x 20 mm plane with and without slots or an edge cut, the parallel-plate lines 20 and 40 mm
 long; ``synth.KNOWN_BOARDS``), solved to rtol 1e-10.
@@ -64,7 +65,8 @@ def import_reference(root: str):
 
 def build_reference(peec, board: synth.Board):
     grids = [peec.Grid(0.0, 0.0, board.d * 1e3, board.nx, board.ny, l.node.copy(), l.xb.copy(), l.yb.copy(),
-                       **{k: np.array(v, float) for k, v in (l.widths or {}).items()})
+                       **{k: np.array(v, float) for k, v in (l.widths or {}).items()},
+                       **{k: np.array(getattr(l, k)) for k in synth.CELL_KEYS if getattr(l, k) is not None})
              for l in board.layers]
     layers = [peec.PlaneLayer(l.name, l.z, g, l.thickness) for l, g in zip(board.layers, grids)]
     branches = [peec.Branch(b.a, b.b, (lambda f, b=b: b.z(f)), f"br{n}", b.kind, b.radius)
@@ -282,6 +284,7 @@ def main():
     peec, kernel = import_reference(args.reference)
     print("routed_pair", flush=True)
     np.savez_compressed(HERE / "routed_pair.npz", **record(peec, synth.routed_pair()))
+    np.savez_compressed(HERE / "routed_pair_fields.npz", **record_fields(peec, synth.routed_pair()))
     if args.routed_only:
         return
     print("known_answers", flush=True)

@@ -18,6 +18,11 @@ class DenseModel:
         self.lay = np.asarray(t.sheet_layer, np.int64)     # each current sheet's node layer
         self.D = D
         self.np_ = len(t.pair_layers)
+        # each capacitance cell's facing share (1 where whole or absent): its admittance is the pair's times it
+        self.share = np.ones((self.np_, self.nx, self.ny))
+        if t.cap_share is not None and len(t.cap_share):
+            pidx = np.concatenate([np.full(int(t.cap_mask[p].sum()), p) for p in range(self.np_)])
+            self.share[pidx, t.cap[:, 2].astype(int), t.cap[:, 3].astype(int)] = t.cap_share
 
     # ---------------------------------------------------------------- views
     def seg(self, v, name):
@@ -71,7 +76,7 @@ class DenseModel:
         oX[:] = (zsh[:, None, None] * X + 1j * w * self.lp(X, "x") - (Vs[:, :-1, :] - Vs[:, 1:, :])) * t.xb
         oY[:] = (zsh[:, None, None] * Y + 1j * w * self.lp(Y, "y") - (Vs[:, :, :-1] - Vs[:, :, 1:])) * t.yb
         for p, (u, l) in enumerate(t.pair_layers):
-            oC[p] = (zcap[p] * C[p] - (Vn[u] - Vn[l])) * t.cap_mask[p]
+            oC[p] = (zcap[p] / self.share[p] * C[p] - (Vn[u] - Vn[l])) * t.cap_mask[p]
         Vf = Vn.reshape(-1)
         for n, (a, b) in enumerate(self.branch_dense()):
             oB[n] = zbr[n] * B[n] - (Vf[a] - Vf[b])
@@ -127,7 +132,7 @@ class DenseModel:
             O[:] = np.einsum("ijkl,lij->kij", T, A)
         C, oC = self.seg(v, "C"), self.seg(out, "C")
         for p in range(self.np_):
-            oC[p] = tab[st.tab_cap0 + p] * C[p] * st.top.cap_mask[p]
+            oC[p] = tab[st.tab_cap0 + p] * self.share[p] * C[p] * st.top.cap_mask[p]
         self.seg(out, "B")[:] = tab[st.tab_br0: st.tab_br0 + st.nbr] * self.seg(v, "B")
         return out
 

@@ -23,7 +23,7 @@ def load(name):
 
 
 def oracle_stack(board):
-    layers = [po.OLayer(l.z, l.thickness, l.node, l.xb, l.yb, l.widths) for l in board.layers]
+    layers = [po.OLayer(l.z, l.thickness, l.node, l.xb, l.yb, l.widths, l.fill) for l in board.layers]
     pairs = [po.OPair(p.upper, p.lower, p.c_per_area, p.tan_delta) for p in board.pairs]
     branches = [po.OBranch(b.a, b.b, b.R, b.L, b.C, b.kind, b.radius) for b in board.branches]
     return po.OracleStack(layers, board.d, branches, pairs, board.sigma, board.precond, board.screen)

@@ -173,3 +173,62 @@ def test_layer_raster_matches_reference(case, bbox, d, sub):
             assert np.array_equal(getattr(g, key), Z[f"ly_{case}_{key}"]), key
     if sub > 1:
         assert set(g.widths()) == {"wx", "wy", "ox", "oy", "rx", "ry"}
+
+
+def _circle(cx, cy, r, n=32):
+    a = 2 * np.pi * np.arange(n) / n
+    return np.stack([cx + r * np.cos(a), cy + r * np.sin(a)], 1)
+
+
+def _pieces_of(g) -> int:
+    """Connected pieces of a layer's copper (nodes joined by strips)."""
+    import scipy.sparse as sp
+    from scipy.sparse.csgraph import connected_components
+    n = g.nx * g.ny
+    idx = np.arange(n).reshape(g.nx, g.ny)
+    a = np.concatenate([idx[:-1, :][g.xb], idx[:, :-1][g.yb]])
+    b = np.concatenate([idx[1:, :][g.xb], idx[:, 1:][g.yb]])
+    _, lab = connected_components(sp.coo_matrix((np.ones(len(a)), (a, b)), shape=(n, n)), directed=False)
+    return len(set(lab[g.node.ravel()].tolist()))
+
+
+PLANE = np.array([[0.0, 0.0], [20.0, 0.0], [20.0, 10.0], [0.0, 10.0]])
+
+
+def test_antipad_webs_conduct_on_the_sub_grid():
+    """The reference's test_raster.py:24-32: 0.36 mm antipads every 0.5 mm along x = 10 leave 0.14 mm webs; point
+    sampling on a 0.5 mm grid loses every node on that line (two pieces), the sub-grid keeps one piece with the
+    webs' cells partly filled."""
+    holes = [_circle(10.0, 0.5 * k, 0.18) for k in range(1, 20)]
+    plane = {"P": [(PLANE, holes)]}
+    assert _pieces_of(raster.build_layer(plane, (0, 0, 20, 10), 0.5)) == 2
+    g = raster.build_layer(plane, (0, 0, 20, 10), 0.5, sub=5)
+    assert _pieces_of(g) == 1
+    assert 0.2 < g.fill[20, 4] < 1.0 and g.fill[5, 5] == 1.0
+
+
+def test_a_slot_narrower_than_the_pitch_still_cuts():
+    """test_raster.py:35-37: a 0.3 mm slot across the plane on a 0.5 mm grid with the sub-grid: two pieces."""
+    halves = [(np.array([[0.0, 0.0], [9.85, 0.0], [9.85, 10.0], [0.0, 10.0]]), []),
+              (np.array([[10.15, 0.0], [20.0, 0.0], [20.0, 10.0], [10.15, 10.0]]), [])]
+    assert _pieces_of(raster.build_layer({"P": halves}, (0, 0, 20, 10), 0.5, sub=5)) == 2
+
+
+def test_capacitance_follows_copper_fill():
+    """test_raster.py:40-56: a plane pair's capacitance counts the copper facing in each cell (the cells' sub-grid
+    fill), not whole cells: perforated planes (96 holes of 0.3 mm radius) have the capacitance of their area,
+    within 3 %."""
+    from groundtruth_gb300 import stack as gs
+    holes = [_circle(2 + 1.0 * i, 2 + 1.0 * j, 0.3) for i in range(16) for j in range(6)]
+
+    def capacitance(h):
+        g = raster.build_layer({"P": [(PLANE, h)]}, (0, 0, 20, 10), 0.25, sub=4)
+        grid = gs.Grid(0.0, 0.0, 0.25, g.nx, g.ny, g.node, g.xb, g.yb, **g.widths(), fill=g.fill, area=g.area)
+        layers = [gs.PlaneLayer(n, z, grid) for n, z in (("top", 0.2e-3), ("bot", 0.0))]
+        st = gs.PlaneStack(layers, capacitance=[gs.PlanePair(0, 1, 8.854e-12 * 4.5 / 0.2e-3, 0.0)], _device=False)
+        return st.top.cap[:, 4].sum()
+
+    def area(poly):
+        return 0.5 * abs(np.sum(poly[:, 0] * np.roll(poly[:, 1], -1) - np.roll(poly[:, 0], -1) * poly[:, 1]))
+    expected = (area(PLANE) - sum(area(h) for h in holes)) / area(PLANE)
+    assert abs(capacitance(holes) / capacitance([]) - expected) < 0.03
