@@ -63,6 +63,49 @@ class Grid:
     fill: Optional[np.ndarray] = None    # (nx, ny) each cell's copper fraction from a sub-grid (None: whole cells)
     area: Optional[np.ndarray] = None    # (nx, ny) each node's measured copper in its cell, a fraction of d^2
     label: Optional[np.ndarray] = None   # (nx, ny) each node's net (-1: none; None: one net)
+    nets: list = field(default_factory=list)   # the net names label indexes
+
+    def xy(self, i, j):
+        """Board coordinates (mm) of node (i, j), arrays too (peec.py:225-227)."""
+        return self.x0 + np.asarray(i) * self.d, self.y0 + np.asarray(j) * self.d
+
+    def nearest_node(self, x: float, y: float, max_dist: Optional[float] = None,
+                     net: Optional[str] = None) -> Optional[tuple]:
+        """The copper node (of `net` only, when given) nearest to (x, y) mm, None when there is none within
+        max_dist (peec.py:229-255); with max_dist only a window around the point is searched."""
+        mask = self.node
+        if net is not None and self.label is not None:
+            if net not in self.nets:
+                return None
+            mask = self.label == self.nets.index(net)
+        ci, cj = int(round((x - self.x0) / self.d)), int(round((y - self.y0) / self.d))
+        if max_dist is not None:
+            r = max(int(math.ceil(max_dist / self.d)) + 1, 2)
+            i0, j0 = max(ci - r, 0), max(cj - r, 0)
+            ii, jj = np.nonzero(mask[i0:min(ci + r + 1, self.nx), j0:min(cj + r + 1, self.ny)])
+            ii, jj = ii + i0, jj + j0
+        else:
+            ii, jj = np.nonzero(mask)
+        if len(ii) == 0:
+            return None
+        px, py = self.xy(ii, jj)
+        d2 = (px - x) ** 2 + (py - y) ** 2
+        k = int(np.argmin(d2))
+        if max_dist is not None and d2[k] > max_dist ** 2:
+            return None
+        return int(ii[k]), int(jj[k])
+
+    def net_at(self, node: tuple) -> str:
+        """The net of a node's copper, "" off copper or without net labels (peec.py:316-320)."""
+        if self.label is None or self.label[node] < 0:
+            return ""
+        return self.nets[self.label[node]]
+
+    @property
+    def extent(self) -> tuple:
+        """(x0, x1, y0, y1) mm that the cells cover, each node at its cell's centre (peec.py:322-327)."""
+        h = self.d / 2
+        return (self.x0 - h, self.x0 + (self.nx - 0.5) * self.d, self.y0 - h, self.y0 + (self.ny - 0.5) * self.d)
 
     def copper_area(self) -> np.ndarray:
         """Each node's copper as a share of its cell (peec.py:257-312), 0 off copper: without a measured area the
@@ -249,6 +292,40 @@ class Solution:
         kx, ky = self.node_field(k, d_mm, copper)
         return np.sqrt(np.abs(kx) ** 2 + np.abs(ky) ** 2)
 
+    def dominant_phase(self) -> float:
+        """The phase at which the plane currents are largest (peec.py:1210-1226): half the angle of the sum of
+        the strip currents squared over all layers (the principal axis of the currents in the complex plane),
+        turned by pi where the currents at that phase run against the signal's own (their real part); 0 for
+        currents that are all zero."""
+        phi = getattr(self, "_phase", None)
+        if phi is not None:
+            return phi
+        sq = complex(np.sum(self.I_x ** 2) + np.sum(self.I_y ** 2))
+        phi = 0.5 * math.atan2(sq.imag, sq.real) if abs(sq) > 0 else 0.0
+        turn = np.exp(-1j * phi)
+        if float(np.sum((self.I_x * turn).real * self.I_x.real) + np.sum((self.I_y * turn).real * self.I_y.real)) < 0:
+            phi += math.pi
+        self._phase = phi
+        return phi
+
+    def sheet_vectors(self, k: int, d_mm: float, copper: bool = False) -> tuple:
+        """Real (Kx, Ky) at the nodes of layer k at the dominant phase (peec.py:1228-1233)."""
+        kx, ky = self.node_field(k, d_mm, copper)
+        turn = np.exp(-1j * self.dominant_phase())
+        return (kx * turn).real, (ky * turn).real
+
+    def layer_share(self, masks: Optional[list] = None) -> np.ndarray:
+        """Each layer's share of the summed strip current magnitudes; masks: per layer (x, y) strip masks to count
+        (peec.py:1235-1247)."""
+        per = np.zeros(len(self.I_x))
+        for k in range(len(self.I_x)):
+            ax, ay = np.abs(self.I_x[k]), np.abs(self.I_y[k])
+            if masks is not None:
+                ax, ay = ax * masks[k][0], ay * masks[k][1]
+            per[k] = ax.sum() + ay.sum()
+        total = per.sum()
+        return per / total if total > 0 else per
+
 
 def native_geometry(st):
     from . import native
@@ -397,6 +474,16 @@ class PlaneStack:
         idx = (self.xa if orient == "x" else self.ya).copy()
         idx[:, 0] = self.sheet_layer[idx[:, 0]]
         return idx
+
+    def face_z(self, k: int, z: float) -> float:
+        """Sheet k's face towards height z (m): a one-sheet layer's centre moved half its copper towards z, a face
+        sheet's own height (its sheet_t is 0) (peec.py:1935-1939)."""
+        t = 0.5 * self.sheet_t[k]
+        return self.sheet_z[k] + (t if z > self.sheet_z[k] else -t)
+
+    def surface_impedance(self, f: float, t: float) -> complex:
+        """Sheet impedance (ohm per square) of copper t thick at f: the one-face slab (peec.py:2144-2148)."""
+        return complex(greens.slab_impedance(t, f, self.sigma))
 
     def face_gap(self, s: int, t: int) -> float:
         """The distance between the faces sheets s and t turn to each other (peec.py:1926-1933)."""

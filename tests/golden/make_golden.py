@@ -25,7 +25,7 @@ split layer and the top one (the faces' shared corrections).
 ``necked_pair_scaled.npz`` / ``faces_stack3_sheet_scaled.npz``: those boards with seeded resistance factors on
 every strip and branch (PlaneStack.set_resistance_scale): products and solves.
 ``necked_pair_fields.npz``: the reference's current-density maps of that board's net 0 (per cell and per
-copper width, Solution.node_field).
+copper width, Solution.node_field; the real vectors at the dominant phase, the layers' current shares).
 ``small_pair_derived.npz`` holds the same for small_pair plus a what-if edit's branches on a derived stack
 (PlaneStack.with_branches), including solves warm-started from the base's solutions.
 
@@ -229,6 +229,11 @@ def record_fields(peec, board: synth.Board) -> dict:
         for copper in (False, True):
             kx, ky = sol.node_field(k, board.d * 1e3, copper=copper)
             out[f"kx{k}_{int(copper)}"], out[f"ky{k}_{int(copper)}"] = kx, ky
+            vx, vy = sol.sheet_vectors(k, board.d * 1e3, copper=copper)
+            out[f"vx{k}_{int(copper)}"], out[f"vy{k}_{int(copper)}"] = vx, vy
+    out.update(phase=np.float64(sol.dominant_phase()), share=sol.layer_share(),
+               share_masked=sol.layer_share([(np.ones_like(sol.I_x[k].real, bool), np.zeros_like(sol.I_y[k].real, bool))
+                                             for k in range(st.N)]))
     return out
 
 
@@ -280,8 +285,13 @@ def main():
     ap.add_argument("--faces-only", action="store_true", help="only the face-sheet boards' fixtures")
     ap.add_argument("--known-only", action="store_true", help="only the known-answer boards' scalars")
     ap.add_argument("--routed-only", action="store_true", help="only the board rasterised from polygons")
+    ap.add_argument("--fields-only", action="store_true", help="only the current-density maps")
     args = ap.parse_args()
     peec, kernel = import_reference(args.reference)
+    if args.fields_only:
+        np.savez_compressed(HERE / "necked_pair_fields.npz", **record_fields(peec, synth.necked_pair()))
+        np.savez_compressed(HERE / "routed_pair_fields.npz", **record_fields(peec, synth.routed_pair()))
+        return
     print("routed_pair", flush=True)
     np.savez_compressed(HERE / "routed_pair.npz", **record(peec, synth.routed_pair()))
     np.savez_compressed(HERE / "routed_pair_fields.npz", **record_fields(peec, synth.routed_pair()))

@@ -102,6 +102,9 @@ def layer_nets(rng) -> dict:
     return {"GND": [pour], "SIG": [track], "VCC": [pad, pad2]}
 
 
+POINTS = [(2.0, 2.0), (10.3, 9.1), (17.9, 4.1), (12.0, 17.6), (30.0, 5.0), (0.0, 24.0)]
+
+
 def layer_cases(peec, rng) -> dict:
     """build_grid of the reference on one layer at sub = 1, 4 and 3, with seeds and tracks (shapely stubbed as in
     copper_cases: the point test synth.copper_at, covers with its border; the thermal heat points left out)."""
@@ -145,6 +148,15 @@ def layer_cases(peec, rng) -> dict:
         g = peec.build_grid({n: _Net(p) for n, p in nets.items()}, bbox, d, seeds, lines, sub)
         out.update({f"ly_{case}_node": g.node, f"ly_{case}_xb": g.xb, f"ly_{case}_yb": g.yb,
                     f"ly_{case}_label": g.label, f"ly_{case}_bridges": np.array(g.bridges, float).reshape(-1, 6)})
+        # the grid's lookups: nearest copper node (any net, one net, within a distance), a node's net, extent
+        near = []
+        for x, y in POINTS:
+            for net, dist in ((None, None), ("VCC", None), ("SIG", 1.0), ("GND", 0.3), ("NC", None)):
+                n = g.nearest_node(x, y, dist, net)
+                near.append((-1, -1) if n is None else n)
+        out[f"ly_{case}_near"] = np.array(near, np.int64)
+        out[f"ly_{case}_net_at"] = np.array([g.net_at(tuple(n)) if n[0] >= 0 else "" for n in near])
+        out[f"ly_{case}_extent"] = np.array(g.extent)
         for key in ("fill", "wx", "wy", "ox", "oy", "area", "rx", "ry"):
             if getattr(g, key) is not None:
                 out[f"ly_{case}_{key}"] = getattr(g, key)

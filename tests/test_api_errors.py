@@ -78,3 +78,14 @@ def test_plane_problem_builds_the_stack_and_route():
     st, routes = host(b)
     assert pp.stack.nb == st.nb and pp.injections == routes[0].injections
     assert np.allclose(pp.psi, routes[0].psi)
+
+
+def test_face_z_and_surface_impedance():
+    """PlaneStack.face_z (peec.py:1935-1939): a one-sheet layer's face towards a height is its centre moved half
+    its copper that way; surface_impedance (2144-2148) is the one-face slab's."""
+    from groundtruth_gb300 import greens
+    st, _ = host(synth.small_pair())
+    for k in range(st.n_sheets):
+        up, down = st.face_z(k, 1.0), st.face_z(k, -1.0)
+        assert up - down == pytest.approx(st.sheet_t[k]) and 0.5 * (up + down) == pytest.approx(st.sheet_z[k])
+    assert st.surface_impedance(1e8, 35e-6) == complex(greens.slab_impedance(35e-6, 1e8, st.sigma))

@@ -151,6 +151,13 @@ def test_current_density_maps_match_reference(name):
         for copper in (False, True):
             kx, ky = sol.node_field(k, board.d * 1e3, copper=copper)
             assert rel(kx, z[f"kx{k}_{int(copper)}"]) < 1e-12 and rel(ky, z[f"ky{k}_{int(copper)}"]) < 1e-12
+            vx, vy = sol.sheet_vectors(k, board.d * 1e3, copper=copper)
+            assert rel(vx, z[f"vx{k}_{int(copper)}"]) < 1e-12 and rel(vy, z[f"vy{k}_{int(copper)}"]) < 1e-12
+    # the dominant phase (peec.py:1210-1226) and the layers' current shares (1235-1247)
+    assert sol.dominant_phase() == pytest.approx(float(z["phase"]), abs=1e-12)
+    assert np.allclose(sol.layer_share(), z["share"], rtol=1e-12, atol=0)
+    masks = [(np.ones(sol.I_x[k].shape, bool), np.zeros(sol.I_y[k].shape, bool)) for k in range(st.N)]
+    assert np.allclose(sol.layer_share(masks), z["share_masked"], rtol=1e-12, atol=0)
 
 
 @pytest.mark.parametrize("name", ["necked_pair", "faces_stack3_diag", "faces_stack3_sheet", "necked_faces",

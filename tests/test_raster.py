@@ -232,3 +232,25 @@ def test_capacitance_follows_copper_fill():
         return 0.5 * abs(np.sum(poly[:, 0] * np.roll(poly[:, 1], -1) - np.roll(poly[:, 0], -1) * poly[:, 1]))
     expected = (area(PLANE) - sum(area(h) for h in holes)) / area(PLANE)
     assert abs(capacitance(holes) / capacitance([]) - expected) < 0.03
+
+
+@pytest.mark.parametrize("case, bbox, d, sub", [("s1", (0.3, 0.2, 21.0, 24.5), 0.5, 1),
+                                                ("s4", (0.3, 0.2, 21.0, 24.5), 0.5, 4)])
+def test_grid_lookups_match_reference(case, bbox, d, sub):
+    """stack.Grid's nearest_node (any net, one net, within a distance, a net the layer lacks), net_at and extent
+    (peec.py:225-327) on the rasterised layer against the reference's Grid."""
+    from groundtruth_gb300 import stack as gs
+    seeds = {"GND": [(4.0, 12.0), (10.1, 9.6), (2.9, 2.7)], "VCC": [(18.0, 4.0), (30.0, 30.0)], "NC": [(1.0, 1.0)]}
+    lines = {"SIG": [(np.array([[5.2, 14.3], [11.0, 16.1], [19.4, 20.2]]), 0.2)],
+             "GND": [(np.array([[3.0, 3.0], [3.0, 6.5], [6.0, 6.5]]), 0.25)],
+             "VCC": [(np.array([[2.8, 2.6], [17.9, 3.9]]), 0.3)]}
+    r = raster.build_layer(_layer_nets(), bbox, d, seeds, lines, sub)
+    g = gs.Grid(r.x0, r.y0, r.d, r.nx, r.ny, r.node, r.xb, r.yb, label=r.label, nets=r.nets)
+    near = []
+    for x, y in [(2.0, 2.0), (10.3, 9.1), (17.9, 4.1), (12.0, 17.6), (30.0, 5.0), (0.0, 24.0)]:
+        for net, dist in ((None, None), ("VCC", None), ("SIG", 1.0), ("GND", 0.3), ("NC", None)):
+            n = g.nearest_node(x, y, dist, net)
+            near.append((-1, -1) if n is None else n)
+    assert np.array_equal(np.array(near), Z[f"ly_{case}_near"])
+    assert [g.net_at(n) if n[0] >= 0 else "" for n in near] == list(Z[f"ly_{case}_net_at"])
+    assert np.allclose(g.extent, Z[f"ly_{case}_extent"], rtol=0, atol=1e-15)
