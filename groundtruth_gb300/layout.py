@@ -310,13 +310,19 @@ def _ancestors(parent):
     return depth
 
 
-def _lca(a, b, parent, depth):
-    while depth[a] > depth[b]:
-        a = parent[a]
-    while depth[b] > depth[a]:
-        b = parent[b]
-    while a != b:
-        a, b = parent[a], parent[b]
+def _lca(a: np.ndarray, b: np.ndarray, parent: np.ndarray, depth: np.ndarray) -> np.ndarray:
+    """The lowest common ancestor of fronts a[q] and b[q], for all q at once: the deeper one lifted to the
+    other's depth, then both together until they meet."""
+    a, b = a.copy(), b.copy()
+    for x, y in ((a, b), (b, a)):
+        m = depth[x] > depth[y]
+        while m.any():
+            x[m] = parent[x[m]]
+            m = depth[x] > depth[y]
+    m = a != b
+    while m.any():
+        a[m], b[m] = parent[a[m]], parent[b[m]]
+        m = a != b
     return a
 
 
@@ -336,16 +342,17 @@ def symbolic(t: Topology, S_pattern: sp.csr_matrix, leaf: int = 48) -> Symbolic:
     while True:
         fu, fv = owner[u], owner[v]
         diff = fu != fv
-        bad = []
-        for a, b, fa, fb in zip(u[diff], v[diff], fu[diff], fv[diff]):
-            l = _lca(fa, fb, parent, depth)
-            if l != fa and l != fb:
-                bad.append((a, b, l))
-        if not bad:
+        a, b, fa, fb = u[diff], v[diff], fu[diff], fv[diff]
+        l = _lca(fa, fb, parent, depth)
+        bad = (l != fa) & (l != fb)
+        if not bad.any():
             break
-        for a, b, l in bad:
-            owner[a] = l
-            owner[b] = l
+        # both ends of each such edge move to the ancestor, the edges taken in order (a node on several takes
+        # the last one's)
+        ends = np.stack([a[bad], b[bad]], axis=1).ravel()[::-1]
+        to = np.repeat(l[bad], 2)[::-1]
+        nodes, last = np.unique(ends, return_index=True)
+        owner[nodes] = to[last]
     nfront = len(parent)
     # factor order: fronts in postorder, within a front by (i, j, layer)
     key = np.lexsort((kept_dense // nxy, pos_j, pos_i, owner))
