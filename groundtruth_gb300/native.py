@@ -23,6 +23,18 @@ U8P = C.POINTER(C.c_uint8)
 DP = C.POINTER(C.c_double)
 
 
+def cap_fill_cells(st) -> "np.ndarray | None":
+    """gt_geometry_desc.cap_fill of a stack: per cell [n_pairs][nx][ny] of the C segment its capacitance's
+    facing copper share (1 elsewhere); None when every cell is whole."""
+    t, D = st.top, st.dense
+    share = t.cap_share
+    if share is None or not len(share) or not np.any(share != 1.0):
+        return None
+    cells = np.ones(len(t.pair_layers) * t.nx * t.ny)
+    cells[D.compact_to_dense[st.ns: st.ns + st.ncap] - D.off_c] = share
+    return cells
+
+
 class GeometryDesc(C.Structure):
     _fields_ = [("n_sheets", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32), ("n_pairs", C.c_int32),
                 ("n_branches", C.c_int32), ("precond_sheet", C.c_int32),
@@ -196,10 +208,8 @@ class Geometry:
         d.n_layers = st.N
         d.sheet_layer = _ptr(arr(st.sheet_layer, np.int32), C.c_int32)
         d.n_twins = len(st.twin_parent)
-        share = t.cap_share
-        if share is not None and len(share) and np.any(share != 1.0):
-            cells = np.ones(len(t.pair_layers) * nx * ny)
-            cells[D.compact_to_dense[st.ns: st.ns + st.ncap] - D.off_c] = share
+        cells = cap_fill_cells(st)
+        if cells is not None:
             d.cap_fill = _ptr(arr(cells, np.float64), C.c_double)
         h = P()
         check(lib, lib.gt_geometry_create(C.byref(d), C.byref(h)), "gt_geometry_create")

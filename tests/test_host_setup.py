@@ -204,3 +204,15 @@ def test_derived_stack_through_the_device_model():
     base = Multifrontal(dst, dst.sterm @ tab[: st.n_table])
     assert rel(m.to_compact(m.precond(x, tab, LowRank(m, base, zbr))), z["prod_precond"]) < 1e-9
     assert rel(m.to_compact(m.precond(x, tab, base)), z["prod_precond"]) > 1e-3     # the update matters
+
+
+def test_capacitance_shares_reach_the_device_cells():
+    """native.cap_fill_cells (the descriptor's cap_fill) puts each capacitance's facing share at its own cell of
+    the C segment, as the numpy device model applies it; None for whole cells."""
+    from groundtruth_gb300 import native
+    z, board = load("routed_pair")
+    st, _ = gs.from_board(board, _device=False)
+    cells = native.cap_fill_cells(st)
+    assert cells is not None and np.array_equal(cells, DenseModel(st).share.ravel())
+    st0, _ = gs.from_board(load("small_pair")[1], _device=False)
+    assert native.cap_fill_cells(st0) is None
