@@ -222,3 +222,18 @@ def test_not_converged_is_reported(name):
     sol = gs.solve_many(routes[:1], fs[:1], tol=board.tol)[0][0]
     assert sol.residual <= board.tol
     assert abs(sol.Z_loop - complex(z["Z0_0"])) <= 1e-8 * abs(complex(z["Z0_0"]))
+
+
+def test_repeated_solves_are_bit_identical():
+    """The reference's determinism checks (a repeated run gives identical numbers: test_numerics_audit.py:245-251,
+    test_speed.py:103-157): the same batch solved twice on one stack takes the same iterations and gives
+    bit-identical currents, potentials and loop impedances (fixed launch order, reductions in a fixed order)."""
+    z, board = load("small_pair")
+    st, routes = gs.from_board(board)
+    fs = [float(f) for f in board.freqs]
+    first = gs.solve_many(routes, fs, tol=board.tol)
+    again = gs.solve_many(routes, fs, tol=board.tol)
+    for pa, pb in zip(first, again):
+        for a, b in zip(pa, pb):
+            assert a.iterations == b.iterations and a.Z_loop == b.Z_loop
+            assert np.array_equal(a.I_x, b.I_x) and np.array_equal(a.I_y, b.I_y) and np.array_equal(a.V, b.V)
