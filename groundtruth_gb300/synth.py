@@ -607,6 +607,35 @@ def necked_pair(seed: int = 17) -> Board:
     return b
 
 
+def track_rail(length_mm: float, width_mm: float, angle: float = 0.0, dy: float = 0.0, d_mm: float = 0.5,
+               sub: int = 4) -> Board:
+    """A copper track `width_mm` wide and `length_mm` long at `angle` degrees between two 1 x 1 mm pads (the
+    reference's track-width rail, tests/test_track_width.py:58-70: one layer, no plane), rasterised with its
+    exact widths (raster.build_layer at sub-grid `sub`, the centreline forced as a track); `dy` moves it off the
+    grid's rows.  Its one net has no trace and its ends at the pads' nodes, for the DC resistance at 0 Hz."""
+    from . import raster
+    a = math.radians(angle)
+    x0, y0 = 3.0, 3.0 + dy
+    x1, y1 = x0 + length_mm * math.cos(a), y0 + length_mm * math.sin(a)
+    h = width_mm / 2
+    u = np.array([-0.5, 0.5, 0.5, length_mm - 0.5, length_mm - 0.5, length_mm + 0.5, length_mm + 0.5,
+                  length_mm - 0.5, length_mm - 0.5, 0.5, 0.5, -0.5])
+    v = np.array([-0.5, -0.5, -h, -h, -0.5, -0.5, 0.5, 0.5, h, h, 0.5, 0.5])
+    outline = np.stack([x0 + math.cos(a) * u - math.sin(a) * v, y0 + math.sin(a) * u + math.cos(a) * v], 1)
+    bbox = (0.0, 0.0, x1 + 3.0, max(y1 + 3.0, 6.0))
+    g = raster.build_layer({"PWR": [(outline, [])]}, bbox, d_mm,
+                           lines={"PWR": [(np.array([[x0, y0], [x1, y1]]), width_mm)]}, sub=sub)
+    grid_nodes = np.argwhere(g.node)
+
+    def node_at(x, y):
+        k = int(np.argmin((grid_nodes[:, 0] * d_mm - x) ** 2 + (grid_nodes[:, 1] * d_mm - y) ** 2))
+        return (0, int(grid_nodes[k, 0]), int(grid_nodes[k, 1]))
+    layer = Layer("F", 0.0, 35e-6, g.node, g.xb, g.yb, g.widths(), g.fill, g.area, g.label)
+    net = Net(np.zeros((0, 8)), node_at(x0, y0), node_at(x1, y1))
+    return Board(f"track_rail{length_mm:g}", d_mm * 1e-3, g.nx, g.ny, [layer], nets=[net], freqs=np.array([0.0]),
+                 precond="diag", tol=1e-10, restart=50)
+
+
 def routed_pair(sub: int = 4) -> Board:
     """A plane pair rasterised from polygons by raster.build_layer (GroundTruth's build_grid) at sub-grid `sub`,
     with the copper's exact widths: a GND pour (a slanted slot, a square hole, a notched corner with a pad in it

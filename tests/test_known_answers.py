@@ -3,7 +3,8 @@ restated on a 40 x 20 mm plane under a microstrip (synth.microstrip): the strip 
 the return current under the trace against image theory, the loop inductance against Wheeler's formula and
 the moment against the loop's area, current spreading at low frequency, a slot's monotonic effect, a cut from
 the edge turning the loop into the board plane, a fully cut plane refused, a plane pair's inductance per
-length (tests/test_plane_pair.py:70-81), and the reciprocity of two loops' mutual impedance.  Each runs on the oracle (CPU)
+length (tests/test_plane_pair.py:70-81), a track's resistance from its rasterised copper
+(tests/test_track_width.py:91-157), and the reciprocity of two loops' mutual impedance.  Each runs on the oracle (CPU)
 and, marked gpu, through the CUDA library."""
 import math
 from pathlib import Path
@@ -138,6 +139,20 @@ def test_known_answer_boards_match_the_reference(solve, name):
         Zr, mr = complex(ref[f"{name}_Z{q}"]), ref[f"{name}_m{q}"]
         assert abs(Z - Zr) <= 1e-8 * abs(Zr), (name, f, Z, Zr)
         assert np.linalg.norm(m - mr) <= 1e-6 * np.linalg.norm(mr), (name, f)
+
+
+@pytest.mark.parametrize("width, angle, dy, tol", [(0.4, 0.0, 0.0, 0.01), (0.1, 0.0, 0.03, 0.01),
+                                                    (0.05, 0.0, 0.06, 0.01), (0.4, 30.0, 0.0, 0.015),
+                                                    (0.15, 45.0, 0.0, 0.015), (0.1, 30.0, 0.0, 0.015)])
+@pytest.mark.parametrize("solve", SOLVERS)
+def test_a_track_has_the_resistance_of_its_cross_section(solve, width, angle, dy, tol):
+    """test_track_width.py:91-157 (TW-1, TW-3): a track rasterised from its copper with exact widths (0.5 mm
+    pitch, 0.125 mm sub-grid), 0.4, 0.1 or 0.05 mm wide, on or off the grid's rows, straight or at 30 or 45
+    degrees (a staircase of x and y strips, each as wide as the border its copper crosses), has the resistance
+    per length 1 / (sigma w t): the difference of a 40 and a 20 mm track's DC resistances over 20 mm, within
+    1 % (straight) / 1.5 % (at an angle)."""
+    r = [solve(synth.track_rail(length, width, angle, dy), 0.0)[1].real for length in (20.0, 40.0)]
+    assert (r[1] - r[0]) / 0.020 == pytest.approx(1 / (5.8e7 * width * 1e-3 * 35e-6), rel=tol)
 
 
 def _two_loops_oracle(board, f):
