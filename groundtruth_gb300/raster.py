@@ -358,8 +358,8 @@ def exact_copper(nets: list, label: np.ndarray, xb: np.ndarray, yb: np.ndarray, 
 
 def coarse_from_fine(nets: list, x0: float, y0: float, d: float, nx: int, ny: int, s: int) -> tuple:
     """Cells, their nets and the copper joining neighbours from a sub-grid of pitch d / s (GroundTruth's
-    _coarse_from_fine, peec.py:774-849).  nets[k] = (outline, holes) polygons of net k (None: none), points of
-    the sub-grid inside them (strictly, holes closed: synth.copper_at) take the first net that holds them.
+    _coarse_from_fine, peec.py:774-849).  nets[k] = net k's copper (a polygon (outline, holes), a list of them, or
+    None), points of the sub-grid inside it (strictly, holes closed: synth.copper_at) take the first net that holds them.
     Returns (label (nx, ny): each cell's net, its largest piece of one net's sub-grid copper inside the cell when
     that spans at least s sub-grid points, else -1; cross_x (nx-1, ny) / cross_y (nx, ny-1): the fraction of
     the s sub-grid strips across the border two cells' kept pieces join by; fill (nx, ny): the kept piece's share
@@ -375,16 +375,19 @@ def coarse_from_fine(nets: list, x0: float, y0: float, d: float, nx: int, ny: in
     for k, poly in enumerate(nets):
         if poly is None:
             continue
-        outline, holes = np.asarray(poly[0], float), [np.asarray(h, float) for h in poly[1]]
-        bx0, by0 = outline.min(axis=0)
-        bx1, by1 = outline.max(axis=0)
+        polys = polygons_of(poly)
+        bx0, by0 = np.min([np.min(np.asarray(o, float), axis=0) for o, _ in polys], axis=0)
+        bx1, by1 = np.max([np.max(np.asarray(o, float), axis=0) for o, _ in polys], axis=0)
         p0, p1 = max(int(math.floor((bx0 - xf[0]) / df)) - 1, 0), min(int(math.ceil((bx1 - xf[0]) / df)) + 2, mx)
         q0, q1 = max(int(math.floor((by0 - yf[0]) / df)) - 1, 0), min(int(math.ceil((by1 - yf[0]) / df)) + 2, my)
         if p0 >= p1 or q0 >= q1:
             continue
         X, Y = np.meshgrid(xf[p0:p1], yf[q0:q1], indexing="ij")
         win = fine[p0:p1, q0:q1]
-        win[copper_at(X, Y, outline, holes) & (win < 0)] = k
+        inside = np.zeros(X.shape, bool)
+        for outline, holes in polys:
+            inside |= copper_at(X, Y, np.asarray(outline, float), [np.asarray(h, float) for h in holes])
+        win[inside & (win < 0)] = k
     same_x = (fine[:-1, :] >= 0) & (fine[:-1, :] == fine[1:, :])         # sub-grid strips within one net
     same_y = (fine[:, :-1] >= 0) & (fine[:, :-1] == fine[:, 1:])
     border_x = ((np.arange(mx - 1) + 1) % s == 0)[:, None]                # ... that cross a cell border
@@ -430,14 +433,81 @@ def coarse_from_fine(nets: list, x0: float, y0: float, d: float, nx: int, ny: in
     return label.reshape(nx, ny), cross_x, cross_y, fill.reshape(nx, ny), off_x, off_y
 
 
-def _covers(px, py, poly) -> np.ndarray:
-    """Points inside a polygon (outline, holes) or on its border (shapely's covers)."""
+PIECE_TOL = 0.005    # peec.py:106: copper of one net within this of itself (mm) is one piece (touching fills)
+
+
+def polygons_of(piece) -> list:
+    """A piece's polygons: a polygon (outline, holes) alone (its outline's first vertex a pair of numbers), or a
+    list of them."""
+    return [piece] if np.isscalar(piece[0][0][0]) else list(piece)
+
+
+def _segment_distance(a0, a1, b0, b1) -> np.ndarray:
+    """Distances between 2D segments a0-a1 (n, 2) and b0-b1 (m, 2), all pairs (n, m): 0 where they cross, else
+    the least of the four end-to-segment distances."""
+    def to_segment(p, q0, q1):
+        d = q1 - q0
+        t = np.clip(np.einsum("nmk,mk->nm", p[:, None, :] - q0[None], d) / np.maximum(np.einsum("mk,mk->m", d, d),
+                                                                                      1e-300), 0.0, 1.0)
+        return np.hypot(*np.moveaxis(p[:, None, :] - (q0[None] + t[..., None] * d[None]), -1, 0))
+
+    def cross(o, p, q):
+        return (p[..., 0] - o[..., 0]) * (q[..., 1] - o[..., 1]) - (p[..., 1] - o[..., 1]) * (q[..., 0] - o[..., 0])
+    A0, A1, B0, B1 = a0[:, None], a1[:, None], b0[None], b1[None]
+    hit = ((cross(A0, A1, B0) * cross(A0, A1, B1) < 0) & (cross(B0, B1, A0) * cross(B0, B1, A1) < 0))
+    dist = np.minimum(np.minimum(to_segment(a0, b0, b1), to_segment(a1, b0, b1)),
+                      np.minimum(to_segment(b0, a0, a1).T, to_segment(b1, a0, a1).T))
+    return np.where(hit, 0.0, dist)
+
+
+def _polygon_distance(p, q) -> float:
+    """The distance between two polygons (outline, holes): 0 where their copper meets or one holds the other's
+    outline, else the least distance between their rings."""
+    pa, pb = ring_edges(*p)
+    qa, qb = ring_edges(*q)
+    if bool(_covers(qa[:1, 0], qa[:1, 1], p)[0]) or bool(_covers(pa[:1, 0], pa[:1, 1], q)[0]):
+        return 0.0
+    return float(_segment_distance(pa, pb, qa, qb).min())
+
+
+def pieces(polygons: list, tol: float = PIECE_TOL) -> list:
+    """One net's polygons grouped into its connected pieces of copper (GroundTruth's _pieces, peec.py:852-873):
+    polygons that meet or lie within tol of each other (transitively) are one piece, a list of polygons; a lone
+    polygon is a piece by itself.  The polygons are those of the net's union (not overlapping)."""
+    n = len(polygons)
+    if n <= 1:
+        return [p for p in polygons]
+    group = list(range(n))
+
+    def root(i):
+        while group[i] != i:
+            group[i] = group[group[i]]
+            i = group[i]
+        return i
+    box = [(np.min(np.asarray(o, float), axis=0) - tol, np.max(np.asarray(o, float), axis=0) + tol) for o, _ in polygons]
+    for i in range(n):
+        for j in range(i + 1, n):
+            if np.any(box[i][1] < box[j][0]) or np.any(box[j][1] < box[i][0]):
+                continue
+            if root(i) != root(j) and _polygon_distance(polygons[i], polygons[j]) <= tol:
+                group[max(root(i), root(j))] = min(root(i), root(j))
+    out = {}
+    for i in range(n):
+        out.setdefault(root(i), []).append(polygons[i])
+    return [members[0] if len(members) == 1 else members for members in out.values()]
+
+
+def _covers(px, py, piece) -> np.ndarray:
+    """Points inside a piece's copper or on its border (shapely's covers)."""
     from .synth import polygon_contains
-    ins, on = polygon_contains(px, py, np.asarray(poly[0], float))
-    out = ins | on
-    for h in poly[1]:
-        hin, _ = polygon_contains(px, py, np.asarray(h, float))
-        out &= ~hin
+    out = np.zeros(np.shape(px), bool)
+    for outline, holes in polygons_of(piece):
+        ins, on = polygon_contains(px, py, np.asarray(outline, float))
+        cov = ins | on
+        for h in holes:
+            hin, _ = polygon_contains(px, py, np.asarray(h, float))
+            cov &= ~hin
+        out |= cov
     return out
 
 
@@ -445,8 +515,9 @@ def _inside(X, Y, pieces: list) -> np.ndarray:
     """Points strictly inside any of the pieces (outline minus closed holes)."""
     from .synth import copper_at
     out = np.zeros(np.shape(X), bool)
-    for outline, holes in pieces:
-        out |= copper_at(X, Y, np.asarray(outline, float), [np.asarray(h, float) for h in holes])
+    for piece in pieces:
+        for outline, holes in polygons_of(piece):
+            out |= copper_at(X, Y, np.asarray(outline, float), [np.asarray(h, float) for h in holes])
     return out
 
 
@@ -485,8 +556,8 @@ class LayerRaster:
 def build_layer(nets: dict, bbox: tuple, d: float, seeds: Optional[dict] = None, lines: Optional[dict] = None,
                 sub: int = 1) -> LayerRaster:
     """A layer's copper on a grid of pitch d over bbox (x0, y0, x1, y1) (GroundTruth's build_grid,
-    peec.py:329-449, heat points left out).  nets {net: [piece (outline, holes), ...]}: each net's copper as its
-    connected pieces (polygons, in the unit of d); seeds {net: [(x, y)]}: points whose nearest free node becomes
+    peec.py:329-449, heat points left out).  nets {net: [piece, ...]}: each net's copper as its connected pieces
+    (a polygon (outline, holes) or a list of polygons, in the unit of d; pieces() groups a net's polygons); seeds {net: [(x, y)]}: points whose nearest free node becomes
     the net's (a via ring or pad smaller than the grid); lines {net: [(polyline, width)]}: tracks claimed by
     rasterise_tracks.  sub = 1: a node is a net's when its point lies inside the net's copper (the first net
     keeps it), a strip when its midpoint does too; sub > 1: cells, joins and offsets from the sub-grid
@@ -514,8 +585,9 @@ def build_layer(nets: dict, bbox: tuple, d: float, seeds: Optional[dict] = None,
         for k, ps in enumerate(per_net):
             if not ps:
                 continue
-            lo = np.min([np.min(np.asarray(o, float), axis=0) for o, _ in ps], axis=0)
-            hi = np.max([np.max(np.asarray(o, float), axis=0) for o, _ in ps], axis=0)
+            outlines = [np.asarray(o, float) for piece in ps for o, _ in polygons_of(piece)]
+            lo = np.min([o.min(axis=0) for o in outlines], axis=0)
+            hi = np.max([o.max(axis=0) for o in outlines], axis=0)
             i0, i1 = max(int(math.floor((lo[0] - x0) / d)) - 1, 0), min(int(math.ceil((hi[0] - x0) / d)) + 2, nx)
             j0, j1 = max(int(math.floor((lo[1] - y0) / d)) - 1, 0), min(int(math.ceil((hi[1] - y0) / d)) + 2, ny)
             if i0 >= i1 or j0 >= j1:
@@ -572,7 +644,7 @@ def build_layer(nets: dict, bbox: tuple, d: float, seeds: Optional[dict] = None,
     if fine:
         edges = []
         for ps in per_net:
-            rings = [ring_edges(o, h) for o, h in ps]
+            rings = [ring_edges(o, h) for piece in ps for o, h in polygons_of(piece)]
             edges.append((np.concatenate([a for a, _ in rings]), np.concatenate([b for _, b in rings]))
                          if rings else None)
         ex_x, ex_y, area, kx, ky = exact_copper(edges, label, xb, yb, x0, y0, d)

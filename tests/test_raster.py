@@ -254,3 +254,50 @@ def test_grid_lookups_match_reference(case, bbox, d, sub):
     assert np.array_equal(np.array(near), Z[f"ly_{case}_near"])
     assert [g.net_at(n) if n[0] >= 0 else "" for n in near] == list(Z[f"ly_{case}_net_at"])
     assert np.allclose(g.extent, Z[f"ly_{case}_extent"], rtol=0, atol=1e-15)
+
+
+def _box(x0, y0, x1, y1):
+    return (np.array([[x0, y0], [x1, y0], [x1, y1], [x0, y1]]), [])
+
+
+def test_pieces_group_copper_that_touches():
+    """raster.pieces (peec.py:852-873): polygons within PIECE_TOL (5 um) of each other, or inside one another's
+    copper, are one piece (transitively); a real gap keeps them apart."""
+    a, b, c = _box(0, 0, 10, 4), _box(10 + 1e-7, 0, 20, 4), _box(20.003, 0, 30, 4)
+    assert len(raster.pieces([a, b, c])) == 1                        # a-b touch, b-c 3 um apart
+    assert len(raster.pieces([a, _box(10.02, 0, 20, 4)])) == 2      # 20 um: two pieces
+    island = _box(3, 1, 4, 2)
+    ring = (np.array([[0.0, 0.0], [8.0, 0.0], [8.0, 8.0], [0.0, 8.0]]), [np.array([[2.0, 2.0], [6.0, 2.0],
+                                                                                   [6.0, 6.0], [2.0, 6.0]])])
+    assert len(raster.pieces([ring, _box(3, 3, 4, 4)])) == 2       # an island in a hole, 1 mm off its edge
+    assert len(raster.pieces([_box(0, 0, 8, 8), island])) == 1      # inside the copper
+    assert raster.pieces([a]) == [a]
+
+
+def _dc_drop(layer_nets, drive, sink, d=0.5, sub=4, bbox=(0, 0, 30, 12)):
+    """The DC resistance between two points of a one-layer copper rasterised by build_layer (oracle solve)."""
+    from test_oracle_golden import oracle_routes, oracle_stack
+    from groundtruth_gb300 import stack as gs, synth
+    g = raster.build_layer(layer_nets, bbox, d, sub=sub)
+    grid = gs.Grid(0.0, 0.0, d, g.nx, g.ny, g.node, g.xb, g.yb, **g.widths(), fill=g.fill, area=g.area)
+    ends = [(0, *grid.nearest_node(*p)) for p in (drive, sink)]
+    board = synth.Board("rail", d * 1e-3, g.nx, g.ny, [synth.Layer("F", 0.0, 35e-6, g.node, g.xb, g.yb, g.widths(),
+                                                                   g.fill, g.area, g.label)],
+                        nets=[synth.Net(np.zeros((0, 8)), *ends)], freqs=np.array([0.0]), tol=1e-12)
+    gs.from_board(board, _device=False)              # the host's checks (connectivity) first
+    return oracle_routes(oracle_stack(board), board)[0].solve(0.0, tol=1e-12)["Z_loop"].real
+
+
+@pytest.mark.parametrize("gap, joined", [(1e-7, True), (0.02, False)])
+def test_copper_that_touches_is_one_piece_and_a_real_gap_is_not(gap, joined):
+    """test_track_width.py:263-285 (TW-12): two 10 x 4 mm fills end to end, gap apart, fed at either end:
+    1e-7 mm apart they conduct as one 20 mm fill (the DC drop within 0.5 %), 0.02 mm apart they are not
+    connected."""
+    from groundtruth_gb300.stack import SolverError
+    fills = raster.pieces([_box(5.0, 4.0, 15.0, 8.0), _box(15.0 + gap, 4.0, 25.0, 8.0)])
+    if not joined:
+        with pytest.raises(SolverError, match="not connected"):
+            _dc_drop({"PWR": fills}, (6.0, 6.0), (24.0, 6.0))
+        return
+    whole = _dc_drop({"PWR": [_box(5.0, 4.0, 25.0, 8.0)]}, (6.0, 6.0), (24.0, 6.0))
+    assert _dc_drop({"PWR": fills}, (6.0, 6.0), (24.0, 6.0)) == pytest.approx(whole, rel=0.005)
