@@ -1,0 +1,124 @@
+"""A plane between two others screens one side's field from the other: the face sheets of a screened layer
+(GroundTruth: PlaneStack._faces, peec.py:1658-1716), against the one-dimensional exact values of a stack of
+conducting slabs, as the reference's own tests state them (tests/test_plane_screening.py:1-28, 152-203).
+
+Each case is a plane line: layers 10 mm wide rasterised from their copper (raster.build_layer, 0.4 mm pitch,
+sub-grid 4), the VDD layer fed along its whole first column and shorted to the GND layer(s) along its last, two
+lengths, their difference the line's inductance per length alone:
+
+  * GND / VDD / GND, 0.1 mm gaps, 70 um copper: the middle plane returns half its current on each face,
+        L' = (mu0 d + Li(t) + Li(t/2)) / 2w,  Li(t) the one-face slab's internal inductance;
+  * VDD / floating plane / GND, 0.2 mm gaps, 35 um copper: the floating plane's faces carry eddy currents,
+        L' = (mu0 2d + 2 Li(t) + Im(2 (k/sigma) tanh(k t/2)) / omega) / w,  k = (1 + j)/delta,
+    transparent at low frequency and screening at high.
+
+The ratios L'(f) / L'(1 MHz) against the exact ones cancel the field's fringing past the strips' edges; solved
+by the oracle and, marked gpu, through the CUDA library."""
+import math
+
+import numpy as np
+import pytest
+
+from groundtruth_gb300 import raster, stack as gs
+from oracle import peec_oracle as po
+
+MU0, SIGMA = 4e-7 * math.pi, 5.8e7
+W, PITCH = 10.0, 0.4
+FREQS = (1e4, 1e6, 3e7, 1e8)
+
+
+def _layers(stack, gaps, length):
+    """[(name, z m, grid, t m)] top down: each layer's copper a box length x W mm, rasterised."""
+    out, z = [], 0.0
+    box = (np.array([[0.0, 0.0], [length, 0.0], [length, W], [0.0, W]]), [])
+    for k, (net, t) in enumerate(stack):
+        if k:
+            z -= (0.5 * stack[k - 1][1] + gaps[k - 1] + 0.5 * t) * 1e-3
+        g = raster.build_layer({net: [box]}, (0.0, 0.0, length, W), PITCH, sub=4)
+        out.append((net, z, g, t * 1e-3))
+    return out
+
+
+def _ends(stack, g):
+    """The shorts at the far end (VDD to every GND, 1 nOhm per node), the GND layers joined at the feed, and the
+    feed: 1/ny A into VDD's and out of the first GND's first column."""
+    nx, ny = g.nx, g.ny
+    vdd = [k for k, (n, _) in enumerate(stack) if n == "VDD"][0]
+    gnd = [k for k, (n, _) in enumerate(stack) if n == "GND"]
+    shorts = [((vdd, nx - 1, j), (k, nx - 1, j)) for j in range(ny) for k in gnd]
+    shorts += [((gnd[0], 0, j), (k, 0, j)) for j in range(ny) for k in gnd[1:]]
+    feed = [((vdd, 0, j), 1.0 / ny) for j in range(ny)] + [((gnd[0], 0, j), -1.0 / ny) for j in range(ny)]
+    return shorts, feed
+
+
+def _oracle_line(stack, gaps, length):
+    layers = _layers(stack, gaps, length)
+    g = layers[0][2]
+    shorts, feed = _ends(stack, g)
+    st = po.OracleStack([po.OLayer(z, t, l.node, l.xb, l.yb, l.widths(), l.fill) for _, z, l, t in layers],
+                        PITCH * 1e-3, [po.OBranch(a, b, 1e-9, 0.0) for a, b in shorts], screen=True)
+    J = np.zeros(st.n_nodes)
+    for node, amps in feed:
+        J[st.nid[node]] += amps
+    out = {}
+    for f in FREQS:
+        Ib, V, its, x = st.solve(f, np.zeros(st.nb, complex), J, tol=1e-5)
+        out[f] = complex(sum(amps * V[st.nid[node]] for node, amps in feed))
+    return out
+
+
+def _device_line(stack, gaps, length):
+    layers = _layers(stack, gaps, length)
+    g = layers[0][2]
+    shorts, feed = _ends(stack, g)
+    grid = lambda l: gs.Grid(0.0, 0.0, PITCH, l.nx, l.ny, l.node, l.xb, l.yb, **l.widths(), fill=l.fill,  # noqa: E731
+                             area=l.area)
+    st = gs.PlaneStack([gs.PlaneLayer(n, z, grid(l), t) for n, z, l, t in layers],
+                       [gs.Branch(a, b, lambda f: 1e-9 + 0j) for a, b in shorts], screen=True)
+    route = gs.RouteExcitation(st, [], injections=feed)
+    return {f: s.Z_loop for f, s in zip(FREQS, gs.solve_many([route], list(FREQS), tol=1e-5)[0])}
+
+
+def _per_length(line, stack, gaps):
+    a, b = line(stack, gaps, 20.0), line(stack, gaps, 40.0)
+    return {f: ((b[f] - a[f]).imag / (2 * math.pi * f)) / 20e-3 for f in FREQS}
+
+
+def _li(t, f):
+    """The one-face slab's internal inductance per square: Im((1+j)/(sigma delta) coth((1+j) t/delta)) / omega."""
+    delta = 1 / math.sqrt(math.pi * f * MU0 * SIGMA)
+    u = (1 + 1j) * t / delta
+    return (u * (1 + np.exp(-2 * u)) / (1 - np.exp(-2 * u)) / (SIGMA * t)).imag / (2 * math.pi * f)
+
+
+def _eddy(t, f):
+    """The floating slab's mode: Im(2 (k/sigma) tanh(k t/2)) / omega per square."""
+    k = (1 + 1j) * math.sqrt(math.pi * f * MU0 * SIGMA)
+    return (2 * k / SIGMA * np.tanh(k * t / 2)).imag / (2 * math.pi * f)
+
+
+LINES = [pytest.param(_oracle_line, id="oracle"), pytest.param(_device_line, id="gpu", marks=pytest.mark.gpu)]
+
+
+@pytest.mark.parametrize("line", LINES)
+def test_a_plane_between_two_others_returns_on_both_faces(line):
+    """GND / VDD / GND: L'(f) / L'(1 MHz) within 1 % of the exact ratio from 10 kHz to 100 MHz, L' within -3 / +5 %
+    of the exact (one-dimensional) value."""
+    per = _per_length(line, [("GND", 0.07), ("VDD", 0.07), ("GND", 0.07)], [0.1, 0.1])
+    exact = {f: (MU0 * 0.1e-3 + _li(70e-6, f) + _li(35e-6, f)) / (2 * W * 1e-3) for f in FREQS}
+    for f in FREQS:
+        assert abs((per[f] / per[1e6]) / (exact[f] / exact[1e6]) - 1) < 0.01, f
+        assert 0.97 < per[f] / exact[f] < 1.05, f
+
+
+@pytest.mark.parametrize("line", LINES)
+def test_a_floating_plane_screens_at_high_frequency_and_lets_the_field_through_at_low(line):
+    """VDD / floating / GND against the same stack without the floating plane: the exact ratio within 1 % at every
+    frequency, 1 within 1e-3 at 10 kHz (transparent), below 0.965 at 30 MHz (its faces' eddy currents)."""
+    per = _per_length(line, [("VDD", 0.035), ("AUX", 0.035), ("GND", 0.035)], [0.2, 0.2])
+    none = _per_length(line, [("VDD", 0.035), ("GND", 0.035)], [0.435])
+    for f in FREQS:
+        exact = (MU0 * 0.4e-3 + 2 * _li(35e-6, f) + _eddy(35e-6, f)) / (MU0 * 0.435e-3 + 2 * _li(35e-6, f))
+        assert abs((per[f] / none[f]) / exact - 1) < 0.01, f
+    assert abs(per[1e4] / none[1e4] - 1) < 1e-3
+    assert per[3e7] / none[3e7] < 0.965
