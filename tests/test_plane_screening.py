@@ -122,3 +122,61 @@ def test_a_floating_plane_screens_at_high_frequency_and_lets_the_field_through_a
         assert abs((per[f] / none[f]) / exact - 1) < 0.01, f
     assert abs(per[1e4] / none[1e4] - 1) < 1e-3
     assert per[3e7] / none[3e7] < 0.965
+
+
+def _six_planes(screen: bool, d: float = 2.0):
+    """Six planes (GND / VDD alternating, 35 um copper, 0.1 / 0.535 / 0.1 / 0.535 / 0.1 mm of dielectric) 24 x 16 mm
+    on d mm cells (the grid cut at the board's edge: edge strips narrower than the pitch), the plane pairs'
+    capacitance, VDD shorted to GND at one end and fed at the other ('sheet' preconditioner), on the oracle:
+    (OracleStack, J)."""
+    names = ["GND", "VDD", "GND", "VDD", "GND", "VDD"]
+    gaps = [0.1, 0.535, 0.1, 0.535, 0.1]
+    t, length, width = 0.035, 24.0, 16.0
+    box = (np.array([[0.0, 0.0], [length, 0.0], [length, width], [0.0, width]]), [])
+    layers, z = [], 0.0
+    for k, net in enumerate(names):
+        if k:
+            z -= (t + gaps[k - 1]) * 1e-3
+        g = raster.build_layer({net: [box]}, (0.0, 0.0, length, width), d, sub=4)
+        layers.append(po.OLayer(z, t * 1e-3, g.node, g.xb, g.yb, g.widths(), g.fill))
+    nx, ny = g.nx, g.ny
+    vdd = [k for k, n in enumerate(names) if n == "VDD"]
+    gnd = [k for k, n in enumerate(names) if n == "GND"]
+    ends = [((vdd[0], nx - 1, j), (k, nx - 1, j)) for j in range(ny) for k in gnd]
+    ends += [((vdd[0], 0, j), (k, 0, j)) for j in range(ny) for k in vdd[1:]]
+    ends += [((gnd[0], 0, j), (k, 0, j)) for j in range(ny) for k in gnd[1:]]
+    pairs = [po.OPair(k, k + 1, 8.854e-12 * 4.3 / (gaps[k] * 1e-3), 0.02) for k in range(5)]
+    st = po.OracleStack(layers, d * 1e-3, [po.OBranch(a, b, 1e-9, 0.0) for a, b in ends], pairs, precond="sheet",
+                        screen=screen)
+    J = np.zeros(st.n_nodes)
+    for j in range(ny):
+        J[st.nid[(vdd[0], 0, j)]] += 1.0 / ny
+        J[st.nid[(gnd[0], 0, j)]] -= 1.0 / ny
+    return st, J
+
+
+def test_the_face_pairs_difference_inductance_stays_positive_beside_narrow_strips():
+    """test_plane_screening.py:256-276: a split layer's two faces share the narrow-strip corrections, so the
+    difference mode (the free space between the faces, about mu0 t / 2 per face) stays positive definite at 15-25
+    pH per square and the whole partial-inductance matrix with it."""
+    st, _ = _six_planes(True)
+    assert len(st.tw_b) and st.dL is not None and np.any(st.dL != 0)
+    L = np.stack([st.Lp_matvec(np.eye(st.ns)[i].astype(complex)).real for i in range(st.ns)], axis=1)
+    a, b = st.tw_a, st.tw_b
+    assert abs(L - L.T).max() < 1e-12 * abs(L).max()
+    diff = 0.5 * (L[np.ix_(a, a)] + L[np.ix_(b, b)] - L[np.ix_(a, b)] - L[np.ix_(b, a)])
+    w = np.linalg.eigvalsh(diff)
+    assert 15e-12 < w.min() and w.max() < 25e-12, (w.min(), w.max())
+    assert np.linalg.eigvalsh(L).min() > 0.0
+
+
+def test_a_split_stack_needs_about_the_iterations_of_the_unsplit_one():
+    """test_plane_screening.py:279-288: the 'sheet' preconditioner on the six planes with and without face sheets
+    takes within 1.3 x the iterations (GMRES to 1e-5) at 20, 100 and 400 MHz."""
+    split, Js = _six_planes(True)
+    plain, Jp = _six_planes(False)
+    assert split.n_sheets == 10 and plain.n_sheets == 6
+    for f in (2e7, 1e8, 4e8):
+        its_s = split.solve(f, np.zeros(split.nb, complex), Js, tol=1e-5)[2]
+        its_p = plain.solve(f, np.zeros(plain.nb, complex), Jp, tol=1e-5)[2]
+        assert its_s <= 1.3 * its_p + 1, (f, its_s, its_p)
