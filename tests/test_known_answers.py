@@ -316,3 +316,67 @@ def test_dc_limit_is_the_resistive_sheet(solve):
     r_trace = greens.trace_resistance(seg, 0.0, b.sigma, b.nets[0].trace_t)
     assert Z.imag == pytest.approx(0.0, abs=1e-12)
     assert Z.real - r_trace == pytest.approx(_dc_drop(b), rel=1e-8)
+
+
+def _solution_oracle(board, f, route=None):
+    """The oracle's solve of a board's first net (or `route` on the host stack) as the mirror's Solution."""
+    st, routes = gs.from_board(board, _device=False)
+    r = route(st) if route is not None else routes[0]
+    ost = oracle_stack(board)
+    Ib, V, its, x = ost.solve(f, r.rhs_top(f), r.J(), tol=board.tol)
+    return r.solution(f, Ib, V, its)
+
+
+def _solution_device(board, f, route=None):
+    st, routes = gs.from_board(board)
+    r = route(st) if route is not None else routes[0]
+    return r.solve(f, tol=board.tol)
+
+
+SOLUTIONS = [pytest.param(_solution_oracle, id="oracle"),
+             pytest.param(_solution_device, id="gpu", marks=pytest.mark.gpu)]
+
+
+@pytest.mark.parametrize("solve", SOLUTIONS)
+def test_the_return_current_flows_back_under_the_trace(solve):
+    """test_vectors.py:42-54: at 100 MHz the plane's current at the dominant phase flows -x right under the +x
+    trace, sums across the plane to the whole signal current back, and carries the full magnitude there; the
+    same currents turned by any phase give the same vectors (test_vectors.py:57-68)."""
+    import dataclasses
+    b = synth.microstrip()
+    b.tol = 1e-8
+    sol = solve(b, 1e8)
+    d_mm = b.d * 1e3
+    kx, ky = sol.sheet_vectors(0, d_mm)
+    i, j = 80, 40
+    assert kx[i, j] < 0 and abs(ky[i, j]) < 0.01 * abs(kx[i, j])
+    assert float(np.sum(kx[i, :]) * b.d) == pytest.approx(-1.0, abs=0.02)
+    y = np.arange(b.ny) * b.d - 10e-3
+    near = np.abs(y) < 3 * H
+    assert np.allclose(np.hypot(kx, ky)[i, near], sol.sheet_current(0, d_mm)[i, near], rtol=0.01)
+    for theta in (0.6, -1.2):
+        turned = dataclasses.replace(sol, I_x=sol.I_x * np.exp(1j * theta), I_y=sol.I_y * np.exp(1j * theta))
+        tx, ty = turned.sheet_vectors(0, d_mm)
+        assert np.allclose(tx, kx, atol=1e-9 * np.abs(kx).max()) and np.allclose(ty, ky, atol=1e-9 * np.abs(kx).max())
+
+
+@pytest.mark.parametrize("solve", SOLUTIONS)
+def test_a_node_where_current_enters_reads_its_strips_heat(solve):
+    """test_density_maps.py:106-123: 1 A into the middle of a 10 x 10 mm plane (0.25 mm cells), out at four nodes
+    near its corners: the mean of the middle node's four strips cancels (0), the heat-consistent density (copper)
+    is sqrt(1/8)/d there (four strips of 0.25 A), highest where the current enters, and away from the feed both
+    definitions agree."""
+    n, d_mm = 41, 0.25
+    node = np.ones((n, n), bool)
+    layer = synth.Layer("F", 0.0, 35e-6, node, np.ones((n - 1, n), bool), np.ones((n, n - 1), bool))
+    board = synth.Board("feed", d_mm * 1e-3, n, n, [layer], freqs=np.array([10.0]), tol=1e-10)
+    c = (0, n // 2, n // 2)
+    out = [(0, 2, 2), (0, n - 3, 2), (0, 2, n - 3), (0, n - 3, n - 3)]
+    route = lambda st: gs.RouteExcitation(st, [], injections=[(c, 1.0)] + [(k, -0.25) for k in out])  # noqa: E731
+    sol = solve(board, 10.0, route)
+    i, j = c[1], c[2]
+    assert sol.sheet_current(0, d_mm)[i, j] == pytest.approx(0.0, abs=1e-6)
+    heat = sol.sheet_current(0, d_mm, True)
+    assert heat[i, j] == pytest.approx(math.sqrt(1 / 8) / (d_mm * 1e-3), rel=1e-6)
+    assert heat[i, j] > heat[i + 1, j] > heat[i + 2, j]
+    assert heat[i, 5] == pytest.approx(sol.sheet_current(0, d_mm)[i, 5], rel=0.02)
