@@ -380,3 +380,18 @@ def test_a_node_where_current_enters_reads_its_strips_heat(solve):
     assert heat[i, j] == pytest.approx(math.sqrt(1 / 8) / (d_mm * 1e-3), rel=1e-6)
     assert heat[i, j] > heat[i + 1, j] > heat[i + 2, j]
     assert heat[i, 5] == pytest.approx(sol.sheet_current(0, d_mm)[i, 5], rel=0.02)
+
+
+@pytest.mark.parametrize("name", ["small_pair", "necked_faces", "routed_pair"])
+def test_a_solutions_state_is_rebuilt_exactly_from_its_currents_and_potentials(name):
+    """test_solver.py:271-300: Solution.state_for rebuilds the solver's unknown vector from the solution's strip,
+    capacitance, branch (and face-pair) currents and its node potentials, every number the same."""
+    from test_oracle_golden import load
+    z, board = load(name)
+    st, routes = gs.from_board(board, _device=False)
+    ost = oracle_stack(board)
+    f = float(board.freqs[0])
+    r = routes[0]
+    Ib, V, its, x = ost.solve(f, r.rhs_top(f), r.J(), tol=1e-8)
+    sol = r.solution(f, Ib, V, its)
+    assert np.array_equal(sol.state_for(st), x)
