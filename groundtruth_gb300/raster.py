@@ -1,9 +1,17 @@
-"""The exact-copper raster's arithmetic (GroundTruth: peec.py:482-705, the parts of build_grid's exact-copper pass
-that need no polygon library): how much copper crosses each cell border along scanlines, the copper area of each
-cell from its outline by Green's theorem, a strip's width and centre from those, copper of a border without a strip
-of its net moved to the nearest strip that has one, and the series factor of a narrow run whose width changes
-along its length; and the walk that claims tracks' cells and strips on a layer's grid (peec.py:893-983).  Polygons are given as their edges (outlines counter-clockwise, holes clockwise: ring_edges), in
-the same length unit as the pitch."""
+"""Copper polygons and tracks onto the solver's grid (GroundTruth: build_grid and its helpers, peec.py:329-983), the
+parts that need no polygon library.
+
+* The exact-copper arithmetic (peec.py:482-771): how much copper crosses each cell border along scanlines
+  (line_cover), each cell's copper area by Green's theorem (cell_areas), a strip's width and centre from those
+  (strip_widths), copper of a border without a strip of its net moved to the nearest strip that has one (adopt),
+  the series factor of a narrow run whose width changes along its length (series_factor), and the pass over a
+  net's copper that measures them (exact_copper).
+* The sub-grid rasteriser (coarse_from_fine, peec.py:774-849), the walk that claims tracks' cells and strips
+  (rasterise_tracks, peec.py:893-983), a net's polygons grouped into pieces (pieces, peec.py:852-873) and the
+  layer rasteriser around them (build_layer, peec.py:329-449).
+
+Polygons are (outline, holes) vertex arrays, or their edges (outlines counter-clockwise, holes clockwise:
+ring_edges), in the same length unit as the pitch."""
 from __future__ import annotations
 
 import math
