@@ -110,3 +110,37 @@ def test_calls_without_a_geometry_are_refused(lib):
     _refused(lib, lib.gt_kernel_spectrum(0, 4, d, dz, 16, 16, one, 1, quad), "bad arguments")
     _refused(lib, lib.gt_kernel_spectrum(4, 4, d, dz, 20, 16, one, 1, quad), "FFT sizes")
     _refused(lib, lib.gt_kernel_spectrum(12, 4, d, dz, 16, 16, one, 1, quad), "cover 2n - 1")
+
+
+def _c_struct(name: str) -> list:
+    """(field, bytes) of a typedef'd struct in include/gt_gb300.h, in declaration order."""
+    text = (ROOT / "include" / "gt_gb300.h").read_text()
+    body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (name, name), text, re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    sizes = {"int32_t": 4, "int64_t": 8, "double": 8, "uint8_t": 1}
+    out = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        m = re.match(r"(?:const\s+)?(\w+)\s*(\*?)\s*(.*)", decl)
+        ctype, ptr, names = m.groups()
+        for nm in names.split(","):
+            nm = nm.strip().lstrip("*")
+            arr = re.match(r"(\w+)\[(\d+)\]", nm)
+            if arr:
+                out.append((arr.group(1), sizes[ctype] * int(arr.group(2))))
+            else:
+                out.append((nm, 8 if ptr or "*" in decl.split(nm)[0] else sizes[ctype]))
+    return out
+
+
+def test_the_ctypes_descriptors_match_the_header():
+    """native.GeometryDesc and SolveOpts have the header's fields, in its order and of its sizes (the ABI the
+    library reads them by)."""
+    import ctypes as C
+    from groundtruth_gb300 import native
+    for struct, cls in (("gt_geometry_desc", native.GeometryDesc), ("gt_solve_opts", native.SolveOpts)):
+        header = _c_struct(struct)
+        ours = [(f[0], C.sizeof(f[1])) for f in cls._fields_]
+        assert ours == header, struct
