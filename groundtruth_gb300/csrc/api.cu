@@ -164,6 +164,8 @@ struct Workspace {
     void *V = nullptr, *w = nullptr, *z = nullptr, *T = nullptr, *zfac = nullptr, *yfac = nullptr, *uvec = nullptr,
          *sd = nullptr, *vcur = nullptr;
     c64* partial = nullptr;
+    // precision 3: the FP32 inner solve's preconditioner applied in FP64 (input, output and the sweeps' vectors)
+    c64 *pr64 = nullptr, *pz64 = nullptr, *zfac64 = nullptr, *yfac64 = nullptr, *uvec64 = nullptr, *sd64 = nullptr;
     GmresState st{};
     int *slot_col = nullptr, *slot_op = nullptr, *g_ptr = nullptr, *g_slot = nullptr, *g_op = nullptr, *col_op = nullptr;
     int* slot_pc = nullptr;      // each slot's factorisation (the preconditioner's tables, panels and pivots)
@@ -202,6 +204,7 @@ struct gt_geometry {
     int* d_sterm_tab = nullptr;
     double* d_sterm_coef = nullptr;
     int64_t maxT = 0;  // largest S * P1 * n0 of the two orientations
+    int device = 0;    // the CUDA device the geometry's buffers live on (current at gt_geometry_create)
     // the last n_lowrank branches are left out of the S-term map: a derived stack whose operators come from
     // gt_operators_derive (its base's factorisations plus a low-rank update)
     int n_lowrank = 0;
@@ -254,6 +257,10 @@ struct gt_operators {
     c64* dinv64 = nullptr;
     c32* dinv32 = nullptr;
     std::vector<int> own;        // the operator whose frequency each factorisation was made at
+    // per factorisation: its branch or capacitance admittances exceed its strips' by more than STIFF_RATIO, so
+    // that FP32 node potentials cannot resolve the voltages across them (a 1 nOhm short beside strips of a
+    // few hundred siemens); the mixed-precision solve applies such a preconditioner in FP64
+    std::vector<char> stiff;
     // a derived set (gt_operators_derive): the panels and pivots above are its base's; nlow branches beyond the
     // base's are added by the Woodbury identity with W = S^-1 U (node order) and Minv = (Z + U^T W)^-1 per
     // factorisation
@@ -314,6 +321,24 @@ template <> const c64* low_w_of<double>(const gt_operators* ops) { return ops->l
 template <typename R> static const cx<R>* low_m_of(const gt_operators* ops);
 template <> const c32* low_m_of<float>(const gt_operators* ops) { return ops->low_m32; }
 template <> const c64* low_m_of<double>(const gt_operators* ops) { return ops->low_m64; }
+
+// A factorisation is stiff when a branch or capacitance admittance of its table exceeds the largest strip
+// admittance by more than this: the preconditioner's branch currents D^-1 (r + y_a - y_b) then rest on node
+// potential differences below FP32's resolution of the potentials themselves (measured: ratios of 1.6e3 solve
+// as usual, 1.6e4 take an extra refinement step, 1.6e6 stall), and the mixed-precision solve applies it in FP64.
+constexpr double STIFF_RATIO = 4096.0;
+
+static std::vector<char> stiffness(const std::vector<c64>& t64, int nf, const Geo& g) {
+    std::vector<char> out(nf, 0);
+    for (int f = 0; f < nf; ++f) {
+        const c64* t = t64.data() + (size_t)f * g.ntab;
+        double strip = 0, tail = 0;
+        for (int e = 0; e < g.tab_cap0; ++e) strip = std::max(strip, std::hypot(t[e].re, t[e].im));
+        for (int e = g.tab_cap0; e < g.ntab; ++e) tail = std::max(tail, std::hypot(t[e].re, t[e].im));
+        out[f] = strip > 0 && tail > STIFF_RATIO * strip;
+    }
+    return out;
+}
 
 static bool good_fft_size(int P) {
     if (P < 8) return false;
@@ -635,6 +660,15 @@ static void fill_ws(Workspace& W, gt_geometry* G, int ncol, int m, int prec, int
     W.sd = p.alloc<unsigned char>((size_t)ncol * G->F.nnode * es);
     if (!dry) GT_CUDA(cudaMemset(W.sd, 0, (size_t)ncol * G->F.nnode * es));
     W.partial = p.alloc<c64>((size_t)ncol * nch * (m + 2));
+    if (prec == 3) {
+        W.pr64 = p.alloc<c64>((size_t)ncol * n);
+        W.pz64 = p.alloc<c64>((size_t)ncol * n);
+        W.zfac64 = p.alloc<c64>((size_t)ncol * G->F.nfac);
+        W.yfac64 = p.alloc<c64>((size_t)ncol * G->F.nfac);
+        W.uvec64 = p.alloc<c64>((size_t)ncol * std::max<int64_t>(G->F.vec_total, 1));
+        W.sd64 = p.alloc<c64>((size_t)ncol * G->F.nnode);
+        if (!dry) GT_CUDA(cudaMemset(W.sd64, 0, (size_t)ncol * G->F.nnode * sizeof(c64)));
+    }
     GmresState& s = W.st;
     s.nslot = ncol;
     s.m = m;
@@ -690,7 +724,7 @@ static void norms64(gt_geometry* G, const c64* v, int64_t ld, int ncol, double* 
 // sqrt(n) so that a unit vector's entries sit near 1)
 template <typename R, typename B = cx<R>>
 static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_col_op, const gt_solve_opts& o,
-                      int* its_out, double* resid_out, cudaStream_t st) {
+                      int* its_out, double* resid_out, cudaStream_t st, bool pc64 = false) {
     constexpr bool narrow = !std::is_same<B, cx<R>>::value;
     Workspace& W = *G->ws;
     const int64_t n = G->geo.n;
@@ -727,6 +761,20 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
     cx<R>* uvec = static_cast<cx<R>*>(W.uvec);
     cx<R>* sd = static_cast<cx<R>*>(W.sd);
     const int64_t lds = (int64_t)(m + 1) * n;
+    // the preconditioner on nsl listed slots (outputs n apart): in precision R, or, for stiff factorisations
+    // (pc64), in FP64 on FP64 copies of the vectors, its result rounded back to R
+    auto apply_pc = [&](const cx<R>* rin, int64_t ldr, cx<R>* out, int nsl, const Groups& g, const int* list) {
+        if constexpr (std::is_same<R, float>::value) {
+            if (pc64) {
+                launch_recast<double, float>(W.pr64, n, rin, ldr, list, n, nsl, st);
+                precond<double>(G, ops, W.pr64, n, W.pz64, n, nsl, W.slot_pc, g, gmax, W.zfac64, W.yfac64, W.uvec64,
+                                W.sd64, st, list);
+                launch_recast<float, double>(out, n, W.pz64, n, list, n, nsl, st);
+                return;
+            }
+        }
+        precond<R>(G, ops, rin, ldr, out, n, nsl, W.slot_pc, g, gmax, zfac, yfac, uvec, sd, st, list);
+    };
     std::vector<int> slot_col, slot_op, slot_pc, gptr, gslot, gop, act;
     auto upload_groups = [&](const std::vector<int>& slots) {
         make_groups(slots, slot_pc, gmax, gptr, gslot, gop);
@@ -811,7 +859,7 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
                 vin = V + (int64_t)j * n;
                 ldin = lds;
             }
-            precond<R>(G, ops, vin, ldin, z, n, na, W.slot_pc, grp, gmax, zfac, yfac, uvec, sd, st, W.act);
+            apply_pc(vin, ldin, z, na, grp, W.act);
             matvec<R>(G, ops, z, nullptr, w, n, na, W.slot_op, 0, T, st, W.act);
             // classical Gram-Schmidt: the dot products read the j+1 basis vectors and w; the update reads
             // them again, reads w and writes it
@@ -865,7 +913,7 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
         act.resize(ns);
         for (int q = 0; q < ns; ++q) act[q] = q;
         grp = upload_groups(act);
-        precond<R>(G, ops, w, n, z, n, ns, W.slot_pc, grp, gmax, zfac, yfac, uvec, sd, st, W.act);
+        apply_pc(w, n, z, ns, grp, W.act);
         // GCR step in FP64: p = the cycle's correction, q = K p, both orthogonalised against the directions
         // held (q orthonormal); then x += alpha p, r -= alpha q with alpha = q^H r
         if (k == K) k = 0;
@@ -929,14 +977,29 @@ static int run_solve(gt_geometry* G, gt_operators* ops, int ncol, const int* col
         if (col_op[c] < 0 || col_op[c] >= ops->nops) throw Invalid("column operator index out of range");
     if (o.precision == 1) return solve_impl<double>(G, ops, ncol, col_op, o, its, res, st);
     if (o.precision == 2) return solve_impl<float, h16c>(G, ops, ncol, col_op, o, its, res, st);
-    if (o.precision != 0) throw Invalid("precision must be 0, 1 or 2");
+    if (o.precision == 3) {
+        if (!solve_fits(G, sizeof(c64))) throw Invalid("precision 3: a front is too large for the FP64 sweeps");
+        return solve_impl<float>(G, ops, ncol, col_op, o, its, res, st, true);
+    }
+    if (o.precision != 0) throw Invalid("precision must be 0, 1, 2 or 3");
     return solve_impl<float>(G, ops, ncol, col_op, o, its, res, st);
+}
+
+// precision 0 becomes 3 when a column's factorisation is stiff and the FP64 sweeps fit its fronts
+static int effective_precision(const gt_geometry* G, const gt_operators* ops, int ncol, const int* col_op, int prec) {
+    if (prec != 0 || !ops || !col_op || ops->stiff.empty() || !solve_fits(G, sizeof(c64))) return prec;
+    for (int c = 0; c < ncol; ++c) {
+        const int q = col_op[c];
+        if (q >= 0 && q < ops->nops && ops->stiff[ops->fslot[q]]) return 3;
+    }
+    return 0;
 }
 
 // The L_p product of n_cols dense FP64 vectors into the strip segments of y, with the FFT passes'
 // intermediate grid in caller-provided scratch (used by gt_lp_product_noalloc, noalloc.cu).  Launches
 // kernels only: no allocation, no synchronisation.
 size_t lp_scratch_bytes(const gt_geometry* G, int ncol) { return (size_t)ncol * (size_t)G->maxT * sizeof(c64); }
+int geometry_device(const gt_geometry* G) { return G->device; }
 
 void lp_with_scratch(gt_geometry* G, int ncol, const c64* x, c64* y, void* scratch, cudaStream_t st) {
     for (int k = 0; k < 2; ++k) {
@@ -1253,6 +1316,7 @@ int gt_geometry_create(const gt_geometry_desc* d, gt_geometry** out) {
     G->d_sterm_tab = p.upload(d->sterm_tab, d->sterm_ptr[d->n_svalues]);
     G->d_sterm_coef = p.upload(d->sterm_coef, d->sterm_ptr[d->n_svalues]);
     GT_CUDA(cudaDeviceSynchronize());
+    GT_CUDA(cudaGetDevice(&G->device));
     *out = G.release();
     return GT_OK;
     GT_GUARD_END
@@ -1315,6 +1379,7 @@ int gt_operators_create_shared(gt_geometry* G, int32_t n_ops, const double* omeg
             }
         O->tab = p.upload(t64.data(), t64.size());
         O->tab32 = p.upload(t32.data(), t32.size());
+        O->stiff = stiffness(t64, nf_ops, g);
     }
     n_ops = nf_ops;        // the factorisation below runs over the factorised operators
     cudaStream_t st = 0;
@@ -1409,6 +1474,7 @@ int gt_operators_derive(gt_geometry* G, const gt_operators* base, int32_t n_ops,
             }
         O->tab = p.upload(t64.data(), t64.size());
         O->tab32 = p.upload(t32.data(), t32.size());
+        O->stiff = stiffness(t64, nf, g);
     }
     O->panel64 = base->panel64;
     O->panel32 = base->panel32;
@@ -1536,6 +1602,9 @@ int gt_solve_device(gt_geometry* G, gt_operators* ops, int32_t n_cols, const int
     if (!G || !ops || !opts || n_cols < 1) throw Invalid("bad arguments");
     std::lock_guard<std::mutex> lk(G->lock);
     cudaStream_t st = (cudaStream_t)stream;
+    gt_solve_opts eo = *opts;
+    eo.precision = effective_precision(G, ops, n_cols, col_op, eo.precision);
+    opts = &eo;
     ensure_ws(G, n_cols, opts->restart, opts->precision, std::max(1, opts->outer_k));
     Workspace& W = *G->ws;
     GT_CUDA(cudaMemcpyAsync(W.b64, rhs_device, (size_t)n_cols * G->geo.n * sizeof(c64), cudaMemcpyDeviceToDevice, st));
@@ -1555,6 +1624,9 @@ int gt_solve(gt_geometry* G, gt_operators* ops, int32_t n_cols, const int32_t* c
     if (!G || !ops || !opts || n_cols < 1 || !rhs || !x_out) throw Invalid("bad arguments");
     std::lock_guard<std::mutex> lk(G->lock);
     cudaStream_t st = (cudaStream_t)stream;
+    gt_solve_opts eo = *opts;
+    eo.precision = effective_precision(G, ops, n_cols, col_op, eo.precision);
+    opts = &eo;
     ensure_ws(G, n_cols, opts->restart, opts->precision, std::max(1, opts->outer_k));
     Workspace& W = *G->ws;
     const int64_t nc = G->n_compact;

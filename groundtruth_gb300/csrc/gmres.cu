@@ -399,6 +399,18 @@ __global__ void to64_kernel(c64* __restrict__ dst, int64_t ldd, const cx<R>* __r
         d[q] = cvt<double>(x[q]);
 }
 
+// dst slot c = src slot c converted to D, for the listed slots (all nslot when list is null): the FP32 inner
+// solve's vectors into and out of an FP64 preconditioner apply
+template <typename D, typename S>
+__global__ void recast_kernel(cx<D>* __restrict__ dst, int64_t ldd, const cx<S>* __restrict__ src, int64_t lds,
+                              const int* __restrict__ list, int64_t n) {
+    const int c = list ? list[blockIdx.y] : (int)blockIdx.y;
+    cx<D>* d = dst + (int64_t)c * ldd;
+    const cx<S>* x = src + (int64_t)c * lds;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+        d[q] = cvt<D>(x[q]);
+}
+
 __global__ void gcr_scale_kernel(c64* __restrict__ p, c64* __restrict__ q, int64_t ld, const c64* __restrict__ nu2,
                                  const int* __restrict__ active, int64_t n) {
     const int c = blockIdx.y;
@@ -423,6 +435,17 @@ void launch_to64(c64* dst, int64_t ldd, const cx<R>* src, int64_t lds, const int
 }
 template void launch_to64<float>(c64*, int64_t, const c32*, int64_t, const int*, int64_t, int, cudaStream_t);
 template void launch_to64<double>(c64*, int64_t, const c64*, int64_t, const int*, int64_t, int, cudaStream_t);
+
+template <typename D, typename S>
+void launch_recast(cx<D>* dst, int64_t ldd, const cx<S>* src, int64_t lds, const int* list, int64_t n, int nslot,
+                   cudaStream_t st) {
+    if (nslot <= 0) return;
+    int blocks = (int)std::min<int64_t>((n + 255) / 256, 1024);
+    recast_kernel<D, S><<<dim3(blocks, nslot), 256, 0, st>>>(dst, ldd, src, lds, list, n);
+    GT_LAUNCH_CHECK();
+}
+template void launch_recast<double, float>(c64*, int64_t, const c32*, int64_t, const int*, int64_t, int, cudaStream_t);
+template void launch_recast<float, double>(c32*, int64_t, const c64*, int64_t, const int*, int64_t, int, cudaStream_t);
 
 void launch_gcr_scale(c64* p, c64* q, int64_t ld, const c64* nu2, const int* active, int64_t n, int ncol,
                       cudaStream_t st) {

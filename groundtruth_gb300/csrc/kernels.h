@@ -189,6 +189,10 @@ void launch_lowrank_rhs(cx<R>* s, int64_t nfac, int c0, int ncol, int k, const i
 // U^T W entries g[c][i] of ncol node-ordered columns
 void launch_lowrank_gather(const c64* w, int64_t nnode, int ncol, int k, const int* ends, c64* g, cudaStream_t st);
 void launch_lowrank_to32(const c64* a, c32* b, int64_t n, cudaStream_t st);
+// dst[c] = src[c] (n entries, converted) for c = list[0 .. nslot) (0 .. nslot when list is null)
+template <typename D, typename S>
+void launch_recast(cx<D>* dst, int64_t ldd, const cx<S>* src, int64_t lds, const int* list, int64_t n, int nslot,
+                   cudaStream_t st);
 void launch_lowrank_to64(const c32* a, c64* b, int64_t n, cudaStream_t st);
 
 // --- Krylov vector work (batched, one basis per slot)

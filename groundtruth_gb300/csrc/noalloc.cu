@@ -11,19 +11,24 @@
 // the library holds it until the process exits.  Host code cannot use the array's name as a device address,
 // so its address is looked up with cudaGetSymbolAddress once per device, the first time this entry point
 // runs with that device current, and cached; make that first call before any stream capture begins.
+// The geometry's own device must be current: a call made with another device current is refused, since it
+// would pair the geometry's buffers with that device's copy of the array.
 // Every call uses the same array: two calls whose kernels overlap on the GPU (other streams, other host
 // threads) race on it.  Nothing in it has to start at zero: the row pass writes every entry the column and
 // inverse-row passes read.
 #include "../../include/gt_gb300.h"
 #include "common.cuh"
 
+#include <exception>
 #include <mutex>
+#include <new>
 #include <string>
 
 struct gt_geometry;
 
 namespace gt {
 size_t lp_scratch_bytes(const gt_geometry* G, int ncol);
+int geometry_device(const gt_geometry* G);
 void lp_with_scratch(gt_geometry* G, int ncol, const c64* x, c64* y, void* scratch, cudaStream_t st);
 void set_error(const std::string& s);
 }  // namespace gt
@@ -68,8 +73,20 @@ extern "C" int gt_lp_product_noalloc(gt_geometry* g, int32_t n_cols, const void*
                           " bytes; pass fewer columns per call");
             return GT_INVALID_ARGUMENT;
         }
+        int dev = -1;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) {
+            gt::set_error(std::string("gt_lp_product_noalloc: cudaGetDevice failed: ") + cudaGetErrorString(e));
+            return GT_DEVICE_ERROR;
+        }
+        if (dev != gt::geometry_device(g)) {
+            gt::set_error("gt_lp_product_noalloc: the geometry lives on device " +
+                          std::to_string(gt::geometry_device(g)) + " but device " + std::to_string(dev) +
+                          " is current; make the geometry's device current");
+            return GT_INVALID_ARGUMENT;
+        }
         void* scratch = nullptr;
-        cudaError_t e = scratch_address(&scratch);
+        e = scratch_address(&scratch);
         if (e != cudaSuccess) {
             gt::set_error(std::string("gt_lp_product_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
             return GT_DEVICE_ERROR;
@@ -79,6 +96,15 @@ extern "C" int gt_lp_product_noalloc(gt_geometry* g, int32_t n_cols, const void*
         return GT_OK;
     } catch (const gt::CudaError& e) {
         gt::set_error(std::string("gt_lp_product_noalloc: ") + cudaGetErrorString(e.code) + " (" + e.where + ")");
+        return e.code == cudaErrorMemoryAllocation ? GT_OUT_OF_MEMORY : GT_DEVICE_ERROR;
+    } catch (const std::bad_alloc&) {
+        gt::set_error("gt_lp_product_noalloc: host allocation failed");
+        return GT_OUT_OF_MEMORY;
+    } catch (const std::exception& e) {
+        gt::set_error(std::string("gt_lp_product_noalloc: ") + e.what());
+        return GT_INVALID_ARGUMENT;
+    } catch (...) {
+        gt::set_error("gt_lp_product_noalloc: unknown failure");
         return GT_DEVICE_ERROR;
     }
 }

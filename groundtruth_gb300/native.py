@@ -59,12 +59,25 @@ class GeometryDesc(C.Structure):
                 ("narrow_rre", DP), ("narrow_twre", DP), ("cap_fill", DP)]
 
 
-PRECISIONS = {"mixed": 0, "fp64": 1, "mixed16": 2}
+PRECISIONS = {"mixed": 0, "fp64": 1, "mixed16": 2, "mixed_pc64": 3}
+
+# the library's rule for a stiff factorisation (STIFF_RATIO in api.cu): a branch or capacitance admittance above
+# this many times the largest strip admittance, where "mixed" solves apply the preconditioner in FP64
+STIFF_RATIO = 4096.0
+
+
+def stiff_table(tab: np.ndarray, tab_cap0: int) -> bool:
+    """Whether an admittance table (strip blocks before tab_cap0, then capacitances and branches) is stiff."""
+    tab = np.asarray(tab)
+    strip = float(np.abs(tab[:tab_cap0]).max()) if tab_cap0 else 0.0
+    tail = float(np.abs(tab[tab_cap0:]).max()) if len(tab) > tab_cap0 else 0.0
+    return strip > 0 and tail > STIFF_RATIO * strip
 
 
 def _precision(name: str) -> int:
     """gt_solve_opts.precision: "mixed" FP32 inner GMRES + FP64 outer, "fp64" all FP64, "mixed16" as "mixed"
-    with the Krylov basis stored in FP16."""
+    with the Krylov basis stored in FP16, "mixed_pc64" as "mixed" with the preconditioner applied in FP64 (what
+    "mixed" becomes by itself on a stiff factorisation)."""
     if name not in PRECISIONS:
         raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
     return PRECISIONS[name]

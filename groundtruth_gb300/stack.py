@@ -973,6 +973,7 @@ class PlaneStack:
             self._admit(len(set(plan)) if plan is not None else len(todo))
             data = [self._freq_tables(k) for k in todo]
             ops = native.Operators(self.handle, todo, data, plan)
+            ops.stiff = any(native.stiff_table(d[4], self.tab_cap0) for d in data)
             with self._lock:
                 for n, k in enumerate(todo):
                     self._ops[k] = (ops, n)
@@ -991,6 +992,7 @@ class PlaneStack:
         if not cached:
             data = [self._freq_tables(k) for k in bobj.keys]
             dobj = native.Operators(self.handle, bobj.keys, data, base=bobj)
+            dobj.stiff = any(native.stiff_table(d[4], self.tab_cap0) for d in data)
             with self._lock:
                 for n, k in enumerate(bobj.keys):
                     self._ops[k] = (dobj, n)
@@ -1025,6 +1027,10 @@ class PlaneStack:
         x0 = self._warm_start(ops, rhs, guesses) if guesses is not None else None
         x = np.zeros_like(rhs)
         its, res, ok = np.zeros(ncol, np.int32), np.zeros(ncol), np.zeros(ncol, bool)
+        if precision == "mixed" and any(getattr(o[0], "stiff", False) for o in ops):
+            # a stiff factorisation (near-short branches): the library applies its preconditioner in FP64; plan
+            # the memory for that
+            precision = "mixed_pc64"
         step = self.columns_that_fit(ncol, restart, precision)
         for c0 in range(0, ncol, step):
             sl = slice(c0, c0 + step)

@@ -125,7 +125,12 @@ typedef struct gt_solve_opts {
     int32_t max_its;        /* total inner iterations allowed per column */
     double inner_tol;       /* relative residual reduction each inner FP32 cycle aims at */
     int32_t precision;      /* 0: FP32 inner GMRES + FP64 refinement, 1: all FP64 (plain drop-in), 2: as 0 with
-                               the inner Krylov basis stored in FP16 (half the Gram-Schmidt traffic) */
+                               the inner Krylov basis stored in FP16 (half the Gram-Schmidt traffic), 3: as 0 with
+                               the preconditioner applied in FP64.  0 becomes 3 by itself when a column's
+                               factorisation is stiff: a branch or capacitance admittance above 4096 times the
+                               largest strip admittance (a near-short, whose current FP32 node potentials cannot
+                               resolve), provided the FP64 sweeps fit its fronts; gt_memory counts what the
+                               precision passed to it needs (pass 3 to plan a stiff solve) */
     int32_t max_outer;      /* refinement steps */
     double reorth;          /* DGKS: re-orthogonalise when ||w|| fell below reorth x its norm before the first
                                Gram-Schmidt pass (0.7: the reference's rule, peec.py:3156; 0: never) */

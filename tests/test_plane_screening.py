@@ -220,3 +220,23 @@ def test_a_thin_dielectric_pair_converges_to_the_dc_distribution_with_the_cell_s
         excess.append(per[1e4] / exact - 1)
     assert 0.0 < excess[0] < 0.11 and 0.0 < excess[1] < 0.045, excess
     assert excess[1] < 0.5 * excess[0] + 0.01, excess
+
+
+def test_near_shorts_make_the_factorisation_stiff_and_ordinary_boards_do_not():
+    """The 1 nOhm shorts of the GND / VDD / GND line put branch admittances of 1e9 S beside strips of a few
+    hundred siemens: FP32 node potentials cannot resolve the volts across them, so the library applies that
+    factorisation's preconditioner in FP64 (native.stiff_table is its rule).  A board of ordinary vias and
+    parts stays on the FP32 preconditioner."""
+    from groundtruth_gb300 import native, synth
+    layers = _layers([("GND", 0.07), ("VDD", 0.07), ("GND", 0.07)], [0.1, 0.1], 20.0)
+    g = layers[0][2]
+    shorts, _ = _ends([("GND", 0.07), ("VDD", 0.07), ("GND", 0.07)], g)
+    grid = lambda l: gs.Grid(0.0, 0.0, PITCH, l.nx, l.ny, l.node, l.xb, l.yb, **l.widths(), fill=l.fill,  # noqa: E731
+                             area=l.area)
+    st = gs.PlaneStack([gs.PlaneLayer(n, z, grid(l), t) for n, z, l, t in layers],
+                       [gs.Branch(a, b, lambda f: 1e-9 + 0j) for a, b in shorts], screen=True, _device=False)
+    for f in FREQS:
+        assert native.stiff_table(st._freq_tables(f)[4], st.tab_cap0), f
+    plain, _ = gs.from_board(synth.small_pair(), _device=False)
+    for f in synth.small_pair().freqs:
+        assert not native.stiff_table(plain._freq_tables(float(f))[4], plain.tab_cap0), f

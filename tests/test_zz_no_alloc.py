@@ -41,12 +41,16 @@ def test_lp_product_without_allocation_matches_the_allocating_entry_point():
 
 
 def test_more_columns_than_the_fixed_scratch_holds_are_refused():
-    pytest.importorskip("torch")
+    torch = pytest.importorskip("torch")
     z, board = load("small_pair")
     st, routes = gs.from_board(board)
     lib = st.handle.lib
-    per_col = 16 * max(st.N * st.P["x"][1] * (st.nx - 1), st.N * st.P["y"][1] * st.nx)
+    # the FFT grid of one column: the larger orientation's sheets x padded row length x rows
+    per_col = 16 * max(st.n_sheets * st.P["x"][1] * (st.nx - 1), st.n_sheets * st.P["y"][1] * st.nx)
     too_many = (32 << 20) // per_col + 1
-    rc = lib.gt_lp_product_noalloc(st.handle.h, too_many, C.c_void_p(1), C.c_void_p(1), None)
+    # real buffers of that many columns: the call must refuse them before any kernel runs
+    X = torch.zeros((too_many, st.handle.n_dense), dtype=torch.complex128, device="cuda")
+    Y = torch.zeros_like(X)
+    rc = lib.gt_lp_product_noalloc(st.handle.h, too_many, C.c_void_p(X.data_ptr()), C.c_void_p(Y.data_ptr()), None)
     assert rc == native.GT_INVALID_ARGUMENT
     assert b"fewer columns" in lib.gt_last_error()
