@@ -13,8 +13,11 @@
 //   pass C  inverse row FFTs, then the fused epilogue on the strips:
 //           out = R_t x + j w L_p x - (V[a] - V[b])     (or rhs - that, for residuals; or L_p x alone)
 // The spectrum is stored (Q1, Q0, S, S) and pre-scaled by 1/(P0 P1).
+#include <type_traits>
+
 #include "common.cuh"
 #include "fft.cuh"
+#include "fftw.cuh"
 #include "kernels.h"
 
 namespace gt {
@@ -248,6 +251,76 @@ __global__ void __launch_bounds__(512) lp_pass_b8(int n0, int P1, int ncol, int 
             }
         }
     }
+}
+
+// Pass B for P0 = 512 in FP32, one warp per pair of rows (fftw.cuh): the two sheets of a column (S = 2) or
+// two columns of one sheet (S = 1).  The warp loads the rows' lower halves (i < n0 <= 256) straight from T,
+// transforms them, multiplies by the S x S spectrum at its pixels (lane 16 s + k1 holds sheet s at
+// p = k1 + 16 k2 and takes the other sheet's value from lane 16 (1 - s) + k1 by a shuffle), transforms
+// back and stores the lower halves.  Warps share nothing but the block's spectrum reads (L1).
+constexpr int BW_WARPS = 4;
+#ifndef GT_BW_MINB
+#define GT_BW_MINB 4        // blocks per SM the register budget is cut for (128 registers)
+#endif
+
+template <int S>
+__global__ void __launch_bounds__(BW_WARPS * 32, GT_BW_MINB) lp_pass_bw(int n0, int P1, int ncol, const float* __restrict__ spec,
+                                                            const c32* __restrict__ tw, c32* __restrict__ T) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int P = 512, Q0 = P / 2 + 1, CPW = S == 2 ? 1 : 2;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    c32* sx = reinterpret_cast<c32*>(smem_raw) + warp * WX_SLOTS;
+    const int c = blockIdx.x;
+    const int b0 = (blockIdx.y * BW_WARPS + warp) * CPW;
+    if (b0 >= ncol) return;                     // the whole warp leaves together
+    c32* row[2];
+    bool ok[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int b = S == 2 ? b0 : b0 + q, s = S == 2 ? q : 0;
+        ok[q] = b < ncol;
+        row[q] = T + (((int64_t)min(b, ncol - 1) * S + s) * P1 + c) * n0;
+    }
+    c32 v[2][16];
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const int j = lane + 32 * r;
+            v[q][r] = (ok[q] && j < n0) ? row[q][j] : zero<float>();
+        }
+    c32 u[32];
+    fft512_fwd2<float, true>(v, u, sx, tw);
+    const float* Kc = spec + (int64_t)min(c, P1 - c) * Q0 * S * S;
+    const int k1 = lane & 15;
+    if constexpr (S == 2) {
+        const int s = lane >> 4;
+#pragma unroll
+        for (int k2 = 0; k2 < 32; ++k2) {
+            const int p = k1 + 16 * k2;
+            const float2 kk = __ldg(reinterpret_cast<const float2*>(Kc + min(p, P - p) * 4 + 2 * s));
+            c32 o;
+            o.re = __shfl_xor_sync(0xffffffffu, u[k2].re, 16);
+            o.im = __shfl_xor_sync(0xffffffffu, u[k2].im, 16);
+            const c32 u0 = s ? o : u[k2], u1 = s ? u[k2] : o;
+            u[k2] = mk<float>(kk.x * u0.re + kk.y * u1.re, kk.x * u0.im + kk.y * u1.im);
+        }
+    } else {
+#pragma unroll
+        for (int k2 = 0; k2 < 32; ++k2) {
+            const int p = k1 + 16 * k2;
+            const float kk = __ldg(Kc + min(p, P - p));
+            u[k2] = kk * u[k2];
+        }
+    }
+    fft512_inv2<float, true>(u, v, sx, tw);
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const int j = lane + 32 * r;
+            if (ok[q] && j < n0) row[q][j] = v[q][r];
+        }
 }
 
 // Row passes for P a power of 8: the first stage of pass A reads the strip row straight from x, the last
@@ -498,8 +571,25 @@ static void launch_b8(const LpArgs<R>& a, int bt, cudaStream_t st) {
 // the fused column pass applies for these lengths and sheet counts
 template <typename R> static bool b8_fits(const LpArgs<R>& a) { return (a.P0 == 64 || a.P0 == 512) && a.S >= 1 && a.S <= 4; }
 
+template <int S>
+static void launch_bw(const LpArgs<float>& a, cudaStream_t st) {
+    constexpr int CPW = S == 2 ? 1 : 2;
+    const size_t sm = (size_t)BW_WARPS * WX_SLOTS * sizeof(c32);
+    set_smem<float>((const void*)lp_pass_bw<S>, sm);
+    lp_pass_bw<S><<<dim3(a.P1, ceil_div(a.ncol, BW_WARPS * CPW)), BW_WARPS * 32, sm, st>>>(a.n0, a.P1, a.ncol, a.spec,
+                                                                                         a.tw0, a.T);
+    GT_LAUNCH_CHECK();
+}
+
 template <typename R, int PB>
 static void launch_b(const LpArgs<R>& a, int bt, cudaStream_t st) {
+    if constexpr (PB == 512 && std::is_same<R, float>::value) {
+        if (a.n0 <= PB / 2 && a.S <= 2) {
+            if (a.S == 2) launch_bw<2>(a, st);
+            else launch_bw<1>(a, st);
+            return;
+        }
+    }
     if constexpr (PB == 64 || PB == 512) {
         if (b8_fits(a)) {
             switch (a.S) {

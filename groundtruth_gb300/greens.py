@@ -49,33 +49,48 @@ def filament_mutual(length, axial, rho):
     return MU0 / (4 * np.pi) * (G(axial + length) - 2 * G(axial) + G(axial - length))
 
 
-def _graded(p: float, q: float, toward, panels: int, order: int):
+def panel_rule(lo: float, hi: float, graded_end, panels: int, order: int):
+    """Gauss-Legendre nodes and weights (order points per panel) over [lo, hi] cut into `panels` panels: equal
+    ones, or, toward an integrable log singularity at graded_end (lo or hi), panels that halve in length so the
+    one touching it is 2^-(panels - 1) of the interval."""
     x, w = gauss(order)
-    if toward is None:
-        e = np.linspace(0.0, 1.0, panels + 1)
+    if graded_end is None:
+        edges = np.linspace(0.0, 1.0, panels + 1)
     else:
-        e = np.concatenate([[0.0], 0.5 ** np.arange(panels - 1, -1, -1)])
-        if toward == q:
-            e = 1.0 - e[::-1]
-    a, b = e[:-1, None], e[1:, None]
-    return (p + (q - p) * (a + (b - a) * (x[None] + 1.0) / 2.0)).ravel(), ((q - p) * (b - a) * w[None] / 2.0).ravel()
+        edges = np.concatenate([[0.0], np.ldexp(1.0, np.arange(1 - panels, 1))])   # 0, 2^(1-p), ..., 1/2, 1
+        if graded_end == hi:
+            edges = 1.0 - edges[::-1]
+    mid, half = 0.5 * (edges[1:] + edges[:-1]), 0.5 * (edges[1:] - edges[:-1])
+    span = hi - lo
+    nodes = lo + span * (mid[:, None] + half[:, None] * x[None, :])
+    return nodes.ravel(), (span * half[:, None] * w[None, :]).ravel()
 
 
 def tape_mutual(length, wa, wb, axial, lateral, dz) -> float:
-    h, k, s = 0.5 * (wa + wb), 0.5 * abs(wa - wb), -lateral
-    cuts = {-h, -k, k, h}
-    if -h < s < h:
-        cuts.add(s)
-    pts = sorted(cuts)
-    tot = 0.0
-    for p, q in zip(pts[:-1], pts[1:]):
-        if q - p <= 0.0:
+    """Mutual inductance of two parallel flat tapes of one length, widths wa and wb, their centres `axial` apart
+    along them, `lateral` across and dz out of plane: the mean filament mutual over all filament pairs,
+    (1 / wa wb) int W(v) M(length, axial, |(lateral + v, dz)|) dv over the pairs' lateral separation v, W(v) the
+    length of the widths' overlap at that separation (min(wa, wb) flat, falling to 0 at |v| = (wa + wb) / 2).
+    The integral is cut at W's corners and at v = -lateral, where filaments line up (a log singularity when dz
+    is 0): graded panels beside that point, four equal ones elsewhere."""
+    reach, flat = 0.5 * (wa + wb), 0.5 * abs(wa - wb)
+    sing = -lateral
+    cuts = {-reach, -flat, flat, reach}
+    if abs(sing) < reach:
+        cuts.add(sing)
+    cuts = sorted(cuts)
+    nodes, weights = [], []
+    for lo, hi in zip(cuts[:-1], cuts[1:]):
+        if hi <= lo:
             continue
-        toward = p if p == s else q if q == s else None
-        v, wt = _graded(p, q, toward, PANELS if toward is not None else 4, ORDER)
-        W = np.clip(np.minimum(0.5 * wa, v + 0.5 * wb) - np.maximum(-0.5 * wa, v - 0.5 * wb), 0.0, None)
-        tot += float(np.sum(wt * W * filament_mutual(length, np.full(len(v), axial), np.sqrt((lateral + v) ** 2 + dz * dz))))
-    return tot / (wa * wb)
+        end = lo if lo == sing else hi if hi == sing else None
+        v, wt = panel_rule(lo, hi, end, PANELS if end is not None else 4, ORDER)
+        nodes.append(v)
+        weights.append(wt)
+    v, wt = np.concatenate(nodes), np.concatenate(weights)
+    overlap = np.clip(np.minimum(reach - np.abs(v), min(wa, wb)), 0.0, None)
+    m = filament_mutual(length, np.full(len(v), float(axial)), np.hypot(lateral + v, dz))
+    return float(np.dot(wt * overlap, m)) / (wa * wb)
 
 
 def strip_self(length: float, width: float, thickness: float = 0.0) -> float:
@@ -85,7 +100,7 @@ def strip_self(length: float, width: float, thickness: float = 0.0) -> float:
 def strip_self_numeric(length: float, width):
     """A flat strip's partial self inductance as the mean filament mutual over its width pairs, by a graded
     Gauss rule toward the coincident pair (kernel.py:187-206).  width may be an array."""
-    s, ws = _graded(0.0, 1.0, 0.0, PANELS, ORDER)
+    s, ws = panel_rule(0.0, 1.0, 0.0, PANELS, ORDER)
     w = np.atleast_1d(np.asarray(width, float)).ravel()
     u = w[:, None] * s[None, :]
     out = 2.0 * (filament_mutual(length, 0.0, u) * ((1.0 - s) * ws)[None, :]).sum(axis=1)
@@ -121,21 +136,6 @@ def side_mutual(length: float, wa, wb, gap, steps=0.0, n: int = 8) -> np.ndarray
     return filament_mutual(length, axial, rho).mean(axis=(1, 2))
 
 
-def strip_kernel(n_axial: int, n_lateral: int, d: float, dz: float) -> np.ndarray:
-    """(2 n_axial - 1, 2 n_lateral - 1) mutual inductances of square strips at every grid offset."""
-    ia = np.arange(-(n_axial - 1), n_axial) * d
-    il = np.arange(-(n_lateral - 1), n_lateral) * d
-    K = filament_mutual(d, ia[:, None], np.sqrt(il[None, :] ** 2 + dz * dz))
-    ca, cl = n_axial - 1, n_lateral - 1
-    for oa in range(min(NEAR, n_axial - 1) + 1):
-        for ol in range(min(NEAR, n_lateral - 1) + 1):
-            m = tape_mutual(d, d, d, oa * d, ol * d, dz)
-            for pa in {ca + oa, ca - oa}:
-                for pl in {cl + ol, cl - ol}:
-                    K[pa, pl] = m
-    return K
-
-
 def near_values(n_axial: int, n_lateral: int, d: float, dz: float) -> np.ndarray:
     """(NEAR+1, NEAR+1) tape-integrated mutual inductances at the nearest offsets (kernel.py:287-294); offsets
     beyond the grid are zero."""
@@ -144,6 +144,20 @@ def near_values(n_axial: int, n_lateral: int, d: float, dz: float) -> np.ndarray
         for ol in range(min(NEAR, n_lateral - 1) + 1):
             out[oa, ol] = tape_mutual(d, d, d, oa * d, ol * d, dz)
     return out
+
+
+def strip_kernel(n_axial: int, n_lateral: int, d: float, dz: float) -> np.ndarray:
+    """(2 n_axial - 1, 2 n_lateral - 1) mutual inductances of square strips (side d, dz apart out of plane) at
+    every grid offset: filaments along the strips' axes, replaced by the tape integral (near_values) where
+    both |offsets| are at most NEAR pitches; the block is even in both offsets."""
+    axial = np.arange(1 - n_axial, n_axial) * d
+    across = np.arange(1 - n_lateral, n_lateral) * d
+    K = filament_mutual(d, axial[:, None], np.hypot(across[None, :], dz))
+    na, nl = min(NEAR, n_axial - 1), min(NEAR, n_lateral - 1)
+    near = near_values(n_axial, n_lateral, d, dz)
+    K[n_axial - 1 - na: n_axial + na, n_lateral - 1 - nl: n_lateral + nl] = \
+        near[np.ix_(np.abs(np.arange(-na, na + 1)), np.abs(np.arange(-nl, nl + 1)))]
+    return K
 
 
 def spectrum_quadrant(K: np.ndarray, P0: int, P1: int) -> np.ndarray:
@@ -155,18 +169,36 @@ def spectrum_quadrant(K: np.ndarray, P0: int, P1: int) -> np.ndarray:
     return np.ascontiguousarray(np.fft.fft2(Z).real[: P0 // 2 + 1, : P1 // 2 + 1])
 
 
+def skin_depth(f, sigma):
+    """delta = 1 / sqrt(pi f mu0 sigma); infinite at f = 0."""
+    with np.errstate(divide="ignore"):
+        return 1.0 / np.sqrt(np.pi * np.asarray(f, float) * MU0 * sigma)
+
+
+def _depths(t, f, sigma) -> np.ndarray:
+    """x = t / delta, the copper's thickness in skin depths (0 at DC)."""
+    t, f = np.broadcast_arrays(np.asarray(t, float), np.asarray(f, float))
+    return np.where(f > 0, t * np.sqrt(np.pi * np.maximum(f, 1e-300) * MU0 * sigma), 0.0)
+
+
+def u_coth_u(x) -> np.ndarray:
+    """u coth u at u = (1 + j) x, x >= 0: the one-face slab's impedance in units of its DC resistance.  Below
+    x = 0.1 its Laurent series to x^4 (u^2 = 2 j x^2, u^4 = -4 x^4): 1 + j 2 x^2 / 3 + 4 x^4 / 45; above, the
+    closed form with coth u = (1 + e^-2u) / (1 - e^-2u), which needs no clamp for thick copper."""
+    x = np.asarray(x, float)
+    u = (1 + 1j) * x
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+        e = np.exp(-2.0 * u)
+        closed = u * (1.0 + e) / (1.0 - e)
+    series = 1.0 + 4.0 * x ** 4 / 45.0 + 1j * (2.0 * x ** 2 / 3.0)
+    return np.where(x < 0.1, series, closed)
+
+
 def slab_impedance(t, f, sigma):
-    """Internal impedance per square of a one-face slab (kernel.py:47-75)."""
-    t = np.asarray(t, float)
-    f = np.asarray(f, float)
-    with np.errstate(divide="ignore", over="ignore", invalid="ignore"):
-        delta = 1.0 / np.sqrt(np.pi * np.maximum(f, 1e-300) * MU0 * sigma)
-        x = np.where(f > 0, t / delta, 0.0)
-        u = (1 + 1j) * np.minimum(x, 30.0)
-        exact = (1 + 1j) * x / np.tanh(np.where(x > 0, u, 1.0))
-        series = 1.0 + 4.0 * x ** 4 / 45.0 + 1j * (2.0 * x ** 2 / 3.0)
-        out = np.where(x < 0.1, series, exact) / (sigma * t)
-    return complex(out) if out.ndim == 0 else out
+    """Internal impedance per square of a slab t thick whose current returns on one face (kernel.py:47-75):
+    u coth u / (sigma t), u = (1 + j) t / delta."""
+    out = u_coth_u(_depths(t, f, sigma)) / (sigma * np.asarray(t, float))
+    return complex(out) if np.ndim(out) == 0 else out
 
 
 def face_sheet_impedance(t, f, sigma):
@@ -186,15 +218,10 @@ def face_sheet_impedance(t, f, sigma):
 
 
 def skin_thickness(t, f, sigma):
-    t = np.asarray(t, float)
-    f = np.asarray(f, float)
-    with np.errstate(divide="ignore", over="ignore", invalid="ignore"):
-        delta = 1.0 / np.sqrt(np.pi * np.maximum(f, 1e-300) * MU0 * sigma)
-        x = np.where(f > 0, t / delta, 0.0)
-        y = np.minimum(2 * x, 60.0)
-        exact = x * (np.sinh(y) + np.sin(y)) / (np.cosh(y) - np.cos(y))
-        out = t / np.where(x < 0.1, 1.0 + 4.0 * x ** 4 / 45.0, exact)
-    return float(out) if out.ndim == 0 else out
+    """The thickness a DC resistance takes to give the slab's AC resistance: t / Re(u coth u), since
+    Re(u coth u) = x (sinh 2x + sin 2x) / (cosh 2x - cos 2x) is the one-face slab's resistance ratio."""
+    out = np.asarray(t, float) / u_coth_u(_depths(t, f, sigma)).real
+    return float(out) if np.ndim(out) == 0 else out
 
 
 def vector_potential(a, b, pts, rho_min: float) -> np.ndarray:

@@ -39,90 +39,97 @@ def ring_edges(outline: np.ndarray, holes=()) -> tuple:
     return np.concatenate(a), np.concatenate(b)
 
 
+def _ragged(start, count) -> tuple:
+    """The members of integer ranges [start_i, start_i + count_i): (owner i, value) pairs, owners ascending."""
+    count = np.maximum(np.asarray(count, np.int64), 0)
+    owner = np.repeat(np.arange(len(count)), count)
+    base = np.cumsum(count) - count
+    return owner, np.asarray(start, np.int64)[owner] + (np.arange(len(owner)) - base[owner])
+
+
 def line_cover(ua, va, ub, vb, u0: float, du: float, n_lines: int, v0: float, d: float, n_cells: int) -> np.ndarray:
-    """(n_lines, n_cells): on each line u = u0 + m du the length of each interval [v0 + (c - 1/2) d, v0 + (c + 1/2) d]
-    inside the polygons with edges (ua, va) -> (ub, vb) (peec.py:533-580).  A scanline: an edge crosses the lines
-    with u in [min, max) of its ends (half open: a vertex on a line counts once, an edge along one not at all),
-    each line's crossings sorted along it bound the inside in pairs, each inside span adds its overlap with every
-    interval; a line with an odd number of crossings is skipped."""
+    """(n_lines, n_cells): on each line u = u0 + m du, the length of each cell interval
+    [v0 + (c - 1/2) d, v0 + (c + 1/2) d] that lies inside the polygons whose edges run (ua, va) -> (ub, vb)
+    (peec.py:533-580).  An edge meets the lines whose u lies in [min, max) of its ends' u (a vertex on a line
+    counts once, an edge along a line not at all); a line's crossings, sorted along it, alternate entering and
+    leaving the copper, and a line meeting an odd number of them is left empty.  With crossings c_1 < c_2 < ...
+    the covered length below v is sum_k (-1)^(k+1) (v - c_k)_+, so each crossing adds +-d to every cell from
+    its own on, less +-(c_k - its cell's lower end) in its own cell: a running sum along the line (a crossing
+    on a cell's lower end adds exactly nothing to that cell)."""
     out = np.zeros((n_lines, n_cells))
-    ua, va, ub, vb = (np.asarray(x, float) for x in (ua, va, ub, vb))
-    if len(ua) == 0 or n_lines <= 0 or n_cells <= 0:
+    ua, va, ub, vb = (np.asarray(a, float).ravel() for a in (ua, va, ub, vb))
+    if not len(ua) or n_lines <= 0 or n_cells <= 0:
         return out
-    lo, hi = np.minimum(ua, ub), np.maximum(ua, ub)
-    first = np.clip(np.ceil((lo - u0) / du), 0, n_lines).astype(np.int64)
-    last = np.clip(np.ceil((hi - u0) / du), 0, n_lines).astype(np.int64)
-    edges = np.flatnonzero(last > first)
-    if len(edges) == 0:
+    lo = np.clip(np.ceil((np.minimum(ua, ub) - u0) / du), 0, n_lines).astype(np.int64)
+    hi = np.clip(np.ceil((np.maximum(ua, ub) - u0) / du), 0, n_lines).astype(np.int64)
+    e, line = _ragged(lo, hi - lo)
+    if not len(e):
         return out
-    cnt = (last - first)[edges]
-    e = np.repeat(edges, cnt)
-    line = np.repeat(first[edges], cnt) + (np.arange(int(cnt.sum())) - np.repeat(np.cumsum(cnt) - cnt, cnt))
-    u = u0 + line * du
-    v = va[e] + (u - ua[e]) * (vb[e] - va[e]) / (ub[e] - ua[e])
+    t = (u0 + line * du - ua[e]) / (ub[e] - ua[e])
+    v = va[e] + t * (vb[e] - va[e])
     order = np.lexsort((v, line))
     line, v = line[order], v[order]
-    per_line = np.bincount(line, minlength=n_lines)
-    pos = np.arange(len(line)) - np.searchsorted(line, line)
-    opens = np.flatnonzero((pos % 2 == 0) & (per_line[line] % 2 == 0))
-    ln, a, b = line[opens], v[opens], v[opens + 1]
-    base, span = v0 - d / 2, n_cells * d
-    a, b = np.clip(a - base, 0.0, span), np.clip(b - base, 0.0, span)
-    keep = b > a
-    ln, a, b = ln[keep], a[keep], b[keep]
-    ca = np.minimum((a / d).astype(np.int64), n_cells - 1)
-    cb = np.minimum((b / d).astype(np.int64), n_cells - 1)
-    size = n_lines * n_cells
-    flat = out.reshape(-1)
-    inside = ca == cb
-    flat += np.bincount(ln[inside] * n_cells + ca[inside], b[inside] - a[inside], size)
-    cross = ~inside
-    l2, a2, b2, ca2, cb2 = ln[cross], a[cross], b[cross], ca[cross], cb[cross]
-    flat += np.bincount(l2 * n_cells + ca2, (ca2 + 1) * d - a2, size)
-    flat += np.bincount(l2 * n_cells + cb2, b2 - cb2 * d, size)
-    # whole intervals between a span's first and last: +d from ca + 1, -d from cb, summed along the line
-    steps = np.zeros((n_lines, n_cells + 1))
-    w = n_lines * (n_cells + 1)
-    steps.reshape(-1)[:] += np.bincount(l2 * (n_cells + 1) + ca2 + 1, np.full(len(l2), d), w)
-    steps.reshape(-1)[:] -= np.bincount(l2 * (n_cells + 1) + cb2, np.full(len(l2), d), w)
-    out += np.cumsum(steps, axis=1)[:, :n_cells]
+    first = np.searchsorted(line, line)
+    rank = np.arange(len(line)) - first
+    count = np.bincount(line, minlength=n_lines)
+    keep = count[line] % 2 == 0
+    line, v, sign = line[keep], v[keep], np.where(rank[keep] % 2 == 0, 1.0, -1.0)
+    span = n_cells * d
+    x = np.clip(v - (v0 - 0.5 * d), 0.0, span)
+    cell = np.minimum((x / d).astype(np.int64), n_cells - 1)
+    steps = np.bincount(line * n_cells + cell, sign * d, n_lines * n_cells).reshape(n_lines, n_cells)
+    out += np.cumsum(steps, axis=1)
+    out.reshape(-1)[:] -= np.bincount(line * n_cells + cell, sign * (x - cell * d), n_lines * n_cells)
     return out
 
 
 def cell_areas(pa, pb, xl: float, yl: float, d: float, wi: int, wj: int, right: np.ndarray) -> np.ndarray:
     """(wi, wj): the copper area of each cell [xl + i d, xl + (i+1) d] x [yl + j d, yl + (j+1) d] inside the
-    polygons with oriented edges pa -> pb, `right` the covered length of each cell's right border
-    (peec.py:583-622).  Green's theorem, area = closed integral of x dy: the edges cut at every grid line, each
-    piece adds (its mean x - the cell's left) dy to its cell; the cell's own right border adds d times its
-    covered length."""
-    out = np.zeros((wi, wj))
+    polygons with oriented edges pa -> pb, copper on their left, `right` the covered length of each cell's right
+    border (line_cover's convention; the areas of peec.py:583-622).  Green's theorem over the boundary of
+    copper-and-cell, area = closed int (x - x_i) dy: the cell's right border adds d times its covered length, its
+    left border nothing, and each polygon edge adds (its mean x - x_i) dy over every stretch of it that lies in
+    the cell.  An edge is cut into its stretches per column (a vertical edge on a border line belongs to the
+    column on its right, where it adds nothing) and each stretch per row."""
+    out = d * np.asarray(right, float)
     pa, pb = np.asarray(pa, float).reshape(-1, 2), np.asarray(pb, float).reshape(-1, 2)
-    if len(pa):
-        xa, ya, xb, yb = pa[:, 0], pa[:, 1], pb[:, 0], pb[:, 1]
-        ts, es = [np.zeros(len(xa)), np.ones(len(xa))], [np.arange(len(xa))] * 2
-        for a, b, origin, n in ((xa, xb, xl, wi + 1), (ya, yb, yl, wj + 1)):
-            lo, hi = np.minimum(a, b), np.maximum(a, b)
-            m0 = np.clip(np.ceil((lo - origin) / d), 0, n).astype(np.int64)
-            m1 = np.clip(np.ceil((hi - origin) / d), 0, n).astype(np.int64)
-            sel = np.flatnonzero(m1 > m0)
-            cnt = (m1 - m0)[sel]
-            e = np.repeat(sel, cnt)
-            m = np.repeat(m0[sel], cnt) + (np.arange(int(cnt.sum())) - np.repeat(np.cumsum(cnt) - cnt, cnt))
-            ts.append((origin + m * d - a[e]) / (b[e] - a[e]))
-            es.append(e)
-        t, e = np.concatenate(ts), np.concatenate(es)
-        order = np.lexsort((t, e))
-        t, e = t[order], e[order]
-        piece = e[1:] == e[:-1]
-        e, t0, t1 = e[:-1][piece], t[:-1][piece], t[1:][piece]
-        x0, y0 = xa[e] + t0 * (xb[e] - xa[e]), ya[e] + t0 * (yb[e] - ya[e])
-        x1, y1 = xa[e] + t1 * (xb[e] - xa[e]), ya[e] + t1 * (yb[e] - ya[e])
-        i = np.floor(((x0 + x1) / 2 - xl) / d).astype(np.int64)
-        j = np.floor(((y0 + y1) / 2 - yl) / d).astype(np.int64)
-        ok = (i >= 0) & (i < wi) & (j >= 0) & (j < wj)
-        add = ((x0 + x1) / 2 - (xl + i * d)) * (y1 - y0)
-        out.reshape(-1)[:] += np.bincount(i[ok] * wj + j[ok], add[ok], wi * wj)
-    return out + d * np.asarray(right, float)
+    if not len(pa):
+        return out
+    xa, ya, xb, yb = pa[:, 0], pa[:, 1], pb[:, 0], pb[:, 1]
+    keep = ya != yb                                       # edges along a row add no dy
+    xa, ya, xb, yb = xa[keep], ya[keep], xb[keep], yb[keep]
+    vertical = xa == xb
+    c0 = np.floor((np.minimum(xa, xb) - xl) / d).astype(np.int64)
+    c1 = np.floor((np.maximum(xa, xb) - xl) / d).astype(np.int64)
+    lo, hi = np.clip(c0, 0, wi - 1), np.clip(c1, 0, wi - 1)
+    e, col = _ragged(lo, np.where((c1 >= 0) & (c0 < wi), hi - lo + 1, 0))
+    # each stretch's x range and the y at its ends
+    left = xl + col * d
+    xs = np.maximum(np.minimum(xa[e], xb[e]), left)
+    xe = np.minimum(np.maximum(xa[e], xb[e]), left + d)
+    vert = vertical[e]
+    use = vert | (xe > xs)
+    e, col, xs, xe, vert, left = e[use], col[use], xs[use], xe[use], vert[use], left[use]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        slope = np.where(vert, 0.0, (yb[e] - ya[e]) / np.where(vert, 1.0, xb[e] - xa[e]))
+    ys = np.where(vert, ya[e], ya[e] + (xs - xa[e]) * slope)
+    ye = np.where(vert, yb[e], ya[e] + (xe - xa[e]) * slope)
+    # dy's sign is the edge's direction; the stretch runs from its lower end (x at it xlo) to its upper one
+    up = yb[e] > ya[e]
+    ylo, yhi = np.minimum(ys, ye), np.maximum(ys, ye)
+    xlo = np.where(ys <= ye, xs, xe)
+    xhi = np.where(ys <= ye, xe, xs)
+    r0 = np.floor((ylo - yl) / d).astype(np.int64)
+    r1 = np.floor((yhi - yl) / d).astype(np.int64)
+    rlo, rhi = np.clip(r0, 0, wj - 1), np.clip(r1, 0, wj - 1)
+    k, row = _ragged(rlo, np.where((r1 >= 0) & (r0 < wj), rhi - rlo + 1, 0))
+    bottom = yl + row * d
+    y0, y1 = np.maximum(ylo[k], bottom), np.minimum(yhi[k], bottom + d)
+    ok = y1 > y0
+    k, row, y0, y1 = k[ok], row[ok], y0[ok], y1[ok]
+    xm = xlo[k] + (0.5 * (y0 + y1) - ylo[k]) / (yhi[k] - ylo[k]) * (xhi[k] - xlo[k])
+    np.add.at(out, (col[k], row), np.where(up[k], 1.0, -1.0) * (xm - left[k]) * (y1 - y0))
+    return out
 
 
 def strip_widths(exists, cross, offset, forced, d: float, exact=None) -> tuple:
@@ -131,13 +138,20 @@ def strip_widths(exists, cross, offset, forced, d: float, exact=None) -> tuple:
     beside it too), else the share of its border the sub-grid saw copper cross, at least a forced track's own
     width, 1 where neither; the centre kept inside the cell; 0 where no strip exists."""
     exists = np.asarray(exists, bool)
-    w = np.where(forced > 0, np.maximum(cross, np.minimum(forced / d, 1.0)), cross)
-    w = np.where(w > 0, np.minimum(w, 1.0), 1.0)
+    cross, offset, forced = (np.asarray(a, float) for a in (cross, offset, forced))
+    # the sub-grid's estimate: the crossed share of the border, raised to a claiming track's own width
+    track = np.where(forced > 0, np.minimum(forced / d, 1.0), 0.0)
+    seen = np.maximum(cross, track)
+    picks = [seen > 0]
+    vals = [np.minimum(seen, 1.0)]
     if exact is not None:
-        w = np.where(exact > 0, np.minimum(exact, 3.0), w)
-    o = np.where(cross > 0, offset, 0.0)
-    lim = np.maximum((1.0 - w) / 2, 0.0)
-    return np.where(exists, w, 0.0), np.where(exists, np.clip(o, -lim, lim), 0.0)
+        exact = np.asarray(exact, float)
+        picks.insert(0, exact > 0)
+        vals.insert(0, np.minimum(exact, 3.0))
+    w = np.select(picks, vals, default=1.0)
+    room = np.maximum(0.5 * (1.0 - w), 0.0)
+    o = np.clip(np.where(cross > 0, offset, 0.0), -room, room)
+    return np.where(exists, w, 0.0), np.where(exists, o, 0.0)
 
 
 def adopt(cov, has, steps, reach: int = 1) -> np.ndarray:
@@ -145,32 +159,29 @@ def adopt(cov, has, steps, reach: int = 1) -> np.ndarray:
     along the offsets `steps` within `reach` steps (of two at one distance, the one with more copper of its own);
     values with none within reach are dropped (peec.py:625-656)."""
     cov, has = np.asarray(cov, float), np.asarray(has, bool)
-    own = np.where(has, cov, 0.0)
-    stray = np.where(has, 0.0, cov)
-    out = own.copy()
     ni, nj = cov.shape
-
-    def shifted(di, dj):
-        src = (slice(max(di, 0), ni + min(di, 0)), slice(max(dj, 0), nj + min(dj, 0)))
-        dst = (slice(max(-di, 0), ni + min(-di, 0)), slice(max(-dj, 0), nj + min(-dj, 0)))
-        return src, dst
+    out = np.where(has, cov, 0.0)
+    own = out.copy()
+    stray = np.where(has, 0.0, cov)
+    ii, jj = np.nonzero(stray > 0)
+    amount = stray[ii, jj]
     for k in range(1, reach + 1):
-        if not np.any(stray > 0):
+        if not len(ii):
             break
-        best = np.full(cov.shape, -1.0)
-        pick = np.full(cov.shape, -1)
+        # the candidates at distance k along each step: their own copper where the net is there, else -1
+        cand = np.full((len(steps), len(ii)), -1.0)
+        ti = np.empty((len(steps), len(ii)), np.int64)
+        tj = np.empty_like(ti)
         for q, (di, dj) in enumerate(steps):
-            src, dst = shifted(di * k, dj * k)
-            nb_has, nb_cov = np.zeros(cov.shape, bool), np.zeros(cov.shape)
-            nb_has[dst], nb_cov[dst] = has[src], own[src]
-            better = (stray > 0) & nb_has & (nb_cov > best)
-            best = np.where(better, nb_cov, best)
-            pick = np.where(better, q, pick)
-        for q, (di, dj) in enumerate(steps):
-            dst, src = shifted(di * k, dj * k)
-            moved = np.where(pick == q, stray, 0.0)
-            out[dst] += moved[src]
-        stray = np.where(pick >= 0, 0.0, stray)
+            ti[q], tj[q] = ii + k * di, jj + k * dj
+            on = (ti[q] >= 0) & (ti[q] < ni) & (tj[q] >= 0) & (tj[q] < nj)
+            hit = np.zeros(len(ii), bool)
+            hit[on] = has[ti[q][on], tj[q][on]]
+            cand[q, hit] = own[ti[q][hit], tj[q][hit]]
+        best = np.argmax(cand, axis=0)                    # the first of equals: steps' order breaks ties
+        found = cand[best, np.arange(len(ii))] >= 0
+        np.add.at(out, (ti[best, np.arange(len(ii))][found], tj[best, np.arange(len(ii))][found]), amount[found])
+        ii, jj, amount = ii[~found], jj[~found], amount[~found]
     return out
 
 
@@ -181,35 +192,33 @@ def series_factor(face, samples: list, has, axis: int) -> np.ndarray:
     lone narrow band only (at most BAND_STRIPS strips, no other strip of the net within 2 ADOPT_FACES along the
     border, copper at every sample line); 1 otherwise (peec.py:659-705)."""
     has = np.asarray(has, bool)
-    h = has if axis == 1 else has.T
-    if not h.any():
+    if not has.any():
         return np.ones(has.shape)
-    f_ = np.asarray(face, float) if axis == 1 else np.asarray(face, float).T
-    rows = [np.asarray(s, float) if axis == 1 else np.asarray(s, float).T for s in samples]
+    along = (lambda a: np.asarray(a, float)) if axis == 1 else (lambda a: np.asarray(a, float).T)
+    h = has if axis == 1 else has.T
     n0, n1 = h.shape
-    start = h & ~np.concatenate([np.zeros((n0, 1), bool), h[:, :-1]], axis=1)
-    run = np.cumsum(start, axis=1) - 1
-    r_i, c_i = np.nonzero(h)
-    key = r_i * n1 + run[r_i, c_i]
-    nk = n0 * n1
-    total = np.bincount(key, f_[h], nk)
-    size = np.bincount(key, minlength=nk)
-    far = n1 + 2 * ADOPT_FACES + 2
-    step = np.where(np.r_[True, r_i[1:] != r_i[:-1]], far, np.r_[far, c_i[1:] - c_i[:-1]])
-    head = step != 1
-    gap_before = np.full(nk, far)
-    gap_before[key[head]] = step[head] - 1
-    gap_after = np.where(np.r_[size[1:] > 0, False], np.r_[gap_before[1:], far], far)
-    lone = (size <= BAND_STRIPS) & (gap_before > 2 * ADOPT_FACES) & (gap_after > 2 * ADOPT_FACES)
-    inv, seen = np.zeros(nk), np.ones(nk, bool)
-    for srow in rows:
-        t = np.bincount(key, srow[h], nk)
-        seen &= t > 0
-        inv += 1.0 / np.maximum(t, 1e-300)
-    harmonic = len(rows) / np.maximum(inv, 1e-300)
+    # the bands: runs of strips along each row; +1 where one begins, -1 just past its end
+    edge = np.diff(np.pad(h.astype(np.int8), ((0, 0), (1, 1))), axis=1)
+    row, beg = np.nonzero(edge == 1)
+    _, end = np.nonzero(edge == -1)
+    size = end - beg
+    wide = 2 * ADOPT_FACES
+    same_prev = np.r_[False, row[1:] == row[:-1]]
+    same_next = np.r_[row[1:] == row[:-1], False]
+    gap_before = np.where(same_prev, beg - np.r_[0, end[:-1]], wide + 1)
+    gap_after = np.where(same_next, np.r_[beg[1:], 0] - end, wide + 1)
+    lone = (size <= BAND_STRIPS) & (gap_before > wide) & (gap_after > wide)
+    heads = np.cumsum(size) - size
+
+    def band_sum(a):
+        return np.add.reduceat(along(a)[h], heads)
+    total = band_sum(face)
+    widths = np.stack([band_sum(smp) for smp in samples])          # (samples, bands)
+    seen = np.all(widths > 0, axis=0)
+    harmonic = len(samples) / np.maximum(np.sum(1.0 / np.maximum(widths, 1e-300), axis=0), 1e-300)
     factor = np.where(lone & seen & (total > 0), harmonic / np.maximum(total, 1e-300), 1.0)
     out = np.ones(h.shape)
-    out[h] = factor[key]
+    out[h] = np.repeat(factor, size)
     return out if axis == 1 else out.T
 
 
@@ -308,10 +317,29 @@ STRIP_SAMPLES = 6    # peec.py:107: lines across each strip's length where its c
 ADOPT_CELLS = 2      # peec.py:111: ... and how far a cell's copper without a node of its net goes to find one
 
 
-def _bounds(pa: np.ndarray, pb: np.ndarray) -> tuple:
-    lo = np.minimum(pa.min(axis=0), pb.min(axis=0))
-    hi = np.maximum(pa.max(axis=0), pb.max(axis=0))
-    return float(lo[0]), float(lo[1]), float(hi[0]), float(hi[1])
+def _window(lo: float, hi: float, origin: float, d: float, n: int) -> tuple:
+    """Grid indices [i0, i1) of the nodes whose cells can hold copper between lo and hi, with two cells of
+    margin below and three above (the adoption reach)."""
+    return max(int(math.floor((lo - origin) / d)) - 2, 0), min(int(math.ceil((hi - origin) / d)) + 3, n)
+
+
+def _border_widths(xa, ya, xe, ye, i0: int, wi: int, j0: int, wj: int, x0: float, y0: float, d: float, strips,
+                   lead: int):
+    """For the strips along x of a window (its cells i0 .. i0+wi, j0 .. j0+wj): the covered length of each
+    strip's border line x = x_i + d/2 over d, copper on lines without a strip of the net adopted by the nearest
+    strip along the border (within ADOPT_FACES), and the series factor of lone narrow bands from the width at
+    STRIP_SAMPLES lines across each strip's length.  The border lines are scanned from the window's lead-th
+    border before the strips' first (lead 1: from its left edge, the lines' cover is also every cell's right
+    border; lead 0: from the first strip's own line), so the lines fall where the reference puts them.  Returns
+    (widths, factors, the cover of every scanned line).  The y strips are the same with x and y swapped."""
+    q = STRIP_SAMPLES
+    along = ((0, 1), (0, -1))
+    lines = line_cover(xa, ya, xe, ye, x0 + (i0 + 0.5 - lead) * d, d, wi - 1 + 2 * lead, y0 + j0 * d, d, wj)
+    width = adopt(lines[lead:lead + wi - 1, :] / d, strips, along, ADOPT_FACES)
+    cuts = line_cover(xa, ya, xe, ye, x0 + (i0 + 0.5 / q) * d, d / q, (wi - 1) * q, y0 + j0 * d, d, wj) / d
+    cuts = cuts.reshape(wi - 1, q, wj)
+    samples = [adopt(cuts[:, p, :], strips, along, ADOPT_FACES) for p in range(q)]
+    return width, series_factor(width, samples, strips, 1), lines
 
 
 def exact_copper(nets: list, label: np.ndarray, xb: np.ndarray, yb: np.ndarray, x0: float, y0: float,
@@ -326,41 +354,28 @@ def exact_copper(nets: list, label: np.ndarray, xb: np.ndarray, yb: np.ndarray, 
     nx, ny = label.shape
     ex_x, ex_y, area = np.zeros((nx - 1, ny)), np.zeros((nx, ny - 1)), np.zeros((nx, ny))
     kx, ky = np.ones((nx - 1, ny)), np.ones((nx, ny - 1))
-    along_rows, along_cols = ((0, 1), (0, -1)), ((1, 0), (-1, 0))
-    q = STRIP_SAMPLES
     for k, edges in enumerate(nets):
         if edges is None or len(edges[0]) == 0:
             continue
-        pa, pb = edges
-        bx0, by0, bx1, by1 = _bounds(pa, pb)
-        i0, i1 = max(int(math.floor((bx0 - x0) / d)) - 2, 0), min(int(math.ceil((bx1 - x0) / d)) + 3, nx)
-        j0, j1 = max(int(math.floor((by0 - y0) / d)) - 2, 0), min(int(math.ceil((by1 - y0) / d)) + 3, ny)
+        pa, pb = (np.asarray(e, float).reshape(-1, 2) for e in edges)
+        lo, hi = np.minimum(pa.min(0), pb.min(0)), np.maximum(pa.max(0), pb.max(0))
+        i0, i1 = _window(lo[0], hi[0], x0, d, nx)
+        j0, j1 = _window(lo[1], hi[1], y0, d, ny)
         wi, wj = i1 - i0, j1 - j0
         if wi < 2 or wj < 2:
             continue
-        xa, ya, xe, ye = pa[:, 0], pa[:, 1], pb[:, 0], pb[:, 1]
-        # vertical borders x = x_i - d/2 (line m: the left border of window column m) and horizontal ones
-        # y = y_j + d/2 between window rows: the copper each cell's stretch of them holds
-        vert = line_cover(xa, ya, xe, ye, x0 + (i0 - 0.5) * d, d, wi + 1, y0 + j0 * d, d, wj)
-        horiz = line_cover(ya, xa, ye, xe, y0 + (j0 + 0.5) * d, d, wj - 1, x0 + i0 * d, d, wi).T
         mine = label[i0:i1, j0:j1] == k
         sx = xb[i0:i1 - 1, j0:j1] & mine[:-1, :]
         sy = yb[i0:i1, j0:j1 - 1] & mine[:, :-1]
-        fx = adopt(vert[1:wi, :] / d, sx, along_rows, ADOPT_FACES)
-        fy = adopt(horiz / d, sy, along_cols, ADOPT_FACES)
-        ex_x[i0:i1 - 1, j0:j1] += fx
-        ex_y[i0:i1, j0:j1 - 1] += fy
-        # the width along each strip: q lines across its length at x_i + (p + 1/2) d / q
-        cut_x = (line_cover(xa, ya, xe, ye, x0 + (i0 + 0.5 / q) * d, d / q, (wi - 1) * q, y0 + j0 * d, d, wj)
-                 / d).reshape(wi - 1, q, wj)
-        cut_y = (line_cover(ya, xa, ye, xe, y0 + (j0 + 0.5 / q) * d, d / q, (wj - 1) * q, x0 + i0 * d, d, wi)
-                 / d).reshape(wj - 1, q, wi)
-        samples_x = [adopt(cut_x[:, p, :], sx, along_rows, ADOPT_FACES) for p in range(q)]
-        samples_y = [adopt(cut_y[:, p, :].T, sy, along_cols, ADOPT_FACES) for p in range(q)]
-        kx[i0:i1 - 1, j0:j1][sx] = series_factor(fx, samples_x, sx, 1)[sx]
-        ky[i0:i1, j0:j1 - 1][sy] = series_factor(fy, samples_y, sy, 0)[sy]
-        cells = cell_areas(pa, pb, x0 + (i0 - 0.5) * d, y0 + (j0 - 0.5) * d, d, wi, wj, vert[1:wi + 1, :]) / (d * d)
-        area[i0:i1, j0:j1] += adopt(np.clip(cells, 0.0, 1.0), mine, along_cols + along_rows, ADOPT_CELLS)
+        wx, fx, borders = _border_widths(pa[:, 0], pa[:, 1], pb[:, 0], pb[:, 1], i0, wi, j0, wj, x0, y0, d, sx, 1)
+        wy, fy, _ = _border_widths(pa[:, 1], pa[:, 0], pb[:, 1], pb[:, 0], j0, wj, i0, wi, y0, x0, d, sy.T, 0)
+        ex_x[i0:i1 - 1, j0:j1] += wx
+        ex_y[i0:i1, j0:j1 - 1] += wy.T
+        kx[i0:i1 - 1, j0:j1][sx] = fx[sx]
+        ky[i0:i1, j0:j1 - 1][sy] = fy.T[sy]
+        cells = cell_areas(pa, pb, x0 + (i0 - 0.5) * d, y0 + (j0 - 0.5) * d, d, wi, wj, borders[1:wi + 1, :]) / (d * d)
+        # a cell's copper with no node of its net goes to the nearest node that has one, across rows first
+        area[i0:i1, j0:j1] += adopt(np.clip(cells, 0.0, 1.0), mine, ((1, 0), (-1, 0), (0, 1), (0, -1)), ADOPT_CELLS)
     return ex_x, ex_y, area, kx, ky
 
 
@@ -372,73 +387,80 @@ def coarse_from_fine(nets: list, x0: float, y0: float, d: float, nx: int, ny: in
     that spans at least s sub-grid points, else -1; cross_x (nx-1, ny) / cross_y (nx, ny-1): the fraction of
     the s sub-grid strips across the border two cells' kept pieces join by; fill (nx, ny): the kept piece's share
     of the cell; off_x / off_y: the crossing strips' mean position along the border from its middle, over d)."""
-    from scipy.sparse.csgraph import connected_components
-    import scipy.sparse as sp
     from .synth import copper_at
     df = d / s
     mx, my = nx * s, ny * s
-    xf = x0 - d / 2 + (np.arange(mx) + 0.5) * df
-    yf = y0 - d / 2 + (np.arange(my) + 0.5) * df
-    fine = -np.ones((mx, my), np.int32)
+    xf = x0 - 0.5 * d + (np.arange(mx) + 0.5) * df
+    yf = y0 - 0.5 * d + (np.arange(my) + 0.5) * df
+    fine = np.full((mx, my), -1, np.int64)
     for k, poly in enumerate(nets):
         if poly is None:
             continue
         polys = polygons_of(poly)
-        bx0, by0 = np.min([np.min(np.asarray(o, float), axis=0) for o, _ in polys], axis=0)
-        bx1, by1 = np.max([np.max(np.asarray(o, float), axis=0) for o, _ in polys], axis=0)
-        p0, p1 = max(int(math.floor((bx0 - xf[0]) / df)) - 1, 0), min(int(math.ceil((bx1 - xf[0]) / df)) + 2, mx)
-        q0, q1 = max(int(math.floor((by0 - yf[0]) / df)) - 1, 0), min(int(math.ceil((by1 - yf[0]) / df)) + 2, my)
-        if p0 >= p1 or q0 >= q1:
+        pts = np.concatenate([np.asarray(o, float) for o, _ in polys])
+        a = np.searchsorted(xf, pts[:, 0].min(), "left"), np.searchsorted(xf, pts[:, 0].max(), "right")
+        b = np.searchsorted(yf, pts[:, 1].min(), "left"), np.searchsorted(yf, pts[:, 1].max(), "right")
+        if a[0] >= a[1] or b[0] >= b[1]:
             continue
-        X, Y = np.meshgrid(xf[p0:p1], yf[q0:q1], indexing="ij")
-        win = fine[p0:p1, q0:q1]
-        inside = np.zeros(X.shape, bool)
+        X, Y = np.meshgrid(xf[a[0]:a[1]], yf[b[0]:b[1]], indexing="ij")
+        hit = np.zeros(X.shape, bool)
         for outline, holes in polys:
-            inside |= copper_at(X, Y, np.asarray(outline, float), [np.asarray(h, float) for h in holes])
-        win[inside & (win < 0)] = k
-    same_x = (fine[:-1, :] >= 0) & (fine[:-1, :] == fine[1:, :])         # sub-grid strips within one net
-    same_y = (fine[:, :-1] >= 0) & (fine[:, :-1] == fine[:, 1:])
-    border_x = ((np.arange(mx - 1) + 1) % s == 0)[:, None]                # ... that cross a cell border
-    border_y = ((np.arange(my - 1) + 1) % s == 0)[None, :]
-    n = mx * my
-    at = np.arange(n).reshape(mx, my)
-    inner_x, inner_y = same_x & ~border_x, same_y & ~border_y           # the cells' pieces: strips inside cells
-    a = np.concatenate([at[:-1, :][inner_x], at[:, :-1][inner_y]])
-    b = np.concatenate([at[1:, :][inner_x], at[:, 1:][inner_y]])
-    _, piece = connected_components(sp.coo_matrix((np.ones(len(a), np.int8), (a, b)), shape=(n, n)), directed=False)
-    piece = piece.reshape(mx, my)
-    cell_of = (np.arange(mx) // s)[:, None] * ny + (np.arange(my) // s)[None, :]
+            hit |= copper_at(X, Y, np.asarray(outline, float), [np.asarray(q, float) for q in holes])
+        win = fine[a[0]:a[1], b[0]:b[1]]
+        win[hit & (win < 0)] = k
     cu = fine >= 0
-    pid = piece[cu]
-    size = np.bincount(pid, minlength=n)
-    p_cell, p_net = np.full(n, -1), np.full(n, -1)
-    p_cell[pid] = cell_of[cu]
-    p_net[pid] = fine[cu]
-    pieces = np.unique(pid)
-    pieces = pieces[np.lexsort((-size[pieces], p_cell[pieces]))]           # per cell, the largest piece first
-    lead = np.ones(len(pieces), bool)
-    lead[1:] = p_cell[pieces[1:]] != p_cell[pieces[:-1]]
-    kept = pieces[lead]
-    kept = kept[size[kept] >= s]
-    label = -np.ones(nx * ny, int)
-    label[p_cell[kept]] = p_net[kept]
+    # pieces: sub-grid points of one net joined inside their cell (4-neighbours), named by their least flat
+    # index through min-label propagation (the join never crosses a cell border)
+    lab = np.where(cu, np.arange(mx * my).reshape(mx, my), np.iinfo(np.int64).max)
+    join_x = cu[:-1, :] & (fine[:-1, :] == fine[1:, :]) & ((np.arange(1, mx) % s) != 0)[:, None]
+    join_y = cu[:, :-1] & (fine[:, :-1] == fine[:, 1:]) & ((np.arange(1, my) % s) != 0)[None, :]
+    while True:
+        new = lab.copy()
+        np.minimum(new[:-1, :], np.where(join_x, lab[1:, :], new[:-1, :]), out=new[:-1, :])
+        np.minimum(new[1:, :], np.where(join_x, lab[:-1, :], new[1:, :]), out=new[1:, :])
+        np.minimum(new[:, :-1], np.where(join_y, lab[:, 1:], new[:, :-1]), out=new[:, :-1])
+        np.minimum(new[:, 1:], np.where(join_y, lab[:, :-1], new[:, 1:]), out=new[:, 1:])
+        if np.array_equal(new, lab):
+            break
+        lab = new
+    size = np.bincount(lab[cu], minlength=mx * my)
+    cell = (np.arange(mx) // s)[:, None] * ny + (np.arange(my) // s)[None, :]
+    # each cell keeps its largest piece (the least name of equals) when it spans at least s points
+    names = np.flatnonzero(size)
+    cell_of = cell.ravel()[names]
+    order = np.lexsort((names, -size[names], cell_of))
+    first = np.r_[True, cell_of[order][1:] != cell_of[order][:-1]]
+    best = names[order][first]
+    best = best[size[best] >= s]
+    label = np.full(nx * ny, -1, np.int64)
+    label[cell.ravel()[best]] = fine.ravel()[best]
     fill = np.zeros(nx * ny)
-    fill[p_cell[kept]] = size[kept] / (s * s)
-    is_kept = np.zeros(n, bool)
-    is_kept[kept] = True
-    on = cu & is_kept[piece]
-    cross_x, off_x = np.zeros((nx - 1, ny)), np.zeros((nx - 1, ny))
-    fi, fj = np.nonzero(same_x & border_x & on[:-1, :] & on[1:, :])
-    np.add.at(cross_x, (fi // s, fj // s), 1.0 / s)
-    np.add.at(off_x, (fi // s, fj // s), ((fj % s + 0.5) / s - 0.5) / s)
-    cross_y, off_y = np.zeros((nx, ny - 1)), np.zeros((nx, ny - 1))
-    fi, fj = np.nonzero(same_y & border_y & on[:, :-1] & on[:, 1:])
-    np.add.at(cross_y, (fi // s, fj // s), 1.0 / s)
-    np.add.at(off_y, (fi // s, fj // s), ((fi % s + 0.5) / s - 0.5) / s)
-    with np.errstate(invalid="ignore", divide="ignore"):
-        off_x = np.where(cross_x > 0, off_x / cross_x, 0.0)
-        off_y = np.where(cross_y > 0, off_y / cross_y, 0.0)
-    return label.reshape(nx, ny), cross_x, cross_y, fill.reshape(nx, ny), off_x, off_y
+    fill[cell.ravel()[best]] = size[best] / (s * s)
+    kept = np.zeros(mx * my, bool)
+    kept[best] = True
+    on = cu & kept[np.where(cu, lab, 0)]
+
+    def crossings(hit, coarse, along, shape):
+        """Sub-grid strips joining two kept pieces across cell borders: per coarse strip their count over s
+        and their mean position along the border from its middle, over d."""
+        i, j = np.nonzero(hit)
+        ci, cj = coarse(i, j)
+        pos = along(i, j) % s
+        count = np.zeros(shape)
+        spread = np.zeros(shape)
+        np.add.at(count, (ci, cj), 1.0)
+        np.add.at(spread, (ci, cj), 2.0 * pos + 1.0 - s)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            off = np.where(count > 0, spread / (2.0 * s * count), 0.0)
+        return count / s, off
+    rows_x = np.arange(s - 1, mx - 1, s)                  # sub-rows whose next sub-row is in the next cell
+    cols_y = np.arange(s - 1, my - 1, s)
+    hit_x = on[rows_x, :] & on[rows_x + 1, :] & (fine[rows_x, :] == fine[rows_x + 1, :])
+    hit_y = on[:, cols_y] & on[:, cols_y + 1] & (fine[:, cols_y] == fine[:, cols_y + 1])
+    cx, ox = crossings(hit_x, lambda i, j: (i, j // s), lambda i, j: j, (nx - 1, ny))
+    cy, oy = crossings(hit_y, lambda i, j: (i // s, j), lambda i, j: i, (nx, ny - 1))
+    return label.reshape(nx, ny), cx, cy, fill.reshape(nx, ny), ox, oy
+
 
 
 PIECE_TOL = 0.005    # peec.py:106: copper of one net within this of itself (mm) is one piece (touching fills)

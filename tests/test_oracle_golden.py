@@ -169,8 +169,15 @@ def test_branch_impedances_match_reference():
 
 def test_routed_board_is_the_rasterised_one():
     """routed_pair's fixture holds the board as raster.build_layer made it from its polygons: made again, the
-    masks and widths are the same, bit for bit."""
+    masks and labels are the same bit for bit and the widths, fills and areas to 1e-12 of their scale (with
+    the same exact zeros)."""
     z, board = load("routed_pair")
     again = synth.routed_pair().to_arrays()
     for k, v in again.items():
-        assert np.array_equal(np.asarray(v), z[f"board_{k}"]), k
+        v, ref = np.asarray(v), z[f"board_{k}"]
+        if v.dtype.kind == "f" and ref.dtype.kind == "f":
+            scale = max(float(np.abs(ref).max(initial=0.0)), 1e-300)
+            assert v.shape == ref.shape and np.array_equal(v == 0, ref == 0), k
+            assert float(np.abs(v - ref).max(initial=0.0)) <= 1e-12 * scale, k
+        else:
+            assert np.array_equal(v, ref), k
