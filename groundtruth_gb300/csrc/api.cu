@@ -143,6 +143,7 @@ struct Scope {
 
 struct Orient {
     int n0, n1, P0, P1, di, dj;
+    int ld0;                                // the FFT grid's row stride: n0 rounded up to a multiple of 16
     int64_t off;
     int rows[2] = {0, 0}, bt[2] = {0, 0};   // tuned launch shapes per precision (0: not tuned)
     float* spec32;
@@ -203,7 +204,7 @@ struct gt_geometry {
     int64_t* d_sterm_ptr = nullptr;
     int* d_sterm_tab = nullptr;
     double* d_sterm_coef = nullptr;
-    int64_t maxT = 0;  // largest S * P1 * n0 of the two orientations
+    int64_t maxT = 0;  // largest S * P1 * ld0 of the two orientations
     int device = 0;    // the CUDA device the geometry's buffers live on (current at gt_geometry_create)
     // the last n_lowrank branches are left out of the S-term map: a derived stack whose operators come from
     // gt_operators_derive (its base's factorisations plus a low-rank update)
@@ -412,6 +413,7 @@ static void matvec(gt_geometry* G, gt_operators* ops, const cx<R>* x, const cx<R
         a.tw1 = tw1_of<R>(o);
         a.spec = spec_of<R>(o);
         a.T = T;
+        a.ldt = o.ld0;
         a.mask = G->geo.mask;
         a.col_op = col_op;
         a.omega = ops->omega;
@@ -1025,6 +1027,7 @@ void lp_with_scratch(gt_geometry* G, int ncol, const c64* x, c64* y, void* scrat
         a.tw1 = o.tw1_64;
         a.spec = o.spec64;
         a.T = static_cast<c64*>(scratch);
+        a.ldt = o.ld0;
         a.mask = G->geo.mask;
         a.mode = 2;
         launch_lp<double>(a, st);
@@ -1225,7 +1228,8 @@ int gt_geometry_create(const gt_geometry_desc* d, gt_geometry** out) {
             (ax == 0 ? o.tw0_64 : o.tw1_64) = p.upload(t64.data(), P);
             (ax == 0 ? o.tw0_32 : o.tw1_32) = p.upload(t32.data(), P);
         }
-        G->maxT = std::max<int64_t>(G->maxT, (int64_t)S * o.P1 * o.n0);
+        o.ld0 = (o.n0 + 15) & ~15;
+        G->maxT = std::max<int64_t>(G->maxT, (int64_t)S * o.P1 * o.ld0);
     }
     // fronts
     const int nf = d->n_fronts;

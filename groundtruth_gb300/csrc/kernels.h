@@ -66,7 +66,8 @@ template <typename R> struct LpArgs {
     const cx<R>* tw0;      // twiddles of the column length P0
     const cx<R>* tw1;      // of the row length P1
     const R* spec;         // (Q1, Q0, S, S)
-    cx<R>* T;              // [ncol][S][P1][n0]
+    cx<R>* T;              // [ncol][S][P1][ldt]
+    int ldt;               // T's row stride (>= n0; a multiple of 16 so the row passes move aligned 128-byte runs)
     const uint8_t* mask;
     const int* col_op;
     const double* omega;

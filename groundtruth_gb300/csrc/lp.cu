@@ -26,7 +26,8 @@ constexpr int MAXS = 8;
 
 template <typename R, int PL>
 __global__ void __launch_bounds__(1024) lp_pass_a(const cx<R>* __restrict__ x, int64_t ldx, int64_t off, int S, int n0, int n1, int P1,
-                          int rows, const cx<R>* __restrict__ tw, cx<R>* __restrict__ T, const int* __restrict__ col_list) {
+                          int rows, const cx<R>* __restrict__ tw, cx<R>* __restrict__ T, const int* __restrict__ col_list,
+                          int ldt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw);
     const int P = PL ? PL : P1;                  // compile-time when specialised
@@ -46,17 +47,17 @@ __global__ void __launch_bounds__(1024) lp_pass_a(const cx<R>* __restrict__ x, i
     __syncthreads();
     fft_row_t<R, false, PL, true, false>(buf + r * stride, r < rows, P, tw, team, t);
     // written transposed: rows (a power of two) consecutive entries per frequency column
-    cx<R>* Ts = T + ((int64_t)blockIdx.z * S + s) * (int64_t)P * n0;
+    cx<R>* Ts = T + ((int64_t)blockIdx.z * S + s) * (int64_t)P * ldt;
     const int lr = __ffs(rows) - 1;
     for (int idx = threadIdx.x; idx < rows * P; idx += blockDim.x) {
         const int c = idx >> lr, rr = idx & (rows - 1);
-        if (i0 + rr < n0) Ts[(int64_t)c * n0 + i0 + rr] = buf[rr * stride + spad(c)];
+        if (i0 + rr < n0) Ts[(int64_t)c * ldt + i0 + rr] = buf[rr * stride + spad(c)];
     }
 }
 
 template <typename R, int PL>
 __global__ void __launch_bounds__(1024) lp_pass_b(int S, int n0, int P0, int P1, int ncol, int bt, const R* __restrict__ spec,
-                          const cx<R>* __restrict__ tw, cx<R>* __restrict__ T) {
+                          const cx<R>* __restrict__ tw, cx<R>* __restrict__ T, int ldt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw);
     const int P = PL ? PL : P0;                  // compile-time when specialised
@@ -69,7 +70,7 @@ __global__ void __launch_bounds__(1024) lp_pass_b(int S, int n0, int P0, int P1,
     const int team = P / 8;
     const int row = threadIdx.x / team, t = threadIdx.x - row * team;
     const int rb = row / S, rs = row - rb * S;
-    cx<R>* Trow = T + (((int64_t)(b0 + rb) * S + rs) * P1 + c) * n0;
+    cx<R>* Trow = T + (((int64_t)(b0 + rb) * S + rs) * P1 + c) * ldt;
     if (row < nrows)
         for (int p = t; p < P; p += team) buf[row * stride + spad(p)] = p < n0 ? Trow[p] : zero<R>();
     __syncthreads();
@@ -153,7 +154,7 @@ __device__ __forceinline__ int b8_stages(cx<R>* b0, cx<R>* b1, int cur, int t, c
 
 template <typename R, int P, int S>
 __global__ void __launch_bounds__(512) lp_pass_b8(int n0, int P1, int ncol, int bt, const R* __restrict__ spec,
-                                                  const cx<R>* __restrict__ tw, cx<R>* __restrict__ T) {
+                                                  const cx<R>* __restrict__ tw, cx<R>* __restrict__ T, int ldt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int TEAM = P / 8, NBF = P / 8, ST = lp_srow(P), Q0 = P / 2 + 1;
     const int c = blockIdx.x;
@@ -162,7 +163,7 @@ __global__ void __launch_bounds__(512) lp_pass_b8(int n0, int P1, int ncol, int 
     const bool act = b < ncol;
     cx<R>* b0 = reinterpret_cast<cx<R>*>(smem_raw) + tb * S * ST;
     cx<R>* b1 = reinterpret_cast<cx<R>*>(smem_raw) + (bt + tb) * S * ST;
-    cx<R>* Trow = T + ((int64_t)min(b, ncol - 1) * S * P1 + c) * n0;      // sheet s at + s * P1 * n0
+    cx<R>* Trow = T + ((int64_t)min(b, ncol - 1) * S * P1 + c) * ldt;     // sheet s at + s * P1 * ldt
     cx<R> v[S][8];
     // forward stage 1 (NS = 1) from T: inputs t + r P/8, the upper half zero
 #pragma unroll
@@ -170,7 +171,7 @@ __global__ void __launch_bounds__(512) lp_pass_b8(int n0, int P1, int ncol, int 
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
             const int p = t + r * NBF;
-            v[s][r] = (act && p < n0) ? Trow[(int64_t)s * P1 * n0 + p] : zero<R>();
+            v[s][r] = (act && p < n0) ? Trow[(int64_t)s * P1 * ldt + p] : zero<R>();
         }
         dft8_h<R, false>(v[s]);
 #pragma unroll
@@ -247,7 +248,7 @@ __global__ void __launch_bounds__(512) lp_pass_b8(int n0, int P1, int ncol, int 
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
                 const int p = t + r * NBF;
-                if (act && p < n0) Trow[(int64_t)s * P1 * n0 + p] = w8[r];
+                if (act && p < n0) Trow[(int64_t)s * P1 * ldt + p] = w8[r];
             }
         }
     }
@@ -265,7 +266,7 @@ constexpr int BW_WARPS = 4;
 
 template <int S>
 __global__ void __launch_bounds__(BW_WARPS * 32, GT_BW_MINB) lp_pass_bw(int n0, int P1, int ncol, const float* __restrict__ spec,
-                                                            const c32* __restrict__ tw, c32* __restrict__ T) {
+                                                            const c32* __restrict__ tw, c32* __restrict__ T, int ldt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int P = 512, Q0 = P / 2 + 1, CPW = S == 2 ? 1 : 2;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -279,7 +280,7 @@ __global__ void __launch_bounds__(BW_WARPS * 32, GT_BW_MINB) lp_pass_bw(int n0, 
     for (int q = 0; q < 2; ++q) {
         const int b = S == 2 ? b0 : b0 + q, s = S == 2 ? q : 0;
         ok[q] = b < ncol;
-        row[q] = T + (((int64_t)min(b, ncol - 1) * S + s) * P1 + c) * n0;
+        row[q] = T + (((int64_t)min(b, ncol - 1) * S + s) * P1 + c) * ldt;
     }
     c32 v[2][16];
 #pragma unroll
@@ -323,12 +324,122 @@ __global__ void __launch_bounds__(BW_WARPS * 32, GT_BW_MINB) lp_pass_bw(int n0, 
         }
 }
 
+// Row passes for P1 = 512 in FP32 (n1 <= 256): a block of RW_WARPS warps takes RW_ROWS = 16 consecutive rows
+// i0 .. i0+15 of one sheet of one column, two rows per warp (fftw.cuh).  The frequency columns pass through a
+// shared tile [c][16] (rows padded to 17) so that each column c's 16 rows are one aligned 128-byte run of T
+// (T's rows are ldt long, a multiple of 16: rows i >= n0 of the run are the transforms of zero rows, which no
+// pass reads).  The tile takes the place of the warps' exchange tiles once every warp is done with its own.
+constexpr int RW_WARPS = 8, RW_ROWS = 2 * RW_WARPS, RW_TS = RW_ROWS + 1;
+#ifndef GT_RW_MINB
+#define GT_RW_MINB 2        // blocks per SM the row passes' register budget is cut for
+#endif
+constexpr size_t RW_SMEM = (size_t)(RW_WARPS * WX_SLOTS > 512 * RW_TS ? RW_WARPS * WX_SLOTS : 512 * RW_TS) * sizeof(c32);
+
+__global__ void __launch_bounds__(RW_WARPS * 32, GT_RW_MINB) lp_pass_aw(const c32* __restrict__ x, int64_t ldx, int64_t off, int S,
+                                                               int n0, int n1, int ldt, const c32* __restrict__ tw,
+                                                               c32* __restrict__ T, const int* __restrict__ col_list) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    c32* sm = reinterpret_cast<c32*>(smem_raw);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i0 = blockIdx.x * RW_ROWS, s = blockIdx.y;
+    const int col = col_list ? col_list[blockIdx.z] : blockIdx.z;
+    const c32* xs = x + (int64_t)col * ldx + off + (int64_t)s * n0 * n1;
+    c32 v[2][16];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int i = i0 + 2 * warp + q;
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const int j = lane + 32 * r;
+            v[q][r] = (i < n0 && j < n1) ? xs[(int64_t)i * n1 + j] : zero<float>();
+        }
+    }
+    c32 u[32];
+    fft512_fwd2<float, true>(v, u, sm + warp * WX_SLOTS, tw);
+    __syncthreads();                               // every warp is past its exchange: the tile may reuse them
+    {
+        const int il = 2 * warp + (lane >> 4), k1 = lane & 15;
+#pragma unroll
+        for (int k2 = 0; k2 < 32; ++k2) sm[(k1 + 16 * k2) * RW_TS + il] = u[k2];
+    }
+    __syncthreads();
+    c32* Ts = T + ((int64_t)blockIdx.z * S + s) * 512 * ldt + i0;
+    for (int idx = threadIdx.x; idx < 512 * (RW_ROWS / 2); idx += RW_WARPS * 32) {
+        const int c = idx >> 3, m = idx & 7;
+        const c32 a = sm[c * RW_TS + 2 * m], b = sm[c * RW_TS + 2 * m + 1];
+        *reinterpret_cast<float4*>(Ts + (int64_t)c * ldt + 2 * m) = make_float4(a.re, a.im, b.re, b.im);
+    }
+}
+
+// mode 0: out = R_t x + j w L - (V[a] - V[b]); 1: out = rhs - (that); 2: out = L
+__global__ void __launch_bounds__(RW_WARPS * 32, GT_RW_MINB) lp_pass_cw(const c32* __restrict__ T, const c32* __restrict__ x,
+                                                               const c32* __restrict__ rhs, c32* __restrict__ out,
+                                                               int64_t ld, int64_t off, int64_t off_v, int S, int n0,
+                                                               int n1, int nx, int ny, int di, int dj, int ldt,
+                                                               const c32* __restrict__ tw, const uint8_t* __restrict__ mask,
+                                                               const int* __restrict__ col_op,
+                                                               const double* __restrict__ omega, const c64* __restrict__ zs,
+                                                               int mode, const int* __restrict__ col_list,
+                                                               const int* __restrict__ sheet_layer) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    c32* sm = reinterpret_cast<c32*>(smem_raw);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i0 = blockIdx.x * RW_ROWS, s = blockIdx.y;
+    const int col = col_list ? col_list[blockIdx.z] : blockIdx.z;
+    const c32* Ts = T + ((int64_t)blockIdx.z * S + s) * 512 * ldt + i0;
+    for (int idx = threadIdx.x; idx < 512 * (RW_ROWS / 2); idx += RW_WARPS * 32) {
+        const int c = idx >> 3, m = idx & 7;
+        const float4 f = *reinterpret_cast<const float4*>(Ts + (int64_t)c * ldt + 2 * m);
+        sm[c * RW_TS + 2 * m] = mk<float>(f.x, f.y);
+        sm[c * RW_TS + 2 * m + 1] = mk<float>(f.z, f.w);
+    }
+    __syncthreads();
+    c32 u[32];
+    {
+        const int il = 2 * warp + (lane >> 4), k1 = lane & 15;
+#pragma unroll
+        for (int k2 = 0; k2 < 32; ++k2) u[k2] = sm[(k1 + 16 * k2) * RW_TS + il];
+    }
+    __syncthreads();                               // the tile is read: its space becomes the warps' exchanges
+    c32 v[2][16];
+    fft512_inv2<float, true>(u, v, sm + warp * WX_SLOTS, tw);
+    const int op = col_op ? col_op[col] : 0;
+    const float w = omega ? float(omega[op]) : 0.0f;
+    const c32 z = zs ? cvt<float>(zs[(int64_t)op * S + s]) : zero<float>();
+    const int64_t base = (int64_t)col * ld;
+    const int layer = sheet_layer ? sheet_layer[s] : s;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int i = i0 + 2 * warp + q;
+        if (i >= n0) continue;
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const int j = lane + 32 * r;
+            if (j >= n1) continue;
+            const int64_t pos = off + ((int64_t)s * n0 + i) * n1 + j;
+            const c32 L = v[q][r];
+            c32 y;
+            if (mode == 2) {
+                y = mask[pos] ? L : zero<float>();
+            } else if (!mask[pos]) {
+                y = zero<float>();
+            } else {
+                const int64_t va = off_v + ((int64_t)layer * nx + i) * ny + j;
+                const int64_t vb = va + (int64_t)di * ny + dj;
+                y = z * x[base + pos] + w * jmul(L) - (x[base + va] - x[base + vb]);
+                if (mode == 1) y = rhs[base + pos] - y;
+            }
+            out[base + pos] = y;
+        }
+    }
+}
+
 // Row passes for P a power of 8: the first stage of pass A reads the strip row straight from x, the last
 // stage of pass C feeds the epilogue from registers; stages alternate two shared buffers.
 template <typename R, int P>
 __global__ void __launch_bounds__(1024) lp_pass_a8(const cx<R>* __restrict__ x, int64_t ldx, int64_t off, int S, int n0,
                                                    int n1, int rows, const cx<R>* __restrict__ tw, cx<R>* __restrict__ T,
-                                                   const int* __restrict__ col_list) {
+                                                   const int* __restrict__ col_list, int ldt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int TEAM = P / 8, NBF = P / 8, ST = lp_srow(P);
     cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw);
@@ -370,11 +481,11 @@ __global__ void __launch_bounds__(1024) lp_pass_a8(const cx<R>* __restrict__ x, 
     }
     __syncthreads();
     const cx<R>* res = buf + (cur ? 0 : rows) * ST;
-    cx<R>* Ts = T + ((int64_t)blockIdx.z * S + s) * (int64_t)P * n0;
+    cx<R>* Ts = T + ((int64_t)blockIdx.z * S + s) * (int64_t)P * ldt;
     const int lr = __ffs(rows) - 1;
     for (int idx = threadIdx.x; idx < rows * P; idx += blockDim.x) {
         const int c = idx >> lr, rr = idx & (rows - 1);
-        if (i0 + rr < n0) Ts[(int64_t)c * n0 + i0 + rr] = res[rr * ST + spad(c)];
+        if (i0 + rr < n0) Ts[(int64_t)c * ldt + i0 + rr] = res[rr * ST + spad(c)];
     }
 }
 
@@ -385,19 +496,20 @@ __global__ void __launch_bounds__(1024) lp_pass_c8(const cx<R>* __restrict__ T, 
                                                    int di, int dj, int rows, const cx<R>* __restrict__ tw,
                                                    const uint8_t* __restrict__ mask, const int* __restrict__ col_op,
                                                    const double* __restrict__ omega, const c64* __restrict__ zs, int mode,
-                                                   const int* __restrict__ col_list, const int* __restrict__ sheet_layer) {
+                                                   const int* __restrict__ col_list, const int* __restrict__ sheet_layer,
+                                                   int ldt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int TEAM = P / 8, NBF = P / 8, ST = lp_srow(P);
     cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw);
     const int i0 = blockIdx.x * rows;
     const int s = blockIdx.y;
     const int col = col_list ? col_list[blockIdx.z] : blockIdx.z;
-    const cx<R>* Ts = T + ((int64_t)blockIdx.z * S + s) * (int64_t)P * n0;
+    const cx<R>* Ts = T + ((int64_t)blockIdx.z * S + s) * (int64_t)P * ldt;
     const int lr = __ffs(rows) - 1;
     for (int idx = threadIdx.x; idx < rows * P; idx += blockDim.x) {
         const int c = idx >> lr, rr = idx & (rows - 1);
         const int i = i0 + rr;
-        buf[rr * ST + spad(c)] = i < n0 ? Ts[(int64_t)c * n0 + i] : zero<R>();
+        buf[rr * ST + spad(c)] = i < n0 ? Ts[(int64_t)c * ldt + i] : zero<R>();
     }
     __syncthreads();
     const int tr = threadIdx.x / TEAM, t = threadIdx.x % TEAM;
@@ -468,7 +580,7 @@ __global__ void __launch_bounds__(1024) lp_pass_c(const cx<R>* __restrict__ T, c
                           int nx, int ny, int di, int dj, int P1, int rows, const cx<R>* __restrict__ tw,
                           const uint8_t* __restrict__ mask, const int* __restrict__ col_op,
                           const double* __restrict__ omega, const c64* __restrict__ zs, int mode,
-                          const int* __restrict__ col_list, const int* __restrict__ sheet_layer) {
+                          const int* __restrict__ col_list, const int* __restrict__ sheet_layer, int ldt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw);
     const int P = PL ? PL : P1;                  // compile-time when specialised
@@ -476,12 +588,12 @@ __global__ void __launch_bounds__(1024) lp_pass_c(const cx<R>* __restrict__ T, c
     const int i0 = blockIdx.x * rows;
     const int s = blockIdx.y;
     const int col = col_list ? col_list[blockIdx.z] : blockIdx.z;
-    const cx<R>* Ts = T + ((int64_t)blockIdx.z * S + s) * (int64_t)P * n0;
+    const cx<R>* Ts = T + ((int64_t)blockIdx.z * S + s) * (int64_t)P * ldt;
     const int lr = __ffs(rows) - 1;
     for (int idx = threadIdx.x; idx < rows * P; idx += blockDim.x) {
         const int c = idx >> lr, rr = idx & (rows - 1);
         const int i = i0 + rr;
-        buf[rr * stride + spad(c)] = i < n0 ? Ts[(int64_t)c * n0 + i] : zero<R>();
+        buf[rr * stride + spad(c)] = i < n0 ? Ts[(int64_t)c * ldt + i] : zero<R>();
     }
     __syncthreads();
     const int team = P / 8;
@@ -516,6 +628,7 @@ __global__ void __launch_bounds__(1024) lp_pass_c(const cx<R>* __restrict__ T, c
 }
 
 // ------------------------------------------------------------------------------------------ launchers
+template <typename R> static int ldt_of(const LpArgs<R>& a) { return a.ldt > 0 ? a.ldt : a.n0; }
 template <typename R> static bool b8_fits(const LpArgs<R>& a);
 template <typename R>
 static void set_smem(const void* fn, size_t bytes) {
@@ -541,13 +654,27 @@ void lp_shapes(const LpArgs<R>& a, int* rows_out, int* bt_out) {
 // the specialised lengths; others run the runtime-length kernels
 #define GT_LP_LENGTHS(X) X(64) X(96) X(128) X(192) X(256) X(384) X(512) X(768) X(1024) X(1536) X(2048)
 
+// the warp row passes apply for P1 = 512 in FP32 with T's rows a multiple of 16
+template <typename R> static bool rw_fits(const LpArgs<R>& a) {
+    return std::is_same<R, float>::value && a.P1 == 512 && a.n1 <= 256 && a.ldt > 0 && a.ldt % 16 == 0;
+}
+
 template <typename R, int PA>
 static void launch_a(const LpArgs<R>& a, int rows, cudaStream_t st) {
+    if constexpr (PA == 512 && std::is_same<R, float>::value) {
+        if (rw_fits(a)) {
+            set_smem<float>((const void*)lp_pass_aw, RW_SMEM);
+            lp_pass_aw<<<dim3(ceil_div(a.n0, RW_ROWS), a.S, a.ncol), RW_WARPS * 32, RW_SMEM, st>>>(
+                a.x, a.ld, a.off, a.S, a.n0, a.n1, a.ldt, a.tw1, a.T, a.col_list);
+            GT_LAUNCH_CHECK();
+            return;
+        }
+    }
     if constexpr (PA == 64 || PA == 512) {
         const size_t sm = (size_t)2 * rows * lp_srow(PA) * sizeof(cx<R>);
         set_smem<R>((const void*)lp_pass_a8<R, PA>, sm);
         lp_pass_a8<R, PA><<<dim3(ceil_div(a.n0, rows), a.S, a.ncol), rows * (PA / 8), sm, st>>>(
-            a.x, a.ld, a.off, a.S, a.n0, a.n1, rows, a.tw1, a.T, a.col_list);
+            a.x, a.ld, a.off, a.S, a.n0, a.n1, rows, a.tw1, a.T, a.col_list, ldt_of(a));
         GT_LAUNCH_CHECK();
         return;
     }
@@ -555,7 +682,7 @@ static void launch_a(const LpArgs<R>& a, int rows, cudaStream_t st) {
     dim3 gA(ceil_div(a.n0, rows), a.S, a.ncol);
     set_smem<R>((const void*)lp_pass_a<R, PA>, smA);
     lp_pass_a<R, PA><<<gA, rows * (a.P1 / 8), smA, st>>>(a.x, a.ld, a.off, a.S, a.n0, a.n1, a.P1, rows, a.tw1, a.T,
-                                                          a.col_list);
+                                                          a.col_list, ldt_of(a));
     GT_LAUNCH_CHECK();
 }
 
@@ -564,7 +691,7 @@ static void launch_b8(const LpArgs<R>& a, int bt, cudaStream_t st) {
     const size_t sm = (size_t)2 * bt * S * lp_srow(P) * sizeof(cx<R>);
     set_smem<R>((const void*)lp_pass_b8<R, P, S>, sm);
     lp_pass_b8<R, P, S><<<dim3(a.P1, ceil_div(a.ncol, bt)), bt * (P / 8), sm, st>>>(a.n0, a.P1, a.ncol, bt, a.spec, a.tw0,
-                                                                                  a.T);
+                                                                                  a.T, ldt_of(a));
     GT_LAUNCH_CHECK();
 }
 
@@ -577,7 +704,7 @@ static void launch_bw(const LpArgs<float>& a, cudaStream_t st) {
     const size_t sm = (size_t)BW_WARPS * WX_SLOTS * sizeof(c32);
     set_smem<float>((const void*)lp_pass_bw<S>, sm);
     lp_pass_bw<S><<<dim3(a.P1, ceil_div(a.ncol, BW_WARPS * CPW)), BW_WARPS * 32, sm, st>>>(a.n0, a.P1, a.ncol, a.spec,
-                                                                                         a.tw0, a.T);
+                                                                                         a.tw0, a.T, ldt_of(a));
     GT_LAUNCH_CHECK();
 }
 
@@ -603,18 +730,29 @@ static void launch_b(const LpArgs<R>& a, int bt, cudaStream_t st) {
     size_t smB = (size_t)bt * a.S * srow(a.P0) * sizeof(cx<R>);
     dim3 gB(a.P1, ceil_div(a.ncol, bt));
     set_smem<R>((const void*)lp_pass_b<R, PB>, smB);
-    lp_pass_b<R, PB><<<gB, bt * a.S * (a.P0 / 8), smB, st>>>(a.S, a.n0, a.P0, a.P1, a.ncol, bt, a.spec, a.tw0, a.T);
+    lp_pass_b<R, PB><<<gB, bt * a.S * (a.P0 / 8), smB, st>>>(a.S, a.n0, a.P0, a.P1, a.ncol, bt, a.spec, a.tw0, a.T,
+                                                              ldt_of(a));
     GT_LAUNCH_CHECK();
 }
 
 template <typename R, int PA>
 static void launch_c(const LpArgs<R>& a, int rows, cudaStream_t st) {
+    if constexpr (PA == 512 && std::is_same<R, float>::value) {
+        if (rw_fits(a)) {
+            set_smem<float>((const void*)lp_pass_cw, RW_SMEM);
+            lp_pass_cw<<<dim3(ceil_div(a.n0, RW_ROWS), a.S, a.ncol), RW_WARPS * 32, RW_SMEM, st>>>(
+                a.T, a.x, a.rhs, a.out, a.ld, a.off, a.off_v, a.S, a.n0, a.n1, a.nx, a.ny, a.di, a.dj, a.ldt, a.tw1,
+                a.mask, a.col_op, a.omega, a.zs, a.mode, a.col_list, a.sheet_layer);
+            GT_LAUNCH_CHECK();
+            return;
+        }
+    }
     if constexpr (PA == 64 || PA == 512) {
         const size_t sm = (size_t)2 * rows * lp_srow(PA) * sizeof(cx<R>);
         set_smem<R>((const void*)lp_pass_c8<R, PA>, sm);
         lp_pass_c8<R, PA><<<dim3(ceil_div(a.n0, rows), a.S, a.ncol), rows * (PA / 8), sm, st>>>(
             a.T, a.x, a.rhs, a.out, a.ld, a.off, a.off_v, a.S, a.n0, a.n1, a.nx, a.ny, a.di, a.dj, rows, a.tw1, a.mask,
-            a.col_op, a.omega, a.zs, a.mode, a.col_list, a.sheet_layer);
+            a.col_op, a.omega, a.zs, a.mode, a.col_list, a.sheet_layer, ldt_of(a));
         GT_LAUNCH_CHECK();
         return;
     }
@@ -623,7 +761,7 @@ static void launch_c(const LpArgs<R>& a, int rows, cudaStream_t st) {
     set_smem<R>((const void*)lp_pass_c<R, PA>, smA);
     lp_pass_c<R, PA><<<gA, rows * (a.P1 / 8), smA, st>>>(a.T, a.x, a.rhs, a.out, a.ld, a.off, a.off_v, a.S, a.n0, a.n1,
                                                           a.nx, a.ny, a.di, a.dj, a.P1, rows, a.tw1, a.mask, a.col_op,
-                                                          a.omega, a.zs, a.mode, a.col_list, a.sheet_layer);
+                                                          a.omega, a.zs, a.mode, a.col_list, a.sheet_layer, ldt_of(a));
     GT_LAUNCH_CHECK();
 }
 

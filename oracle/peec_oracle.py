@@ -47,6 +47,9 @@ GMRES_EXTRA_CYCLES = 24      # peec.py:98
 GMRES_PROGRESS = 0.7         # peec.py:99
 GMRES_CHECK_MISSES = 4       # peec.py:100
 LU_PIVOT_THRESHOLD = 0.1     # peec.py:105
+# FFT threads of the L_p product: all host cores (-1), as the reference's fft_workers() defaults (peec.py:136-149,
+# a per-thread setting there); a process that solves alongside others on the same host sets it to 1
+FFT_WORKERS = -1
 TAPE_PANELS, TAPE_ORDER = 30, 8   # kernel.py:215-216
 
 
@@ -810,12 +813,12 @@ class OracleStack:
                 continue
             X = np.zeros(shape, complex)
             X[tuple(idx.T)] = I_s[lo:hi]
-            F = fft2(X, s=P, axes=(1, 2), workers=-1)
+            F = fft2(X, s=P, axes=(1, 2), workers=FFT_WORKERS)
             G = np.zeros_like(F)
             for t in range(S):
                 for s in range(S):
                     G[t] += self._full(orient, t, s) * F[s]
-            Y = ifft2(G, axes=(1, 2), workers=-1, overwrite_x=True)
+            Y = ifft2(G, axes=(1, 2), workers=FFT_WORKERS, overwrite_x=True)
             out[lo:hi] = Y[tuple(idx.T)]
         if self.dL is not None:             # strips narrower than the pitch (peec.py:2129-2132)
             out += self.dL * I_s

@@ -37,7 +37,9 @@ microstrip over a 40 x 20 mm plane with and without slots or an edge cut, the pa
 long; ``synth.KNOWN_BOARDS``), solved to rtol 1e-10.
 
 ``--full`` additionally runs the 256 x 256 slotted plane pair (a few nets x frequencies, minutes per solve)
-and stores only its scalar outputs (Z_loop, its, current norms).
+and stores only its scalar outputs (Z_loop, its, current norms).  ``--currents-only`` stores the reference's
+full plane current maps (I_x, I_y) of three of its columns across the band (slotted_pair_currents.npz), which
+the benchmark compares the GPU build's solution with.
 """
 from __future__ import annotations
 
@@ -276,6 +278,31 @@ def record_known(peec) -> dict:
     return out
 
 
+# the full-size columns whose plane currents are stored: (net, frequency index) of the slotted pair's 8 nets x
+# 32 frequencies, spanning the band (1 MHz, 28.3 MHz, 1 GHz)
+CURRENT_COLUMNS = ((0, 0), (1, 15), (0, 31))
+
+
+def record_currents(peec, board: synth.Board) -> dict:
+    """The reference's own plane currents I_x, I_y (sheets x strips, rounded to complex64, far below the 1e-6
+    the GPU build is held to) and Z_loop for CURRENT_COLUMNS of the full-size slotted pair, solved to board.tol
+    with GMRES(board.restart)."""
+    st, routes = build_reference(peec, board)
+    peec.gmres_restart = lambda n, r=board.restart: r
+    peec.PlaneStack.solve.__defaults__ = (board.tol, 8, None)
+    out = {"cols": np.array(CURRENT_COLUMNS, np.int64), "freqs": np.asarray(board.freqs)}
+    for n, (k, q) in enumerate(CURRENT_COLUMNS):
+        t0 = time.perf_counter()
+        sol = routes[k].solve(float(board.freqs[q]))
+        out[f"Ix{n}"] = np.asarray(sol.I_x).astype(np.complex64)
+        out[f"Iy{n}"] = np.asarray(sol.I_y).astype(np.complex64)
+        out[f"Z{n}"] = np.complex128(sol.Z_loop)
+        out[f"its{n}"] = np.int64(sol.iterations)
+        print(f"  slotted_pair net {k} f {board.freqs[q]:.4g}: its {sol.iterations} Z {sol.Z_loop:.10g} "
+              f"({time.perf_counter() - t0:.1f} s)", flush=True)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", required=True)
@@ -286,8 +313,13 @@ def main():
     ap.add_argument("--known-only", action="store_true", help="only the known-answer boards' scalars")
     ap.add_argument("--routed-only", action="store_true", help="only the board rasterised from polygons")
     ap.add_argument("--fields-only", action="store_true", help="only the current-density maps")
+    ap.add_argument("--currents-only", action="store_true",
+                    help="only the full-size slotted pair's plane currents (slotted_pair_currents.npz)")
     args = ap.parse_args()
     peec, kernel = import_reference(args.reference)
+    if args.currents_only:
+        np.savez_compressed(HERE / "slotted_pair_currents.npz", **record_currents(peec, synth.slotted_pair()))
+        return
     if args.fields_only:
         np.savez_compressed(HERE / "necked_pair_fields.npz", **record_fields(peec, synth.necked_pair()))
         np.savez_compressed(HERE / "routed_pair_fields.npz", **record_fields(peec, synth.routed_pair()))

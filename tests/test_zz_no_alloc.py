@@ -45,8 +45,10 @@ def test_more_columns_than_the_fixed_scratch_holds_are_refused():
     z, board = load("small_pair")
     st, routes = gs.from_board(board)
     lib = st.handle.lib
-    # the FFT grid of one column: the larger orientation's sheets x padded row length x rows
-    per_col = 16 * max(st.n_sheets * st.P["x"][1] * (st.nx - 1), st.n_sheets * st.P["y"][1] * st.nx)
+    # the FFT grid of one column: the larger orientation's sheets x padded row length x rows (rows rounded up
+    # to a multiple of 16)
+    pad = lambda n: (n + 15) // 16 * 16  # noqa: E731
+    per_col = 16 * max(st.n_sheets * st.P["x"][1] * pad(st.nx - 1), st.n_sheets * st.P["y"][1] * pad(st.nx))
     too_many = (32 << 20) // per_col + 1
     # real buffers of that many columns: the call must refuse them before any kernel runs
     X = torch.zeros((too_many, st.handle.n_dense), dtype=torch.complex128, device="cuda")
