@@ -60,7 +60,9 @@ def parse():
                     help="precondition every other frequency with its neighbour's factorisation (half the LDL^T)")
     ap.add_argument("--levels", action="store_true",
                     help="also time each elimination level of the triangular solves (key 'solve_levels')")
-    ap.add_argument("--workload", default="slotted_pair", choices=["slotted_pair", "what_if"],
+    ap.add_argument("--boards", type=int, default=64, help="uneven: boards in the batch")
+    ap.add_argument("--concurrency", type=int, default=8, help="uneven: boards in flight at once")
+    ap.add_argument("--workload", default="slotted_pair", choices=["slotted_pair", "what_if", "uneven"],
                     help="what_if: latency of interactive edits (added vias / decoupling parts) on a solved "
                          "512 x 512 board, warm-started derived stacks (a line of its own, not the headline)")
     ap.add_argument("--requests", type=int, default=24, help="what_if: timed edits")
@@ -572,8 +574,66 @@ def run_what_if(args):
         print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------------------------------ uneven batch
+def run_uneven(args):
+    """The uneven-batch workload: --boards seeded boards (sides 64-512, 2-6 layers, cut-outs, stitching vias,
+    1-16 nets x 4-16 frequencies; synth.uneven_board), every (net, frequency) of every board solved to the
+    boards' tolerance.  Host setup (topology, symbolic analysis, spectra) is outside the timed region; a step
+    factorises every board's frequencies and solves all its columns, first one board after another, then with
+    --concurrency boards in flight on streams of their own (batch.solve_all); value is the latter's solves/s.
+    Each board's result in the mix is checked against its result alone."""
+    import torch
+    from groundtruth_gb300 import batch, native, synth
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    t0 = time.perf_counter()
+    boards = [synth.uneven_board(s) for s in range(args.boards)]
+    jobs = batch.prepare(boards)
+    setup_s = time.perf_counter() - t0
+    nsolve = sum(len(j.cols) for j in jobs)
+    for j in jobs:                       # warm-up: workspaces and tuned launch shapes per board
+        batch.solve_board(j)
+    lib = native.load()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    alone = batch.solve_all(jobs, concurrency=1)
+    t_alone = time.perf_counter() - t0
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", 0)))
+    clocks.start()
+    l0 = lib.gt_launch_count()
+    t0 = time.perf_counter()
+    mixed = batch.solve_all(jobs, concurrency=args.concurrency)
+    t_mixed = time.perf_counter() - t0
+    launches = int(lib.gt_launch_count() - l0)
+    ck = clocks.stop()
+    dev = max(float(np.linalg.norm(a.x - m.x) / max(np.linalg.norm(a.x), 1e-300)) for a, m in zip(alone, mixed))
+    groups = {}
+    for j in jobs:
+        groups[str(j.group)] = groups.get(str(j.group), 0) + 1
+    line = {"metric": "uneven batch solves/s", "value": nsolve / t_mixed, "unit": "solves/s", "n_gpus": 1,
+            "steps": 1, "warmup": 1, "ms_per_step": t_mixed * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64 inner / c128 refinement", "data": "synthetic (seeded)",
+            "config": {"workload": f"uneven: {args.boards} boards (sides 64-512, 2-6 layers, cut-outs, vias, 1-16 "
+                                   "nets x 4-16 log f), factorisation + solve of every column per step",
+                       "solves_per_step": nsolve, "tol": boards[0].tol, "concurrency": args.concurrency,
+                       "fft_groups": groups},
+            "one_board_at_a_time": {"value": nsolve / t_alone, "unit": "solves/s", "seconds": round(t_alone, 2)},
+            "max_rel_diff_mix_vs_alone": dev,
+            "max_rel_residual": float(max(m.residual.max() for m in mixed)),
+            "iterations": {"mean": float(np.mean(np.concatenate([m.its for m in mixed]))),
+                           "max": int(max(m.its.max() for m in mixed))},
+            "factorise_s_sum": round(sum(m.factorise_s for m in mixed), 2),
+            "setup_s": round(setup_s, 1), "gpu_launches": launches, "clocks": ck}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "uneven":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the headline workload only"}))
+            return
+        run_uneven(args)
+        return
     if args.workload == "what_if":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the headline workload only"}))

@@ -371,8 +371,21 @@ __global__ void __launch_bounds__(RW_WARPS * 32, GT_RW_MINB) lp_pass_aw(const c3
     }
 }
 
+// Pass C for P1 = 512 in FP32 (n1 <= 256): each warp takes two rows i, i+1 of one sheet of one column and
+// reads them straight from T, with no block-wide staging: lane L loads the two rows' values at frequency
+// columns c = L + 32 m (m < 16) as one 16-byte load each (rows i, i+1 are adjacent in T, i even), which gives it
+// the k2 = L/16 + 2 m terms of k1 = L mod 16 (c = k1 + 16 k2) for both rows; one exchange with lane L ^ 16
+// leaves lane 16 q + k1 holding row q at every k2, the inverse FFT's layout (fftw.cuh).  Warps are
+// independent, so one warp's loads overlap another's transforms.
+constexpr int CW_WARPS = 4;
+#ifndef GT_CW_MINB
+#define GT_CW_MINB 5        // blocks per SM the register budget is cut for (102 registers)
+#endif
+constexpr size_t CW_SMEM = (size_t)CW_WARPS * WX_SLOTS * sizeof(c32);
+
 // mode 0: out = R_t x + j w L - (V[a] - V[b]); 1: out = rhs - (that); 2: out = L
-__global__ void __launch_bounds__(RW_WARPS * 32, GT_RW_MINB) lp_pass_cw(const c32* __restrict__ T, const c32* __restrict__ x,
+__global__ void __launch_bounds__(CW_WARPS * 32, GT_CW_MINB) lp_pass_cw(const c32* __restrict__ T,
+                                                               const c32* __restrict__ x,
                                                                const c32* __restrict__ rhs, c32* __restrict__ out,
                                                                int64_t ld, int64_t off, int64_t off_v, int S, int n0,
                                                                int n1, int nx, int ny, int di, int dj, int ldt,
@@ -384,23 +397,24 @@ __global__ void __launch_bounds__(RW_WARPS * 32, GT_RW_MINB) lp_pass_cw(const c3
     extern __shared__ __align__(16) unsigned char smem_raw[];
     c32* sm = reinterpret_cast<c32*>(smem_raw);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int i0 = blockIdx.x * RW_ROWS, s = blockIdx.y;
+    const int i = (blockIdx.x * CW_WARPS + warp) * 2, s = blockIdx.y;
+    if (i >= n0) return;                           // the whole warp leaves together
     const int col = col_list ? col_list[blockIdx.z] : blockIdx.z;
-    const c32* Ts = T + ((int64_t)blockIdx.z * S + s) * 512 * ldt + i0;
-    for (int idx = threadIdx.x; idx < 512 * (RW_ROWS / 2); idx += RW_WARPS * 32) {
-        const int c = idx >> 3, m = idx & 7;
-        const float4 f = *reinterpret_cast<const float4*>(Ts + (int64_t)c * ldt + 2 * m);
-        sm[c * RW_TS + 2 * m] = mk<float>(f.x, f.y);
-        sm[c * RW_TS + 2 * m + 1] = mk<float>(f.z, f.w);
-    }
-    __syncthreads();
+    const c32* Ts = T + ((int64_t)blockIdx.z * S + s) * 512 * ldt + i;
+    const int q = lane >> 4;
     c32 u[32];
-    {
-        const int il = 2 * warp + (lane >> 4), k1 = lane & 15;
 #pragma unroll
-        for (int k2 = 0; k2 < 32; ++k2) u[k2] = sm[(k1 + 16 * k2) * RW_TS + il];
+    for (int m = 0; m < 16; ++m) {
+        const float4 f = *reinterpret_cast<const float4*>(Ts + (int64_t)(lane + 32 * m) * ldt);
+        // mine: row q at k2 = q + 2m; the partner's: row q at k2 = 1 - q + 2m, for which it sends its row-q value
+        const c32 r0 = mk<float>(f.x, f.y), r1 = mk<float>(f.z, f.w);
+        const c32 mine = q ? r1 : r0, send = q ? r0 : r1;
+        c32 got;
+        got.re = __shfl_xor_sync(0xffffffffu, send.re, 16);
+        got.im = __shfl_xor_sync(0xffffffffu, send.im, 16);
+        u[2 * m] = q ? got : mine;
+        u[2 * m + 1] = q ? mine : got;
     }
-    __syncthreads();                               // the tile is read: its space becomes the warps' exchanges
     c32 v[2][16];
     fft512_inv2<float, true>(u, v, sm + warp * WX_SLOTS, tw);
     const int op = col_op ? col_op[col] : 0;
@@ -409,22 +423,22 @@ __global__ void __launch_bounds__(RW_WARPS * 32, GT_RW_MINB) lp_pass_cw(const c3
     const int64_t base = (int64_t)col * ld;
     const int layer = sheet_layer ? sheet_layer[s] : s;
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
-        const int i = i0 + 2 * warp + q;
-        if (i >= n0) continue;
+    for (int qq = 0; qq < 2; ++qq) {
+        const int ii = i + qq;
+        if (ii >= n0) continue;
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
             const int j = lane + 32 * r;
             if (j >= n1) continue;
-            const int64_t pos = off + ((int64_t)s * n0 + i) * n1 + j;
-            const c32 L = v[q][r];
+            const int64_t pos = off + ((int64_t)s * n0 + ii) * n1 + j;
+            const c32 L = v[qq][r];
             c32 y;
             if (mode == 2) {
                 y = mask[pos] ? L : zero<float>();
             } else if (!mask[pos]) {
                 y = zero<float>();
             } else {
-                const int64_t va = off_v + ((int64_t)layer * nx + i) * ny + j;
+                const int64_t va = off_v + ((int64_t)layer * nx + ii) * ny + j;
                 const int64_t vb = va + (int64_t)di * ny + dj;
                 y = z * x[base + pos] + w * jmul(L) - (x[base + va] - x[base + vb]);
                 if (mode == 1) y = rhs[base + pos] - y;
@@ -739,8 +753,8 @@ template <typename R, int PA>
 static void launch_c(const LpArgs<R>& a, int rows, cudaStream_t st) {
     if constexpr (PA == 512 && std::is_same<R, float>::value) {
         if (rw_fits(a)) {
-            set_smem<float>((const void*)lp_pass_cw, RW_SMEM);
-            lp_pass_cw<<<dim3(ceil_div(a.n0, RW_ROWS), a.S, a.ncol), RW_WARPS * 32, RW_SMEM, st>>>(
+            set_smem<float>((const void*)lp_pass_cw, CW_SMEM);
+            lp_pass_cw<<<dim3(ceil_div(a.n0, 2 * CW_WARPS), a.S, a.ncol), CW_WARPS * 32, CW_SMEM, st>>>(
                 a.T, a.x, a.rhs, a.out, a.ld, a.off, a.off_v, a.S, a.n0, a.n1, a.nx, a.ny, a.di, a.dj, a.ldt, a.tw1,
                 a.mask, a.col_op, a.omega, a.zs, a.mode, a.col_list, a.sheet_layer);
             GT_LAUNCH_CHECK();

@@ -6,6 +6,7 @@ PlaneStack, ``Operators`` factorises frequencies, ``solve`` / ``apply`` run batc
 from __future__ import annotations
 
 import ctypes as C
+import sys
 import os
 from pathlib import Path
 
@@ -354,12 +355,21 @@ def _ops_and_index(ops: list):
     return obj, np.array([k for _, k in ops], np.int32)
 
 
+def current_stream() -> int:
+    """The calling thread's current PyTorch CUDA stream when torch has initialised CUDA (so that solves issued
+    under torch.cuda.stream(s) run on s, beside other streams' work), else 0 (the default stream)."""
+    torch = sys.modules.get("torch")
+    if torch is not None and torch.cuda.is_available() and torch.cuda.is_initialized():
+        return int(torch.cuda.current_stream().cuda_stream)
+    return 0
+
+
 def solve(geom: Geometry, ops: list, rhs: np.ndarray, tol: float, restart: int = 50, max_its: int = 2000,
           inner_tol: float = 1e-5, precision: str = "mixed", max_outer: int = 40, reorth: float = 0.7,
-          outer_k: int = 8, x0: np.ndarray | None = None, out: np.ndarray | None = None):
+          outer_k: int = 8, x0: np.ndarray | None = None, out: np.ndarray | None = None, stream: int | None = None):
     """rhs: (ncol, n_compact) complex in the reference's order; x0: optional starting points (same shape);
-    out: optional C-contiguous complex128 array of that shape to receive x (e.g. page-locked host memory).
-    Returns (x, its, resid, converged)."""
+    out: optional C-contiguous complex128 array of that shape to receive x (e.g. page-locked host memory);
+    stream: a cudaStream_t (default: current_stream()).  Returns (x, its, resid, converged)."""
     lib = geom.lib
     obj, idx = _ops_and_index(ops)
     rhs = np.ascontiguousarray(rhs, np.complex128)
@@ -377,8 +387,9 @@ def solve(geom: Geometry, ops: list, rhs: np.ndarray, tol: float, restart: int =
     res = np.zeros(ncol)
     o = SolveOpts(tol, restart, max_its, inner_tol, _precision(precision), max_outer, reorth, outer_k,
                   0 if x0 is None else 1)
+    st = current_stream() if stream is None else stream
     rc = lib.gt_solve(geom.h, obj.h, ncol, _ptr(idx, C.c_int32), _ptr(rhs.view(np.float64), C.c_double), C.byref(o),
-                      _ptr(x.view(np.float64), C.c_double), _ptr(its, C.c_int32), _ptr(res, C.c_double), None)
+                      _ptr(x.view(np.float64), C.c_double), _ptr(its, C.c_int32), _ptr(res, C.c_double), P(st))
     if rc not in (GT_OK, GT_NOT_CONVERGED):
         check(lib, rc, "gt_solve")
     return x, its, res, res <= tol

@@ -432,9 +432,22 @@ def random_board(seed: int, side=(24, 48), n_layers=(2, 6), n_nets=(1, 2), n_fre
         cells = _manhattan_walk(rng, s, mid, e, int(rng.integers(4, 12)), 2, nx - 3, ny - 3)
         pts = [(c[0] * d, c[1] * d) for c in cells]
         nets.append(Net(_segments(pts, z_sig, z_face, 0.15e-3), (0, *s), (0, *e)))
-    freqs = np.sort(np.exp(rng.uniform(math.log(1e6), math.log(1e9), n_freq)))
+    if isinstance(n_freq, tuple):           # a count drawn from the range, log-spaced over the band
+        freqs = np.geomspace(1e6, 1e9, int(rng.integers(n_freq[0], n_freq[1] + 1)))
+    else:
+        freqs = np.sort(np.exp(rng.uniform(math.log(1e6), math.log(1e9), n_freq)))
     return Board(f"random_{seed}", d, nx, ny, layers, [], branches, nets, freqs, precond="diag", tol=1e-10,
                  restart=50)
+
+
+def uneven_board(seed: int, tol: float = 1e-8) -> Board:
+    """One board of the uneven-batch workload at its full sizes: raster sides U[64, 512] per axis, pitch
+    U[0.2, 0.5] mm, 2-6 plane layers with gaps U[0.1, 1.5] mm, 0-8 polygon cut-outs of 3-8 vertices per layer,
+    stitching vias at a Poisson density of 0-4 per cm2, 1-16 random-walk nets and 4-16 log-spaced frequencies
+    from 1 MHz to 1 GHz; solved to `tol`."""
+    b = random_board(10_000 + seed, side=(64, 512), n_layers=(2, 6), n_nets=(1, 16), n_freq=(4, 16))
+    b.name, b.tol = f"uneven_{seed}", tol
+    return b
 
 
 def six_sheet(seed: int = 21) -> Board:

@@ -67,6 +67,15 @@ def _real_times(A: np.ndarray, X: np.ndarray) -> np.ndarray:
 
 
 @dataclass
+class BorderPlan:
+    """A bordered edit's border columns (frequencies, KCL injection vectors) and the step that composes its
+    answers from their solve_batch results."""
+    freqs: list
+    Js: list
+    compose: Callable
+
+
+@dataclass
 class EditResult:
     solutions: dict                     # (net, frequency) -> EditColumn
     seconds: float                      # wall time of the edit, derived stack to the last answer on the host
@@ -165,6 +174,22 @@ class WhatIf:
 
     def _bordered(self, extra: list, nets, freqs) -> EditResult:
         t0 = time.perf_counter()
+        plan = self.border_plan(extra, nets, freqs)
+        t1 = time.perf_counter()
+        raw = self._raw(self.stack, plan.freqs, [np.zeros(self.stack.nb, complex)] * len(plan.Js), plan.Js,
+                        self.tol * self.border_tol)
+        t2 = time.perf_counter()
+        res = plan.compose(raw)
+        res.seconds = time.perf_counter() - t0
+        res.parts.update({"derive_stack_s": t1 - t0, "border_solve_s": t2 - t1})
+        return res
+
+    def border_plan(self, extra: list, nets, freqs) -> "BorderPlan":
+        """The device work of a bordered edit, apart from running it: its border columns (the base system's
+        response to each new branch's unit injection at each frequency: frequencies and KCL vectors, solved to
+        tol x border_tol), and the host step that composes the edit's answers from their solutions (a list of
+        solve_batch results in the same order).  A server merges many edits' border columns into one device
+        solve (serve.Server)."""
         st = self.stack
         dst = st.with_branches(extra, device=False)
         droutes = {k: self.routes[k].on(dst) for k in nets}
@@ -176,7 +201,6 @@ class WhatIf:
         ka, kb = kept[na], kept[nbn]
         arm = np.array([0.5 * np.cross(st.pos(b.a), st.pos(b.b)) for b in extra])        # (k, 3)
         freqs = [float(f) for f in freqs]
-        t1 = time.perf_counter()
         # X_F: the base system's response to each new branch's unit injection (+1 at a, -1 at b), per frequency
         fcols = [(f, j) for f in freqs for j in range(k)]
         Js = []
@@ -185,11 +209,18 @@ class WhatIf:
             J[na[j]] += 1.0
             J[nbn[j]] -= 1.0
             Js.append(J)
-        raw = self._raw(st, [f for f, _ in fcols], [np.zeros(nb, complex)] * len(fcols), Js,
-                        self.tol * self.border_tol)
+        return BorderPlan([f for f, _ in fcols], Js,
+                          lambda raw: self._compose(extra, nets, freqs, dst, droutes, na, nbn, ka, kb, kept, arm,
+                                                    fcols, raw))
+
+    def _compose(self, extra, nets, freqs, dst, droutes, na, nbn, ka, kb, kept, arm, fcols, raw) -> EditResult:
+        """A bordered edit's answers from its border solutions (raw: solve_batch results of its border
+        columns)."""
+        t2 = time.perf_counter()
+        st = self.stack
+        nb, k, n_nodes = st.nb, len(extra), st.n_nodes
         XF = {c: r[3] for c, r in zip(fcols, raw)}
         rF = {c: r[4] * np.sqrt(2.0) for c, r in zip(fcols, raw)}      # ||F_j|| = sqrt 2
-        t2 = time.perf_counter()
 
         def at(v, idx):                        # rows of v at kept indices idx, zero where a node is not kept
             return np.where((idx >= 0).reshape((-1,) + (1,) * (v.ndim - 1)), v[np.maximum(idx, 0)], 0.0)
@@ -240,9 +271,9 @@ class WhatIf:
             cols_out.update((c, _column(sol)) for c, sol in zip(redo_cols, out))
         t4 = time.perf_counter()
         cols = [(net, f) for net in nets for f in freqs]
-        return EditResult({c: cols_out[c] for c in cols}, t4 - t0, [r[2] for r in raw],
-                          {"derive_stack_s": t1 - t0, "border_solve_s": t2 - t1, "compose_s": t3 - t2,
-                           "redo_s": t4 - t3, "border_columns": len(fcols), "cold_redo": len(redo_cols)})
+        return EditResult({c: cols_out[c] for c in cols}, t4 - t2, [r[2] for r in raw],
+                          {"compose_s": t3 - t2, "redo_s": t4 - t3, "border_columns": len(fcols),
+                           "cold_redo": len(redo_cols)})
 
     def _derived(self, branches: list, nets, freqs) -> EditResult:
         t0 = time.perf_counter()

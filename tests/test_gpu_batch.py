@@ -1,0 +1,34 @@
+"""Uneven boards solved side by side (groundtruth_gb300.batch): each board's solutions, iteration counts and loop
+impedances are the same when it is solved alone and when it shares the device with others on their own streams,
+and every column meets its tolerance.  Needs a GPU."""
+import numpy as np
+import pytest
+
+from groundtruth_gb300 import batch, synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def jobs():
+    boards = [synth.random_board(s, side=(24, 64), n_layers=(2, 5), n_nets=(1, 3), n_freq=(2, 4)) for s in
+              (41, 42, 43, 44, 45)]
+    return batch.prepare(boards)
+
+
+def test_a_board_solves_the_same_alone_and_in_the_mix(jobs):
+    alone = [batch.solve_all([j], concurrency=1)[0] for j in jobs]
+    mixed = batch.solve_all(jobs, concurrency=4)
+    for a, m, j in zip(alone, mixed, jobs):
+        assert a.name == m.name == j.name
+        assert np.array_equal(a.its, m.its), j.name
+        assert np.linalg.norm(a.x - m.x) <= 1e-12 * np.linalg.norm(a.x), j.name
+        assert np.allclose(a.Z, m.Z, rtol=1e-12, atol=0), j.name
+        assert np.all(m.residual <= j.tol), (j.name, m.residual.max())
+
+
+def test_a_budget_smaller_than_one_board_runs_the_boards_one_at_a_time(jobs):
+    small = batch.solve_all(jobs[:3], concurrency=3, budget_bytes=1)
+    ref = [batch.solve_all([j], concurrency=1)[0] for j in jobs[:3]]
+    for a, b in zip(small, ref):
+        assert np.linalg.norm(a.x - b.x) <= 1e-12 * np.linalg.norm(b.x)
