@@ -62,7 +62,8 @@ def parse():
                     help="also time each elimination level of the triangular solves (key 'solve_levels')")
     ap.add_argument("--boards", type=int, default=64, help="uneven: boards in the batch")
     ap.add_argument("--concurrency", type=int, default=8, help="uneven: boards in flight at once")
-    ap.add_argument("--workload", default="slotted_pair", choices=["slotted_pair", "what_if", "uneven"],
+    ap.add_argument("--budget-gb", type=float, default=120.0, help="serve: device-memory budget (GB)")
+    ap.add_argument("--workload", default="slotted_pair", choices=["slotted_pair", "what_if", "uneven", "serve"],
                     help="what_if: latency of interactive edits (added vias / decoupling parts) on a solved "
                          "512 x 512 board, warm-started derived stacks (a line of its own, not the headline)")
     ap.add_argument("--requests", type=int, default=24, help="what_if: timed edits")
@@ -541,12 +542,6 @@ def run_what_if(args):
     launches = int(lib.gt_launch_count() - l0)
     ck = clocks.stop()
     sv = np.array(service)
-    # FIFO single server, Poisson arrivals
-    arr = np.cumsum(np.random.default_rng(7).exponential(1.0 / args.rate, len(sv)))
-    fin, lat = 0.0, []
-    for a, s in zip(arr, sv):
-        fin = max(a, fin) + s
-        lat.append(fin - a)
     ms = lambda x: round(float(x) * 1e3, 2)
     line = {
         "metric": "what-if edit latency (p50)", "value": ms(np.median(sv)), "unit": "ms", "n_gpus": 1,
@@ -559,8 +554,7 @@ def run_what_if(args):
         "mean_ms": ms(sv.mean()), "max_ms": ms(sv.max()), "columns_per_request": float(np.mean(cols)),
         "solves_per_s": round(float(sum(cols) / sv.sum()), 2),
         "sustainable_edits_per_s": round(float(1.0 / sv.mean()), 3),
-        "queue": {"rate_per_s": args.rate, "stable": bool(args.rate * sv.mean() < 1.0),
-                  "p50_ms": ms(np.median(lat)), "p99_ms": ms(np.quantile(lat, 0.99))},
+        "note": "edits one after another (service time); arrivals and batching: --workload serve",
         "iterations_mean": round(float(np.mean(its)), 1), "max_residual": worst,
         "method": args.what_if_method,
         "cold_redo_columns": int(sum(p["cold_redo"] for p in parts)),
@@ -626,8 +620,121 @@ def run_uneven(args):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------------------------------ serving
+def _serve_requests(board, n_base_branches: int, n: int, seed: int):
+    """n what-if requests of the serving workload: a third add 1-4 stitching vias, a third move one decoupling
+    part (removed, added elsewhere), a third toggle the slot; each answered on 1-8 nets at 1-16 frequencies."""
+    from groundtruth_gb300 import serve, stack as gs, synth
+    rng = np.random.default_rng(seed)
+    freqs = [float(f) for f in board.freqs]
+    out = []
+    for r in range(n):
+        nets = sorted(int(k) for k in rng.choice(len(board.nets), size=int(rng.integers(1, 9)), replace=False))
+        fq = sorted(int(q) for q in rng.choice(len(freqs), size=int(rng.integers(1, 17)), replace=False))
+        kind = r % 3
+        if kind == 2:
+            out.append(serve.Request(nets=nets, freqs=[freqs[q] for q in fq], geometry="toggled"))
+            continue
+        extra = synth.what_if_branches(board, seed=5000 + r, n_via=int(rng.integers(1, 5)) if kind == 0 else 0,
+                                       n_part=0 if kind == 0 else 1)
+        out.append(serve.Request(nets=nets, freqs=[freqs[q] for q in fq],
+                                 branches=[gs.Branch(b.a, b.b, b.z, f"edit{r}_{m}", b.kind, b.radius)
+                                           for m, b in enumerate(extra)],
+                                 remove=[int(rng.integers(0, n_base_branches))] if kind == 1 else []))
+    return out
+
+
+def run_serve(args):
+    """The serving workload: the 512 x 512 what-if board (GND slot, PWR split, 12 nets x 16 frequencies) and its
+    slot-toggled twin resident on the device (spectra, factorisations, base solutions; their setup is reported,
+    not timed), and a Poisson stream of --requests what-if requests at --rate per second, each submitted at its
+    arrival time to the continuous-batching server (serve.Server) under a --budget-gb device budget.  Latency is
+    arrival to answer; throughput is the answered (net, frequency) columns over the stream's span.  The same
+    requests served one after another (each waiting for the previous answer) are the serial comparator."""
+    import threading
+    import torch
+    from groundtruth_gb300 import native, serve, stack as gs, synth, whatif
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    t0 = time.perf_counter()
+    geos, board = {}, None
+    for name, slot in (("base", True), ("toggled", False)):
+        b = synth.what_if_base(slot=slot)
+        board = board or b
+        st, routes = gs.from_board(b)
+        wi = whatif.WhatIf(st, routes, b.freqs, tol=b.tol, max_cols=args.max_cols, border_tol=args.border_tol,
+                           restart=args.restart, inner_tol=args.inner_tol, reorth=args.reorth, max_its=args.max_its)
+        wi.baseline()
+        geos[name] = wi
+    setup_s = time.perf_counter() - t0
+    srv = serve.Server(geos, budget_bytes=args.budget_gb * 1e9, restart=args.restart)
+    warm = _serve_requests(board, geos["base"].stack.nbr, max(args.warmup, 1), seed=11)
+    for r in warm:
+        srv.submit(r).result()
+    reqs = _serve_requests(board, geos["base"].stack.nbr, args.requests, seed=12)
+    gaps = np.random.default_rng(13).exponential(1.0 / args.rate, len(reqs))
+    lib = native.load()
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", 0)))
+    clocks.start()
+    l0 = lib.gt_launch_count()
+    futs = [None] * len(reqs)
+    t_start = time.perf_counter()
+
+    def feed():
+        t = t_start
+        for i, (r, g) in enumerate(zip(reqs, gaps)):
+            t += g
+            time.sleep(max(0.0, t - time.perf_counter()))
+            r.arrival = time.perf_counter()
+            futs[i] = srv.submit(r)
+    feeder = threading.Thread(target=feed)
+    feeder.start()
+    feeder.join()
+    answers = [f.result() for f in futs]
+    t_end = time.perf_counter()
+    launches = int(lib.gt_launch_count() - l0)
+    ck = clocks.stop()
+    batches = srv.batches[len(warm):]
+    lat = np.array([a.latency_s for a in answers])
+    ncols = sum(len(a.result.solutions) for a in answers)
+    worst = max(c.residual for a in answers for c in a.result.solutions.values())
+    # serial: the same requests one after another
+    t0 = time.perf_counter()
+    serial = []
+    for r in reqs:
+        r.arrival = 0.0
+        a = srv.submit(r).result()
+        serial.append(a.latency_s)
+    t_serial = time.perf_counter() - t0
+    srv.close()
+    ms = lambda x: round(float(x) * 1e3, 1)
+    line = {"metric": "what-if serving latency p50 / p99 and solves/s", "value": ms(np.median(lat)), "unit": "ms",
+            "n_gpus": 1, "higher_is_better": False, "impl": "gb300", "dtype": "c64 inner / c128 refinement",
+            "data": "synthetic (seeded)",
+            "config": {"workload": f"what_if_base {board.nx}x{board.ny} @{board.d * 1e3:g} mm, GND slot + split PWR, "
+                                   f"{len(board.nets)} nets x {len(board.freqs)} f; requests: 1-4 vias | move a decap | "
+                                   "toggle the slot, on 1-8 nets x 1-16 f", "rate_per_s": args.rate,
+                       "requests": len(reqs), "tol": board.tol, "budget_gb": args.budget_gb,
+                       "max_batch_columns": srv.max_cols},
+            "p50_ms": ms(np.median(lat)), "p99_ms": ms(np.quantile(lat, 0.99)), "max_ms": ms(lat.max()),
+            "solves_per_s": round(ncols / (t_end - t_start), 2), "answered_columns": ncols,
+            "span_s": round(t_end - t_start, 2),
+            "batches": {"count": len(batches), "requests_mean": round(float(np.mean([b["requests"] for b in batches])), 2),
+                        "columns_mean": round(float(np.mean([b["columns"] for b in batches])), 1),
+                        "seconds_mean": round(float(np.mean([b["seconds"] for b in batches])), 3)},
+            "serial": {"p50_ms": ms(np.median(serial)), "solves_per_s": round(ncols / t_serial, 2),
+                       "seconds": round(t_serial, 2)},
+            "max_residual_bound": worst, "setup_s": round(setup_s, 1), "gpu_launches": launches, "clocks": ck}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "serve":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the headline workload only"}))
+            return
+        run_serve(args)
+        return
     if args.workload == "uneven":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the headline workload only"}))
