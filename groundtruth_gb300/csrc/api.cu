@@ -878,7 +878,7 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
                 launch_reduce(W.partial, nchu, 0, ns, S.active, S.hn2, 1, 0, st);
                 launch_dgks(S, j, st);
             }
-            {
+            if (o.reorth > 0) {         // DGKS second pass (the slots launch_dgks flagged)
                 Scope sc(P, "gs_reorth", st);
                 launch_dots<R, B>(V, n, lds, j + 1, w, n, n, ns, S.reorth, W.partial, nch, st, vs);
                 launch_reduce(W.partial, nch, j + 1, ns, S.reorth, S.h2vec, S.ldh, 0, st);
