@@ -661,7 +661,9 @@ def run_serve(args):
         b = synth.what_if_base(slot=slot)
         board = board or b
         st, routes = gs.from_board(b)
-        wi = whatif.WhatIf(st, routes, b.freqs, tol=b.tol, max_cols=args.max_cols, border_tol=args.border_tol,
+        st.fp32_panels = name != "base"           # the toggled board takes plain solves only
+        # the server's budget sizes its batches (solve_batch still splits what would not fit the device)
+        wi = whatif.WhatIf(st, routes, b.freqs, tol=b.tol, max_cols=1 << 20, border_tol=args.border_tol,
                            restart=args.restart, inner_tol=args.inner_tol, reorth=args.reorth, max_its=args.max_its)
         wi.baseline()
         geos[name] = wi
@@ -714,7 +716,10 @@ def run_serve(args):
                                    f"{len(board.nets)} nets x {len(board.freqs)} f; requests: 1-4 vias | move a decap | "
                                    "toggle the slot, on 1-8 nets x 1-16 f", "rate_per_s": args.rate,
                        "requests": len(reqs), "tol": board.tol, "budget_gb": args.budget_gb,
-                       "max_batch_columns": srv.max_cols},
+                       "max_batch_columns": srv.max_cols,
+                       "resident_gb": round(srv.resident_bytes / 1e9, 1),
+                       "budget": "the requests' working memory; the resident geometries (spectra, factorisations, "
+                                 "base solutions) beside it"},
             "p50_ms": ms(np.median(lat)), "p99_ms": ms(np.quantile(lat, 0.99)), "max_ms": ms(lat.max()),
             "solves_per_s": round(ncols / (t_end - t_start), 2), "answered_columns": ncols,
             "span_s": round(t_end - t_start, 2),

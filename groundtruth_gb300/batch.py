@@ -6,9 +6,10 @@ Boards are grouped by their padded FFT sizes and sheet counts (the L_p kernels' 
 largest first.  Up to `concurrency` boards are in flight at once, each on a host thread of its own with a CUDA
 stream of its own: a board factorises its frequencies, scatters its right-hand sides into device memory and
 runs one batched device solve of all its columns (gt_solve_device), so the kernels of small boards, which alone
-fill only a few SMs, overlap on the device.  A board is admitted when its solve's device memory (gt_memory: the
-workspace, the dense vectors and its factorisations) fits the budget left by the boards in flight; a board
-larger than the whole budget runs alone and splits its columns.  A board's result does not depend on what else
+fill only a few SMs, overlap on the device.  A board is admitted when its device memory (its factorisations,
+kept as FP32 panels only, and the workspace and dense vectors of all its columns) fits the budget left by the
+boards in flight; a board larger than the whole budget runs alone within it, factorising its frequencies in
+chunks and solving their columns in batches that fit.  A board's result does not depend on what else
 is in flight: its kernels see only its own buffers and run in the same order on its stream.
 """
 from __future__ import annotations
@@ -85,44 +86,68 @@ class MemoryBudget:
             self.cv.notify_all()
 
 
-def _device_bytes(job: BoardJob, ncol: int, restart: int, precision: str) -> int:
-    m = native.memory(job.stack.handle, ncol, restart, precision)
-    return int(m["need"] + 2 * ncol * job.stack.handle.n_dense * 16 + job.stack.factorisation_bytes(len(job.freqs)))
+def _column_bytes(job: BoardJob, restart: int, precision: str) -> int:
+    """Device bytes one more column adds to a solve: its workspace share and its dense right-hand side and
+    solution."""
+    h = job.stack.handle
+    one = native.memory(h, 1, restart, precision)["need"]
+    return int(native.memory(h, 2, restart, precision)["need"] - one + 2 * h.n_dense * 16)
 
 
-def solve_board(job: BoardJob, stream=None, restart: int = 50, precision: str = "mixed",
-                max_its: int = 4000) -> BoardResult:
-    """Factorise a board's frequencies and solve all its columns in one batched device run on `stream` (a
-    torch.cuda.Stream; the current one when None)."""
+def _device_bytes(job: BoardJob, restart: int, precision: str) -> int:
+    """What a board asks of the budget: its factorisations and all its columns at once."""
+    return int(job.stack.factorisation_bytes(len(job.freqs)) + len(job.cols) * _column_bytes(job, restart, precision))
+
+
+def solve_board(job: BoardJob, stream=None, restart: int = 50, precision: str = "mixed", max_its: int = 4000,
+                avail_bytes: Optional[int] = None) -> BoardResult:
+    """Factorise a board's frequencies and solve all its columns on `stream` (a torch.cuda.Stream; the current
+    one when None) within avail_bytes of device memory (default: 90 % of the free memory): the factorisations
+    keep their FP32 panels only and are made in chunks of frequencies that take at most half the memory, each
+    chunk's columns solved in batches that fit the rest, the chunk's factorisations released after it."""
     import torch
     st = job.stack
+    st.fp32_panels = True
     stream = stream or torch.cuda.current_stream()
+    n = st.handle.n_dense
+    ncol = len(job.cols)
+    x = np.zeros((ncol, st.handle.n_compact), complex)
+    its = np.zeros(ncol, np.int32)
+    res = np.zeros(ncol)
+    t_fact = 0.0
     with torch.cuda.stream(stream):
         t0 = time.perf_counter()
-        ops = st.factorise(job.freqs, together=True)
-        t_fact = time.perf_counter() - t0
-        obj = ops[0][0]
-        col_op = np.array([ops[q][1] for (_, q) in job.cols], np.int32)
-        rhs = np.stack([st.rhs_vector(job.routes[k].rhs_top(job.freqs[q]), job.routes[k].J()) for k, q in job.cols])
-        prec = "mixed_pc64" if precision == "mixed" and getattr(obj, "stiff", False) else precision
-        ncol = len(job.cols)
-        step = st.columns_that_fit(ncol, restart, prec)
-        n = st.handle.n_dense
-        x = np.zeros_like(rhs)
-        its = np.zeros(ncol, np.int32)
-        res = np.zeros(ncol)
-        for c0 in range(0, ncol, step):
-            sl = slice(c0, min(ncol, c0 + step))
-            m = sl.stop - sl.start
-            B = torch.zeros((m, n), dtype=torch.complex128, device="cuda")
-            X = torch.zeros_like(B)
-            st.handle.to_dense(rhs[sl], B.data_ptr(), stream.cuda_stream)
-            its[sl], res[sl] = st.handle.solve_device(obj, col_op[sl], B.data_ptr(), X.data_ptr(), job.tol,
-                                                      restart=restart, max_its=max_its, precision=prec,
-                                                      stream=stream.cuda_stream, reorth=0.0)
-            x[sl] = st.handle.to_compact(X.data_ptr(), m, stream.cuda_stream)
-            del B, X
-        stream.synchronize()
+        avail = int(avail_bytes if avail_bytes is not None else 0.9 * native.memory(st.handle, 1)["free"])
+        nq = len(job.freqs)
+        chunk = max(1, min(nq, int(0.5 * avail // max(st.factorisation_bytes(1), 1))))
+        per_col = _column_bytes(job, restart, precision)
+        for q0 in range(0, nq, chunk):
+            qs = list(range(q0, min(nq, q0 + chunk)))
+            tf = time.perf_counter()
+            ops = st.factorise([job.freqs[q] for q in qs], together=True)
+            t_fact += time.perf_counter() - tf
+            obj = ops[0][0]
+            prec = "mixed_pc64" if precision == "mixed" and getattr(obj, "stiff", False) else precision
+            mine = [c for c, (_, q) in enumerate(job.cols) if q0 <= q < q0 + len(qs)]
+            room = max(avail - st.resident_bytes(len(qs)), per_col)
+            step = max(1, min(len(mine), int(room // per_col), st.columns_that_fit(len(mine), restart, prec)))
+            for c0 in range(0, len(mine), step):
+                sel = mine[c0: c0 + step]
+                m = len(sel)
+                rhs = np.stack([st.rhs_vector(job.routes[k].rhs_top(job.freqs[q]), job.routes[k].J())
+                                for k, q in (job.cols[c] for c in sel)])
+                col_op = np.array([ops[job.cols[c][1] - q0][1] for c in sel], np.int32)
+                B = torch.zeros((m, n), dtype=torch.complex128, device="cuda")
+                X = torch.zeros_like(B)
+                st.handle.to_dense(rhs, B.data_ptr(), stream.cuda_stream)
+                its[sel], res[sel] = st.handle.solve_device(obj, col_op, B.data_ptr(), X.data_ptr(), job.tol,
+                                                            restart=restart, max_its=max_its, precision=prec,
+                                                            stream=stream.cuda_stream, reorth=0.0)
+                x[sel] = st.handle.to_compact(X.data_ptr(), m, stream.cuda_stream)
+                del B, X
+            stream.synchronize()
+            del ops, obj
+            st.release_operators()
         seconds = time.perf_counter() - t0
     Z = np.zeros(ncol, complex)
     for c, (k, q) in enumerate(job.cols):
@@ -147,9 +172,9 @@ def solve_all(jobs: list, concurrency: int = 8, budget_bytes: Optional[int] = No
         job = jobs[i]
         if not hasattr(local, "stream"):
             local.stream = torch.cuda.Stream()
-        need = budget.acquire(_device_bytes(job, len(job.cols), restart, precision))
+        need = budget.acquire(_device_bytes(job, restart, precision))
         try:
-            return i, solve_board(job, local.stream, restart, precision)
+            return i, solve_board(job, local.stream, restart, precision, avail_bytes=need)
         finally:
             budget.release(need)
 

@@ -17,6 +17,7 @@
 #include <chrono>
 #include <cmath>
 #include <complex>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -465,6 +466,8 @@ static void precond(gt_geometry* G, gt_operators* ops, const cx<R>* r, int64_t l
                     cudaStream_t st,
                     const int* col_list = nullptr) {
     Profiler* P = &G->prof;
+    if (!panel_of<R>(ops) || !panel_rm_of<R>(ops))
+        throw Invalid("these operators keep their FP32 panels only (GT_OPS_FP32_PANELS): no FP64 preconditioner");
     const double es = sizeof(cx<R>), n = (double)G->geo.n, nfac = (double)G->F.nfac;
     const double nodes = (double)G->geo.S * G->geo.nx * G->geo.ny, nXYC = (double)(G->geo.off_b - G->geo.off_x);
     // the factor's panels are read once per column group in each direction
@@ -534,14 +537,29 @@ static void precond(gt_geometry* G, gt_operators* ops, const cx<R>* r, int64_t l
     }
 }
 
-// the solve kernels hold a front's rows for 8 columns plus up to 16 warps' partial sums in shared memory
-static bool solve_fits(const gt_geometry* G, size_t elem) {
-    return (size_t)(G->max_nf + 16 * 32) * 8 * elem <= 220 * 1024;
+// The triangular sweeps stage, per block, a front's rows for every column of a group in shared memory: the own
+// and boundary rows of the forward assembly (max_nown + max_nf), the own rows plus up to 17 x 32 rows of tiles
+// and partial sums of the forward products (max_nown + 544), the front's rows plus up to 16 x 32 partial sums of
+// the backward products (max_nf + 512).  The widest group of 8, 4 or 2 columns whose staging fits a block's
+// 227 KB is taken (narrower groups read the panel once per fewer columns); 0 when not even 2 fit.
+static int group_width(const gt_geometry* G, size_t elem) {
+    size_t nown = 1;
+    for (int v : G->level_maxnown) nown = std::max(nown, (size_t)v);
+    const size_t nf = (size_t)std::max(G->max_nf, 1);
+    const size_t rows = std::max({nown + nf, nown + 544, nf + 512});
+    const char* cap_env = std::getenv("GT_GROUP_WIDTH");       // a lower cap, for tests of the narrow groups
+    const int cap = cap_env ? std::atoi(cap_env) : 8;
+    for (int gc : {8, 4, 2})
+        if (gc <= cap && (size_t)gc * rows * elem <= 227 * 1024) return gc;
+    return 0;
 }
 
+static bool solve_fits(const gt_geometry* G, size_t elem) { return group_width(G, elem) > 0; }
+
 static int group_max(const gt_geometry* G, size_t elem) {
-    if (!solve_fits(G, elem)) throw Invalid("a front is too large for the triangular-solve kernels' shared memory");
-    return 8;
+    const int gc = group_width(G, elem);
+    if (!gc) throw Invalid("a front is too large for the triangular-solve kernels' shared memory");
+    return gc;
 }
 
 
@@ -750,7 +768,7 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
     GT_CUDA(cudaMemcpyAsync(h_bnorm.data(), W.bnorm, ncol * sizeof(double), cudaMemcpyDeviceToHost, st));
     GT_CUDA(cudaMemcpyAsync(h_rho.data(), W.rho, ncol * sizeof(double), cudaMemcpyDeviceToHost, st));
     GT_CUDA(cudaStreamSynchronize(st));
-    const int gmax = group_max(G, sizeof(cx<R>));
+    const int gmax = group_max(G, pc64 ? sizeof(c64) : sizeof(cx<R>));
     B* V = static_cast<B*>(W.V);
     cx<R>* vcur = narrow ? static_cast<cx<R>*>(W.vcur) : nullptr;
     const R bscale = narrow ? R(std::ldexp(1.0, (int)std::lround(0.5 * std::log2((double)n)))) : R(1);
@@ -977,6 +995,8 @@ static int run_solve(gt_geometry* G, gt_operators* ops, int ncol, const int* col
     if (o.max_outer < 1) o.max_outer = 1;
     for (int c = 0; c < ncol; ++c)
         if (col_op[c] < 0 || col_op[c] >= ops->nops) throw Invalid("column operator index out of range");
+    if ((o.precision == 1 || o.precision == 3) && (!ops->panel64 || !ops->panel64_rm))
+        throw Invalid("precision 1 and 3 need the FP64 panels these operators did not keep (GT_OPS_FP32_PANELS)");
     if (o.precision == 1) return solve_impl<double>(G, ops, ncol, col_op, o, its, res, st);
     if (o.precision == 2) return solve_impl<float, h16c>(G, ops, ncol, col_op, o, its, res, st);
     if (o.precision == 3) {
@@ -1340,7 +1360,14 @@ int gt_operators_create(gt_geometry* G, int32_t n_ops, const double* omega, cons
 int gt_operators_create_shared(gt_geometry* G, int32_t n_ops, const double* omega, const double* zs,
                                const double* zcap, const double* zbr, const double* table, const int32_t* factor_of,
                                gt_operators** out) {
+    return gt_operators_create_ex(G, n_ops, omega, zs, zcap, zbr, table, factor_of, 0, out);
+}
+
+int gt_operators_create_ex(gt_geometry* G, int32_t n_ops, const double* omega, const double* zs,
+                           const double* zcap, const double* zbr, const double* table, const int32_t* factor_of,
+                           int32_t flags, gt_operators** out) {
     GT_GUARD_BEGIN
+    if (flags & ~GT_OPS_FP32_PANELS) throw Invalid("unknown operator flags");
     if (!G || !out || n_ops < 1) throw Invalid("bad arguments");
     if (G->n_lowrank)
         throw Invalid("the geometry's last branches are a low-rank update of a base: make its operators with "
@@ -1385,6 +1412,10 @@ int gt_operators_create_shared(gt_geometry* G, int32_t n_ops, const double* omeg
         O->tab32 = p.upload(t32.data(), t32.size());
         O->stiff = stiffness(t64, nf_ops, g);
     }
+    // FP32 panels only: the FP64 factor lives in temporary memory while it is made and converted, and no FP64
+    // row-major copy is made; a stiff set keeps its FP64 panels, which its FP64 preconditioner needs
+    const bool keep64 = !(flags & GT_OPS_FP32_PANELS) ||
+                        std::any_of(O->stiff.begin(), O->stiff.end(), [](char v) { return v != 0; });
     n_ops = nf_ops;        // the factorisation below runs over the factorised operators
     cudaStream_t st = 0;
     const Fronts& F = G->F;
@@ -1393,10 +1424,10 @@ int gt_operators_create_shared(gt_geometry* G, int32_t n_ops, const double* omeg
     c64* upd = tmp.alloc<c64>((size_t)n_ops * std::max<int64_t>(F.upd_total, 1));
     int* status = tmp.alloc<int>(1);
     GT_CUDA(cudaMemsetAsync(status, 0, sizeof(int), st));
-    O->panel64 = p.alloc<c64>((size_t)n_ops * F.panel_total);
+    O->panel64 = (keep64 ? p : tmp).alloc<c64>((size_t)n_ops * F.panel_total);
     O->panel32 = p.alloc<c32>((size_t)n_ops * F.panel_total);
     O->panel32_rm = p.alloc<c32>((size_t)n_ops * F.panel_total);
-    O->panel64_rm = p.alloc<c64>((size_t)n_ops * F.panel_total);
+    O->panel64_rm = keep64 ? p.alloc<c64>((size_t)n_ops * F.panel_total) : nullptr;
     O->dinv64 = p.alloc<c64>((size_t)n_ops * F.nfac);
     O->dinv32 = p.alloc<c32>((size_t)n_ops * F.nfac);
     Profiler* P = &G->prof;
@@ -1430,6 +1461,7 @@ int gt_operators_create_shared(gt_geometry* G, int32_t n_ops, const double* omeg
     P->flush();
     if (h_status) throw Invalid("the Schur complement has a zero or non-finite pivot (a piece of copper with no "
                                 "path to its reference node?)");
+    if (!keep64) O->panel64 = nullptr;   // freed with the temporary memory
     *out = O.release();
     return GT_OK;
     GT_GUARD_END
@@ -1451,6 +1483,8 @@ int gt_operators_derive(gt_geometry* G, const gt_operators* base, int32_t n_ops,
     for (int e = 0; e < 2 * bg.nbr; ++e)
         if (G->h_branch_nodes[e] != BG->h_branch_nodes[e]) throw Invalid("the base's branches must lead the geometry's");
     if (n_ops != base->nops) throw Invalid("n_ops must equal the base's operator count");
+    if (!base->panel64 || !base->panel64_rm)
+        throw Invalid("derive from operators that kept their FP64 panels (made without GT_OPS_FP32_PANELS)");
     if (k > G->F.nfac) throw Invalid("more added branches than kept nodes");
     std::lock_guard<std::mutex> lk(G->lock);
     std::unique_ptr<gt_operators> O(new gt_operators());

@@ -171,6 +171,7 @@ void launch_bnd_inv(const Fronts& F, c64* panel, int max_nbnd, int nops, cudaStr
 // Finish the solve panels: the own block gets its inverse below an explicit unit diagonal (moved from the
 // upper triangle, which becomes zero; the pivots go to dinv as 1/D), and the FP32 column-major, FP32 / FP64
 // row-major copies are written.
+// r64 (the FP64 row-major copy) may be null: operators that keep their FP32 panels only
 __global__ void panel_convert_kernel(Fronts F, c64* __restrict__ p64, c32* __restrict__ p32, c32* __restrict__ r32,
                                      c64* __restrict__ r64, c64* __restrict__ d64, c32* __restrict__ d32) {
     const int f = blockIdx.x;
@@ -196,11 +197,11 @@ __global__ void panel_convert_kernel(Fronts F, c64* __restrict__ p64, c32* __res
             p64[base + qt] = zero<double>();
             p32[base + qt] = zero<float>();
             r32[base + (int64_t)k * nown + i] = zero<float>();
-            r64[base + (int64_t)k * nown + i] = zero<double>();
+            if (r64) r64[base + (int64_t)k * nown + i] = zero<double>();
         }
         p32[base + q] = cvt<float>(v);
         r32[base + (int64_t)i * nown + k] = cvt<float>(v);
-        r64[base + (int64_t)i * nown + k] = v;
+        if (r64) r64[base + (int64_t)i * nown + k] = v;
     }
 }
 
@@ -221,7 +222,6 @@ void launch_panel_convert(const Fronts& F, c64* p64, c32* p32, c32* r32, c64* r6
 // the block into 32-row (32-column) tiles and the product's inner dimension into segments whose partial sums
 // meet in shared memory.  The launch shape is chosen per level so that the top of the tree, with few fronts,
 // still spreads over every SM.  Panel elements are read once per task by consecutive lanes, LB loads in flight.
-constexpr int GMAXC = 8;
 constexpr int LB = 8;
 constexpr int SOLVE_THREADS = 512;
 
@@ -241,15 +241,29 @@ __device__ __forceinline__ void lds2(const c64* p, c64& a, c64& b) {
     b = p[1];
 }
 
-// acc[c] += a * x[c] over all GMAXC columns of one k-major shared row x (unused columns hold zeros)
-template <typename R>
+// acc += a * u as four fused multiply-adds (the plain complex expression costs two products and two sums more)
+__device__ __forceinline__ void cfma(c32& acc, c32 a, c32 u) {
+    acc.re = __fmaf_rn(a.re, u.re, acc.re);
+    acc.re = __fmaf_rn(-a.im, u.im, acc.re);
+    acc.im = __fmaf_rn(a.re, u.im, acc.im);
+    acc.im = __fmaf_rn(a.im, u.re, acc.im);
+}
+__device__ __forceinline__ void cfma(c64& acc, c64 a, c64 u) {
+    acc.re = __fma_rn(a.re, u.re, acc.re);
+    acc.re = __fma_rn(-a.im, u.im, acc.re);
+    acc.im = __fma_rn(a.re, u.im, acc.im);
+    acc.im = __fma_rn(a.im, u.re, acc.im);
+}
+
+// acc[c] += a * x[c] over all GC columns of one k-major shared row x (unused columns hold zeros)
+template <typename R, int GC>
 __device__ __forceinline__ void mac_row(cx<R>* acc, cx<R> a, const cx<R>* x) {
 #pragma unroll
-    for (int c2 = 0; c2 < GMAXC / 2; ++c2) {
+    for (int c2 = 0; c2 < GC / 2; ++c2) {
         cx<R> u, v;
         lds2(x + 2 * c2, u, v);
-        acc[2 * c2] += a * u;
-        acc[2 * c2 + 1] += a * v;
+        cfma(acc[2 * c2], a, u);
+        cfma(acc[2 * c2 + 1], a, v);
     }
 }
 
@@ -262,12 +276,12 @@ __device__ __forceinline__ void prefetch_run(const cx<R>* __restrict__ A, int ld
     for (int u = 0; u < LB; ++u) l[u] = u < cnt ? A[u * lda] : zero<R>();
 }
 
-template <typename R>
+template <typename R, int GC>
 __device__ __forceinline__ void sweep(const cx<R>* __restrict__ A, int lda, const cx<R>* x, int xs, int cnt,
                                       const cx<R>* l0, cx<R>* acc) {
 #pragma unroll
     for (int u = 0; u < LB; ++u)
-        if (u < cnt) mac_row<R>(acc, l0[u], x + u * xs);
+        if (u < cnt) mac_row<R, GC>(acc, l0[u], x + u * xs);
     A += LB * lda;
     x += LB * xs;
     int t = LB;
@@ -276,28 +290,28 @@ __device__ __forceinline__ void sweep(const cx<R>* __restrict__ A, int lda, cons
 #pragma unroll
         for (int u = 0; u < LB; ++u) l[u] = A[u * lda];
 #pragma unroll
-        for (int u = 0; u < LB; ++u) mac_row<R>(acc, l[u], x + u * xs);
+        for (int u = 0; u < LB; ++u) mac_row<R, GC>(acc, l[u], x + u * xs);
         A += LB * lda;
         x += LB * xs;
     }
     for (; t < cnt; ++t) {
-        mac_row<R>(acc, *A, x);
+        mac_row<R, GC>(acc, *A, x);
         A += lda;
         x += xs;
     }
 }
 
 // The forward rows of front f for a group: own rows of w (s in factor order plus the children's updates)
-// into ws (k-major, ldw = GMAXC) and boundary rows r0 <= p < r1 into wt ([c][TR]).  Loads are issued four
+// into ws (k-major, ldw = GC) and boundary rows r0 <= p < r1 into wt ([c][TR]).  Loads are issued four
 // at a time per thread ahead of their stores.
-template <typename R>
+template <typename R, int GC>
 __device__ __forceinline__ void fwd_gather(const Fronts& F, int f, const int* gs, int gc, const cx<R>* __restrict__ sf,
                                            const cx<R>* __restrict__ uvec, cx<R>* ws, cx<R>* wt, int TR, int r0, int r1) {
     const int nown = (int)F.nown[f];
     const int64_t own0 = F.own_start[f];
     const int tid = threadIdx.x, nth = blockDim.x;
     const int tot = gc * nown;
-    for (int q = tot + tid; q < GMAXC * nown; q += nth) ws[(q % nown) * GMAXC + q / nown] = zero<R>();
+    for (int q = tot + tid; q < GC * nown; q += nth) ws[(q % nown) * GC + q / nown] = zero<R>();
     for (int q0 = tid; q0 < tot; q0 += 4 * nth) {
         cx<R> v[4];
 #pragma unroll
@@ -308,7 +322,7 @@ __device__ __forceinline__ void fwd_gather(const Fronts& F, int f, const int* gs
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             const int q = q0 + u * nth;
-            if (q < tot) ws[(q % nown) * GMAXC + q / nown] = v[u];
+            if (q < tot) ws[(q % nown) * GC + q / nown] = v[u];
         }
     }
     __syncthreads();
@@ -331,7 +345,7 @@ __device__ __forceinline__ void fwd_gather(const Fronts& F, int f, const int* gs
                 const int q = q0 + u * nth;
                 if (q >= tc) break;
                 const int c = q / nb;
-                if (p[u] < nown) ws[p[u] * GMAXC + c] += v[u];
+                if (p[u] < nown) ws[p[u] * GC + c] += v[u];
                 else if (p[u] >= r0 && p[u] < r1) wt[c * TR + p[u] - r0] += v[u];
             }
         }
@@ -341,25 +355,25 @@ __device__ __forceinline__ void fwd_gather(const Fronts& F, int f, const int* gs
 
 // Forward assembly of a front split over several blocks, once per (front, group): w_own to wasm (factor
 // order), the children's updates of the boundary rows to the front's own update-vector slots.
-template <typename R>
+template <typename R, int GC>
 __global__ void __launch_bounds__(256) fwd_assemble_kernel(Fronts F, const int64_t* __restrict__ front_list,
                                                            const cx<R>* sf, cx<R>* __restrict__ uvec, cx<R>* wasm,
                                                            Groups G, int ldw, int TR) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    cx<R>* ws = reinterpret_cast<cx<R>*>(smem_raw);   // [k][GMAXC]
-    cx<R>* wt = ws + GMAXC * ldw;                      // [c][TR] boundary rows
+    cx<R>* ws = reinterpret_cast<cx<R>*>(smem_raw);   // [k][GC]
+    cx<R>* wt = ws + GC * ldw;                      // [c][TR] boundary rows
     const int g = blockIdx.x % G.ngroup;
     const int f = (int)front_list[blockIdx.x / G.ngroup];
     const int* gs = G.gslot + G.gptr[g];
     const int gc = G.gptr[g + 1] - G.gptr[g];
     const int nown = (int)F.nown[f], nbnd = (int)F.nbnd[f], nf = nown + nbnd;
     const int64_t own0 = F.own_start[f];
-    for (int q = threadIdx.x; q < GMAXC * TR; q += blockDim.x) wt[q] = zero<R>();
+    for (int q = threadIdx.x; q < GC * TR; q += blockDim.x) wt[q] = zero<R>();
     __syncthreads();
-    fwd_gather<R>(F, f, gs, gc, sf, uvec, ws, wt, TR, nown, nf);
+    fwd_gather<R, GC>(F, f, gs, gc, sf, uvec, ws, wt, TR, nown, nf);
     for (int q = threadIdx.x; q < gc * nown; q += blockDim.x) {
         const int c = q / nown, r = q - c * nown;
-        wasm[(int64_t)gs[c] * F.nfac + own0 + r] = ws[r * GMAXC + c];
+        wasm[(int64_t)gs[c] * F.nfac + own0 + r] = ws[r * GC + c];
     }
     for (int q = threadIdx.x; q < gc * nbnd; q += blockDim.x) {
         const int c = q / nbnd, j = q - c * nbnd;
@@ -368,7 +382,7 @@ __global__ void __launch_bounds__(256) fwd_assemble_kernel(Fronts F, const int64
 }
 
 // pre: the front was assembled by fwd_assemble_kernel (own rows in wasm, boundary rows in uvec)
-template <typename R>
+template <typename R, int GC>
 __global__ void __launch_bounds__(SOLVE_THREADS, 2) fwd_gemv_kernel(Fronts F, const int64_t* __restrict__ front_list, int nblk,
                                                                  int rt, int kseg, const cx<R>* __restrict__ panel,
                                                                  const cx<R>* __restrict__ dinv, const cx<R>* sf,
@@ -376,9 +390,9 @@ __global__ void __launch_bounds__(SOLVE_THREADS, 2) fwd_gemv_kernel(Fronts F, co
                                                                  const cx<R>* wasm, Groups G, int ldw, int pre) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int TR = 32 * rt;
-    cx<R>* ws = reinterpret_cast<cx<R>*>(smem_raw);   // [k][GMAXC] own rows of w
-    cx<R>* wt = ws + GMAXC * ldw;                      // [c][TR] the block's boundary rows of w
-    cx<R>* red = wt + GMAXC * TR;                      // [seg][c][TR] partial sums
+    cx<R>* ws = reinterpret_cast<cx<R>*>(smem_raw);   // [k][GC] own rows of w
+    cx<R>* wt = ws + GC * ldw;                      // [c][TR] the block's boundary rows of w
+    cx<R>* red = wt + GC * TR;                      // [seg][c][TR] partial sums
     const int b = blockIdx.x % nblk, rest = blockIdx.x / nblk;
     const int g = rest % G.ngroup;
     const int f = (int)front_list[rest / G.ngroup];
@@ -402,37 +416,37 @@ __global__ void __launch_bounds__(SOLVE_THREADS, 2) fwd_gemv_kernel(Fronts F, co
     // lanes past the block's rows sweep its last row (results dropped)
     const cx<R>* A = P + (int64_t)k0 * nf + min(r, r1 - 1);
     if (pre) {
-        for (int q = tid; q < GMAXC * nown; q += nth) {
+        for (int q = tid; q < GC * nown; q += nth) {
             const int c = q / nown, r = q - c * nown;
-            ws[r * GMAXC + c] = c < gc ? wasm[(int64_t)gs[c] * F.nfac + own0 + r] : zero<R>();
+            ws[r * GC + c] = c < gc ? wasm[(int64_t)gs[c] * F.nfac + own0 + r] : zero<R>();
         }
-        for (int q = tid; q < GMAXC * TR; q += nth) {
+        for (int q = tid; q < GC * TR; q += nth) {
             const int c = q / TR, rr = q - c * TR, row = r0 + rr;
             wt[q] = (c < gc && row >= nown && row < r1)
                         ? uvec[(int64_t)gs[c] * F.vec_total + F.vec_off[f] + (row - nown)] : zero<R>();
         }
         __syncthreads();
     } else {
-        for (int q = tid; q < GMAXC * TR; q += nth) wt[q] = zero<R>();
+        for (int q = tid; q < GC * TR; q += nth) wt[q] = zero<R>();
         __syncthreads();
-        fwd_gather<R>(F, f, gs, gc, sf, uvec, ws, wt, TR, r0, r1);
+        fwd_gather<R, GC>(F, f, gs, gc, sf, uvec, ws, wt, TR, r0, r1);
     }
     cx<R> l0[LB];
     prefetch_run<R>(A, nf, k1 - k0, l0);
-    cx<R> acc[GMAXC];
+    cx<R> acc[GC];
 #pragma unroll
-    for (int c = 0; c < GMAXC; ++c) acc[c] = zero<R>();
-    sweep<R>(A, nf, ws + k0 * GMAXC, GMAXC, k1 - k0, l0, acc);
+    for (int c = 0; c < GC; ++c) acc[c] = zero<R>();
+    sweep<R, GC>(A, nf, ws + k0 * GC, GC, k1 - k0, l0, acc);
     if (kseg > 1) {
 #pragma unroll
-        for (int c = 0; c < GMAXC; ++c)
-            if (c < gc) red[(seg * GMAXC + c) * TR + rl] = acc[c];
+        for (int c = 0; c < GC; ++c)
+            if (c < gc) red[(seg * GC + c) * TR + rl] = acc[c];
         __syncthreads();
         for (int q = tid; q < gc * TR; q += nth) {
             const int c = q / TR, rr = q - c * TR;
             if (r0 + rr >= r1) continue;
             cx<R> v = red[c * TR + rr];
-            for (int sg = 1; sg < kseg; ++sg) v += red[(sg * GMAXC + c) * TR + rr];
+            for (int sg = 1; sg < kseg; ++sg) v += red[(sg * GC + c) * TR + rr];
             const int row = r0 + rr;
             if (row < nown) z[(int64_t)gs[c] * F.nfac + own0 + row] = dinv[(int64_t)op * F.nfac + own0 + row] * v;
             else uvec[(int64_t)gs[c] * F.vec_total + F.vec_off[f] + (row - nown)] = wt[c * TR + rr] + v;
@@ -441,17 +455,17 @@ __global__ void __launch_bounds__(SOLVE_THREADS, 2) fwd_gemv_kernel(Fronts F, co
         if (r < nown) {
             const cx<R> dv = dinv[(int64_t)op * F.nfac + own0 + r];
 #pragma unroll
-            for (int c = 0; c < GMAXC; ++c)
+            for (int c = 0; c < GC; ++c)
                 if (c < gc) z[(int64_t)gs[c] * F.nfac + own0 + r] = dv * acc[c];
         } else {
 #pragma unroll
-            for (int c = 0; c < GMAXC; ++c)
+            for (int c = 0; c < GC; ++c)
                 if (c < gc) uvec[(int64_t)gs[c] * F.vec_total + F.vec_off[f] + (r - nown)] = wt[c * TR + rl] + acc[c];
         }
     }
 }
 
-template <typename R>
+template <typename R, int GC>
 __global__ void __launch_bounds__(SOLVE_THREADS, 2) bwd_gemv_kernel(Fronts F, const int64_t* __restrict__ front_list, int nblk,
                                                                  int ct, int iseg, int cw,
                                                                  const cx<R>* __restrict__ panel_rm,
@@ -459,8 +473,8 @@ __global__ void __launch_bounds__(SOLVE_THREADS, 2) bwd_gemv_kernel(Fronts F, co
                                                                  cx<R>* __restrict__ sd, Groups G, int ldv) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int TC = cw * ct;       // a tile: cw columns, its warp's 32 / cw lane groups take alternate rows
-    cx<R>* v = reinterpret_cast<cx<R>*>(smem_raw);    // [i - kb0][GMAXC]: rows kb0 .. nf of [z_own; y_bnd]
-    cx<R>* red = v + GMAXC * ldv;                      // [seg][c][TC]
+    cx<R>* v = reinterpret_cast<cx<R>*>(smem_raw);    // [i - kb0][GC]: rows kb0 .. nf of [z_own; y_bnd]
+    cx<R>* red = v + GC * ldv;                      // [seg][c][TC]
     const int b = blockIdx.x % nblk, rest = blockIdx.x / nblk;
     const int g = rest % G.ngroup;
     const int f = (int)front_list[rest / G.ngroup];
@@ -489,9 +503,9 @@ __global__ void __launch_bounds__(SOLVE_THREADS, 2) bwd_gemv_kernel(Fronts F, co
     cx<R> l0[LB];
     prefetch_run<R>(A, nph * nown, cnt, l0);
     const int nv = nf - kb0, tot = gc * nv;
-    for (int q = gc * nv + tid; q < GMAXC * nv; q += nth) {
+    for (int q = gc * nv + tid; q < GC * nv; q += nth) {
         const int c = q / nv;
-        v[(q - c * nv) * GMAXC + c] = zero<R>();
+        v[(q - c * nv) * GC + c] = zero<R>();
     }
     for (int q0 = tid; q0 < tot; q0 += 4 * nth) {
         int64_t src[4];
@@ -509,38 +523,38 @@ __global__ void __launch_bounds__(SOLVE_THREADS, 2) bwd_gemv_kernel(Fronts F, co
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             const int q = q0 + u * nth;
-            if (q < tot) v[(q % nv) * GMAXC + q / nv] = x[u];
+            if (q < tot) v[(q % nv) * GC + q / nv] = x[u];
         }
     }
     __syncthreads();
-    cx<R> acc[GMAXC];
+    cx<R> acc[GC];
 #pragma unroll
-    for (int c = 0; c < GMAXC; ++c) acc[c] = zero<R>();
-    sweep<R>(A, nph * nown, v + (i0 + ph - kb0) * GMAXC, nph * GMAXC, cnt, l0, acc);
+    for (int c = 0; c < GC; ++c) acc[c] = zero<R>();
+    sweep<R, GC>(A, nph * nown, v + (i0 + ph - kb0) * GC, nph * GC, cnt, l0, acc);
     if (nph == 2) {
 #pragma unroll
-        for (int c = 0; c < GMAXC; ++c) {
+        for (int c = 0; c < GC; ++c) {
             acc[c].re += __shfl_xor_sync(0xffffffffu, acc[c].re, 16);
             acc[c].im += __shfl_xor_sync(0xffffffffu, acc[c].im, 16);
         }
     }
     if (iseg > 1) {
 #pragma unroll
-        for (int c = 0; c < GMAXC; ++c)
-            if (c < gc && ph == 0) red[(seg * GMAXC + c) * TC + kl] = acc[c];
+        for (int c = 0; c < GC; ++c)
+            if (c < gc && ph == 0) red[(seg * GC + c) * TC + kl] = acc[c];
         __syncthreads();
         for (int q = tid; q < gc * TC; q += nth) {
             const int c = q / TC, kk = q - c * TC;
             if (kb0 + kk >= kb1) continue;
             cx<R> s = red[c * TC + kk];
-            for (int sg = 1; sg < iseg; ++sg) s += red[(sg * GMAXC + c) * TC + kk];
+            for (int sg = 1; sg < iseg; ++sg) s += red[(sg * GC + c) * TC + kk];
             y[(int64_t)gs[c] * F.nfac + own0 + kb0 + kk] = s;
             sd[(int64_t)gs[c] * F.nnode + F.iperm[own0 + kb0 + kk]] = s;
         }
     } else if (valid && ph == 0) {
         const int64_t node = F.iperm[own0 + k];
 #pragma unroll
-        for (int c = 0; c < GMAXC; ++c)
+        for (int c = 0; c < GC; ++c)
             if (c < gc) {
                 y[(int64_t)gs[c] * F.nfac + own0 + k] = acc[c];
                 sd[(int64_t)gs[c] * F.nnode + node] = acc[c];
@@ -561,11 +575,10 @@ static void solve_shape(int ntask, int ntile, int inner, int& per_blk, int& nseg
     }
 }
 
-template <typename R>
-void launch_fwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, int max_nown,
-                      const cx<R>* panel, const cx<R>* dinv, const cx<R>* sf, cx<R>* z, cx<R>* uvec, cx<R>* wasm,
-                      const Groups& G, int gmax, cudaStream_t st) {
-    if (gmax > GMAXC) throw CudaError{cudaErrorInvalidValue, "column group larger than the solve kernels take"};
+template <typename R, int GC>
+static void fwd_level_gc(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, int max_nown,
+                         const cx<R>* panel, const cx<R>* dinv, const cx<R>* sf, cx<R>* z, cx<R>* uvec, cx<R>* wasm,
+                         const Groups& G, cudaStream_t st) {
     const int ntask = nf_level * G.ngroup;
     const int ntile = ceil_div(max_nf, 32);
     int rt, kseg;
@@ -574,23 +587,21 @@ void launch_fwd_level(const Fronts& F, const int64_t* front_list, int nf_level, 
     const int pre = nblk > 1;
     if (pre) {
         const int TRa = std::max(max_nf - 1, 1);
-        const size_t sa = (size_t)GMAXC * (ldw + TRa) * sizeof(cx<R>);
-        smem_attr<R>((const void*)fwd_assemble_kernel<R>, sa);
-        fwd_assemble_kernel<R><<<ntask, 256, sa, st>>>(F, front_list, sf, uvec, wasm, G, ldw, TRa);
+        const size_t sa = (size_t)GC * (ldw + TRa) * sizeof(cx<R>);
+        smem_attr<R>((const void*)fwd_assemble_kernel<R, GC>, sa);
+        fwd_assemble_kernel<R, GC><<<ntask, 256, sa, st>>>(F, front_list, sf, uvec, wasm, G, ldw, TRa);
         GT_LAUNCH_CHECK();
     }
-    const size_t sm = (size_t)GMAXC * (ldw + 32 * rt + (kseg > 1 ? kseg * 32 * rt : 0)) * sizeof(cx<R>);
-    smem_attr<R>((const void*)fwd_gemv_kernel<R>, sm);
-    fwd_gemv_kernel<R><<<ntask * nblk, 32 * rt * kseg, sm, st>>>(F, front_list, nblk, rt, kseg, panel, dinv, sf, z, uvec,
+    const size_t sm = (size_t)GC * (ldw + 32 * rt + (kseg > 1 ? kseg * 32 * rt : 0)) * sizeof(cx<R>);
+    smem_attr<R>((const void*)fwd_gemv_kernel<R, GC>, sm);
+    fwd_gemv_kernel<R, GC><<<ntask * nblk, 32 * rt * kseg, sm, st>>>(F, front_list, nblk, rt, kseg, panel, dinv, sf, z, uvec,
                                                                 wasm, G, ldw, pre);
     GT_LAUNCH_CHECK();
 }
 
-template <typename R>
-void launch_bwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, int max_nown,
-                      const cx<R>* panel_rm, const cx<R>* z, cx<R>* y, cx<R>* sd, const Groups& G, int gmax,
-                      cudaStream_t st) {
-    if (gmax > GMAXC) throw CudaError{cudaErrorInvalidValue, "column group larger than the solve kernels take"};
+template <typename R, int GC>
+static void bwd_level_gc(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, int max_nown,
+                         const cx<R>* panel_rm, const cx<R>* z, cx<R>* y, cx<R>* sd, const Groups& G, cudaStream_t st) {
     const int ntask = nf_level * G.ngroup;
     // tiles of 16 columns (two lane groups on alternate rows) where they waste fewer lanes than 32
     const int cw = ceil_div(max_nown, 16) * 16 - max_nown < ceil_div(max_nown, 32) * 32 - max_nown ? 16 : 32;
@@ -598,11 +609,37 @@ void launch_bwd_level(const Fronts& F, const int64_t* front_list, int nf_level, 
     int ct, iseg;
     solve_shape(ntask, ntile, max_nf, ct, iseg);
     const int nblk = ceil_div(ntile, ct), ldv = std::max(max_nf, 1);
-    const size_t sm = (size_t)GMAXC * (ldv + (iseg > 1 ? iseg * cw * ct : 0)) * sizeof(cx<R>);
-    smem_attr<R>((const void*)bwd_gemv_kernel<R>, sm);
-    bwd_gemv_kernel<R><<<ntask * nblk, 32 * ct * iseg, sm, st>>>(F, front_list, nblk, ct, iseg, cw, panel_rm, z, y, sd,
+    const size_t sm = (size_t)GC * (ldv + (iseg > 1 ? iseg * cw * ct : 0)) * sizeof(cx<R>);
+    smem_attr<R>((const void*)bwd_gemv_kernel<R, GC>, sm);
+    bwd_gemv_kernel<R, GC><<<ntask * nblk, 32 * ct * iseg, sm, st>>>(F, front_list, nblk, ct, iseg, cw, panel_rm, z, y, sd,
                                                                  G, ldv);
     GT_LAUNCH_CHECK();
+}
+
+// the column-group widths the sweep kernels are built for: a front's rows for GC columns are staged in shared
+// memory, so wide fronts take narrower groups (the panel is then read once per fewer columns)
+template <typename R>
+void launch_fwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, int max_nown,
+                      const cx<R>* panel, const cx<R>* dinv, const cx<R>* sf, cx<R>* z, cx<R>* uvec, cx<R>* wasm,
+                      const Groups& G, int gmax, cudaStream_t st) {
+    switch (gmax) {
+        case 8: fwd_level_gc<R, 8>(F, front_list, nf_level, max_nf, max_nown, panel, dinv, sf, z, uvec, wasm, G, st); return;
+        case 4: fwd_level_gc<R, 4>(F, front_list, nf_level, max_nf, max_nown, panel, dinv, sf, z, uvec, wasm, G, st); return;
+        case 2: fwd_level_gc<R, 2>(F, front_list, nf_level, max_nf, max_nown, panel, dinv, sf, z, uvec, wasm, G, st); return;
+        default: throw CudaError{cudaErrorInvalidValue, "column group width must be 8, 4 or 2"};
+    }
+}
+
+template <typename R>
+void launch_bwd_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, int max_nown,
+                      const cx<R>* panel_rm, const cx<R>* z, cx<R>* y, cx<R>* sd, const Groups& G, int gmax,
+                      cudaStream_t st) {
+    switch (gmax) {
+        case 8: bwd_level_gc<R, 8>(F, front_list, nf_level, max_nf, max_nown, panel_rm, z, y, sd, G, st); return;
+        case 4: bwd_level_gc<R, 4>(F, front_list, nf_level, max_nf, max_nown, panel_rm, z, y, sd, G, st); return;
+        case 2: bwd_level_gc<R, 2>(F, front_list, nf_level, max_nf, max_nown, panel_rm, z, y, sd, G, st); return;
+        default: throw CudaError{cudaErrorInvalidValue, "column group width must be 8, 4 or 2"};
+    }
 }
 
 template void launch_fwd_level<float>(const Fronts&, const int64_t*, int, int, int, const c32*, const c32*, const c32*, c32*, c32*, c32*, const Groups&, int, cudaStream_t);

@@ -60,6 +60,8 @@ class GeometryDesc(C.Structure):
                 ("narrow_rre", DP), ("narrow_twre", DP), ("cap_fill", DP)]
 
 
+GT_OPS_FP32_PANELS = 1                 # gt_operators_create_ex: keep only the FP32 copies of the factor panels
+
 PRECISIONS = {"mixed": 0, "fp64": 1, "mixed16": 2, "mixed_pc64": 3}
 
 # the library's rule for a stiff factorisation (STIFF_RATIO in api.cu): a branch or capacitance admittance above
@@ -120,6 +122,7 @@ def load():
     lib.gt_node_field.argtypes = [P, C.c_int32, P, C.c_double, P, P, P]
     lib.gt_operators_derive.argtypes = [P, P, C.c_int32, DP, DP, DP, DP, DP, C.POINTER(P)]
     lib.gt_operators_create_shared.argtypes = [P, C.c_int32, DP, DP, DP, DP, DP, I32P, C.POINTER(P)]
+    lib.gt_operators_create_ex.argtypes = [P, C.c_int32, DP, DP, DP, DP, DP, I32P, C.c_int32, C.POINTER(P)]
     lib.gt_kernel_spectrum.argtypes = [C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_int32, C.c_int32, DP,
                                        C.c_int32, DP]
     lib.gt_moment.argtypes = [P, C.c_int32, P, DP, C.c_double, DP, P]
@@ -309,11 +312,14 @@ class Geometry:
 class Operators:
     """Factorised Schur complements at several frequencies (gt_operators_create)."""
 
-    def __init__(self, geom: Geometry, keys: list, data: list, factor_of=None, base: "Operators | None" = None):
+    def __init__(self, geom: Geometry, keys: list, data: list, factor_of=None, base: "Operators | None" = None,
+                 fp32_panels: bool = False):
         """factor_of: optional per-operator index of the operator whose factorisation preconditions it
         (gt_operators_create_shared); None: every operator its own.  base: the base stack's operators at the
         same keys, for a derived geometry (gt_operators_derive: the base's factorisations plus a low-rank
-        update for the added branches); kept alive as long as these."""
+        update for the added branches); kept alive as long as these.  fp32_panels: keep only the FP32 copies of
+        the factor (a third of the memory; precision "mixed" / "mixed16" solves only, no derived operators on
+        them; a stiff set keeps its FP64 panels anyway)."""
         lib = geom.lib
         self.geom = geom
         w = np.array([x[0] for x in data], np.float64)
@@ -334,9 +340,11 @@ class Operators:
         else:
             fo = None if factor_of is None else np.ascontiguousarray(factor_of, np.int32)
             self.factor_of = fo
-            check(lib, lib.gt_operators_create_shared(geom.h, len(data), *args,
-                                                      None if fo is None else _ptr(fo, C.c_int32), C.byref(h)),
-                  "gt_operators_create_shared")
+            check(lib, lib.gt_operators_create_ex(geom.h, len(data), *args,
+                                                  None if fo is None else _ptr(fo, C.c_int32),
+                                                  GT_OPS_FP32_PANELS if fp32_panels else 0, C.byref(h)),
+                  "gt_operators_create_ex")
+        self.fp32_panels = bool(fp32_panels) and base is None
         self.h = h
         self.keys = list(keys)
 

@@ -4,8 +4,9 @@ interactive candidate solves, suggest.py:318-325 and 452-465, on PlaneStack.with
 Each geometry stays resident on the device with its kernel spectra, its factorisations at the served
 frequencies and its base solutions (whatif.WhatIf).  Requests arrive on any thread (submit) and return a Future.
 One batcher thread takes every request waiting when the device is free, up to the columns the memory budget
-admits (the Krylov workspace per column, after the resident factorisations), and runs them as ONE device
-solve per geometry:
+admits (the budget governs the requests' working memory, the Krylov workspace and vectors per column; the
+resident geometries are outside it and reported as resident_bytes), and runs them as ONE device solve per
+geometry:
 
 * an edit that adds stitching vias or moves a decoupling part (a removal plus an addition) contributes its
   border columns, the base system's response to each new branch's unit injection at each asked frequency, to
@@ -56,8 +57,8 @@ class Answer:
 
 
 class Server:
-    """Serves Requests on resident geometries {name: WhatIf} (their baselines solved) with continuous batching
-    against budget_bytes of device memory (the resident factorisations counted first)."""
+    """Serves Requests on resident geometries {name: WhatIf} (their baselines solved) with continuous batching,
+    the requests' working memory admitted against budget_bytes."""
 
     def __init__(self, geometries: dict, budget_bytes: float = 120e9, max_cols: Optional[int] = None,
                  restart: int = 50):
@@ -68,13 +69,15 @@ class Server:
         self.restart = restart
         self.q: "queue.Queue" = queue.Queue()
         self.streams = {name: torch.cuda.Stream() for name in self.geo}
-        # columns per batch: the workspace per column against what the budget leaves after the resident state
-        base = self.geo["base"].stack
-        one = native.memory(base.handle, 1, restart)["need"]
-        per = max(native.memory(base.handle, 2, restart)["need"] - one, 1)
-        resident = sum(w.stack.factorisation_bytes(len(w.freqs)) for w in self.geo.values())
-        fit = int((budget_bytes - resident - one) // per) + 1
+        # columns per batch: the workspace per column (the largest geometry's) against the budget
+        one = per = 1
+        for w in self.geo.values():
+            o = native.memory(w.stack.handle, 1, restart)["need"]
+            one = max(one, o)
+            per = max(per, native.memory(w.stack.handle, 2, restart)["need"] - o)
+        fit = int((budget_bytes - one) // per) + 1
         self.max_cols = max(1, min(fit, max_cols or fit))
+        self.resident_bytes = sum(w.stack.resident_bytes(len(w.freqs)) for w in self.geo.values())
         self.batches = []
         self._stop = threading.Event()
         self._thread = threading.Thread(target=self._loop, name="what-if batcher", daemon=True)

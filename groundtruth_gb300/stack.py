@@ -416,6 +416,9 @@ class PlaneStack:
         self._schur_structure(leaf)
         self._lock = threading.Lock()
         self._ops: OrderedDict = OrderedDict()
+        # keep only the FP32 copies of the factor panels (a third of the memory): for stacks that only take
+        # "mixed" solves and are not the base of derived stacks (native.Operators(fp32_panels=True))
+        self.fp32_panels = False
         self.handle = native_geometry(self) if _device else None
 
     # ------------------------------------------------------------------ construction
@@ -972,7 +975,7 @@ class PlaneStack:
             plan = borrow_plan(todo) if borrow else None
             self._admit(len(set(plan)) if plan is not None else len(todo))
             data = [self._freq_tables(k) for k in todo]
-            ops = native.Operators(self.handle, todo, data, plan)
+            ops = native.Operators(self.handle, todo, data, plan, fp32_panels=self.fp32_panels)
             ops.stiff = any(native.stiff_table(d[4], self.tab_cap0) for d in data)
             with self._lock:
                 for n, k in enumerate(todo):
@@ -1063,12 +1066,25 @@ class PlaneStack:
     MEMORY_HEADROOM = 0.9         # of the device's free memory a solve or a factorisation may take
 
     def factorisation_bytes(self, n_fact: int) -> int:
-        """Device bytes of n_fact factorisations (gt_operators_create_shared): each one's panels in FP64 and FP32,
-        column- and row-major, its pivots and tables, and while it is made the Schur values and update matrices."""
+        """Device bytes of n_fact factorisations while they are made (gt_operators_create_ex): each one's panels in
+        FP64 and FP32, column- and row-major (with fp32_panels the FP32 pair kept and the FP64 factor in
+        temporary memory), its pivots and tables, and the Schur values and update matrices."""
         sym = self.sym
-        per = sym.panel_total * (16 + 8 + 8 + 16) + sym.n * (16 + 8) + self.n_table * (16 + 8)
+        panel = (16 + 8 + 8) if self.fp32_panels else (16 + 8 + 8 + 16)
+        per = sym.panel_total * panel + sym.n * (16 + 8) + self.n_table * (16 + 8)
         made = self.sterm.shape[0] * 16 + max(sym.upd_total, 1) * 16
         return int(n_fact * (per + made))
+
+    def resident_bytes(self, n_fact: int) -> int:
+        """Device bytes n_fact factorisations hold once made."""
+        sym = self.sym
+        panel = (8 + 8) if self.fp32_panels else (16 + 8 + 8 + 16)
+        return int(n_fact * (sym.panel_total * panel + sym.n * (16 + 8) + self.n_table * (16 + 8)))
+
+    def release_operators(self):
+        """Drop this stack's cached factorisations (their device memory goes when nothing else holds them)."""
+        with self._lock:
+            self._ops.clear()
 
     def _admit(self, n_fact: int):
         """The memory gate for factorisations (_MemoryGate, peec.py:1442-1501): when n_fact more would not fit

@@ -166,6 +166,17 @@ int gt_operators_create(gt_geometry* g, int32_t n_ops, const double* omega, cons
 int gt_operators_create_shared(gt_geometry* g, int32_t n_ops, const double* omega, const double* zs,
                                const double* zcap, const double* zbr, const double* table, const int32_t* factor_of,
                                gt_operators** out);
+/* As gt_operators_create_shared with flags.  GT_OPS_FP32_PANELS: keep only the FP32 copies of the factor panels
+ * (column- and row-major, 16 bytes per entry instead of 48): the FP64 factor is made in temporary memory and
+ * freed once converted, no FP64 row-major copy is made.  Such operators serve precision 0 and 2 solves and FP32
+ * applications; precision 1 and 3, FP64 preconditioner applications and gt_operators_derive on them return
+ * GT_INVALID_ARGUMENT.  A stiff set (see gt_solve_opts.precision) keeps its FP64 panels regardless.  For hosts
+ * that keep many factorisations resident under a memory budget (the reference's memory gate and relief ladder,
+ * peec.py:1388-1501, 2425-2430, trade factorisations for memory the same way). */
+#define GT_OPS_FP32_PANELS 1
+int gt_operators_create_ex(gt_geometry* g, int32_t n_ops, const double* omega, const double* zs,
+                           const double* zcap, const double* zbr, const double* table, const int32_t* factor_of,
+                           int32_t flags, gt_operators** out);
 /* Operators of a derived geometry (n_lowrank > 0) from its base's (peec.py:2345-2377): operator q is the
  * base's operator q with the added branches, preconditioned by the base's factorisation of q plus the
  * Woodbury identity for the added branches (S' = S + U diag(1/z) U^T; only an n_lowrank x n_lowrank matrix

@@ -32,3 +32,40 @@ def test_a_budget_smaller_than_one_board_runs_the_boards_one_at_a_time(jobs):
     ref = [batch.solve_all([j], concurrency=1)[0] for j in jobs[:3]]
     for a, b in zip(small, ref):
         assert np.linalg.norm(a.x - b.x) <= 1e-12 * np.linalg.norm(b.x)
+
+
+def _columns(st, routes, freqs, precision="mixed"):
+    return st.solve_batch(freqs, [routes[0].rhs_top(f) for f in freqs], [routes[0].J()] * len(freqs), tol=1e-10,
+                          precision=precision, reorth=0.0)
+
+
+def test_operators_with_fp32_panels_only_solve_the_same_and_refuse_fp64():
+    """FP32-panel operators (a third of the factor's memory) give the mixed solve the same panels, so the same
+    answers bit for bit; an FP64 solve on them is refused with a clear error."""
+    from groundtruth_gb300 import stack as gs
+    b = synth.small_pair()
+    st, routes = gs.from_board(b)
+    freqs = [float(f) for f in b.freqs]
+    ref = _columns(st, routes, freqs)
+    st.release_operators()
+    st.fp32_panels = True
+    got = _columns(st, routes, freqs)
+    for a, c in zip(ref, got):
+        assert np.array_equal(a[3], c[3])
+    with pytest.raises(RuntimeError, match="FP64 panels"):
+        _columns(st, routes, freqs, precision="fp64")
+
+
+@pytest.mark.parametrize("width", ["4", "2"])
+def test_narrow_column_groups_give_the_same_solutions(width, monkeypatch):
+    """Fronts too wide for 8 columns' staging take groups of 4 or 2 (the panel read once per fewer columns):
+    the same board solved with the group width capped equals its solve with groups of 8."""
+    from groundtruth_gb300 import stack as gs
+    b = synth.small_stack3()
+    st, routes = gs.from_board(b)
+    freqs = [float(f) for f in b.freqs] * 3           # more columns per operator than a group holds
+    ref = _columns(st, routes, freqs)
+    monkeypatch.setenv("GT_GROUP_WIDTH", width)
+    got = _columns(st, routes, freqs)
+    for a, c in zip(ref, got):
+        assert np.linalg.norm(a[3] - c[3]) <= 1e-12 * np.linalg.norm(a[3])
