@@ -148,6 +148,7 @@ def solve_board(job: BoardJob, stream=None, restart: int = 50, precision: str = 
             stream.synchronize()
             del ops, obj
             st.release_operators()
+        st.trim()                     # the board's workspace goes back before the next board takes memory
         seconds = time.perf_counter() - t0
     Z = np.zeros(ncol, complex)
     for c, (k, q) in enumerate(job.cols):

@@ -1346,6 +1346,18 @@ int gt_geometry_create(const gt_geometry_desc* d, gt_geometry** out) {
     GT_GUARD_END
 }
 
+int gt_geometry_trim(gt_geometry* G) {
+    GT_GUARD_BEGIN
+    if (!G) throw Invalid("null geometry");
+    std::lock_guard<std::mutex> lk(G->lock);
+    if (G->ws) {
+        GT_CUDA(cudaDeviceSynchronize());
+        G->ws.reset();
+    }
+    return GT_OK;
+    GT_GUARD_END
+}
+
 void gt_geometry_free(gt_geometry* g) {
     if (!g) return;
     cudaDeviceSynchronize();

@@ -17,7 +17,7 @@
 // The register DFTs below take their inner twiddles W32^m (and W16, W8, W4 as its powers) from literal
 // tables; the quarter and half turns are exact sign swaps.  The W512 twiddles are the host-computed FP64
 // table rounded to the working precision (the one the Stockham passes use), combined from W^t, W^2t, W^4t,
-// W^8t by at most three products.
+// W^8t by at most three products, once per lane for both of its rows.
 #pragma once
 #include "common.cuh"
 
@@ -146,19 +146,24 @@ template <typename R, bool INV> __device__ __forceinline__ cx<R> twm(cx<R> a, cx
     return INV ? mk<R>(a.re * w.re + a.im * w.im, a.im * w.re - a.re * w.im) : a * w;
 }
 
-// v[k] *= W512^(+-t k), k = 1..15, from the table entries W^t, W^2t, W^4t, W^8t (tw: W512^m, m < 512); each
-// power the product of at most four of them, made as it is used
+// v0[k] and v1[k] *= W512^(+-t k), k = 1..15 (the two rows a lane holds share its twiddles), from the table
+// entries W^t, W^2t, W^4t, W^8t (tw: W512^m, m < 512); each power the product of at most four of them, made once
+// as it is used
 template <typename R, bool INV>
-__device__ __forceinline__ void tw512_lane(cx<R>* v, int t, const cx<R>* __restrict__ tw) {
+__device__ __forceinline__ void tw512_lane2(cx<R>* v0, cx<R>* v1, int t, const cx<R>* __restrict__ tw) {
     const cx<R> w1 = tw[t], w2 = tw[2 * t], w4 = tw[4 * t], w8 = tw[8 * t];
-    v[8] = twm<R, INV>(v[8], w8);
+    v0[8] = twm<R, INV>(v0[8], w8);
+    v1[8] = twm<R, INV>(v1[8], w8);
 #pragma unroll
     for (int k = 1; k < 8; ++k) {
         cx<R> w = (k & 1) ? w1 : ((k & 2) ? w2 : w4);
         if ((k & 1) && (k & 2)) w = w * w2;
         if ((k & 3) && (k & 4)) w = w * w4;
-        v[k] = twm<R, INV>(v[k], w);
-        v[k + 8] = twm<R, INV>(v[k + 8], w * w8);
+        const cx<R> wh = w * w8;
+        v0[k] = twm<R, INV>(v0[k], w);
+        v1[k] = twm<R, INV>(v1[k], w);
+        v0[k + 8] = twm<R, INV>(v0[k + 8], wh);
+        v1[k + 8] = twm<R, INV>(v1[k + 8], wh);
     }
 }
 
@@ -173,13 +178,13 @@ template <typename R, bool HALF>
 __device__ __forceinline__ void fft512_fwd2(cx<R> (&v)[2][16], cx<R> (&u)[32], cx<R>* __restrict__ sx,
                                             const cx<R>* __restrict__ tw) {
     const int lane = threadIdx.x & 31;
+    rdft<R, false, 16, HALF>(v[0]);
+    rdft<R, false, 16, HALF>(v[1]);
+    tw512_lane2<R, false>(v[0], v[1], lane, tw);
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
-        rdft<R, false, 16, HALF>(v[q]);
-        tw512_lane<R, false>(v[q], lane, tw);
+    for (int q = 0; q < 2; ++q)
 #pragma unroll
         for (int k1 = 0; k1 < 16; ++k1) sx[q * WX_ROW + k1 * 33 + lane] = v[q][k1];
-    }
     __syncwarp();
     const int q = lane >> 4, k1 = lane & 15;
 #pragma unroll
@@ -202,13 +207,13 @@ __device__ __forceinline__ void fft512_inv2(cx<R> (&u)[32], cx<R> (&v)[2][16], c
     }
     __syncwarp();
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
+    for (int q = 0; q < 2; ++q)
 #pragma unroll
         for (int k1 = 0; k1 < 16; ++k1) v[q][k1] = sx[q * WX_ROW + k1 * 33 + lane];
-        tw512_lane<R, true>(v[q], lane, tw);
-        rdft<R, true, 16, false, LO>(v[q]);
-    }
     __syncwarp();
+    tw512_lane2<R, true>(v[0], v[1], lane, tw);
+    rdft<R, true, 16, false, LO>(v[0]);
+    rdft<R, true, 16, false, LO>(v[1]);
 }
 
 }  // namespace gt

@@ -403,11 +403,13 @@ __global__ void __launch_bounds__(CW_WARPS * 32, GT_CW_MINB) lp_pass_cw(const c3
     const c32* Ts = T + ((int64_t)blockIdx.z * S + s) * 512 * ldt + i;
     const int q = lane >> 4;
     c32 u[32];
+    float4 f[16];                                  // every load in flight before the first exchange
+#pragma unroll
+    for (int m = 0; m < 16; ++m) f[m] = __ldg(reinterpret_cast<const float4*>(Ts + (int64_t)(lane + 32 * m) * ldt));
 #pragma unroll
     for (int m = 0; m < 16; ++m) {
-        const float4 f = *reinterpret_cast<const float4*>(Ts + (int64_t)(lane + 32 * m) * ldt);
         // mine: row q at k2 = q + 2m; the partner's: row q at k2 = 1 - q + 2m, for which it sends its row-q value
-        const c32 r0 = mk<float>(f.x, f.y), r1 = mk<float>(f.z, f.w);
+        const c32 r0 = mk<float>(f[m].x, f[m].y), r1 = mk<float>(f[m].z, f[m].w);
         const c32 mine = q ? r1 : r0, send = q ? r0 : r1;
         c32 got;
         got.re = __shfl_xor_sync(0xffffffffu, send.re, 16);

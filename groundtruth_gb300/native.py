@@ -109,6 +109,7 @@ def load():
     lib.gt_geometry_create.argtypes = [C.POINTER(GeometryDesc), C.POINTER(P)]
     lib.gt_geometry_free.argtypes = [P]
     lib.gt_geometry_free.restype = None
+    lib.gt_geometry_trim.argtypes = [P]
     lib.gt_operators_create.argtypes = [P, C.c_int32, DP, DP, DP, DP, DP, C.POINTER(P)]
     lib.gt_operators_free.argtypes = [P]
     lib.gt_operators_free.restype = None
@@ -253,6 +254,10 @@ class Geometry:
         if rc not in (GT_OK, GT_NOT_CONVERGED):
             check(self.lib, rc, "gt_solve_device")
         return its, res
+
+    def trim(self):
+        """gt_geometry_trim: free the solve workspace (reallocated by the next solve)."""
+        check(self.lib, self.lib.gt_geometry_trim(self.h), "gt_geometry_trim")
 
     def to_dense(self, compact: np.ndarray, dense_ptr: int, stream: int = 0):
         c = np.ascontiguousarray(np.atleast_2d(compact), np.complex128)

@@ -69,12 +69,14 @@ class Server:
         self.restart = restart
         self.q: "queue.Queue" = queue.Queue()
         self.streams = {name: torch.cuda.Stream() for name in self.geo}
-        # columns per batch: the workspace per column (the largest geometry's) against the budget
-        one = per = 1
+        # columns per batch: every geometry keeps a workspace as wide as the widest batch it took, so the budget
+        # holds max_cols columns of each geometry's workspace
+        one = per = 0
         for w in self.geo.values():
+            w.stack.trim()                         # what the baselines left behind
             o = native.memory(w.stack.handle, 1, restart)["need"]
-            one = max(one, o)
-            per = max(per, native.memory(w.stack.handle, 2, restart)["need"] - o)
+            one += o
+            per += max(native.memory(w.stack.handle, 2, restart)["need"] - o, 1)
         fit = int((budget_bytes - one) // per) + 1
         self.max_cols = max(1, min(fit, max_cols or fit))
         self.resident_bytes = sum(w.stack.resident_bytes(len(w.freqs)) for w in self.geo.values())

@@ -1081,6 +1081,11 @@ class PlaneStack:
         panel = (8 + 8) if self.fp32_panels else (16 + 8 + 8 + 16)
         return int(n_fact * (sym.panel_total * panel + sym.n * (16 + 8) + self.n_table * (16 + 8)))
 
+    def trim(self):
+        """Free the device solve workspace of this stack (the next solve makes it again)."""
+        if self.handle is not None:
+            self.handle.trim()
+
     def release_operators(self):
         """Drop this stack's cached factorisations (their device memory goes when nothing else holds them)."""
         with self._lock:
@@ -1099,6 +1104,7 @@ class PlaneStack:
             self._ops.clear()
         import gc
         gc.collect()
+        self.trim()                   # and the solve workspace, which the next solve makes again
         free = native.memory(self.handle, 1)["free"]
         if need > self.MEMORY_HEADROOM * free:
             raise MemoryError(f"{n_fact} factorisations need {need / 2**30:.1f} GiB, "

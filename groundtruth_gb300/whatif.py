@@ -152,6 +152,7 @@ class WhatIf:
         self.base_psi_ib = {(k, f): complex(np.dot(self.routes[k].psi, x[: st.nb])) for (k, f), x in zip(cols, xs)}
         self.base_r_trace = {(k, f): float(greens.trace_resistance(self.routes[k].segments, f, st.sigma,
                                                                    self.routes[k].trace_t)) for k, f in cols}
+        st.trim()                     # the baseline's workspace (all its columns) is not kept for the edits
         return time.perf_counter() - t0
 
     def evaluate(self, branches: list, nets, freqs, remove=()) -> EditResult:

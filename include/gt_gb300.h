@@ -152,6 +152,10 @@ int64_t gt_launch_count(void);
 /* Build a geometry on the current CUDA device (peec.py:1559-1593, gpu.py:617-666). */
 int gt_geometry_create(const gt_geometry_desc* desc, gt_geometry** out);
 void gt_geometry_free(gt_geometry* g);
+/* Free the geometry's solve workspace (the Krylov bases and vectors sized for its largest solve so far); the next
+ * solve allocates what it needs again.  For hosts that keep many geometries and solve them in turn under one
+ * memory budget (the reference's memory gate, peec.py:1388-1501, releases solver memory between jobs). */
+int gt_geometry_trim(gt_geometry* g);
 
 /* Factorise the Schur complement at n_ops frequencies (peec.py:2345-2445, 2465-2511):
  * omega[n_ops]; zs[n_ops*(S + n_twins)] sheet impedances per square (then the face couplings, with face sheets); zcap[n_ops*n_pairs] and zbr[n_ops*n_branches]

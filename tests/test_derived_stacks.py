@@ -285,11 +285,16 @@ def test_borrowed_columns_that_miss_get_their_own_factorisation(monkeypatch):
 
 
 def test_factorisations_are_admitted_against_free_memory(monkeypatch):
-    """The memory gate for factorisations: cached ones are dropped when new ones would not fit, MemoryError
-    when they still do not."""
+    """The memory gate for factorisations: cached ones and the solve workspace are dropped when new ones would
+    not fit, MemoryError when they still do not."""
     from groundtruth_gb300 import native
     st = host_stack(synth.small_pair())
-    st.handle = object()
+    trims = []
+
+    class Handle:
+        def trim(self):
+            trims.append(1)
+    st.handle = Handle()
     one = st.factorisation_bytes(1)
     assert one > st.sym.panel_total * 48 and st.factorisation_bytes(4) == 4 * one
     free = [10 * one]
@@ -300,7 +305,7 @@ def test_factorisations_are_admitted_against_free_memory(monkeypatch):
     free[0] = 2 * one
     with pytest.raises(MemoryError):
         st._admit(4)
-    assert not st._ops                              # dropped before giving up
+    assert not st._ops and trims                    # dropped before giving up
 
 
 @pytest.mark.parametrize("name", ["small_pair", "capacitance_only", "faces_stack3", "six_sheet"])

@@ -52,7 +52,7 @@ def test_operators_with_fp32_panels_only_solve_the_same_and_refuse_fp64():
     got = _columns(st, routes, freqs)
     for a, c in zip(ref, got):
         assert np.array_equal(a[3], c[3])
-    with pytest.raises(RuntimeError, match="FP64 panels"):
+    with pytest.raises(ValueError, match="FP64 panels"):
         _columns(st, routes, freqs, precision="fp64")
 
 
