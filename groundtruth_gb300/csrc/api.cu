@@ -33,6 +33,19 @@ static thread_local std::string t_last_error;
 std::atomic<long long> g_launches{0};
 void set_error(const std::string& s) { t_last_error = s; }
 
+void raise_smem(const void* fn, size_t bytes) {
+    if (bytes <= 48 * 1024) return;
+    static std::mutex lock;
+    static std::map<std::pair<int, const void*>, size_t> cap;
+    int dev = 0;
+    GT_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(lock);
+    size_t& c = cap[{dev, fn}];
+    if (bytes <= c) return;
+    GT_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    c = bytes;
+}
+
 struct Invalid : std::runtime_error {
     using std::runtime_error::runtime_error;
 };

@@ -57,6 +57,11 @@ struct CudaError {
 // kernels launched by the library (gt_launch_count)
 extern std::atomic<long long> g_launches;
 
+// Let `fn` take `bytes` of dynamic shared memory on the current device.  The cap only ever rises: host
+// threads that launch the same kernel with different sizes on their own streams must not lower it between
+// another thread's raise and its launch.
+void raise_smem(const void* fn, size_t bytes);
+
 #define GT_LAUNCH_CHECK()               \
     do {                                \
         ::gt::g_launches.fetch_add(1);  \

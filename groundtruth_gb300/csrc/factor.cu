@@ -226,9 +226,7 @@ constexpr int LB = 8;
 constexpr int SOLVE_THREADS = 512;
 
 template <typename R>
-static void smem_attr(const void* fn, size_t bytes) {
-    if (bytes > 48 * 1024) GT_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-}
+static void smem_attr(const void* fn, size_t bytes) { raise_smem(fn, bytes); }
 
 // two consecutive columns' entries of a k-major shared vector (one 16-byte load in FP32)
 __device__ __forceinline__ void lds2(const c32* p, c32& a, c32& b) {

@@ -647,9 +647,7 @@ __global__ void __launch_bounds__(1024) lp_pass_c(const cx<R>* __restrict__ T, c
 template <typename R> static int ldt_of(const LpArgs<R>& a) { return a.ldt > 0 ? a.ldt : a.n0; }
 template <typename R> static bool b8_fits(const LpArgs<R>& a);
 template <typename R>
-static void set_smem(const void* fn, size_t bytes) {
-    if (bytes > 48 * 1024) GT_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-}
+static void set_smem(const void* fn, size_t bytes) { raise_smem(fn, bytes); }
 
 template <typename R>
 void lp_shapes(const LpArgs<R>& a, int* rows_out, int* bt_out) {

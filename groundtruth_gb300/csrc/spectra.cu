@@ -96,9 +96,7 @@ void kernel_spectrum(int na, int nl, double d, double dz, int P0, int P1, const 
     GT_LAUNCH_CHECK();
     // rows (length P1), then the columns c <= P1/2 (length P0), keeping rows <= P0/2 of their real parts
     size_t sm1 = (size_t)srow(P1) * sizeof(c64), sm0 = (size_t)srow(P0) * sizeof(c64);
-    if (std::max(sm0, sm1) > 48 * 1024)
-        GT_CUDA(cudaFuncSetAttribute((const void*)fft_lines_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)std::max(sm0, sm1)));
+    raise_smem((const void*)fft_lines_kernel, std::max(sm0, sm1));
     fft_lines_kernel<<<P0, P1 / 8, sm1, st>>>(Z, P1, P1, 1, P0, tw1, nullptr, 0);
     GT_LAUNCH_CHECK();
     fft_lines_kernel<<<Q1, P0 / 8, sm0, st>>>(Z, P0, 1, P1, Q1, tw0, T, Q0);
