@@ -213,6 +213,11 @@ struct gt_geometry {
     std::vector<double> level_panel;   // panel entries (sum of nf x nown) of each level
     int max_nf = 0;
     int64_t* d_order = nullptr;
+    // the factorisation's order: each level's small fronts, then its large ones (nf >= tiled_nf, the blocked
+    // multi-CTA elimination), with the large ones' counts and extents per level
+    int64_t* d_forder = nullptr;
+    std::vector<int> level_nbig, level_bigmaxnf, level_bigmaxnown, level_smallmaxnf;
+    int tiled_nf = 256;
     int64_t n_compact = 0, n_strips = 0;
     int64_t* d_c2d = nullptr;
     int64_t* d_sterm_ptr = nullptr;
@@ -1316,6 +1321,34 @@ int gt_geometry_create(const gt_geometry_desc* d, gt_geometry** out) {
         G->level_maxnown.push_back(mo);
         G->max_nf = std::max(G->max_nf, mx);
     }
+    {
+        if (const char* e = std::getenv("GT_TILED_NF")) G->tiled_nf = std::max(1, std::atoi(e));
+        std::vector<int64_t> ord;
+        ord.reserve(nf);
+        for (int h = 0; h < d->n_levels; ++h) {
+            std::vector<int64_t> small, big;
+            int bmx = 1, bmo = 1, smx = 1;
+            for (int64_t q = d->level_ptr[h]; q < d->level_ptr[h + 1]; ++q) {
+                const int64_t f = d->front_order[q];
+                const int nff = (int)(d->nown[f] + d->nbnd[f]);
+                if (nff >= G->tiled_nf) {
+                    big.push_back(f);
+                    bmx = std::max(bmx, nff);
+                    bmo = std::max<int>(bmo, (int)d->nown[f]);
+                } else {
+                    small.push_back(f);
+                    smx = std::max(smx, nff);
+                }
+            }
+            ord.insert(ord.end(), small.begin(), small.end());
+            ord.insert(ord.end(), big.begin(), big.end());
+            G->level_nbig.push_back((int)big.size());
+            G->level_bigmaxnf.push_back(bmx);
+            G->level_bigmaxnown.push_back(bmo);
+            G->level_smallmaxnf.push_back(smx);
+        }
+        G->d_forder = p.upload(ord.data(), ord.size());
+    }
     if (d->n_lowrank < 0 || d->n_lowrank > d->n_branches || d->n_lowrank > LOWRANK_MAX)
         throw Invalid("n_lowrank must be in 0 .. min(n_branches, 64)");
     G->n_lowrank = d->n_lowrank;
@@ -1460,11 +1493,19 @@ int gt_operators_create_ex(gt_geometry* G, int32_t n_ops, const double* omega, c
         Scope sc(P, "factor_assemble", st);
         launch_assemble_s(G->d_sterm_ptr, G->d_sterm_tab, G->d_sterm_coef, F.nsv, O->tab, g.ntab, svals, n_ops, st);
     }
+    // every front starts from zero: its own columns and its children's updates are added in
+    GT_CUDA(cudaMemsetAsync(O->panel64, 0, (size_t)n_ops * F.panel_total * sizeof(c64), st));
+    GT_CUDA(cudaMemsetAsync(upd, 0, (size_t)n_ops * std::max<int64_t>(F.upd_total, 1) * sizeof(c64), st));
     const int nlev = (int)G->level_ptr.size() - 1;
     for (int h = 0; h < nlev; ++h) {
-        int nfl = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);
+        const int nfl = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);
+        const int nbig = G->level_nbig[h], nsmall = nfl - nbig;
+        const int64_t* lst = G->d_forder + G->level_ptr[h];
         Scope sc(P, P->levels ? ("factor.L" + std::to_string(h)).c_str() : "factor_levels", st);
-        launch_factor_level(F, G->d_order + G->level_ptr[h], nfl, G->level_maxnf[h], svals, O->panel64, upd, n_ops, status, st);
+        if (nsmall) launch_factor_level(F, lst, nsmall, G->level_smallmaxnf[h], svals, O->panel64, upd, n_ops, status, st);
+        if (nbig)
+            launch_factor_tiled(F, lst + nsmall, nbig, G->level_bigmaxnf[h], G->level_bigmaxnown[h], svals, O->panel64,
+                                upd, n_ops, status, st);
     }
     int max_nown = 1;
     for (int h = 0; h < nlev; ++h) max_nown = std::max(max_nown, G->level_maxnown[h]);

@@ -47,23 +47,15 @@ struct FrontView {
     }
 };
 
-__global__ void factor_level_kernel(Fronts F, const int64_t* __restrict__ front_list, const c64* __restrict__ svals,
-                                    c64* __restrict__ panel, c64* __restrict__ upd, int* __restrict__ status) {
-    const int f = (int)front_list[blockIdx.x];
-    const int op = blockIdx.y;
-    const int nown = (int)F.nown[f], nbnd = (int)F.nbnd[f], nf = nown + nbnd;
-    FrontView Fv{panel + (int64_t)op * F.panel_total + F.panel_off[f], upd + (int64_t)op * F.upd_total + F.upd_off[f], nf,
-                 nown, nbnd};
+// A front's entries before elimination: the own columns of S and the children's update matrices, one child
+// at a time (their boundaries overlap).  The front starts zeroed (the panels and update matrices are cleared
+// by one memset before the first level).
+__device__ void assemble_front(const Fronts& F, int f, int op, const c64* __restrict__ svals, const FrontView& Fv,
+                               const c64* __restrict__ upd) {
     const int tid = threadIdx.x, nth = blockDim.x;
-    // zero the front
-    for (int64_t q = tid; q < (int64_t)nf * nown; q += nth) Fv.panel[q] = zero<double>();
-    for (int64_t q = tid; q < (int64_t)nbnd * nbnd; q += nth) Fv.upd[q] = zero<double>();
-    __syncthreads();
-    // own columns of S
     const c64* sv = svals + (int64_t)op * F.nsv;
     for (int64_t e = F.ent_ptr[f] + tid; e < F.ent_ptr[f + 1]; e += nth) Fv.at(F.ent_row[e], F.ent_col[e]) += sv[F.ent_s[e]];
     __syncthreads();
-    // children's update matrices, one child at a time (their boundaries overlap)
     for (int64_t ci = F.child_ptr[f]; ci < F.child_ptr[f + 1]; ++ci) {
         const int c = (int)F.child_idx[ci];
         const int nb = (int)F.nbnd[c];
@@ -75,16 +67,40 @@ __global__ void factor_level_kernel(Fronts F, const int64_t* __restrict__ front_
         }
         __syncthreads();
     }
-    // eliminate the own columns
+}
+
+__device__ __forceinline__ FrontView front_view(const Fronts& F, int f, int op, c64* panel, c64* upd) {
+    const int nown = (int)F.nown[f], nbnd = (int)F.nbnd[f];
+    return FrontView{panel + (int64_t)op * F.panel_total + F.panel_off[f], upd + (int64_t)op * F.upd_total + F.upd_off[f],
+                     nown + nbnd, nown, nbnd};
+}
+
+__device__ __forceinline__ c64 pivot_inverse(c64 d, int* status) {
+    const double dd = d.re * d.re + d.im * d.im;
+    if (!(dd > 1e-300) || !isfinite(dd)) {
+        atomicOr(status, 1);
+        d = mk<double>(1e-150, 0.0);
+    }
+    return cdiv(mk<double>(1.0, 0.0), d);
+}
+
+// Small fronts: one CTA per (front, operator) assembles the front and eliminates its own columns by rank-1
+// updates in place.
+__global__ void factor_level_kernel(Fronts F, const int64_t* __restrict__ front_list, const c64* __restrict__ svals,
+                                    c64* __restrict__ panel, c64* __restrict__ upd, int* __restrict__ status) {
+    const int f = (int)front_list[blockIdx.x];
+    const int op = blockIdx.y;
+    const FrontView Fv = front_view(F, f, op, panel, upd);
+    const int nf = Fv.nf, nown = Fv.nown;
+    assemble_front(F, f, op, svals, Fv, upd);
+    const int tid = threadIdx.x, nth = blockDim.x;
     const int warp = tid >> 5, lane = tid & 31, nwarp = nth >> 5;
     for (int k = 0; k < nown; ++k) {
-        c64 d = Fv.panel[(int64_t)k * nf + k];
-        double dd = d.re * d.re + d.im * d.im;
-        if (!(dd > 1e-300) || !isfinite(dd)) {
-            if (tid == 0) atomicOr(status, 1);
-            d = mk<double>(1e-150, 0.0);
-        }
-        const c64 dinv = cdiv(mk<double>(1.0, 0.0), d);
+        const c64 d = Fv.panel[(int64_t)k * nf + k];
+        const double dd = d.re * d.re + d.im * d.im;
+        if ((!(dd > 1e-300) || !isfinite(dd)) && tid == 0) atomicOr(status, 1);
+        const c64 dinv = (!(dd > 1e-300) || !isfinite(dd)) ? cdiv(mk<double>(1.0, 0.0), mk<double>(1e-150, 0.0))
+                                                            : cdiv(mk<double>(1.0, 0.0), d);
         const c64* colk = Fv.panel + (int64_t)k * nf;
         for (int j = k + 1 + warp; j < nf; j += nwarp) {
             const c64 ljd = colk[j] * dinv;
@@ -101,6 +117,163 @@ void launch_factor_level(const Fronts& F, const int64_t* front_list, int nf_leve
     int threads = max_nf >= 256 ? 512 : 256;
     factor_level_kernel<<<dim3(nf_level, nops), threads, 0, st>>>(F, front_list, svals, panel, upd, status);
     GT_LAUNCH_CHECK();
+}
+
+// Large fronts: blocked elimination, FB own columns per step, every step over many CTAs (the top of the tree
+// has a few fronts per operator, and an SM's FP64 rate is 1/152 of the GPU's):
+//   diag   one warp per (front, operator) factors the FB x FB diagonal block in shared memory (lane = row)
+//   rows   L21 = A21 L11^-T D^-1 for the rows below it, one thread per row, 128 rows per CTA
+//   trail  A22 -= L21 D L21^T over 64 x 64 tiles of the trailing lower triangle, one tile per CTA
+// The arithmetic is the rank-1 kernel's, the updates of a block summed before they are subtracted.
+constexpr int FB = 32, FT = 64, ROWS_CTA = 128;
+
+__global__ void assemble_fronts_kernel(Fronts F, const int64_t* __restrict__ front_list, const c64* __restrict__ svals,
+                                       c64* __restrict__ panel, c64* __restrict__ upd) {
+    const int f = (int)front_list[blockIdx.x];
+    const int op = blockIdx.y;
+    assemble_front(F, f, op, svals, front_view(F, f, op, panel, upd), upd);
+}
+
+__global__ void __launch_bounds__(32) tiled_diag_kernel(Fronts F, const int64_t* __restrict__ front_list, int kb,
+                                                        c64* __restrict__ panel, c64* __restrict__ upd,
+                                                        int* __restrict__ status) {
+    __shared__ c64 a[FB][FB + 1];
+    const int f = (int)front_list[blockIdx.x];
+    const FrontView Fv = front_view(F, f, blockIdx.y, panel, upd);
+    const int nb = min(FB, Fv.nown - kb);
+    if (nb <= 0) return;
+    const int i = threadIdx.x;
+    for (int j = 0; j < nb; ++j)
+        a[i][j] = (i < nb && j <= i) ? Fv.panel[(int64_t)(kb + j) * Fv.nf + kb + i] : zero<double>();
+    __syncwarp();
+    for (int k = 0; k < nb; ++k) {
+        const c64 dinv = pivot_inverse(a[k][k], status);
+        const c64 lik = a[i][k];
+        for (int j = k + 1; j <= i && i < nb; ++j) a[i][j] -= lik * (a[j][k] * dinv);
+        __syncwarp();
+        if (i > k && i < nb) a[i][k] = lik * dinv;
+        __syncwarp();
+    }
+    if (i < nb)
+        for (int j = 0; j <= i; ++j) Fv.panel[(int64_t)(kb + j) * Fv.nf + kb + i] = a[i][j];
+}
+
+__global__ void __launch_bounds__(ROWS_CTA) tiled_rows_kernel(Fronts F, const int64_t* __restrict__ front_list, int kb,
+                                                              c64* __restrict__ panel, c64* __restrict__ upd) {
+    __shared__ c64 l11[FB][FB];
+    __shared__ c64 dv[FB];
+    const int f = (int)front_list[blockIdx.y];
+    const FrontView Fv = front_view(F, f, blockIdx.z, panel, upd);
+    const int nb = min(FB, Fv.nown - kb);
+    if (nb <= 0) return;
+    const int i = kb + nb + blockIdx.x * ROWS_CTA + threadIdx.x;
+    if (kb + nb + blockIdx.x * ROWS_CTA >= Fv.nf) return;             // the whole CTA is past the front
+    for (int q = threadIdx.x; q < FB * FB; q += ROWS_CTA) {
+        const int r = q / FB, c = q - r * FB;
+        l11[r][c] = (r < nb && c < r) ? Fv.panel[(int64_t)(kb + c) * Fv.nf + kb + r] : zero<double>();
+        if (r == c) dv[r] = r < nb ? Fv.panel[(int64_t)(kb + r) * Fv.nf + kb + r] : mk<double>(1.0, 0.0);
+    }
+    __syncthreads();
+    if (i >= Fv.nf) return;
+    c64 w[FB];                                                          // w = l D: the row's updates to come
+#pragma unroll
+    for (int k = 0; k < FB; ++k) {
+        if (k < nb) {
+            c64 t = Fv.panel[(int64_t)(kb + k) * Fv.nf + i];
+#pragma unroll
+            for (int m = 0; m < k; ++m) t -= w[m] * l11[k][m];
+            w[k] = t;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < FB; ++k)
+        if (k < nb) Fv.panel[(int64_t)(kb + k) * Fv.nf + i] = cdiv(w[k], dv[k]);
+}
+
+// tile t of the lower triangle of a T x T tile grid: (bi, bj), bj <= bi
+__device__ __forceinline__ void lower_tile(int t, int& bi, int& bj) {
+    int b = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
+    while ((int64_t)b * (b + 1) / 2 > t) --b;
+    while ((int64_t)(b + 1) * (b + 2) / 2 <= t) ++b;
+    bi = b;
+    bj = t - b * (b + 1) / 2;
+}
+
+constexpr size_t TRAIL_SMEM = 2 * (size_t)FB * FT * sizeof(c64);
+
+__global__ void __launch_bounds__(256) tiled_trail_kernel(Fronts F, const int64_t* __restrict__ front_list, int kb,
+                                                          c64* __restrict__ panel, c64* __restrict__ upd) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    c64* As = reinterpret_cast<c64*>(smem_raw);          // [m][FT]: L(i0 + r, kb + m)
+    c64* Bs = As + FB * FT;                              // [m][FT]: L(j0 + c, kb + m) d_m
+    const int f = (int)front_list[blockIdx.y];
+    const FrontView Fv = front_view(F, f, blockIdx.z, panel, upd);
+    const int nb = min(FB, Fv.nown - kb);
+    if (nb <= 0) return;
+    const int t0 = kb + nb, n2 = Fv.nf - t0;
+    const int T = (n2 + FT - 1) / FT;
+    if ((int64_t)blockIdx.x >= (int64_t)T * (T + 1) / 2) return;
+    int bi, bj;
+    lower_tile(blockIdx.x, bi, bj);
+    const int i0 = t0 + bi * FT, j0 = t0 + bj * FT;
+    for (int q = threadIdx.x; q < FB * FT; q += 256) {
+        const int m = q / FT, r = q - m * FT;
+        c64 a = zero<double>(), b = zero<double>();
+        if (m < nb) {
+            const c64* col = Fv.panel + (int64_t)(kb + m) * Fv.nf;
+            if (i0 + r < Fv.nf) a = col[i0 + r];
+            if (j0 + r < Fv.nf) b = col[j0 + r] * col[kb + m];
+        }
+        As[q] = a;
+        Bs[q] = b;
+    }
+    __syncthreads();
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    c64 acc[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[r][c] = zero<double>();
+    for (int m = 0; m < nb; ++m) {
+        c64 a[4], b[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) a[r] = As[m * FT + tx + 16 * r];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) b[c] = Bs[m * FT + ty + 16 * c];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) acc[r][c] += a[r] * b[c];
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const int j = j0 + ty + 16 * c;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int i = i0 + tx + 16 * r;
+            if (i < Fv.nf && j <= i) Fv.at(i, j) -= acc[r][c];
+        }
+    }
+}
+
+void launch_factor_tiled(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, int max_nown,
+                         const c64* svals, c64* panel, c64* upd, int nops, int* status, cudaStream_t st) {
+    assemble_fronts_kernel<<<dim3(nf_level, nops), 512, 0, st>>>(F, front_list, svals, panel, upd);
+    GT_LAUNCH_CHECK();
+    raise_smem((const void*)tiled_trail_kernel, TRAIL_SMEM);
+    for (int kb = 0; kb < max_nown; kb += FB) {
+        tiled_diag_kernel<<<dim3(nf_level, nops), 32, 0, st>>>(F, front_list, kb, panel, upd, status);
+        GT_LAUNCH_CHECK();
+        const int below = max_nf - kb - 1;              // rows below the block (at least this front's nb of them)
+        if (below <= 0) continue;
+        tiled_rows_kernel<<<dim3(ceil_div(below, ROWS_CTA), nf_level, nops), ROWS_CTA, 0, st>>>(F, front_list, kb, panel,
+                                                                                                 upd);
+        GT_LAUNCH_CHECK();
+        const int T = ceil_div(below, FT);
+        tiled_trail_kernel<<<dim3((unsigned)((int64_t)T * (T + 1) / 2), nf_level, nops), 256, TRAIL_SMEM, st>>>(
+            F, front_list, kb, panel, upd);
+        GT_LAUNCH_CHECK();
+    }
 }
 
 // Selective inversion: the inverse X of each front's own block (unit lower triangular; D on the diagonal

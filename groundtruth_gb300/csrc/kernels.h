@@ -148,6 +148,9 @@ void launch_assemble_s(const int64_t* ptr, const int* tab_idx, const double* coe
 // one elimination level: fronts front_list[0..nf) for each operator
 void launch_factor_level(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, const c64* svals,
                          c64* panel, c64* upd, int nops, int* status, cudaStream_t st);
+// one level's large fronts (blocked elimination over many CTAs); the fronts start zeroed
+void launch_factor_tiled(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, int max_nown,
+                         const c64* svals, c64* panel, c64* upd, int nops, int* status, cudaStream_t st);
 // each front's own block replaced by its inverse (in place, FP64; the unit diagonal and the pivots untouched)
 void launch_invert_own(const Fronts& F, c64* panel, int max_nown, int nops, cudaStream_t st);
 // each front's boundary rows replaced by -L_bnd Linv_own (in place, FP64; after launch_invert_own)

@@ -79,6 +79,8 @@ class Server:
             per += max(native.memory(w.stack.handle, 2, restart)["need"] - o, 1)
         fit = int((budget_bytes - one) // per) + 1
         self.max_cols = max(1, min(fit, max_cols or fit))
+        for w in self.geo.values():          # every device solve of a geometry in batches of at most that
+            w.max_cols = self.max_cols
         self.resident_bytes = sum(w.stack.resident_bytes(len(w.freqs)) for w in self.geo.values())
         self.batches = []
         self._stop = threading.Event()
@@ -99,9 +101,24 @@ class Server:
 
     # ------------------------------------------------------------------ batcher
     def _columns(self, req: Request) -> int:
-        if req.geometry != "base":
+        """Device columns of a request: its nets at its frequencies on another geometry or on a derived stack
+        (an edit that joins separate copper), else its border columns."""
+        if req.geometry != "base" or self._joins(self.geo["base"], req):
             return len(req.nets) * len(req.freqs)
         return (len(req.branches) + len(req.remove)) * len(req.freqs)
+
+    @staticmethod
+    def _joins(wi: WhatIf, req: Request) -> bool:
+        """True when the edit needs the derived stack: a new branch off the base's nodes or between separate
+        pieces of copper."""
+        st = wi.stack
+        if not req.branches and not req.remove:
+            return True
+        for b in req.branches:
+            ia, ib = st.node_id(b.a), st.node_id(b.b)
+            if ia < 0 or ib < 0 or tuple(b.a) == tuple(b.b) or st.full_label[ia] != st.full_label[ib]:
+                return True
+        return False
 
     def _loop(self):
         carry = []
@@ -165,6 +182,8 @@ class Server:
                         if Js else []
                     for fut, plan, c0 in plans:
                         results[id(fut)] = plan.compose(raw[c0: c0 + len(plan.Js)])
+                    if direct:
+                        st.trim()              # the derived stacks' workspaces take the base's place
                     for req, fut in direct:    # an edit that joins separate copper: the derived stack
                         results[id(fut)] = wi.evaluate(req.branches, req.nets, req.freqs, remove=req.remove)
                 else:

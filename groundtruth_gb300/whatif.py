@@ -287,6 +287,8 @@ class WhatIf:
         t2 = time.perf_counter()
         budget = {c: self.warm_budget * self.base[c].iterations + self.kw.get("restart", 50) for c in cols}
         sols, redo, _ = self._solve(dst, droutes, cols, guesses, budget)
+        dst.release_operators()           # its device memory now, not when the collector finds the stack
+        dst.trim()
         t3 = time.perf_counter()
         return EditResult({c: _column(sol) for c, sol in zip(cols, sols)}, t3 - t0, [s.iterations for s in sols],
                           {"derive_stack_s": t1 - t0, "operators_s": t2 - t1, "solve_s": t3 - t2,
