@@ -63,7 +63,10 @@ def parse():
     ap.add_argument("--boards", type=int, default=64, help="uneven: boards in the batch")
     ap.add_argument("--concurrency", type=int, default=8, help="uneven: boards in flight at once")
     ap.add_argument("--budget-gb", type=float, default=120.0, help="serve: device-memory budget (GB)")
-    ap.add_argument("--workload", default="slotted_pair", choices=["slotted_pair", "what_if", "uneven", "serve"],
+    ap.add_argument("--side", type=int, default=1024, help="largest: raster side (nodes per axis)")
+    ap.add_argument("--largest-nets", type=int, default=16, help="largest: nets solved (of 32)")
+    ap.add_argument("--largest-freqs", type=int, default=1, help="largest: frequencies solved (of 64)")
+    ap.add_argument("--workload", default="slotted_pair", choices=["slotted_pair", "what_if", "uneven", "serve", "largest"],
                     help="what_if: latency of interactive edits (added vias / decoupling parts) on a solved "
                          "512 x 512 board, warm-started derived stacks (a line of its own, not the headline)")
     ap.add_argument("--requests", type=int, default=24, help="what_if: timed edits")
@@ -626,6 +629,68 @@ def run_uneven(args):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------------------------------ largest instance
+def run_largest(args):
+    """The largest single instance: six plane layers of --side x --side nodes at 0.1 mm (synth.largest_board:
+    1024 x 1024 is ~12.4 M strips; 32 nets x 64 frequencies), of which the first --largest-nets nets at
+    --largest-freqs frequencies spread over the band are solved.  Host setup (topology, symbolic analysis,
+    spectra, right-hand sides) is reported, not timed; the timed step factorises the frequencies (FP32 panels
+    kept, one frequency at a time when that is all the memory holds) and solves every column
+    (batch.solve_board).  Reported per kernel family: device time, algorithmic GB/s and its fraction of the
+    measured HBM bandwidth; per column: the FP64 backward error ||b - Kx|| / ||b|| (the oracle cannot run at this
+    size)."""
+    import torch
+    from groundtruth_gb300 import batch, native, synth
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    t0 = time.perf_counter()
+    board = synth.largest_board(args.side)
+    nq = len(board.freqs)
+    qs = sorted(set(int(round(v)) for v in np.linspace(0, nq - 1, max(1, args.largest_freqs)))) \
+        if args.largest_freqs > 1 else [nq // 2]
+    board.freqs = np.asarray(board.freqs)[qs]
+    board.nets = board.nets[: args.largest_nets]
+    job = batch.prepare([board])[0]
+    st = job.stack
+    setup_s = time.perf_counter() - t0
+    lib = native.load()
+    torch.cuda.synchronize()
+    st.handle.profile(True)
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", 0)))
+    clocks.start()
+    l0 = lib.gt_launch_count()
+    t0 = time.perf_counter()
+    res = batch.solve_board(job)
+    torch.cuda.synchronize()
+    t_step = time.perf_counter() - t0
+    launches = int(lib.gt_launch_count() - l0)
+    ck = clocks.stop()
+    prof = st.handle.profile()
+    st.handle.profile(False)
+    peak, peak_kind = peaks()
+    fam = {k: {"ms": round(v[0], 1), "GBps": round(v[1] / (v[0] * 1e-3) / 1e9, 1) if v[1] > 0 else None,
+               "frac": round(v[1] / (v[0] * 1e-3) / 1e9 / peak, 3) if v[1] > 0 else None, "regions": v[2]}
+           for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
+    sym = st.sym
+    ncol = len(job.cols)
+    line = {"metric": "largest instance solves/s", "value": ncol / t_step, "unit": "solves/s", "n_gpus": 1,
+            "steps": 1, "warmup": 0, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64 inner / c128 refinement", "data": "synthetic (seeded)",
+            "config": {"workload": f"largest: 6 layers x {args.side}^2 at 0.1 mm, slots + cut-outs + vias; "
+                                   f"{len(board.nets)} nets x {len(board.freqs)} f of 32 x 64, factorisation + "
+                                   "solve per step", "tol": board.tol, "freqs_hz": [float(f) for f in board.freqs],
+                       "strips": int(st.ns), "unknowns": int(st.handle.n_compact), "schur_unknowns": int(sym.n),
+                       "panel_entries": int(sym.panel_total), "update_entries": int(sym.upd_total),
+                       "largest_front": int(max(sym.nown + sym.nbnd))},
+            "seconds": {"setup_untimed": round(setup_s, 1), "factorise": round(res.factorise_s, 1),
+                        "step": round(t_step, 1)},
+            "backward_error": {"max": float(res.residual.max()), "per_column": [float(r) for r in res.residual]},
+            "iterations": {"mean": float(np.mean(res.its)), "max": int(np.max(res.its))},
+            "Z_loop": [[float(z.real), float(z.imag)] for z in res.Z],
+            "kernel_families": fam, "peak_GBps": peak, "peak_kind": peak_kind, "gpu_launches": launches,
+            "clocks": ck}
+    print(json.dumps(line), flush=True)
+
+
 # ------------------------------------------------------------------------------------------ serving
 def _serve_requests(board, n_base_branches: int, n: int, seed: int):
     """n what-if requests of the serving workload: a third add 1-4 stitching vias, a third move one decoupling
@@ -751,6 +816,12 @@ def main():
             print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the headline workload only"}))
             return
         run_uneven(args)
+        return
+    if args.workload == "largest":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the headline workload only"}))
+            return
+        run_largest(args)
         return
     if args.workload == "what_if":
         if args.impl == "reference":

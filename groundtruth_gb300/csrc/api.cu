@@ -558,8 +558,8 @@ static void precond(gt_geometry* G, gt_operators* ops, const cx<R>* r, int64_t l
 // The triangular sweeps stage, per block, a front's rows for every column of a group in shared memory: the own
 // and boundary rows of the forward assembly (max_nown + max_nf), the own rows plus up to 17 x 32 rows of tiles
 // and partial sums of the forward products (max_nown + 544), the front's rows plus up to 16 x 32 partial sums of
-// the backward products (max_nf + 512).  The widest group of 8, 4 or 2 columns whose staging fits a block's
-// 227 KB is taken (narrower groups read the panel once per fewer columns); 0 when not even 2 fit.
+// the backward products (max_nf + 512).  The widest group of 8, 4, 2 or 1 columns whose staging fits a block's
+// 227 KB is taken (narrower groups read the panel once per fewer columns); 0 when not even one column fits.
 static int group_width(const gt_geometry* G, size_t elem) {
     size_t nown = 1;
     for (int v : G->level_maxnown) nown = std::max(nown, (size_t)v);
@@ -567,7 +567,7 @@ static int group_width(const gt_geometry* G, size_t elem) {
     const size_t rows = std::max({nown + nf, nown + 544, nf + 512});
     const char* cap_env = std::getenv("GT_GROUP_WIDTH");       // a lower cap, for tests of the narrow groups
     const int cap = cap_env ? std::atoi(cap_env) : 8;
-    for (int gc : {8, 4, 2})
+    for (int gc : {8, 4, 2, 1})
         if (gc <= cap && (size_t)gc * rows * elem <= 227 * 1024) return gc;
     return 0;
 }
@@ -1271,6 +1271,12 @@ int gt_geometry_create(const gt_geometry_desc* d, gt_geometry** out) {
     }
     // fronts
     const int nf = d->n_fronts;
+    for (int f = 0; f < nf; ++f) {           // every front's panel and update matrix inside their storage
+        const int64_t no = d->nown[f], nb = d->nbnd[f];
+        if (no < 0 || nb < 0 || d->panel_off[f] < 0 || d->upd_off[f] < 0 ||
+            d->panel_off[f] + (no + nb) * no > d->panel_total || d->upd_off[f] + nb * nb > d->upd_total)
+            throw Invalid("a front's panel or update matrix lies outside panel_total / upd_total");
+    }
     Fronts& F = G->F;
     F.nfront = nf;
     F.own_start = p.upload(d->own_start, nf);
@@ -1493,9 +1499,9 @@ int gt_operators_create_ex(gt_geometry* G, int32_t n_ops, const double* omega, c
         Scope sc(P, "factor_assemble", st);
         launch_assemble_s(G->d_sterm_ptr, G->d_sterm_tab, G->d_sterm_coef, F.nsv, O->tab, g.ntab, svals, n_ops, st);
     }
-    // every front starts from zero: its own columns and its children's updates are added in
+    // every front's panel starts from zero: its own columns and its children's updates are added in (the update
+    // matrices' slots are reused across levels; each front clears its own)
     GT_CUDA(cudaMemsetAsync(O->panel64, 0, (size_t)n_ops * F.panel_total * sizeof(c64), st));
-    GT_CUDA(cudaMemsetAsync(upd, 0, (size_t)n_ops * std::max<int64_t>(F.upd_total, 1) * sizeof(c64), st));
     const int nlev = (int)G->level_ptr.size() - 1;
     for (int h = 0; h < nlev; ++h) {
         const int nfl = (int)(G->level_ptr[h + 1] - G->level_ptr[h]);

@@ -48,11 +48,14 @@ struct FrontView {
 };
 
 // A front's entries before elimination: the own columns of S and the children's update matrices, one child
-// at a time (their boundaries overlap).  The front starts zeroed (the panels and update matrices are cleared
-// by one memset before the first level).
+// at a time (their boundaries overlap).  The panels start zeroed (one memset before the first level); the
+// update matrix's slot is shared with matrices of other levels (its last owner's was assembled into its
+// parent at an earlier level) and is cleared here.
 __device__ void assemble_front(const Fronts& F, int f, int op, const c64* __restrict__ svals, const FrontView& Fv,
                                const c64* __restrict__ upd) {
     const int tid = threadIdx.x, nth = blockDim.x;
+    for (int64_t q = tid; q < (int64_t)Fv.nbnd * Fv.nbnd; q += nth) Fv.upd[q] = zero<double>();
+    __syncthreads();
     const c64* sv = svals + (int64_t)op * F.nsv;
     for (int64_t e = F.ent_ptr[f] + tid; e < F.ent_ptr[f + 1]; e += nth) Fv.at(F.ent_row[e], F.ent_col[e]) += sv[F.ent_s[e]];
     __syncthreads();
@@ -436,6 +439,7 @@ __device__ __forceinline__ void mac_row(cx<R>* acc, cx<R> a, const cx<R>* x) {
         cfma(acc[2 * c2], a, u);
         cfma(acc[2 * c2 + 1], a, v);
     }
+    if constexpr (GC % 2 == 1) cfma(acc[GC - 1], a, x[GC - 1]);
 }
 
 // acc[c] += sum_{t < cnt} A[t * lda] x[t * xs + c]: A a strided run of panel elements (part of one row or
@@ -797,7 +801,8 @@ void launch_fwd_level(const Fronts& F, const int64_t* front_list, int nf_level, 
         case 8: fwd_level_gc<R, 8>(F, front_list, nf_level, max_nf, max_nown, panel, dinv, sf, z, uvec, wasm, G, st); return;
         case 4: fwd_level_gc<R, 4>(F, front_list, nf_level, max_nf, max_nown, panel, dinv, sf, z, uvec, wasm, G, st); return;
         case 2: fwd_level_gc<R, 2>(F, front_list, nf_level, max_nf, max_nown, panel, dinv, sf, z, uvec, wasm, G, st); return;
-        default: throw CudaError{cudaErrorInvalidValue, "column group width must be 8, 4 or 2"};
+        case 1: fwd_level_gc<R, 1>(F, front_list, nf_level, max_nf, max_nown, panel, dinv, sf, z, uvec, wasm, G, st); return;
+        default: throw CudaError{cudaErrorInvalidValue, "column group width must be 8, 4, 2 or 1"};
     }
 }
 
@@ -809,7 +814,8 @@ void launch_bwd_level(const Fronts& F, const int64_t* front_list, int nf_level, 
         case 8: bwd_level_gc<R, 8>(F, front_list, nf_level, max_nf, max_nown, panel_rm, z, y, sd, G, st); return;
         case 4: bwd_level_gc<R, 4>(F, front_list, nf_level, max_nf, max_nown, panel_rm, z, y, sd, G, st); return;
         case 2: bwd_level_gc<R, 2>(F, front_list, nf_level, max_nf, max_nown, panel_rm, z, y, sd, G, st); return;
-        default: throw CudaError{cudaErrorInvalidValue, "column group width must be 8, 4 or 2"};
+        case 1: bwd_level_gc<R, 1>(F, front_list, nf_level, max_nf, max_nown, panel_rm, z, y, sd, G, st); return;
+        default: throw CudaError{cudaErrorInvalidValue, "column group width must be 8, 4, 2 or 1"};
     }
 }
 

@@ -66,15 +66,20 @@ __global__ void __launch_bounds__(1024) lp_pass_b(int S, int n0, int P0, int P1,
     const int b0 = blockIdx.y * bt;
     const int nb = min(bt, ncol - b0);
     const int nrows = nb * S;
-    // each team loads, transforms and stores its own row (column b, sheet s)
-    const int team = P / 8;
-    const int row = threadIdx.x / team, t = threadIdx.x - row * team;
-    const int rb = row / S, rs = row - rb * S;
-    cx<R>* Trow = T + (((int64_t)(b0 + rb) * S + rs) * P1 + c) * ldt;
-    if (row < nrows)
-        for (int p = t; p < P; p += team) buf[row * stride + spad(p)] = p < n0 ? Trow[p] : zero<R>();
-    __syncthreads();
-    fft_row_t<R, false, PL, true, false>(buf + row * stride, row < nrows, P, tw, team, t);
+    // each team loads, transforms and stores its own rows (column b, sheet s): rows r0 + slot for r0 = 0,
+    // nslot, ... (more rows than a block's threads hold teams for: six sheets at P = 2048)
+    const int team = P / 8, nslot = blockDim.x / team;
+    const int slot = threadIdx.x / team, t = threadIdx.x - slot * team;
+    for (int r0 = 0; r0 < nrows; r0 += nslot) {
+        const int row = r0 + slot;
+        if (row < nrows) {
+            const int rb = row / S, rs = row - rb * S;
+            const cx<R>* Trow = T + (((int64_t)(b0 + rb) * S + rs) * P1 + c) * ldt;
+            for (int p = t; p < P; p += team) buf[row * stride + spad(p)] = p < n0 ? Trow[p] : zero<R>();
+        }
+        __syncthreads();
+        fft_row_t<R, false, PL, true, false>(buf + min(row, nrows - 1) * stride, row < nrows, P, tw, team, t);
+    }
     // spectrum multiply-add over sheets, one (column, pixel) per thread iteration
     const int Q0 = P / 2 + 1;
     const int q1 = min(c, P1 - c);
@@ -103,9 +108,15 @@ __global__ void __launch_bounds__(1024) lp_pass_b(int S, int n0, int P0, int P1,
         }
     }
     __syncthreads();
-    fft_row_t<R, true, PL, false, true>(buf + row * stride, row < nrows, P, tw, team, t);
-    if (row < nrows)
-        for (int p = t; p < n0; p += team) Trow[p] = buf[row * stride + spad(p)];
+    for (int r0 = 0; r0 < nrows; r0 += nslot) {
+        const int row = r0 + slot;
+        fft_row_t<R, true, PL, false, true>(buf + min(row, nrows - 1) * stride, row < nrows, P, tw, team, t);
+        if (row < nrows) {
+            const int rb = row / S, rs = row - rb * S;
+            cx<R>* Trow = T + (((int64_t)(b0 + rb) * S + rs) * P1 + c) * ldt;
+            for (int p = t; p < n0; p += team) Trow[p] = buf[row * stride + spad(p)];
+        }
+    }
 }
 
 // Pass B for P a power of 8 (all stages radix 8) with the spectrum multiply fused in registers.  A team of
@@ -743,9 +754,9 @@ static void launch_b(const LpArgs<R>& a, int bt, cudaStream_t st) {
     }
     size_t smB = (size_t)bt * a.S * srow(a.P0) * sizeof(cx<R>);
     dim3 gB(a.P1, ceil_div(a.ncol, bt));
+    const int team = a.P0 / 8, threads = std::min(bt * a.S, 1024 / team) * team;
     set_smem<R>((const void*)lp_pass_b<R, PB>, smB);
-    lp_pass_b<R, PB><<<gB, bt * a.S * (a.P0 / 8), smB, st>>>(a.S, a.n0, a.P0, a.P1, a.ncol, bt, a.spec, a.tw0, a.T,
-                                                              ldt_of(a));
+    lp_pass_b<R, PB><<<gB, threads, smB, st>>>(a.S, a.n0, a.P0, a.P1, a.ncol, bt, a.spec, a.tw0, a.T, ldt_of(a));
     GT_LAUNCH_CHECK();
 }
 

@@ -221,6 +221,65 @@ def dense_layout(t: Topology) -> Dense:
 
 
 # ------------------------------------------------------------------------------------------ symbolic
+def update_slots(height: np.ndarray, parent: np.ndarray, size: np.ndarray) -> tuple:
+    """Element offsets of the fronts' update matrices, storage shared between matrices that are never live at
+    the same time, and the storage's length.  The factorisation runs level by level (a front's level is its
+    height in the elimination tree): front f's matrix is written at its own level and read when its parent's
+    level assembles it, so it is live over levels height[f] .. height[parent[f]], both ends included (at a
+    level, fronts read their children's matrices while other fronts of the level write theirs).  Slots are
+    placed first fit over the free blocks, the largest matrices of a level first; a block comes free after the
+    last level of its matrix."""
+    import bisect
+    nfront = len(size)
+    end = np.where(parent >= 0, height[np.maximum(parent, 0)], height)
+    nlev = int(height.max()) + 1 if nfront else 0
+    starts = [[] for _ in range(nlev)]
+    ends = [[] for _ in range(nlev)]
+    for f in range(nfront):
+        if size[f] > 0:
+            starts[int(height[f])].append(f)
+            ends[int(end[f])].append(f)
+    off = np.zeros(nfront, np.int64)
+    free_off, free_len = [], []          # free blocks below the high-water mark, sorted by offset, merged
+    top = 0
+
+    def release(o, n):
+        i = bisect.bisect_left(free_off, o)
+        if i > 0 and free_off[i - 1] + free_len[i - 1] == o:          # joins the block before it
+            i -= 1
+            free_len[i] += n
+        else:
+            free_off.insert(i, o)
+            free_len.insert(i, n)
+        if i + 1 < len(free_off) and free_off[i] + free_len[i] == free_off[i + 1]:   # and the one after it
+            free_len[i] += free_len.pop(i + 1)
+            free_off.pop(i + 1)
+
+    for h in range(nlev):
+        for f in sorted(starts[h], key=lambda f: -int(size[f])):
+            n = int(size[f])
+            for i in range(len(free_off)):
+                if free_len[i] >= n:
+                    off[f] = free_off[i]
+                    if free_len[i] == n:
+                        free_off.pop(i)
+                        free_len.pop(i)
+                    else:
+                        free_off[i] += n
+                        free_len[i] -= n
+                    break
+            else:
+                if free_off and free_off[-1] + free_len[-1] == top:       # extend the last free block
+                    off[f] = free_off.pop()
+                    free_len.pop()
+                else:
+                    off[f] = top
+                top = int(off[f]) + n
+        for f in ends[h]:
+            release(int(off[f]), int(size[f]))
+    return off, top
+
+
 @dataclass
 class Symbolic:
     n: int                       # kept nodes (factor dimension)
@@ -412,7 +471,7 @@ def symbolic(t: Topology, S_pattern: sp.csr_matrix, leaf: int = 48) -> Symbolic:
     panel = nf * nown
     panel_off = np.concatenate([[0], np.cumsum(panel)[:-1]]).astype(np.int64)
     upd = nbnd * nbnd
-    upd_off = np.concatenate([[0], np.cumsum(upd)[:-1]]).astype(np.int64)
+    upd_off, upd_total = update_slots(height, parent, upd)
     vec_off = np.concatenate([[0], np.cumsum(nbnd)[:-1]]).astype(np.int64)
     # assembly entries: S lower entry (r, c) goes to the front owning column c
     ef = front_of_fac[s_col]
@@ -442,5 +501,5 @@ def symbolic(t: Topology, S_pattern: sp.csr_matrix, leaf: int = 48) -> Symbolic:
     ent_ptr = np.searchsorted(ef[eo], np.arange(nfront + 1)).astype(np.int64)
     return Symbolic(n, perm, iperm, own_start, nown, nbnd, bnd_ptr, bnd_idx, parent, height, order.astype(np.int64),
                     level_ptr.astype(np.int64), child_ptr, child_idx, cmap_ptr, cmap_idx, panel_off, upd_off, vec_off,
-                    int(panel.sum()), int(upd.sum()), int(nbnd.sum()), ent_ptr, erow[eo], ecol[eo], eo.astype(np.int64),
+                    int(panel.sum()), upd_total, int(nbnd.sum()), ent_ptr, erow[eo], ecol[eo], eo.astype(np.int64),
                     s_row, s_col)

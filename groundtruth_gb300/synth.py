@@ -379,15 +379,18 @@ def small_stack3(seed: int = 9) -> Board:
 
 
 def random_board(seed: int, side=(24, 48), n_layers=(2, 6), n_nets=(1, 2), n_freq: int = 2, slots: bool = False,
-                 cut_max: int = 8) -> Board:
+                 cut_max: int = 8, pitch_mm: Optional[float] = None) -> Board:
     """A seeded board drawn like the uneven-batch workload (sides, pitch, 2-6 plane layers with gaps
     U[0.1, 1.5] mm, 0-8 polygon cut-outs of 3-8 vertices per layer, stitching vias at a Poisson density of
     0-4 per cm2, random-walk nets, log-spaced frequencies in [1 MHz, 1 GHz]), with the raster sides drawn from
     `side` (small enough for the FP64 oracle); `slots`: also one straight slot per layer (the largest
-    instance's layers).  The nets' return nodes are on the top plane and connected there."""
+    instance's layers); `pitch_mm`: this pitch instead of the drawn one.  The nets' return nodes are on the top
+    plane and connected there."""
     rng = np.random.default_rng(seed)
     nx, ny = (int(rng.integers(side[0], side[1] + 1)) for _ in range(2))
     d = float(rng.uniform(0.2, 0.5)) * 1e-3
+    if pitch_mm is not None:
+        d = pitch_mm * 1e-3
     t = 35e-6
     nl = int(rng.integers(n_layers[0], n_layers[1] + 1))
     zs = [0.0]
@@ -447,6 +450,17 @@ def uneven_board(seed: int, tol: float = 1e-8) -> Board:
     from 1 MHz to 1 GHz; solved to `tol`."""
     b = random_board(10_000 + seed, side=(64, 512), n_layers=(2, 6), n_nets=(1, 16), n_freq=(4, 16))
     b.name, b.tol = f"uneven_{seed}", tol
+    return b
+
+
+def largest_board(n: int = 1024, pitch_mm: float = 0.1, n_nets: int = 32, n_freq: int = 64, seed: int = 5,
+                  tol: float = 1e-8) -> Board:
+    """The largest single instance: six plane layers of n x n nodes at pitch_mm (1024 x 1024 at 0.1 mm: a
+    10 cm board, ~12.6 M strips), cut-outs and a slot on every layer, stitching vias, n_nets random-walk nets
+    and n_freq log-spaced frequencies from 1 MHz to 1 GHz."""
+    b = random_board(seed, side=(n, n), n_layers=(6, 6), n_nets=(n_nets, n_nets), n_freq=(n_freq, n_freq),
+                     slots=True, cut_max=3, pitch_mm=pitch_mm)
+    b.name, b.tol = f"largest_{n}", tol
     return b
 
 

@@ -56,7 +56,7 @@ def test_operators_with_fp32_panels_only_solve_the_same_and_refuse_fp64():
         _columns(st, routes, freqs, precision="fp64")
 
 
-@pytest.mark.parametrize("width", ["4", "2"])
+@pytest.mark.parametrize("width", ["4", "2", "1"])
 def test_narrow_column_groups_give_the_same_solutions(width, monkeypatch):
     """Fronts too wide for 8 columns' staging take groups of 4 or 2 (the panel read once per fewer columns):
     the same board solved with the group width capped equals its solve with groups of 8."""

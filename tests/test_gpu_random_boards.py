@@ -36,3 +36,25 @@ def test_solves_match_oracle(case, precision):
             assert rel(sol.state_for(st)[: st.ns], Ib[: ost.ns]) < 1e-7
             assert abs(sol.Z_loop - ref["Z_loop"]) <= 1e-8 * abs(ref["Z_loop"]), (k, q, sol.Z_loop, ref["Z_loop"])
             assert sol.residual <= board.tol
+
+
+def test_six_sheet_column_pass_with_more_rows_than_threads():
+    """Six sheets on a 600-row raster: the column FFTs (P0 = 1536) need 6 x 192 threads per column, more than a
+    block holds, so the column pass transforms its rows in slots (the largest instance's 2048-point columns
+    do the same).  The FP64 and FP32 L_p products against the oracle's."""
+    from groundtruth_gb300 import native
+    nx, ny, d, t = 600, 12, 0.3e-3, 35e-6
+    layers = [synth._full_layer(f"L{k}", -k * 0.4e-3, t, nx, ny, d) for k in range(6)]
+    pts = [(20 * d, 6 * d), (580 * d, 6 * d)]
+    net = synth.Net(synth._segments(pts, 0.15e-3 + t, 0.5 * t, 0.15e-3), (0, 20, 6), (0, 580, 6))
+    board = synth.Board("thin_six", d, nx, ny, layers, nets=[net], freqs=np.array([1e7]))
+    ost = oracle_stack(board)
+    st, routes = gs.from_board(board)
+    obj, k = st.factorise([1e7])[0]
+    rng = np.random.default_rng(9)
+    I = rng.standard_normal(st.ns) + 1j * rng.standard_normal(st.ns)
+    ref = ost.Lp_matvec(I)
+    x = np.zeros(st.handle.n_compact, complex)
+    x[: st.ns] = I
+    assert rel(native.apply(st.handle, obj, "lp", x, k, "fp64")[0][: st.ns], ref) < 1e-12
+    assert rel(native.apply(st.handle, obj, "lp", x, k, "fp32")[0][: st.ns], ref) < 1e-5
