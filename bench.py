@@ -62,6 +62,7 @@ def parse():
                     help="also time each elimination level of the triangular solves (key 'solve_levels')")
     ap.add_argument("--boards", type=int, default=64, help="uneven: boards in the batch")
     ap.add_argument("--concurrency", type=int, default=8, help="uneven: boards in flight at once")
+    ap.add_argument("--no-alone", action="store_true", help="uneven: skip the one-board-at-a-time pass")
     ap.add_argument("--budget-gb", type=float, default=120.0, help="serve: device-memory budget (GB)")
     ap.add_argument("--side", type=int, default=1024, help="largest: raster side (nodes per axis)")
     ap.add_argument("--largest-nets", type=int, default=16, help="largest: nets solved (of 32)")
@@ -604,10 +605,13 @@ def run_uneven(args):
     t_mixed = time.perf_counter() - t0
     launches = int(lib.gt_launch_count() - l0)
     ck = clocks.stop()
-    t0 = time.perf_counter()
-    alone = batch.solve_all(jobs, concurrency=1)
-    t_alone = time.perf_counter() - t0
-    dev = max(float(np.linalg.norm(a.x - m.x) / max(np.linalg.norm(a.x), 1e-300)) for a, m in zip(alone, mixed))
+    alone, t_alone = None, None
+    if not args.no_alone:
+        t0 = time.perf_counter()
+        alone = batch.solve_all(jobs, concurrency=1)
+        t_alone = time.perf_counter() - t0
+    dev = max(float(np.linalg.norm(a.x - m.x) / max(np.linalg.norm(a.x), 1e-300)) for a, m in zip(alone, mixed)) \
+        if alone else None
     groups = {}
     for j in jobs:
         groups[str(j.group)] = groups.get(str(j.group), 0) + 1
@@ -619,7 +623,8 @@ def run_uneven(args):
                        "solves_per_step": nsolve, "tol": boards[0].tol, "concurrency": args.concurrency,
                        "warmup": f"the smallest board of each FFT group ({len(smallest)} boards)",
                        "fft_groups": groups},
-            "one_board_at_a_time": {"value": nsolve / t_alone, "unit": "solves/s", "seconds": round(t_alone, 2)},
+            "one_board_at_a_time": {"value": nsolve / t_alone, "unit": "solves/s", "seconds": round(t_alone, 2)}
+            if alone else None,
             "max_rel_diff_mix_vs_alone": dev,
             "max_rel_residual": float(max(m.residual.max() for m in mixed)),
             "iterations": {"mean": float(np.mean(np.concatenate([m.its for m in mixed]))),
