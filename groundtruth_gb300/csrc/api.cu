@@ -218,6 +218,9 @@ struct gt_geometry {
     int64_t* d_forder = nullptr;
     std::vector<int> level_nbig, level_bigmaxnf, level_bigmaxnown, level_smallmaxnf;
     int tiled_nf = 256;
+    // every large front (all levels), for the blocked selective inversion
+    int64_t* d_bigfronts = nullptr;
+    int nbig = 0, bigmax_nf = 1, bigmax_nown = 1;
     int64_t n_compact = 0, n_strips = 0;
     int64_t* d_c2d = nullptr;
     int64_t* d_sterm_ptr = nullptr;
@@ -1354,6 +1357,16 @@ int gt_geometry_create(const gt_geometry_desc* d, gt_geometry** out) {
             G->level_smallmaxnf.push_back(smx);
         }
         G->d_forder = p.upload(ord.data(), ord.size());
+        std::vector<int64_t> big;
+        for (int f = 0; f < nf; ++f) {
+            const int nff = (int)(d->nown[f] + d->nbnd[f]);
+            if (nff < G->tiled_nf) continue;
+            big.push_back(f);
+            G->bigmax_nf = std::max(G->bigmax_nf, nff);
+            G->bigmax_nown = std::max<int>(G->bigmax_nown, (int)d->nown[f]);
+        }
+        G->nbig = (int)big.size();
+        G->d_bigfronts = p.upload(big.data(), big.size());
     }
     if (d->n_lowrank < 0 || d->n_lowrank > d->n_branches || d->n_lowrank > LOWRANK_MAX)
         throw Invalid("n_lowrank must be in 0 .. min(n_branches, 64)");
@@ -1517,15 +1530,20 @@ int gt_operators_create_ex(gt_geometry* G, int32_t n_ops, const double* omega, c
     for (int h = 0; h < nlev; ++h) max_nown = std::max(max_nown, G->level_maxnown[h]);
     {
         Scope sc(P, "factor_invert", st);
-        launch_invert_own(F, O->panel64, max_nown, n_ops, st);
+        launch_invert_own(F, O->panel64, max_nown, n_ops, G->tiled_nf, st);
     }
     {
         Scope sc(P, "factor_bnd_inv", st);
-        launch_bnd_inv(F, O->panel64, G->max_nf, n_ops, st);
+        launch_bnd_inv(F, O->panel64, G->max_nf, n_ops, G->tiled_nf, st);
+    }
+    {
+        Scope sc(P, "factor_invert_tiled", st);
+        launch_invert_tiled(F, G->d_bigfronts, G->nbig, G->bigmax_nf, G->bigmax_nown, O->panel64, n_ops, st);
     }
     {
         Scope sc(P, "factor_convert", st);
-        launch_panel_convert(F, O->panel64, O->panel32, O->panel32_rm, O->panel64_rm, O->dinv64, O->dinv32, n_ops, st);
+        launch_panel_convert(F, O->panel64, O->panel32, O->panel32_rm, O->panel64_rm, O->dinv64, O->dinv32, n_ops,
+                             G->tiled_nf, st);
     }
     int h_status = 0;
     GT_CUDA(cudaMemcpy(&h_status, status, sizeof(int), cudaMemcpyDeviceToHost));

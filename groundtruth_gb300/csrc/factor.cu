@@ -285,10 +285,10 @@ void launch_factor_tiled(const Fronts& F, const int64_t* front_list, int nf_leve
 // lower triangle stays intact while other rows read it; panel_convert moves X into place.  One thread per
 // row, rows of large fronts over several blocks, no barriers.
 constexpr int INV_ROWS = 128;
-__global__ void __launch_bounds__(INV_ROWS) invert_own_kernel(Fronts F, c64* __restrict__ panel, int nchunk) {
+__global__ void __launch_bounds__(INV_ROWS) invert_own_kernel(Fronts F, c64* __restrict__ panel, int nchunk, int tiled_nf) {
     const int f = blockIdx.x / nchunk, chunk = blockIdx.x - f * nchunk, op = blockIdx.y;
     const int nown = (int)F.nown[f], nf = nown + (int)F.nbnd[f];
-    if (chunk * INV_ROWS >= nown) return;
+    if (chunk * INV_ROWS >= nown || nf >= tiled_nf) return;      // large fronts: the blocked inversion
     const int i = chunk * INV_ROWS + threadIdx.x;
     c64* L = panel + (int64_t)op * F.panel_total + F.panel_off[f];
     const int kmax = min(nown, chunk * INV_ROWS + INV_ROWS) - 2;   // the block's largest row - 1
@@ -302,9 +302,9 @@ __global__ void __launch_bounds__(INV_ROWS) invert_own_kernel(Fronts F, c64* __r
     }
 }
 
-void launch_invert_own(const Fronts& F, c64* panel, int max_nown, int nops, cudaStream_t st) {
+void launch_invert_own(const Fronts& F, c64* panel, int max_nown, int nops, int tiled_nf, cudaStream_t st) {
     const int nchunk = std::max(1, ceil_div(max_nown, INV_ROWS));
-    invert_own_kernel<<<dim3(F.nfront * nchunk, nops), INV_ROWS, 0, st>>>(F, panel, nchunk);
+    invert_own_kernel<<<dim3(F.nfront * nchunk, nops), INV_ROWS, 0, st>>>(F, panel, nchunk, tiled_nf);
     GT_LAUNCH_CHECK();
 }
 
@@ -313,11 +313,11 @@ void launch_invert_own(const Fronts& F, c64* panel, int max_nown, int nops, cuda
 // m > k of its own row, which are still the factor's.  One thread per row (rows of a warp consecutive, so
 // the row loads coalesce and the Linv loads broadcast); the rows of large fronts spread over many blocks.
 constexpr int BND_ROWS = 128;
-__global__ void __launch_bounds__(BND_ROWS) bnd_inv_kernel(Fronts F, c64* __restrict__ panel, int nchunk) {
+__global__ void __launch_bounds__(BND_ROWS) bnd_inv_kernel(Fronts F, c64* __restrict__ panel, int nchunk, int tiled_nf) {
     const int f = blockIdx.x / nchunk, chunk = blockIdx.x - f * nchunk, op = blockIdx.y;
     const int nown = (int)F.nown[f], nbnd = (int)F.nbnd[f], nf = nown + nbnd;
     const int j = nown + chunk * BND_ROWS + threadIdx.x;
-    if (chunk * BND_ROWS >= nbnd) return;
+    if (chunk * BND_ROWS >= nbnd || nf >= tiled_nf) return;
     c64* L = panel + (int64_t)op * F.panel_total + F.panel_off[f];
     const bool act = j < nf;
     const int jr = act ? j : nf - 1;
@@ -338,10 +338,172 @@ __global__ void __launch_bounds__(BND_ROWS) bnd_inv_kernel(Fronts F, c64* __rest
     }
 }
 
-void launch_bnd_inv(const Fronts& F, c64* panel, int max_nbnd, int nops, cudaStream_t st) {
+void launch_bnd_inv(const Fronts& F, c64* panel, int max_nbnd, int nops, int tiled_nf, cudaStream_t st) {
     const int nchunk = std::max(1, ceil_div(max_nbnd, BND_ROWS));
-    bnd_inv_kernel<<<dim3(F.nfront * nchunk, nops), BND_ROWS, 0, st>>>(F, panel, nchunk);
+    bnd_inv_kernel<<<dim3(F.nfront * nchunk, nops), BND_ROWS, 0, st>>>(F, panel, nchunk, tiled_nf);
     GT_LAUNCH_CHECK();
+}
+
+// Selective inversion of large fronts, blocked.  The inverted panel [Linv_own; -L_bnd Linv_own] is the first
+// nown columns of the inverse of the unit lower triangular T = [L_own 0; L_bnd I], so it is computed in place
+// as the forward substitution T Y = [I; 0], FB rows of T per step (kb = FB k, nb = the step's rows):
+//   inv_rows   Y[kb.., c] = L_kk^-1 Y[kb.., c] for columns c < kb (their right-hand sides accumulated so far)
+//   inv_diag   L_kk -> its inverse, in place, by one warp (a lane per row; D stays on the diagonal)
+//   inv_trail  Y[i, c] -= L[i, kb..] Y[kb.., c] for the rows i below the block: first the columns c < kb,
+//              then the block's own columns, whose Y takes the place of the L it is made from (each tile
+//              reads its rows of L before it writes; the c < kb pass has read them all by then).
+// The panel's upper triangle stays zero; the diagonal keeps D for panel_convert.
+__global__ void __launch_bounds__(ROWS_CTA) inv_rows_kernel(Fronts F, const int64_t* __restrict__ front_list, int kb,
+                                                            c64* __restrict__ panel) {
+    __shared__ c64 l11[FB][FB];
+    const int f = (int)front_list[blockIdx.y];
+    const int op = blockIdx.z;
+    const int nown = (int)F.nown[f], nf = nown + (int)F.nbnd[f];
+    const int nb = min(FB, nown - kb);
+    if (nb <= 0 || blockIdx.x * ROWS_CTA >= kb) return;
+    c64* P = panel + (int64_t)op * F.panel_total + F.panel_off[f];
+    for (int q = threadIdx.x; q < FB * FB; q += ROWS_CTA) {
+        const int r = q / FB, c = q - r * FB;
+        l11[r][c] = (r < nb && c < r) ? P[(int64_t)(kb + c) * nf + kb + r] : zero<double>();
+    }
+    __syncthreads();
+    const int c = blockIdx.x * ROWS_CTA + threadIdx.x;
+    if (c >= kb) return;
+    c64* col = P + (int64_t)c * nf + kb;
+    c64 y[FB];
+#pragma unroll
+    for (int r = 0; r < FB; ++r) {
+        if (r < nb) {
+            c64 t = col[r];
+#pragma unroll
+            for (int m = 0; m < r; ++m) t -= l11[r][m] * y[m];
+            y[r] = t;
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < FB; ++r)
+        if (r < nb) col[r] = y[r];
+}
+
+__global__ void __launch_bounds__(32) inv_diag_kernel(Fronts F, const int64_t* __restrict__ front_list, int kb,
+                                                      c64* __restrict__ panel) {
+    __shared__ c64 a[FB][FB + 1];
+    const int f = (int)front_list[blockIdx.x];
+    const int op = blockIdx.y;
+    const int nown = (int)F.nown[f], nf = nown + (int)F.nbnd[f];
+    const int nb = min(FB, nown - kb);
+    if (nb <= 0) return;
+    c64* P = panel + (int64_t)op * F.panel_total + F.panel_off[f];
+    const int i = threadIdx.x;
+    for (int j = 0; j < FB; ++j) a[i][j] = (i < nb && j < i) ? P[(int64_t)(kb + j) * nf + kb + i] : zero<double>();
+    __syncwarp();
+    if (i >= nb) return;
+    // X[i, k] = -(L[i, k] + sum_{k < m < i} X[i, m] L[m, k]), k descending: lane i needs only its own row of X
+    c64 x[FB];
+#pragma unroll
+    for (int k = FB - 1; k >= 0; --k) {
+        if (k < i) {
+            c64 acc = a[i][k];
+#pragma unroll
+            for (int m = k + 1; m < FB; ++m)
+                if (m < i) acc += x[m] * a[m][k];
+            x[k] = mk<double>(-acc.re, -acc.im);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < FB; ++k)
+        if (k < i) P[(int64_t)(kb + k) * nf + kb + i] = x[k];
+}
+
+// rows i >= kb + nb of the front; mode 0: columns c < kb (tile grid rt x ct), mode 1: the block's columns
+__global__ void __launch_bounds__(256) inv_trail_kernel(Fronts F, const int64_t* __restrict__ front_list, int kb,
+                                                        c64* __restrict__ panel, int mode) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    c64* As = reinterpret_cast<c64*>(smem_raw);          // [m][FT]: L(i0 + r, kb + m)
+    c64* Bs = As + FB * FT;                              // [m][FT]: Y(kb + m, c0 + c)
+    const int f = (int)front_list[blockIdx.y];
+    const int op = blockIdx.z;
+    const int nown = (int)F.nown[f], nf = nown + (int)F.nbnd[f];
+    const int nb = min(FB, nown - kb);
+    if (nb <= 0) return;
+    const int t0 = kb + nb, n2 = nf - t0;
+    if (n2 <= 0) return;
+    const int rt = (n2 + FT - 1) / FT;
+    const int ncols = mode == 0 ? kb : nb;
+    if (ncols <= 0) return;
+    const int ct = (ncols + FT - 1) / FT;
+    if ((int)blockIdx.x >= rt * ct) return;
+    const int bi = blockIdx.x % rt, bj = blockIdx.x / rt;
+    const int i0 = t0 + bi * FT, c0 = (mode == 0 ? 0 : kb) + bj * FT;
+    const int c1 = mode == 0 ? kb : kb + nb;             // columns c0 .. min(c0 + FT, c1)
+    c64* P = panel + (int64_t)op * F.panel_total + F.panel_off[f];
+    for (int q = threadIdx.x; q < FB * FT; q += 256) {
+        const int m = q / FT, r = q - m * FT;
+        c64 a = zero<double>(), b = zero<double>();
+        if (m < nb) {
+            if (i0 + r < nf) a = P[(int64_t)(kb + m) * nf + i0 + r];
+            const int c = c0 + r;
+            // Y(kb + m, c): the block row's solved entries; in mode 1 the block's inverse, unit diagonal
+            if (c < c1) b = (mode == 1 && c - kb == m) ? mk<double>(1.0, 0.0)
+                                                       : (mode == 1 && c - kb > m) ? zero<double>()
+                                                                                   : P[(int64_t)c * nf + kb + m];
+        }
+        As[q] = a;
+        Bs[q] = b;
+    }
+    __syncthreads();
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    c64 acc[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[r][c] = zero<double>();
+    for (int m = 0; m < nb; ++m) {
+        c64 a[4], b[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) a[r] = As[m * FT + tx + 16 * r];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) b[c] = Bs[m * FT + ty + 16 * c];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) acc[r][c] += a[r] * b[c];
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const int j = c0 + ty + 16 * c;
+        if (j >= c1) continue;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int i = i0 + tx + 16 * r;
+            if (i >= nf) continue;
+            c64& y = P[(int64_t)j * nf + i];
+            y = (mode == 1 ? zero<double>() : y) - acc[r][c];
+        }
+    }
+}
+
+void launch_invert_tiled(const Fronts& F, const int64_t* front_list, int nfront, int max_nf, int max_nown, c64* panel,
+                         int nops, cudaStream_t st) {
+    if (nfront <= 0) return;
+    raise_smem((const void*)inv_trail_kernel, TRAIL_SMEM);
+    for (int kb = 0; kb < max_nown; kb += FB) {
+        if (kb > 0) {
+            inv_rows_kernel<<<dim3(ceil_div(kb, ROWS_CTA), nfront, nops), ROWS_CTA, 0, st>>>(F, front_list, kb, panel);
+            GT_LAUNCH_CHECK();
+        }
+        inv_diag_kernel<<<dim3(nfront, nops), 32, 0, st>>>(F, front_list, kb, panel);
+        GT_LAUNCH_CHECK();
+        const int below = max_nf - kb - 1;
+        if (below <= 0) continue;
+        const int rt = ceil_div(below, FT);
+        if (kb > 0) {
+            inv_trail_kernel<<<dim3(rt * ceil_div(kb, FT), nfront, nops), 256, TRAIL_SMEM, st>>>(F, front_list, kb, panel, 0);
+            GT_LAUNCH_CHECK();
+        }
+        inv_trail_kernel<<<dim3(rt, nfront, nops), 256, TRAIL_SMEM, st>>>(F, front_list, kb, panel, 1);
+        GT_LAUNCH_CHECK();
+    }
 }
 
 // Finish the solve panels: the own block gets its inverse below an explicit unit diagonal (moved from the
@@ -349,15 +511,23 @@ void launch_bnd_inv(const Fronts& F, c64* panel, int max_nbnd, int nops, cudaStr
 // row-major copies are written.
 // r64 (the FP64 row-major copy) may be null: operators that keep their FP32 panels only
 __global__ void panel_convert_kernel(Fronts F, c64* __restrict__ p64, c32* __restrict__ p32, c32* __restrict__ r32,
-                                     c64* __restrict__ r64, c64* __restrict__ d64, c32* __restrict__ d32) {
+                                     c64* __restrict__ r64, c64* __restrict__ d64, c32* __restrict__ d32, int tiled_nf) {
     const int f = blockIdx.x;
     const int op = blockIdx.y;
     const int nown = (int)F.nown[f], nf = nown + (int)F.nbnd[f];
+    const bool in_place = nf >= tiled_nf;                       // the blocked inversion: X below the diagonal
     const int64_t base = (int64_t)op * F.panel_total + F.panel_off[f];
     const int64_t dbase = (int64_t)op * F.nfac + F.own_start[f];
     for (int64_t q = threadIdx.x; q < (int64_t)nf * nown; q += blockDim.x) {
         int k = int(q / nf), i = int(q - (int64_t)k * nf);      // column-major element (i, k)
-        if (i < k) continue;                                     // the upper triangle: with its partner below
+        if (i < k) {                                             // the upper triangle: zero
+            if (in_place) {
+                p32[base + q] = zero<float>();
+                r32[base + (int64_t)i * nown + k] = zero<float>();
+                if (r64) r64[base + (int64_t)i * nown + k] = zero<double>();
+            }
+            continue;                                            // (else with its partner below)
+        }
         c64 v = p64[base + q];
         if (i == k) {
             const c64 dv = cdiv(mk<double>(1.0, 0.0), v);
@@ -365,7 +535,7 @@ __global__ void panel_convert_kernel(Fronts F, c64* __restrict__ p64, c32* __res
             d32[dbase + i] = cvt<float>(dv);
             v = mk<double>(1.0, 0.0);
             p64[base + q] = v;
-        } else if (i < nown) {
+        } else if (i < nown && !in_place) {
             // X[i, k] from its transposed position (k, i), which becomes zero
             const int64_t qt = (int64_t)i * nf + k;
             v = p64[base + qt];
@@ -382,8 +552,8 @@ __global__ void panel_convert_kernel(Fronts F, c64* __restrict__ p64, c32* __res
 }
 
 void launch_panel_convert(const Fronts& F, c64* p64, c32* p32, c32* r32, c64* r64, c64* d64, c32* d32, int nops,
-                          cudaStream_t st) {
-    panel_convert_kernel<<<dim3(F.nfront, nops), 256, 0, st>>>(F, p64, p32, r32, r64, d64, d32);
+                          int tiled_nf, cudaStream_t st) {
+    panel_convert_kernel<<<dim3(F.nfront, nops), 256, 0, st>>>(F, p64, p32, r32, r64, d64, d32, tiled_nf);
     GT_LAUNCH_CHECK();
 }
 

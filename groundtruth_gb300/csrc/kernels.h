@@ -152,12 +152,16 @@ void launch_factor_level(const Fronts& F, const int64_t* front_list, int nf_leve
 void launch_factor_tiled(const Fronts& F, const int64_t* front_list, int nf_level, int max_nf, int max_nown,
                          const c64* svals, c64* panel, c64* upd, int nops, int* status, cudaStream_t st);
 // each front's own block replaced by its inverse (in place, FP64; the unit diagonal and the pivots untouched)
-void launch_invert_own(const Fronts& F, c64* panel, int max_nown, int nops, cudaStream_t st);
+void launch_invert_own(const Fronts& F, c64* panel, int max_nown, int nops, int tiled_nf, cudaStream_t st);
 // each front's boundary rows replaced by -L_bnd Linv_own (in place, FP64; after launch_invert_own)
-void launch_bnd_inv(const Fronts& F, c64* panel, int max_nbnd, int nops, cudaStream_t st);
+void launch_bnd_inv(const Fronts& F, c64* panel, int max_nbnd, int nops, int tiled_nf, cudaStream_t st);
+// both at once for the listed (large) fronts, blocked over many CTAs; the two above skip fronts of tiled_nf rows
+// or more, and panel_convert takes their inverse in place
+void launch_invert_tiled(const Fronts& F, const int64_t* front_list, int nfront, int max_nf, int max_nown, c64* panel,
+                         int nops, cudaStream_t st);
 // the solve panels: own blocks get a unit diagonal and zeros above it (pivot reciprocals to d64 / d32,
 // [op][nfac]); FP32 column-major, FP32 and FP64 row-major copies
-void launch_panel_convert(const Fronts& F, c64* p64, c32* p32, c32* r32, c64* r64, c64* d64, c32* d32, int nops,
+void launch_panel_convert(const Fronts& F, c64* p64, c32* p32, c32* r32, c64* r64, c64* d64, c32* d32, int nops, int tiled_nf,
                           cudaStream_t st);
 
 // triangular solves, per level; groups of columns sharing an operator

