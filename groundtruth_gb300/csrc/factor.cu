@@ -907,17 +907,14 @@ __global__ void __launch_bounds__(SOLVE_THREADS, 2) bwd_gemv_kernel(Fronts F, co
     }
 }
 
-// Launch shape of a level: with enough (front, group) tasks to fill the GPU a block takes a whole small
-// front; otherwise a block takes one 32-row (32-column) tile and splits the inner dimension over warps.
+// Launch shape of a level.  The inner dimension is split into segments of about 64 whose partial sums meet
+// in a fixed order, their count set by the level's largest front alone: a column's arithmetic (and so its
+// rounding) does not depend on how many columns share the solve.  Unsplit small fronts, with enough
+// (front, group) tasks to fill the GPU, go whole to a block.
 static void solve_shape(int ntask, int ntile, int inner, int& per_blk, int& nseg) {
     const int fill = 8 * 152;
-    if ((int64_t)ntask * ntile >= fill && ntile <= 4 && (int64_t)ntask >= fill / 2) {
-        per_blk = ntile;
-        nseg = 1;
-    } else {
-        per_blk = 1;
-        nseg = std::max(1, std::min(SOLVE_THREADS / 32, (inner + 63) / 64));
-    }
+    nseg = std::max(1, std::min(SOLVE_THREADS / 32, (inner + 63) / 64));
+    per_blk = (nseg == 1 && (int64_t)ntask * ntile >= fill && ntile <= 4 && (int64_t)ntask >= fill / 2) ? ntile : 1;
 }
 
 template <typename R, int GC>

@@ -69,3 +69,18 @@ def test_narrow_column_groups_give_the_same_solutions(width, monkeypatch):
     got = _columns(st, routes, freqs)
     for a, c in zip(ref, got):
         assert np.linalg.norm(a[3] - c[3]) <= 1e-12 * np.linalg.norm(a[3])
+
+
+def test_a_column_solves_the_same_in_any_batch():
+    """A column's device arithmetic is its own: solved with every other column of the board, or alone, its
+    iterations and solution are the same bit for bit (the triangular sweeps' partial sums meet in an order set
+    by the fronts, not by how many columns share the launch)."""
+    from groundtruth_gb300 import stack as gs
+    b = synth.random_board(45, side=(24, 64), n_layers=(2, 5), n_nets=(1, 3), n_freq=(2, 4))
+    st, routes = gs.from_board(b)
+    freqs = [float(f) for f in b.freqs] * 4                 # enough columns for the many-task launch shapes
+    together = _columns(st, routes, freqs)
+    for q, f in enumerate(freqs[: len(b.freqs)]):
+        alone = _columns(st, routes, [f])[0]
+        assert alone[2] == together[q][2]                   # iterations
+        assert np.array_equal(alone[3], together[q][3])     # solution
