@@ -48,6 +48,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 GPU comparator")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffers) leg")
+    ap.add_argument("--e2e-chunks", type=int, default=4,
+                    help="e2e: frequency groups factorised while earlier groups solve (native.solve_sweep; 1: "
+                         "factorise everything first)")
     ap.add_argument("--reorth", type=float, default=0.0,
                     help="DGKS re-orthogonalisation ratio (0.7: the reference rule; 0: none, the FP64 refinement guards the answer)")
     ap.add_argument("--max-its", type=int, default=4000)
@@ -423,24 +426,36 @@ def run_gpu(args):
     # e2e through the C ABI from host buffers: factorise all frequencies + solve + copy out, every step
     e2e_t, e2e_parts = [], []
     # the step's inputs and outputs in page-locked host memory
+    # the columns by frequency, so that the sweep's frequency groups are contiguous rows of the host buffers
+    by_f = sorted(range(ncol), key=lambda c: (cols[c][1], cols[c][0]))
+    key_f = np.array([cols[c][1] for c in by_f])
     rhs_pin = torch.empty(rhs_c.shape, dtype=torch.complex128, pin_memory=True).numpy()
     x_pin = torch.empty(rhs_c.shape, dtype=torch.complex128, pin_memory=True).numpy()
-    rhs_pin[...] = rhs_c
+    rhs_pin[...] = rhs_c[by_f]
+    skw = dict(restart=args.restart, inner_tol=args.inner_tol, max_its=args.max_its, reorth=args.reorth,
+               outer_k=args.outer_k, precision=args.precision)
+    sweep = args.e2e_chunks > 1 and not args.borrow
     for k in range(0 if args.no_e2e else max(1, min(args.steps, 2))):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         data = [st._freq_tables(f) for f in freqs]
         t1 = time.perf_counter()
-        ops2 = native.Operators(st.handle, freqs, data, gs.borrow_plan(freqs) if args.borrow else None)
-        t2 = time.perf_counter()
-        xh, its2, res2, ok2 = native.solve(st.handle, [(ops2, q) for (_, q) in cols], rhs_pin, args.tol,
-                                           restart=args.restart, inner_tol=args.inner_tol, max_its=args.max_its,
-                                           reorth=args.reorth, outer_k=args.outer_k, precision=args.precision,
-                                           out=x_pin)
+        if sweep:       # factorisation of later frequency groups overlapped with the solves of earlier ones
+            xh, its2, res2, ok2 = native.solve_sweep(st.handle, freqs, data, key_f, rhs_pin, args.tol,
+                                                     chunks=args.e2e_chunks, out=x_pin, **skw)
+            t2 = t1
+        else:
+            ops2 = native.Operators(st.handle, freqs, data, gs.borrow_plan(freqs) if args.borrow else None)
+            t2 = time.perf_counter()
+            xh, its2, res2, ok2 = native.solve(st.handle, [(ops2, int(q)) for q in key_f], rhs_pin, args.tol,
+                                               out=x_pin, **skw)
+            del ops2
         e2e_t.append(time.perf_counter() - t0)
-        e2e_parts.append({"tables_s": round(t1 - t0, 3), "operators_s": round(t2 - t1, 3),
-                          "solve_s": round(e2e_t[-1] - t2 + t0, 3)})
-        del ops2
+        e2e_parts.append({"tables_s": round(t1 - t0, 3),
+                          **({"factorise_and_solve_overlapped_s": round(e2e_t[-1] - t1 + t0, 3),
+                              "frequency_groups": args.e2e_chunks} if sweep else
+                             {"operators_s": round(t2 - t1, 3), "solve_s": round(e2e_t[-1] - t2 + t0, 3)}),
+                          "max_rel_residual": float(np.max(res2))})
     e2e = None
     if e2e_t:
         e2e = {"value": world * ncol / float(np.median(e2e_t)), "unit": "solves/s",

@@ -65,6 +65,13 @@ struct Pool {
         ptrs.push_back(p);
         return static_cast<T*>(p);
     }
+    // on a stream: ordered before that stream's kernels (a pageable cudaMemcpy may still be landing when it
+    // returns, ordered only on the legacy default stream)
+    template <typename T> T* upload(const T* h, size_t n, cudaStream_t st) {
+        T* d = alloc<T>(n);
+        if (n && h) GT_CUDA(cudaMemcpyAsync(d, h, n * sizeof(T), cudaMemcpyHostToDevice, st));
+        return d;
+    }
     template <typename T> T* upload(const T* h, size_t n) {
         T* d = alloc<T>(n);
         if (n && h) GT_CUDA(cudaMemcpy(d, h, n * sizeof(T), cudaMemcpyHostToDevice));
@@ -79,13 +86,17 @@ struct Pool {
 
 // Per-kernel-family timing with CUDA events on the launch stream (gt_profile).
 struct Profiler {
+    // a geometry's solves and its operator sets' factorisations may run at once on two host threads: the
+    // records are kept under a lock, and each flush settles only the regions of its own stream
     bool on = false;
     bool levels = false;   // also time each elimination level of the triangular solves
     struct Rec {
         int fam;
         cudaEvent_t a, b;
         double bytes;
+        cudaStream_t st;
     };
+    std::mutex lock;
     std::vector<Rec> pending;
     std::vector<cudaEvent_t> free_events;
     std::vector<std::string> names;
@@ -95,23 +106,37 @@ struct Profiler {
     };
     std::map<int, Acc> acc;
     int family(const char* n) {
+        std::lock_guard<std::mutex> lk(lock);
         for (size_t i = 0; i < names.size(); ++i)
             if (names[i] == n) return (int)i;
         names.push_back(n);
         return (int)names.size() - 1;
     }
     cudaEvent_t ev() {
-        if (!free_events.empty()) {
-            cudaEvent_t e = free_events.back();
-            free_events.pop_back();
-            return e;
+        {
+            std::lock_guard<std::mutex> lk(lock);
+            if (!free_events.empty()) {
+                cudaEvent_t e = free_events.back();
+                free_events.pop_back();
+                return e;
+            }
         }
         cudaEvent_t e;
         GT_CUDA(cudaEventCreate(&e));
         return e;
     }
-    void flush() {
+    void push(const Rec& r) {
+        std::lock_guard<std::mutex> lk(lock);
+        pending.push_back(r);
+    }
+    void flush(cudaStream_t st) {
+        std::lock_guard<std::mutex> lk(lock);
+        std::vector<Rec> keep;
         for (auto& r : pending) {
+            if (r.st != st) {
+                keep.push_back(r);
+                continue;
+            }
             float ms = 0;
             GT_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
             auto& a = acc[r.fam];
@@ -121,7 +146,7 @@ struct Profiler {
             free_events.push_back(r.a);
             free_events.push_back(r.b);
         }
-        pending.clear();
+        pending.swap(keep);
     }
     ~Profiler() {
         for (auto& r : pending) {
@@ -132,6 +157,7 @@ struct Profiler {
     }
 };
 
+// A CUDA-event region of a kernel family on a stream (a no-op while the profiler is off).
 struct Scope {
     Profiler* p;
     int fam;
@@ -149,7 +175,7 @@ struct Scope {
         if (!p) return;
         try {
             cudaEvent_t b = p->ev();
-            if (cudaEventRecord(b, st) == cudaSuccess) p->pending.push_back({fam, a, b, bytes});
+            if (cudaEventRecord(b, st) == cudaSuccess) p->push({fam, a, b, bytes, st});
         } catch (...) {
         }
     }
@@ -300,7 +326,7 @@ namespace gt {
 
 // the operators' sheet impedances [op][S] and, with face sheets, the face couplings [op][ntw] from the host's
 // zs [op][S + ntw]
-static void upload_zs(gt_operators* O, const gt_geometry* G, const double* zs, int n_ops) {
+static void upload_zs(gt_operators* O, const gt_geometry* G, const double* zs, int n_ops, cudaStream_t st = 0) {
     const int S = G->geo.S, ntw = G->ntw, ld = S + ntw;
     std::vector<c64> a((size_t)n_ops * S), b((size_t)n_ops * std::max(ntw, 1));
     for (int q = 0; q < n_ops; ++q) {
@@ -308,8 +334,9 @@ static void upload_zs(gt_operators* O, const gt_geometry* G, const double* zs, i
         for (int m = 0; m < ntw; ++m)
             b[(size_t)q * ntw + m] = mk<double>(zs[2 * ((size_t)q * ld + S + m)], zs[2 * ((size_t)q * ld + S + m) + 1]);
     }
-    O->zs = O->pool.upload(a.data(), a.size());
-    O->zmut = O->pool.upload(b.data(), b.size());
+    O->zs = O->pool.upload(a.data(), a.size(), st);
+    O->zmut = O->pool.upload(b.data(), b.size(), st);
+    GT_CUDA(cudaStreamSynchronize(st));      // a and b go out of scope
 }
 
 static int status_of(const CudaError& e) {
@@ -650,26 +677,29 @@ static void lowrank_w(gt_geometry* G, const gt_operators* base, int nf, int k, c
 
 static int nchunks(int64_t n) { return (int)((n + 2047) / 2048); }  // DOT_CHUNK in gmres.cu
 
-static void fill_ws(Workspace& W, gt_geometry* G, int ncol, int m, int prec, int kmax);
+static void fill_ws(Workspace& W, gt_geometry* G, int ncol, int m, int prec, int kmax, cudaStream_t st);
 
-static void ensure_ws(gt_geometry* G, int ncol, int m, int prec, int kmax) {
+// The solve workspace for ncol columns, made on first use; its clears are ordered on the solve's stream st.
+static void ensure_ws(gt_geometry* G, int ncol, int m, int prec, int kmax, cudaStream_t st) {
     auto& w = G->ws;
     if (w && w->ncol >= ncol && w->m >= m && w->prec == prec && w->kmax >= kmax) return;
-    w.reset();
-    cudaDeviceSynchronize();
+    if (w) {                       // the old one's last kernels are done before its memory goes
+        cudaDeviceSynchronize();
+        w.reset();
+    }
     w.reset(new Workspace());
-    fill_ws(*w, G, ncol, m, prec, kmax);
+    fill_ws(*w, G, ncol, m, prec, kmax, st);
 }
 
 // the bytes fill_ws would allocate (nothing is allocated)
 static size_t ws_bytes(gt_geometry* G, int ncol, int m, int prec, int kmax) {
     Workspace W;
     W.pool.dry = true;
-    fill_ws(W, G, ncol, m, prec, kmax);
+    fill_ws(W, G, ncol, m, prec, kmax, 0);
     return W.pool.bytes;
 }
 
-static void fill_ws(Workspace& W, gt_geometry* G, int ncol, int m, int prec, int kmax) {
+static void fill_ws(Workspace& W, gt_geometry* G, int ncol, int m, int prec, int kmax, cudaStream_t st) {
     const bool dry = W.pool.dry;
     W.ncol = ncol;
     W.m = m;
@@ -699,7 +729,7 @@ static void fill_ws(Workspace& W, gt_geometry* G, int ncol, int m, int prec, int
     W.uvec = p.alloc<unsigned char>((size_t)ncol * std::max<int64_t>(G->F.vec_total, 1) * es);
     // node-ordered s / y of the preconditioner: entries of nodes that are not kept stay zero
     W.sd = p.alloc<unsigned char>((size_t)ncol * G->F.nnode * es);
-    if (!dry) GT_CUDA(cudaMemset(W.sd, 0, (size_t)ncol * G->F.nnode * es));
+    if (!dry) GT_CUDA(cudaMemsetAsync(W.sd, 0, (size_t)ncol * G->F.nnode * es, st));
     W.partial = p.alloc<c64>((size_t)ncol * nch * (m + 2));
     if (prec == 3) {
         W.pr64 = p.alloc<c64>((size_t)ncol * n);
@@ -708,7 +738,7 @@ static void fill_ws(Workspace& W, gt_geometry* G, int ncol, int m, int prec, int
         W.yfac64 = p.alloc<c64>((size_t)ncol * G->F.nfac);
         W.uvec64 = p.alloc<c64>((size_t)ncol * std::max<int64_t>(G->F.vec_total, 1));
         W.sd64 = p.alloc<c64>((size_t)ncol * G->F.nnode);
-        if (!dry) GT_CUDA(cudaMemset(W.sd64, 0, (size_t)ncol * G->F.nnode * sizeof(c64)));
+        if (!dry) GT_CUDA(cudaMemsetAsync(W.sd64, 0, (size_t)ncol * G->F.nnode * sizeof(c64), st));
     }
     GmresState& s = W.st;
     s.nslot = ncol;
@@ -749,7 +779,7 @@ static void fill_ws(Workspace& W, gt_geometry* G, int ncol, int m, int prec, int
     W.its_col = p.alloc<int>(ncol);
     if (dry) return;
     GT_CUDA(cudaMallocHost(&W.flag_host, sizeof(int)));
-    GT_CUDA(cudaMemset(W.V, 0, (size_t)ncol * (m + 1) * n * eb));
+    GT_CUDA(cudaMemsetAsync(W.V, 0, (size_t)ncol * (m + 1) * n * eb, st));
 }
 
 // ||v_c|| for ncol FP64 dense vectors -> out (device)
@@ -995,10 +1025,10 @@ static int solve_impl(gt_geometry* G, gt_operators* ops, int ncol, const int* h_
         GT_CUDA(cudaMemcpyAsync(its_slot.data(), S.its_total, ns * sizeof(int), cudaMemcpyDeviceToHost, st));
         GT_CUDA(cudaStreamSynchronize(st));
         for (int s = 0; s < ns; ++s) h_its[slot_col[s]] = its_slot[s];
-        P->flush();
+        P->flush(st);
     }
     if (!verified) true_residual();
-    P->flush();
+    P->flush(st);
     bool all = true;
     for (int c = 0; c < ncol; ++c) {
         double rr = h_bnorm[c] > 0 ? h_rho[c] / h_bnorm[c] : 0.0;
@@ -1449,7 +1479,15 @@ int gt_operators_create_ex(gt_geometry* G, int32_t n_ops, const double* omega, c
     if (G->n_lowrank)
         throw Invalid("the geometry's last branches are a low-rank update of a base: make its operators with "
                       "gt_operators_derive");
-    std::lock_guard<std::mutex> lk(G->lock);
+    // No geometry lock: the factorisation reads only the geometry's fixed data (and its profiler, which has a
+    // lock of its own), so a geometry's next operator set can be made while it solves with the last one.  It
+    // runs on a non-blocking stream of its own, which neither the legacy default stream nor a caller's stream
+    // orders it against.
+    struct OwnStream {
+        cudaStream_t s{};
+        OwnStream() { GT_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)); }
+        ~OwnStream() { cudaStreamDestroy(s); }
+    } own_stream;
     std::unique_ptr<gt_operators> O(new gt_operators());
     O->g = G;
     O->nops = n_ops;
@@ -1471,10 +1509,11 @@ int gt_operators_create_ex(gt_geometry* G, int32_t n_ops, const double* omega, c
         if (O->fslot[q] < 0) O->fslot[q] = O->fslot[factor_of[q]];
     const int nf_ops = O->nfact = (int)own.size();
     O->own = own;
-    O->omega = p.upload(omega, n_ops);
-    upload_zs(O.get(), G, zs, n_ops);
-    O->zcap = p.upload(reinterpret_cast<const c64*>(zcap), (size_t)n_ops * g.np);
-    O->zbr = p.upload(reinterpret_cast<const c64*>(zbr), (size_t)n_ops * g.nbr);
+    cudaStream_t st = own_stream.s;
+    O->omega = p.upload(omega, n_ops, st);
+    upload_zs(O.get(), G, zs, n_ops, st);
+    O->zcap = p.upload(reinterpret_cast<const c64*>(zcap), (size_t)n_ops * g.np, st);
+    O->zbr = p.upload(reinterpret_cast<const c64*>(zbr), (size_t)n_ops * g.nbr, st);
     {
         // the admittance tables of the factorised operators (the preconditioner's D^-1 and the Schur values)
         std::vector<c64> t64((size_t)nf_ops * g.ntab);
@@ -1485,16 +1524,16 @@ int gt_operators_create_ex(gt_geometry* G, int32_t n_ops, const double* omega, c
                 t64[dst] = mk<double>(table[src], table[src + 1]);
                 t32[dst] = mk<float>((float)table[src], (float)table[src + 1]);
             }
-        O->tab = p.upload(t64.data(), t64.size());
-        O->tab32 = p.upload(t32.data(), t32.size());
+        O->tab = p.upload(t64.data(), t64.size(), st);
+        O->tab32 = p.upload(t32.data(), t32.size(), st);
         O->stiff = stiffness(t64, nf_ops, g);
+        GT_CUDA(cudaStreamSynchronize(st));   // t64 and t32 go out of scope
     }
     // FP32 panels only: the FP64 factor lives in temporary memory while it is made and converted, and no FP64
     // row-major copy is made; a stiff set keeps its FP64 panels, which its FP64 preconditioner needs
     const bool keep64 = !(flags & GT_OPS_FP32_PANELS) ||
                         std::any_of(O->stiff.begin(), O->stiff.end(), [](char v) { return v != 0; });
     n_ops = nf_ops;        // the factorisation below runs over the factorised operators
-    cudaStream_t st = 0;
     const Fronts& F = G->F;
     Pool tmp;
     c64* svals = tmp.alloc<c64>((size_t)n_ops * F.nsv);
@@ -1546,9 +1585,9 @@ int gt_operators_create_ex(gt_geometry* G, int32_t n_ops, const double* omega, c
                              G->tiled_nf, st);
     }
     int h_status = 0;
-    GT_CUDA(cudaMemcpy(&h_status, status, sizeof(int), cudaMemcpyDeviceToHost));
+    GT_CUDA(cudaMemcpyAsync(&h_status, status, sizeof(int), cudaMemcpyDeviceToHost, st));
     GT_CUDA(cudaStreamSynchronize(st));
-    P->flush();
+    P->flush(st);
     if (h_status) throw Invalid("the Schur complement has a zero or non-finite pivot (a piece of copper with no "
                                 "path to its reference node?)");
     if (!keep64) O->panel64 = nullptr;   // freed with the temporary memory
@@ -1688,7 +1727,7 @@ int gt_operators_derive(gt_geometry* G, const gt_operators* base, int32_t n_ops,
         O->low_m32 = p.upload(m32.data(), m32.size());
         GT_CUDA(cudaStreamSynchronize(st));
     }
-    P->flush();
+    P->flush(st);
     *out = O.release();
     return GT_OK;
     GT_GUARD_END
@@ -1733,7 +1772,7 @@ int gt_solve_device(gt_geometry* G, gt_operators* ops, int32_t n_cols, const int
     gt_solve_opts eo = *opts;
     eo.precision = effective_precision(G, ops, n_cols, col_op, eo.precision);
     opts = &eo;
-    ensure_ws(G, n_cols, opts->restart, opts->precision, std::max(1, opts->outer_k));
+    ensure_ws(G, n_cols, opts->restart, opts->precision, std::max(1, opts->outer_k), st);
     Workspace& W = *G->ws;
     GT_CUDA(cudaMemcpyAsync(W.b64, rhs_device, (size_t)n_cols * G->geo.n * sizeof(c64), cudaMemcpyDeviceToDevice, st));
     if (opts->use_guess)
@@ -1755,7 +1794,7 @@ int gt_solve(gt_geometry* G, gt_operators* ops, int32_t n_cols, const int32_t* c
     gt_solve_opts eo = *opts;
     eo.precision = effective_precision(G, ops, n_cols, col_op, eo.precision);
     opts = &eo;
-    ensure_ws(G, n_cols, opts->restart, opts->precision, std::max(1, opts->outer_k));
+    ensure_ws(G, n_cols, opts->restart, opts->precision, std::max(1, opts->outer_k), st);
     Workspace& W = *G->ws;
     const int64_t nc = G->n_compact;
     Pool tmp;
@@ -1830,6 +1869,7 @@ int gt_apply(gt_geometry* G, gt_operators* ops, int32_t kind, int32_t precision,
             yo = tmp.alloc<c32>((size_t)n_cols * n);
             // round the input to FP32 through a refine-style copy: y = 1.0 * x
             std::vector<c64> hx((size_t)n_cols * n);
+            GT_CUDA(cudaStreamSynchronize(st));          // xin was made on the caller's stream
             GT_CUDA(cudaMemcpy(hx.data(), xin, hx.size() * sizeof(c64), cudaMemcpyDeviceToHost));
             std::vector<c32> h32(hx.size());
             for (size_t i = 0; i < hx.size(); ++i) h32[i] = cvt<float>(hx[i]);
@@ -1940,6 +1980,7 @@ int gt_kernel_spectrum(int32_t n_axial, int32_t n_lateral, double d, double dz, 
 int gt_profile(gt_geometry* G, char* names, int32_t names_cap, double* ms, double* bytes, int32_t* launches,
                int32_t cap) {
     if (!G) return 0;
+    std::lock_guard<std::mutex> lk(G->prof.lock);
     if (names == nullptr && cap < 0) {  // toggle: cap = -1 off, -2 on (and reset), -3 on with levels
         G->prof.on = cap <= -2;
         G->prof.levels = cap == -3;

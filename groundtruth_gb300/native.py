@@ -408,6 +408,66 @@ def solve(geom: Geometry, ops: list, rhs: np.ndarray, tol: float, restart: int =
     return x, its, res, res <= tol
 
 
+def solve_sweep(geom: Geometry, keys: list, tables: list, col_key: np.ndarray, rhs: np.ndarray, tol: float,
+                chunks: int = 4, out: np.ndarray | None = None, stream: int | None = None, fp32_panels: bool = False,
+                **solve_kw):
+    """A frequency sweep from host buffers, its factorisation overlapped with its solves: the operators (keys,
+    tables as for Operators) are made in `chunks` contiguous groups of frequencies by a second host thread,
+    each group on a stream of its own (gt_operators_create_ex takes no geometry lock), while the columns of
+    the groups already made are solved on `stream` (gt_solve).  The FP64 factorisation (the FP64 pipes, few SMs
+    at the top of the elimination tree) so runs beside the FP32 solve instead of before it.  Column c of rhs
+    is at frequency index col_key[c]; the columns of a group must be contiguous rows of rhs (sort them by
+    frequency), so that page-locked rhs and out pass to each solve as views.  Returns (x, its, resid,
+    converged) like solve."""
+    import threading
+    rhs = np.asarray(rhs)
+    col_key = np.asarray(col_key)
+    nq, ncol = len(keys), rhs.shape[0]
+    bounds = np.linspace(0, nq, max(1, min(chunks, nq)) + 1).round().astype(int)
+    groups = [range(bounds[i], bounds[i + 1]) for i in range(len(bounds) - 1) if bounds[i + 1] > bounds[i]]
+    group_of = np.empty(nq, np.int64)
+    for gi, g in enumerate(groups):
+        group_of[list(g)] = gi
+    gcol = group_of[col_key]
+    if np.any(np.diff(gcol) < 0):
+        raise ValueError("the columns must be sorted by their frequency's group")
+    x = out if out is not None else np.zeros(rhs.shape, np.complex128)
+    its = np.zeros(ncol, np.int32)
+    res = np.zeros(ncol)
+    made = [None] * len(groups)
+    ready = [threading.Event() for _ in groups]
+    failed = []
+
+    def factorise():
+        try:
+            for gi, g in enumerate(groups):
+                made[gi] = Operators(geom, [keys[q] for q in g], [tables[q] for q in g], fp32_panels=fp32_panels)
+                ready[gi].set()
+        except BaseException as e:          # handed to the solving thread
+            failed.append(e)
+            for r in ready:
+                r.set()
+
+    th = threading.Thread(target=factorise, name="sweep factorisation", daemon=True)
+    th.start()
+    try:
+        for gi, g in enumerate(groups):
+            ready[gi].wait()
+            if failed:
+                raise failed[0]
+            sel = np.flatnonzero(gcol == gi)
+            if not len(sel):
+                made[gi] = None
+                continue
+            a, b = int(sel[0]), int(sel[-1]) + 1
+            ops = [(made[gi], int(col_key[c]) - g.start) for c in range(a, b)]
+            _, its[a:b], res[a:b], _ = solve(geom, ops, rhs[a:b], tol, out=x[a:b], stream=stream, **solve_kw)
+            made[gi] = None                 # the group's factorisations go before the next group's solve
+    finally:
+        th.join()
+    return x, its, res, res <= tol
+
+
 def memory(geom: Geometry, n_cols: int, restart: int = 50, precision: str = "mixed", outer_k: int = 8) -> dict:
     """gt_memory: {"need": bytes a solve of n_cols columns allocates, "held": the geometry's workspace now,
     "free" / "total": the device's}."""

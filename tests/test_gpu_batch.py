@@ -84,3 +84,24 @@ def test_a_column_solves_the_same_in_any_batch():
         alone = _columns(st, routes, [f])[0]
         assert alone[2] == together[q][2]                   # iterations
         assert np.array_equal(alone[3], together[q][3])     # solution
+
+
+@pytest.mark.parametrize("chunks", [2, 3])
+def test_a_sweep_factorised_beside_its_solves_equals_the_plain_solve(chunks):
+    """native.solve_sweep (later frequency groups factorised on a second thread and stream while earlier ones
+    solve) gives the plain path's results bit for bit: the same factorisations, and columns whose arithmetic
+    does not depend on the batch they are solved in."""
+    from groundtruth_gb300 import native, stack as gs
+    b = synth.small_stack3()
+    st, routes = gs.from_board(b)
+    freqs = [float(f) for f in np.geomspace(1e6, 1e9, 6)]
+    cols = [(k, q) for q in range(len(freqs)) for k in range(len(routes))]
+    rhs = np.stack([st.rhs_vector(routes[k].rhs_top(freqs[q]), routes[k].J()) for k, q in cols])
+    data = [st._freq_tables(f) for f in freqs]
+    key = np.array([q for _, q in cols])
+    ops = native.Operators(st.handle, freqs, data)
+    x0, its0, res0, ok0 = native.solve(st.handle, [(ops, int(q)) for q in key], rhs, 1e-10, reorth=0.0)
+    x1, its1, res1, ok1 = native.solve_sweep(st.handle, freqs, data, key, rhs, 1e-10, chunks=chunks, reorth=0.0)
+    assert ok0.all() and ok1.all()
+    assert np.array_equal(its0, its1)
+    assert np.array_equal(x0, x1)
