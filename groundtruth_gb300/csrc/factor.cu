@@ -18,6 +18,27 @@
 
 namespace gt {
 
+// Complex multiply-accumulate as four explicit FMAs (acc += a u; cfms: acc -= a u): written out, the
+// product and the sum round as separate operations (six instructions instead of four on the FP64 pipe).
+__device__ __forceinline__ void cfma(c32& acc, c32 a, c32 u) {
+    acc.re = __fmaf_rn(a.re, u.re, acc.re);
+    acc.re = __fmaf_rn(-a.im, u.im, acc.re);
+    acc.im = __fmaf_rn(a.re, u.im, acc.im);
+    acc.im = __fmaf_rn(a.im, u.re, acc.im);
+}
+__device__ __forceinline__ void cfma(c64& acc, c64 a, c64 u) {
+    acc.re = __fma_rn(a.re, u.re, acc.re);
+    acc.re = __fma_rn(-a.im, u.im, acc.re);
+    acc.im = __fma_rn(a.re, u.im, acc.im);
+    acc.im = __fma_rn(a.im, u.re, acc.im);
+}
+__device__ __forceinline__ void cfms(c64& acc, c64 a, c64 u) {
+    acc.re = __fma_rn(-a.re, u.re, acc.re);
+    acc.re = __fma_rn(a.im, u.im, acc.re);
+    acc.im = __fma_rn(-a.re, u.im, acc.im);
+    acc.im = __fma_rn(-a.im, u.re, acc.im);
+}
+
 __global__ void assemble_s_kernel(const int64_t* __restrict__ ptr, const int* __restrict__ tab_idx,
                                   const double* __restrict__ coef, int64_t nsv, const c64* __restrict__ table, int ntab,
                                   c64* __restrict__ svals) {
@@ -107,7 +128,10 @@ __global__ void factor_level_kernel(Fronts F, const int64_t* __restrict__ front_
         const c64* colk = Fv.panel + (int64_t)k * nf;
         for (int j = k + 1 + warp; j < nf; j += nwarp) {
             const c64 ljd = colk[j] * dinv;
-            for (int i = j + lane; i < nf; i += 32) Fv.at(i, j) -= colk[i] * ljd;
+            for (int i = j + lane; i < nf; i += 32) {
+                c64& v = Fv.at(i, j);
+                cfms(v, colk[i], ljd);
+            }
         }
         __syncthreads();
         for (int i = k + 1 + tid; i < nf; i += nth) Fv.panel[(int64_t)k * nf + i] = Fv.panel[(int64_t)k * nf + i] * dinv;
@@ -184,7 +208,7 @@ __global__ void __launch_bounds__(ROWS_CTA) tiled_rows_kernel(Fronts F, const in
         if (k < nb) {
             c64 t = Fv.panel[(int64_t)(kb + k) * Fv.nf + i];
 #pragma unroll
-            for (int m = 0; m < k; ++m) t -= w[m] * l11[k][m];
+            for (int m = 0; m < k; ++m) cfms(t, w[m], l11[k][m]);
             w[k] = t;
         }
     }
@@ -246,7 +270,7 @@ __global__ void __launch_bounds__(256) tiled_trail_kernel(Fronts F, const int64_
 #pragma unroll
         for (int r = 0; r < 4; ++r)
 #pragma unroll
-            for (int c = 0; c < 4; ++c) acc[r][c] += a[r] * b[c];
+            for (int c = 0; c < 4; ++c) cfma(acc[r][c], a[r], b[c]);
     }
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
@@ -297,7 +321,7 @@ __global__ void __launch_bounds__(INV_ROWS) invert_own_kernel(Fronts F, c64* __r
         if (k >= i || i >= nown) continue;
         c64 acc = L[(int64_t)k * nf + i];
         const c64* Lk = L + (int64_t)k * nf;
-        for (int m = k + 1; m < i; ++m) acc += Xi[m] * Lk[m];
+        for (int m = k + 1; m < i; ++m) cfma(acc, Xi[m], Lk[m]);
         Xi[k] = mk<double>(-acc.re, -acc.im);
     }
 }
@@ -328,12 +352,12 @@ __global__ void __launch_bounds__(BND_ROWS) bnd_inv_kernel(Fronts F, c64* __rest
         for (; m + 4 <= nown; m += 4) {
             const c64 a0 = L[(int64_t)m * nf + jr], a1 = L[(int64_t)(m + 1) * nf + jr];
             const c64 a2 = L[(int64_t)(m + 2) * nf + jr], a3 = L[(int64_t)(m + 3) * nf + jr];
-            acc += a0 * L[(int64_t)m * nf + k];
-            acc += a1 * L[(int64_t)(m + 1) * nf + k];
-            acc += a2 * L[(int64_t)(m + 2) * nf + k];
-            acc += a3 * L[(int64_t)(m + 3) * nf + k];
+            cfma(acc, a0, L[(int64_t)m * nf + k]);
+            cfma(acc, a1, L[(int64_t)(m + 1) * nf + k]);
+            cfma(acc, a2, L[(int64_t)(m + 2) * nf + k]);
+            cfma(acc, a3, L[(int64_t)(m + 3) * nf + k]);
         }
-        for (; m < nown; ++m) acc += L[(int64_t)m * nf + jr] * L[(int64_t)m * nf + k];
+        for (; m < nown; ++m) cfma(acc, L[(int64_t)m * nf + jr], L[(int64_t)m * nf + k]);
         if (act) L[(int64_t)k * nf + j] = mk<double>(-acc.re, -acc.im);
     }
 }
@@ -376,7 +400,7 @@ __global__ void __launch_bounds__(ROWS_CTA) inv_rows_kernel(Fronts F, const int6
         if (r < nb) {
             c64 t = col[r];
 #pragma unroll
-            for (int m = 0; m < r; ++m) t -= l11[r][m] * y[m];
+            for (int m = 0; m < r; ++m) cfms(t, l11[r][m], y[m]);
             y[r] = t;
         }
     }
@@ -406,7 +430,7 @@ __global__ void __launch_bounds__(32) inv_diag_kernel(Fronts F, const int64_t* _
             c64 acc = a[i][k];
 #pragma unroll
             for (int m = k + 1; m < FB; ++m)
-                if (m < i) acc += x[m] * a[m][k];
+                if (m < i) cfma(acc, x[m], a[m][k]);
             x[k] = mk<double>(-acc.re, -acc.im);
         }
     }
@@ -467,7 +491,7 @@ __global__ void __launch_bounds__(256) inv_trail_kernel(Fronts F, const int64_t*
 #pragma unroll
         for (int r = 0; r < 4; ++r)
 #pragma unroll
-            for (int c = 0; c < 4; ++c) acc[r][c] += a[r] * b[c];
+            for (int c = 0; c < 4; ++c) cfma(acc[r][c], a[r], b[c]);
     }
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
@@ -583,20 +607,6 @@ __device__ __forceinline__ void lds2(const c32* p, c32& a, c32& b) {
 __device__ __forceinline__ void lds2(const c64* p, c64& a, c64& b) {
     a = p[0];
     b = p[1];
-}
-
-// acc += a * u as four fused multiply-adds (the plain complex expression costs two products and two sums more)
-__device__ __forceinline__ void cfma(c32& acc, c32 a, c32 u) {
-    acc.re = __fmaf_rn(a.re, u.re, acc.re);
-    acc.re = __fmaf_rn(-a.im, u.im, acc.re);
-    acc.im = __fmaf_rn(a.re, u.im, acc.im);
-    acc.im = __fmaf_rn(a.im, u.re, acc.im);
-}
-__device__ __forceinline__ void cfma(c64& acc, c64 a, c64 u) {
-    acc.re = __fma_rn(a.re, u.re, acc.re);
-    acc.re = __fma_rn(-a.im, u.im, acc.re);
-    acc.im = __fma_rn(a.re, u.im, acc.im);
-    acc.im = __fma_rn(a.im, u.re, acc.im);
 }
 
 // acc[c] += a * x[c] over all GC columns of one k-major shared row x (unused columns hold zeros)
@@ -907,14 +917,23 @@ __global__ void __launch_bounds__(SOLVE_THREADS, 2) bwd_gemv_kernel(Fronts F, co
     }
 }
 
-// Launch shape of a level.  The inner dimension is split into segments of about 64 whose partial sums meet
-// in a fixed order, their count set by the level's largest front alone: a column's arithmetic (and so its
-// rounding) does not depend on how many columns share the solve.  Unsplit small fronts, with enough
-// (front, group) tasks to fill the GPU, go whole to a block.
-static void solve_shape(int ntask, int ntile, int inner, int& per_blk, int& nseg) {
+// Launch shape of a level, chosen from the level's fronts alone, never from the number of column groups in the
+// solve: the split of the inner dimension sets the order in which partial sums meet, so a column's arithmetic
+// (and rounding) must not depend on how many columns share the launch.  The choice assumes a nominal
+// NOMINAL_GROUPS groups per front (the sweep batches 8 columns per group): with enough (front, group) tasks
+// to fill the GPU a block takes a whole small front; otherwise a block takes one 32-row (32-column) tile and
+// splits the inner dimension over warps.
+constexpr int NOMINAL_GROUPS = 32;
+static void solve_shape(int nfront_level, int ntile, int inner, int& per_blk, int& nseg) {
     const int fill = 8 * 152;
-    nseg = std::max(1, std::min(SOLVE_THREADS / 32, (inner + 63) / 64));
-    per_blk = (nseg == 1 && (int64_t)ntask * ntile >= fill && ntile <= 4 && (int64_t)ntask >= fill / 2) ? ntile : 1;
+    const int64_t ntask = (int64_t)nfront_level * NOMINAL_GROUPS;
+    if (ntask * ntile >= fill && ntile <= 4 && ntask >= fill / 2) {
+        per_blk = ntile;
+        nseg = 1;
+    } else {
+        per_blk = 1;
+        nseg = std::max(1, std::min(SOLVE_THREADS / 32, (inner + 63) / 64));
+    }
 }
 
 template <typename R, int GC>
@@ -924,7 +943,7 @@ static void fwd_level_gc(const Fronts& F, const int64_t* front_list, int nf_leve
     const int ntask = nf_level * G.ngroup;
     const int ntile = ceil_div(max_nf, 32);
     int rt, kseg;
-    solve_shape(ntask, ntile, max_nown, rt, kseg);
+    solve_shape(nf_level, ntile, max_nown, rt, kseg);
     const int nblk = ceil_div(ntile, rt), ldw = std::max(max_nown, 1);
     const int pre = nblk > 1;
     if (pre) {
@@ -949,7 +968,7 @@ static void bwd_level_gc(const Fronts& F, const int64_t* front_list, int nf_leve
     const int cw = ceil_div(max_nown, 16) * 16 - max_nown < ceil_div(max_nown, 32) * 32 - max_nown ? 16 : 32;
     const int ntile = ceil_div(max_nown, cw);
     int ct, iseg;
-    solve_shape(ntask, ntile, max_nf, ct, iseg);
+    solve_shape(nf_level, ntile, max_nf, ct, iseg);
     const int nblk = ceil_div(ntile, ct), ldv = std::max(max_nf, 1);
     const size_t sm = (size_t)GC * (ldv + (iseg > 1 ? iseg * cw * ct : 0)) * sizeof(cx<R>);
     smem_attr<R>((const void*)bwd_gemv_kernel<R, GC>, sm);
