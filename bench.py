@@ -48,9 +48,11 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 GPU comparator")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffers) leg")
-    ap.add_argument("--e2e-chunks", type=int, default=4,
-                    help="e2e: frequency groups factorised while earlier groups solve (native.solve_sweep; 1: "
-                         "factorise everything first)")
+    ap.add_argument("--e2e-chunks", type=int, default=1,
+                    help="e2e: frequency groups factorised while earlier groups solve (native.solve_sweep); 1 "
+                         "(default): factorise every frequency, then solve all columns in one batch — measured "
+                         "faster here (4 groups: 8.16 s a step against 6.9 s: four 64-column solves pay the "
+                         "sweeps' latency-bound top levels and the per-step host work four times)")
     ap.add_argument("--reorth", type=float, default=0.0,
                     help="DGKS re-orthogonalisation ratio (0.7: the reference rule; 0: none, the FP64 refinement guards the answer)")
     ap.add_argument("--max-its", type=int, default=4000)
