@@ -50,6 +50,17 @@ struct Invalid : std::runtime_error {
     using std::runtime_error::runtime_error;
 };
 
+// a bounded device wait that gave up (GT_TIMEOUT)
+struct Timeout : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+// after a call's kernels have finished: did a TMA wait of the L_p pass give up?
+static void check_device_waits() {
+    if (lp_take_wait_timeouts())
+        throw Timeout("a TMA load of the L_p product's FFT grid did not arrive within its wait limit");
+}
+
 // Device allocations owned by an object, freed together.
 struct Pool {
     std::vector<void*> ptrs;
@@ -1121,6 +1132,10 @@ void lp_with_scratch(gt_geometry* G, int ncol, const c64* x, c64* y, void* scrat
         gt::set_error(e.what());                                     \
         return GT_INVALID_ARGUMENT;                                  \
     }                                                                \
+    catch (const gt::Timeout& e) {                                   \
+        gt::set_error(e.what());                                     \
+        return GT_TIMEOUT;                                           \
+    }                                                                \
     catch (const std::bad_alloc&) {                                  \
         gt::set_error("host allocation failed");                     \
         return GT_OUT_OF_MEMORY;                                     \
@@ -1780,6 +1795,7 @@ int gt_solve_device(gt_geometry* G, gt_operators* ops, int32_t n_cols, const int
     int rc = run_solve(G, ops, n_cols, col_op, opts, its_out, resid_out, st);
     GT_CUDA(cudaMemcpyAsync(x_device, W.x64, (size_t)n_cols * G->geo.n * sizeof(c64), cudaMemcpyDeviceToDevice, st));
     GT_CUDA(cudaStreamSynchronize(st));
+    check_device_waits();
     if (rc != GT_OK) gt::set_error("GMRES did not converge for at least one column");
     return rc;
     GT_GUARD_END
@@ -1811,6 +1827,7 @@ int gt_solve(gt_geometry* G, gt_operators* ops, int32_t n_cols, const int32_t* c
     launch_gather(G->d_c2d, nc, W.x64, G->geo.n, d_c, nc, n_cols, st);
     GT_CUDA(cudaMemcpyAsync(x_out, d_c, (size_t)n_cols * nc * sizeof(c64), cudaMemcpyDeviceToHost, st));
     GT_CUDA(cudaStreamSynchronize(st));
+    check_device_waits();
     if (rc != GT_OK) gt::set_error("GMRES did not converge for at least one column");
     return rc;
     GT_GUARD_END
@@ -1908,6 +1925,7 @@ int gt_apply(gt_geometry* G, gt_operators* ops, int32_t kind, int32_t precision,
     launch_gather(G->d_c2d, nc, yout, n, d_c, nc, n_cols, st);
     GT_CUDA(cudaMemcpyAsync(y, d_c, (size_t)n_cols * nc * sizeof(c64), cudaMemcpyDeviceToHost, st));
     GT_CUDA(cudaStreamSynchronize(st));
+    check_device_waits();
     return GT_OK;
     GT_GUARD_END
 }

@@ -80,6 +80,8 @@ template <typename R> struct LpArgs {
 };
 
 template <typename R> void launch_lp(const LpArgs<R>& a, cudaStream_t st);
+// TMA waits of the L_p pass that gave up since the last call (and clears the count); read once the kernels are done
+unsigned int lp_take_wait_timeouts();
 // one of the three passes (0: row FFTs, 1: column FFTs + spectrum, 2: inverse row FFTs + epilogue)
 template <typename R> void launch_lp_pass(const LpArgs<R>& a, int pass, cudaStream_t st);
 // the launch shapes launch_lp would use for these arguments

@@ -20,6 +20,10 @@
 #include "fftw.cuh"
 #include "kernels.h"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cstdlib>
+
 namespace gt {
 
 constexpr int MAXS = 8;
@@ -461,6 +465,132 @@ __global__ void __launch_bounds__(CW_WARPS * 32, GT_CW_MINB) lp_pass_cw(const c3
     }
 }
 
+// Pass C with its T tile brought in by TMA (P1 = 512, FP32).  A block of RW_WARPS warps takes 16 rows
+// i0 .. i0+15 of one sheet of one column: one thread issues two cp.async.bulk.tensor loads of the tile
+// [c = 0..511][16 rows] (two 256-row boxes of 128 bytes each, 128-byte swizzle) onto an mbarrier, so the whole
+// 64 KB tile arrives as full 128-byte lines with no registers spent on it; each warp then reads its two rows'
+// values at its lanes' frequency columns as 16-byte pieces (the swizzle puts the 8 columns a bank group
+// serves on 8 different 16-byte chunks), and the tile's memory becomes the warps' FFT exchange tiles.
+// T is viewed as a 2-D tensor of floats: x = 2 ldt (a row of T), y = (column slot x S + sheet) x 512 + c.
+constexpr int CT_WARPS = RW_WARPS, CT_TILE_BYTES = 512 * 16 * 8;
+constexpr size_t CT_SMEM = 1024 + (size_t)(CT_TILE_BYTES > RW_WARPS * WX_SLOTS * (int)sizeof(c32)
+                                               ? CT_TILE_BYTES : RW_WARPS * WX_SLOTS * sizeof(c32));
+constexpr uint32_t CT_SPIN_LIMIT = 1u << 22;      // mbarrier polls before a load counts as lost (~seconds)
+
+__device__ unsigned int g_lp_wait_timeouts = 0;   // TMA waits that gave up (read and cleared by the host)
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}" : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+    for (uint32_t it = 0; it < CT_SPIN_LIMIT; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__global__ void __launch_bounds__(CT_WARPS * 32, GT_RW_MINB) lp_pass_ct(const __grid_constant__ CUtensorMap tmap,
+                                                                const c32* __restrict__ x,
+                                                                const c32* __restrict__ rhs, c32* __restrict__ out,
+                                                                int64_t ld, int64_t off, int64_t off_v, int S, int n0,
+                                                                int n1, int nx, int ny, int di, int dj,
+                                                                const c32* __restrict__ tw, const uint8_t* __restrict__ mask,
+                                                                const int* __restrict__ col_op,
+                                                                const double* __restrict__ omega, const c64* __restrict__ zs,
+                                                                int mode, const int* __restrict__ col_list,
+                                                                const int* __restrict__ sheet_layer) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    // the 128-byte swizzle repeats every 1024 bytes: the tile starts on a 1024-byte boundary
+    unsigned char* tile = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i0 = blockIdx.x * 16, s = blockIdx.y;
+    const uint32_t b = smem_u32(&bar);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(CT_TILE_BYTES) : "memory");
+        const int y0 = (blockIdx.z * S + s) * 512;
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+            asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+                         ::"r"(smem_u32(tile + h * (CT_TILE_BYTES / 2))), "l"(&tmap), "r"(2 * i0), "r"(y0 + 256 * h),
+                         "r"(b) : "memory");
+    }
+    if (!mbar_wait_bounded(b, 0)) {
+        // the tile did not arrive: record it and leave once the copies in flight have landed (or given up on)
+        if (threadIdx.x == 0) atomicAdd(&g_lp_wait_timeouts, 1u);
+        mbar_wait_bounded(b, 0);
+        return;
+    }
+    const int i = i0 + 2 * warp;
+    const int q = lane >> 4;
+    c32 u[32];
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+        const int c = lane + 32 * m;
+        // rows i, i+1 of column c: 16-byte chunk `warp` of the 128-byte line c, swizzled by c mod 8
+        const float4 f = *reinterpret_cast<const float4*>(tile + c * 128 + ((warp ^ (c & 7)) << 4));
+        const c32 r0 = mk<float>(f.x, f.y), r1 = mk<float>(f.z, f.w);
+        const c32 mine = q ? r1 : r0, send = q ? r0 : r1;
+        c32 got;
+        got.re = __shfl_xor_sync(0xffffffffu, send.re, 16);
+        got.im = __shfl_xor_sync(0xffffffffu, send.im, 16);
+        u[2 * m] = q ? got : mine;
+        u[2 * m + 1] = q ? mine : got;
+    }
+    __syncthreads();                               // every warp has its values: the tile becomes exchange tiles
+    if (i >= n0) return;                           // the whole warp leaves together (no barrier follows)
+    c32 v[2][16];
+    fft512_inv2<float, true>(u, v, reinterpret_cast<c32*>(tile) + warp * WX_SLOTS, tw);
+    const int col = col_list ? col_list[blockIdx.z] : blockIdx.z;
+    const int op = col_op ? col_op[col] : 0;
+    const float w = omega ? float(omega[op]) : 0.0f;
+    const c32 z = zs ? cvt<float>(zs[(int64_t)op * S + s]) : zero<float>();
+    const int64_t base = (int64_t)col * ld;
+    const int layer = sheet_layer ? sheet_layer[s] : s;
+#pragma unroll
+    for (int qq = 0; qq < 2; ++qq) {
+        const int ii = i + qq;
+        if (ii >= n0) continue;
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const int j = lane + 32 * r;
+            if (j >= n1) continue;
+            const int64_t pos = off + ((int64_t)s * n0 + ii) * n1 + j;
+            const c32 L = v[qq][r];
+            c32 yv;
+            if (mode == 2) {
+                yv = mask[pos] ? L : zero<float>();
+            } else if (!mask[pos]) {
+                yv = zero<float>();
+            } else {
+                const int64_t va = off_v + ((int64_t)layer * nx + ii) * ny + j;
+                const int64_t vb = va + (int64_t)di * ny + dj;
+                yv = z * x[base + pos] + w * jmul(L) - (x[base + va] - x[base + vb]);
+                if (mode == 1) yv = rhs[base + pos] - yv;
+            }
+            out[base + pos] = yv;
+        }
+    }
+}
+
+unsigned int lp_take_wait_timeouts() {
+    unsigned int h = 0, zero_v = 0;
+    GT_CUDA(cudaMemcpyFromSymbol(&h, g_lp_wait_timeouts, sizeof(h)));
+    if (h) GT_CUDA(cudaMemcpyToSymbol(g_lp_wait_timeouts, &zero_v, sizeof(zero_v)));
+    return h;
+}
+
 // Row passes for P a power of 8: the first stage of pass A reads the strip row straight from x, the last
 // stage of pass C feeds the epilogue from registers; stages alternate two shared buffers.
 template <typename R, int P>
@@ -760,9 +890,54 @@ static void launch_b(const LpArgs<R>& a, int bt, cudaStream_t st) {
     GT_LAUNCH_CHECK();
 }
 
+// cuTensorMapEncodeTiled from the driver (no link against libcuda: the runtime hands out its entry point)
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// pass C through TMA tiles unless GT_LP_TMA=0 (the per-warp 16-byte loads of lp_pass_cw instead; both compute
+// the same values in the same order)
+static bool lp_tma_enabled() {
+    const char* e = std::getenv("GT_LP_TMA");
+    return !(e && e[0] == '0') && tensor_map_encoder() != nullptr;
+}
+
+// T as a 2-D float tensor: rows of 2 ldt floats, ncol x S x 512 of them; boxes of 16 complex values x 256
+// frequency columns, 128-byte swizzle
+static CUtensorMap t_tensor_map(const LpArgs<float>& a) {
+    CUtensorMap m;
+    const cuuint64_t dims[2] = {(cuuint64_t)2 * a.ldt, (cuuint64_t)a.ncol * a.S * 512};
+    const cuuint64_t strides[1] = {(cuuint64_t)a.ldt * sizeof(c32)};
+    const cuuint32_t box[2] = {32, 256}, estr[2] = {1, 1};
+    const CUresult r = tensor_map_encoder()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)a.T, dims, strides, box, estr,
+                                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw CudaError{cudaErrorInvalidValue, "cuTensorMapEncodeTiled of the FFT grid T"};
+    return m;
+}
+
 template <typename R, int PA>
 static void launch_c(const LpArgs<R>& a, int rows, cudaStream_t st) {
     if constexpr (PA == 512 && std::is_same<R, float>::value) {
+        // TMA wants T 16-byte aligned, its rows a multiple of 16 bytes (ldt % 16 == 0 gives 128) and each box's
+        // first float at a multiple of 16 bytes (2 x 16 i0 floats)
+        if (rw_fits(a) && lp_tma_enabled() && (reinterpret_cast<uintptr_t>(a.T) & 15) == 0) {
+            const CUtensorMap m = t_tensor_map(a);
+            set_smem<float>((const void*)lp_pass_ct, CT_SMEM);
+            lp_pass_ct<<<dim3(ceil_div(a.n0, 16), a.S, a.ncol), CT_WARPS * 32, CT_SMEM, st>>>(
+                m, a.x, a.rhs, a.out, a.ld, a.off, a.off_v, a.S, a.n0, a.n1, a.nx, a.ny, a.di, a.dj, a.tw1, a.mask,
+                a.col_op, a.omega, a.zs, a.mode, a.col_list, a.sheet_layer);
+            GT_LAUNCH_CHECK();
+            return;
+        }
         if (rw_fits(a)) {
             set_smem<float>((const void*)lp_pass_cw, CW_SMEM);
             lp_pass_cw<<<dim3(ceil_div(a.n0, 2 * CW_WARPS), a.S, a.ncol), CW_WARPS * 32, CW_SMEM, st>>>(
