@@ -475,11 +475,18 @@ __global__ void __launch_bounds__(CW_WARPS * 32, GT_CW_MINB) lp_pass_cw(const c3
 constexpr int CT_WARPS = RW_WARPS, CT_TILE_BYTES = 512 * 16 * 8;
 constexpr size_t CT_SMEM = 1024 + (size_t)(CT_TILE_BYTES > RW_WARPS * WX_SLOTS * (int)sizeof(c32)
                                                ? CT_TILE_BYTES : RW_WARPS * WX_SLOTS * sizeof(c32));
-constexpr uint32_t CT_SPIN_LIMIT = 1u << 22;      // mbarrier polls before a load counts as lost (~seconds)
+constexpr uint64_t CT_WAIT_NS = 1000000000ull;     // a tile not in after a second counts as lost
+constexpr uint32_t CT_SPIN_LIMIT = 1u << 26;        // and polls, should the timer not advance
 
 __device__ unsigned int g_lp_wait_timeouts = 0;   // TMA waits that gave up (read and cleared by the host)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
     uint32_t ok;
@@ -488,9 +495,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
     return ok != 0;
 }
 
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
-    for (uint32_t it = 0; it < CT_SPIN_LIMIT; ++it)
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, uint64_t wait_ns) {
+    const uint64_t t0 = global_ns();
+    for (uint32_t it = 0; it < CT_SPIN_LIMIT; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
+        if (global_ns() - t0 > wait_ns) return false;
+    }
     return false;
 }
 
@@ -503,7 +513,10 @@ __global__ void __launch_bounds__(CT_WARPS * 32, GT_RW_MINB) lp_pass_ct(const __
                                                                 const int* __restrict__ col_op,
                                                                 const double* __restrict__ omega, const c64* __restrict__ zs,
                                                                 int mode, const int* __restrict__ col_list,
-                                                                const int* __restrict__ sheet_layer) {
+                                                                const int* __restrict__ sheet_layer,
+                                                                uint32_t missing_bytes, uint64_t wait_ns) {
+    // missing_bytes: 0, except when a test makes the wait run out (the barrier then expects bytes no load
+    // brings; the loads themselves are the usual two)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
     // the 128-byte swizzle repeats every 1024 bytes: the tile starts on a 1024-byte boundary
@@ -518,7 +531,8 @@ __global__ void __launch_bounds__(CT_WARPS * 32, GT_RW_MINB) lp_pass_ct(const __
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(CT_TILE_BYTES) : "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b),
+                     "r"(CT_TILE_BYTES + missing_bytes) : "memory");
         const int y0 = (blockIdx.z * S + s) * 512;
 #pragma unroll
         for (int h = 0; h < 2; ++h)
@@ -526,10 +540,35 @@ __global__ void __launch_bounds__(CT_WARPS * 32, GT_RW_MINB) lp_pass_ct(const __
                          ::"r"(smem_u32(tile + h * (CT_TILE_BYTES / 2))), "l"(&tmap), "r"(2 * i0), "r"(y0 + 256 * h),
                          "r"(b) : "memory");
     }
-    if (!mbar_wait_bounded(b, 0)) {
+    // while the tile is in flight: ask L2 for the lines the epilogue will read (the strips' x, the potentials
+    // at both ends of each strip, the mask), so that they are on chip when the inverse FFT is done
+    {
+        const int ip = i0 + 2 * warp;
+        const int colp = col_list ? col_list[blockIdx.z] : blockIdx.z;
+        const int64_t basep = (int64_t)colp * ld;
+        const int layerp = sheet_layer ? sheet_layer[s] : s;
+#pragma unroll
+        for (int qq = 0; qq < 2; ++qq) {
+            const int ii = ip + qq;
+            if (ii >= n0) continue;
+            const int64_t row = off + ((int64_t)s * n0 + ii) * n1;
+            const int j = 16 * lane;                         // lane L: the L-th 128-byte line (16 values) of a row
+            if (j < n1) {
+                const int64_t va = off_v + ((int64_t)layerp * nx + ii) * ny + j;
+                if (mode != 2) {
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(x + basep + row + j));
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(x + basep + va));
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(x + basep + va + (int64_t)di * ny + dj));
+                    if (mode == 1) asm volatile("prefetch.global.L2 [%0];" ::"l"(rhs + basep + row + j));
+                }
+            }
+            if (128 * lane < n1) asm volatile("prefetch.global.L2 [%0];" ::"l"(mask + row + 128 * lane));
+        }
+    }
+    if (!mbar_wait_bounded(b, 0, wait_ns)) {
         // the tile did not arrive: record it and leave once the copies in flight have landed (or given up on)
         if (threadIdx.x == 0) atomicAdd(&g_lp_wait_timeouts, 1u);
-        mbar_wait_bounded(b, 0);
+        mbar_wait_bounded(b, 0, wait_ns);
         return;
     }
     const int i = i0 + 2 * warp;
@@ -931,10 +970,15 @@ static void launch_c(const LpArgs<R>& a, int rows, cudaStream_t st) {
         // first float at a multiple of 16 bytes (2 x 16 i0 floats)
         if (rw_fits(a) && lp_tma_enabled() && (reinterpret_cast<uintptr_t>(a.T) & 15) == 0) {
             const CUtensorMap m = t_tensor_map(a);
+            // GT_LP_TMA_TEST_SHORTFALL=1 (tests only): the barrier waits for 16 bytes that never come, with a
+            // 1 ms limit, so that the GT_TIMEOUT path runs without a lost load
+            const char* t = std::getenv("GT_LP_TMA_TEST_SHORTFALL");
+            const bool shortfall = t && t[0] == '1';
             set_smem<float>((const void*)lp_pass_ct, CT_SMEM);
             lp_pass_ct<<<dim3(ceil_div(a.n0, 16), a.S, a.ncol), CT_WARPS * 32, CT_SMEM, st>>>(
                 m, a.x, a.rhs, a.out, a.ld, a.off, a.off_v, a.S, a.n0, a.n1, a.nx, a.ny, a.di, a.dj, a.tw1, a.mask,
-                a.col_op, a.omega, a.zs, a.mode, a.col_list, a.sheet_layer);
+                a.col_op, a.omega, a.zs, a.mode, a.col_list, a.sheet_layer, shortfall ? 16u : 0u,
+                shortfall ? 1000000ull : CT_WAIT_NS);
             GT_LAUNCH_CHECK();
             return;
         }

@@ -45,3 +45,22 @@ def test_tma_tiles_give_the_solves_of_the_plain_loads(bench_board, monkeypatch):
     for a, c in zip(out["1"], out["0"]):
         assert a[2] == c[2] and np.array_equal(a[3], c[3])
         assert a[4] <= 1e-10
+
+
+def test_a_tma_wait_that_runs_out_is_reported_and_the_device_stays_usable(bench_board, monkeypatch):
+    """Failure detection without a fault: the barrier is told to expect 16 bytes more than the two tile loads
+    bring (GT_LP_TMA_TEST_SHORTFALL, with a 1 ms wait limit), so every block's wait runs out; the product
+    returns GT_TIMEOUT (RuntimeError here), and the next product on the same context is right."""
+    b, st, routes = bench_board
+    obj, k = st.factorise([float(b.freqs[0])])[0]
+    rng = np.random.default_rng(6)
+    x = np.zeros((2, st.handle.n_compact), complex)
+    x[:, : st.ns] = rng.standard_normal((2, st.ns)) + 1j * rng.standard_normal((2, st.ns))
+    monkeypatch.setenv("GT_LP_TMA", "1")
+    monkeypatch.setenv("GT_LP_TMA_TEST_SHORTFALL", "1")
+    with pytest.raises(RuntimeError, match="did not arrive"):
+        native.apply(st.handle, obj, "lp", x, k, "fp32")
+    monkeypatch.delenv("GT_LP_TMA_TEST_SHORTFALL")
+    got = native.apply(st.handle, obj, "lp", x, k, "fp32")
+    ref = native.apply(st.handle, obj, "lp", x, k, "fp64")
+    assert np.linalg.norm(got - ref) <= 1e-5 * np.linalg.norm(ref)
